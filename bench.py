@@ -1,0 +1,388 @@
+"""Benchmark: Gvoxels/s of SDF -> mesh dual contouring at 1024^3 on one GB300.
+
+Workload (one "step"): the CSG SDF -- a rounded box (half-size 0.7, radius
+0.05) minus a smooth union (k = 0.02) of 64 seeded spheres, unioned with a
+torus (0.5, 0.1) -- meshed at 1024^3 cells over [-1, 1]^3: grid evaluation,
+sign changes, crossings, mass-point vertices with normals, quads -> triangle
+indices, all on the device.  A voxel is a cell; value = N^3 * steps / time.
+
+  value        device time per step (CUDA events on the launching stream),
+               mesh buffers resident, L2 flushed between steps (outside the
+               events)
+  e2e          the C-ABI call a user makes per job: s2m_mesh_create (device
+               buffers, pipeline, count readback) + the mesh copied to pinned
+               host memory + s2m_mesh_free
+  roofline     the dominant kernel, from CUDA events around every launch of
+               the timed steps
+  cpu_baseline the CPU oracle (restatement of the reference rule, OpenMP on all
+               host cores) on a bounded window of slices of the same job
+
+--impl reference times that CPU implementation alone (the reference itself
+is Rust + wgpu and cannot run here) and prints the same line.
+N > 1 GPUs (torchrun): independent replicas, one job per rank, no collective
+on the data path ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FULL = 1024
+BOUNDS = 2.0
+METRIC = "Gvoxels/s at 1024^3"
+UNIT = "Gvoxels/s"
+WORKLOAD = "csg64_1024"
+CPU_SAMPLE_SLICES = 16     # cpu_baseline: cell slices [504, 520) of the 1024^3 job
+REF_STEP_SLICES = 4        # --impl reference: cell slices per step
+CPU_Z0 = 504
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--resolution", type=int, default=N_FULL)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload():
+    from sdf2mesh_gb300 import workloads
+    return workloads.csg64(seed=0)
+
+
+def cpu_sample(n_slices, z0, resolution, threads=0):
+    """The oracle (reference rule, binary32) on cell slices [z0, z0 + n) of the job."""
+    import oracle
+    _, prm = workload()
+    t = time.perf_counter()
+    m = oracle.mesh(oracle.CSG, prm, resolution, BOUNDS, z_begin=z0, z_end=z0 + n_slices, threads=threads)
+    dt = time.perf_counter() - t
+    return dt, m
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_arm(a):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    N = a.resolution
+    z0 = max(0, min(CPU_Z0, N - REF_STEP_SLICES))
+    cells = REF_STEP_SLICES * N * N
+    for _ in range(a.warmup):
+        cpu_sample(REF_STEP_SLICES, z0, N)
+    times = []
+    for _ in range(a.steps):
+        dt, _ = cpu_sample(REF_STEP_SLICES, z0, N)
+        times.append(dt)
+    tot = sum(times)
+    v = cells * a.steps / tot / 1e9
+    sample = (f"cell slices [{z0}, {z0 + REF_STEP_SLICES}) of the {N}^3 job per step "
+              f"({cells} voxels), quads included")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": tot / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "resolution": N, "bounds": BOUNDS, "sdf": "csg64 seed 0",
+                   "implementation": "CPU oracle: C++ restatement of the reference rule, OpenMP"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": host_threads(), "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference (Rust + wgpu) is unavailable on this box: no Rust toolchain, no graphics stack",
+    }), flush=True)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        hi = max(sm)
+        load = [x for x in sm if x >= 0.5 * hi] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def ours(a):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    import sdf2mesh_gb300 as s2m
+    from sdf2mesh_gb300 import build as b
+    b.build()
+    L = s2m.load_library()
+
+    N = a.resolution
+    src, _ = workload()
+    t0 = time.perf_counter()
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    compile_s = time.perf_counter() - t0
+    fp32_ops, sfu_ops = sdf.op_counts()
+
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    state = s2m.AppState(resolution=N, bounds=BOUNDS)
+    mesh = s2m.mesh_device(sdf, state, sp)
+    info = mesh.info()
+    nverts, ntris = int(info.nverts), int(info.ntris)
+    launches_per_step = int(info.kernel_launches)
+
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > 126 MB L2
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(a.warmup):
+        mesh.run_async(sp)
+        mesh.sync(sp)
+
+    # ---- device-timed steps -------------------------------------------------
+    mesh.set_profiling(True)
+    mesh.reset_profile()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    wall0 = time.perf_counter()
+    for i in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+        mesh.run_async(sp)
+        with torch.cuda.stream(stream):
+            evs[i][1].record(stream)
+        mesh.sync(sp)
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    mesh.set_profiling(False)
+    step_ms = [s.elapsed_time(e) for s, e in evs]
+    tot_ms = sum(step_ms)
+    prof = mesh.profile()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    voxels_step = float(N) ** 3
+    value = voxels_step * a.steps * ws / (tot_ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI: create -> pinned host copy -> free ----
+    host_pos = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
+    host_nrm = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
+    host_key = torch.empty(nverts + 1, dtype=torch.int64, pin_memory=True)
+    host_tri = torch.empty(3 * ntris + 3, dtype=torch.int32, pin_memory=True)
+    p = state.params()
+    err = ctypes.create_string_buffer(4096)
+    e2e_ms = []
+    d2h = 0
+    barrier()
+    for i in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        h = ctypes.c_void_p()
+        rc = L.s2m_mesh_create(sdf.handle, ctypes.byref(p), ctypes.c_void_p(sp), ctypes.byref(h), err, len(err))
+        if rc != 0:
+            raise RuntimeError(err.value.decode())
+        mi = s2m.MeshInfo()
+        L.s2m_mesh_get_info(h, ctypes.byref(mi))
+        if mi.nverts != nverts or mi.ntris != ntris:
+            raise RuntimeError("e2e mesh differs from the timed mesh")
+        rc = L.s2m_mesh_copy_to_host(h, host_pos.data_ptr(), host_nrm.data_ptr(), host_key.data_ptr(),
+                                     host_tri.data_ptr(), ctypes.c_void_p(sp))
+        L.s2m_mesh_free(h)
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+        if rc != 0:
+            raise RuntimeError("copy to host failed")
+        d2h = nverts * (12 + 12 + 8) + ntris * 12
+    barrier()
+    e2e_tot = sum(e2e_ms)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_tot], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_tot = float(t.item())
+    e2e_value = voxels_step * a.steps * ws / (e2e_tot * 1e-3) / 1e9
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel -------------------------------------
+    ms = prof["ms"]
+    dom = max(ms, key=lambda k: ms[k])
+    fp32_peak = s2m.measure_fp32_peak(sp)  # Gop/s, one FP32 add or mul per lane per cycle
+    pk, pk_kind = peaks()
+    n_eval = max(1, prof["launches"]["eval_planes"])
+    roof = {}
+    kernels = {}
+    for k in ms:
+        nl = prof["launches"][k]
+        kernels[k] = {"launches_per_step": nl // a.steps, "ms_per_step": ms[k] / a.steps,
+                      "share": ms[k] / max(1e-9, sum(ms.values()))}
+    eval_gops = fp32_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
+    eval_sfu = sfu_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
+    # contouring passes: bytes they must move per job (state them in one place)
+    V, T = nverts, ntris
+    contour_bytes = (V * (32 + 32)            # vcompact: candidate read + vertex write (pos, nrm, key)
+                     + 8.0 * N * N            # rowcnt + rowstart
+                     + V * 8 + T * 12)        # quads: key read + triangle indices
+    contour_ms = (ms["vcompact"] + ms["rowscan"] + ms["quads"]) / a.steps
+    contour_gbs = contour_bytes / (contour_ms * 1e-3) / 1e9 if contour_ms > 0 else None
+    if dom in ("eval_planes", "cells"):
+        per_launch_ms = ms["eval_planes"] / n_eval
+        roof = {"bound": "fp32", "kernel": "s2m_eval_planes", "achieved": eval_gops, "peak": fp32_peak,
+                "unit": "Gop/s", "frac": eval_gops / fp32_peak,
+                "peak_source": "measured: s2m_fp32_probe (FP32 add/mul issue rate, this GPU, this run)",
+                "traffic": None, "ms_per_launch": per_launch_ms,
+                "algorithmic": f"{fp32_ops:g} FP32 + {sfu_ops:g} SFU ops per lattice point x "
+                               f"{prof['eval_points'] / n_eval:.0f} points per launch",
+                "sfu_gops": eval_sfu, "dominant_by_time": dom}
+    else:
+        roof = {"bound": "hbm", "kernel": dom, "achieved": contour_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": (contour_gbs or 0) / pk["hbm_gbs"], "peak_source": pk_kind, "traffic": None}
+    contour = {"bound": "hbm", "achieved": contour_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+               "frac": (contour_gbs or 0) / pk["hbm_gbs"], "peak_source": f"{pk_kind} (MEASURED_PEAKS hbm_gbs)",
+               "bytes_per_job": contour_bytes}
+
+    cpu = None
+    if not a.no_cpu_baseline:
+        n = min(CPU_SAMPLE_SLICES, N)
+        z0 = max(0, min(CPU_Z0, N - n))
+        dt, _ = cpu_sample(n, z0, N)
+        cpu = {"value": n * N * N / dt / 1e9, "unit": UNIT, "cores": host_threads(), "kind": "port",
+               "sample": f"CPU oracle (reference rule, binary32, OpenMP) on cell slices [{z0}, {z0 + n}) "
+                         f"of the {N}^3 job: {n * N * N} voxels in {dt:.2f} s"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": tot_ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "resolution": N, "bounds": BOUNDS,
+                   "sdf": "rounded box - smooth union (k=0.02) of 64 spheres (splitmix64 seed 0) + torus",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "precision": "reference rule in binary32, no FMA contraction, IEEE div/sqrt"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_tot / a.steps,
+                "path": "s2m_mesh_create + s2m_mesh_copy_to_host (pinned) + s2m_mesh_free; inputs are the "
+                        "compiled SDF module and a 48-byte parameter block passed as kernel arguments"},
+        "roofline": roof,
+        "roofline_contouring": contour,
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": launches_per_step * a.steps,
+        "mesh": {"vertices": nverts, "triangles": ntris, "invalid_quads": int(info.invalid_quads),
+                 "candidate_cells": int(info.candidate_cells), "slab_depth": int(info.slab_depth)},
+        "compile_s": compile_s,
+        "triangles_per_s": ntris * a.steps * ws / (tot_ms * 1e-3),
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line), flush=True)
+    mesh.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        ours(a)
+
+
+if __name__ == "__main__":
+    main()

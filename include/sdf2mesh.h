@@ -1,0 +1,198 @@
+/*
+ * sdf2mesh.h -- C ABI of libsdf2mesh_gb300.so, the GB300 (sm_103a) engine
+ * that meshes signed distance functions by dual contouring.
+ *
+ * The reference (WilstonOreo/sdf2mesh) has no FFI: its boundary is a Rust
+ * binary and a wgpu module.  Each entry point below names the reference code
+ * it stands in for (paths relative to the reference sources); INTEGRATION.md
+ * shows the binding a host program adds.
+ *
+ * Conventions
+ *   - Every function returns an s2m_status (0 = S2M_OK) unless noted; on
+ *     failure, when `err` is non-null, a NUL-terminated message is written
+ *     into err[0..errlen).  No exception or abort crosses this boundary.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default
+ *     stream).  Device work is stream-ordered.
+ *   - Handles are opaque; the caller frees each with its *_free function.
+ *     An s2m_sdf is immutable after compilation and may be shared between
+ *     threads; an s2m_mesh is used by one thread at a time.
+ */
+#ifndef SDF2MESH_GB300_H
+#define SDF2MESH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define S2M_ABI_VERSION 1
+
+typedef enum {
+  S2M_OK = 0,
+  S2M_E_INVALID = 1,      /* bad argument                                         */
+  S2M_E_IO = 2,           /* file could not be read or written                    */
+  S2M_E_PARSE = 3,        /* WGSL / GLSL source rejected by the frontend          */
+  S2M_E_MISSING_SDF = 4,  /* no sdf3d / named GLSL function (shadertoy.rs MissingSdf) */
+  S2M_E_NVRTC = 5,        /* NVRTC could not compile the lowered source           */
+  S2M_E_CUDA = 6,         /* CUDA runtime error                                   */
+  S2M_E_OOM = 7,          /* device allocation failed                             */
+  S2M_E_OVERFLOW = 8,     /* mesh exceeds the largest supported buffers            */
+  S2M_E_TIMEOUT = 9,      /* a bounded device wait expired (kernel error flag)    */
+  S2M_E_NO_DEVICE = 10    /* no CUDA device                                       */
+} s2m_status;
+
+typedef enum { S2M_LANG_WGSL = 0, S2M_LANG_GLSL = 1 } s2m_lang;
+
+/* Compile flags. */
+#define S2M_COMPILE_FMAD 0x1u  /* allow FMA contraction: faster, no longer bit-exact
+                                  with the reference rule's binary32 arithmetic     */
+
+/* Job flags (s2m_params.flags). */
+#define S2M_JOB_POW2_ROUNDING 0x1u  /* round resolution up to a power of two as the
+                                       reference CLI does (main.rs:141-148)         */
+#define S2M_JOB_SLICE_LAG 0x2u      /* reproduce the reference's read-before-submit
+                                       slice lag (main.rs:324-355): only cell slices
+                                       0..N-2 are emitted, labelled z+1             */
+#define S2M_JOB_EXACT_CORNERS 0x4u  /* re-evaluate every off-lattice corner of every
+                                       cell (verification mode; slower)             */
+
+typedef struct s2m_sdf s2m_sdf;
+typedef struct s2m_mesh s2m_mesh;
+
+/* Job parameters.  Stands in for AppState (main.rs:12-64, 139-175). */
+typedef struct {
+  uint32_t resolution;    /* cells per axis N (>= 2)                       */
+  float bounds;           /* edge of the centred cube [-B/2, B/2]^3        */
+  float eps;              /* normal epsilon (reference: 1e-4)              */
+  uint32_t flags;         /* S2M_JOB_*                                     */
+  uint32_t slab_depth;    /* cell slices per slab; 0 = automatic           */
+  uint32_t reserved;
+  uint64_t max_vertices;  /* initial vertex capacity; 0 = automatic        */
+  uint64_t max_triangles; /* initial triangle capacity; 0 = automatic      */
+} s2m_params;
+
+/* Result description; device pointers stay owned by the s2m_mesh. */
+typedef struct {
+  uint64_t nverts;
+  uint64_t ntris;
+  uint64_t invalid_quads;   /* quads dropped as in mesh.rs:270-277           */
+  uint64_t cells;           /* N^3 voxels of the job                         */
+  uint64_t candidate_cells; /* cells whose exact corners were re-evaluated   */
+  uint32_t resolution;      /* N actually used (after optional rounding)     */
+  uint32_t slab_depth;
+  const float *d_pos;       /* device: 3 * nverts  (x, y, z)                 */
+  const float *d_nrm;       /* device: 3 * nverts  unit normals              */
+  const uint64_t *d_cell;   /* device: nverts keys x | y<<16 | z<<32 | signs<<48 */
+  const uint32_t *d_tris;   /* device: 3 * ntris vertex indices              */
+  uint64_t kernel_launches; /* kernels launched by the last run              */
+} s2m_mesh_info;
+
+/* ---- shader front end (src/shader.rs, src/shadertoy.rs) --------------- */
+
+/* Sdf3DShader::from_path + shader_source_input (shader.rs:44-67, 159-203):
+   expand `use` / `include` lines of a .sdf3d file.  *out is malloc'ed; free
+   it with s2m_free_string. */
+int s2m_preprocess_file(const char *path, char **out, char *err, size_t errlen);
+
+/* The same expansion on in-memory .sdf3d text (shader.rs:159-203); `include`
+   paths resolve against the working directory, then `base_dir` (may be
+   NULL).  *out is malloc'ed; free it with s2m_free_string. */
+int s2m_preprocess_source(const char *source, const char *base_dir, char **out, char *err, size_t errlen);
+
+/* Compile an SDF source (WGSL .sdf3d text after preprocessing, or GLSL) to a
+   device module for sm_103a: frontend -> CUDA C -> NVRTC.  Stands in for
+   Sdf3DShader::add_to_source + create_shader_module (shader.rs:155-157,
+   220-225) and, for GLSL, from_glsl_fragment_shader (shader.rs:73-104);
+   `sdf_name` is the GLSL function (default "sdf"). */
+int s2m_compile(const char *source, int lang, const char *sdf_name, uint32_t compile_flags,
+                s2m_sdf **out, char *err, size_t errlen);
+
+/* s2m_preprocess_file (WGSL) or a GLSL file read, then s2m_compile. */
+int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t compile_flags,
+                     s2m_sdf **out, char *err, size_t errlen);
+
+/* The lowered CUDA C of a compiled SDF (for --debug-cuda); owned by sdf. */
+const char *s2m_sdf_cuda_source(const s2m_sdf *sdf);
+
+/* Algorithmic FP32 and SFU operations of one sdf3d evaluation. */
+int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops);
+
+void s2m_sdf_free(s2m_sdf *sdf);
+
+/* Frontend only (no device): lower a source to CUDA C.  *out is malloc'ed. */
+int s2m_translate(const char *source, int lang, const char *sdf_name, char **out,
+                  double *fp32_ops, double *sfu_ops, char *err, size_t errlen);
+
+/* WGSL text surgery (shadertoy.rs:248-352).  *out is malloc'ed. */
+int s2m_wgsl_remove_function(const char *wgsl, const char *function_name, char **out);
+int s2m_wgsl_rename_function(const char *wgsl, const char *old_name, const char *new_name,
+                             char **out);
+int s2m_wgsl_has_function(const char *wgsl, const char *function_name); /* 1 / 0 */
+
+void s2m_free_string(char *s);
+
+/* ---- meshing (dualcontour.wgsl:161-180, main.rs:298-356, mesh.rs:267-341) */
+
+/* Mesh an SDF: grid evaluation, sign changes, crossings, vertex placement
+   and quad emission, all on the device, into buffers owned by *out.
+   Synchronises `stream` at the end (the counts are read back). */
+int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream,
+                    s2m_mesh **out, char *err, size_t errlen);
+
+/* Re-run the same job into the mesh's existing buffers, stream-ordered,
+   without synchronising (for timing).  Counts become valid after
+   s2m_mesh_sync. */
+int s2m_mesh_run_async(s2m_mesh *mesh, void *stream);
+
+/* Wait for `stream`, read the counts back and check the device error flags. */
+int s2m_mesh_sync(s2m_mesh *mesh, void *stream, char *err, size_t errlen);
+
+int s2m_mesh_get_info(const s2m_mesh *mesh, s2m_mesh_info *info);
+
+/* Copy the mesh to caller-owned host buffers (any may be NULL):
+   pos / nrm 3*nverts floats, cell nverts keys, tris 3*ntris indices. */
+int s2m_mesh_copy_to_host(const s2m_mesh *mesh, float *pos, float *nrm, uint64_t *cell,
+                          uint32_t *tris, void *stream);
+
+/* TriangleMesh::write_to_file (mesh.rs:182-196): STL or PLY by extension. */
+int s2m_mesh_write(const s2m_mesh *mesh, const char *path, char *err, size_t errlen);
+
+void s2m_mesh_free(s2m_mesh *mesh);
+
+/* Per-kernel device time of a mesh's runs, from CUDA events recorded on the
+   launching stream around every kernel while profiling is enabled.  Kinds:
+   0 grid evaluation, 1 cell pass, 2 vertex compaction, 3 row scan, 4 quads.
+   Accumulates over runs until reset; read after s2m_mesh_sync. */
+#define S2M_KERNEL_KINDS 5
+typedef struct {
+  double ms[S2M_KERNEL_KINDS];
+  uint64_t launches[S2M_KERNEL_KINDS];
+  double eval_points;      /* lattice points evaluated by kind-0 launches */
+  double cells;            /* cells classified by kind-1 launches         */
+} s2m_profile;
+int s2m_mesh_set_profiling(s2m_mesh *mesh, int enable);
+int s2m_mesh_get_profile(const s2m_mesh *mesh, s2m_profile *out);
+int s2m_mesh_reset_profile(s2m_mesh *mesh);
+
+/* ---- host writers (mesh.rs:8-141) -------------------------------------- */
+
+/* ASCII STL with Rust `{}` float text, facet normal (v2-v0) x (v1-v0). */
+int s2m_write_stl(const float *pos, const uint32_t *tris, uint64_t ntris, const char *path);
+/* ASCII PLY with per-vertex normals. */
+int s2m_write_ply(const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris,
+                  uint64_t ntris, const char *path);
+
+/* ---- diagnostics --------------------------------------------------------- */
+
+const char *s2m_status_string(int status);
+int s2m_abi_version(void);
+/* Measured FP32 issue rate of the current device in Gop/s (one FP32 add or
+   mul per lane per cycle), from a dependent-chain microkernel. */
+int s2m_measure_fp32_peak(double *gops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDF2MESH_GB300_H */

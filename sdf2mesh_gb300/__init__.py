@@ -1,0 +1,436 @@
+"""sdf2mesh_gb300 -- SDF to triangle mesh by dual contouring on one GB300.
+
+Python mirror of the reference's interface (WilstonOreo/sdf2mesh), over the C
+ABI of libsdf2mesh_gb300.so (include/sdf2mesh.h):
+
+  Sdf3DShader.from_path(path)                      src/shader.rs:44-67
+  Sdf3DShader.from_glsl_fragment_shader(path, sdf) src/shader.rs:73-104
+  Sdf3DShader.write_to_file(path)                  src/shader.rs:206-209 (--debug-wgsl)
+  AppState.from_args(resolution, bounds)           src/bin/sdf2mesh/main.rs:139-175
+  generate(shader, state) -> TriangleMesh          src/bin/sdf2mesh/main.rs:298-357
+  TriangleMesh.write_to_file / write_stl_to_file / write_ply_to_file
+                                                   src/mesh.rs:167-210
+
+All meshing runs on the GPU through the library; there is no CPU path.  The
+library must have been built (python -m sdf2mesh_gb300.build) and a CUDA
+device must be present, otherwise these calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from dataclasses import dataclass, field
+
+import numpy as np
+
+__all__ = [
+    "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate",
+    "load_library", "translate", "wgsl_remove_function", "wgsl_rename_function", "wgsl_has_function",
+    "LANG_WGSL", "LANG_GLSL", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "COMPILE_FMAD",
+]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libsdf2mesh_gb300.so")
+
+LANG_WGSL, LANG_GLSL = 0, 1
+COMPILE_FMAD = 0x1
+JOB_POW2_ROUNDING, JOB_SLICE_LAG, JOB_EXACT_CORNERS = 0x1, 0x2, 0x4
+
+S2M_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "IO", 3: "PARSE", 4: "MISSING_SDF", 5: "NVRTC", 6: "CUDA",
+                7: "OOM", 8: "OVERFLOW", 9: "TIMEOUT", 10: "NO_DEVICE"}
+
+
+class S2MError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.name = STATUS_NAMES.get(status, str(status))
+        super().__init__(f"[{self.name}] {message}")
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("resolution", ctypes.c_uint32), ("bounds", ctypes.c_float), ("eps", ctypes.c_float),
+        ("flags", ctypes.c_uint32), ("slab_depth", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+        ("max_vertices", ctypes.c_uint64), ("max_triangles", ctypes.c_uint64),
+    ]
+
+
+class MeshInfo(ctypes.Structure):
+    _fields_ = [
+        ("nverts", ctypes.c_uint64), ("ntris", ctypes.c_uint64), ("invalid_quads", ctypes.c_uint64),
+        ("cells", ctypes.c_uint64), ("candidate_cells", ctypes.c_uint64), ("resolution", ctypes.c_uint32),
+        ("slab_depth", ctypes.c_uint32), ("d_pos", ctypes.c_void_p), ("d_nrm", ctypes.c_void_p),
+        ("d_cell", ctypes.c_void_p), ("d_tris", ctypes.c_void_p), ("kernel_launches", ctypes.c_uint64),
+    ]
+
+
+KERNEL_KINDS = ("eval_planes", "cells", "vcompact", "rowscan", "quads")
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double * 5), ("launches", ctypes.c_uint64 * 5), ("eval_points", ctypes.c_double),
+                ("cells", ctypes.c_double)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load libsdf2mesh_gb300.so (built in-tree); raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise S2MError(1, f"{p} is not built; run `python -m sdf2mesh_gb300.build`")
+        L = ctypes.CDLL(p)
+        c_char_pp = ctypes.POINTER(ctypes.c_char_p)
+        vp, sz, u32, u64, i = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+        dp = ctypes.POINTER(ctypes.c_double)
+        sigs = {
+            "s2m_abi_version": ([], i),
+            "s2m_status_string": ([i], ctypes.c_char_p),
+            "s2m_free_string": ([vp], None),
+            "s2m_preprocess_file": ([ctypes.c_char_p, ctypes.POINTER(vp), ctypes.c_char_p, sz], i),
+            "s2m_preprocess_source": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp), ctypes.c_char_p,
+                                       sz], i),
+            "s2m_translate": ([ctypes.c_char_p, i, ctypes.c_char_p, ctypes.POINTER(vp), dp, dp,
+                               ctypes.c_char_p, sz], i),
+            "s2m_compile": ([ctypes.c_char_p, i, ctypes.c_char_p, u32, ctypes.POINTER(vp), ctypes.c_char_p, sz], i),
+            "s2m_compile_file": ([ctypes.c_char_p, i, ctypes.c_char_p, u32, ctypes.POINTER(vp),
+                                  ctypes.c_char_p, sz], i),
+            "s2m_sdf_cuda_source": ([vp], ctypes.c_char_p),
+            "s2m_sdf_op_counts": ([vp, dp, dp], i),
+            "s2m_sdf_free": ([vp], None),
+            "s2m_wgsl_remove_function": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)], i),
+            "s2m_wgsl_rename_function": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                          ctypes.POINTER(vp)], i),
+            "s2m_wgsl_has_function": ([ctypes.c_char_p, ctypes.c_char_p], i),
+            "s2m_mesh_create": ([vp, ctypes.POINTER(Params), vp, ctypes.POINTER(vp), ctypes.c_char_p, sz], i),
+            "s2m_mesh_run_async": ([vp, vp], i),
+            "s2m_mesh_sync": ([vp, vp, ctypes.c_char_p, sz], i),
+            "s2m_mesh_get_info": ([vp, ctypes.POINTER(MeshInfo)], i),
+            "s2m_mesh_copy_to_host": ([vp, vp, vp, vp, vp, vp], i),
+            "s2m_mesh_write": ([vp, ctypes.c_char_p, ctypes.c_char_p, sz], i),
+            "s2m_mesh_free": ([vp], None),
+            "s2m_write_stl": ([vp, vp, u64, ctypes.c_char_p], i),
+            "s2m_write_ply": ([vp, vp, u64, vp, u64, ctypes.c_char_p], i),
+            "s2m_measure_fp32_peak": ([dp, vp], i),
+            "s2m_mesh_set_profiling": ([vp, i], i),
+            "s2m_mesh_get_profile": ([vp, ctypes.POINTER(Profile)], i),
+            "s2m_mesh_reset_profile": ([vp], i),
+        }
+        for name, (args, res) in sigs.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        del c_char_pp
+        _lib = L
+        return L
+
+
+def _errbuf():
+    return ctypes.create_string_buffer(8192)
+
+
+def _check(rc: int, err=None, what: str = ""):
+    if rc != S2M_OK:
+        msg = err.value.decode(errors="replace") if err is not None else ""
+        raise S2MError(rc, f"{what}: {msg}" if what else msg)
+
+
+def _take_string(p: ctypes.c_void_p) -> str:
+    if not p.value:
+        return ""
+    s = ctypes.string_at(p.value).decode()
+    load_library().s2m_free_string(p)
+    return s
+
+
+# ---------------------------------------------------------------------------
+# Shader front end
+
+
+def translate(source: str, lang: int = LANG_WGSL, sdf_name: str = "sdf"):
+    """Lower an SDF source to CUDA C (frontend only, no GPU). Returns (cuda, fp32_ops, sfu_ops)."""
+    L = load_library()
+    out = ctypes.c_void_p()
+    fp, sfu = ctypes.c_double(), ctypes.c_double()
+    err = _errbuf()
+    rc = L.s2m_translate(source.encode(), lang, sdf_name.encode(), ctypes.byref(out), ctypes.byref(fp),
+                         ctypes.byref(sfu), err, len(err))
+    _check(rc, err, "translate")
+    return _take_string(out), fp.value, sfu.value
+
+
+def wgsl_remove_function(wgsl: str, function_name: str) -> str:
+    out = ctypes.c_void_p()
+    rc = load_library().s2m_wgsl_remove_function(wgsl.encode(), function_name.encode(), ctypes.byref(out))
+    if rc != S2M_OK:
+        raise S2MError(rc, f"Function {function_name} not found in shader")
+    return _take_string(out)
+
+
+def wgsl_rename_function(wgsl: str, old: str, new: str) -> str:
+    out = ctypes.c_void_p()
+    rc = load_library().s2m_wgsl_rename_function(wgsl.encode(), old.encode(), new.encode(), ctypes.byref(out))
+    if rc != S2M_OK:
+        raise S2MError(rc, f"Function `{old}` not found in shader")
+    return _take_string(out)
+
+
+def wgsl_has_function(wgsl: str, function_name: str) -> bool:
+    return bool(load_library().s2m_wgsl_has_function(wgsl.encode(), function_name.encode()))
+
+
+class CompiledSdf:
+    """An SDF compiled for sm_103a (frontend -> CUDA C -> NVRTC)."""
+
+    def __init__(self, handle: ctypes.c_void_p):
+        self._h = handle
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def cuda_source(self) -> str:
+        return load_library().s2m_sdf_cuda_source(self._h).decode()
+
+    def op_counts(self):
+        fp, sfu = ctypes.c_double(), ctypes.c_double()
+        load_library().s2m_sdf_op_counts(self._h, ctypes.byref(fp), ctypes.byref(sfu))
+        return fp.value, sfu.value
+
+    def close(self):
+        if self._h:
+            load_library().s2m_sdf_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Sdf3DShader:
+    """The SDF source: preprocessed WGSL (`.sdf3d`) or GLSL with a named function."""
+
+    source: str = ""
+    lang: int = LANG_WGSL
+    sdf_name: str = "sdf"
+
+    @classmethod
+    def from_path(cls, path: str) -> "Sdf3DShader":
+        """Read a .sdf3d file and expand its `use` / `include` lines (shader.rs:44-67)."""
+        L = load_library()
+        out = ctypes.c_void_p()
+        err = _errbuf()
+        _check(L.s2m_preprocess_file(os.fspath(path).encode(), ctypes.byref(out), err, len(err)), err, path)
+        return cls(_take_string(out), LANG_WGSL, "sdf")
+
+    @classmethod
+    def from_source(cls, source: str, lang: int = LANG_WGSL, sdf_name: str = "sdf",
+                    base_dir: str | None = None) -> "Sdf3DShader":
+        """In-memory source; WGSL gets the same `use` / `include` expansion as a file."""
+        if lang == LANG_WGSL:
+            L = load_library()
+            out = ctypes.c_void_p()
+            err = _errbuf()
+            _check(L.s2m_preprocess_source(source.encode(), (base_dir or "").encode(), ctypes.byref(out), err,
+                                           len(err)), err, "preprocess")
+            source = _take_string(out)
+        return cls(source, lang, sdf_name)
+
+    @classmethod
+    def from_glsl_fragment_shader(cls, path: str, sdf: str = "sdf") -> "Sdf3DShader":
+        with open(path) as f:
+            return cls(f.read(), LANG_GLSL, sdf)
+
+    def write_to_file(self, path: str) -> None:
+        with open(path, "w") as f:
+            f.write(self.source)
+
+    def compile(self, fmad: bool = False) -> CompiledSdf:
+        L = load_library()
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        rc = L.s2m_compile(self.source.encode(), self.lang, self.sdf_name.encode(),
+                           COMPILE_FMAD if fmad else 0, ctypes.byref(h), err, len(err))
+        _check(rc, err, "compile")
+        return CompiledSdf(h)
+
+
+@dataclass
+class AppState:
+    """Job parameters (main.rs:12-64, 139-175).
+
+    `reference_rounding` rounds a non-power-of-two resolution up as the
+    reference CLI does; `slice_lag` reproduces its read-before-submit lag.
+    """
+
+    resolution: int = 256
+    bounds: float = 2.0
+    eps: float = 1e-4
+    reference_rounding: bool = False
+    slice_lag: bool = False
+    exact_corners: bool = False
+    slab_depth: int = 0
+    max_vertices: int = 0
+    max_triangles: int = 0
+
+    @classmethod
+    def from_args(cls, resolution: int | None = None, bounds: float | None = None, **kw) -> "AppState":
+        """The reference CLI's defaults and quirks: N=256, B=2, pow2 rounding, slice lag."""
+        kw.setdefault("reference_rounding", True)
+        kw.setdefault("slice_lag", True)
+        return cls(resolution if resolution is not None else 256, bounds if bounds is not None else 2.0, **kw)
+
+    def params(self) -> Params:
+        flags = ((JOB_POW2_ROUNDING if self.reference_rounding else 0) | (JOB_SLICE_LAG if self.slice_lag else 0)
+                 | (JOB_EXACT_CORNERS if self.exact_corners else 0))
+        return Params(self.resolution, self.bounds, self.eps, flags, self.slab_depth, 0, self.max_vertices,
+                      self.max_triangles)
+
+
+class DeviceMesh:
+    """A mesh in device memory (owned by the library)."""
+
+    def __init__(self, handle: ctypes.c_void_p, sdf: CompiledSdf):
+        self._h = handle
+        self._sdf = sdf  # keep the module alive
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> MeshInfo:
+        mi = MeshInfo()
+        load_library().s2m_mesh_get_info(self._h, ctypes.byref(mi))
+        return mi
+
+    def run_async(self, stream: int = 0) -> None:
+        _check(load_library().s2m_mesh_run_async(self._h, ctypes.c_void_p(stream)), None, "run")
+
+    def sync(self, stream: int = 0) -> None:
+        err = _errbuf()
+        _check(load_library().s2m_mesh_sync(self._h, ctypes.c_void_p(stream), err, len(err)), err, "sync")
+
+    def set_profiling(self, enable: bool = True) -> None:
+        """Record CUDA events around every kernel of later runs."""
+        _check(load_library().s2m_mesh_set_profiling(self._h, 1 if enable else 0), None, "profiling")
+
+    def profile(self) -> dict:
+        """Accumulated per-kernel device time (ms) and launch counts."""
+        pr = Profile()
+        _check(load_library().s2m_mesh_get_profile(self._h, ctypes.byref(pr)), None, "profile")
+        return {"ms": {k: pr.ms[i] for i, k in enumerate(KERNEL_KINDS)},
+                "launches": {k: int(pr.launches[i]) for i, k in enumerate(KERNEL_KINDS)},
+                "eval_points": pr.eval_points, "cells": pr.cells}
+
+    def reset_profile(self) -> None:
+        _check(load_library().s2m_mesh_reset_profile(self._h), None, "profile")
+
+    def to_host(self, stream: int = 0) -> "TriangleMesh":
+        mi = self.info()
+        nv, nt = int(mi.nverts), int(mi.ntris)
+        pos = np.empty((nv, 3), np.float32)
+        nrm = np.empty((nv, 3), np.float32)
+        cell = np.empty(nv, np.uint64)
+        tris = np.empty((nt, 3), np.uint32)
+        _check(load_library().s2m_mesh_copy_to_host(self._h, pos.ctypes.data, nrm.ctypes.data, cell.ctypes.data,
+                                                     tris.ctypes.data, ctypes.c_void_p(stream)), None, "copy")
+        return TriangleMesh(pos, nrm, tris, cell, int(mi.invalid_quads), mi)
+
+    def write_to_file(self, path: str) -> None:
+        err = _errbuf()
+        _check(load_library().s2m_mesh_write(self._h, os.fspath(path).encode(), err, len(err)), err, "write")
+
+    def close(self):
+        if self._h:
+            load_library().s2m_mesh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class TriangleMesh:
+    """Host mesh: vertices (positions + normals) and triangle indices (mesh.rs:143-211)."""
+
+    positions: np.ndarray
+    normals: np.ndarray
+    triangle_indices: np.ndarray
+    cells: np.ndarray = field(default_factory=lambda: np.empty(0, np.uint64))
+    invalid_quads: int = 0
+    info: object = None
+
+    @property
+    def cell_xyz(self) -> np.ndarray:
+        """Cell labels (x, y, z) of each vertex (mesh.rs:213-227)."""
+        c = self.cells.astype(np.uint64)
+        return np.stack([c & 0xFFFF, (c >> 16) & 0xFFFF, (c >> 32) & 0xFFFF], axis=1).astype(np.uint16)
+
+    @property
+    def signs(self) -> np.ndarray:
+        return ((self.cells >> np.uint64(48)) & np.uint64(0xF)).astype(np.uint8)
+
+    def write_stl_to_file(self, path: str) -> None:
+        pos = np.ascontiguousarray(self.positions, np.float32)
+        tris = np.ascontiguousarray(self.triangle_indices, np.uint32)
+        _check(load_library().s2m_write_stl(pos.ctypes.data, tris.ctypes.data, len(tris), os.fspath(path).encode()),
+               None, f"write {path}")
+
+    def write_ply_to_file(self, path: str) -> None:
+        pos = np.ascontiguousarray(self.positions, np.float32)
+        nrm = np.ascontiguousarray(self.normals, np.float32)
+        tris = np.ascontiguousarray(self.triangle_indices, np.uint32)
+        _check(load_library().s2m_write_ply(pos.ctypes.data, nrm.ctypes.data, len(pos), tris.ctypes.data,
+                                            len(tris), os.fspath(path).encode()), None, f"write {path}")
+
+    def write_to_file(self, path: str) -> None:
+        ext = os.path.splitext(os.fspath(path))[1][1:].upper()
+        if ext == "STL":
+            self.write_stl_to_file(path)
+        elif ext == "PLY":
+            self.write_ply_to_file(path)
+        else:
+            raise S2MError(1, f"Unknown file extension: {ext}")
+
+
+def mesh_device(sdf, state: AppState, stream: int = 0) -> DeviceMesh:
+    """Run the whole pipeline on the GPU; the mesh stays in device memory."""
+    compiled = sdf.compile() if isinstance(sdf, Sdf3DShader) else sdf
+    L = load_library()
+    p = state.params()
+    h = ctypes.c_void_p()
+    err = _errbuf()
+    rc = L.s2m_mesh_create(compiled.handle, ctypes.byref(p), ctypes.c_void_p(stream), ctypes.byref(h), err, len(err))
+    _check(rc, err, "mesh")
+    return DeviceMesh(h, compiled)
+
+
+def generate(sdf, state: AppState | None = None, stream: int = 0) -> TriangleMesh:
+    """Shader (or compiled SDF) + job parameters -> host TriangleMesh."""
+    dm = mesh_device(sdf, state or AppState(), stream)
+    try:
+        return dm.to_host(stream)
+    finally:
+        dm.close()
+
+
+def measure_fp32_peak(stream: int = 0) -> float:
+    """Measured FP32 add/mul issue rate of the current GPU, Gop/s."""
+    g = ctypes.c_double()
+    _check(load_library().s2m_measure_fp32_peak(ctypes.byref(g), ctypes.c_void_p(stream)), None, "fp32 probe")
+    return g.value

@@ -1,0 +1,764 @@
+// runtime.cu -- libsdf2mesh_gb300.so: NVRTC compilation of lowered SDFs,
+// the slab-streamed dual-contouring pipeline on one GB300, and the C ABI
+// declared in include/sdf2mesh.h.
+//
+// Pipeline of one job (reference: src/bin/sdf2mesh/main.rs:298-363 and
+// src/mesh.rs:267-341, which run one z-slice per dispatch with a host
+// round-trip each):
+//   for each slab of D cell slices:
+//     s2m_eval_planes   lattice planes of the slab into an L2-sized ring (NVRTC)
+//     s2m_cells         classify cells, exact corners, vertices   (NVRTC)
+//     s2m_vcompact      ordered vertex compaction, row counts     (nvcc)
+//   s2m_rowscan         row starts of the sorted vertex list      (nvcc)
+//   s2m_quads           quads -> triangles, ordered               (nvcc)
+// Everything is stream-ordered; the host reads back a few counters at the end.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/sdf2mesh.h"
+#include "frontend.h"
+#include "mesh_io.h"
+#include "s2m_device.h"
+#include "static_kernels.cuh"
+
+// Sources embedded at build time (s2m_embedded.inc is generated from the
+// .cuh / .h files by build.py).
+#include "s2m_embedded.inc"
+
+namespace {
+
+void set_err(char *err, size_t errlen, const std::string &msg) {
+  if (!err || errlen == 0) return;
+  size_t n = std::min(errlen - 1, msg.size());
+  std::memcpy(err, msg.data(), n);
+  err[n] = 0;
+}
+
+char *dup_string(const std::string &s) {
+  char *p = static_cast<char *>(std::malloc(s.size() + 1));
+  if (p) std::memcpy(p, s.c_str(), s.size() + 1);
+  return p;
+}
+
+#define S2_CUDA(call)                                                                          \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      set_err(err, errlen, std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+      return e_ == cudaErrorMemoryAllocation ? S2M_E_OOM : S2M_E_CUDA;                         \
+    }                                                                                          \
+  } while (0)
+
+int device_sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+  }
+  return sms;
+}
+
+}  // namespace
+
+struct s2m_sdf {
+  std::string user_cuda;
+  double fp32_ops = 0, sfu_ops = 0;
+  uint32_t flags = 0;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t k_eval = nullptr, k_cells = nullptr;
+};
+
+struct s2m_mesh {
+  const s2m_sdf *sdf = nullptr;
+  s2m_params params{};
+  S2Job job{};
+  int N = 0, D = 0, nzc = 0, nslabs = 0;
+  // workspace
+  float *ring = nullptr;
+  unsigned long long *slab_ctrl = nullptr;  // [cell status | vc status | counters]
+  size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
+  unsigned long long *cand_key = nullptr;
+  float *cand_pos = nullptr, *cand_nrm = nullptr;
+  unsigned long long cand_cap = 0;
+  unsigned long long *cand_totals = nullptr;  // nslabs
+  // outputs and job counters
+  float *pos = nullptr, *nrm = nullptr;
+  unsigned long long *key = nullptr;
+  unsigned *tris = nullptr;
+  unsigned long long vcap = 0, tcap = 0;
+  unsigned long long *vbase = nullptr;  // nslabs + 1
+  unsigned *rowcnt = nullptr, *rowstart = nullptr;
+  unsigned long long *scan_status = nullptr;
+  size_t scan_tiles = 0, quad_tiles = 0;
+  unsigned long long *jobctl = nullptr;  // [ntris, invalid, ncand, err | counters[8]]
+  // host results
+  unsigned long long *h_read = nullptr;  // pinned readback
+  uint64_t nverts = 0, ntris = 0, invalid = 0, ncand = 0;
+  uint32_t errflags = 0;
+  uint64_t launches = 0;
+  // optional per-kernel timing: an event pair around each launch
+  bool profile = false;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ev_kind;
+  std::vector<double> ev_units;
+  size_t ev_used = 0;
+  s2m_profile prof{};
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// NVRTC
+
+int compile_module(s2m_sdf *s, char *err, size_t errlen) {
+  std::string src;
+  src += "// sdf2mesh_gb300 per-SDF module\n";
+  src += kS2mDeviceH;
+  src += kS2mLookbackCuh;
+  src += kS2mPreludeCuh;
+  src += s->user_cuda;
+  src += kS2mDcKernelsCuh;
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "s2m_module.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+    set_err(err, errlen, "nvrtcCreateProgram failed");
+    return S2M_E_NVRTC;
+  }
+  std::vector<const char *> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device",
+                                    "-lineinfo", "--extra-device-vectorization"};
+  opts.push_back((s->flags & S2M_COMPILE_FMAD) ? "--fmad=true" : "--fmad=false");
+  nvrtcResult rc = nvrtcCompileProgram(prog, int(opts.size()), opts.data());
+  if (rc != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    if (n) nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    set_err(err, errlen, std::string("NVRTC: ") + nvrtcGetErrorString(rc) + "\n" + log);
+    return S2M_E_NVRTC;
+  }
+  size_t cubin_n = 0;
+  nvrtcGetCUBINSize(prog, &cubin_n);
+  std::vector<char> cubin(cubin_n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  cudaError_t ce = cudaLibraryLoadData(&s->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (ce != cudaSuccess) {
+    set_err(err, errlen, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce));
+    return ce == cudaErrorNoDevice || ce == cudaErrorInsufficientDriver ? S2M_E_NO_DEVICE : S2M_E_CUDA;
+  }
+  if (cudaLibraryGetKernel(&s->k_eval, s->lib, "s2m_eval_planes") != cudaSuccess ||
+      cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess) {
+    set_err(err, errlen, "kernels missing from the compiled module");
+    return S2M_E_CUDA;
+  }
+  return S2M_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Job setup
+
+// main.rs:139-148: a resolution that is not a power of two becomes 2 << ilog2.
+uint32_t reference_resolution(uint32_t r) {
+  if (__builtin_popcount(r) > 1) {
+    uint32_t lg = 31u - uint32_t(__builtin_clz(r));
+    r = 2u << lg;
+  }
+  return r;
+}
+
+void free_buffers(s2m_mesh *m) {
+  void *ptrs[] = {m->ring, m->slab_ctrl, m->cand_key, m->cand_pos, m->cand_nrm, m->cand_totals, m->pos, m->nrm,
+                  m->key, m->tris, m->vbase, m->rowcnt, m->rowstart, m->scan_status, m->jobctl};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (m->h_read) cudaFreeHost(m->h_read);
+  m->ring = nullptr; m->slab_ctrl = nullptr; m->cand_key = nullptr; m->cand_pos = nullptr; m->cand_nrm = nullptr;
+  m->cand_totals = nullptr; m->pos = nullptr; m->nrm = nullptr; m->key = nullptr; m->tris = nullptr;
+  m->vbase = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr; m->jobctl = nullptr;
+  m->h_read = nullptr;
+}
+
+int setup_job(s2m_mesh *m, char *err, size_t errlen) {
+  const s2m_params &p = m->params;
+  uint32_t N = p.resolution;
+  if (p.flags & S2M_JOB_POW2_ROUNDING) N = reference_resolution(N);
+  if (N < 2 || N > 65535) {
+    set_err(err, errlen, "resolution must be in [2, 65535]");
+    return S2M_E_INVALID;
+  }
+  if (!(p.bounds > 0.0f) || !std::isfinite(p.bounds)) {
+    set_err(err, errlen, "bounds must be a positive finite number");
+    return S2M_E_INVALID;
+  }
+  m->N = int(N);
+  S2Job &j = m->job;
+  j.N = int(N);
+  j.P = int(N) + 1;
+  j.pitch = (j.P + 31) / 32 * 32;
+  j.plane = (long long)j.P * j.pitch;
+  // Bounds3D::cube(B, 0) in binary32 (lib.rs:115-118), size per
+  // dualcontour.wgsl:23-24.
+  volatile float half = p.bounds * 0.5f;
+  volatile float mn = 0.0f - half;
+  volatile float mx = 0.0f + half;
+  volatile float ext = mx - mn;
+  j.bmin = mn;
+  j.size = ext / float(N - 1u);
+  j.eps = p.eps;
+  j.guard = j.size;  // one cell: far above any rounding difference of a corner
+  j.lag = (p.flags & S2M_JOB_SLICE_LAG) ? 1 : 0;
+  j.exact = (p.flags & S2M_JOB_EXACT_CORNERS) ? 1 : 0;
+  m->nzc = j.lag ? int(N) - 1 : int(N);
+  // Slab depth: the ring of D + 1 lattice planes is sized to stay resident in
+  // the 126 MB L2 between the evaluation and the cell pass.
+  int D = int(p.slab_depth);
+  if (D <= 0) {
+    double plane_bytes = double(j.plane) * 4.0;
+    D = int(48.0e6 / plane_bytes) - 1;
+    D = std::max(1, std::min(D, 64));
+  }
+  D = std::max(1, std::min(D, std::max(1, m->nzc)));
+  m->D = D;
+  j.ring = D + 1;
+  m->nslabs = m->nzc > 0 ? (m->nzc + D - 1) / D : 0;
+  return S2M_OK;
+}
+
+int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long vcap, unsigned long long tcap,
+                  char *err, size_t errlen) {
+  free_buffers(m);
+  const S2Job &j = m->job;
+  const unsigned long long N = (unsigned long long)m->N;
+  const unsigned long long cells_per_slab = (unsigned long long)m->D * N * N;
+  m->cand_cap = std::max<unsigned long long>(1024, std::min(cand_cap, cells_per_slab));
+  m->vcap = std::max<unsigned long long>(1024, vcap);
+  m->tcap = std::max<unsigned long long>(2048, tcap);
+  m->cell_tiles = (cells_per_slab + S2_CELL_TILE - 1) / S2_CELL_TILE;
+  m->vc_tiles = (m->cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
+  m->slab_ctrl_words = m->cell_tiles + m->vc_tiles + 1;
+  m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
+  m->quad_tiles = (m->vcap + S2_Q_TILE - 1) / S2_Q_TILE;
+  size_t ring_floats = size_t(j.ring) * size_t(j.plane);
+  S2_CUDA(cudaMalloc(&m->ring, ring_floats * sizeof(float)));
+  S2_CUDA(cudaMalloc(&m->slab_ctrl, m->slab_ctrl_words * 8));
+  S2_CUDA(cudaMalloc(&m->cand_key, m->cand_cap * 8));
+  S2_CUDA(cudaMalloc(&m->cand_pos, m->cand_cap * 12));
+  S2_CUDA(cudaMalloc(&m->cand_nrm, m->cand_cap * 12));
+  S2_CUDA(cudaMalloc(&m->cand_totals, size_t(std::max(1, m->nslabs)) * 8));
+  S2_CUDA(cudaMalloc(&m->pos, m->vcap * 12));
+  S2_CUDA(cudaMalloc(&m->nrm, m->vcap * 12));
+  S2_CUDA(cudaMalloc(&m->key, m->vcap * 8));
+  S2_CUDA(cudaMalloc(&m->tris, m->tcap * 12));
+  S2_CUDA(cudaMalloc(&m->vbase, size_t(m->nslabs + 1) * 8));
+  S2_CUDA(cudaMalloc(&m->rowcnt, N * N * 4));
+  S2_CUDA(cudaMalloc(&m->rowstart, (N * N + 1) * 4));
+  S2_CUDA(cudaMalloc(&m->scan_status, (m->scan_tiles + m->quad_tiles) * 8));
+  S2_CUDA(cudaMalloc(&m->jobctl, 8 * 8));
+  S2_CUDA(cudaMallocHost(&m->h_read, size_t(8 + m->nslabs + 1) * 8));
+  return S2M_OK;
+}
+
+// Device pointers of the counters inside jobctl.
+struct JobCtl {
+  unsigned long long *ntris, *invalid, *ncand;
+  unsigned *err;
+  unsigned *counters;
+};
+JobCtl jobctl(const s2m_mesh *m) {
+  JobCtl c;
+  c.ntris = m->jobctl + 0;
+  c.invalid = m->jobctl + 1;
+  c.ncand = m->jobctl + 2;
+  c.err = reinterpret_cast<unsigned *>(m->jobctl + 3);
+  c.counters = reinterpret_cast<unsigned *>(m->jobctl + 4);  // 8 x u32
+  return c;
+}
+
+// Two events per launch when profiling (created once, reused every run).
+cudaError_t prof_mark(s2m_mesh *m, cudaStream_t st, int kind, double units, bool after) {
+  if (!m->profile) return cudaSuccess;
+  if (m->ev_used == m->ev.size()) {
+    cudaEvent_t e;
+    cudaError_t rc = cudaEventCreate(&e);
+    if (rc != cudaSuccess) return rc;
+    m->ev.push_back(e);
+    m->ev_kind.push_back(0);
+    m->ev_units.push_back(0);
+  }
+  if (!after) {
+    m->ev_kind[m->ev_used] = kind;
+    m->ev_units[m->ev_used] = units;
+  }
+  return cudaEventRecord(m->ev[m->ev_used++], st);
+}
+
+void prof_collect(s2m_mesh *m) {
+  for (size_t i = 0; i + 1 < m->ev_used; i += 2) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, m->ev[i], m->ev[i + 1]) != cudaSuccess) continue;
+    int k = m->ev_kind[i];
+    m->prof.ms[k] += ms;
+    m->prof.launches[k] += 1;
+    if (k == 0) m->prof.eval_points += m->ev_units[i];
+    if (k == 1) m->prof.cells += m->ev_units[i];
+  }
+  m->ev_used = 0;
+}
+
+#define S2_LAUNCH(kind, units, call)                                   \
+  do {                                                                 \
+    cudaError_t e_ = prof_mark(m, st, kind, double(units), false);     \
+    if (e_ != cudaSuccess) return e_;                                  \
+    if ((e_ = (call)) != cudaSuccess) return e_;                       \
+    if ((e_ = prof_mark(m, st, kind, 0, true)) != cudaSuccess) return e_; \
+    ++m->launches;                                                     \
+  } while (0)
+
+cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
+  const S2Job &j = m->job;
+  const JobCtl c = jobctl(m);
+  const unsigned long long N = (unsigned long long)m->N;
+  const int sms = device_sm_count();
+  m->launches = 0;
+  m->ev_used = 0;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(m->jobctl, 0, 8 * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->vbase, 0, size_t(m->nslabs + 1) * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->rowcnt, 0, N * N * 4, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->scan_status, 0, (m->scan_tiles + m->quad_tiles) * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->cand_totals, 0, size_t(std::max(1, m->nslabs)) * 8, st)) != cudaSuccess) return e;
+
+  S2Slab slab;
+  slab.ring = m->ring;
+  slab.status = m->slab_ctrl;
+  slab.status2 = m->slab_ctrl + m->cell_tiles;
+  slab.tile_counter = reinterpret_cast<unsigned *>(m->slab_ctrl + m->cell_tiles + m->vc_tiles);
+  slab.cand_key = m->cand_key;
+  slab.cand_pos = m->cand_pos;
+  slab.cand_nrm = m->cand_nrm;
+  slab.cand_cap = m->cand_cap;
+  slab.err = c.err;
+
+  S2MeshDev md;
+  md.pos = m->pos;
+  md.nrm = m->nrm;
+  md.key = m->key;
+  md.tris = m->tris;
+  md.vcap = m->vcap;
+  md.tcap = m->tcap;
+  md.vbase = m->vbase;
+  md.rowcnt = m->rowcnt;
+  md.rowstart = m->rowstart;
+  md.scan_status = m->scan_status;
+  md.counters = c.counters;
+  md.ntris = c.ntris;
+  md.invalid = c.invalid;
+  md.ncand = c.ncand;
+  md.err = c.err;
+
+  const long long pts = (long long)j.P * j.P;
+  const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
+  const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
+  for (int s = 0; s < m->nslabs; ++s) {
+    int zc0 = s * m->D;
+    int zc1 = std::min(m->nzc, zc0 + m->D);
+    int k0 = s == 0 ? 0 : zc0 + 1;
+    int nk = zc1 - k0 + 1;
+    S2Job jj = j;
+    float *ring = m->ring;
+    void *eargs[] = {&jj, &ring, &k0, &nk};
+    dim3 eg(eval_blocks, unsigned((nk + S2_EVAL_RUN - 1) / S2_EVAL_RUN));
+    S2_LAUNCH(0, double(pts) * nk,
+              cudaLaunchKernel((const void *)m->sdf->k_eval, eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
+    if ((e = cudaMemsetAsync(m->slab_ctrl, 0, m->slab_ctrl_words * 8, st)) != cudaSuccess) return e;
+    slab.cand_total = m->cand_totals + s;
+    unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
+    unsigned cg = unsigned((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
+    void *cargs[] = {&jj, &slab, &zc0, &zc1};
+    S2_LAUNCH(1, ncells, cudaLaunchKernel((const void *)m->sdf->k_cells, dim3(cg), dim3(S2_CELL_BLOCK), cargs, 0, st));
+    S2_LAUNCH(2, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, slab, md, s), cudaGetLastError()));
+  }
+  const unsigned scan_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->scan_tiles, size_t(sms) * 8)));
+  S2_LAUNCH(3, 0, (s2m_rowscan<<<scan_grid, S2_SCAN_BLOCK, 0, st>>>(md, N * N), cudaGetLastError()));
+  const unsigned q_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->quad_tiles, size_t(sms) * 8)));
+  S2_LAUNCH(4, 0, (s2m_quads<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, m->nslabs, unsigned(m->scan_tiles)),
+                   cudaGetLastError()));
+  return cudaSuccess;
+}
+
+int readback(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
+  S2_CUDA(cudaMemcpyAsync(m->h_read, m->jobctl, 4 * 8, cudaMemcpyDeviceToHost, st));
+  S2_CUDA(cudaMemcpyAsync(m->h_read + 4, m->vbase + m->nslabs, 8, cudaMemcpyDeviceToHost, st));
+  S2_CUDA(cudaMemcpyAsync(m->h_read + 8, m->cand_totals, size_t(std::max(1, m->nslabs)) * 8,
+                          cudaMemcpyDeviceToHost, st));
+  S2_CUDA(cudaStreamSynchronize(st));
+  prof_collect(m);
+  m->ntris = m->h_read[0];
+  m->invalid = m->h_read[1];
+  m->errflags = unsigned(m->h_read[3] & 0xffffffffull);
+  m->nverts = m->h_read[4];
+  m->ncand = 0;
+  for (int s = 0; s < m->nslabs; ++s) m->ncand += m->h_read[8 + s];
+  return S2M_OK;
+}
+
+unsigned long long max_slab_candidates(const s2m_mesh *m) {
+  unsigned long long mx = 0;
+  for (int s = 0; s < m->nslabs; ++s) mx = std::max(mx, m->h_read[8 + s]);
+  return mx;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+
+extern "C" {
+
+int s2m_abi_version(void) { return S2M_ABI_VERSION; }
+
+const char *s2m_status_string(int s) {
+  switch (s) {
+    case S2M_OK: return "ok";
+    case S2M_E_INVALID: return "invalid argument";
+    case S2M_E_IO: return "i/o error";
+    case S2M_E_PARSE: return "parse error";
+    case S2M_E_MISSING_SDF: return "missing sdf function";
+    case S2M_E_NVRTC: return "NVRTC compile error";
+    case S2M_E_CUDA: return "CUDA error";
+    case S2M_E_OOM: return "out of device memory";
+    case S2M_E_OVERFLOW: return "mesh too large";
+    case S2M_E_TIMEOUT: return "device wait timed out";
+    case S2M_E_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+void s2m_free_string(char *s) { std::free(s); }
+
+int s2m_preprocess_file(const char *path, char **out, char *err, size_t errlen) {
+  if (!path || !out) return S2M_E_INVALID;
+  std::string text, e;
+  if (!s2m::preprocess_sdf3d_file(path, text, e, nullptr)) {
+    set_err(err, errlen, e);
+    return S2M_E_IO;
+  }
+  *out = dup_string(text);
+  return S2M_OK;
+}
+
+int s2m_preprocess_source(const char *source, const char *base_dir, char **out, char *err, size_t errlen) {
+  if (!source || !out) {
+    set_err(err, errlen, "null argument");
+    return S2M_E_INVALID;
+  }
+  *out = dup_string(s2m::preprocess_sdf3d_text(source, "", base_dir ? base_dir : "", nullptr));
+  return S2M_OK;
+}
+
+int s2m_translate(const char *source, int lang, const char *sdf_name, char **out, double *fp32_ops,
+                  double *sfu_ops, char *err, size_t errlen) {
+  if (!source) return S2M_E_INVALID;
+  s2m::FrontendResult r = s2m::translate(source, lang == S2M_LANG_GLSL ? s2m::Lang::GLSL : s2m::Lang::WGSL,
+                                         sdf_name ? sdf_name : "sdf");
+  if (!r.ok) {
+    set_err(err, errlen, r.error);
+    return r.status ? r.status : S2M_E_PARSE;
+  }
+  if (out) *out = dup_string(r.cuda);
+  if (fp32_ops) *fp32_ops = r.fp32_ops;
+  if (sfu_ops) *sfu_ops = r.sfu_ops;
+  return S2M_OK;
+}
+
+int s2m_compile(const char *source, int lang, const char *sdf_name, uint32_t compile_flags, s2m_sdf **out,
+                char *err, size_t errlen) {
+  if (!source || !out) return S2M_E_INVALID;
+  *out = nullptr;
+  s2m::FrontendResult r = s2m::translate(source, lang == S2M_LANG_GLSL ? s2m::Lang::GLSL : s2m::Lang::WGSL,
+                                         sdf_name ? sdf_name : "sdf");
+  if (!r.ok) {
+    set_err(err, errlen, r.error);
+    return r.status ? r.status : S2M_E_PARSE;
+  }
+  s2m_sdf *s = new s2m_sdf();
+  s->user_cuda = r.cuda;
+  s->fp32_ops = r.fp32_ops;
+  s->sfu_ops = r.sfu_ops;
+  s->flags = compile_flags;
+  int rc = compile_module(s, err, errlen);
+  if (rc != S2M_OK) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return S2M_OK;
+}
+
+int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t compile_flags, s2m_sdf **out,
+                     char *err, size_t errlen) {
+  if (!path || !out) return S2M_E_INVALID;
+  std::string text;
+  if (lang == S2M_LANG_GLSL) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) {
+      set_err(err, errlen, std::string("could not read ") + path);
+      return S2M_E_IO;
+    }
+    std::ostringstream ss;
+    ss << f.rdbuf();
+    text = ss.str();
+  } else {
+    std::string e;
+    if (!s2m::preprocess_sdf3d_file(path, text, e, nullptr)) {
+      set_err(err, errlen, e);
+      return S2M_E_IO;
+    }
+  }
+  return s2m_compile(text.c_str(), lang, sdf_name, compile_flags, out, err, errlen);
+}
+
+const char *s2m_sdf_cuda_source(const s2m_sdf *sdf) { return sdf ? sdf->user_cuda.c_str() : nullptr; }
+
+int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
+  if (!sdf) return S2M_E_INVALID;
+  if (fp32_ops) *fp32_ops = sdf->fp32_ops;
+  if (sfu_ops) *sfu_ops = sdf->sfu_ops;
+  return S2M_OK;
+}
+
+void s2m_sdf_free(s2m_sdf *sdf) {
+  if (!sdf) return;
+  if (sdf->lib) cudaLibraryUnload(sdf->lib);
+  delete sdf;
+}
+
+int s2m_wgsl_remove_function(const char *wgsl, const char *fn, char **out) {
+  if (!wgsl || !fn || !out) return S2M_E_INVALID;
+  std::string r;
+  bool found = s2m::wgsl_remove_function(wgsl, fn, r);
+  *out = found ? dup_string(r) : nullptr;
+  return found ? S2M_OK : S2M_E_MISSING_SDF;
+}
+
+int s2m_wgsl_rename_function(const char *wgsl, const char *old_name, const char *new_name, char **out) {
+  if (!wgsl || !old_name || !new_name || !out) return S2M_E_INVALID;
+  std::string r;
+  bool found = s2m::wgsl_rename_function(wgsl, old_name, new_name, r);
+  *out = found ? dup_string(r) : nullptr;
+  return found ? S2M_OK : S2M_E_MISSING_SDF;
+}
+
+int s2m_wgsl_has_function(const char *wgsl, const char *fn) {
+  if (!wgsl || !fn) return 0;
+  return s2m::wgsl_has_function(wgsl, fn) ? 1 : 0;
+}
+
+int s2m_mesh_run_async(s2m_mesh *m, void *stream) {
+  if (!m || !m->sdf) return S2M_E_INVALID;
+  cudaError_t e = enqueue(m, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? S2M_E_OOM : S2M_E_CUDA;
+  return S2M_OK;
+}
+
+int s2m_mesh_sync(s2m_mesh *m, void *stream, char *err, size_t errlen) {
+  if (!m) return S2M_E_INVALID;
+  int rc = readback(m, static_cast<cudaStream_t>(stream), err, errlen);
+  if (rc != S2M_OK) return rc;
+  if (m->errflags & S2_ERR_LOOKBACK) {
+    set_err(err, errlen, "a device-side look-back wait hit its limit");
+    return S2M_E_TIMEOUT;
+  }
+  if (m->errflags & S2_ERR_INDEX_OVF) {
+    set_err(err, errlen, "more than 2^32 - 2 vertices");
+    return S2M_E_OVERFLOW;
+  }
+  if (m->errflags & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF)) {
+    set_err(err, errlen, "mesh buffers overflowed");
+    return S2M_E_OVERFLOW;
+  }
+  return S2M_OK;
+}
+
+int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, s2m_mesh **out, char *err,
+                    size_t errlen) {
+  if (!sdf || !params || !out) return S2M_E_INVALID;
+  *out = nullptr;
+  s2m_mesh *m = new s2m_mesh();
+  m->sdf = sdf;
+  m->params = *params;
+  if (!(m->params.eps > 0.0f)) m->params.eps = 1e-4f;
+  int rc = setup_job(m, err, errlen);
+  if (rc != S2M_OK) {
+    delete m;
+    return rc;
+  }
+  const unsigned long long N = (unsigned long long)m->N;
+  const unsigned long long cells_per_slab = (unsigned long long)m->D * N * N;
+  unsigned long long cand_cap = std::min(cells_per_slab, cells_per_slab / 8 + 65536);
+  unsigned long long vcap = params->max_vertices ? params->max_vertices
+                                                 : std::min(N * N * N, std::max<unsigned long long>(65536, 12 * N * N));
+  unsigned long long tcap = params->max_triangles ? params->max_triangles : std::max<unsigned long long>(131072, 3 * vcap);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen);
+    if (rc != S2M_OK) break;
+    cudaError_t e = enqueue(m, st);
+    if (e != cudaSuccess) {
+      set_err(err, errlen, std::string("launch: ") + cudaGetErrorString(e));
+      rc = S2M_E_CUDA;
+      break;
+    }
+    rc = readback(m, st, err, errlen);
+    if (rc != S2M_OK) break;
+    if (m->errflags & S2_ERR_LOOKBACK) {
+      set_err(err, errlen, "a device-side look-back wait hit its limit");
+      rc = S2M_E_TIMEOUT;
+      break;
+    }
+    if (m->errflags & S2_ERR_INDEX_OVF) {
+      set_err(err, errlen, "more than 2^32 - 2 vertices");
+      rc = S2M_E_OVERFLOW;
+      break;
+    }
+    if (!(m->errflags & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF))) {
+      rc = S2M_OK;
+      break;
+    }
+    // Exact totals are known even after an overflow: grow to them and re-run.
+    if (m->errflags & S2_ERR_CAND_OVF) cand_cap = std::min(cells_per_slab, max_slab_candidates(m) + 4096);
+    if (m->errflags & (S2_ERR_VERT_OVF | S2_ERR_CAND_OVF)) vcap = std::max<unsigned long long>(vcap, m->nverts + m->nverts / 8 + 4096);
+    if (m->errflags & S2_ERR_CAND_OVF) vcap = std::max(vcap, std::min(N * N * N, 2 * vcap));
+    tcap = std::max<unsigned long long>(tcap, std::max<unsigned long long>(m->ntris + m->ntris / 8 + 4096, 3 * vcap));
+    rc = S2M_E_OVERFLOW;
+    set_err(err, errlen, "mesh buffers overflowed after resizing");
+  }
+  if (rc != S2M_OK) {
+    free_buffers(m);
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return S2M_OK;
+}
+
+int s2m_mesh_get_info(const s2m_mesh *m, s2m_mesh_info *info) {
+  if (!m || !info) return S2M_E_INVALID;
+  std::memset(info, 0, sizeof(*info));
+  info->nverts = m->nverts;
+  info->ntris = m->ntris;
+  info->invalid_quads = m->invalid;
+  info->cells = (uint64_t)m->N * m->N * m->N;
+  info->candidate_cells = m->ncand;
+  info->resolution = uint32_t(m->N);
+  info->slab_depth = uint32_t(m->D);
+  info->d_pos = m->pos;
+  info->d_nrm = m->nrm;
+  info->d_cell = reinterpret_cast<const uint64_t *>(m->key);
+  info->d_tris = m->tris;
+  info->kernel_launches = m->launches;
+  return S2M_OK;
+}
+
+int s2m_mesh_copy_to_host(const s2m_mesh *m, float *pos, float *nrm, uint64_t *cell, uint32_t *tris, void *stream) {
+  if (!m) return S2M_E_INVALID;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  if (pos && m->nverts) e = cudaMemcpyAsync(pos, m->pos, m->nverts * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && nrm && m->nverts) e = cudaMemcpyAsync(nrm, m->nrm, m->nverts * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && cell && m->nverts) e = cudaMemcpyAsync(cell, m->key, m->nverts * 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && tris && m->ntris) e = cudaMemcpyAsync(tris, m->tris, m->ntris * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? S2M_OK : S2M_E_CUDA;
+}
+
+int s2m_mesh_write(const s2m_mesh *m, const char *path, char *err, size_t errlen) {
+  if (!m || !path) return S2M_E_INVALID;
+  std::vector<float> pos(m->nverts * 3), nrm(m->nverts * 3);
+  std::vector<uint32_t> tris(m->ntris * 3);
+  int rc = s2m_mesh_copy_to_host(m, pos.data(), nrm.data(), nullptr, tris.data(), nullptr);
+  if (rc != S2M_OK) {
+    set_err(err, errlen, "device to host copy failed");
+    return rc;
+  }
+  return s2m::write_mesh_file(path, pos.data(), nrm.data(), m->nverts, tris.data(), m->ntris, err, errlen);
+}
+
+int s2m_mesh_set_profiling(s2m_mesh *m, int enable) {
+  if (!m) return S2M_E_INVALID;
+  m->profile = enable != 0;
+  return S2M_OK;
+}
+
+int s2m_mesh_get_profile(const s2m_mesh *m, s2m_profile *out) {
+  if (!m || !out) return S2M_E_INVALID;
+  *out = m->prof;
+  return S2M_OK;
+}
+
+int s2m_mesh_reset_profile(s2m_mesh *m) {
+  if (!m) return S2M_E_INVALID;
+  m->prof = s2m_profile{};
+  return S2M_OK;
+}
+
+void s2m_mesh_free(s2m_mesh *m) {
+  if (!m) return;
+  for (cudaEvent_t e : m->ev) cudaEventDestroy(e);
+  free_buffers(m);
+  delete m;
+}
+
+int s2m_write_stl(const float *pos, const uint32_t *tris, uint64_t ntris, const char *path) {
+  return s2m::write_stl(path, pos, tris, ntris) ? S2M_OK : S2M_E_IO;
+}
+
+int s2m_write_ply(const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris, uint64_t ntris,
+                  const char *path) {
+  return s2m::write_ply(path, pos, nrm, nverts, tris, ntris) ? S2M_OK : S2M_E_IO;
+}
+
+int s2m_measure_fp32_peak(double *gops, void *stream) {
+  if (!gops) return S2M_E_INVALID;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int sms = device_sm_count();
+  const int blocks = sms * 8, iters = 8192;
+  float *out = nullptr;
+  if (cudaMalloc(&out, size_t(blocks) * 4) != cudaSuccess) return S2M_E_OOM;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, st);
+    s2m_fp32_probe<<<blocks, 256, 0, st>>>(out, iters, 0, 0.999f, 1e-3f);
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    double ops = double(blocks) * 256.0 * iters * 8.0 * 2.0;
+    if (rep > 0) best = std::max(best, ops / (double(ms) * 1e-3) / 1e9);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return S2M_E_CUDA;
+  *gops = best;
+  return S2M_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// s2m_device.h -- structures shared by the host runtime, the nvcc-compiled
+// kernels and the NVRTC-compiled per-SDF kernels.  Plain C types only (NVRTC
+// compiles this without system headers).
+#pragma once
+
+// Lattice: grid point (i, j, k), 0 <= i, j, k <= N, has the coordinates
+// c(i) = bmin + size * i, rounded in binary32 exactly as the reference
+// computes a cell's lower corner (dualcontour.wgsl:22-27).  Planes of the
+// lattice live in a ring of `ring` planes; plane k sits in slot k % ring,
+// row j at offset j * pitch, so a z-slab of cells and its upper plane are
+// resident together.
+struct S2Job {
+  int N;                   // cells per axis
+  int P;                   // lattice points per axis (N + 1)
+  int pitch;               // floats per lattice row (P rounded up to 32)
+  int ring;                // planes in the ring
+  long long plane;         // floats per plane (P * pitch)
+  float bmin;              // lower corner of the box (same on every axis)
+  float size;              // cell edge (bmax - bmin) / (N - 1)
+  float eps;               // normal epsilon
+  float guard;             // |f| below which off-lattice corners are re-evaluated
+  int lag;                 // 1: labels are z + 1 (reference slice lag)
+  int exact;               // 1: re-evaluate off-lattice corners of every cell
+};
+
+// Per-slab buffers of the cell pass.
+struct S2Slab {
+  float *ring;                    // lattice ring
+  unsigned long long *status;     // look-back words of s2m_cells tiles
+  unsigned long long *status2;    // look-back words of s2m_vcompact tiles
+  unsigned *tile_counter;         // [0] s2m_cells, [1] s2m_vcompact
+  unsigned long long *cand_key;   // candidate results (key | has_vertex << 63)
+  float *cand_pos;                // 3 per candidate
+  float *cand_nrm;                // 3 per candidate
+  unsigned long long cand_cap;    // capacity of the candidate arrays
+  unsigned long long *cand_total; // out: candidates of this slab (exact even on overflow)
+  unsigned *err;                  // error flags (S2_ERR_*)
+};
+
+// Mesh outputs and the cross-slab counters.
+struct S2MeshDev {
+  float *pos;                     // 3 * vcap
+  float *nrm;                     // 3 * vcap
+  unsigned long long *key;        // vcap: x | y << 16 | z << 32 | signs << 48
+  unsigned *tris;                 // 3 * tcap
+  unsigned long long vcap;
+  unsigned long long tcap;
+  unsigned long long *vbase;      // nslabs + 1 running vertex offsets
+  unsigned *rowcnt;               // N * N vertices per (z label, y) row
+  unsigned *rowstart;             // N * N + 1 exclusive prefix of rowcnt
+  unsigned long long *scan_status;  // look-back words (row scan, quads)
+  unsigned *counters;             // [2] row scan, [3] quads tile counters
+  unsigned long long *ntris;      // out: triangles (exact even on overflow)
+  unsigned long long *invalid;    // out: invalid quads (mesh.rs:275-277)
+  unsigned long long *ncand;      // out: candidates over all slabs
+  unsigned *err;
+};
+
+#define S2_ERR_LOOKBACK 0x1u      /* a look-back wait hit its iteration limit   */
+#define S2_ERR_CAND_OVF 0x2u      /* candidate arrays too small                 */
+#define S2_ERR_VERT_OVF 0x4u      /* vertex arrays too small                    */
+#define S2_ERR_TRI_OVF 0x8u       /* triangle array too small                   */
+#define S2_ERR_INDEX_OVF 0x10u    /* more than 2^32 - 2 vertices                */
+
+#define S2_CELL_BLOCK 256
+#define S2_CELL_CPT 4
+#define S2_CELL_TILE (S2_CELL_BLOCK * S2_CELL_CPT)
+#define S2_EVAL_BLOCK 256
+#define S2_EVAL_RUN 4
+#define S2_VC_BLOCK 256
+#define S2_VC_CPT 4
+#define S2_VC_TILE (S2_VC_BLOCK * S2_VC_CPT)
+#define S2_SCAN_BLOCK 256
+#define S2_SCAN_CPT 8
+#define S2_SCAN_TILE (S2_SCAN_BLOCK * S2_SCAN_CPT)
+#define S2_Q_BLOCK 256
+#define S2_Q_VPT 2
+#define S2_Q_TILE (S2_Q_BLOCK * S2_Q_VPT)
+#define S2_NO_VERTEX 0xFFFFFFFFu

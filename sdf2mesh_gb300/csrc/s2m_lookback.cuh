@@ -1,0 +1,84 @@
+// s2m_lookback.cuh -- single-pass, order-preserving tile prefix sums
+// (decoupled look-back) used by every compaction of the pipeline.
+//
+// Each tile publishes its aggregate, then walks back over its predecessors'
+// status words (32 at a time, one per lane) until it meets an inclusive
+// prefix.  Tiles take their ids from an atomic counter when they start, so a
+// tile only ever waits for tiles that are already running; every wait is
+// still bounded: after S2_SPIN_LIMIT polls the tile raises S2_ERR_LOOKBACK in
+// the job's error word and continues, and every write that uses the offset is
+// bounds-checked against its buffer's capacity.
+#pragma once
+
+#define S2_LB_AGG 1ull
+#define S2_LB_PRE 2ull
+#define S2_LB_MASK ((1ull << 62) - 1ull)
+#define S2_SPIN_LIMIT (1u << 22)
+#define S2_FULL 0xffffffffu
+
+__device__ __forceinline__ void s2_st_release(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long s2_ld_acquire(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned s2_lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Called by all 32 lanes of one warp; returns the exclusive prefix of
+// `aggregate` over tiles 0 .. tile-1 (the same value in every lane).
+__device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *status, unsigned tile,
+                                                          unsigned long long aggregate, unsigned *err) {
+  const unsigned lane = threadIdx.x & 31u;
+  if (tile == 0) {
+    if (lane == 0) s2_st_release(status, (S2_LB_PRE << 62) | aggregate);
+    return 0ull;
+  }
+  if (lane == 0) s2_st_release(status + tile, (S2_LB_AGG << 62) | aggregate);
+  unsigned long long excl = 0;
+  long long base = (long long)tile - 1;
+  unsigned spins = 0;
+  for (;;) {
+    long long idx = base - (long long)lane;
+    unsigned long long w = idx >= 0 ? s2_ld_acquire(status + idx) : (S2_LB_PRE << 62);
+    unsigned flag = (unsigned)(w >> 62);
+    unsigned pmask = __ballot_sync(S2_FULL, flag == 2u);
+    unsigned zmask = __ballot_sync(S2_FULL, flag == 0u);
+    unsigned first = pmask ? (unsigned)(__ffs(pmask) - 1) : 32u;
+    unsigned need = first >= 31u ? S2_FULL : ((2u << first) - 1u);
+    if (zmask & need) {
+      if (++spins > S2_SPIN_LIMIT) {
+        if (lane == 0) atomicOr(err, S2_ERR_LOOKBACK);
+        break;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    unsigned long long v = (lane <= first) ? (w & S2_LB_MASK) : 0ull;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(S2_FULL, v, o);
+    excl += v;
+    if (first < 32u) break;
+    base -= 32;
+  }
+  if (lane == 0) s2_st_release(status + tile, (S2_LB_PRE << 62) | (excl + aggregate));
+  return excl;
+}
+
+// Exclusive scan of one value per warp-slot: `vals` holds 32 entries; warp 0
+// replaces them by their exclusive prefix and returns the total.
+__device__ __forceinline__ unsigned s2_warp_exclusive32(unsigned *vals) {
+  const unsigned lane = threadIdx.x & 31u;
+  unsigned v = vals[lane];
+  unsigned inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned t = __shfl_up_sync(S2_FULL, inc, o);
+    if ((int)lane >= o) inc += t;
+  }
+  vals[lane] = inc - v;
+  return __shfl_sync(S2_FULL, inc, 31);
+}

@@ -1,0 +1,308 @@
+// s2m_prelude.cuh -- vector types and shader builtins for SDF code lowered
+// from WGSL / GLSL by the sdf2mesh_gb300 frontend.
+//
+// The same header is compiled by NVRTC (device) and by a host C++ compiler
+// (frontend tests), so every function is __host__ __device__.  Arithmetic is
+// written out operation by operation in the order the WGSL builtin
+// definitions give (e.g. dot sums components left to right, mix is
+// e1 * (1 - t) + e2 * t, normalize divides by length), so that with FMA
+// contraction disabled the device and the host round identically.
+#pragma once
+
+#if defined(__CUDACC_RTC__) || defined(__CUDACC__)
+#define S2HD __host__ __device__ __forceinline__
+#else
+#include <cmath>
+#include <cstring>
+#define S2HD inline
+using std::sqrt;
+inline float __int_as_float(unsigned x) { float f; std::memcpy(&f, &x, 4); return f; }
+#endif
+
+template <class T, int N> struct s2vec;
+
+template <class T> struct s2vec<T, 2> {
+  T x, y;
+  S2HD T &operator[](int i) { return i == 0 ? x : y; }
+  S2HD T operator[](int i) const { return i == 0 ? x : y; }
+};
+template <class T> struct s2vec<T, 3> {
+  T x, y, z;
+  S2HD T &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  S2HD T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+template <class T> struct s2vec<T, 4> {
+  T x, y, z, w;
+  S2HD T &operator[](int i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+  S2HD T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+};
+
+typedef s2vec<float, 2> s2v2;
+typedef s2vec<float, 3> s2v3;
+typedef s2vec<float, 4> s2v4;
+
+// Constructors from a component list.
+template <class T> S2HD s2vec<T, 2> s2mk(T a, T b) { s2vec<T, 2> r; r.x = a; r.y = b; return r; }
+template <class T> S2HD s2vec<T, 3> s2mk(T a, T b, T c) { s2vec<T, 3> r; r.x = a; r.y = b; r.z = c; return r; }
+template <class T> S2HD s2vec<T, 4> s2mk(T a, T b, T c, T d) { s2vec<T, 4> r; r.x = a; r.y = b; r.z = c; r.w = d; return r; }
+template <class T, int N> S2HD s2vec<T, N> s2splat(T a) { s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = a; return r; }
+
+// Swizzle read: s2sw<0, 2, 1>(v) is v.xzy.
+template <int A, int B, class T, int N> S2HD s2vec<T, 2> s2sw(const s2vec<T, N> &v) { return s2mk(v[A], v[B]); }
+template <int A, int B, int C, class T, int N> S2HD s2vec<T, 3> s2sw(const s2vec<T, N> &v) { return s2mk(v[A], v[B], v[C]); }
+template <int A, int B, int C, int D, class T, int N> S2HD s2vec<T, 4> s2sw(const s2vec<T, N> &v) { return s2mk(v[A], v[B], v[C], v[D]); }
+
+// Component-wise operators.
+#define S2_VV_OP(op)                                                                         \
+  template <class T, int N> S2HD s2vec<T, N> operator op(const s2vec<T, N> &a, const s2vec<T, N> &b) { \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = a[i] op b[i]; return r; }              \
+  template <class T, int N> S2HD s2vec<T, N> operator op(const s2vec<T, N> &a, T b) {        \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = a[i] op b; return r; }                 \
+  template <class T, int N> S2HD s2vec<T, N> operator op(T a, const s2vec<T, N> &b) {        \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = a op b[i]; return r; }                 \
+  template <class T, int N> S2HD s2vec<T, N> &operator op##=(s2vec<T, N> &a, const s2vec<T, N> &b) { \
+    for (int i = 0; i < N; ++i) a[i] = a[i] op b[i]; return a; }                             \
+  template <class T, int N> S2HD s2vec<T, N> &operator op##=(s2vec<T, N> &a, T b) {          \
+    for (int i = 0; i < N; ++i) a[i] = a[i] op b; return a; }
+S2_VV_OP(+)
+S2_VV_OP(-)
+S2_VV_OP(*)
+S2_VV_OP(/)
+#undef S2_VV_OP
+
+template <class T, int N> S2HD s2vec<T, N> operator-(const s2vec<T, N> &a) {
+  s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = -a[i]; return r;
+}
+
+#define S2_CMP_OP(name, op)                                                                     \
+  template <class T, int N> S2HD s2vec<bool, N> name(const s2vec<T, N> &a, const s2vec<T, N> &b) { \
+    s2vec<bool, N> r; for (int i = 0; i < N; ++i) r[i] = a[i] op b[i]; return r; }
+S2_CMP_OP(s2_lt, <)
+S2_CMP_OP(s2_le, <=)
+S2_CMP_OP(s2_gt, >)
+S2_CMP_OP(s2_ge, >=)
+S2_CMP_OP(s2_eq, ==)
+S2_CMP_OP(s2_ne, !=)
+#undef S2_CMP_OP
+S2HD bool s2_lt(float a, float b) { return a < b; }
+S2HD bool s2_le(float a, float b) { return a <= b; }
+S2HD bool s2_gt(float a, float b) { return a > b; }
+S2HD bool s2_ge(float a, float b) { return a >= b; }
+S2HD bool s2_eq(float a, float b) { return a == b; }
+S2HD bool s2_ne(float a, float b) { return a != b; }
+S2HD bool s2_lt(int a, int b) { return a < b; }
+S2HD bool s2_le(int a, int b) { return a <= b; }
+S2HD bool s2_gt(int a, int b) { return a > b; }
+S2HD bool s2_ge(int a, int b) { return a >= b; }
+S2HD bool s2_eq(int a, int b) { return a == b; }
+S2HD bool s2_ne(int a, int b) { return a != b; }
+S2HD bool s2_lt(unsigned a, unsigned b) { return a < b; }
+S2HD bool s2_le(unsigned a, unsigned b) { return a <= b; }
+S2HD bool s2_gt(unsigned a, unsigned b) { return a > b; }
+S2HD bool s2_ge(unsigned a, unsigned b) { return a >= b; }
+S2HD bool s2_eq(unsigned a, unsigned b) { return a == b; }
+S2HD bool s2_ne(unsigned a, unsigned b) { return a != b; }
+S2HD bool s2_eq(bool a, bool b) { return a == b; }
+S2HD bool s2_ne(bool a, bool b) { return a != b; }
+
+template <int N> S2HD bool s2_all(const s2vec<bool, N> &v) { bool r = true; for (int i = 0; i < N; ++i) r = r && v[i]; return r; }
+template <int N> S2HD bool s2_any(const s2vec<bool, N> &v) { bool r = false; for (int i = 0; i < N; ++i) r = r || v[i]; return r; }
+S2HD bool s2_all(bool v) { return v; }
+S2HD bool s2_any(bool v) { return v; }
+
+// Conversions between element types (WGSL vec3<f32>(vec3<i32>), GLSL vec3(ivec3)).
+template <class U, class T, int N> S2HD s2vec<U, N> s2cvt(const s2vec<T, N> &v) {
+  s2vec<U, N> r; for (int i = 0; i < N; ++i) r[i] = U(v[i]); return r;
+}
+
+// Matrices: C columns of R-component float vectors (WGSL matCxR, GLSL matC / matCxR).
+template <int C, int R> struct s2mat {
+  s2vec<float, R> c[C];
+  S2HD s2vec<float, R> &operator[](int i) { return c[i]; }
+  S2HD const s2vec<float, R> &operator[](int i) const { return c[i]; }
+};
+template <int C, int R> S2HD s2vec<float, R> operator*(const s2mat<C, R> &m, const s2vec<float, C> &v) {
+  s2vec<float, R> r;
+  for (int j = 0; j < R; ++j) {
+    float s = m.c[0][j] * v[0];
+    for (int i = 1; i < C; ++i) s = s + m.c[i][j] * v[i];
+    r[j] = s;
+  }
+  return r;
+}
+template <int C, int R> S2HD s2vec<float, C> operator*(const s2vec<float, R> &v, const s2mat<C, R> &m) {
+  s2vec<float, C> r;
+  for (int i = 0; i < C; ++i) {
+    float s = v[0] * m.c[i][0];
+    for (int j = 1; j < R; ++j) s = s + v[j] * m.c[i][j];
+    r[i] = s;
+  }
+  return r;
+}
+template <int K, int C, int R> S2HD s2mat<C, R> operator*(const s2mat<K, R> &a, const s2mat<C, K> &b) {
+  s2mat<C, R> r;
+  for (int i = 0; i < C; ++i) r.c[i] = a * b.c[i];
+  return r;
+}
+template <int C, int R> S2HD s2mat<C, R> operator*(const s2mat<C, R> &a, float s) {
+  s2mat<C, R> r; for (int i = 0; i < C; ++i) r.c[i] = a.c[i] * s; return r;
+}
+template <int C, int R> S2HD s2mat<C, R> operator*(float s, const s2mat<C, R> &a) {
+  s2mat<C, R> r; for (int i = 0; i < C; ++i) r.c[i] = s * a.c[i]; return r;
+}
+template <int C, int R> S2HD s2mat<C, R> operator+(const s2mat<C, R> &a, const s2mat<C, R> &b) {
+  s2mat<C, R> r; for (int i = 0; i < C; ++i) r.c[i] = a.c[i] + b.c[i]; return r;
+}
+template <int C, int R> S2HD s2mat<C, R> operator-(const s2mat<C, R> &a, const s2mat<C, R> &b) {
+  s2mat<C, R> r; for (int i = 0; i < C; ++i) r.c[i] = a.c[i] - b.c[i]; return r;
+}
+template <int C, int R> S2HD s2mat<C, R> operator-(const s2mat<C, R> &a) {
+  s2mat<C, R> r; for (int i = 0; i < C; ++i) r.c[i] = -a.c[i]; return r;
+}
+template <int C> S2HD s2vec<float, C> &operator*=(s2vec<float, C> &v, const s2mat<C, C> &m) { v = v * m; return v; }
+template <int C> S2HD s2mat<C, C> &operator*=(s2mat<C, C> &a, const s2mat<C, C> &b) { a = a * b; return a; }
+template <int C, int R> S2HD s2mat<R, C> s2_transpose(const s2mat<C, R> &m) {
+  s2mat<R, C> r;
+  for (int i = 0; i < C; ++i) for (int j = 0; j < R; ++j) r.c[j][i] = m.c[i][j];
+  return r;
+}
+// Matrix from column-major scalars / columns; diagonal from a scalar (GLSL mat2(s)).
+template <int C, int R> S2HD s2mat<C, R> s2mat_diag(float s) {
+  s2mat<C, R> r;
+  for (int i = 0; i < C; ++i) for (int j = 0; j < R; ++j) r.c[i][j] = (i == j) ? s : 0.0f;
+  return r;
+}
+S2HD s2mat<2, 2> s2mat22(float a, float b, float c, float d) { s2mat<2, 2> m; m.c[0] = s2mk(a, b); m.c[1] = s2mk(c, d); return m; }
+S2HD s2mat<2, 2> s2mat22(s2v2 a, s2v2 b) { s2mat<2, 2> m; m.c[0] = a; m.c[1] = b; return m; }
+S2HD s2mat<3, 3> s2mat33(float a, float b, float c, float d, float e, float f, float g, float h, float i) {
+  s2mat<3, 3> m; m.c[0] = s2mk(a, b, c); m.c[1] = s2mk(d, e, f); m.c[2] = s2mk(g, h, i); return m;
+}
+S2HD s2mat<3, 3> s2mat33(s2v3 a, s2v3 b, s2v3 c) { s2mat<3, 3> m; m.c[0] = a; m.c[1] = b; m.c[2] = c; return m; }
+
+// ---------------------------------------------------------------------------
+// Scalar builtins (binary32).
+S2HD float s2_abs(float x) { return fabsf(x); }
+S2HD int s2_abs(int x) { return x < 0 ? -x : x; }
+S2HD unsigned s2_abs(unsigned x) { return x; }
+S2HD float s2_sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+S2HD int s2_sign(int x) { return x > 0 ? 1 : (x < 0 ? -1 : 0); }
+S2HD float s2_floor(float x) { return floorf(x); }
+S2HD float s2_ceil(float x) { return ceilf(x); }
+S2HD float s2_trunc(float x) { return truncf(x); }
+S2HD float s2_round(float x) { return rintf(x); }
+S2HD float s2_fract(float x) { return x - floorf(x); }
+S2HD float s2_sqrt(float x) { return sqrtf(x); }
+S2HD float s2_inversesqrt(float x) { return 1.0f / sqrtf(x); }
+S2HD float s2_exp(float x) { return expf(x); }
+S2HD float s2_exp2(float x) { return exp2f(x); }
+S2HD float s2_log(float x) { return logf(x); }
+S2HD float s2_log2(float x) { return log2f(x); }
+S2HD float s2_pow(float x, float y) { return powf(x, y); }
+S2HD float s2_sin(float x) { return sinf(x); }
+S2HD float s2_cos(float x) { return cosf(x); }
+S2HD float s2_tan(float x) { return tanf(x); }
+S2HD float s2_asin(float x) { return asinf(x); }
+S2HD float s2_acos(float x) { return acosf(x); }
+S2HD float s2_atan(float x) { return atanf(x); }
+S2HD float s2_atan2(float y, float x) { return atan2f(y, x); }
+S2HD float s2_sinh(float x) { return sinhf(x); }
+S2HD float s2_cosh(float x) { return coshf(x); }
+S2HD float s2_tanh(float x) { return tanhf(x); }
+S2HD float s2_min(float a, float b) { return fminf(a, b); }
+S2HD float s2_max(float a, float b) { return fmaxf(a, b); }
+S2HD int s2_min(int a, int b) { return a < b ? a : b; }
+S2HD int s2_max(int a, int b) { return a > b ? a : b; }
+S2HD unsigned s2_min(unsigned a, unsigned b) { return a < b ? a : b; }
+S2HD unsigned s2_max(unsigned a, unsigned b) { return a > b ? a : b; }
+S2HD float s2_clamp(float e, float lo, float hi) { return fminf(fmaxf(e, lo), hi); }
+S2HD int s2_clamp(int e, int lo, int hi) { return s2_min(s2_max(e, lo), hi); }
+S2HD unsigned s2_clamp(unsigned e, unsigned lo, unsigned hi) { return s2_min(s2_max(e, lo), hi); }
+S2HD float s2_saturate(float e) { return fminf(fmaxf(e, 0.0f), 1.0f); }
+S2HD float s2_mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+S2HD float s2_step(float edge, float x) { return edge <= x ? 1.0f : 0.0f; }
+S2HD float s2_smoothstep(float lo, float hi, float x) {
+  float t = s2_clamp((x - lo) / (hi - lo), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+S2HD float s2_fmod_glsl(float x, float y) { return x - y * floorf(x / y); }
+S2HD float s2_fmod_wgsl(float x, float y) { return x - y * truncf(x / y); }
+S2HD int s2_imod(int x, int y) { return y == 0 ? 0 : x % y; }
+S2HD unsigned s2_imod(unsigned x, unsigned y) { return y == 0 ? 0u : x % y; }
+S2HD float s2_fma(float a, float b, float c) { return fmaf(a, b, c); }
+S2HD float s2_radians(float x) { return x * 0.017453292519943295f; }
+S2HD float s2_degrees(float x) { return x * 57.29577951308232f; }
+S2HD float s2_length(float x) { return fabsf(x); }
+S2HD float s2_distance(float a, float b) { return fabsf(a - b); }
+S2HD float s2_dot(float a, float b) { return a * b; }
+
+// Component-wise vector variants of the scalar builtins.
+#define S2_VEC1(name)                                                                     \
+  template <class T, int N> S2HD s2vec<T, N> name(const s2vec<T, N> &a) {                 \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = name(a[i]); return r; }
+#define S2_VEC2(name)                                                                     \
+  template <class T, int N> S2HD s2vec<T, N> name(const s2vec<T, N> &a, const s2vec<T, N> &b) { \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = name(a[i], b[i]); return r; }      \
+  template <class T, int N> S2HD s2vec<T, N> name(const s2vec<T, N> &a, T b) {            \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = name(a[i], b); return r; }
+#define S2_VEC3(name)                                                                     \
+  template <class T, int N> S2HD s2vec<T, N> name(const s2vec<T, N> &a, const s2vec<T, N> &b, const s2vec<T, N> &c) { \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = name(a[i], b[i], c[i]); return r; } \
+  template <class T, int N> S2HD s2vec<T, N> name(const s2vec<T, N> &a, T b, T c) {       \
+    s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = name(a[i], b, c); return r; }
+S2_VEC1(s2_abs) S2_VEC1(s2_sign) S2_VEC1(s2_floor) S2_VEC1(s2_ceil) S2_VEC1(s2_trunc)
+S2_VEC1(s2_round) S2_VEC1(s2_fract) S2_VEC1(s2_sqrt) S2_VEC1(s2_inversesqrt) S2_VEC1(s2_exp)
+S2_VEC1(s2_exp2) S2_VEC1(s2_log) S2_VEC1(s2_log2) S2_VEC1(s2_sin) S2_VEC1(s2_cos) S2_VEC1(s2_tan)
+S2_VEC1(s2_asin) S2_VEC1(s2_acos) S2_VEC1(s2_atan) S2_VEC1(s2_sinh) S2_VEC1(s2_cosh)
+S2_VEC1(s2_tanh) S2_VEC1(s2_saturate) S2_VEC1(s2_radians) S2_VEC1(s2_degrees)
+S2_VEC2(s2_pow) S2_VEC2(s2_atan2) S2_VEC2(s2_min) S2_VEC2(s2_max) S2_VEC2(s2_fmod_glsl)
+S2_VEC2(s2_fmod_wgsl) S2_VEC2(s2_imod)
+S2_VEC3(s2_clamp) S2_VEC3(s2_fma) S2_VEC3(s2_mix)
+#undef S2_VEC1
+#undef S2_VEC2
+#undef S2_VEC3
+// mix(vec, vec, scalar), step(scalar, vec), step(vec, vec), smoothstep variants.
+template <int N> S2HD s2vec<float, N> s2_mix(const s2vec<float, N> &a, const s2vec<float, N> &b, float t) {
+  s2vec<float, N> r; for (int i = 0; i < N; ++i) r[i] = s2_mix(a[i], b[i], t); return r;
+}
+template <int N> S2HD s2vec<float, N> s2_step(const s2vec<float, N> &e, const s2vec<float, N> &x) {
+  s2vec<float, N> r; for (int i = 0; i < N; ++i) r[i] = s2_step(e[i], x[i]); return r;
+}
+template <int N> S2HD s2vec<float, N> s2_step(float e, const s2vec<float, N> &x) {
+  s2vec<float, N> r; for (int i = 0; i < N; ++i) r[i] = s2_step(e, x[i]); return r;
+}
+template <int N> S2HD s2vec<float, N> s2_smoothstep(const s2vec<float, N> &lo, const s2vec<float, N> &hi, const s2vec<float, N> &x) {
+  s2vec<float, N> r; for (int i = 0; i < N; ++i) r[i] = s2_smoothstep(lo[i], hi[i], x[i]); return r;
+}
+template <int N> S2HD s2vec<float, N> s2_smoothstep(float lo, float hi, const s2vec<float, N> &x) {
+  s2vec<float, N> r; for (int i = 0; i < N; ++i) r[i] = s2_smoothstep(lo, hi, x[i]); return r;
+}
+template <class T, int N> S2HD s2vec<T, N> s2_select(const s2vec<T, N> &f, const s2vec<T, N> &t, const s2vec<bool, N> &c) {
+  s2vec<T, N> r; for (int i = 0; i < N; ++i) r[i] = c[i] ? t[i] : f[i]; return r;
+}
+template <class T, int N> S2HD s2vec<T, N> s2_select(const s2vec<T, N> &f, const s2vec<T, N> &t, bool c) { return c ? t : f; }
+template <class T> S2HD T s2_select(T f, T t, bool c) { return c ? t : f; }
+
+// Geometric builtins.
+template <int N> S2HD float s2_dot(const s2vec<float, N> &a, const s2vec<float, N> &b) {
+  float s = a[0] * b[0];
+  for (int i = 1; i < N; ++i) s = s + a[i] * b[i];
+  return s;
+}
+template <int N> S2HD int s2_dot(const s2vec<int, N> &a, const s2vec<int, N> &b) {
+  int s = a[0] * b[0];
+  for (int i = 1; i < N; ++i) s = s + a[i] * b[i];
+  return s;
+}
+template <int N> S2HD float s2_length(const s2vec<float, N> &a) { return sqrtf(s2_dot(a, a)); }
+template <int N> S2HD float s2_distance(const s2vec<float, N> &a, const s2vec<float, N> &b) { return s2_length(a - b); }
+template <int N> S2HD s2vec<float, N> s2_normalize(const s2vec<float, N> &a) {
+  float l = s2_length(a);
+  s2vec<float, N> r; for (int i = 0; i < N; ++i) r[i] = a[i] / l; return r;
+}
+S2HD float s2_normalize(float a) { return a / fabsf(a); }
+S2HD s2v3 s2_cross(const s2v3 &a, const s2v3 &b) {
+  return s2mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <int N> S2HD s2vec<float, N> s2_reflect(const s2vec<float, N> &e1, const s2vec<float, N> &e2) {
+  return e1 - 2.0f * s2_dot(e2, e1) * e2;
+}

@@ -1,0 +1,84 @@
+"""Comparison of a GPU mesh with the CPU oracle's.
+
+Bit-exact SDFs (only +, -, *, /, sqrt, min, max, abs, clamp: every operation
+correctly rounded on both sides) must match exactly: the same vertices in
+the same order with the same bits, the same triangles, the same invalid-quad
+count.  SDFs with transcendental functions (Mandelbulb) may differ in the
+last bits of an evaluation, so a cell whose corner values straddle zero by
+less than a stated epsilon ("tie cell") may flip; everything else must match.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+import oracle
+
+
+def assert_bit_exact(gpu, ref, what=""):
+    assert gpu.positions.shape[0] == ref.nverts, f"{what}: vertices {gpu.positions.shape[0]} != {ref.nverts}"
+    assert np.array_equal(gpu.cell_xyz, ref.cell), f"{what}: vertex cells differ"
+    assert np.array_equal(gpu.signs, ref.signs), f"{what}: sign bits differ"
+    gp = np.ascontiguousarray(gpu.positions, np.float32).view(np.uint32)
+    rp = np.ascontiguousarray(ref.pos, np.float32).view(np.uint32)
+    bad = np.nonzero((gp != rp).any(axis=1))[0]
+    assert bad.size == 0, f"{what}: {bad.size} positions differ, first {bad[:5]}"
+    gn = np.ascontiguousarray(gpu.normals, np.float32).view(np.uint32)
+    rn = np.ascontiguousarray(ref.nrm, np.float32).view(np.uint32)
+    assert np.array_equal(gn, rn), f"{what}: normals differ"
+    assert gpu.triangle_indices.shape == ref.tris.shape, f"{what}: triangles {gpu.triangle_indices.shape} != {ref.tris.shape}"
+    assert np.array_equal(gpu.triangle_indices, ref.tris), f"{what}: triangle indices differ"
+    assert gpu.invalid_quads == ref.invalid_quads, f"{what}: invalid quads {gpu.invalid_quads} != {ref.invalid_quads}"
+
+
+def keys_of(cell_xyz):
+    c = np.asarray(cell_xyz, np.uint64)
+    return c[:, 0] | (c[:, 1] << np.uint64(16)) | (c[:, 2] << np.uint64(32))
+
+
+def tie_cells(kind, params, resolution, bounds, keys, eps, slice_lag=False):
+    """The subset of cell keys whose reference corner values include one with |f| <= eps."""
+    out = []
+    for k in np.asarray(keys, np.uint64):
+        x, y, z = int(k & 0xFFFF), int((k >> 16) & 0xFFFF), int((k >> 32) & 0xFFFF)
+        if slice_lag:
+            z -= 1
+        c = oracle.cell_corners(kind, params, resolution, bounds, x, y, z)
+        if np.min(np.abs(c)) <= eps:
+            out.append(int(k))
+    return set(out)
+
+
+def compare_with_ties(gpu, ref, kind, params, resolution, bounds, eps, h, pos_tol_cells=1e-5, slice_lag=False):
+    """Topology equal outside tie cells; positions within pos_tol_cells * h.
+
+    Returns a dict with the counts of tie cells and the max position error
+    (in cells) over the common vertices."""
+    gk = keys_of(gpu.cell_xyz)
+    rk = keys_of(ref.cell)
+    gset, rset = set(gk.tolist()), set(rk.tolist())
+    only = (gset ^ rset)
+    ties = tie_cells(kind, params, resolution, bounds, list(only), eps, slice_lag)
+    assert only <= ties, f"{len(only - ties)} vertex cells differ outside tie cells, e.g. {sorted(only - ties)[:5]}"
+    common = np.array(sorted(gset & rset), np.uint64)
+    gi = np.searchsorted(gk, common)
+    ri = np.searchsorted(rk, common)
+    gs, rs = gpu.signs[gi], ref.signs[ri]
+    sign_diff = set(common[gs != rs].tolist())
+    sd_ties = tie_cells(kind, params, resolution, bounds, list(sign_diff), eps, slice_lag)
+    assert sign_diff <= sd_ties, f"{len(sign_diff - sd_ties)} sign words differ outside tie cells"
+    # positions of common vertices whose cell is not a tie
+    err = np.abs(gpu.positions[gi].astype(np.float64) - ref.pos[ri].astype(np.float64)).max(axis=1) / h
+    flips = ties | sd_ties
+    near = np.array([int(k) not in flips for k in common.tolist()], bool)
+    max_err = float(err[near].max()) if near.any() else 0.0
+    # a vertex may move when a neighbouring corner flips within eps; count those
+    moved = int((err[near] > pos_tol_cells).sum())
+    # triangles as sets of key triples
+    def tri_keys(keys, tris):
+        t = keys[np.asarray(tris, np.int64)]
+        return set(map(tuple, t.tolist()))
+    gt, rt = tri_keys(gk, gpu.triangle_indices), tri_keys(rk, ref.tris)
+    tdiff = gt ^ rt
+    touching = {t for t in tdiff if any(v in flips or v in only for v in t)}
+    return {"tie_cells": len(flips | only), "vertex_only_one_side": len(only), "max_pos_err_cells": max_err,
+            "moved": moved, "tri_diff": len(tdiff), "tri_diff_unexplained": len(tdiff - touching)}

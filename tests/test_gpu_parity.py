@@ -1,0 +1,189 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Every case below runs libsdf2mesh_gb300.so on the GPU (NVRTC-compiled
+evaluation + cell kernels, nvcc-compiled compaction and quad kernels) and the
+oracle's restatement of the reference rule (dualcontour.wgsl:22-180,
+main.rs:298-356, mesh.rs:213-331) on the same SDF, bounds and resolution.
+SDFs built from correctly rounded operations must match bit for bit:
+vertex cells, sign bits, positions, normals, triangle indices and the
+invalid-quad count.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+import sdf2mesh_gb300 as s2m
+from sdf2mesh_gb300 import workloads
+from tests.parity import assert_bit_exact, compare_with_ties, keys_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torus_sdf(lib):
+    src, prm = workloads.torus(0.5, 0.2)
+    return s2m.Sdf3DShader.from_source(src).compile(), prm
+
+
+def run(sdf, N, B=2.0, **kw):
+    return s2m.generate(sdf, s2m.AppState(resolution=N, bounds=B, **kw))
+
+
+def test_torus_128_plain(torus_sdf):
+    sdf, prm = torus_sdf
+    gpu = run(sdf, 128)
+    ref = oracle.mesh(oracle.TORUS, prm, 128, 2.0)
+    assert ref.nverts > 10000
+    assert_bit_exact(gpu, ref, "torus 128")
+
+
+def test_torus_reference_file(lib):
+    """examples/torus.sdf3d text as the reference ships it, through the file path."""
+    import os
+    import tempfile
+    d = tempfile.mkdtemp()
+    p = os.path.join(d, "torus.sdf3d")
+    with open(p, "w") as f:
+        f.write("use sdf3d::*;\n\nfn sdf3d(p: vec3f) -> f32 {\n    return sdf3d_torus(p, vec2(0.5, 0.2));\n}\n")
+    sdf = s2m.Sdf3DShader.from_path(p).compile()
+    gpu = run(sdf, 64)
+    ref = oracle.mesh(oracle.TORUS, [0.5, 0.2], 64, 2.0)
+    assert_bit_exact(gpu, ref, "torus file 64")
+
+
+@pytest.mark.parametrize("N", [2, 3, 5, 17, 33, 100])
+def test_torus_odd_sizes(torus_sdf, N):
+    sdf, prm = torus_sdf
+    assert_bit_exact(run(sdf, N), oracle.mesh(oracle.TORUS, prm, N, 2.0), f"torus {N}")
+
+
+def test_slice_lag_and_rounding(torus_sdf):
+    """The reference CLI: pow2 rounding (96 -> 128) and the read-before-submit slice lag."""
+    sdf, prm = torus_sdf
+    gpu = s2m.generate(sdf, s2m.AppState.from_args(resolution=96, bounds=2.0))
+    assert gpu.info.resolution == 128
+    ref = oracle.mesh(oracle.TORUS, prm, 128, 2.0, slice_lag=True)
+    assert_bit_exact(gpu, ref, "torus 96->128 lag")
+    assert int(gpu.cell_xyz[:, 2].min()) >= 1
+
+
+def test_slice_lag_surface_at_bounds(lib):
+    """A box larger than the domain: the surface crosses the bounds, the lag
+    drops slice 0's neighbours and the invalid-quad count must match."""
+    src = "use sdf3d::*;\nfn sdf3d(p: vec3f) -> f32 {\n  return sdf3d_sphere(p - vec3f(0.0, 0.0, -0.9), 0.6);\n}\n"
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    gpu = s2m.generate(sdf, s2m.AppState(resolution=64, bounds=2.0, slice_lag=True))
+    # same SDF as a tree program: sphere at (0, 0, -0.9), r = 0.6
+    ref = oracle.mesh(oracle.TREE, [0, 0.0, 0.0, -0.9, 0.6], 64, 2.0, slice_lag=True)
+    assert ref.invalid_quads > 0
+    assert_bit_exact(gpu, ref, "sphere at bounds, lag")
+
+
+@pytest.mark.parametrize("depth", [1, 2, 5, 13, 64])
+def test_slab_depth_invariance(torus_sdf, depth):
+    sdf, prm = torus_sdf
+    gpu = run(sdf, 72, slab_depth=depth)
+    assert_bit_exact(gpu, oracle.mesh(oracle.TORUS, prm, 72, 2.0), f"slab depth {depth}")
+
+
+def test_exact_corner_mode_matches(torus_sdf):
+    sdf, prm = torus_sdf
+    a = run(sdf, 80)
+    b = run(sdf, 80, exact_corners=True)
+    assert b.info.candidate_cells >= a.info.candidate_cells
+    assert_bit_exact(b, oracle.mesh(oracle.TORUS, prm, 80, 2.0), "exact corners")
+
+
+def test_overflow_regrow(torus_sdf):
+    """Tiny initial capacities: the library regrows to the exact totals and re-runs."""
+    sdf, prm = torus_sdf
+    gpu = run(sdf, 96, max_vertices=100, max_triangles=100)
+    assert_bit_exact(gpu, oracle.mesh(oracle.TORUS, prm, 96, 2.0), "regrow")
+
+
+def test_empty_and_full(lib):
+    for body, what in (("return -1.0;", "all inside"), ("return 1.0;", "all outside"),
+                       ("return sdf3d_sphere(p, 0.001);", "sphere below one cell")):
+        src = "use sdf3d::*;\nfn sdf3d(p: vec3f) -> f32 {\n  " + body + "\n}\n"
+        gpu = run(s2m.Sdf3DShader.from_source(src).compile(), 32)
+        assert gpu.positions.shape[0] == 0, what
+        assert gpu.triangle_indices.shape[0] == 0, what
+
+
+def test_zero_level_grid(lib):
+    """f == 0 on lattice planes: `> 0` sign tests and the t == 0 crossing rule (dualcontour.wgsl:120)."""
+    for n, d in (((1.0, 0.0, 0.0), 0.0), ((0.0, 1.0, 0.0), 0.25), ((0.0, 0.0, -1.0), 0.0),
+                 ((0.6, 0.0, 0.8), 0.1)):
+        src = ("fn sdf3d(p: vec3f) -> f32 {\n  return dot(p, vec3f(%r, %r, %r)) - %r;\n}\n" % (*n, d))
+        gpu = run(s2m.Sdf3DShader.from_source(src).compile(), 17)
+        ref = oracle.mesh(oracle.TREE, [4, *n, d], 17, 2.0)
+        assert ref.nverts > 0
+        assert_bit_exact(gpu, ref, f"plane {n} {d}")
+
+
+def test_csg64_128(lib):
+    src, prm = workloads.csg64(seed=0)
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    gpu = run(sdf, 128)
+    ref = oracle.mesh(oracle.CSG, prm, 128, 2.0)
+    assert ref.nverts > 1000
+    assert_bit_exact(gpu, ref, "csg64 128")
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_trees(lib, seed):
+    src, prog = workloads.random_tree(seed)
+    N = [48, 64, 96, 40][seed % 4]
+    gpu = run(s2m.Sdf3DShader.from_source(src).compile(), N)
+    ref = oracle.mesh(oracle.TREE, prog, N, 2.0)
+    assert_bit_exact(gpu, ref, f"tree {seed}")
+
+
+def test_mandelbulb_ties(lib):
+    """Transcendentals differ in the last bits between CUDA and the host libm:
+    topology must agree outside tie cells (some corner |f| <= 1e-5)."""
+    src, prm = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
+    sdf = s2m.Sdf3DShader.from_source(src, s2m.LANG_GLSL, "sdf").compile()
+    N, B = 96, 2.5
+    gpu = run(sdf, N, B)
+    ref = oracle.mesh(oracle.MANDELBULB, prm, N, B)
+    assert ref.nverts > 1000
+    h = B / (N - 1)
+    r = compare_with_ties(gpu, ref, oracle.MANDELBULB, prm, N, B, eps=1e-5, h=h)
+    assert r["tri_diff_unexplained"] == 0, r
+    assert r["vertex_only_one_side"] <= max(5, ref.nverts // 1000), r
+
+
+def test_csg64_1024_slice_window(lib):
+    """Full-size CSG (1024^3): the GPU's vertices of a window of slices equal
+    the oracle's for the same window, bit for bit; the whole mesh is a closed
+    2-manifold where it does not touch the bounds."""
+    src, prm = workloads.csg64(seed=0)
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    N = 1024
+    gpu = run(sdf, N)
+    z0, z1 = 500, 503
+    ref = oracle.mesh(oracle.CSG, prm, N, 2.0, z_begin=z0, z_end=z1, skip_quads=True)
+    z = gpu.cell_xyz[:, 2]
+    sel = (z >= z0) & (z < z1)
+    assert int(sel.sum()) == ref.nverts > 0
+    assert np.array_equal(gpu.cell_xyz[sel], ref.cell)
+    assert np.array_equal(gpu.signs[sel], ref.signs)
+    assert np.array_equal(gpu.positions[sel].view(np.uint32), ref.pos.astype(np.float32).view(np.uint32))
+    assert np.array_equal(gpu.normals[sel].view(np.uint32), ref.nrm.astype(np.float32).view(np.uint32))
+    # closed 2-manifold: every undirected edge shared by exactly two triangles
+    t = gpu.triangle_indices.astype(np.int64)
+    assert t.max() < gpu.positions.shape[0]
+    e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
+    e.sort(axis=1)
+    code = e[:, 0] * np.int64(1 << 32) + e[:, 1]
+    _, counts = np.unique(code, return_counts=True)
+    assert gpu.invalid_quads == 0
+    assert (counts == 2).all(), np.bincount(counts)
+    # keys sorted (z, y, x) like the reference's VertexList
+    k = keys_of(gpu.cell_xyz)
+    kz = (k >> np.uint64(32)) * np.uint64(1 << 32) + ((k >> np.uint64(16)) & np.uint64(0xFFFF)) * np.uint64(1 << 16) \
+        + (k & np.uint64(0xFFFF))
+    assert (np.diff(kz.astype(np.int64)) > 0).all()
