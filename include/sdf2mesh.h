@@ -163,9 +163,10 @@ void s2m_mesh_free(s2m_mesh *mesh);
 
 /* Per-kernel device time of a mesh's runs, from CUDA events recorded on the
    launching stream around every kernel while profiling is enabled.  Kinds:
-   0 grid evaluation, 1 cell pass, 2 vertex compaction, 3 row scan, 4 quads.
+   0 grid evaluation, 1 cell classification, 2 vertex placement, 3 vertex
+   compaction, 4 row scan, 5 quads.
    Accumulates over runs until reset; read after s2m_mesh_sync. */
-#define S2M_KERNEL_KINDS 5
+#define S2M_KERNEL_KINDS 6
 typedef struct {
   double ms[S2M_KERNEL_KINDS];
   uint64_t launches[S2M_KERNEL_KINDS];

@@ -66,11 +66,11 @@ class MeshInfo(ctypes.Structure):
     ]
 
 
-KERNEL_KINDS = ("eval_planes", "cells", "vcompact", "rowscan", "quads")
+KERNEL_KINDS = ("eval_planes", "cells", "vertices", "vcompact", "rowscan", "quads")
 
 
 class Profile(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_double * 5), ("launches", ctypes.c_uint64 * 5), ("eval_points", ctypes.c_double),
+    _fields_ = [("ms", ctypes.c_double * 6), ("launches", ctypes.c_uint64 * 6), ("eval_points", ctypes.c_double),
                 ("cells", ctypes.c_double)]
 
 

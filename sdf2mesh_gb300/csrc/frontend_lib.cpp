@@ -7,7 +7,9 @@
 // function follows the published distance formulas the reference also uses
 // (I. Quilez, "distance functions"), operation for operation, because
 // `.sdf3d` files call them by these names and expect the same values.
+#include <climits>
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <sstream>
 
@@ -133,6 +135,13 @@ static bool read_file(const std::string &path, std::string &out) {
   return true;
 }
 
+// Canonical path of an existing file, or the text itself.
+static std::string canonical(const std::string &path) {
+  char buf[PATH_MAX];
+  if (!path.empty() && realpath(path.c_str(), buf)) return std::string(buf);
+  return path;
+}
+
 static void expand(const std::string &text, const std::string &self_path, const std::string &base_dir,
                    std::string &out, std::vector<std::string> *log, int depth) {
   for (const std::string &line : split_lines(text)) {
@@ -146,6 +155,9 @@ static void expand(const std::string &text, const std::string &self_path, const 
       }
       if (t.rfind("include", 0) == 0) {
         std::string file = directive_arg(t, "include");
+        // shader.rs:186-188 skips an include of the file itself; here the
+        // comparison is on canonical paths, since includes also resolve
+        // relative to the including file.
         if (file != self_path && depth < 64) {
           std::string body;
           std::string resolved = file;
@@ -154,11 +166,13 @@ static void expand(const std::string &text, const std::string &self_path, const 
             resolved = base_dir + "/" + file;
             ok = read_file(resolved, body);
           }
+          if (ok && !self_path.empty() && canonical(resolved) == canonical(self_path)) ok = false, body.clear(),
+              resolved.clear();
           if (ok) {
             size_t slash = resolved.find_last_of('/');
             std::string dir = slash == std::string::npos ? base_dir : resolved.substr(0, slash);
-            expand(body, file, dir, out, log, depth + 1);
-          } else if (log) {
+            expand(body, resolved, dir, out, log, depth + 1);
+          } else if (log && !resolved.empty()) {
             log->push_back("Could not include \"" + file + "\"");
           }
         }

@@ -79,7 +79,7 @@ struct s2m_sdf {
   double fp32_ops = 0, sfu_ops = 0;
   uint32_t flags = 0;
   cudaLibrary_t lib = nullptr;
-  cudaKernel_t k_eval = nullptr, k_cells = nullptr;
+  cudaKernel_t k_eval = nullptr, k_cells = nullptr, k_vertices = nullptr;
 };
 
 struct s2m_mesh {
@@ -89,22 +89,23 @@ struct s2m_mesh {
   int N = 0, D = 0, nzc = 0, nslabs = 0;
   // workspace
   float *ring = nullptr;
-  unsigned long long *slab_ctrl = nullptr;  // [cell status | vc status | counters]
+  unsigned long long *slab_ctrl = nullptr;  // [cell-tile status | tile counter]
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
+  // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
-  float *cand_pos = nullptr, *cand_nrm = nullptr;
+  float *cand_val = nullptr, *cand_pos = nullptr, *cand_nrm = nullptr;
   unsigned long long cand_cap = 0;
-  unsigned long long *cand_totals = nullptr;  // nslabs
+  unsigned long long *cand_base = nullptr;    // nslabs + 1
+  unsigned long long *cand_status = nullptr;  // vc_tiles
   // outputs and job counters
   float *pos = nullptr, *nrm = nullptr;
   unsigned long long *key = nullptr;
   unsigned *tris = nullptr;
   unsigned long long vcap = 0, tcap = 0;
-  unsigned long long *vbase = nullptr;  // nslabs + 1
   unsigned *rowcnt = nullptr, *rowstart = nullptr;
   unsigned long long *scan_status = nullptr;
   size_t scan_tiles = 0, quad_tiles = 0;
-  unsigned long long *jobctl = nullptr;  // [ntris, invalid, ncand, err | counters[8]]
+  unsigned long long *jobctl = nullptr;  // [ntris, invalid, vtotal, err | counters[8]]
   // host results
   unsigned long long *h_read = nullptr;  // pinned readback
   uint64_t nverts = 0, ntris = 0, invalid = 0, ncand = 0;
@@ -161,7 +162,8 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
     return ce == cudaErrorNoDevice || ce == cudaErrorInsufficientDriver ? S2M_E_NO_DEVICE : S2M_E_CUDA;
   }
   if (cudaLibraryGetKernel(&s->k_eval, s->lib, "s2m_eval_planes") != cudaSuccess ||
-      cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess) {
+      cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess ||
+      cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
   }
@@ -181,15 +183,16 @@ uint32_t reference_resolution(uint32_t r) {
 }
 
 void free_buffers(s2m_mesh *m) {
-  void *ptrs[] = {m->ring, m->slab_ctrl, m->cand_key, m->cand_pos, m->cand_nrm, m->cand_totals, m->pos, m->nrm,
-                  m->key, m->tris, m->vbase, m->rowcnt, m->rowstart, m->scan_status, m->jobctl};
+  void *ptrs[] = {m->ring, m->slab_ctrl, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
+                  m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
+                  m->jobctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (m->h_read) cudaFreeHost(m->h_read);
-  m->ring = nullptr; m->slab_ctrl = nullptr; m->cand_key = nullptr; m->cand_pos = nullptr; m->cand_nrm = nullptr;
-  m->cand_totals = nullptr; m->pos = nullptr; m->nrm = nullptr; m->key = nullptr; m->tris = nullptr;
-  m->vbase = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr; m->jobctl = nullptr;
-  m->h_read = nullptr;
+  m->ring = nullptr; m->slab_ctrl = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
+  m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
+  m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
+  m->jobctl = nullptr; m->h_read = nullptr;
 }
 
 int setup_job(s2m_mesh *m, char *err, size_t errlen) {
@@ -244,37 +247,38 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   const S2Job &j = m->job;
   const unsigned long long N = (unsigned long long)m->N;
   const unsigned long long cells_per_slab = (unsigned long long)m->D * N * N;
-  m->cand_cap = std::max<unsigned long long>(1024, std::min(cand_cap, cells_per_slab));
-  m->vcap = std::max<unsigned long long>(1024, vcap);
+  m->cand_cap = std::max<unsigned long long>(1024, std::min(cand_cap, N * N * N));
+  m->vcap = std::max<unsigned long long>(1024, std::min(vcap, N * N * N));
   m->tcap = std::max<unsigned long long>(2048, tcap);
   m->cell_tiles = (cells_per_slab + S2_CELL_TILE - 1) / S2_CELL_TILE;
   m->vc_tiles = (m->cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
-  m->slab_ctrl_words = m->cell_tiles + m->vc_tiles + 1;
+  m->slab_ctrl_words = m->cell_tiles + 1;
   m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   m->quad_tiles = (m->vcap + S2_Q_TILE - 1) / S2_Q_TILE;
   size_t ring_floats = size_t(j.ring) * size_t(j.plane);
   S2_CUDA(cudaMalloc(&m->ring, ring_floats * sizeof(float)));
   S2_CUDA(cudaMalloc(&m->slab_ctrl, m->slab_ctrl_words * 8));
   S2_CUDA(cudaMalloc(&m->cand_key, m->cand_cap * 8));
+  S2_CUDA(cudaMalloc(&m->cand_val, m->cand_cap * 32));
   S2_CUDA(cudaMalloc(&m->cand_pos, m->cand_cap * 12));
   S2_CUDA(cudaMalloc(&m->cand_nrm, m->cand_cap * 12));
-  S2_CUDA(cudaMalloc(&m->cand_totals, size_t(std::max(1, m->nslabs)) * 8));
+  S2_CUDA(cudaMalloc(&m->cand_base, size_t(m->nslabs + 1) * 8));
+  S2_CUDA(cudaMalloc(&m->cand_status, m->vc_tiles * 8));
   S2_CUDA(cudaMalloc(&m->pos, m->vcap * 12));
   S2_CUDA(cudaMalloc(&m->nrm, m->vcap * 12));
   S2_CUDA(cudaMalloc(&m->key, m->vcap * 8));
   S2_CUDA(cudaMalloc(&m->tris, m->tcap * 12));
-  S2_CUDA(cudaMalloc(&m->vbase, size_t(m->nslabs + 1) * 8));
   S2_CUDA(cudaMalloc(&m->rowcnt, N * N * 4));
   S2_CUDA(cudaMalloc(&m->rowstart, (N * N + 1) * 4));
   S2_CUDA(cudaMalloc(&m->scan_status, (m->scan_tiles + m->quad_tiles) * 8));
   S2_CUDA(cudaMalloc(&m->jobctl, 8 * 8));
-  S2_CUDA(cudaMallocHost(&m->h_read, size_t(8 + m->nslabs + 1) * 8));
+  S2_CUDA(cudaMallocHost(&m->h_read, 8 * 8));
   return S2M_OK;
 }
 
 // Device pointers of the counters inside jobctl.
 struct JobCtl {
-  unsigned long long *ntris, *invalid, *ncand;
+  unsigned long long *ntris, *invalid, *vtotal;
   unsigned *err;
   unsigned *counters;
 };
@@ -282,7 +286,7 @@ JobCtl jobctl(const s2m_mesh *m) {
   JobCtl c;
   c.ntris = m->jobctl + 0;
   c.invalid = m->jobctl + 1;
-  c.ncand = m->jobctl + 2;
+  c.vtotal = m->jobctl + 2;
   c.err = reinterpret_cast<unsigned *>(m->jobctl + 3);
   c.counters = reinterpret_cast<unsigned *>(m->jobctl + 4);  // 8 x u32
   return c;
@@ -337,21 +341,26 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->ev_used = 0;
   cudaError_t e;
   if ((e = cudaMemsetAsync(m->jobctl, 0, 8 * 8, st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(m->vbase, 0, size_t(m->nslabs + 1) * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->cand_base, 0, size_t(m->nslabs + 1) * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->cand_status, 0, m->vc_tiles * 8, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->rowcnt, 0, N * N * 4, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->scan_status, 0, (m->scan_tiles + m->quad_tiles) * 8, st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(m->cand_totals, 0, size_t(std::max(1, m->nslabs)) * 8, st)) != cudaSuccess) return e;
 
   S2Slab slab;
   slab.ring = m->ring;
   slab.status = m->slab_ctrl;
-  slab.status2 = m->slab_ctrl + m->cell_tiles;
-  slab.tile_counter = reinterpret_cast<unsigned *>(m->slab_ctrl + m->cell_tiles + m->vc_tiles);
-  slab.cand_key = m->cand_key;
-  slab.cand_pos = m->cand_pos;
-  slab.cand_nrm = m->cand_nrm;
-  slab.cand_cap = m->cand_cap;
+  slab.tile_counter = reinterpret_cast<unsigned *>(m->slab_ctrl + m->cell_tiles);
   slab.err = c.err;
+
+  S2Cand cand;
+  cand.key = m->cand_key;
+  cand.val = m->cand_val;
+  cand.pos = m->cand_pos;
+  cand.nrm = m->cand_nrm;
+  cand.cap = m->cand_cap;
+  cand.base = m->cand_base;
+  cand.status = m->cand_status;
+  cand.tile_counter = c.counters + 0;
 
   S2MeshDev md;
   md.pos = m->pos;
@@ -360,19 +369,17 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   md.tris = m->tris;
   md.vcap = m->vcap;
   md.tcap = m->tcap;
-  md.vbase = m->vbase;
+  md.vtotal = c.vtotal;
   md.rowcnt = m->rowcnt;
   md.rowstart = m->rowstart;
   md.scan_status = m->scan_status;
   md.counters = c.counters;
   md.ntris = c.ntris;
   md.invalid = c.invalid;
-  md.ncand = c.ncand;
   md.err = c.err;
 
   const long long pts = (long long)j.P * j.P;
   const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
-  const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
   for (int s = 0; s < m->nslabs; ++s) {
     int zc0 = s * m->D;
     int zc1 = std::min(m->nzc, zc0 + m->D);
@@ -385,41 +392,37 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     S2_LAUNCH(0, double(pts) * nk,
               cudaLaunchKernel((const void *)m->sdf->k_eval, eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
     if ((e = cudaMemsetAsync(m->slab_ctrl, 0, m->slab_ctrl_words * 8, st)) != cudaSuccess) return e;
-    slab.cand_total = m->cand_totals + s;
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
     unsigned cg = unsigned((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-    void *cargs[] = {&jj, &slab, &zc0, &zc1};
+    int si = s;
+    void *cargs[] = {&jj, &slab, &cand, &zc0, &zc1, &si};
     S2_LAUNCH(1, ncells, cudaLaunchKernel((const void *)m->sdf->k_cells, dim3(cg), dim3(S2_CELL_BLOCK), cargs, 0, st));
-    S2_LAUNCH(2, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, slab, md, s), cudaGetLastError()));
   }
+  S2Job jj = j;
+  int nslabs = m->nslabs;
+  void *vargs[] = {&jj, &cand, &nslabs};
+  const unsigned vx_grid = unsigned(sms) * 16;
+  S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)m->sdf->k_vertices, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));
+  const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
+  S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs), cudaGetLastError()));
   const unsigned scan_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->scan_tiles, size_t(sms) * 8)));
-  S2_LAUNCH(3, 0, (s2m_rowscan<<<scan_grid, S2_SCAN_BLOCK, 0, st>>>(md, N * N), cudaGetLastError()));
+  S2_LAUNCH(4, 0, (s2m_rowscan<<<scan_grid, S2_SCAN_BLOCK, 0, st>>>(md, N * N), cudaGetLastError()));
   const unsigned q_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->quad_tiles, size_t(sms) * 8)));
-  S2_LAUNCH(4, 0, (s2m_quads<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, m->nslabs, unsigned(m->scan_tiles)),
-                   cudaGetLastError()));
+  S2_LAUNCH(5, 0, (s2m_quads<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, unsigned(m->scan_tiles)), cudaGetLastError()));
   return cudaSuccess;
 }
 
 int readback(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   S2_CUDA(cudaMemcpyAsync(m->h_read, m->jobctl, 4 * 8, cudaMemcpyDeviceToHost, st));
-  S2_CUDA(cudaMemcpyAsync(m->h_read + 4, m->vbase + m->nslabs, 8, cudaMemcpyDeviceToHost, st));
-  S2_CUDA(cudaMemcpyAsync(m->h_read + 8, m->cand_totals, size_t(std::max(1, m->nslabs)) * 8,
-                          cudaMemcpyDeviceToHost, st));
+  S2_CUDA(cudaMemcpyAsync(m->h_read + 4, m->cand_base + m->nslabs, 8, cudaMemcpyDeviceToHost, st));
   S2_CUDA(cudaStreamSynchronize(st));
   prof_collect(m);
   m->ntris = m->h_read[0];
   m->invalid = m->h_read[1];
+  m->nverts = m->h_read[2];
   m->errflags = unsigned(m->h_read[3] & 0xffffffffull);
-  m->nverts = m->h_read[4];
-  m->ncand = 0;
-  for (int s = 0; s < m->nslabs; ++s) m->ncand += m->h_read[8 + s];
+  m->ncand = m->h_read[4];
   return S2M_OK;
-}
-
-unsigned long long max_slab_candidates(const s2m_mesh *m) {
-  unsigned long long mx = 0;
-  for (int s = 0; s < m->nslabs; ++s) mx = std::max(mx, m->h_read[8 + s]);
-  return mx;
 }
 
 }  // namespace
@@ -608,13 +611,14 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
     return rc;
   }
   const unsigned long long N = (unsigned long long)m->N;
-  const unsigned long long cells_per_slab = (unsigned long long)m->D * N * N;
-  unsigned long long cand_cap = std::min(cells_per_slab, cells_per_slab / 8 + 65536);
+  const unsigned long long N3 = N * N * N;
+  unsigned long long cand_cap = std::min(N3, std::max<unsigned long long>(65536, 8 * N * N));
   unsigned long long vcap = params->max_vertices ? params->max_vertices
-                                                 : std::min(N * N * N, std::max<unsigned long long>(65536, 12 * N * N));
-  unsigned long long tcap = params->max_triangles ? params->max_triangles : std::max<unsigned long long>(131072, 3 * vcap);
+                                                 : std::min(N3, std::max<unsigned long long>(65536, 6 * N * N));
+  unsigned long long tcap = params->max_triangles ? params->max_triangles : std::max<unsigned long long>(131072, 2 * vcap + 4096);
+  if (params->max_vertices) cand_cap = std::min(N3, std::max<unsigned long long>(1024, params->max_vertices));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  for (int attempt = 0; attempt < 4; ++attempt) {
+  for (int attempt = 0; attempt < 5; ++attempt) {
     rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen);
     if (rc != S2M_OK) break;
     cudaError_t e = enqueue(m, st);
@@ -639,11 +643,16 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
       rc = S2M_OK;
       break;
     }
-    // Exact totals are known even after an overflow: grow to them and re-run.
-    if (m->errflags & S2_ERR_CAND_OVF) cand_cap = std::min(cells_per_slab, max_slab_candidates(m) + 4096);
-    if (m->errflags & (S2_ERR_VERT_OVF | S2_ERR_CAND_OVF)) vcap = std::max<unsigned long long>(vcap, m->nverts + m->nverts / 8 + 4096);
-    if (m->errflags & S2_ERR_CAND_OVF) vcap = std::max(vcap, std::min(N * N * N, 2 * vcap));
-    tcap = std::max<unsigned long long>(tcap, std::max<unsigned long long>(m->ntris + m->ntris / 8 + 4096, 3 * vcap));
+    // The totals of the stage that overflowed are exact (offsets are counted
+    // even where the writes were dropped): grow to them and run again.
+    if (m->errflags & S2_ERR_CAND_OVF) {
+      cand_cap = std::min<unsigned long long>(N3, m->ncand + m->ncand / 16 + 4096);
+      vcap = std::max(vcap, cand_cap);
+    } else if (m->errflags & S2_ERR_VERT_OVF) {
+      vcap = std::min<unsigned long long>(N3, m->nverts + m->nverts / 16 + 4096);
+    }
+    if (m->errflags & S2_ERR_TRI_OVF) tcap = m->ntris + m->ntris / 16 + 4096;
+    tcap = std::max(tcap, 2 * vcap + 4096);
     rc = S2M_E_OVERFLOW;
     set_err(err, errlen, "mesh buffers overflowed after resizing");
   }

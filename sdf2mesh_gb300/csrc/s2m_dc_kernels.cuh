@@ -96,18 +96,14 @@ __device__ __forceinline__ bool s2_classify(const S2Job &j, const float *__restr
   return false;
 }
 
-struct S2Vertex {
-  bool has;
-  unsigned signs;
-  float pos[3];
-  float nrm[3];
-};
-
 // dualcontour.wgsl:72-131 (crossings, counting rule, mass point) and
-// :161-180 (normal, sign bits) on the cell's exact corner values.
-__device__ __forceinline__ S2Vertex s2_vertex(const S2Job &j, const float *__restrict__ ring, S2Cell c) {
-  float v[8];
-  s2_load_corners(j, ring, c, v);
+// :161-180 (normal, sign bits) on one candidate cell.  `v` holds the cell's
+// lattice values; corners whose reference coordinates are off the lattice are
+// re-evaluated here at those coordinates, so the rule sees exactly the
+// reference's 8 values.  Writes the vertex and returns the final key
+// (x | y << 16 | label << 32 | signs << 48 | has_vertex << 63).
+__device__ __forceinline__ unsigned long long s2_vertex(const S2Job &j, S2Cell c, float v[8], float pos[3],
+                                                        float nrm[3]) {
   float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
   float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
   unsigned off = s2_off_mask(j, c);
@@ -140,33 +136,33 @@ __device__ __forceinline__ S2Vertex s2_vertex(const S2Job &j, const float *__res
       }
     }
   }
-  S2Vertex r;
-  r.signs = (v[1] > 0.0f ? 1u : 0u) | (v[2] > 0.0f ? 2u : 0u) | (v[4] > 0.0f ? 4u : 0u) | (v[0] > 0.0f ? 8u : 0u);
-  r.has = count > 1.0f;
-  if (!r.has) return r;
+  const unsigned signs = (v[1] > 0.0f ? 1u : 0u) | (v[2] > 0.0f ? 2u : 0u) | (v[4] > 0.0f ? 4u : 0u) | (v[0] > 0.0f ? 8u : 0u);
+  const unsigned long long zl = (unsigned long long)(j.lag ? c.z + 1 : c.z);
+  unsigned long long key = (unsigned long long)c.x | ((unsigned long long)c.y << 16) | (zl << 32) |
+                           ((unsigned long long)signs << 48);
+  if (!(count > 1.0f)) return key;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     float bsize = __fsub_rn(mx[a], mn[a]);
-    r.pos[a] = __fadd_rn(mn[a], __fdiv_rn(__fmul_rn(bsize, avg[a]), count));
+    pos[a] = __fadd_rn(mn[a], __fdiv_rn(__fmul_rn(bsize, avg[a]), count));
   }
-  s2v3 n = s2m_user_normal(s2mk(r.pos[0], r.pos[1], r.pos[2]), j.eps);
+  s2v3 n = s2m_user_normal(s2mk(pos[0], pos[1], pos[2]), j.eps);
   float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(n.x, n.x), __fmul_rn(n.y, n.y)), __fmul_rn(n.z, n.z)));
-  r.nrm[0] = __fdiv_rn(n.x, len);
-  r.nrm[1] = __fdiv_rn(n.y, len);
-  r.nrm[2] = __fdiv_rn(n.z, len);
-  return r;
+  nrm[0] = __fdiv_rn(n.x, len);
+  nrm[1] = __fdiv_rn(n.y, len);
+  nrm[2] = __fdiv_rn(n.z, len);
+  return key | (1ull << 63);
 }
 
-// Cell pass of one slab (cell slices zc0 .. zc1 - 1): classify every cell,
-// compact the candidates in (z, y, x) order with a look-back prefix over
-// tiles, then place the vertex of each candidate at its global slot.
+// Cell pass of one slab (cell slices zc0 .. zc1 - 1): classify every cell and
+// append the candidates, in (z, y, x) order, to the job's candidate list at
+// cand.base[slab] + (look-back prefix over tiles), each with its 8 lattice
+// corner values.  The last tile publishes cand.base[slab + 1].
 extern "C" __global__ void __launch_bounds__(S2_CELL_BLOCK)
-s2m_cells(S2Job job, S2Slab slab, int zc0, int zc1) {
+s2m_cells(S2Job job, S2Slab slab, S2Cand cand, int zc0, int zc1, int slab_index) {
   __shared__ unsigned s_tile;
   __shared__ unsigned s_warp[32];
-  __shared__ unsigned s_cand[S2_CELL_TILE];
   __shared__ unsigned long long s_excl;
-  __shared__ unsigned s_total;
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(slab.tile_counter, 1u);
   __syncthreads();
@@ -174,59 +170,72 @@ s2m_cells(S2Job job, S2Slab slab, int zc0, int zc1) {
   const long long ncells = (long long)(zc1 - zc0) * job.N * job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
   if (tile >= ntiles) return;
+  const unsigned long long base = cand.base[slab_index];
 
   unsigned ballots[S2_CELL_CPT];
 #pragma unroll
   for (int m = 0; m < S2_CELL_CPT; ++m) {
     long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
-    bool cand = c < ncells && s2_classify(job, slab.ring, s2_cell_of(job, c, zc0));
-    ballots[m] = __ballot_sync(S2_FULL, cand);
+    bool is_cand = c < ncells && s2_classify(job, slab.ring, s2_cell_of(job, c, zc0));
+    ballots[m] = __ballot_sync(S2_FULL, is_cand);
     if (lane == 0) s_warp[m * 8 + warp] = __popc(ballots[m]);
   }
   __syncthreads();
   if (warp == 0) {
     unsigned tot = s2_warp_exclusive32(s_warp);
-    if (lane == 0) s_total = tot;
+    unsigned long long excl = s2_lookback(slab.status, tile, tot, slab.err);
+    if (lane == 0) {
+      s_excl = excl;
+      if (tile == ntiles - 1) cand.base[slab_index + 1] = base + excl + tot;
+    }
   }
   __syncthreads();
   const unsigned lt = s2_lanemask_lt();
 #pragma unroll
   for (int m = 0; m < S2_CELL_CPT; ++m) {
-    if ((ballots[m] >> lane) & 1u) {
-      unsigned slot = s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
-      s_cand[slot] = (unsigned)(m * S2_CELL_BLOCK + tid);
-    }
-  }
-  const unsigned total = s_total;
-  if (warp == 0) {
-    unsigned long long excl = s2_lookback(slab.status, tile, total, slab.err);
-    if (lane == 0) {
-      s_excl = excl;
-      if (tile == ntiles - 1) *slab.cand_total = excl + total;
-    }
-  }
-  __syncthreads();
-  const unsigned long long excl = s_excl;
-  for (unsigned k = tid; k < total; k += S2_CELL_BLOCK) {
-    long long c = (long long)tile * S2_CELL_TILE + s_cand[k];
-    S2Cell cell = s2_cell_of(job, c, zc0);
-    S2Vertex vx = s2_vertex(job, slab.ring, cell);
-    unsigned long long o = excl + k;
-    if (o >= slab.cand_cap) {
+    if (!((ballots[m] >> lane) & 1u)) continue;
+    unsigned long long o = base + s_excl + s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
+    if (o >= cand.cap) {
       atomicOr(slab.err, S2_ERR_CAND_OVF);
       continue;
     }
-    unsigned long long zl = (unsigned long long)(job.lag ? cell.z + 1 : cell.z);
-    unsigned long long key = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | (zl << 32) |
-                             ((unsigned long long)vx.signs << 48) | ((vx.has ? 1ull : 0ull) << 63);
-    slab.cand_key[o] = key;
-    if (vx.has) {
-      slab.cand_pos[3 * o] = vx.pos[0];
-      slab.cand_pos[3 * o + 1] = vx.pos[1];
-      slab.cand_pos[3 * o + 2] = vx.pos[2];
-      slab.cand_nrm[3 * o] = vx.nrm[0];
-      slab.cand_nrm[3 * o + 1] = vx.nrm[1];
-      slab.cand_nrm[3 * o + 2] = vx.nrm[2];
+    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
+    S2Cell cell = s2_cell_of(job, c, zc0);
+    float v[8];
+    s2_load_corners(job, slab.ring, cell, v);
+    cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
+    float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+}
+
+// Vertices of every candidate of the job, one candidate per thread (dense:
+// candidates are a small fraction of the cells).  Rewrites cand.key with the
+// final key and writes cand.pos / cand.nrm for cells with a vertex.
+extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
+s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
+  const unsigned long long n = min(cand.base[nslabs], cand.cap);
+  for (unsigned long long o = (unsigned long long)blockIdx.x * S2_VX_BLOCK + threadIdx.x; o < n;
+       o += (unsigned long long)gridDim.x * S2_VX_BLOCK) {
+    unsigned long long k = cand.key[o];
+    S2Cell c;
+    c.x = (int)(k & 0xffffull);
+    c.y = (int)((k >> 16) & 0xffffull);
+    c.z = (int)((k >> 32) & 0xffffull);
+    const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
+    float4 a = src[0], b = src[1];
+    float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float pos[3], nrm[3];
+    unsigned long long key = s2_vertex(job, c, v, pos, nrm);
+    cand.key[o] = key;
+    if (key >> 63) {
+      cand.pos[3 * o] = pos[0];
+      cand.pos[3 * o + 1] = pos[1];
+      cand.pos[3 * o + 2] = pos[2];
+      cand.nrm[3 * o] = nrm[0];
+      cand.nrm[3 * o + 1] = nrm[1];
+      cand.nrm[3 * o + 2] = nrm[2];
     }
   }
 }

@@ -27,14 +27,23 @@ struct S2Job {
 struct S2Slab {
   float *ring;                    // lattice ring
   unsigned long long *status;     // look-back words of s2m_cells tiles
-  unsigned long long *status2;    // look-back words of s2m_vcompact tiles
-  unsigned *tile_counter;         // [0] s2m_cells, [1] s2m_vcompact
-  unsigned long long *cand_key;   // candidate results (key | has_vertex << 63)
-  float *cand_pos;                // 3 per candidate
-  float *cand_nrm;                // 3 per candidate
-  unsigned long long cand_cap;    // capacity of the candidate arrays
-  unsigned long long *cand_total; // out: candidates of this slab (exact even on overflow)
+  unsigned *tile_counter;         // [0] s2m_cells
   unsigned *err;                  // error flags (S2_ERR_*)
+};
+
+// Candidate cells of the whole job, in (z, y, x) order: cells that may carry
+// a vertex.  s2m_cells appends them slab by slab; s2m_vertices places their
+// vertices; s2m_vcompact keeps those with a vertex.
+struct S2Cand {
+  unsigned long long *key;        // x | y << 16 | z << 32; after s2m_vertices the final
+                                  // key (label, signs << 48, has_vertex << 63)
+  float *val;                     // 8 lattice corner values per candidate (32-byte aligned)
+  float *pos;                     // 3 per candidate
+  float *nrm;                     // 3 per candidate
+  unsigned long long cap;         // capacity of the arrays
+  unsigned long long *base;       // nslabs + 1 running offsets (exact even on overflow)
+  unsigned long long *status;     // look-back words of s2m_vcompact tiles
+  unsigned *tile_counter;         // s2m_vcompact
 };
 
 // Mesh outputs and the cross-slab counters.
@@ -45,7 +54,7 @@ struct S2MeshDev {
   unsigned *tris;                 // 3 * tcap
   unsigned long long vcap;
   unsigned long long tcap;
-  unsigned long long *vbase;      // nslabs + 1 running vertex offsets
+  unsigned long long *vtotal;     // out: vertices of the job (exact even on overflow)
   unsigned *rowcnt;               // N * N vertices per (z label, y) row
   unsigned *rowstart;             // N * N + 1 exclusive prefix of rowcnt
   unsigned long long *scan_status;  // look-back words (row scan, quads)
@@ -67,6 +76,7 @@ struct S2MeshDev {
 #define S2_CELL_TILE (S2_CELL_BLOCK * S2_CELL_CPT)
 #define S2_EVAL_BLOCK 256
 #define S2_EVAL_RUN 4
+#define S2_VX_BLOCK 128
 #define S2_VC_BLOCK 256
 #define S2_VC_CPT 4
 #define S2_VC_TILE (S2_VC_BLOCK * S2_VC_CPT)

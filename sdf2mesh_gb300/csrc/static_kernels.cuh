@@ -5,26 +5,24 @@
 #include "s2m_device.h"
 #include "s2m_lookback.cuh"
 
-// Compact the candidates of one slab that carry a vertex into the global
-// vertex arrays (reference order: z, then y, then x), count vertices per
-// (z label, y) row, and publish the running vertex offset for the next slab.
-// Persistent grid; tiles are taken in order from slab.tile_counter[1].
-__global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Slab slab, S2MeshDev mesh, int slab_index) {
+// Keep the candidates that carry a vertex, in order (z, then y, then x, as
+// the reference's VertexList), in the mesh's vertex arrays; count vertices
+// per (z label, y) row.  Persistent grid; tiles are taken in order from
+// cand.tile_counter, the prefix comes from the look-back over tiles.
+__global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand cand, S2MeshDev mesh, int nslabs) {
   __shared__ unsigned s_tile;
   __shared__ unsigned s_warp[32];
-  __shared__ unsigned s_total;
   __shared__ unsigned long long s_excl;
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const unsigned long long ncand = min(*slab.cand_total, slab.cand_cap);
+  const unsigned long long ncand = min(cand.base[nslabs], cand.cap);
   const unsigned ntiles = (unsigned)((ncand + S2_VC_TILE - 1) / S2_VC_TILE);
-  const unsigned long long base = mesh.vbase[slab_index];
   if (ntiles == 0) {
-    if (blockIdx.x == 0 && tid == 0) mesh.vbase[slab_index + 1] = base;
+    if (blockIdx.x == 0 && tid == 0) *mesh.vtotal = 0;
     return;
   }
   const unsigned lt = s2_lanemask_lt();
   for (;;) {
-    if (tid == 0) s_tile = atomicAdd(slab.tile_counter + 1, 1u);
+    if (tid == 0) s_tile = atomicAdd(cand.tile_counter, 1u);
     __syncthreads();
     const unsigned tile = s_tile;
     if (tile >= ntiles) break;
@@ -33,21 +31,17 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Slab sl
 #pragma unroll
     for (int m = 0; m < S2_VC_CPT; ++m) {
       unsigned long long o = (unsigned long long)tile * S2_VC_TILE + m * S2_VC_BLOCK + tid;
-      keys[m] = o < ncand ? slab.cand_key[o] : 0ull;
+      keys[m] = o < ncand ? cand.key[o] : 0ull;
       ballots[m] = __ballot_sync(S2_FULL, (keys[m] >> 63) != 0ull);
       if (lane == 0) s_warp[m * 8 + warp] = __popc(ballots[m]);
     }
     __syncthreads();
     if (warp == 0) {
       unsigned tot = s2_warp_exclusive32(s_warp);
-      if (lane == 0) s_total = tot;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      unsigned long long excl = s2_lookback(slab.status2, tile, s_total, slab.err);
+      unsigned long long excl = s2_lookback(cand.status, tile, tot, mesh.err);
       if (lane == 0) {
         s_excl = excl;
-        if (tile == ntiles - 1) mesh.vbase[slab_index + 1] = base + excl + s_total;
+        if (tile == ntiles - 1) *mesh.vtotal = excl + tot;
       }
     }
     __syncthreads();
@@ -55,7 +49,7 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Slab sl
     for (int m = 0; m < S2_VC_CPT; ++m) {
       if ((ballots[m] >> lane) & 1u) {
         unsigned long long o = (unsigned long long)tile * S2_VC_TILE + m * S2_VC_BLOCK + tid;
-        unsigned long long v = base + s_excl + s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
+        unsigned long long v = s_excl + s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
         unsigned long long key = keys[m] & ~(1ull << 63);
         unsigned y = (unsigned)((key >> 16) & 0xffffu), zl = (unsigned)((key >> 32) & 0xffffu);
         atomicAdd(mesh.rowcnt + (unsigned long long)zl * job.N + y, 1u);
@@ -65,12 +59,12 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Slab sl
           continue;
         }
         mesh.key[v] = key;
-        mesh.pos[3 * v] = slab.cand_pos[3 * o];
-        mesh.pos[3 * v + 1] = slab.cand_pos[3 * o + 1];
-        mesh.pos[3 * v + 2] = slab.cand_pos[3 * o + 2];
-        mesh.nrm[3 * v] = slab.cand_nrm[3 * o];
-        mesh.nrm[3 * v + 1] = slab.cand_nrm[3 * o + 1];
-        mesh.nrm[3 * v + 2] = slab.cand_nrm[3 * o + 2];
+        mesh.pos[3 * v] = cand.pos[3 * o];
+        mesh.pos[3 * v + 1] = cand.pos[3 * o + 1];
+        mesh.pos[3 * v + 2] = cand.pos[3 * o + 2];
+        mesh.nrm[3 * v] = cand.nrm[3 * o];
+        mesh.nrm[3 * v + 1] = cand.nrm[3 * o + 1];
+        mesh.nrm[3 * v + 2] = cand.nrm[3 * o + 2];
       }
     }
     __syncthreads();
@@ -191,13 +185,13 @@ __device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, un
   return r;
 }
 
-__global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads(S2Job job, S2MeshDev mesh, int nslabs, unsigned scan_tiles) {
+__global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads(S2Job job, S2MeshDev mesh, unsigned scan_tiles) {
   __shared__ unsigned s_tile;
   __shared__ unsigned s_warp[32];
   __shared__ unsigned s_total;
   __shared__ unsigned long long s_excl;
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const unsigned long long V = mesh.vbase[nslabs];
+  const unsigned long long V = *mesh.vtotal;
   if (V > mesh.vcap) return;  // vertex overflow: the host re-runs with larger buffers
   unsigned long long *status = mesh.scan_status + scan_tiles;
   const unsigned ntiles = (unsigned)((V + S2_Q_TILE - 1) / S2_Q_TILE);

@@ -1,0 +1,51 @@
+"""Extract the reference's own test vectors into tests/golden/.
+
+The reference's only tests (src/shadertoy.rs:354-453) pin its WGSL text
+surgery: `remove_function` (:357-392) and `rename_function` (:394-401).  This
+script reads those tests as text from a reference checkout and writes their
+inputs and expected facts to wgsl_surgery.json.  Run from the repository root:
+
+    python tests/golden/make_golden.py /path/to/sdf2mesh
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+
+def raw_strings(text):
+    return re.findall(r'r#"(.*?)"#', text, flags=re.S)
+
+
+def main(ref_root):
+    src = open(os.path.join(ref_root, "src", "shadertoy.rs")).read()
+    tests = src[src.index("#[cfg(test)]"):]
+    remove_block = tests[tests.index("fn remove_function()"):tests.index("fn rename_function()")]
+    rename_block = tests[tests.index("fn rename_function()"):tests.index("fn test_naga()")]
+    remove_in = raw_strings(remove_block)[0]
+    rename_in = raw_strings(rename_block)[0]
+    out = {
+        "source": "src/shadertoy.rs:357-401 (WilstonOreo/sdf2mesh)",
+        "remove_function": {
+            "input": remove_in,
+            "steps": [
+                {"remove": "fn main_1()", "contains": ["fn mainImage(fragColor"], "absent": ["fn main_1()"]},
+                {"remove": "fn main(", "contains": ["fn mainImage(fragColor"], "absent": ["fn main()"]},
+                {"remove": "fn mainImage(", "trim_equals": "@fragment"},
+            ],
+        },
+        "rename_function": {
+            "input": rename_in, "old": "normal", "new": "sdf3d_normal",
+            "contains": ["fn sdf3d_normal(p_4: vec3<f32>, epsilon: f32) -> vec3<f32>"],
+        },
+    }
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "wgsl_surgery.json"), "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

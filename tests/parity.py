@@ -82,3 +82,58 @@ def compare_with_ties(gpu, ref, kind, params, resolution, bounds, eps, h, pos_to
     touching = {t for t in tdiff if any(v in flips or v in only for v in t)}
     return {"tie_cells": len(flips | only), "vertex_only_one_side": len(only), "max_pos_err_cells": max_err,
             "moved": moved, "tri_diff": len(tdiff), "tri_diff_unexplained": len(tdiff - touching)}
+
+
+def reference_quads(cell_xyz, signs):
+    """Vectorised restatement of VertexList::fetch_triangle_indices
+    (mesh.rs:267-331, Quad::swap / make_triangles / is_valid lib.rs:190-211)
+    over a sorted vertex list.  Returns (triangles (T, 3) uint32, invalid
+    quad count, missing cells (M, 3) of the invalid quads)."""
+    c = np.asarray(cell_xyz, np.int64)
+    keys = c[:, 0] | (c[:, 1] << 16) | (c[:, 2] << 32)
+    V = len(keys)
+    s = np.asarray(signs, np.int64)
+    b0, b1, b2, b3 = (s & 1) != 0, (s & 2) != 0, (s & 4) != 0, (s & 8) != 0
+    x, y, z = c[:, 0], c[:, 1], c[:, 2]
+    idx = np.arange(V, dtype=np.int64)
+    NONE = np.int64(0xFFFFFFFF)
+
+    def find(xx, yy, zz):
+        k = xx | (yy << 16) | (zz << 32)
+        pos = np.searchsorted(keys, k)
+        ok = (pos < V) & (keys[np.minimum(pos, V - 1)] == k)
+        return np.where(ok, pos, NONE)
+
+    quads = np.full((V, 3, 4), NONE, np.int64)
+    active = np.zeros((V, 3), bool)
+    swap = np.zeros((V, 3), bool)
+    m = (b0 != b3) & (y > 0) & (z > 0)
+    quads[m, 0] = np.stack([find(x[m], y[m] - 1, z[m] - 1), find(x[m], y[m], z[m] - 1), idx[m],
+                            find(x[m], y[m] - 1, z[m])], 1)
+    active[:, 0], swap[:, 0] = m, b0
+    m = (b1 != b3) & (x > 0) & (z > 0)
+    quads[m, 1] = np.stack([find(x[m] - 1, y[m], z[m] - 1), find(x[m], y[m], z[m] - 1), idx[m],
+                            find(x[m] - 1, y[m], z[m])], 1)
+    active[:, 1], swap[:, 1] = m, ~b1
+    m = (b2 != b3) & (x > 0) & (y > 0)
+    quads[m, 2] = np.stack([find(x[m] - 1, y[m] - 1, z[m]), find(x[m], y[m] - 1, z[m]), idx[m],
+                            find(x[m] - 1, y[m], z[m])], 1)
+    active[:, 2], swap[:, 2] = m, b2
+    quads = np.where(swap[..., None], quads[..., ::-1], quads)
+    valid = active & (quads != NONE).all(-1)
+    invalid = active & ~valid
+    q = quads[valid]
+    tris = np.stack([q[:, [2, 1, 0]], q[:, [0, 3, 2]]], 1).reshape(-1, 3).astype(np.uint32)
+    # cells whose vertex an invalid quad looked for and did not find
+    missing = []
+    for vi, qi in zip(*np.nonzero(invalid)):
+        xx, yy, zz = c[vi]
+        cand = {0: [(xx, yy - 1, zz - 1), (xx, yy, zz - 1), (xx, yy - 1, zz)],
+                1: [(xx - 1, yy, zz - 1), (xx, yy, zz - 1), (xx - 1, yy, zz)],
+                2: [(xx - 1, yy - 1, zz), (xx, yy - 1, zz), (xx - 1, yy, zz)]}[int(qi)]
+        for cc in cand:
+            k = cc[0] | (cc[1] << 16) | (cc[2] << 32)
+            p = np.searchsorted(keys, k)
+            if not (p < V and keys[p] == k):
+                missing.append(cc)
+    return tris, int(invalid.sum()), np.array(missing, np.int64).reshape(-1, 3)

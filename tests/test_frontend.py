@@ -1,0 +1,193 @@
+"""The shader front end: `.sdf3d` preprocessing (shader.rs:44-67, 159-203),
+WGSL / GLSL lowering to CUDA C, and the WGSL text helpers
+(shadertoy.rs:248-352) -- all on the CPU.
+
+The lowered CUDA C is also valid host C++ (s2m_prelude.cuh is
+__host__ __device__); compiled with g++ -ffp-contract=off it must evaluate
+every fixture SDF bit-for-bit like the oracle's hand restatement.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import sdf2mesh_gb300 as s2m
+from sdf2mesh_gb300 import workloads
+from tests.hostsdf import compile_host, eval_host
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+REF_EXAMPLES = "/root/reference/examples"
+
+
+def lower(src, lang=s2m.LANG_WGSL, name="sdf"):
+    if lang == s2m.LANG_WGSL:
+        src = s2m.Sdf3DShader.from_source(src).source
+    return s2m.translate(src, lang, name)
+
+
+def points(n=20000, seed=1, lo=-1.2, hi=1.2):
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32).astype(np.float64)
+    # include lattice coordinates of a 64^3 job exactly as the kernel forms them
+    size = np.float32(np.float32(2.0) / np.float32(63))
+    c = (np.float32(-1.0) + size * np.arange(64, dtype=np.float32)).astype(np.float64)
+    g = np.stack(np.meshgrid(c[::7], c[::5], c[::3], indexing="ij"), -1).reshape(-1, 3)
+    return np.concatenate([p, g])
+
+
+def assert_same_bits(a, b):
+    a32, b32 = a.astype(np.float32), b.astype(np.float32)
+    same = (a32.view(np.uint32) == b32.view(np.uint32)) | (np.isnan(a32) & np.isnan(b32))
+    assert same.all(), f"{(~same).sum()} of {len(a)} differ; first {np.nonzero(~same)[0][:5]}"
+
+
+def test_torus_lowering_bit_exact(lib, oracle_lib):
+    src, prm = workloads.torus()
+    cuda, fp32, sfu = lower(src)
+    assert (fp32, sfu) == (8.0, 2.0)
+    p = points()
+    assert_same_bits(eval_host(cuda, p), oracle.evaluate(oracle.TORUS, prm, p))
+
+
+def test_csg64_lowering_bit_exact(lib, oracle_lib):
+    src, prm = workloads.csg64(seed=0)
+    cuda, fp32, sfu = lower(src)
+    assert fp32 > 1000 and sfu > 64
+    p = points(5000)
+    assert_same_bits(eval_host(cuda, p), oracle.evaluate(oracle.CSG, prm, p))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_tree_lowering_bit_exact(lib, oracle_lib, seed):
+    src, prog = workloads.random_tree(seed)
+    cuda, _, _ = lower(src)
+    p = points(4000, seed=seed)
+    assert_same_bits(eval_host(cuda, p), oracle.evaluate(oracle.TREE, prog, p))
+
+
+def test_mandelbulb_glsl_lowering_bit_exact_on_host(lib, oracle_lib):
+    """Same host libm on both sides: the GLSL lowering (swizzle-assign, for /
+    continue, atan/asin/pow/log/sin/cos) matches the oracle's restatement."""
+    src, prm = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
+    cuda, fp32, sfu = lower(src, s2m.LANG_GLSL, "sdf")
+    assert sfu > 8 * 6
+    p = points(5000, lo=-1.25, hi=1.25)
+    assert_same_bits(eval_host(cuda, p), oracle.evaluate(oracle.MANDELBULB, prm, p))
+
+
+def test_normal_is_tetrahedral_sum(lib):
+    """sdf3d_normal (sdf3d_normal.wgsl:4-10): sum of v_i * f(p + v_i * eps), not normalised."""
+    src, _ = workloads.sphere(0.5)
+    cuda, _, _ = lower(src)
+    L = compile_host(cuda)
+    p = np.array([[0.3, -0.2, 0.7]], np.float32)
+    out = np.zeros(3, np.float32)
+    L.normal_points(1, p.ctypes.data, np.float32(1e-4), out.ctypes.data)
+    f32 = np.float32
+    eps = f32(1e-4)
+    vs = [(1, -1, -1), (-1, -1, 1), (-1, 1, -1), (1, 1, 1)]
+    acc = None
+    for v in vs:
+        v = np.array(v, np.float32)
+        q = p[0] + v * eps
+        d = f32(np.sqrt(f32(f32(f32(q[0] * q[0]) + f32(q[1] * q[1])) + f32(q[2] * q[2])))) - f32(0.5)
+        term = v * f32(d)
+        acc = term if acc is None else (acc + term).astype(np.float32)
+    assert np.array_equal(out.view(np.uint32), acc.astype(np.float32).view(np.uint32))
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+@pytest.mark.parametrize("name", ["torus.sdf3d", "martin_cube.sdf3d", "p_key.sdf3d"])
+def test_reference_examples_lower_and_run(lib, name):
+    sh = s2m.Sdf3DShader.from_path(os.path.join(REF_EXAMPLES, name))
+    cuda, fp32, _ = s2m.translate(sh.source)
+    assert fp32 > 0
+    B = 40.0 if name == "p_key.sdf3d" else 2.0
+    v = eval_host(cuda, points(3000, lo=-B / 2, hi=B / 2))
+    assert np.isfinite(v).all()
+    assert (v < 0).any() and (v > 0).any(), "the surface crosses the box"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+def test_reference_mandelmesh_glsl(lib, oracle_lib):
+    """examples/mandelmesh.frag: 5 iterations, power 8, bailout 2, offset 0.003."""
+    text = open(os.path.join(REF_EXAMPLES, "mandelmesh.frag")).read()
+    cuda, _, _ = s2m.translate(text, s2m.LANG_GLSL, "sdf")
+    p = points(3000, lo=-1.25, hi=1.25)
+    ref = oracle.evaluate(oracle.MANDELBULB, [8.0, 5, 2.0, 0.003], p)
+    assert_same_bits(eval_host(cuda, p), ref)
+
+
+def test_glsl_missing_function(lib):
+    with pytest.raises(s2m.S2MError) as e:
+        s2m.translate("#version 450\nfloat other(vec3 p) { return p.x; }\nvoid main() {}\n", s2m.LANG_GLSL, "sdf")
+    assert e.value.name == "MISSING_SDF"
+
+
+def test_wgsl_missing_sdf3d(lib):
+    with pytest.raises(s2m.S2MError) as e:
+        s2m.translate("fn f(p: vec3f) -> f32 { return p.x; }\n")
+    assert e.value.name == "MISSING_SDF"
+
+
+def test_parse_error_names_line(lib):
+    with pytest.raises(s2m.S2MError) as e:
+        s2m.translate("fn sdf3d(p: vec3f) -> f32 {\n  let a = ;\n  return a;\n}\n")
+    assert "line 2" in str(e.value)
+
+
+def test_preprocess_use_and_include(lib, tmp_path):
+    inc = tmp_path / "shapes.wgsl"
+    inc.write_text("fn my_ball(p: vec3f) -> f32 { return sdf3d_sphere(p, 0.5); }\n")
+    main = tmp_path / "m.sdf3d"
+    main.write_text('use sdf3d::primitives;\nuse nothing::here;\ninclude "shapes.wgsl";\n'
+                    'include "m.sdf3d";\nfn sdf3d(p: vec3f) -> f32 { return my_ball(p); }\n')
+    sh = s2m.Sdf3DShader.from_path(os.fspath(main))
+    assert "fn sdf3d_sphere(" in sh.source          # use sdf3d::primitives
+    assert "nothing::here" not in sh.source         # unknown modules are dropped
+    assert "fn my_ball(" in sh.source               # include, relative to the file
+    assert sh.source.count("fn sdf3d(") == 1        # self-include ignored
+    cuda, _, _ = s2m.translate(sh.source)
+    v = eval_host(cuda, np.array([[0.5, 0.0, 0.0], [0.0, 0.0, 0.0]]))
+    assert v[0] == 0.0 and v[1] == -0.5
+
+
+def test_builtin_modules(lib):
+    for use, fns in (("sdf3d::*", ["sdf3d_box", "sdf3d_torus", "sdf3d_normal"]),
+                     ("sdf3d::normal", ["sdf3d_normal"]), ("sdf::op", ["sdf_op_smooth_union"]),
+                     ("sdf::*", ["sdf_op_smooth_subtraction"])):
+        sh = s2m.Sdf3DShader.from_source(f"use {use};\n")
+        for fn in fns:
+            assert f"fn {fn}(" in sh.source, (use, fn)
+
+
+def test_golden_remove_function(lib):
+    g = json.load(open(os.path.join(GOLDEN, "wgsl_surgery.json")))["remove_function"]
+    w = g["input"]
+    for step in g["steps"]:
+        w = s2m.wgsl_remove_function(w, step["remove"])
+        for c in step.get("contains", []):
+            assert c in w
+        for c in step.get("absent", []):
+            assert c not in w
+        if "trim_equals" in step:
+            assert w.strip() == step["trim_equals"]
+
+
+def test_golden_rename_function(lib):
+    g = json.load(open(os.path.join(GOLDEN, "wgsl_surgery.json")))["rename_function"]
+    out = s2m.wgsl_rename_function(g["input"], g["old"], g["new"])
+    for c in g["contains"]:
+        assert c in out
+
+
+def test_text_helpers_errors(lib):
+    with pytest.raises(s2m.S2MError):
+        s2m.wgsl_remove_function("fn a() {}\n", "fn b(")
+    assert s2m.wgsl_has_function("  fn sdf3d(p: vec3f) -> f32 {}", "sdf3d")
+    assert not s2m.wgsl_has_function("fn sdf3dx(p: vec3f) -> f32 {}", "sdf3d")
