@@ -366,6 +366,8 @@ def ours(a):
         "mesh": {"vertices": nverts, "triangles": ntris, "invalid_quads": int(info.invalid_quads),
                  "candidate_cells": int(info.candidate_cells), "slab_depth": int(info.slab_depth)},
         "compile_s": compile_s,
+        "eval_variant": sdf.eval_variant()[0],
+        "eval_variant_ns_per_point": sdf.eval_variant()[1],
         "triangles_per_s": ntris * a.steps * ws / (tot_ms * 1e-3),
         "wall_s_timed": wall,
     }

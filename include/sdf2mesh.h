@@ -119,6 +119,13 @@ const char *s2m_sdf_cuda_source(const s2m_sdf *sdf);
 /* Algorithmic FP32 and SFU operations of one sdf3d evaluation. */
 int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops);
 
+/* Evaluation-kernel variant the autotuner chose for this SDF on its first
+   job (-1: not tuned yet): its name, and the measured ns per lattice point
+   of each of the S2M_EVAL_VARIANTS variants.  No reference counterpart (the
+   reference has one fixed kernel, dualcontour.wgsl:161-162). */
+#define S2M_EVAL_VARIANTS 6
+int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point);
+
 void s2m_sdf_free(s2m_sdf *sdf);
 
 /* Frontend only (no device): lower a source to CUDA C.  *out is malloc'ed. */

@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libs2m_oracle.so")
 SPHERE, TORUS, CSG, MANDELBULB, TREE = 0, 1, 2, 3, 4
 F32, F64 = 0, 1
 FLAG_SLICE_LAG = 1
+FLAG_QEF = 2
 
 _lock = threading.Lock()
 _lib = None
@@ -111,11 +112,11 @@ class OracleMesh:
 
 
 def mesh(kind, params, resolution, bounds, *, eps=1e-4, slice_lag=False, precision=F32,
-         z_begin=-1, z_end=-1, threads=0, skip_quads=False) -> OracleMesh:
+         z_begin=-1, z_end=-1, threads=0, skip_quads=False, qef=False) -> OracleMesh:
     L = lib()
     a, ap = _fparams(params)
-    p = _Params(resolution, bounds, eps, FLAG_SLICE_LAG if slice_lag else 0, z_begin, z_end,
-                threads, 1 if skip_quads else 0)
+    flags = (FLAG_SLICE_LAG if slice_lag else 0) | (FLAG_QEF if qef else 0)
+    p = _Params(resolution, bounds, eps, flags, z_begin, z_end, threads, 1 if skip_quads else 0)
     m = _Mesh()
     rc = L.oracle_mesh_run(kind, ap, len(a), precision, ctypes.byref(p), ctypes.byref(m))
     if rc != 0:

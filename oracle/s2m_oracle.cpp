@@ -293,6 +293,158 @@ CellOut<T> eval_cell(const Job<T> &j, const F &f, int x, int y, int z) {
   return o;
 }
 
+// ---------------------------------------------------------------------------
+// Precision mode (ORACLE_FLAG_QEF).  Corners come from the lattice c(i) =
+// bmin + size * i, shared by neighbouring cells, so all cells agree on every
+// sign.  Each sign-change edge gives a crossing q (cell-local, in [0,1]^3, t
+// as in dualcontour.wgsl:72-74) and a unit normal n (the tetrahedral
+// gradient of sdf3d_normal.wgsl:4-10 at the crossing, normalised); the
+// vertex minimises sum (n . (x - q))^2 around the mass point.  The sums are
+// accumulated in T with Neumaier compensation; the 3x3 solve is binary64:
+// cyclic Jacobi eigen-decomposition, eigenvalues below 0.1 of the largest
+// dropped, x = c + V D^+ V^T (A^T b - A c), clamped to the cell.
+
+template <class T> struct KSum {
+  T s = 0, c = 0;
+  void add(T x) {
+    T t = s + x;
+    if (m_abs(s) >= m_abs(x)) c = c + ((s - t) + x);
+    else c = c + ((x - t) + s);
+    s = t;
+  }
+  T value() const { return s + c; }
+};
+
+// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (binary64).
+// a: row-major symmetric matrix (overwritten); v: eigenvectors in columns.
+inline void jacobi3(double a[3][3], double v[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) v[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 24; ++sweep) {
+    double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (!(off > 1e-30 * diag)) break;
+    for (int pq = 0; pq < 3; ++pq) {
+      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+      const double apq = a[p][q];
+      if (apq == 0.0) continue;
+      const double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
+      const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+      const double c = 1.0 / std::sqrt(t * t + 1.0);
+      const double sn = t * c;
+      for (int k = 0; k < 3; ++k) {  // A <- A J (columns p, q)
+        const double akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - sn * akq;
+        a[k][q] = sn * akp + c * akq;
+      }
+      for (int k = 0; k < 3; ++k) {  // A <- J^T A (rows p, q)
+        const double apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - sn * aqk;
+        a[q][k] = sn * apk + c * aqk;
+      }
+      for (int k = 0; k < 3; ++k) {  // V <- V J
+        const double vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = c * vkp - sn * vkq;
+        v[k][q] = sn * vkp + c * vkq;
+      }
+    }
+  }
+}
+
+// x = c + pinv(A) (b - A c), eigenvalues < 0.1 * max dropped; clamped to [0,1].
+inline void qef_solve(const double A[6], const double b[3], const double c[3], double x[3]) {
+  double a[3][3] = {{A[0], A[1], A[2]}, {A[1], A[3], A[4]}, {A[2], A[4], A[5]}};
+  double r[3];
+  for (int i = 0; i < 3; ++i) r[i] = b[i] - ((a[i][0] * c[0] + a[i][1] * c[1]) + a[i][2] * c[2]);
+  double v[3][3];
+  jacobi3(a, v);
+  double lmax = std::fmax(std::fabs(a[0][0]), std::fmax(std::fabs(a[1][1]), std::fabs(a[2][2])));
+  double y[3];
+  for (int k = 0; k < 3; ++k) {
+    double vr = (v[0][k] * r[0] + v[1][k] * r[1]) + v[2][k] * r[2];
+    double l = a[k][k];
+    y[k] = (lmax > 0.0 && std::fabs(l) >= 0.1 * lmax) ? vr / l : 0.0;
+  }
+  for (int i = 0; i < 3; ++i) {
+    double d = (v[i][0] * y[0] + v[i][1] * y[1]) + v[i][2] * y[2];
+    double xi = c[i] + d;
+    x[i] = xi < 0.0 ? 0.0 : (xi > 1.0 ? 1.0 : xi);
+  }
+}
+
+template <class T, class F> V3<T> tetra_normal(const F &f, V3<T> p, T e) {
+  V3<T> v1 = {T(1), T(-1), T(-1)}, v2 = {T(-1), T(-1), T(1)};
+  V3<T> v3 = {T(-1), T(1), T(-1)}, v4 = {T(1), T(1), T(1)};
+  V3<T> n = v1 * f(p + v1 * e) + v2 * f(p + v2 * e);
+  n = n + v3 * f(p + v3 * e);
+  n = n + v4 * f(p + v4 * e);
+  return n;
+}
+
+template <class T> T lattice_coord(const Job<T> &j, int a, int i) { return j.bmin[a] + j.size[a] * T(i); }
+
+template <class T, class F>
+CellOut<T> eval_cell_qef(const Job<T> &j, const F &f, int x, int y, int z) {
+  int pos[3] = {x, y, z};
+  T lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = lattice_coord(j, a, pos[a]);
+    hi[a] = lattice_coord(j, a, pos[a] + 1);
+  }
+  T c[8];
+  for (int k = 0; k < 8; ++k)
+    c[k] = f(V3<T>{(k & 1) ? hi[0] : lo[0], (k & 2) ? hi[1] : lo[1], (k & 4) ? hi[2] : lo[2]});
+  static const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
+  static const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
+  static const int eax[12] = {2, 2, 2, 2, 1, 1, 1, 1, 0, 0, 0, 0};
+  KSum<T> sA[6], sb[3], sq[3];
+  int m = 0;
+  for (int e = 0; e < 12; ++e) {
+    T a = c[ea[e]], b = c[eb[e]];
+    if ((a > T(0)) == (b > T(0))) continue;
+    T t = adapt(a, b);
+    T q[3], w[3];
+    for (int ax = 0; ax < 3; ++ax) {
+      if (ax == eax[e]) {
+        q[ax] = t;
+        w[ax] = lo[ax] + j.size[ax] * t;
+      } else {
+        bool one = (ea[e] >> ax) & 1;
+        q[ax] = one ? T(1) : T(0);
+        w[ax] = one ? hi[ax] : lo[ax];
+      }
+    }
+    V3<T> n = tetra_normal(f, V3<T>{w[0], w[1], w[2]}, j.eps);
+    T len = length3(n);
+    ++m;
+    for (int ax = 0; ax < 3; ++ax) sq[ax].add(q[ax]);
+    if (!(len > T(0))) continue;
+    T nn[3] = {n.x / len, n.y / len, n.z / len};
+    T d = (nn[0] * q[0] + nn[1] * q[1]) + nn[2] * q[2];
+    sA[0].add(nn[0] * nn[0]); sA[1].add(nn[0] * nn[1]); sA[2].add(nn[0] * nn[2]);
+    sA[3].add(nn[1] * nn[1]); sA[4].add(nn[1] * nn[2]); sA[5].add(nn[2] * nn[2]);
+    for (int ax = 0; ax < 3; ++ax) sb[ax].add(nn[ax] * d);
+  }
+  CellOut<T> o;
+  o.signs = uint8_t((c[1] > T(0) ? 1 : 0) | (c[2] > T(0) ? 2 : 0) | (c[4] > T(0) ? 4 : 0) | (c[0] > T(0) ? 8 : 0));
+  o.has_vertex = m > 0;
+  if (!o.has_vertex) return o;
+  double A[6], bb[3], cc[3], xs[3];
+  for (int i = 0; i < 6; ++i) A[i] = double(sA[i].value());
+  for (int ax = 0; ax < 3; ++ax) {
+    bb[ax] = double(sb[ax].value());
+    cc[ax] = double(sq[ax].value()) / double(m);
+  }
+  qef_solve(A, bb, cc, xs);
+  for (int ax = 0; ax < 3; ++ax) o.pos[ax] = T(double(lo[ax]) + double(j.size[ax]) * xs[ax]);
+  V3<T> n = tetra_normal(f, V3<T>{o.pos[0], o.pos[1], o.pos[2]}, j.eps);
+  T len = length3(n);
+  o.nrm[0] = n.x / len;
+  o.nrm[1] = n.y / len;
+  o.nrm[2] = n.z / len;
+  return o;
+}
+
 struct Item {
   uint16_t x, y, z;
   uint8_t signs;
@@ -348,6 +500,7 @@ int run(int kind, const float *sp, int ns, const oracle_params *pp, oracle_mesh 
   Job<T> j = make_job<T>(pp->resolution, pp->bounds, pp->eps);
   const int N = j.N;
   const bool lag = pp->flags & ORACLE_FLAG_SLICE_LAG;
+  const bool qef = pp->flags & ORACLE_FLAG_QEF;
   // main.rs:298-356: cells of slice z are labelled z; with the read-before-
   // submit lag, iteration z reads slice z-1, so only slices 0..N-2 surface,
   // labelled +1.
@@ -368,7 +521,7 @@ int run(int kind, const float *sp, int ns, const oracle_params *pp, oracle_mesh 
       rows[y].clear();
       rowx[y].clear();
       for (int x = 0; x < N; ++x) {
-        CellOut<T> c = eval_cell(j, f, x, y, z);
+        CellOut<T> c = qef ? eval_cell_qef(j, f, x, y, z) : eval_cell(j, f, x, y, z);
         if (c.has_vertex) {
           rows[y].push_back(c);
           rowx[y].push_back(x);

@@ -51,7 +51,12 @@ enum {
 enum { ORACLE_F32 = 0, ORACLE_F64 = 1 };
 
 enum {
-  ORACLE_FLAG_SLICE_LAG = 1  /* reproduce main.rs:324-355 (read-before-submit)      */
+  ORACLE_FLAG_SLICE_LAG = 1, /* reproduce main.rs:324-355 (read-before-submit)      */
+  ORACLE_FLAG_QEF = 2        /* precision mode: corners from the shared lattice, a
+                                QEF vertex (normal-equation sums with Neumaier
+                                compensation in the oracle's precision, 3x3 solve
+                                in binary64); not a reference rule: the reference
+                                places the mass point (dualcontour.wgsl:86-131) */
 };
 
 typedef struct {

@@ -106,6 +106,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_sdf_cuda_source": ([vp], ctypes.c_char_p),
             "s2m_sdf_op_counts": ([vp, dp, dp], i),
             "s2m_sdf_free": ([vp], None),
+            "s2m_sdf_eval_variant": ([vp, ctypes.c_char_p, sz, dp], i),
             "s2m_wgsl_remove_function": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)], i),
             "s2m_wgsl_rename_function": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                           ctypes.POINTER(vp)], i),
@@ -205,6 +206,13 @@ class CompiledSdf:
         fp, sfu = ctypes.c_double(), ctypes.c_double()
         load_library().s2m_sdf_op_counts(self._h, ctypes.byref(fp), ctypes.byref(sfu))
         return fp.value, sfu.value
+
+    def eval_variant(self):
+        """(name, ns per lattice point of each variant) chosen by the autotuner; name is 'untuned' before the first job."""
+        name = ctypes.create_string_buffer(64)
+        ns = (ctypes.c_double * 6)()
+        load_library().s2m_sdf_eval_variant(self._h, name, 64, ns)
+        return name.value.decode(), list(ns)
 
     def close(self):
         if self._h:

@@ -2592,7 +2592,9 @@ FrontendResult translate(const std::string &source, Lang lang, const std::string
         Parser(M, toks, Lang::WGSL).parse_module();
       }
     }
+    bool std_normal = false;
     if (!find_fn(M, "sdf3d_normal", 2)) {
+      std_normal = true;
       // The reference needs sdf3d_normal in scope (`use sdf3d::normal;`, or
       // appended for GLSL at shader.rs:87); supply the library one.
       std::vector<Tok> toks = lex(builtin_module_source("sdf3d::normal"), Lang::WGSL);
@@ -2631,6 +2633,25 @@ FrontendResult translate(const std::string &source, Lang lang, const std::string
     for (Func *f : order) E.function(f);
     E.out << "S2HD float s2m_user_sdf(float x, float y, float z) { return " << sdf->cname << "(s2mk(x, y, z)); }\n";
     E.out << "S2HD s2v3 s2m_user_normal(s2v3 p, float eps) { return " << nrm->cname << "(p, eps); }\n";
+    // The library's tetrahedral normal (as `use` inserts it, or supplied
+    // above): the kernels may then evaluate it as a loop over the four
+    // directions with the same arithmetic, one sdf3d call site instead of four.
+    if (!std_normal) {
+      auto squash = [](const std::string &t) {
+        std::string o;
+        for (char ch : t)
+          if (!std::isspace((unsigned char)ch)) o.push_back(ch);
+        return o;
+      };
+      std::string lib = builtin_module_source("sdf3d::normal");
+      size_t at = lib.find("fn sdf3d_normal(");
+      std::string fn = squash(lib.substr(at));
+      std::string src = squash(source);
+      size_t first = src.find("fnsdf3d_normal(");
+      std_normal = first != std::string::npos && src.find("fnsdf3d_normal(", first + 1) == std::string::npos &&
+                   src.compare(first, fn.size(), fn) == 0;
+    }
+    if (std_normal) E.out << "#define S2M_STD_NORMAL 1\n";
     r.cuda = E.out.str();
     for (auto &w : M.warnings) r.warnings.push_back(w);
     r.ok = true;

@@ -74,12 +74,27 @@ int device_sm_count() {
 
 }  // namespace
 
+// Evaluation-kernel variants compiled into every SDF module (the table in
+// s2m_dc_kernels.cuh): name, z-run length.
+struct EvalVariant {
+  const char *name;
+  int run;
+};
+constexpr EvalVariant kEvalVariants[] = {{"s2m_eval_b2r4", 4}, {"s2m_eval_b3r4", 4}, {"s2m_eval_b4r4", 4},
+                                         {"s2m_eval_b4r1", 1}, {"s2m_eval_b6r4", 4}, {"s2m_eval_b8r4", 4}};
+constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
+
 struct s2m_sdf {
   std::string user_cuda;
   double fp32_ops = 0, sfu_ops = 0;
   uint32_t flags = 0;
   cudaLibrary_t lib = nullptr;
-  cudaKernel_t k_eval = nullptr, k_cells = nullptr, k_vertices = nullptr;
+  cudaKernel_t k_eval[kNumEvalVariants] = {};
+  cudaKernel_t k_cells = nullptr, k_vertices = nullptr;
+  // autotuned evaluation variant (-1: not tuned yet) and its timings (ns per point)
+  mutable std::mutex tune_mu;
+  mutable int eval_variant = -1;
+  mutable double tune_ns[kNumEvalVariants] = {};
 };
 
 struct s2m_mesh {
@@ -161,8 +176,12 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
     set_err(err, errlen, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce));
     return ce == cudaErrorNoDevice || ce == cudaErrorInsufficientDriver ? S2M_E_NO_DEVICE : S2M_E_CUDA;
   }
-  if (cudaLibraryGetKernel(&s->k_eval, s->lib, "s2m_eval_planes") != cudaSuccess ||
-      cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess ||
+  for (int v = 0; v < kNumEvalVariants; ++v)
+    if (cudaLibraryGetKernel(&s->k_eval[v], s->lib, kEvalVariants[v].name) != cudaSuccess) {
+      set_err(err, errlen, std::string("kernel missing from the compiled module: ") + kEvalVariants[v].name);
+      return S2M_E_CUDA;
+    }
+  if (cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess ||
       cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
@@ -380,6 +399,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
 
   const long long pts = (long long)j.P * j.P;
   const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
+  const int ev = m->sdf->eval_variant >= 0 ? m->sdf->eval_variant : 0;
+  const int run = kEvalVariants[ev].run;
   for (int s = 0; s < m->nslabs; ++s) {
     int zc0 = s * m->D;
     int zc1 = std::min(m->nzc, zc0 + m->D);
@@ -388,9 +409,9 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     S2Job jj = j;
     float *ring = m->ring;
     void *eargs[] = {&jj, &ring, &k0, &nk};
-    dim3 eg(eval_blocks, unsigned((nk + S2_EVAL_RUN - 1) / S2_EVAL_RUN));
+    dim3 eg(eval_blocks, unsigned((nk + run - 1) / run));
     S2_LAUNCH(0, double(pts) * nk,
-              cudaLaunchKernel((const void *)m->sdf->k_eval, eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
+              cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
     if ((e = cudaMemsetAsync(m->slab_ctrl, 0, m->slab_ctrl_words * 8, st)) != cudaSuccess) return e;
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
     unsigned cg = unsigned((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
@@ -410,6 +431,61 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   const unsigned q_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->quad_tiles, size_t(sms) * 8)));
   S2_LAUNCH(5, 0, (s2m_quads<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, unsigned(m->scan_tiles)), cudaGetLastError()));
   return cudaSuccess;
+}
+
+// Autotuner: time every evaluation variant on the job's first planes (into
+// the job's own ring, which the pipeline overwrites afterwards) and keep the
+// fastest for this SDF.  Runs once per SDF, on its first job.
+int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
+  const s2m_sdf *sdf = m->sdf;
+  std::lock_guard<std::mutex> lock(sdf->tune_mu);
+  if (sdf->eval_variant >= 0) return S2M_OK;
+  if (std::getenv("S2M_EVAL_VARIANT")) {
+    int v = std::atoi(std::getenv("S2M_EVAL_VARIANT"));
+    sdf->eval_variant = (v >= 0 && v < kNumEvalVariants) ? v : 0;
+    return S2M_OK;
+  }
+  const S2Job &j = m->job;
+  const long long pts = (long long)j.P * j.P;
+  int nk = std::min(j.ring, 8);
+  // small jobs: too little work per launch to rank the variants; keep the default
+  if (double(pts) * nk < 2.0e6) {
+    sdf->eval_variant = 0;
+    return S2M_OK;
+  }
+  cudaEvent_t a, b;
+  S2_CUDA(cudaEventCreate(&a));
+  S2_CUDA(cudaEventCreate(&b));
+  const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
+  double best = 1e300;
+  int best_v = 0;
+  for (int v = 0; v < kNumEvalVariants; ++v) {
+    float ms_best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      S2Job jj = j;
+      float *ring = m->ring;
+      int k0 = 0;
+      void *args[] = {&jj, &ring, &k0, &nk};
+      dim3 eg(eval_blocks, unsigned((nk + kEvalVariants[v].run - 1) / kEvalVariants[v].run));
+      S2_CUDA(cudaEventRecord(a, st));
+      S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], eg, dim3(S2_EVAL_BLOCK), args, 0, st));
+      S2_CUDA(cudaEventRecord(b, st));
+      S2_CUDA(cudaEventSynchronize(b));
+      float ms = 0;
+      S2_CUDA(cudaEventElapsedTime(&ms, a, b));
+      if (rep > 0) ms_best = std::min(ms_best, ms);
+    }
+    double ns = double(ms_best) * 1e6 / (double(pts) * nk);
+    sdf->tune_ns[v] = ns;
+    if (ns < best) {
+      best = ns;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  sdf->eval_variant = best_v;
+  return S2M_OK;
 }
 
 int readback(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
@@ -537,6 +613,15 @@ int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t 
 
 const char *s2m_sdf_cuda_source(const s2m_sdf *sdf) { return sdf ? sdf->user_cuda.c_str() : nullptr; }
 
+int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point) {
+  if (!sdf) return S2M_E_INVALID;
+  int v = sdf->eval_variant;
+  if (name && namelen) set_err(name, namelen, v >= 0 ? kEvalVariants[v].name : "untuned");
+  if (ns_per_point)
+    for (int i = 0; i < kNumEvalVariants; ++i) ns_per_point[i] = sdf->tune_ns[i];
+  return v;
+}
+
 int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
   if (!sdf) return S2M_E_INVALID;
   if (fp32_ops) *fp32_ops = sdf->fp32_ops;
@@ -621,6 +706,7 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
   for (int attempt = 0; attempt < 5; ++attempt) {
     rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen);
     if (rc != S2M_OK) break;
+    if (m->sdf->eval_variant < 0 && (rc = autotune_eval(m, st, err, errlen)) != S2M_OK) break;
     cudaError_t e = enqueue(m, st);
     if (e != cudaSuccess) {
       set_err(err, errlen, std::string("launch: ") + cudaGetErrorString(e));

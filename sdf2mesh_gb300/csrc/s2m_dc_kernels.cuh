@@ -24,23 +24,39 @@ __device__ __forceinline__ unsigned s2_off_lattice(const S2Job &j, int i) {
 }
 
 // Evaluate planes k0 .. k0 + nk - 1 of the lattice into the ring.
-// grid.x covers the P * P points of a plane, grid.y runs of S2_EVAL_RUN planes.
-extern "C" __global__ void __launch_bounds__(S2_EVAL_BLOCK)
-s2m_eval_planes(S2Job job, float *__restrict__ ring, int k0, int nk) {
+// grid.x covers the P * P points of a plane, grid.y runs of RUN planes; each
+// thread walks its run along z.  The variants below differ only in RUN and in
+// the occupancy the compiler must allow (__launch_bounds__ minimum blocks),
+// which trades registers against latency hiding; the runtime's autotuner
+// times them per SDF and keeps the fastest.
+template <int RUN>
+__device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restrict__ ring, int k0, int nk) {
   long long idx = (long long)blockIdx.x * S2_EVAL_BLOCK + threadIdx.x;
   long long pts = (long long)job.P * job.P;
   if (idx >= pts) return;
   int i = (int)(idx % job.P);
   int jy = (int)(idx / job.P);
   float x = s2_coord(job, i), y = s2_coord(job, jy);
-  int kb = k0 + (int)blockIdx.y * S2_EVAL_RUN;
-  int ke = min(kb + S2_EVAL_RUN, k0 + nk);
+  int kb = k0 + (int)blockIdx.y * RUN;
+  int ke = min(kb + RUN, k0 + nk);
   long long row = (long long)jy * job.pitch + i;
+#pragma unroll 1
   for (int k = kb; k < ke; ++k) {
     float z = s2_coord(job, k);
     ring[(long long)(k % job.ring) * job.plane + row] = s2m_user_sdf(x, y, z);
   }
 }
+
+#define S2_EVAL_VARIANT(NAME, MINB, RUN)                                                          \
+  extern "C" __global__ void __launch_bounds__(S2_EVAL_BLOCK, MINB)                               \
+  NAME(S2Job job, float *__restrict__ ring, int k0, int nk) { s2_eval_planes<RUN>(job, ring, k0, nk); }
+// Keep this table in step with kEvalVariants in runtime.cu.
+S2_EVAL_VARIANT(s2m_eval_b2r4, 2, 4)
+S2_EVAL_VARIANT(s2m_eval_b3r4, 3, 4)
+S2_EVAL_VARIANT(s2m_eval_b4r4, 4, 4)
+S2_EVAL_VARIANT(s2m_eval_b4r1, 4, 1)
+S2_EVAL_VARIANT(s2m_eval_b6r4, 6, 4)
+S2_EVAL_VARIANT(s2m_eval_b8r4, 8, 4)
 
 struct S2Cell {
   int x, y, z;
@@ -106,9 +122,18 @@ __device__ __forceinline__ unsigned long long s2_vertex(const S2Job &j, S2Cell c
                                                         float nrm[3]) {
   float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
   float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
-  unsigned off = s2_off_mask(j, c);
-  for (int k = 1; k < 8; ++k)
-    if ((off >> k) & 1u) v[k] = s2m_user_sdf((k & 1) ? mx[0] : mn[0], (k & 2) ? mx[1] : mn[1], (k & 4) ? mx[2] : mn[2]);
+  // Off-lattice corners, one sdf3d call site in a loop (a warp runs the
+  // largest count among its lanes instead of every inlined copy).
+  unsigned off = s2_off_mask(j, c) & 0xfeu;
+#pragma unroll 1
+  while (off) {
+    const int k = __ffs(off) - 1;
+    off &= off - 1u;
+    const float f = s2m_user_sdf((k & 1) ? mx[0] : mn[0], (k & 2) ? mx[1] : mn[1], (k & 4) ? mx[2] : mn[2]);
+#pragma unroll
+    for (int q = 1; q < 8; ++q)
+      if (q == k) v[q] = f;
+  }
 
   // 12 edges in the reference order: 4 along z, 4 along y, 4 along x.
   // Each: corner a, corner b, axis of t, the two fixed local coordinates.
@@ -146,7 +171,27 @@ __device__ __forceinline__ unsigned long long s2_vertex(const S2Job &j, S2Cell c
     float bsize = __fsub_rn(mx[a], mn[a]);
     pos[a] = __fadd_rn(mn[a], __fdiv_rn(__fmul_rn(bsize, avg[a]), count));
   }
+#ifdef S2M_STD_NORMAL
+  // sdf3d_normal.wgsl:4-10 as a loop: n = ((t0 + t1) + t2) + t3 with
+  // t_i = d_i * sdf3d(p + d_i * eps), the order the library function adds in.
+  s2v3 n;
+#pragma unroll 1
+  for (int i = 0; i < 4; ++i) {
+    const float dx = (i == 0 || i == 3) ? 1.0f : -1.0f;
+    const float dy = (i >= 2) ? 1.0f : -1.0f;
+    const float dz = (i == 1 || i == 3) ? 1.0f : -1.0f;
+    const float f = s2m_user_sdf(__fadd_rn(pos[0], __fmul_rn(dx, j.eps)), __fadd_rn(pos[1], __fmul_rn(dy, j.eps)),
+                                 __fadd_rn(pos[2], __fmul_rn(dz, j.eps)));
+    const float tx = __fmul_rn(dx, f), ty = __fmul_rn(dy, f), tz = __fmul_rn(dz, f);
+    if (i == 0) {
+      n.x = tx; n.y = ty; n.z = tz;
+    } else {
+      n.x = __fadd_rn(n.x, tx); n.y = __fadd_rn(n.y, ty); n.z = __fadd_rn(n.z, tz);
+    }
+  }
+#else
   s2v3 n = s2m_user_normal(s2mk(pos[0], pos[1], pos[2]), j.eps);
+#endif
   float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(n.x, n.x), __fmul_rn(n.y, n.y)), __fmul_rn(n.z, n.z)));
   nrm[0] = __fdiv_rn(n.x, len);
   nrm[1] = __fdiv_rn(n.y, len);

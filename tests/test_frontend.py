@@ -191,3 +191,17 @@ def test_text_helpers_errors(lib):
         s2m.wgsl_remove_function("fn a() {}\n", "fn b(")
     assert s2m.wgsl_has_function("  fn sdf3d(p: vec3f) -> f32 {}", "sdf3d")
     assert not s2m.wgsl_has_function("fn sdf3dx(p: vec3f) -> f32 {}", "sdf3d")
+
+
+def test_standard_normal_marker(lib):
+    """The library normal (inserted by `use` or supplied) is marked so the
+    kernels may loop over its four directions; a user-defined one is not."""
+    src, _ = workloads.torus()
+    assert "S2M_STD_NORMAL" in lower(src)[0]
+    custom = ("use sdf3d::primitives;\n"
+              "fn sdf3d_normal(p: vec3f, eps: f32) -> vec3f {\n"
+              "  let h = vec3f(eps, 0.0, 0.0);\n"
+              "  return vec3f(sdf3d(p + h.xyy) - sdf3d(p - h.xyy), sdf3d(p + h.yxy) - sdf3d(p - h.yxy),\n"
+              "               sdf3d(p + h.yyx) - sdf3d(p - h.yyx));\n}\n"
+              "fn sdf3d(p: vec3f) -> f32 { return sdf3d_sphere(p, 0.5); }\n")
+    assert "S2M_STD_NORMAL" not in lower(custom)[0]

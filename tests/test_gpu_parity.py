@@ -188,3 +188,41 @@ def test_csg64_1024_full_size(lib, oracle_lib):
     assert (np.diff(k.astype(np.int64)) > 0).all()
     for zz in sorted(set(int(v) for v in missing[:, 2]))[:4]:
         window_matches(max(0, zz - 1), min(N, zz + 2))
+
+
+def test_custom_normal_function(lib, oracle_lib):
+    """A user-defined sdf3d_normal is what the kernel calls (dualcontour.wgsl:170):
+    positions still match the oracle bit for bit, normals are the custom
+    central difference, normalised."""
+    custom = ("use sdf3d::primitives;\n"
+              "fn sdf3d_normal(p: vec3f, eps: f32) -> vec3f {\n"
+              "  let h = vec3f(eps, 0.0, 0.0);\n"
+              "  return vec3f(sdf3d(p + h.xyy) - sdf3d(p - h.xyy), sdf3d(p + h.yxy) - sdf3d(p - h.yxy),\n"
+              "               sdf3d(p + h.yyx) - sdf3d(p - h.yyx));\n}\n"
+              "fn sdf3d(p: vec3f) -> f32 { return sdf3d_sphere(p, 0.5); }\n")
+    gpu = run(s2m.Sdf3DShader.from_source(custom).compile(), 48)
+    ref = oracle.mesh(oracle.SPHERE, [0.5], 48, 2.0)
+    assert np.array_equal(gpu.cell_xyz, ref.cell)
+    assert np.array_equal(gpu.positions.view(np.uint32), ref.pos.astype(np.float32).view(np.uint32))
+    radial = ref.pos / np.linalg.norm(ref.pos, axis=1, keepdims=True)
+    assert (np.sum(gpu.normals * radial, axis=1) > 0.999).all()
+
+
+@pytest.mark.parametrize("variant", range(6))
+def test_eval_variants_identical(lib, variant, monkeypatch):
+    """Every evaluation-kernel variant the autotuner may pick gives the same bits."""
+    src, prm = workloads.csg64(seed=1)
+    monkeypatch.setenv("S2M_EVAL_VARIANT", str(variant))
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    gpu = run(sdf, 96)
+    assert sdf.eval_variant()[0] != "untuned"
+    assert_bit_exact(gpu, oracle.mesh(oracle.CSG, prm, 96, 2.0), f"variant {variant}")
+
+
+def test_autotuner_picks_a_variant(lib):
+    src, _ = workloads.csg64(seed=0)
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    assert sdf.eval_variant()[0] == "untuned"
+    run(sdf, 512)  # large enough for the tuner to time (>= 2e6 points per trial)
+    name, ns = sdf.eval_variant()
+    assert name.startswith("s2m_eval_") and all(x > 0 for x in ns)
