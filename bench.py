@@ -41,7 +41,6 @@ N_FULL = 1024
 BOUNDS = 2.0
 METRIC = "Gvoxels/s at 1024^3"
 UNIT = "Gvoxels/s"
-WORKLOAD = "csg64_1024"
 CPU_SAMPLE_SLICES = 16     # cpu_baseline: cell slices [504, 520) of the 1024^3 job
 REF_STEP_SLICES = 4        # --impl reference: cell slices per step
 CPU_Z0 = 504
@@ -53,7 +52,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--resolution", type=int, default=N_FULL)
+    ap.add_argument("--resolution", type=int, default=None)
+    ap.add_argument("--workload", default="csg64_1024", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -65,9 +65,25 @@ def dist_env():
     return ws, rank, local
 
 
+# name -> (resolution, bounds, precision mode, description)
+WORKLOADS = {
+    "csg64_1024": (1024, 2.0, False, "rounded box - smooth union (k=0.02) of 64 spheres (splitmix64 seed 0) + torus"),
+    "mandelbulb_2048": (2048, 2.5, True, "Mandelbulb power 8, 8 iterations, bailout 2 (GLSL), precision mode: "
+                                         "QEF vertex, FP32 compensated sums, FP64 solve"),
+}
+_ACTIVE = {"name": "csg64_1024"}
+
+
 def workload():
     from sdf2mesh_gb300 import workloads
+    if _ACTIVE["name"] == "mandelbulb_2048":
+        return workloads.mandelbulb(8.0, 8, 2.0, 0.003)
     return workloads.csg64(seed=0)
+
+
+def oracle_kind():
+    import oracle
+    return oracle.MANDELBULB if _ACTIVE["name"] == "mandelbulb_2048" else oracle.CSG
 
 
 def cpu_sample(n_slices, z0, resolution, threads=0):
@@ -75,7 +91,8 @@ def cpu_sample(n_slices, z0, resolution, threads=0):
     import oracle
     _, prm = workload()
     t = time.perf_counter()
-    m = oracle.mesh(oracle.CSG, prm, resolution, BOUNDS, z_begin=z0, z_end=z0 + n_slices, threads=threads)
+    _, bounds, qef, _ = WORKLOADS[_ACTIVE["name"]]
+    m = oracle.mesh(oracle_kind(), prm, resolution, bounds, z_begin=z0, z_end=z0 + n_slices, threads=threads, qef=qef)
     dt = time.perf_counter() - t
     return dt, m
 
@@ -110,7 +127,8 @@ def reference_arm(a):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": tot / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "resolution": N, "bounds": BOUNDS, "sdf": "csg64 seed 0",
+        "config": {"workload": _ACTIVE["name"], "resolution": N, "bounds": WORKLOADS[_ACTIVE["name"]][1],
+                   "sdf": WORKLOADS[_ACTIVE["name"]][3],
                    "implementation": "CPU oracle: C++ restatement of the reference rule, OpenMP"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": host_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -198,13 +216,15 @@ def ours(a):
     N = a.resolution
     src, _ = workload()
     t0 = time.perf_counter()
-    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    _, bounds, qef, desc = WORKLOADS[a.workload]
+    lang = s2m.LANG_GLSL if a.workload.startswith("mandelbulb") else s2m.LANG_WGSL
+    sdf = s2m.Sdf3DShader.from_source(src, lang, "sdf").compile()
     compile_s = time.perf_counter() - t0
     fp32_ops, sfu_ops = sdf.op_counts()
 
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
-    state = s2m.AppState(resolution=N, bounds=BOUNDS)
+    state = s2m.AppState(resolution=N, bounds=bounds, qef=qef)
     mesh = s2m.mesh_device(sdf, state, sp)
     info = mesh.info()
     nverts, ntris = int(info.nverts), int(info.ntris)
@@ -337,22 +357,23 @@ def ours(a):
 
     cpu = None
     if not a.no_cpu_baseline:
-        n = min(CPU_SAMPLE_SLICES, N)
+        n = min(CPU_SAMPLE_SLICES if a.workload == "csg64_1024" else 4, N)
         z0 = max(0, min(CPU_Z0, N - n))
         dt, _ = cpu_sample(n, z0, N)
         cpu = {"value": n * N * N / dt / 1e9, "unit": UNIT, "cores": host_threads(), "kind": "port",
                "sample": f"CPU oracle (reference rule, binary32, OpenMP) on cell slices [{z0}, {z0 + n}) "
                          f"of the {N}^3 job: {n * N * N} voxels in {dt:.2f} s"}
 
+    metric = METRIC if a.workload == "csg64_1024" and N == 1024 else f"Gvoxels/s at {N}^3 ({a.workload})"
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": tot_ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "resolution": N, "bounds": BOUNDS,
-                   "sdf": "rounded box - smooth union (k=0.02) of 64 spheres (splitmix64 seed 0) + torus",
+        "config": {"workload": a.workload, "resolution": N, "bounds": bounds, "sdf": desc,
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
-                   "precision": "reference rule in binary32, no FMA contraction, IEEE div/sqrt"},
+                   "precision": ("precision mode: lattice corners, QEF vertex, FP32 compensated sums, FP64 solve"
+                                 if qef else "reference rule in binary32, no FMA contraction, IEEE div/sqrt")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_tot / a.steps,
                 "path": "s2m_mesh_create + s2m_mesh_copy_to_host (pinned) + s2m_mesh_free; inputs are the "
@@ -380,6 +401,9 @@ def ours(a):
 
 def main():
     a = parse()
+    _ACTIVE["name"] = a.workload
+    if a.resolution is None:
+        a.resolution = WORKLOADS[a.workload][0]
     if a.impl == "reference":
         reference_arm(a)
     else:

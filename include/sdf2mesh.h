@@ -57,6 +57,11 @@ typedef enum { S2M_LANG_WGSL = 0, S2M_LANG_GLSL = 1 } s2m_lang;
                                        0..N-2 are emitted, labelled z+1             */
 #define S2M_JOB_EXACT_CORNERS 0x4u  /* re-evaluate every off-lattice corner of every
                                        cell (verification mode; slower)             */
+#define S2M_JOB_QEF 0x8u            /* precision mode (no reference counterpart; the
+                                       reference places the mass point,
+                                       dualcontour.wgsl:86-131): corners from the
+                                       shared lattice, a QEF vertex from the crossing
+                                       normals, FP32 compensated sums, FP64 solve  */
 
 typedef struct s2m_sdf s2m_sdf;
 typedef struct s2m_mesh s2m_mesh;
@@ -183,6 +188,45 @@ typedef struct {
 int s2m_mesh_set_profiling(s2m_mesh *mesh, int enable);
 int s2m_mesh_get_profile(const s2m_mesh *mesh, s2m_profile *out);
 int s2m_mesh_reset_profile(s2m_mesh *mesh);
+
+/* ---- batching: many jobs in one persistent launch -----------------------
+   No reference counterpart (the reference meshes one SDF per process run).
+   A batch job is a CSG program: a postfix list of floats, each opcode
+   followed by its operands, evaluated on the device by an interpreter whose
+   arithmetic is that of the library function of the same name
+   (src/sdf3d_primitives.wgsl:7-36, src/sdf_op.wgsl:7-23), so no per-job
+   compilation is needed.  Operands:
+     SPHERE cx cy cz r            sdf3d_sphere(p - c, r)
+     BOX cx cy cz bx by bz        sdf3d_box(p - c, b)            (full size b)
+     TORUS cx cy cz R r           sdf3d_torus(p - c, vec2(R, r))
+     CAPSULE ax ay az bx by bz r  sdf3d_capsule(p, a, b, r)
+     PLANE nx ny nz d             dot(p, n) - d
+     UNION / SUBTRACT / INTERSECT  min(a, b) / max(a, -b) / max(a, b)
+     SMOOTH_UNION k, SMOOTH_INTERSECTION k, SMOOTH_SUBTRACTION k
+                                   sdf_op_smooth_*(a, b, k)
+   s2m_batch_run meshes every job added since the last run in one launch of
+   a persistent kernel over a device work queue (waves of at most
+   memory_budget_bytes of device memory; 0 = no limit).  Job results stay on
+   the device until s2m_batch_free. */
+enum {
+  S2M_CSG_SPHERE = 0, S2M_CSG_BOX = 1, S2M_CSG_TORUS = 2, S2M_CSG_CAPSULE = 3, S2M_CSG_PLANE = 4,
+  S2M_CSG_UNION = 10, S2M_CSG_SUBTRACT = 11, S2M_CSG_INTERSECT = 12, S2M_CSG_SMOOTH_UNION = 13,
+  S2M_CSG_SMOOTH_INTERSECTION = 14, S2M_CSG_SMOOTH_SUBTRACTION = 15
+};
+typedef struct s2m_batch s2m_batch;
+int s2m_batch_create(s2m_batch **out, uint64_t memory_budget_bytes);
+int s2m_batch_add_csg(s2m_batch *b, const float *program, uint32_t len, const s2m_params *params,
+                      uint32_t *job_id, char *err, size_t errlen);
+/* Device bytes the job needs while it runs (lattice, candidates, mesh). */
+uint64_t s2m_batch_job_footprint(const s2m_batch *b, uint32_t job);
+/* Synchronises `stream`. */
+int s2m_batch_run(s2m_batch *b, void *stream, char *err, size_t errlen);
+int s2m_batch_job_info(const s2m_batch *b, uint32_t job, s2m_mesh_info *info);
+int s2m_batch_job_copy_to_host(const s2m_batch *b, uint32_t job, float *pos, float *nrm, uint64_t *cell,
+                               uint32_t *tris, void *stream);
+/* Device time of the last run's persistent launches, their count, jobs in the batch. */
+int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, uint32_t *njobs);
+void s2m_batch_free(s2m_batch *b);
 
 /* ---- host writers (mesh.rs:8-141) -------------------------------------- */
 

@@ -77,6 +77,16 @@ template <class T> T op_smooth_union(T d1, T d2, T k) {
   T h = clampT(T(0.5) + T(0.5) * (d2 - d1) / k, T(0), T(1));
   return mixT(d2, d1, h) - k * h * (T(1) - h);
 }
+// sdf_op.wgsl:13-17
+template <class T> T op_smooth_intersection(T d1, T d2, T k) {
+  T h = clampT(T(0.5) - T(0.5) * (d2 - d1) / k, T(0), T(1));
+  return mixT(d2, d1, h) + k * h * (T(1) - h);
+}
+// sdf_op.wgsl:19-23
+template <class T> T op_smooth_subtraction(T d1, T d2, T k) {
+  T h = clampT(T(0.5) - T(0.5) * (d2 + d1) / k, T(0), T(1));
+  return mixT(d2, -d1, h) + k * h * (T(1) - h);
+}
 
 // ---------------------------------------------------------------------------
 // Fixture SDFs.  Parameters arrive as f32 (exactly what a .sdf3d literal
@@ -150,6 +160,7 @@ template <class T> struct Sdf {
   //  11 subtract(a b -> max(a, -b))
   //  12 intersect (a b -> max(a, b))
   //  13 smooth-union k (a b -> sdf_op_smooth_union(a, b, k))
+  //  14 smooth-intersection k, 15 smooth-subtraction k (sdf_op.wgsl:13-23)
   T tree(V3<T> p) const {
     T stack[64];
     int sp = 0;
@@ -167,6 +178,8 @@ template <class T> struct Sdf {
         case 11: { T b = stack[--sp]; stack[sp - 1] = m_max(stack[sp - 1], -b); } break;
         case 12: { T b = stack[--sp]; stack[sp - 1] = m_max(stack[sp - 1], b); } break;
         case 13: { T b = stack[--sp]; stack[sp - 1] = op_smooth_union(stack[sp - 1], b, a[0]); i += 1; } break;
+        case 14: { T b = stack[--sp]; stack[sp - 1] = op_smooth_intersection(stack[sp - 1], b, a[0]); i += 1; } break;
+        case 15: { T b = stack[--sp]; stack[sp - 1] = op_smooth_subtraction(stack[sp - 1], b, a[0]); i += 1; } break;
         default: return T(NAN);
       }
     }

@@ -25,9 +25,9 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = [
-    "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate",
+    "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate", "Batch",
     "load_library", "translate", "wgsl_remove_function", "wgsl_rename_function", "wgsl_has_function",
-    "LANG_WGSL", "LANG_GLSL", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "COMPILE_FMAD",
+    "LANG_WGSL", "LANG_GLSL", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "JOB_QEF", "COMPILE_FMAD",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -35,7 +35,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libsdf2mesh_gb300.so")
 
 LANG_WGSL, LANG_GLSL = 0, 1
 COMPILE_FMAD = 0x1
-JOB_POW2_ROUNDING, JOB_SLICE_LAG, JOB_EXACT_CORNERS = 0x1, 0x2, 0x4
+JOB_POW2_ROUNDING, JOB_SLICE_LAG, JOB_EXACT_CORNERS, JOB_QEF = 0x1, 0x2, 0x4, 0x8
 
 S2M_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "IO", 3: "PARSE", 4: "MISSING_SDF", 5: "NVRTC", 6: "CUDA",
@@ -122,6 +122,15 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_write_ply": ([vp, vp, u64, vp, u64, ctypes.c_char_p], i),
             "s2m_measure_fp32_peak": ([dp, vp], i),
             "s2m_mesh_set_profiling": ([vp, i], i),
+            "s2m_batch_create": ([ctypes.POINTER(vp), u64], i),
+            "s2m_batch_add_csg": ([vp, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(Params),
+                                   ctypes.POINTER(u32), ctypes.c_char_p, sz], i),
+            "s2m_batch_job_footprint": ([vp, u32], u64),
+            "s2m_batch_run": ([vp, vp, ctypes.c_char_p, sz], i),
+            "s2m_batch_job_info": ([vp, u32, ctypes.POINTER(MeshInfo)], i),
+            "s2m_batch_job_copy_to_host": ([vp, u32, vp, vp, vp, vp, vp], i),
+            "s2m_batch_stats": ([vp, dp, ctypes.POINTER(u64), ctypes.POINTER(u32)], i),
+            "s2m_batch_free": ([vp], None),
             "s2m_mesh_get_profile": ([vp, ctypes.POINTER(Profile)], i),
             "s2m_mesh_reset_profile": ([vp], i),
         }
@@ -289,6 +298,7 @@ class AppState:
     reference_rounding: bool = False
     slice_lag: bool = False
     exact_corners: bool = False
+    qef: bool = False
     slab_depth: int = 0
     max_vertices: int = 0
     max_triangles: int = 0
@@ -302,7 +312,7 @@ class AppState:
 
     def params(self) -> Params:
         flags = ((JOB_POW2_ROUNDING if self.reference_rounding else 0) | (JOB_SLICE_LAG if self.slice_lag else 0)
-                 | (JOB_EXACT_CORNERS if self.exact_corners else 0))
+                 | (JOB_EXACT_CORNERS if self.exact_corners else 0) | (JOB_QEF if self.qef else 0))
         return Params(self.resolution, self.bounds, self.eps, flags, self.slab_depth, 0, self.max_vertices,
                       self.max_triangles)
 
@@ -414,6 +424,70 @@ class TriangleMesh:
             self.write_ply_to_file(path)
         else:
             raise S2MError(1, f"Unknown file extension: {ext}")
+
+
+class Batch:
+    """Many CSG jobs meshed in one persistent launch (s2m_batch_*).
+
+    A job is a CSG program: a postfix list of floats, opcodes S2M_CSG_* each
+    followed by its operands (see include/sdf2mesh.h); `workloads.random_tree`
+    returns one beside the equivalent .sdf3d source."""
+
+    def __init__(self, memory_budget_bytes: int = 0):
+        self._h = ctypes.c_void_p()
+        _check(load_library().s2m_batch_create(ctypes.byref(self._h), memory_budget_bytes), None, "batch")
+        self.njobs = 0
+
+    def add_csg(self, program, state: AppState) -> int:
+        prog = np.ascontiguousarray(np.asarray(program, np.float32))
+        p = state.params()
+        jid = ctypes.c_uint32()
+        err = _errbuf()
+        rc = load_library().s2m_batch_add_csg(self._h, prog.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                              len(prog), ctypes.byref(p), ctypes.byref(jid), err, len(err))
+        _check(rc, err, "batch add")
+        self.njobs += 1
+        return int(jid.value)
+
+    def footprint(self, job: int) -> int:
+        return int(load_library().s2m_batch_job_footprint(self._h, job))
+
+    def run(self, stream: int = 0) -> None:
+        err = _errbuf()
+        _check(load_library().s2m_batch_run(self._h, ctypes.c_void_p(stream), err, len(err)), err, "batch run")
+
+    def info(self, job: int) -> MeshInfo:
+        mi = MeshInfo()
+        _check(load_library().s2m_batch_job_info(self._h, job, ctypes.byref(mi)), None, "batch info")
+        return mi
+
+    def mesh(self, job: int, stream: int = 0) -> "TriangleMesh":
+        mi = self.info(job)
+        nv, nt = int(mi.nverts), int(mi.ntris)
+        pos = np.empty((nv, 3), np.float32)
+        nrm = np.empty((nv, 3), np.float32)
+        cell = np.empty(nv, np.uint64)
+        tris = np.empty((nt, 3), np.uint32)
+        _check(load_library().s2m_batch_job_copy_to_host(self._h, job, pos.ctypes.data, nrm.ctypes.data,
+                                                          cell.ctypes.data, tris.ctypes.data,
+                                                          ctypes.c_void_p(stream)), None, "batch copy")
+        return TriangleMesh(pos, nrm, tris, cell, int(mi.invalid_quads), mi)
+
+    def stats(self):
+        ms, launches, n = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_uint32()
+        load_library().s2m_batch_stats(self._h, ctypes.byref(ms), ctypes.byref(launches), ctypes.byref(n))
+        return ms.value, int(launches.value), int(n.value)
+
+    def close(self):
+        if self._h:
+            load_library().s2m_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def mesh_device(sdf, state: AppState, stream: int = 0) -> DeviceMesh:

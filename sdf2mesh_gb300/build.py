@@ -32,11 +32,12 @@ EMBEDDED = [
     ("kS2mDeviceH", "s2m_device.h"),
     ("kS2mLookbackCuh", "s2m_lookback.cuh"),
     ("kS2mPreludeCuh", "s2m_prelude.cuh"),
+    ("kS2mDcCoreCuh", "s2m_dc_core.cuh"),
     ("kS2mDcKernelsCuh", "s2m_dc_kernels.cuh"),
 ]
-SOURCES = ["runtime.cu", "frontend.cpp", "frontend_lib.cpp", "mesh_io.cpp"]
+SOURCES = ["runtime.cu", "batch.cu", "frontend.cpp", "frontend_lib.cpp", "mesh_io.cpp"]
 HEADERS = ["frontend.h", "mesh_io.h", "static_kernels.cuh", "s2m_device.h", "s2m_lookback.cuh",
-           "s2m_prelude.cuh", "s2m_dc_kernels.cuh"]
+           "s2m_prelude.cuh", "s2m_dc_core.cuh", "s2m_dc_kernels.cuh", "s2m_workers.cuh"]
 
 
 def _mtime(p):

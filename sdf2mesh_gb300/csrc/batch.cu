@@ -1,0 +1,846 @@
+// batch.cu -- many meshing jobs in one persistent launch.
+//
+// A batch job is a CSG program (a postfix list of the library's primitives
+// and operators, evaluated by an interpreter on the device, so no per-job
+// compilation) plus its own resolution and bounds.  All jobs of a batch run
+// in ONE launch of s2m_batch_kernel: its blocks take tickets from a device
+// work queue in which every job contributes six stages in order --
+//   E evaluate the job's lattice, C classify cells (ordered candidate list),
+//   X place vertices, V compact vertices, R scan row starts, Q emit quads --
+// each stage a run of items.  A block that takes an item of stage s of a job
+// first waits until every item of stage s-1 of that job is done.  Those items
+// hold lower tickets, so they were taken by blocks already running: the wait
+// always ends (it is still bounded, and a block that gives up raises an error
+// flag instead of hanging).  Jobs overlap on the device: while the last items
+// of one job's stage finish, blocks already work on the next jobs.
+//
+// The dual-contouring rule is the one of the per-job pipeline
+// (s2m_dc_core.cuh, s2m_workers.cuh): the reference's mass point or the
+// precision-mode QEF, bit-identical to the per-job path for the same SDF.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sdf2mesh.h"
+#include "s2m_device.h"
+#include "s2m_lookback.cuh"
+#include "s2m_dc_core.cuh"
+#include "s2m_workers.cuh"
+
+// ---------------------------------------------------------------------------
+// CSG program interpreter.  Opcodes and operands are floats; the arithmetic of
+// each opcode is that of the library function it names
+// (src/sdf3d_primitives.wgsl:7-36, src/sdf_op.wgsl:7-23), operation for
+// operation, so a program and the equivalent .sdf3d source give the same bits.
+
+#define S2_CSG_STACK 32
+
+struct S2CsgSdf {
+  const float *prog;
+  int len;
+
+  __device__ __forceinline__ static float len3(float x, float y, float z) {
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+  }
+  __device__ __forceinline__ static float len2(float x, float y) {
+    return __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
+  }
+  __device__ __forceinline__ static float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+  // mix(e1, e2, t) = e1 * (1 - t) + e2 * t
+  __device__ __forceinline__ static float mix(float a, float b, float t) {
+    return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
+  }
+
+  __device__ float operator()(float x, float y, float z) const {
+    float st[S2_CSG_STACK];
+    int sp = 0;
+    int i = 0;
+    while (i < len) {
+      const int op = (int)__ldg(prog + i);
+      const float *a = prog + i + 1;
+      switch (op) {
+        case S2M_CSG_SPHERE: {  // sdf3d_sphere(p - c, r)
+          const float dx = __fsub_rn(x, __ldg(a)), dy = __fsub_rn(y, __ldg(a + 1)), dz = __fsub_rn(z, __ldg(a + 2));
+          st[sp++] = __fsub_rn(len3(dx, dy, dz), __ldg(a + 3));
+          i += 5;
+          break;
+        }
+        case S2M_CSG_BOX: {  // sdf3d_box(p - c, b), b the full size
+          const float qx = __fsub_rn(fabsf(__fsub_rn(x, __ldg(a))), __fmul_rn(0.5f, __ldg(a + 3)));
+          const float qy = __fsub_rn(fabsf(__fsub_rn(y, __ldg(a + 1))), __fmul_rn(0.5f, __ldg(a + 4)));
+          const float qz = __fsub_rn(fabsf(__fsub_rn(z, __ldg(a + 2))), __fmul_rn(0.5f, __ldg(a + 5)));
+          const float outside = len3(fmaxf(qx, 0.0f), fmaxf(qy, 0.0f), fmaxf(qz, 0.0f));
+          st[sp++] = __fadd_rn(outside, fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f));
+          i += 7;
+          break;
+        }
+        case S2M_CSG_TORUS: {  // sdf3d_torus(p - c, vec2(R, r))
+          const float dx = __fsub_rn(x, __ldg(a)), dy = __fsub_rn(y, __ldg(a + 1)), dz = __fsub_rn(z, __ldg(a + 2));
+          const float qx = __fsub_rn(len2(dx, dz), __ldg(a + 3));
+          st[sp++] = __fsub_rn(len2(qx, dy), __ldg(a + 4));
+          i += 6;
+          break;
+        }
+        case S2M_CSG_CAPSULE: {  // sdf3d_capsule(p, a, b, r)
+          const float pax = __fsub_rn(x, __ldg(a)), pay = __fsub_rn(y, __ldg(a + 1)), paz = __fsub_rn(z, __ldg(a + 2));
+          const float bax = __fsub_rn(__ldg(a + 3), __ldg(a)), bay = __fsub_rn(__ldg(a + 4), __ldg(a + 1)),
+                      baz = __fsub_rn(__ldg(a + 5), __ldg(a + 2));
+          const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(pax, bax), __fmul_rn(pay, bay)), __fmul_rn(paz, baz));
+          const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(bax, bax), __fmul_rn(bay, bay)), __fmul_rn(baz, baz));
+          const float h = clamp01(__fdiv_rn(d1, d2));
+          st[sp++] = __fsub_rn(len3(__fsub_rn(pax, __fmul_rn(bax, h)), __fsub_rn(pay, __fmul_rn(bay, h)),
+                                    __fsub_rn(paz, __fmul_rn(baz, h))),
+                               __ldg(a + 6));
+          i += 8;
+          break;
+        }
+        case S2M_CSG_PLANE: {  // dot(p, n) - d
+          const float d = __fadd_rn(__fadd_rn(__fmul_rn(x, __ldg(a)), __fmul_rn(y, __ldg(a + 1))), __fmul_rn(z, __ldg(a + 2)));
+          st[sp++] = __fsub_rn(d, __ldg(a + 3));
+          i += 5;
+          break;
+        }
+        case S2M_CSG_UNION: {
+          const float b = st[--sp];
+          st[sp - 1] = fminf(st[sp - 1], b);
+          i += 1;
+          break;
+        }
+        case S2M_CSG_SUBTRACT: {  // max(a, -b)
+          const float b = st[--sp];
+          st[sp - 1] = fmaxf(st[sp - 1], -b);
+          i += 1;
+          break;
+        }
+        case S2M_CSG_INTERSECT: {
+          const float b = st[--sp];
+          st[sp - 1] = fmaxf(st[sp - 1], b);
+          i += 1;
+          break;
+        }
+        case S2M_CSG_SMOOTH_UNION: {  // sdf_op_smooth_union(a, b, k)
+          const float b = st[--sp], d1 = st[sp - 1], k = __ldg(a);
+          const float h = clamp01(__fadd_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
+          st[sp - 1] = __fsub_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
+          i += 2;
+          break;
+        }
+        case S2M_CSG_SMOOTH_INTERSECTION: {  // sdf_op_smooth_intersection(a, b, k)
+          const float b = st[--sp], d1 = st[sp - 1], k = __ldg(a);
+          const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
+          st[sp - 1] = __fadd_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
+          i += 2;
+          break;
+        }
+        case S2M_CSG_SMOOTH_SUBTRACTION: {  // sdf_op_smooth_subtraction(a, b, k)
+          const float b = st[--sp], d1 = st[sp - 1], k = __ldg(a);
+          const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fadd_rn(b, d1)), k)));
+          st[sp - 1] = __fadd_rn(mix(b, -d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
+          i += 2;
+          break;
+        }
+        default:
+          return __int_as_float(0x7fc00000);  // rejected on the host; never reached
+      }
+    }
+    return st[sp - 1];
+  }
+
+  __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
+    s2_tetra_normal(*this, px, py, pz, eps, n);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Device-side batch description.
+
+enum { S2_ST_EVAL = 0, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_ST_ROWS, S2_ST_QUADS, S2_NSTAGES };
+#define S2_B_EVAL_ITEM 2048
+#define S2_B_VERT_CHUNK 256
+#define S2_ERR_BATCH_WAIT 0x20u
+
+struct S2BatchJob {
+  S2Job job;                        // ring == P: the whole lattice is resident
+  const float *prog;
+  int prog_len;
+  int nzc;                          // cell slices emitted (N, or N - 1 with the slice lag)
+  float *lattice;
+  S2Cand cand;
+  S2MeshDev mesh;
+  unsigned long long *cell_status;  // look-back words of the classification tiles
+  unsigned *xcounter;               // vertex chunk counter
+  unsigned *done;                   // completed items per stage
+  unsigned nitems[S2_NSTAGES];
+  unsigned scan_tiles;
+};
+
+struct S2BatchSeg {
+  unsigned long long start;  // first ticket
+  unsigned job, stage, count, pad;
+};
+
+struct S2BatchCtl {
+  unsigned long long next;  // ticket counter
+  unsigned err;
+  unsigned pad;
+};
+
+// Results gathered for the host: ntris, invalid, vtotal, err, candidates.
+struct S2BatchResult {
+  unsigned long long ntris, invalid, vtotal, ncand;
+  unsigned err, pad;
+};
+
+__device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned item) {
+  const S2Job &j = J.job;
+  const S2CsgSdf f{J.prog, J.prog_len};
+  const long long P = j.P, pp = P * P, total = pp * P;
+#pragma unroll 1
+  for (int r = 0; r < S2_B_EVAL_ITEM / 256; ++r) {
+    const long long idx = (long long)item * S2_B_EVAL_ITEM + r * 256 + threadIdx.x;
+    if (idx >= total) break;
+    const int k = (int)(idx / pp);
+    const long long rem = idx - (long long)k * pp;
+    const int y = (int)(rem / P), x = (int)(rem - (long long)y * P);
+    J.lattice[(long long)k * j.plane + (long long)y * j.pitch + x] = f(s2_coord(j, x), s2_coord(j, y), s2_coord(j, k));
+  }
+}
+
+// Classification tile `tile` of the job (the tickets of this stage come in
+// tile order, so the look-back only waits for tiles already taken).
+__device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned tile) {
+  __shared__ unsigned s_warp[32];
+  __shared__ unsigned long long s_excl;
+  const S2Job &job = J.job;
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const long long ncells = (long long)J.nzc * job.N * job.N;
+  const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
+  unsigned ballots[S2_CELL_CPT];
+#pragma unroll
+  for (int m = 0; m < S2_CELL_CPT; ++m) {
+    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
+    bool is_cand = c < ncells && s2_classify<true>(job, J.lattice, s2_cell_of(job, c, 0));
+    ballots[m] = __ballot_sync(S2_FULL, is_cand);
+    if (lane == 0) s_warp[m * 8 + warp] = __popc(ballots[m]);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    unsigned tot = s2_warp_exclusive32(s_warp);
+    unsigned long long excl = s2_lookback(J.cell_status, tile, tot, J.mesh.err);
+    if (lane == 0) {
+      s_excl = excl;
+      if (tile == ntiles - 1) J.cand.base[1] = excl + tot;
+    }
+  }
+  __syncthreads();
+  const unsigned lt = s2_lanemask_lt();
+#pragma unroll
+  for (int m = 0; m < S2_CELL_CPT; ++m) {
+    if (!((ballots[m] >> lane) & 1u)) continue;
+    unsigned long long o = s_excl + s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
+    if (o >= J.cand.cap) {
+      atomicOr(J.mesh.err, S2_ERR_CAND_OVF);
+      continue;
+    }
+    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
+    S2Cell cell = s2_cell_of(job, c, 0);
+    float v[8];
+    s2_load_corners<true>(job, J.lattice, cell, v);
+    J.cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
+    float4 *dst = reinterpret_cast<float4 *>(J.cand.val + 8 * o);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+  __syncthreads();  // s_warp / s_excl are reused by the block's next item
+}
+
+__device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
+  __shared__ unsigned s_chunk;
+  const S2Job &job = J.job;
+  const S2CsgSdf f{J.prog, J.prog_len};
+  const unsigned long long n = min(__ldcg(J.cand.base + 1), J.cand.cap);
+  const unsigned nchunks = (unsigned)((n + S2_B_VERT_CHUNK - 1) / S2_B_VERT_CHUNK);
+  for (;;) {
+    if (threadIdx.x == 0) s_chunk = atomicAdd(J.xcounter, 1u);
+    __syncthreads();
+    const unsigned chunk = s_chunk;
+    __syncthreads();
+    if (chunk >= nchunks) break;
+    const unsigned long long o = (unsigned long long)chunk * S2_B_VERT_CHUNK + threadIdx.x;
+    if (o < n) {
+      unsigned long long k = __ldcg(J.cand.key + o);
+      S2Cell c;
+      c.x = (int)(k & 0xffffull);
+      c.y = (int)((k >> 16) & 0xffffull);
+      c.z = (int)((k >> 32) & 0xffffull);
+      const float4 *src = reinterpret_cast<const float4 *>(J.cand.val + 8 * o);
+      const float4 a = __ldcg(src), b = __ldcg(src + 1);
+      float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+      float pos[3], nrm[3];
+      const unsigned long long key = job.qef ? s2_vertex_qef(f, job, c, v, pos, nrm) : s2_vertex(f, job, c, v, pos, nrm);
+      J.cand.key[o] = key;
+      if (key >> 63) {
+        J.cand.pos[3 * o] = pos[0];
+        J.cand.pos[3 * o + 1] = pos[1];
+        J.cand.pos[3 * o + 2] = pos[2];
+        J.cand.nrm[3 * o] = nrm[0];
+        J.cand.nrm[3 * o + 1] = nrm[1];
+        J.cand.nrm[3 * o + 2] = nrm[2];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__restrict__ jobs,
+                                                        const S2BatchSeg *__restrict__ segs, int nsegs,
+                                                        unsigned long long total, S2BatchCtl *ctl) {
+  __shared__ unsigned long long s_ticket;
+  __shared__ int s_ok;
+  const unsigned tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_ticket = atomicAdd(&ctl->next, 1ull);
+    __syncthreads();
+    const unsigned long long ticket = s_ticket;
+    if (ticket >= total) break;
+    int lo = 0, hi = nsegs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].start <= ticket) lo = mid;
+      else hi = mid - 1;
+    }
+    const S2BatchSeg sg = segs[lo];
+    const unsigned item = (unsigned)(ticket - sg.start);
+    const S2BatchJob &J = jobs[sg.job];
+    if (tid == 0) {
+      int ok = 1;
+      if (sg.stage > 0) {
+        // wait for every item of the previous stage of this job (lower tickets)
+        // bounded by time: 30 s of the GPU's global timer
+        const unsigned need = J.nitems[sg.stage - 1];
+        unsigned long long t0 = 0;
+        for (unsigned spins = 0;; ++spins) {
+          unsigned d;
+          asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(d) : "l"(J.done + sg.stage - 1) : "memory");
+          if (d >= need) break;
+          unsigned long long now;
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+          if (spins == 0) t0 = now;
+          if (now - t0 > 30000000000ull) {
+            atomicOr(&ctl->err, S2_ERR_BATCH_WAIT);
+            ok = 0;
+            break;
+          }
+          __nanosleep(128);
+        }
+      }
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (s_ok) {
+      switch (sg.stage) {
+        case S2_ST_EVAL: s2b_stage_eval(J, item); break;
+        case S2_ST_CELLS: s2b_stage_cells(J, item); break;
+        case S2_ST_VERT: s2b_stage_vertices(J); break;
+        case S2_ST_VCOMPACT: s2_vcompact_worker(J.job, J.cand, J.mesh, 1, item == 0); break;
+        case S2_ST_ROWS: s2_rowscan_worker(J.mesh, (unsigned long long)J.job.N * J.job.N); break;
+        case S2_ST_QUADS: s2_quads_worker(J.job, J.mesh, J.scan_tiles, item == 0); break;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(J.done + sg.stage, 1u);
+    }
+  }
+}
+
+__global__ void s2m_batch_results(const S2BatchJob *__restrict__ jobs, int n, S2BatchResult *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const S2BatchJob &J = jobs[i];
+  S2BatchResult r;
+  r.ntris = *J.mesh.ntris;
+  r.invalid = *J.mesh.invalid;
+  r.vtotal = *J.mesh.vtotal;
+  r.ncand = J.cand.base[1];
+  r.err = *J.mesh.err;
+  r.pad = 0;
+  out[i] = r;
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+namespace {
+
+void set_err(char *err, size_t errlen, const std::string &msg) {
+  if (!err || errlen == 0) return;
+  size_t n = std::min(errlen - 1, msg.size());
+  std::memcpy(err, msg.data(), n);
+  err[n] = 0;
+}
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 152;
+}
+
+// Operands per opcode, or -1 for an unknown opcode.
+int csg_operands(int op) {
+  switch (op) {
+    case S2M_CSG_SPHERE: return 4;
+    case S2M_CSG_BOX: return 6;
+    case S2M_CSG_TORUS: return 5;
+    case S2M_CSG_CAPSULE: return 7;
+    case S2M_CSG_PLANE: return 4;
+    case S2M_CSG_UNION:
+    case S2M_CSG_SUBTRACT:
+    case S2M_CSG_INTERSECT: return 0;
+    case S2M_CSG_SMOOTH_UNION:
+    case S2M_CSG_SMOOTH_INTERSECTION:
+    case S2M_CSG_SMOOTH_SUBTRACTION: return 1;
+  }
+  return -1;
+}
+
+// Well-formed: known opcodes, operands present, the stack never underflows
+// or exceeds S2_CSG_STACK, and one value is left.
+bool csg_validate(const float *p, uint32_t n, std::string &why) {
+  int sp = 0;
+  uint32_t i = 0;
+  while (i < n) {
+    float fo = p[i];
+    int op = int(fo);
+    if (float(op) != fo || csg_operands(op) < 0) {
+      why = "unknown opcode at " + std::to_string(i);
+      return false;
+    }
+    int nops = csg_operands(op);
+    if (i + 1 + uint32_t(nops) > n) {
+      why = "missing operands at " + std::to_string(i);
+      return false;
+    }
+    for (int k = 0; k < nops; ++k)
+      if (!std::isfinite(p[i + 1 + k])) {
+        why = "non-finite operand at " + std::to_string(i + 1 + k);
+        return false;
+      }
+    if (op < 10) {
+      if (++sp > S2_CSG_STACK) {
+        why = "program needs more than 32 stack entries";
+        return false;
+      }
+    } else if (--sp < 1) {
+      why = "operator without two operands at " + std::to_string(i);
+      return false;
+    }
+    i += 1 + uint32_t(nops);
+  }
+  if (sp != 1) {
+    why = "program leaves " + std::to_string(sp) + " values on the stack";
+    return false;
+  }
+  return true;
+}
+
+struct HostJob {
+  std::vector<float> prog;
+  s2m_params params;
+  S2Job job{};
+  int N = 0, nzc = 0;
+  unsigned long long cand_cap = 0, vcap = 0, tcap = 0;
+  // placement in the run's arena
+  size_t zero_off = 0, data_off = 0;
+  int run = -1;  // index of the run (arena) holding the results, -1 = not run yet
+  // results
+  uint64_t nverts = 0, ntris = 0, invalid = 0, ncand = 0;
+  uint32_t err = 0;
+  bool ok = false;
+  // device outputs
+  float *pos = nullptr, *nrm = nullptr;
+  unsigned long long *key = nullptr;
+  unsigned *tris = nullptr;
+};
+
+size_t al(size_t b) { return (b + 255) / 256 * 256; }
+
+// Bytes of the zeroed control region and of the data region of a job.
+void job_sizes(const HostJob &h, size_t &zero_bytes, size_t &data_bytes) {
+  const unsigned long long N = (unsigned long long)h.N;
+  const unsigned long long ncells = (unsigned long long)h.nzc * N * N;
+  const size_t cell_tiles = (ncells + S2_CELL_TILE - 1) / S2_CELL_TILE;
+  const size_t vc_tiles = (h.cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
+  const size_t scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
+  const size_t quad_tiles = (h.vcap + S2_Q_TILE - 1) / S2_Q_TILE;
+  zero_bytes = al(2 * 8) + al(vc_tiles * 8) + al(cell_tiles * 8) + al((scan_tiles + quad_tiles) * 8) + al(N * N * 4) +
+               al(8 * 4) /*counters*/ + al(8 * 4) /*done*/ + al(8 * 8) /*ntris, invalid, vtotal, err*/ + al(4);
+  data_bytes = al(size_t(h.job.ring) * size_t(h.job.plane) * 4) + al(h.cand_cap * 8) + al(h.cand_cap * 32) +
+               al(h.cand_cap * 12) * 2 + al((N * N + 1) * 4) + al(h.vcap * 12) * 2 + al(h.vcap * 8) + al(h.tcap * 12);
+}
+
+}  // namespace
+
+struct s2m_batch {
+  std::vector<HostJob> jobs;
+  std::vector<void *> arenas;  // one per run; results of a run's jobs live in its arena
+  uint64_t budget = 0;
+  int blocks_per_sm = 0;
+  double last_ms = 0;
+  uint64_t last_launches = 0;
+};
+
+namespace {
+
+// Run jobs `idx` in one persistent launch (new arena).  Returns S2M_OK or an error.
+int run_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, char *err, size_t errlen) {
+  std::vector<size_t> zb(idx.size()), db(idx.size());
+  size_t ztot = 0, dtot = 0;
+  for (size_t i = 0; i < idx.size(); ++i) {
+    job_sizes(b->jobs[idx[i]], zb[i], db[i]);
+    ztot += zb[i];
+    dtot += db[i];
+  }
+  size_t prog_bytes = 0;
+  for (int j : idx) prog_bytes += al(b->jobs[j].prog.size() * 4);
+  const size_t jobs_bytes = al(idx.size() * sizeof(S2BatchJob));
+  const size_t segs_bytes = al(idx.size() * S2_NSTAGES * sizeof(S2BatchSeg));
+  const size_t res_bytes = al(idx.size() * sizeof(S2BatchResult));
+  const size_t ctl_bytes = al(sizeof(S2BatchCtl));
+  const size_t total = ztot + ctl_bytes + dtot + prog_bytes + jobs_bytes + segs_bytes + res_bytes;
+  char *arena = nullptr;
+  cudaError_t e = cudaMalloc(&arena, total);
+  if (e != cudaSuccess) {
+    set_err(err, errlen, std::string("batch arena (") + std::to_string(total) + " bytes): " + cudaGetErrorString(e));
+    return S2M_E_OOM;
+  }
+  b->arenas.push_back(arena);
+  const int run_id = int(b->arenas.size()) - 1;
+
+  // host images of the job table, segments and programs
+  std::vector<S2BatchJob> dj(idx.size());
+  std::vector<S2BatchSeg> segs;
+  std::vector<char> progs(prog_bytes);
+  size_t zoff = 0, doff = ztot + ctl_bytes, poff = 0;
+  unsigned long long ticket = 0;
+  for (size_t i = 0; i < idx.size(); ++i) {
+    HostJob &h = b->jobs[idx[i]];
+    const unsigned long long N = (unsigned long long)h.N;
+    const unsigned long long ncells = (unsigned long long)h.nzc * N * N;
+    const size_t cell_tiles = (ncells + S2_CELL_TILE - 1) / S2_CELL_TILE;
+    const size_t vc_tiles = (h.cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
+    const size_t scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
+    const size_t quad_tiles = (h.vcap + S2_Q_TILE - 1) / S2_Q_TILE;
+    S2BatchJob &J = dj[i];
+    std::memset(&J, 0, sizeof(J));
+    J.job = h.job;
+    J.nzc = h.nzc;
+    char *z = arena + zoff;
+    J.cand.base = reinterpret_cast<unsigned long long *>(z); z += al(2 * 8);
+    J.cand.status = reinterpret_cast<unsigned long long *>(z); z += al(vc_tiles * 8);
+    J.cell_status = reinterpret_cast<unsigned long long *>(z); z += al(cell_tiles * 8);
+    J.mesh.scan_status = reinterpret_cast<unsigned long long *>(z); z += al((scan_tiles + quad_tiles) * 8);
+    J.mesh.rowcnt = reinterpret_cast<unsigned *>(z); z += al(N * N * 4);
+    unsigned *counters = reinterpret_cast<unsigned *>(z); z += al(8 * 4);
+    J.done = reinterpret_cast<unsigned *>(z); z += al(8 * 4);
+    unsigned long long *ctl = reinterpret_cast<unsigned long long *>(z); z += al(8 * 8);
+    z += al(4);
+    zoff += zb[i];
+    J.mesh.counters = counters;
+    J.cand.tile_counter = counters + 0;
+    J.xcounter = counters + 1;
+    J.mesh.ntris = ctl + 0;
+    J.mesh.invalid = ctl + 1;
+    J.mesh.vtotal = ctl + 2;
+    J.mesh.err = reinterpret_cast<unsigned *>(ctl + 3);
+    char *d = arena + doff;
+    J.lattice = reinterpret_cast<float *>(d); d += al(size_t(h.job.ring) * size_t(h.job.plane) * 4);
+    J.cand.key = reinterpret_cast<unsigned long long *>(d); d += al(h.cand_cap * 8);
+    J.cand.val = reinterpret_cast<float *>(d); d += al(h.cand_cap * 32);
+    J.cand.pos = reinterpret_cast<float *>(d); d += al(h.cand_cap * 12);
+    J.cand.nrm = reinterpret_cast<float *>(d); d += al(h.cand_cap * 12);
+    J.mesh.rowstart = reinterpret_cast<unsigned *>(d); d += al((N * N + 1) * 4);
+    J.mesh.pos = reinterpret_cast<float *>(d); d += al(h.vcap * 12);
+    J.mesh.nrm = reinterpret_cast<float *>(d); d += al(h.vcap * 12);
+    J.mesh.key = reinterpret_cast<unsigned long long *>(d); d += al(h.vcap * 8);
+    J.mesh.tris = reinterpret_cast<unsigned *>(d); d += al(h.tcap * 12);
+    doff += db[i];
+    J.cand.cap = h.cand_cap;
+    J.mesh.vcap = h.vcap;
+    J.mesh.tcap = h.tcap;
+    J.scan_tiles = unsigned(scan_tiles);
+    std::memcpy(progs.data() + poff, h.prog.data(), h.prog.size() * 4);
+    J.prog = reinterpret_cast<const float *>(arena + ztot + ctl_bytes + dtot + poff);
+    J.prog_len = int(h.prog.size());
+    poff += al(h.prog.size() * 4);
+    // items per stage
+    const unsigned long long P = (unsigned long long)h.job.P;
+    const unsigned long long n2 = N * N;
+    J.nitems[S2_ST_EVAL] = unsigned((P * P * P + S2_B_EVAL_ITEM - 1) / S2_B_EVAL_ITEM);
+    J.nitems[S2_ST_CELLS] = unsigned(std::max<size_t>(1, cell_tiles));
+    J.nitems[S2_ST_VERT] = unsigned(std::min<unsigned long long>(128, std::max<unsigned long long>(1, n2 / 2048)));
+    J.nitems[S2_ST_VCOMPACT] = unsigned(std::min<unsigned long long>(64, std::max<unsigned long long>(1, n2 / 8192)));
+    J.nitems[S2_ST_ROWS] = unsigned(std::min<unsigned long long>(16, std::max<unsigned long long>(1, n2 / 16384)));
+    J.nitems[S2_ST_QUADS] = unsigned(std::min<unsigned long long>(64, std::max<unsigned long long>(1, n2 / 8192)));
+    for (int s = 0; s < S2_NSTAGES; ++s) {
+      S2BatchSeg sg;
+      sg.start = ticket;
+      sg.job = unsigned(i);
+      sg.stage = unsigned(s);
+      sg.count = J.nitems[s];
+      sg.pad = 0;
+      segs.push_back(sg);
+      ticket += J.nitems[s];
+    }
+    h.run = run_id;
+    h.pos = J.mesh.pos;
+    h.nrm = J.mesh.nrm;
+    h.key = J.mesh.key;
+    h.tris = J.mesh.tris;
+  }
+  char *d_prog = arena + ztot + ctl_bytes + dtot;
+  S2BatchJob *d_jobs = reinterpret_cast<S2BatchJob *>(d_prog + prog_bytes);
+  S2BatchSeg *d_segs = reinterpret_cast<S2BatchSeg *>(reinterpret_cast<char *>(d_jobs) + jobs_bytes);
+  S2BatchResult *d_res = reinterpret_cast<S2BatchResult *>(reinterpret_cast<char *>(d_segs) + segs_bytes);
+  S2BatchCtl *d_ctl = reinterpret_cast<S2BatchCtl *>(arena + ztot);
+
+#define S2B_CUDA(call)                                                                 \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      set_err(err, errlen, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+      return S2M_E_CUDA;                                                               \
+    }                                                                                  \
+  } while (0)
+  S2B_CUDA(cudaMemsetAsync(arena, 0, ztot + ctl_bytes, st));
+  S2B_CUDA(cudaMemcpyAsync(d_prog, progs.data(), prog_bytes, cudaMemcpyHostToDevice, st));
+  S2B_CUDA(cudaMemcpyAsync(d_jobs, dj.data(), idx.size() * sizeof(S2BatchJob), cudaMemcpyHostToDevice, st));
+  S2B_CUDA(cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(S2BatchSeg), cudaMemcpyHostToDevice, st));
+  if (b->blocks_per_sm <= 0) {
+    int nb = 0;
+    S2B_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, s2m_batch_kernel, 256, 0));
+    b->blocks_per_sm = std::max(1, nb);
+  }
+  const int grid = device_sms() * b->blocks_per_sm;
+  cudaEvent_t e0, e1;
+  S2B_CUDA(cudaEventCreate(&e0));
+  S2B_CUDA(cudaEventCreate(&e1));
+  S2B_CUDA(cudaEventRecord(e0, st));
+  s2m_batch_kernel<<<grid, 256, 0, st>>>(d_jobs, d_segs, int(segs.size()), ticket, d_ctl);
+  S2B_CUDA(cudaGetLastError());
+  S2B_CUDA(cudaEventRecord(e1, st));
+  s2m_batch_results<<<unsigned((idx.size() + 127) / 128), 128, 0, st>>>(d_jobs, int(idx.size()), d_res);
+  S2B_CUDA(cudaGetLastError());
+  std::vector<S2BatchResult> res(idx.size());
+  S2BatchCtl hctl;
+  S2B_CUDA(cudaMemcpyAsync(res.data(), d_res, idx.size() * sizeof(S2BatchResult), cudaMemcpyDeviceToHost, st));
+  S2B_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(hctl), cudaMemcpyDeviceToHost, st));
+  S2B_CUDA(cudaStreamSynchronize(st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->last_ms += ms;
+  b->last_launches += 2;
+  if (hctl.err & S2_ERR_BATCH_WAIT) {
+    set_err(err, errlen, "a batch stage wait hit its limit");
+    return S2M_E_TIMEOUT;
+  }
+  for (size_t i = 0; i < idx.size(); ++i) {
+    HostJob &h = b->jobs[idx[i]];
+    h.ntris = res[i].ntris;
+    h.invalid = res[i].invalid;
+    h.nverts = res[i].vtotal;
+    h.ncand = res[i].ncand;
+    h.err = res[i].err;
+    h.ok = (h.err & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF | S2_ERR_LOOKBACK | S2_ERR_INDEX_OVF)) == 0;
+  }
+  return S2M_OK;
+#undef S2B_CUDA
+}
+
+}  // namespace
+
+extern "C" {
+
+int s2m_batch_create(s2m_batch **out, uint64_t memory_budget_bytes) {
+  if (!out) return S2M_E_INVALID;
+  s2m_batch *b = new s2m_batch();
+  b->budget = memory_budget_bytes;
+  *out = b;
+  return S2M_OK;
+}
+
+int s2m_batch_add_csg(s2m_batch *b, const float *program, uint32_t len, const s2m_params *params,
+                      uint32_t *job_id, char *err, size_t errlen) {
+  if (!b || !program || !params) {
+    set_err(err, errlen, "null argument");
+    return S2M_E_INVALID;
+  }
+  std::string why;
+  if (!csg_validate(program, len, why)) {
+    set_err(err, errlen, "invalid CSG program: " + why);
+    return S2M_E_INVALID;
+  }
+  HostJob h;
+  h.prog.assign(program, program + len);
+  h.params = *params;
+  uint32_t N = params->resolution;
+  if (params->flags & S2M_JOB_POW2_ROUNDING)
+    if (__builtin_popcount(N) > 1) N = 2u << (31u - uint32_t(__builtin_clz(N)));
+  if (N < 2 || N > 4096) {
+    set_err(err, errlen, "batch resolution must be in [2, 4096]");
+    return S2M_E_INVALID;
+  }
+  if (!(params->bounds > 0.0f) || !std::isfinite(params->bounds)) {
+    set_err(err, errlen, "bounds must be a positive finite number");
+    return S2M_E_INVALID;
+  }
+  h.N = int(N);
+  S2Job &j = h.job;
+  j.N = int(N);
+  j.P = int(N) + 1;
+  j.pitch = (j.P + 31) / 32 * 32;
+  j.plane = (long long)j.P * j.pitch;
+  j.ring = j.P;
+  // Bounds3D::cube(B, 0) and dualcontour.wgsl:23-24 in binary32 (as the per-job path)
+  volatile float half = params->bounds * 0.5f;
+  volatile float mn = 0.0f - half;
+  volatile float mx = 0.0f + half;
+  volatile float ext = mx - mn;
+  j.bmin = mn;
+  j.size = ext / float(N - 1u);
+  j.eps = params->eps > 0.0f ? params->eps : 1e-4f;
+  j.guard = j.size;
+  j.lag = (params->flags & S2M_JOB_SLICE_LAG) ? 1 : 0;
+  j.exact = (params->flags & S2M_JOB_EXACT_CORNERS) ? 1 : 0;
+  j.qef = (params->flags & S2M_JOB_QEF) ? 1 : 0;
+  h.nzc = j.lag ? int(N) - 1 : int(N);
+  const unsigned long long n3 = (unsigned long long)N * N * N, n2 = (unsigned long long)N * N;
+  h.cand_cap = std::min(n3, std::max<unsigned long long>(4096, 8 * n2));
+  h.vcap = params->max_vertices ? params->max_vertices : std::min(h.cand_cap, std::max<unsigned long long>(4096, 6 * n2));
+  h.vcap = std::min(h.vcap, h.cand_cap);
+  h.tcap = params->max_triangles ? params->max_triangles : 2 * h.vcap + 4096;
+  b->jobs.push_back(std::move(h));
+  if (job_id) *job_id = uint32_t(b->jobs.size() - 1);
+  return S2M_OK;
+}
+
+uint64_t s2m_batch_job_footprint(const s2m_batch *b, uint32_t job) {
+  if (!b || job >= b->jobs.size()) return 0;
+  size_t z, d;
+  job_sizes(b->jobs[job], z, d);
+  return z + d + al(b->jobs[job].prog.size() * 4) + sizeof(S2BatchJob) + S2_NSTAGES * sizeof(S2BatchSeg);
+}
+
+int s2m_batch_run(s2m_batch *b, void *stream, char *err, size_t errlen) {
+  if (!b) return S2M_E_INVALID;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  b->last_ms = 0;
+  b->last_launches = 0;
+  std::vector<int> pending;
+  for (size_t i = 0; i < b->jobs.size(); ++i)
+    if (b->jobs[i].run < 0) pending.push_back(int(i));
+  for (int round = 0; round < 4 && !pending.empty(); ++round) {
+    // waves under the memory budget, in submission order
+    size_t w0 = 0;
+    while (w0 < pending.size()) {
+      std::vector<int> wave;
+      uint64_t used = 0;
+      for (size_t i = w0; i < pending.size(); ++i) {
+        uint64_t fp = s2m_batch_job_footprint(b, uint32_t(pending[i]));
+        if (!wave.empty() && b->budget && used + fp > b->budget) break;
+        wave.push_back(pending[i]);
+        used += fp;
+      }
+      int rc = run_wave(b, wave, st, err, errlen);
+      if (rc != S2M_OK) return rc;
+      w0 += wave.size();
+    }
+    // jobs whose buffers overflowed run again with their exact totals
+    std::vector<int> again;
+    for (int i : pending) {
+      HostJob &h = b->jobs[i];
+      if (h.ok) continue;
+      if (h.err & (S2_ERR_LOOKBACK | S2_ERR_INDEX_OVF)) {
+        set_err(err, errlen, "job " + std::to_string(i) + ": device error flags " + std::to_string(h.err));
+        return (h.err & S2_ERR_LOOKBACK) ? S2M_E_TIMEOUT : S2M_E_OVERFLOW;
+      }
+      const unsigned long long n3 = (unsigned long long)h.N * h.N * h.N;
+      if (h.err & S2_ERR_CAND_OVF) {
+        h.cand_cap = std::min<unsigned long long>(n3, h.ncand + h.ncand / 16 + 4096);
+        h.vcap = h.cand_cap;
+      } else if (h.err & S2_ERR_VERT_OVF) {
+        h.vcap = std::min<unsigned long long>(h.cand_cap, h.nverts + h.nverts / 16 + 4096);
+      }
+      if (h.err & S2_ERR_TRI_OVF) h.tcap = h.ntris + h.ntris / 16 + 4096;
+      h.tcap = std::max<unsigned long long>(h.tcap, 2 * h.vcap + 4096);
+      h.run = -1;
+      again.push_back(i);
+    }
+    pending.swap(again);
+  }
+  if (!pending.empty()) {
+    set_err(err, errlen, "batch jobs still overflow after resizing");
+    return S2M_E_OVERFLOW;
+  }
+  return S2M_OK;
+}
+
+int s2m_batch_job_info(const s2m_batch *b, uint32_t job, s2m_mesh_info *info) {
+  if (!b || !info || job >= b->jobs.size()) return S2M_E_INVALID;
+  const HostJob &h = b->jobs[job];
+  std::memset(info, 0, sizeof(*info));
+  if (h.run < 0) return S2M_E_INVALID;
+  info->nverts = h.nverts;
+  info->ntris = h.ntris;
+  info->invalid_quads = h.invalid;
+  info->cells = (uint64_t)h.N * h.N * h.N;
+  info->candidate_cells = h.ncand;
+  info->resolution = uint32_t(h.N);
+  info->slab_depth = uint32_t(h.N);
+  info->d_pos = h.pos;
+  info->d_nrm = h.nrm;
+  info->d_cell = reinterpret_cast<const uint64_t *>(h.key);
+  info->d_tris = h.tris;
+  info->kernel_launches = 0;
+  return S2M_OK;
+}
+
+int s2m_batch_job_copy_to_host(const s2m_batch *b, uint32_t job, float *pos, float *nrm, uint64_t *cell,
+                               uint32_t *tris, void *stream) {
+  if (!b || job >= b->jobs.size() || b->jobs[job].run < 0) return S2M_E_INVALID;
+  const HostJob &h = b->jobs[job];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  if (pos && h.nverts) e = cudaMemcpyAsync(pos, h.pos, h.nverts * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && nrm && h.nverts) e = cudaMemcpyAsync(nrm, h.nrm, h.nverts * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && cell && h.nverts) e = cudaMemcpyAsync(cell, h.key, h.nverts * 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && tris && h.ntris) e = cudaMemcpyAsync(tris, h.tris, h.ntris * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? S2M_OK : S2M_E_CUDA;
+}
+
+int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, uint32_t *njobs) {
+  if (!b) return S2M_E_INVALID;
+  if (kernel_ms) *kernel_ms = b->last_ms;
+  if (launches) *launches = b->last_launches;
+  if (njobs) *njobs = uint32_t(b->jobs.size());
+  return S2M_OK;
+}
+
+void s2m_batch_free(s2m_batch *b) {
+  if (!b) return;
+  for (void *a : b->arenas) cudaFree(a);
+  delete b;
+}
+
+}  // extern "C"

@@ -146,6 +146,7 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
   src += kS2mDeviceH;
   src += kS2mLookbackCuh;
   src += kS2mPreludeCuh;
+  src += kS2mDcCoreCuh;
   src += s->user_cuda;
   src += kS2mDcKernelsCuh;
   nvrtcProgram prog;
@@ -244,6 +245,7 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   j.guard = j.size;  // one cell: far above any rounding difference of a corner
   j.lag = (p.flags & S2M_JOB_SLICE_LAG) ? 1 : 0;
   j.exact = (p.flags & S2M_JOB_EXACT_CORNERS) ? 1 : 0;
+  j.qef = (p.flags & S2M_JOB_QEF) ? 1 : 0;
   m->nzc = j.lag ? int(N) - 1 : int(N);
   // Slab depth: the ring of D + 1 lattice planes is sized to stay resident in
   // the 126 MB L2 between the evaluation and the cell pass.

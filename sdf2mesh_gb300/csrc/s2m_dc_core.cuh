@@ -1,0 +1,337 @@
+// s2m_dc_core.cuh -- the dual-contouring rule on one cell, independent of
+// how the SDF is evaluated: lattice coordinates, candidate classification,
+// the reference's mass-point vertex (dualcontour.wgsl:22-180) and the
+// precision-mode QEF vertex.  Every function that evaluates the SDF takes an
+// evaluator `f` with
+//     float f(float x, float y, float z) const;            // sdf3d
+//     void f.normal(float x, float y, float z, float eps, float n[3]) const;
+//                                                           // sdf3d_normal, not normalised
+// NVRTC instantiates it with the lowered user SDF (s2m_dc_kernels.cuh); the
+// batch engine with its CSG program interpreter (s2m_batch.cuh).
+// All arithmetic of the rule is explicitly rounded binary32 / binary64.
+#pragma once
+
+__device__ __forceinline__ float s2_coord(const S2Job &j, int i) {
+  return __fadd_rn(j.bmin, __fmul_rn(j.size, (float)i));
+}
+// 1 if mn(i - 1) + size differs (bitwise) from the lattice coordinate c(i).
+__device__ __forceinline__ unsigned s2_off_lattice(const S2Job &j, int i) {
+  float hi = __fadd_rn(s2_coord(j, i - 1), j.size);
+  return __float_as_uint(hi) != __float_as_uint(s2_coord(j, i)) ? 1u : 0u;
+}
+
+struct S2Cell {
+  int x, y, z;
+};
+
+__device__ __forceinline__ S2Cell s2_cell_of(const S2Job &j, long long c, int zc0) {
+  S2Cell r;
+  r.x = (int)(c % j.N);
+  long long q = c / j.N;
+  r.y = (int)(q % j.N);
+  r.z = zc0 + (int)(q / j.N);
+  return r;
+}
+
+// The 8 lattice values of a cell, corner index bx | by << 1 | bz << 2.
+// CG: read through L2 only (lattices written earlier in the same launch by
+// other blocks, as in the persistent batch kernel).
+template <bool CG = false>
+__device__ __forceinline__ void s2_load_corners(const S2Job &j, const float *__restrict__ ring, S2Cell c, float v[8]) {
+  const float *p0 = ring + (long long)(c.z % j.ring) * j.plane + (long long)c.y * j.pitch + c.x;
+  const float *p1 = ring + (long long)((c.z + 1) % j.ring) * j.plane + (long long)c.y * j.pitch + c.x;
+  const float *p[8] = {p0, p0 + 1, p0 + j.pitch, p0 + j.pitch + 1, p1, p1 + 1, p1 + j.pitch, p1 + j.pitch + 1};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = CG ? __ldcg(p[k]) : __ldg(p[k]);
+}
+
+// Mask of corners whose reference coordinates are not lattice points.
+__device__ __forceinline__ unsigned s2_off_mask(const S2Job &j, S2Cell c) {
+  unsigned ox = s2_off_lattice(j, c.x + 1), oy = s2_off_lattice(j, c.y + 1), oz = s2_off_lattice(j, c.z + 1);
+  unsigned m = 0;
+  for (int k = 1; k < 8; ++k)
+    if (((k & 1) && ox) || ((k & 2) && oy) || ((k & 4) && oz)) m |= 1u << k;
+  return m;
+}
+
+// A cell is a candidate when it may carry a vertex: its lattice corners do
+// not all share a sign, or one of its off-lattice corners is within the
+// guard band of zero (its reference value could then have the other sign).
+template <bool CG = false>
+__device__ __forceinline__ bool s2_classify(const S2Job &j, const float *__restrict__ ring, S2Cell c) {
+  float v[8];
+  s2_load_corners<CG>(j, ring, c, v);
+  unsigned pos = 0;
+  for (int k = 0; k < 8; ++k) pos |= (v[k] > 0.0f ? 1u : 0u) << k;
+  if (pos != 0u && pos != 0xffu) return true;
+  if (j.qef) return false;  // precision mode uses the lattice values as they are
+  unsigned off = s2_off_mask(j, c);
+  if (!off) return false;
+  if (j.exact) return true;
+  for (int k = 1; k < 8; ++k)
+    if ((off >> k) & 1u)
+      if (!(fabsf(v[k]) >= j.guard)) return true;
+  return false;
+}
+
+// sdf3d_normal.wgsl:4-10 as a loop with one sdf3d call site:
+// n = ((t0 + t1) + t2) + t3 with t_i = d_i * sdf3d(p + d_i * eps), the order
+// the library function adds in.
+template <class F>
+__device__ __forceinline__ void s2_tetra_normal(const F &f, float px, float py, float pz, float eps, float n[3]) {
+#pragma unroll 1
+  for (int i = 0; i < 4; ++i) {
+    const float dx = (i == 0 || i == 3) ? 1.0f : -1.0f;
+    const float dy = (i >= 2) ? 1.0f : -1.0f;
+    const float dz = (i == 1 || i == 3) ? 1.0f : -1.0f;
+    const float v = f(__fadd_rn(px, __fmul_rn(dx, eps)), __fadd_rn(py, __fmul_rn(dy, eps)),
+                      __fadd_rn(pz, __fmul_rn(dz, eps)));
+    const float tx = __fmul_rn(dx, v), ty = __fmul_rn(dy, v), tz = __fmul_rn(dz, v);
+    if (i == 0) {
+      n[0] = tx; n[1] = ty; n[2] = tz;
+    } else {
+      n[0] = __fadd_rn(n[0], tx); n[1] = __fadd_rn(n[1], ty); n[2] = __fadd_rn(n[2], tz);
+    }
+  }
+}
+
+__device__ __forceinline__ float s2_len3(const float n[3]) {
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(n[0], n[0]), __fmul_rn(n[1], n[1])), __fmul_rn(n[2], n[2])));
+}
+
+// dualcontour.wgsl:72-131 (crossings, counting rule, mass point) and
+// :161-180 (normal, sign bits) on one candidate cell.  `v` holds the cell's
+// lattice values; corners whose reference coordinates are off the lattice are
+// re-evaluated here at those coordinates, so the rule sees exactly the
+// reference's 8 values.  Writes the vertex and returns the final key
+// (x | y << 16 | label << 32 | signs << 48 | has_vertex << 63).
+template <class F>
+__device__ __forceinline__ unsigned long long s2_vertex(const F &sdf, const S2Job &j, S2Cell c, float v[8],
+                                                        float pos[3], float nrm[3]) {
+  float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
+  float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
+  // Off-lattice corners, one sdf3d call site in a loop (a warp runs the
+  // largest count among its lanes instead of every inlined copy).
+  unsigned off = s2_off_mask(j, c) & 0xfeu;
+#pragma unroll 1
+  while (off) {
+    const int k = __ffs(off) - 1;
+    off &= off - 1u;
+    const float f = sdf((k & 1) ? mx[0] : mn[0], (k & 2) ? mx[1] : mn[1], (k & 4) ? mx[2] : mn[2]);
+#pragma unroll
+    for (int q = 1; q < 8; ++q)
+      if (q == k) v[q] = f;
+  }
+
+  // 12 edges in the reference order: 4 along z, 4 along y, 4 along x.
+  // Each: corner a, corner b, axis of t, the two fixed local coordinates.
+  const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
+  const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
+  const int eax[12] = {2, 2, 2, 2, 1, 1, 1, 1, 0, 0, 0, 0};
+  const float eu[12] = {0, 0, 1, 1, 0, 0, 1, 1, 0, 0, 1, 1};
+  const float ev[12] = {0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 0, 1};
+  float avg[3] = {0.0f, 0.0f, 0.0f};
+  float count = 0.0f;
+#pragma unroll
+  for (int e = 0; e < 12; ++e) {
+    float a = v[ea[e]], b = v[eb[e]];
+    if ((a > 0.0f) != (b > 0.0f)) {
+      float t = __fdiv_rn(__fsub_rn(0.0f, a), __fsub_rn(b, a));
+      float w[3];
+      if (eax[e] == 2) { w[0] = eu[e]; w[1] = ev[e]; w[2] = t; }
+      else if (eax[e] == 1) { w[0] = eu[e]; w[1] = t; w[2] = ev[e]; }
+      else { w[0] = t; w[1] = eu[e]; w[2] = ev[e]; }
+      if (w[0] > 0.0f || w[1] > 0.0f || w[2] > 0.0f) {
+        avg[0] = __fadd_rn(avg[0], w[0]);
+        avg[1] = __fadd_rn(avg[1], w[1]);
+        avg[2] = __fadd_rn(avg[2], w[2]);
+        count = __fadd_rn(count, 1.0f);
+      }
+    }
+  }
+  const unsigned signs = (v[1] > 0.0f ? 1u : 0u) | (v[2] > 0.0f ? 2u : 0u) | (v[4] > 0.0f ? 4u : 0u) | (v[0] > 0.0f ? 8u : 0u);
+  const unsigned long long zl = (unsigned long long)(j.lag ? c.z + 1 : c.z);
+  unsigned long long key = (unsigned long long)c.x | ((unsigned long long)c.y << 16) | (zl << 32) |
+                           ((unsigned long long)signs << 48);
+  if (!(count > 1.0f)) return key;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float bsize = __fsub_rn(mx[a], mn[a]);
+    pos[a] = __fadd_rn(mn[a], __fdiv_rn(__fmul_rn(bsize, avg[a]), count));
+  }
+  float n[3];
+  sdf.normal(pos[0], pos[1], pos[2], j.eps, n);
+  float len = s2_len3(n);
+  nrm[0] = __fdiv_rn(n[0], len);
+  nrm[1] = __fdiv_rn(n[1], len);
+  nrm[2] = __fdiv_rn(n[2], len);
+  return key | (1ull << 63);
+}
+
+// ---------------------------------------------------------------------------
+// Precision mode.  Corners are the lattice values (shared by neighbouring
+// cells, so signs agree and the mesh closes).  Every sign-change edge gives a
+// crossing q in cell-local coordinates (t as in dualcontour.wgsl:72-74) and
+// a unit normal (the SDF's gradient there); the vertex minimises
+// sum (n . (x - q))^2 around the mass point.  The normal-equation sums are
+// binary32 with Neumaier compensation; the 3x3 solve is binary64 (cyclic
+// Jacobi eigen-decomposition, eigenvalues below 0.1 of the largest dropped,
+// x = c + V D^+ V^T (A^T b - A c), clamped to the cell).
+
+struct S2KSum {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.0f; c = 0.0f; }
+  __device__ __forceinline__ void add(float x) {
+    float t = __fadd_rn(s, x);
+    if (fabsf(s) >= fabsf(x)) c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, t), x));
+    else c = __fadd_rn(c, __fadd_rn(__fsub_rn(x, t), s));
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
+};
+
+__device__ __forceinline__ void s2_jacobi3(double a[3][3], double v[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) v[i][k] = i == k ? 1.0 : 0.0;
+#pragma unroll 1
+  for (int sweep = 0; sweep < 24; ++sweep) {
+    double off = __dadd_rn(__dadd_rn(__dmul_rn(a[0][1], a[0][1]), __dmul_rn(a[0][2], a[0][2])), __dmul_rn(a[1][2], a[1][2]));
+    double diag = __dadd_rn(__dadd_rn(__dmul_rn(a[0][0], a[0][0]), __dmul_rn(a[1][1], a[1][1])), __dmul_rn(a[2][2], a[2][2]));
+    if (!(off > __dmul_rn(1e-30, diag))) break;
+#pragma unroll
+    for (int pq = 0; pq < 3; ++pq) {
+      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+      const double apq = a[p][q];
+      if (apq == 0.0) continue;
+      const double theta = __ddiv_rn(__dsub_rn(a[q][q], a[p][p]), __dmul_rn(2.0, apq));
+      const double t = __ddiv_rn(theta >= 0.0 ? 1.0 : -1.0,
+                                 __dadd_rn(fabs(theta), __dsqrt_rn(__dadd_rn(__dmul_rn(theta, theta), 1.0))));
+      const double cs = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(__dmul_rn(t, t), 1.0)));
+      const double sn = __dmul_rn(t, cs);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double akp = a[k][p], akq = a[k][q];
+        a[k][p] = __dsub_rn(__dmul_rn(cs, akp), __dmul_rn(sn, akq));
+        a[k][q] = __dadd_rn(__dmul_rn(sn, akp), __dmul_rn(cs, akq));
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double apk = a[p][k], aqk = a[q][k];
+        a[p][k] = __dsub_rn(__dmul_rn(cs, apk), __dmul_rn(sn, aqk));
+        a[q][k] = __dadd_rn(__dmul_rn(sn, apk), __dmul_rn(cs, aqk));
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = __dsub_rn(__dmul_rn(cs, vkp), __dmul_rn(sn, vkq));
+        v[k][q] = __dadd_rn(__dmul_rn(sn, vkp), __dmul_rn(cs, vkq));
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void s2_qef_solve(const double A[6], const double b[3], const double c[3], double x[3]) {
+  double a[3][3] = {{A[0], A[1], A[2]}, {A[1], A[3], A[4]}, {A[2], A[4], A[5]}};
+  double r[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    r[i] = __dsub_rn(b[i], __dadd_rn(__dadd_rn(__dmul_rn(a[i][0], c[0]), __dmul_rn(a[i][1], c[1])), __dmul_rn(a[i][2], c[2])));
+  double v[3][3];
+  s2_jacobi3(a, v);
+  const double lmax = fmax(fabs(a[0][0]), fmax(fabs(a[1][1]), fabs(a[2][2])));
+  double y[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double vr = __dadd_rn(__dadd_rn(__dmul_rn(v[0][k], r[0]), __dmul_rn(v[1][k], r[1])), __dmul_rn(v[2][k], r[2]));
+    const double l = a[k][k];
+    y[k] = (lmax > 0.0 && fabs(l) >= __dmul_rn(0.1, lmax)) ? __ddiv_rn(vr, l) : 0.0;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double d = __dadd_rn(__dadd_rn(__dmul_rn(v[i][0], y[0]), __dmul_rn(v[i][1], y[1])), __dmul_rn(v[i][2], y[2]));
+    const double xi = __dadd_rn(c[i], d);
+    x[i] = xi < 0.0 ? 0.0 : (xi > 1.0 ? 1.0 : xi);
+  }
+}
+
+template <class F>
+__device__ __forceinline__ unsigned long long s2_vertex_qef(const F &sdf, const S2Job &j, S2Cell c, const float v[8],
+                                                            float pos[3], float nrm[3]) {
+  const float lo[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
+  const float hi[3] = {s2_coord(j, c.x + 1), s2_coord(j, c.y + 1), s2_coord(j, c.z + 1)};
+  S2KSum sA[6], sb[3], sq[3];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) sA[i].init();
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { sb[i].init(); sq[i].init(); }
+  int m = 0;
+#pragma unroll 1
+  for (int e = 0; e < 12; ++e) {
+    // edges in the reference order: 4 along z, 4 along y, 4 along x
+    // corner indices of edge e's ends, one nibble per edge (dualcontour.wgsl:99-114)
+    const unsigned long long EA = 0x624051403120ull, EB = 0x735173627564ull;
+    const int a_ = int((EA >> (4 * e)) & 0xfull), b_ = int((EB >> (4 * e)) & 0xfull);
+    const int ax = e < 4 ? 2 : (e < 8 ? 1 : 0);
+    float va = 0.0f, vb = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k == a_) va = v[k];
+      if (k == b_) vb = v[k];
+    }
+    if ((va > 0.0f) == (vb > 0.0f)) continue;
+    const float t = __fdiv_rn(__fsub_rn(0.0f, va), __fsub_rn(vb, va));
+    float q[3], w[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d == ax) {
+        q[d] = t;
+        w[d] = __fadd_rn(lo[d], __fmul_rn(j.size, t));
+      } else {
+        const bool one = (a_ >> d) & 1;
+        q[d] = one ? 1.0f : 0.0f;
+        w[d] = one ? hi[d] : lo[d];
+      }
+    }
+    float n[3];
+    sdf.normal(w[0], w[1], w[2], j.eps, n);
+    const float len = s2_len3(n);
+    ++m;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sq[d].add(q[d]);
+    if (!(len > 0.0f)) continue;
+    const float nn[3] = {__fdiv_rn(n[0], len), __fdiv_rn(n[1], len), __fdiv_rn(n[2], len)};
+    const float dd = __fadd_rn(__fadd_rn(__fmul_rn(nn[0], q[0]), __fmul_rn(nn[1], q[1])), __fmul_rn(nn[2], q[2]));
+    sA[0].add(__fmul_rn(nn[0], nn[0]));
+    sA[1].add(__fmul_rn(nn[0], nn[1]));
+    sA[2].add(__fmul_rn(nn[0], nn[2]));
+    sA[3].add(__fmul_rn(nn[1], nn[1]));
+    sA[4].add(__fmul_rn(nn[1], nn[2]));
+    sA[5].add(__fmul_rn(nn[2], nn[2]));
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sb[d].add(__fmul_rn(nn[d], dd));
+  }
+  const unsigned signs = (v[1] > 0.0f ? 1u : 0u) | (v[2] > 0.0f ? 2u : 0u) | (v[4] > 0.0f ? 4u : 0u) | (v[0] > 0.0f ? 8u : 0u);
+  const unsigned long long zl = (unsigned long long)(j.lag ? c.z + 1 : c.z);
+  const unsigned long long key = (unsigned long long)c.x | ((unsigned long long)c.y << 16) | (zl << 32) |
+                                 ((unsigned long long)signs << 48);
+  if (m == 0) return key;
+  double A[6], b[3], cc[3], xs[3];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) A[i] = (double)sA[i].value();
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    b[d] = (double)sb[d].value();
+    cc[d] = __ddiv_rn((double)sq[d].value(), (double)m);
+  }
+  s2_qef_solve(A, b, cc, xs);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) pos[d] = __double2float_rn(__dadd_rn((double)lo[d], __dmul_rn((double)j.size, xs[d])));
+  float n[3];
+  sdf.normal(pos[0], pos[1], pos[2], j.eps, n);
+  const float len = s2_len3(n);
+  nrm[0] = __fdiv_rn(n[0], len);
+  nrm[1] = __fdiv_rn(n[1], len);
+  nrm[2] = __fdiv_rn(n[2], len);
+  return key | (1ull << 63);
+}
+

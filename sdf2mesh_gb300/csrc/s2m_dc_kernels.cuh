@@ -14,14 +14,18 @@
 // reference's 8 values.  All arithmetic of the vertex rule uses explicitly
 // rounded binary32 intrinsics (no contraction, whatever the SDF's flags).
 
-__device__ __forceinline__ float s2_coord(const S2Job &j, int i) {
-  return __fadd_rn(j.bmin, __fmul_rn(j.size, (float)i));
-}
-// 1 if mn(i - 1) + size differs (bitwise) from the lattice coordinate c(i).
-__device__ __forceinline__ unsigned s2_off_lattice(const S2Job &j, int i) {
-  float hi = __fadd_rn(s2_coord(j, i - 1), j.size);
-  return __float_as_uint(hi) != __float_as_uint(s2_coord(j, i)) ? 1u : 0u;
-}
+// The lowered user SDF as the evaluator of s2m_dc_core.cuh.
+struct S2UserSdf {
+  __device__ __forceinline__ float operator()(float x, float y, float z) const { return s2m_user_sdf(x, y, z); }
+  __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
+#ifdef S2M_STD_NORMAL
+    s2_tetra_normal(*this, px, py, pz, eps, n);
+#else
+    s2v3 r = s2m_user_normal(s2mk(px, py, pz), eps);
+    n[0] = r.x; n[1] = r.y; n[2] = r.z;
+#endif
+  }
+};
 
 // Evaluate planes k0 .. k0 + nk - 1 of the lattice into the ring.
 // grid.x covers the P * P points of a plane, grid.y runs of RUN planes; each
@@ -57,147 +61,6 @@ S2_EVAL_VARIANT(s2m_eval_b4r4, 4, 4)
 S2_EVAL_VARIANT(s2m_eval_b4r1, 4, 1)
 S2_EVAL_VARIANT(s2m_eval_b6r4, 6, 4)
 S2_EVAL_VARIANT(s2m_eval_b8r4, 8, 4)
-
-struct S2Cell {
-  int x, y, z;
-};
-
-__device__ __forceinline__ S2Cell s2_cell_of(const S2Job &j, long long c, int zc0) {
-  S2Cell r;
-  r.x = (int)(c % j.N);
-  long long q = c / j.N;
-  r.y = (int)(q % j.N);
-  r.z = zc0 + (int)(q / j.N);
-  return r;
-}
-
-// The 8 lattice values of a cell, corner index bx | by << 1 | bz << 2.
-__device__ __forceinline__ void s2_load_corners(const S2Job &j, const float *__restrict__ ring, S2Cell c, float v[8]) {
-  const float *p0 = ring + (long long)(c.z % j.ring) * j.plane + (long long)c.y * j.pitch + c.x;
-  const float *p1 = ring + (long long)((c.z + 1) % j.ring) * j.plane + (long long)c.y * j.pitch + c.x;
-  v[0] = __ldg(p0);
-  v[1] = __ldg(p0 + 1);
-  v[2] = __ldg(p0 + j.pitch);
-  v[3] = __ldg(p0 + j.pitch + 1);
-  v[4] = __ldg(p1);
-  v[5] = __ldg(p1 + 1);
-  v[6] = __ldg(p1 + j.pitch);
-  v[7] = __ldg(p1 + j.pitch + 1);
-}
-
-// Mask of corners whose reference coordinates are not lattice points.
-__device__ __forceinline__ unsigned s2_off_mask(const S2Job &j, S2Cell c) {
-  unsigned ox = s2_off_lattice(j, c.x + 1), oy = s2_off_lattice(j, c.y + 1), oz = s2_off_lattice(j, c.z + 1);
-  unsigned m = 0;
-  for (int k = 1; k < 8; ++k)
-    if (((k & 1) && ox) || ((k & 2) && oy) || ((k & 4) && oz)) m |= 1u << k;
-  return m;
-}
-
-// A cell is a candidate when it may carry a vertex: its lattice corners do
-// not all share a sign, or one of its off-lattice corners is within the
-// guard band of zero (its reference value could then have the other sign).
-__device__ __forceinline__ bool s2_classify(const S2Job &j, const float *__restrict__ ring, S2Cell c) {
-  float v[8];
-  s2_load_corners(j, ring, c, v);
-  unsigned pos = 0;
-  for (int k = 0; k < 8; ++k) pos |= (v[k] > 0.0f ? 1u : 0u) << k;
-  if (pos != 0u && pos != 0xffu) return true;
-  unsigned off = s2_off_mask(j, c);
-  if (!off) return false;
-  if (j.exact) return true;
-  for (int k = 1; k < 8; ++k)
-    if ((off >> k) & 1u)
-      if (!(fabsf(v[k]) >= j.guard)) return true;
-  return false;
-}
-
-// dualcontour.wgsl:72-131 (crossings, counting rule, mass point) and
-// :161-180 (normal, sign bits) on one candidate cell.  `v` holds the cell's
-// lattice values; corners whose reference coordinates are off the lattice are
-// re-evaluated here at those coordinates, so the rule sees exactly the
-// reference's 8 values.  Writes the vertex and returns the final key
-// (x | y << 16 | label << 32 | signs << 48 | has_vertex << 63).
-__device__ __forceinline__ unsigned long long s2_vertex(const S2Job &j, S2Cell c, float v[8], float pos[3],
-                                                        float nrm[3]) {
-  float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
-  float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
-  // Off-lattice corners, one sdf3d call site in a loop (a warp runs the
-  // largest count among its lanes instead of every inlined copy).
-  unsigned off = s2_off_mask(j, c) & 0xfeu;
-#pragma unroll 1
-  while (off) {
-    const int k = __ffs(off) - 1;
-    off &= off - 1u;
-    const float f = s2m_user_sdf((k & 1) ? mx[0] : mn[0], (k & 2) ? mx[1] : mn[1], (k & 4) ? mx[2] : mn[2]);
-#pragma unroll
-    for (int q = 1; q < 8; ++q)
-      if (q == k) v[q] = f;
-  }
-
-  // 12 edges in the reference order: 4 along z, 4 along y, 4 along x.
-  // Each: corner a, corner b, axis of t, the two fixed local coordinates.
-  const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
-  const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
-  const int eax[12] = {2, 2, 2, 2, 1, 1, 1, 1, 0, 0, 0, 0};
-  const float eu[12] = {0, 0, 1, 1, 0, 0, 1, 1, 0, 0, 1, 1};
-  const float ev[12] = {0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 0, 1};
-  float avg[3] = {0.0f, 0.0f, 0.0f};
-  float count = 0.0f;
-#pragma unroll
-  for (int e = 0; e < 12; ++e) {
-    float a = v[ea[e]], b = v[eb[e]];
-    if ((a > 0.0f) != (b > 0.0f)) {
-      float t = __fdiv_rn(__fsub_rn(0.0f, a), __fsub_rn(b, a));
-      float w[3];
-      if (eax[e] == 2) { w[0] = eu[e]; w[1] = ev[e]; w[2] = t; }
-      else if (eax[e] == 1) { w[0] = eu[e]; w[1] = t; w[2] = ev[e]; }
-      else { w[0] = t; w[1] = eu[e]; w[2] = ev[e]; }
-      if (w[0] > 0.0f || w[1] > 0.0f || w[2] > 0.0f) {
-        avg[0] = __fadd_rn(avg[0], w[0]);
-        avg[1] = __fadd_rn(avg[1], w[1]);
-        avg[2] = __fadd_rn(avg[2], w[2]);
-        count = __fadd_rn(count, 1.0f);
-      }
-    }
-  }
-  const unsigned signs = (v[1] > 0.0f ? 1u : 0u) | (v[2] > 0.0f ? 2u : 0u) | (v[4] > 0.0f ? 4u : 0u) | (v[0] > 0.0f ? 8u : 0u);
-  const unsigned long long zl = (unsigned long long)(j.lag ? c.z + 1 : c.z);
-  unsigned long long key = (unsigned long long)c.x | ((unsigned long long)c.y << 16) | (zl << 32) |
-                           ((unsigned long long)signs << 48);
-  if (!(count > 1.0f)) return key;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    float bsize = __fsub_rn(mx[a], mn[a]);
-    pos[a] = __fadd_rn(mn[a], __fdiv_rn(__fmul_rn(bsize, avg[a]), count));
-  }
-#ifdef S2M_STD_NORMAL
-  // sdf3d_normal.wgsl:4-10 as a loop: n = ((t0 + t1) + t2) + t3 with
-  // t_i = d_i * sdf3d(p + d_i * eps), the order the library function adds in.
-  s2v3 n;
-#pragma unroll 1
-  for (int i = 0; i < 4; ++i) {
-    const float dx = (i == 0 || i == 3) ? 1.0f : -1.0f;
-    const float dy = (i >= 2) ? 1.0f : -1.0f;
-    const float dz = (i == 1 || i == 3) ? 1.0f : -1.0f;
-    const float f = s2m_user_sdf(__fadd_rn(pos[0], __fmul_rn(dx, j.eps)), __fadd_rn(pos[1], __fmul_rn(dy, j.eps)),
-                                 __fadd_rn(pos[2], __fmul_rn(dz, j.eps)));
-    const float tx = __fmul_rn(dx, f), ty = __fmul_rn(dy, f), tz = __fmul_rn(dz, f);
-    if (i == 0) {
-      n.x = tx; n.y = ty; n.z = tz;
-    } else {
-      n.x = __fadd_rn(n.x, tx); n.y = __fadd_rn(n.y, ty); n.z = __fadd_rn(n.z, tz);
-    }
-  }
-#else
-  s2v3 n = s2m_user_normal(s2mk(pos[0], pos[1], pos[2]), j.eps);
-#endif
-  float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(n.x, n.x), __fmul_rn(n.y, n.y)), __fmul_rn(n.z, n.z)));
-  nrm[0] = __fdiv_rn(n.x, len);
-  nrm[1] = __fdiv_rn(n.y, len);
-  nrm[2] = __fdiv_rn(n.z, len);
-  return key | (1ull << 63);
-}
 
 // Cell pass of one slab (cell slices zc0 .. zc1 - 1): classify every cell and
 // append the candidates, in (z, y, x) order, to the job's candidate list at
@@ -272,7 +135,8 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
     float4 a = src[0], b = src[1];
     float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     float pos[3], nrm[3];
-    unsigned long long key = s2_vertex(job, c, v, pos, nrm);
+    const S2UserSdf sdf;
+    unsigned long long key = job.qef ? s2_vertex_qef(sdf, job, c, v, pos, nrm) : s2_vertex(sdf, job, c, v, pos, nrm);
     cand.key[o] = key;
     if (key >> 63) {
       cand.pos[3 * o] = pos[0];

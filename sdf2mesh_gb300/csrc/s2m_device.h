@@ -21,6 +21,7 @@ struct S2Job {
   float guard;             // |f| below which off-lattice corners are re-evaluated
   int lag;                 // 1: labels are z + 1 (reference slice lag)
   int exact;               // 1: re-evaluate off-lattice corners of every cell
+  int qef;                 // 1: precision mode (lattice corners, QEF vertex, FP64 solve)
 };
 
 // Per-slab buffers of the cell pass.

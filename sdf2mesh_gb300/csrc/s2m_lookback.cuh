@@ -30,6 +30,12 @@ __device__ __forceinline__ unsigned s2_lanemask_lt() {
   return m;
 }
 
+// Loads of data that other blocks of the same launch wrote: cached in L2
+// only, never served from a stale L1 line.
+__device__ __forceinline__ unsigned long long s2_ldcg(const unsigned long long *p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned s2_ldcg(const unsigned *p) { return __ldcg(p); }
+__device__ __forceinline__ float s2_ldcg(const float *p) { return __ldcg(p); }
+
 // Called by all 32 lanes of one warp; returns the exclusive prefix of
 // `aggregate` over tiles 0 .. tile-1 (the same value in every lane).
 __device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *status, unsigned tile,

@@ -226,3 +226,66 @@ def test_autotuner_picks_a_variant(lib):
     run(sdf, 512)  # large enough for the tuner to time (>= 2e6 points per trial)
     name, ns = sdf.eval_variant()
     assert name.startswith("s2m_eval_") and all(x > 0 for x in ns)
+
+
+# ---------------------------------------------------------------------------
+# Precision mode (S2M_JOB_QEF): lattice corners, QEF vertex, FP32 compensated
+# sums, FP64 solve.  The oracle's binary32 build runs the same arithmetic, so
+# correctly rounded SDFs match it bit for bit; the all-binary64 oracle is the
+# accuracy yardstick: topology equal outside tie cells and every common vertex
+# within QEF_TOL_CELLS cell sizes.
+QEF_TOL_CELLS = 1e-3
+
+
+@pytest.mark.parametrize("case", ["torus64", "torus128", "csg96", "tree2", "tree3", "tree7"])
+def test_qef_bit_exact_with_oracle(lib, case):
+    if case.startswith("torus"):
+        src, prm = workloads.torus()
+        kind, N = oracle.TORUS, int(case[5:])
+    elif case == "csg96":
+        src, prm = workloads.csg64(seed=0)
+        kind, N = oracle.CSG, 96
+    else:
+        src, prm = workloads.random_tree(int(case[4:]))
+        kind, N = oracle.TREE, 64
+    gpu = run(s2m.Sdf3DShader.from_source(src).compile(), N, qef=True)
+    ref = oracle.mesh(kind, prm, N, 2.0, qef=True)
+    assert ref.nverts > 100
+    assert_bit_exact(gpu, ref, f"qef {case}")
+
+
+def test_qef_against_fp64_oracle(lib):
+    src, prm = workloads.csg64(seed=0)
+    N = 128
+    gpu = run(s2m.Sdf3DShader.from_source(src).compile(), N, qef=True)
+    ref = oracle.mesh(oracle.CSG, prm, N, 2.0, qef=True, precision=oracle.F64)
+    h = 2.0 / (N - 1)
+    r = compare_with_ties(gpu, ref, oracle.CSG, prm, N, 2.0, eps=1e-6, h=h)
+    assert r["tri_diff_unexplained"] == 0, r
+    assert r["max_pos_err_cells"] < QEF_TOL_CELLS, r
+
+
+def test_qef_mandelbulb_vs_fp64(lib):
+    src, prm = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
+    N, B = 96, 2.5
+    gpu = run(s2m.Sdf3DShader.from_source(src, s2m.LANG_GLSL, "sdf").compile(), N, B, qef=True)
+    ref = oracle.mesh(oracle.MANDELBULB, prm, N, B, qef=True, precision=oracle.F64)
+    r = compare_with_ties(gpu, ref, oracle.MANDELBULB, prm, N, B, eps=1e-5, h=B / (N - 1))
+    assert r["tri_diff_unexplained"] == 0, r
+    assert r["vertex_only_one_side"] <= max(5, ref.nverts // 1000), r
+
+
+def test_qef_1024_watertight(lib):
+    """Precision mode closes the reference rule's holes: at 1024^3 the CSG mesh
+    has no invalid quad and every edge is shared by exactly two triangles."""
+    from tests.parity import reference_quads
+    src, _ = workloads.csg64(seed=0)
+    gpu = run(s2m.Sdf3DShader.from_source(src).compile(), 1024, qef=True)
+    assert gpu.invalid_quads == 0
+    tris, invalid, _ = reference_quads(gpu.cell_xyz, gpu.signs)
+    assert invalid == 0 and np.array_equal(tris, gpu.triangle_indices)
+    t = gpu.triangle_indices.astype(np.int64)
+    e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
+    e.sort(axis=1)
+    _, counts = np.unique(e[:, 0] * np.int64(1 << 32) + e[:, 1], return_counts=True)
+    assert (counts == 2).all()

@@ -162,3 +162,29 @@ def test_numpy_quad_rule_matches_oracle(oracle_lib, case):
     tris, invalid, _ = reference_quads(m.cell, m.signs)
     assert invalid == m.invalid_quads
     assert np.array_equal(tris, m.tris)
+
+
+@pytest.mark.parametrize("N", [32, 96])
+def test_qef_precision_mode_known_answers(oracle_lib, N):
+    """Precision mode: lattice corners (neighbours agree), QEF vertex with a
+    binary64 solve.  Closed, oriented torus (genus 1), vertices within a cell
+    of the analytic surface and no farther than the mass point's, binary32
+    sums within 1e-3 cells of the all-binary64 rule."""
+    R, r = 0.5, 0.2
+    a = oracle.mesh(oracle.TORUS, [R, r], N, 2.0, qef=True)
+    b = oracle.mesh(oracle.TORUS, [R, r], N, 2.0, qef=True, precision=oracle.F64)
+    mp = oracle.mesh(oracle.TORUS, [R, r], N, 2.0)
+    h = 2.0 / (N - 1)
+
+    def dist(p):
+        p = p.astype(np.float64)
+        q = np.sqrt(p[:, 0] ** 2 + p[:, 2] ** 2) - R
+        return np.abs(np.sqrt(q ** 2 + p[:, 1] ** 2) - r)
+
+    assert dist(a.pos).max() < 0.25 * h
+    assert dist(a.pos).max() <= dist(mp.pos).max() * 1.05
+    s = manifold_stats(a)
+    assert (s["counts"] == 2).all() and s["oriented"] and a.invalid_quads == 0
+    assert a.nverts - s["E"] + s["F"] == 0
+    assert np.array_equal(a.cell, b.cell)
+    assert np.abs(a.pos - b.pos).max() < 1e-3 * h
