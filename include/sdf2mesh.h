@@ -189,6 +189,52 @@ int s2m_mesh_set_profiling(s2m_mesh *mesh, int enable);
 int s2m_mesh_get_profile(const s2m_mesh *mesh, s2m_profile *out);
 int s2m_mesh_reset_profile(s2m_mesh *mesh);
 
+/* ---- meshing without device allocation ---------------------------------
+   No counterpart in the reference: an addition for callers that may not
+   allocate device memory while they mesh -- programs that reserve the GPU's
+   memory up front in their own arena (renderers, simulators, engines with a
+   fixed memory plan), that run under a hard memory quota, or that must not
+   pay the device-wide synchronisation a cudaMalloc / cudaFree can cause in
+   the middle of a frame or a timed loop.
+
+   s2m_mesh_noalloc meshes one job like s2m_mesh_create, but every scratch
+   buffer of the pipeline (lattice planes, candidate cells, scan words,
+   counters) lives in one fixed array of S2M_NOALLOC_SCRATCH_BYTES inside the
+   library, which every GPU that loads the library holds until the process
+   exits.  The caller allocates the outputs (device memory) and the library
+   allocates nothing: no cudaMalloc, cudaFree or allocating library call.
+   Compile the SDF beforehand (s2m_compile loads a module, which allocates).
+
+   Limits: resolution <= S2M_NOALLOC_MAX_RESOLUTION (larger is rejected with
+   S2M_E_INVALID before any device work); the surface must fit the scratch's
+   candidate-cell capacity (S2M_E_OVERFLOW otherwise).  If the caller's
+   vertex or triangle capacity is too small the call returns S2M_E_OVERFLOW
+   with the exact nverts / ntris needed.
+   Concurrency: every call shares the one array, so calls whose device work
+   overlaps (other host threads, or other streams without ordering between
+   them) race; serialise them.  The first call on a device looks up the
+   array's device address (cudaGetSymbolAddress) with that device current;
+   make that first call before any stream capture.  The call synchronises
+   `stream` (it reads the counts back). */
+#define S2M_NOALLOC_SCRATCH_BYTES (64u << 20)
+#define S2M_NOALLOC_MAX_RESOLUTION 256u
+typedef struct {
+  float *pos;              /* in: device, 3 * max_vertices floats          */
+  float *nrm;              /* in: device, 3 * max_vertices floats          */
+  uint64_t *cell;          /* in: device, max_vertices keys (as s2m_mesh_info.d_cell) */
+  uint32_t *tris;          /* in: device, 3 * max_triangles indices        */
+  uint64_t max_vertices;   /* in                                           */
+  uint64_t max_triangles;  /* in                                           */
+  uint64_t nverts;         /* out (exact, also on S2M_E_OVERFLOW)          */
+  uint64_t ntris;          /* out (exact when the vertices fit)            */
+  uint64_t invalid_quads;  /* out                                          */
+  uint64_t candidate_cells;/* out                                          */
+  uint32_t resolution;     /* out: N used                                  */
+  uint32_t reserved;
+} s2m_noalloc_mesh;
+int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_mesh *out, void *stream,
+                     char *err, size_t errlen);
+
 /* ---- batching: many jobs in one persistent launch -----------------------
    No reference counterpart (the reference meshes one SDF per process run).
    A batch job is a CSG program: a postfix list of floats, each opcode

@@ -66,6 +66,17 @@ class MeshInfo(ctypes.Structure):
     ]
 
 
+class NoallocMesh(ctypes.Structure):
+    """s2m_noalloc_mesh: caller-owned device outputs and the counts written back."""
+    _fields_ = [("pos", ctypes.c_void_p), ("nrm", ctypes.c_void_p), ("cell", ctypes.c_void_p),
+                ("tris", ctypes.c_void_p), ("max_vertices", ctypes.c_uint64), ("max_triangles", ctypes.c_uint64),
+                ("nverts", ctypes.c_uint64), ("ntris", ctypes.c_uint64), ("invalid_quads", ctypes.c_uint64),
+                ("candidate_cells", ctypes.c_uint64), ("resolution", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+NOALLOC_SCRATCH_BYTES = 64 << 20
+NOALLOC_MAX_RESOLUTION = 256
+
 KERNEL_KINDS = ("eval_planes", "cells", "vertices", "vcompact", "rowscan", "quads")
 
 
@@ -121,6 +132,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_write_stl": ([vp, vp, u64, ctypes.c_char_p], i),
             "s2m_write_ply": ([vp, vp, u64, vp, u64, ctypes.c_char_p], i),
             "s2m_measure_fp32_peak": ([dp, vp], i),
+            "s2m_mesh_noalloc": ([vp, ctypes.POINTER(Params), ctypes.POINTER(NoallocMesh), vp, ctypes.c_char_p, sz],
+                                 i),
             "s2m_mesh_set_profiling": ([vp, i], i),
             "s2m_batch_create": ([ctypes.POINTER(vp), u64], i),
             "s2m_batch_add_csg": ([vp, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(Params),

@@ -506,6 +506,56 @@ int readback(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
 }  // namespace
 
 // ===========================================================================
+// Meshing without device allocation: the pipeline's scratch in one fixed
+// array.  In host code `s2m_noalloc_scratch` names a host-side stand-in, not
+// device memory, so its device address is looked up once per device and
+// passed to the kernels as a pointer.
+
+static __device__ __align__(256) unsigned char s2m_noalloc_scratch[S2M_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+int noalloc_scratch(unsigned char **ptr, char *err, size_t errlen) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_err(err, errlen, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return S2M_E_NO_DEVICE;
+  }
+  if (dev < 0 || dev >= kNoallocMaxDevices) {
+    set_err(err, errlen, "device ordinal beyond the no-allocation table");
+    return S2M_E_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, s2m_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_err(err, errlen, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+      return S2M_E_CUDA;
+    }
+    g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return S2M_OK;
+}
+
+// Carve `bytes` (rounded up to 256) off the scratch; false when it is full.
+template <class T> bool carve(unsigned char *base, size_t &used, size_t count, T **out) {
+  size_t bytes = (count * sizeof(T) + 255) / 256 * 256;
+  if (used + bytes > size_t(S2M_NOALLOC_SCRATCH_BYTES)) return false;
+  *out = reinterpret_cast<T *>(base + used);
+  used += bytes;
+  return true;
+}
+
+}  // namespace
+
+// ===========================================================================
 // C ABI
 
 extern "C" {
@@ -750,6 +800,107 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
     return rc;
   }
   *out = m;
+  return S2M_OK;
+}
+
+int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_mesh *out, void *stream,
+                     char *err, size_t errlen) {
+  if (!sdf || !params || !out || !out->pos || !out->nrm || !out->cell || !out->tris) {
+    set_err(err, errlen, "null argument");
+    return S2M_E_INVALID;
+  }
+  s2m_mesh m;  // host bookkeeping only; every device pointer below is scratch or the caller's
+  m.sdf = sdf;
+  m.params = *params;
+  if (!(m.params.eps > 0.0f)) m.params.eps = 1e-4f;
+  // Slabs of at most 8 cell slices keep the lattice ring small.
+  if (m.params.slab_depth == 0 || m.params.slab_depth > 8) m.params.slab_depth = 8;
+  int rc = setup_job(&m, err, errlen);
+  if (rc != S2M_OK) return rc;
+  if (uint32_t(m.N) > S2M_NOALLOC_MAX_RESOLUTION) {
+    set_err(err, errlen, "resolution " + std::to_string(m.N) + " exceeds the no-allocation limit of " +
+                             std::to_string(S2M_NOALLOC_MAX_RESOLUTION));
+    return S2M_E_INVALID;
+  }
+  out->resolution = uint32_t(m.N);
+  unsigned char *base = nullptr;
+  rc = noalloc_scratch(&base, err, errlen);
+  if (rc != S2M_OK) return rc;
+
+  const S2Job &j = m.job;
+  const unsigned long long N = (unsigned long long)m.N;
+  const unsigned long long cells_per_slab = (unsigned long long)m.D * N * N;
+  m.cell_tiles = (cells_per_slab + S2_CELL_TILE - 1) / S2_CELL_TILE;
+  m.slab_ctrl_words = m.cell_tiles + 1;
+  m.scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
+  size_t used = 0;
+  bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
+            carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
+            carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
+            carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
+            carve(base, used, size_t(8), &m.jobctl);
+  if (!ok) {
+    set_err(err, errlen, "no-allocation scratch too small for this job");
+    return S2M_E_INVALID;
+  }
+  // The rest holds the candidate list and its scan words: 64 bytes per
+  // candidate plus one scan word per S2_VC_TILE candidates and one quad
+  // scan word per S2_Q_TILE vertices (vertices never outnumber candidates).
+  size_t left = size_t(S2M_NOALLOC_SCRATCH_BYTES) - used;
+  const double per_cand = 64.0 + 8.0 / S2_VC_TILE + 8.0 / S2_Q_TILE;
+  unsigned long long cap = (unsigned long long)((double(left) - 8 * 256.0 - 8.0 * double(m.scan_tiles)) / per_cand);
+  cap = cap / 1024 * 1024;
+  m.cand_cap = cap;
+  m.vc_tiles = (cap + S2_VC_TILE - 1) / S2_VC_TILE;
+  m.vcap = std::min<unsigned long long>(out->max_vertices, cap);
+  m.tcap = out->max_triangles;
+  m.quad_tiles = (m.vcap + S2_Q_TILE - 1) / S2_Q_TILE;
+  ok = carve(base, used, size_t(cap), &m.cand_key) && carve(base, used, size_t(cap) * 8, &m.cand_val) &&
+       carve(base, used, size_t(cap) * 3, &m.cand_pos) && carve(base, used, size_t(cap) * 3, &m.cand_nrm) &&
+       carve(base, used, size_t(m.vc_tiles), &m.cand_status) &&
+       carve(base, used, size_t(m.scan_tiles + m.quad_tiles), &m.scan_status);
+  if (!ok || cap == 0) {
+    set_err(err, errlen, "no-allocation scratch layout failed");
+    return S2M_E_INVALID;
+  }
+  m.pos = out->pos;
+  m.nrm = out->nrm;
+  m.key = reinterpret_cast<unsigned long long *>(out->cell);
+  m.tris = out->tris;
+  unsigned long long counts[8] = {0};
+  m.h_read = counts;  // pageable host words for the count read-back
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = enqueue(&m, st);
+  if (e != cudaSuccess) {
+    set_err(err, errlen, std::string("launch: ") + cudaGetErrorString(e));
+    return S2M_E_CUDA;
+  }
+  rc = readback(&m, st, err, errlen);
+  m.h_read = nullptr;
+  if (rc != S2M_OK) return rc;
+  out->nverts = m.nverts;
+  out->ntris = m.ntris;
+  out->invalid_quads = m.invalid;
+  out->candidate_cells = m.ncand;
+  if (m.errflags & S2_ERR_LOOKBACK) {
+    set_err(err, errlen, "a device-side look-back wait hit its limit");
+    return S2M_E_TIMEOUT;
+  }
+  if (m.errflags & S2_ERR_CAND_OVF) {
+    set_err(err, errlen, "the surface has " + std::to_string(m.ncand) + " candidate cells; the scratch holds " +
+                             std::to_string(cap));
+    return S2M_E_OVERFLOW;
+  }
+  if (m.errflags & (S2_ERR_VERT_OVF | S2_ERR_INDEX_OVF)) {
+    set_err(err, errlen, "the mesh has " + std::to_string(m.nverts) + " vertices; the output holds " +
+                             std::to_string(out->max_vertices));
+    return S2M_E_OVERFLOW;
+  }
+  if (m.errflags & S2_ERR_TRI_OVF) {
+    set_err(err, errlen, "the mesh has " + std::to_string(m.ntris) + " triangles; the output holds " +
+                             std::to_string(out->max_triangles));
+    return S2M_E_OVERFLOW;
+  }
   return S2M_OK;
 }
 
