@@ -67,11 +67,31 @@ def dist_env():
 
 # name -> (resolution, bounds, precision mode, description)
 WORKLOADS = {
+    "batch256": (0, 2.0, False, "256 seeded random CSG trees (sphere/box/torus/capsule; union/subtract/intersect/"
+                                "smooth-min), resolutions log-uniform over {64,96,128,192,256,384}"),
+    "serve": (0, 2.0, False, "Poisson arrivals (seeded), 90% random CSG trees + 10% Mandelbulbs, resolution "
+                             "round(exp U(ln 64, ln 1024)), 120 GB admission budget"),
     "csg64_1024": (1024, 2.0, False, "rounded box - smooth union (k=0.02) of 64 spheres (splitmix64 seed 0) + torus"),
     "mandelbulb_2048": (2048, 2.5, True, "Mandelbulb power 8, 8 iterations, bailout 2 (GLSL), precision mode: "
                                          "QEF vertex, FP32 compensated sums, FP64 solve"),
 }
 _ACTIVE = {"name": "csg64_1024"}
+
+
+def reduce_max(value: float, device=None) -> float:
+    """Max over ranks (replicas: the job-wide time is the slowest rank's)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard(items, rank: int, world: int):
+    """Jobs of one rank: round-robin, disjoint, together complete (no data-path collective)."""
+    return items[rank::world]
 
 
 def workload():
@@ -265,11 +285,7 @@ def ours(a):
     step_ms = [s.elapsed_time(e) for s, e in evs]
     tot_ms = sum(step_ms)
     prof = mesh.profile()
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
+    tot_ms = reduce_max(tot_ms, dev)
     voxels_step = float(N) ** 3
     value = voxels_step * a.steps * ws / (tot_ms * 1e-3) / 1e9
 
@@ -305,11 +321,7 @@ def ours(a):
         d2h = nverts * (12 + 12 + 8) + ntris * 12
     barrier()
     e2e_tot = sum(e2e_ms)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_tot], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_tot = float(t.item())
+    e2e_tot = reduce_max(e2e_tot, dev)
     e2e_value = voxels_step * a.steps * ws / (e2e_tot * 1e-3) / 1e9
 
     if rank != 0:
@@ -399,8 +411,190 @@ def ours(a):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Batching and serving workloads (spec changes (2) and (3)).
+
+
+def batch_jobs(n=256, seed=4):
+    from sdf2mesh_gb300 import workloads
+    rng = workloads.SplitMix64(seed)
+    jobs = []
+    for i in range(n):
+        src, prog = workloads.random_tree(i)
+        N = workloads.log_uniform_resolution(rng)
+        jobs.append((src, prog, N))
+    return jobs
+
+
+def plain_per_job(jobs, precompiled=None):
+    """The plain pipeline, one job at a time: compile the .sdf3d source (NVRTC) and mesh it
+    (s2m_mesh_create), or with `precompiled` modules only mesh it.  Returns seconds per job."""
+    import sdf2mesh_gb300 as s2m
+    t = time.perf_counter()
+    for k, (src, _, N) in enumerate(jobs):
+        sdf = precompiled[k] if precompiled else s2m.Sdf3DShader.from_source(src).compile()
+        m = s2m.mesh_device(sdf, s2m.AppState(resolution=N, bounds=2.0))
+        m.close()
+        if not precompiled:
+            sdf.close()
+    return (time.perf_counter() - t) / len(jobs)
+
+
+def batch_arm(a):
+    import torch
+    torch.cuda.set_device(0)
+    import sdf2mesh_gb300 as s2m
+    from sdf2mesh_gb300 import build as b
+    b.build()
+    jobs = batch_jobs()
+    voxels = float(sum(N ** 3 for _, _, N in jobs))
+
+    def one():
+        bt = s2m.Batch()
+        for _, prog, N in jobs:
+            bt.add_csg(prog, s2m.AppState(resolution=N, bounds=2.0))
+        t = time.perf_counter()
+        bt.run()
+        dt = time.perf_counter() - t
+        ms, launches, _ = bt.stats()
+        bt.close()
+        return dt, ms, launches
+
+    for _ in range(a.warmup):
+        one()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    res = [one() for _ in range(a.steps)]
+    clk = clocks.stop()
+    wall = sum(r[0] for r in res)
+    dev_ms = sum(r[1] for r in res)
+    launches = res[0][2]
+    # plain per-job pipeline on a bounded sample of the same jobs (first 32)
+    sample = jobs[:32]
+    plain_compile = plain_per_job(sample)
+    pre = [s2m.Sdf3DShader.from_source(src).compile() for src, _, _ in sample]
+    plain_per_job(sample[:4], pre[:4])  # warm (autotune, pools)
+    plain_mesh = plain_per_job(sample, pre)
+    sample_vox = float(sum(N ** 3 for _, _, N in sample)) / len(sample)
+    mps = len(jobs) * a.steps / wall
+    line = {
+        "metric": "meshes/s (batch of 256 CSG jobs)", "value": mps, "unit": "meshes/s", "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": wall / a.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch256", "jobs": len(jobs), "sdf": WORKLOADS["batch256"][3], "bounds": 2.0,
+                   "path": "s2m_batch_run: one persistent launch over a device work queue, CSG interpreter"},
+        "gvoxels_per_s": voxels * a.steps / wall / 1e9,
+        "device_ms_per_step": dev_ms / a.steps,
+        "gpu_launches": launches * a.steps,
+        "plain_per_job": {"meshes_per_s_with_compile": 1.0 / plain_compile, "meshes_per_s_precompiled": 1.0 / plain_mesh,
+                          "sample": "first 32 jobs of the same list, mean voxels per job %.3g vs %.3g in the batch"
+                                    % (sample_vox, voxels / len(jobs)),
+                          "speedup_vs_with_compile": mps / (1.0 / plain_compile),
+                          "speedup_vs_precompiled_same_mix": (voxels / len(jobs) / sample_vox) * mps / (1.0 / plain_mesh)},
+        "e2e": {"value": mps, "unit": "meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def serve_requests(rate, n, seed):
+    """Poisson arrivals at `rate` req/s: 90% random CSG trees, 10% Mandelbulbs."""
+    import math
+    from sdf2mesh_gb300 import workloads
+    rng = workloads.SplitMix64(seed)
+    t = 0.0
+    reqs = []
+    for i in range(n):
+        t += -math.log(1.0 - rng.u01()) / rate
+        N = int(round(math.exp(rng.uniform(math.log(64), math.log(1024)))))
+        if rng.u01() < 0.1:
+            reqs.append((t, "mandelbulb", None, None, N))
+        else:
+            src, prog = workloads.random_tree(int(rng.next() % 100000))
+            reqs.append((t, "csg", src, prog, N))
+    return reqs
+
+
+def serve_arm(a):
+    import threading
+    import torch
+    torch.cuda.set_device(0)
+    import sdf2mesh_gb300 as s2m
+    from sdf2mesh_gb300 import build as b
+    from sdf2mesh_gb300 import workloads
+    b.build()
+    mb_src, _ = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
+    mb = s2m.Sdf3DShader.from_source(mb_src, s2m.LANG_GLSL, "sdf").compile()
+    rates = [10, 30, 100, 300, 1000, 2000]
+    nreq = 48
+    table = []
+    for rate in rates:
+        reqs = serve_requests(rate, nreq, seed=rate)
+        # served: continuous batching
+        server = s2m.Server(memory_budget_bytes=120 << 30, max_inflight=2, max_batch_jobs=64, keep_results=False)
+        t0 = time.perf_counter()
+        for (t, kind, src, prog, N) in reqs:
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            st = s2m.AppState(resolution=N, bounds=2.5 if kind == "mandelbulb" else 2.0)
+            if kind == "csg":
+                server.submit_csg(prog, st)
+            else:
+                server.submit_sdf(mb, st)
+        server.drain(3600)
+        sst = server.stats()
+        server.close()
+        # plain per-job pipeline: one job at a time in arrival order, each compiling its source
+        lat = []
+        t0 = time.perf_counter()
+        for (t, kind, src, prog, N) in reqs:
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            if kind == "csg":
+                sdf = s2m.Sdf3DShader.from_source(src).compile()
+                m = s2m.mesh_device(sdf, s2m.AppState(resolution=N, bounds=2.0))
+            else:
+                sdf = s2m.Sdf3DShader.from_source(mb_src, s2m.LANG_GLSL, "sdf").compile()
+                m = s2m.mesh_device(sdf, s2m.AppState(resolution=N, bounds=2.5))
+            m.close()
+            sdf.close()
+            lat.append((time.perf_counter() - t0 - t) * 1e3)
+        span = time.perf_counter() - t0
+        lat.sort()
+        plain = {"meshes_per_s": len(reqs) / span, "p50_ms": lat[len(lat) // 2],
+                 "p99_ms": lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]}
+        table.append({"rate": rate, "served": {"meshes_per_s": sst["meshes_per_s"], "p50_ms": sst["p50_ms"],
+                                               "p99_ms": sst["p99_ms"], "launches": sst["batches"],
+                                               "gvoxels_per_s": sst["gvoxels_per_s"],
+                                               "peak_gb": sst["peak_bytes"] / 1e9},
+                      "plain_per_job": plain, "speedup": sst["meshes_per_s"] / plain["meshes_per_s"]})
+        print(json.dumps(table[-1]), file=sys.stderr, flush=True)
+    top = table[-1]
+    line = {
+        "metric": "served meshes/s (Poisson stream, 2000 req/s offered)", "value": top["served"]["meshes_per_s"],
+        "unit": "meshes/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
+        "ms_per_step": 1e3 / max(1e-9, top["served"]["meshes_per_s"]), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serve", "requests_per_rate": nreq, "rates": rates, "sdf": WORKLOADS["serve"][3],
+                   "plain_per_job": "one request at a time in arrival order: NVRTC compile of its source + "
+                                    "s2m_mesh_create"},
+        "p50_ms": top["served"]["p50_ms"], "p99_ms": top["served"]["p99_ms"],
+        "sweep": table,
+        "e2e": {"value": top["served"]["meshes_per_s"], "unit": "meshes/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.impl == "ours" and a.workload == "batch256":
+        return batch_arm(a)
+    if a.impl == "ours" and a.workload == "serve":
+        return serve_arm(a)
     _ACTIVE["name"] = a.workload
     if a.resolution is None:
         a.resolution = WORKLOADS[a.workload][0]

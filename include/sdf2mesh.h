@@ -186,6 +186,9 @@ typedef struct {
   double cells;            /* cells classified by kind-1 launches         */
 } s2m_profile;
 int s2m_mesh_set_profiling(s2m_mesh *mesh, int enable);
+/* Replay the mesh's launch sequence as a CUDA graph in s2m_mesh_run_async
+   (captured on the first run on a stream; not while profiling). */
+int s2m_mesh_set_graph(s2m_mesh *mesh, int enable);
 int s2m_mesh_get_profile(const s2m_mesh *mesh, s2m_profile *out);
 int s2m_mesh_reset_profile(s2m_mesh *mesh);
 
@@ -274,6 +277,44 @@ int s2m_batch_job_copy_to_host(const s2m_batch *b, uint32_t job, float *pos, flo
 int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, uint32_t *njobs);
 void s2m_batch_free(s2m_batch *b);
 
+/* ---- serving: continuous batching ---------------------------------------
+   No reference counterpart.  A request loop on its own host threads:
+   requests (CSG programs, or compiled SDFs) from any thread are admitted in
+   arrival order while their device footprint fits memory_budget_bytes and
+   fewer than max_inflight persistent launches run; each admitted group is one
+   launch on its own stream, so requests that arrive while others are on the
+   GPU start as soon as a slot and memory free up and overlap with them.
+   Compiled-SDF requests run the per-job pipeline on a third stream.
+   Latency = completion - submission (host clock). */
+typedef struct s2m_server s2m_server;
+typedef struct {
+  uint64_t memory_budget_bytes;  /* admission limit; 0 = none                         */
+  uint32_t max_inflight;         /* concurrent persistent launches (default 2)        */
+  uint32_t max_batch_jobs;       /* requests per launch (default 1024)                */
+  uint32_t keep_results;         /* 1: meshes stay on the device until s2m_server_release */
+  uint32_t reserved;
+} s2m_server_config;
+typedef struct {
+  uint64_t submitted, completed, failed, batches, peak_bytes;
+  double p50_ms, p99_ms, mean_ms;   /* latency of completed requests            */
+  double span_s;                    /* first submission to last completion      */
+  double meshes_per_s, gvoxels_per_s;
+} s2m_server_stats;
+int s2m_server_create(const s2m_server_config *cfg, s2m_server **out, char *err, size_t errlen);
+int s2m_server_submit_csg(s2m_server *s, const float *program, uint32_t len, const s2m_params *params,
+                          uint64_t *request_id, char *err, size_t errlen);
+int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *params, uint64_t *request_id,
+                          char *err, size_t errlen);
+/* S2M_OK once the request completed, S2M_E_TIMEOUT if it has not yet, or its error. */
+int s2m_server_wait(s2m_server *s, uint64_t request_id, double timeout_s, s2m_mesh_info *info, char *err,
+                    size_t errlen);
+int s2m_server_copy_to_host(s2m_server *s, uint64_t request_id, float *pos, float *nrm, uint64_t *cell,
+                            uint32_t *tris);
+int s2m_server_release(s2m_server *s, uint64_t request_id);
+int s2m_server_drain(s2m_server *s, double timeout_s);
+int s2m_server_get_stats(s2m_server *s, s2m_server_stats *out);
+void s2m_server_free(s2m_server *s);
+
 /* ---- host writers (mesh.rs:8-141) -------------------------------------- */
 
 /* ASCII STL with Rust `{}` float text, facet normal (v2-v0) x (v1-v0). */
@@ -289,6 +330,8 @@ int s2m_abi_version(void);
 /* Measured FP32 issue rate of the current device in Gop/s (one FP32 add or
    mul per lane per cycle), from a dependent-chain microkernel. */
 int s2m_measure_fp32_peak(double *gops, void *stream);
+/* Measured SFU (MUFU) issue rate in Gop/s, from a reciprocal-square-root chain. */
+int s2m_measure_sfu_peak(double *gops, void *stream);
 
 #ifdef __cplusplus
 }

@@ -25,7 +25,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = [
-    "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate", "Batch",
+    "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate", "Batch", "Server",
     "load_library", "translate", "wgsl_remove_function", "wgsl_rename_function", "wgsl_has_function",
     "LANG_WGSL", "LANG_GLSL", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "JOB_QEF", "COMPILE_FMAD",
 ]
@@ -76,6 +76,18 @@ class NoallocMesh(ctypes.Structure):
 
 NOALLOC_SCRATCH_BYTES = 64 << 20
 NOALLOC_MAX_RESOLUTION = 256
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
+                ("max_batch_jobs", ctypes.c_uint32), ("keep_results", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double), ("span_s", ctypes.c_double),
+                ("meshes_per_s", ctypes.c_double), ("gvoxels_per_s", ctypes.c_double)]
+
 
 KERNEL_KINDS = ("eval_planes", "cells", "vertices", "vcompact", "rowscan", "quads")
 
@@ -135,6 +147,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_mesh_noalloc": ([vp, ctypes.POINTER(Params), ctypes.POINTER(NoallocMesh), vp, ctypes.c_char_p, sz],
                                  i),
             "s2m_mesh_set_profiling": ([vp, i], i),
+            "s2m_mesh_set_graph": ([vp, i], i),
+            "s2m_measure_sfu_peak": ([dp, vp], i),
             "s2m_batch_create": ([ctypes.POINTER(vp), u64], i),
             "s2m_batch_add_csg": ([vp, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(Params),
                                    ctypes.POINTER(u32), ctypes.c_char_p, sz], i),
@@ -144,6 +158,16 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_batch_job_copy_to_host": ([vp, u32, vp, vp, vp, vp, vp], i),
             "s2m_batch_stats": ([vp, dp, ctypes.POINTER(u64), ctypes.POINTER(u32)], i),
             "s2m_batch_free": ([vp], None),
+            "s2m_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(vp), ctypes.c_char_p, sz], i),
+            "s2m_server_submit_csg": ([vp, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(Params),
+                                       ctypes.POINTER(u64), ctypes.c_char_p, sz], i),
+            "s2m_server_submit_sdf": ([vp, vp, ctypes.POINTER(Params), ctypes.POINTER(u64), ctypes.c_char_p, sz], i),
+            "s2m_server_wait": ([vp, u64, ctypes.c_double, ctypes.POINTER(MeshInfo), ctypes.c_char_p, sz], i),
+            "s2m_server_copy_to_host": ([vp, u64, vp, vp, vp, vp], i),
+            "s2m_server_release": ([vp, u64], i),
+            "s2m_server_drain": ([vp, ctypes.c_double], i),
+            "s2m_server_get_stats": ([vp, ctypes.POINTER(ServerStats)], i),
+            "s2m_server_free": ([vp], None),
             "s2m_mesh_get_profile": ([vp, ctypes.POINTER(Profile)], i),
             "s2m_mesh_reset_profile": ([vp], i),
         }
@@ -353,6 +377,10 @@ class DeviceMesh:
         err = _errbuf()
         _check(load_library().s2m_mesh_sync(self._h, ctypes.c_void_p(stream), err, len(err)), err, "sync")
 
+    def set_graph(self, enable: bool = True) -> None:
+        """Replay the pipeline as a CUDA graph in run_async."""
+        _check(load_library().s2m_mesh_set_graph(self._h, 1 if enable else 0), None, "graph")
+
     def set_profiling(self, enable: bool = True) -> None:
         """Record CUDA events around every kernel of later runs."""
         _check(load_library().s2m_mesh_set_profiling(self._h, 1 if enable else 0), None, "profiling")
@@ -503,6 +531,79 @@ class Batch:
             pass
 
 
+class Server:
+    """Continuous-batching request loop (s2m_server_*): submit CSG programs or
+    compiled SDFs from any thread; results complete asynchronously."""
+
+    def __init__(self, memory_budget_bytes: int = 0, max_inflight: int = 2, max_batch_jobs: int = 1024,
+                 keep_results: bool = True):
+        cfg = ServerConfig(memory_budget_bytes, max_inflight, max_batch_jobs, 1 if keep_results else 0, 0)
+        self._h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(load_library().s2m_server_create(ctypes.byref(cfg), ctypes.byref(self._h), err, len(err)), err,
+               "server")
+        self._keep = []
+
+    def submit_csg(self, program, state: AppState) -> int:
+        prog = np.ascontiguousarray(np.asarray(program, np.float32))
+        p = state.params()
+        rid = ctypes.c_uint64()
+        err = _errbuf()
+        _check(load_library().s2m_server_submit_csg(self._h, prog.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                     len(prog), ctypes.byref(p), ctypes.byref(rid), err, len(err)),
+               err, "submit")
+        return int(rid.value)
+
+    def submit_sdf(self, sdf: "CompiledSdf", state: AppState) -> int:
+        self._keep.append(sdf)
+        p = state.params()
+        rid = ctypes.c_uint64()
+        err = _errbuf()
+        _check(load_library().s2m_server_submit_sdf(self._h, sdf.handle, ctypes.byref(p), ctypes.byref(rid), err,
+                                                     len(err)), err, "submit")
+        return int(rid.value)
+
+    def wait(self, request: int, timeout_s: float = 600.0) -> MeshInfo:
+        mi = MeshInfo()
+        err = _errbuf()
+        _check(load_library().s2m_server_wait(self._h, request, timeout_s, ctypes.byref(mi), err, len(err)), err,
+               f"request {request}")
+        return mi
+
+    def mesh(self, request: int) -> "TriangleMesh":
+        mi = self.wait(request)
+        nv, nt = int(mi.nverts), int(mi.ntris)
+        pos = np.empty((nv, 3), np.float32)
+        nrm = np.empty((nv, 3), np.float32)
+        cell = np.empty(nv, np.uint64)
+        tris = np.empty((nt, 3), np.uint32)
+        _check(load_library().s2m_server_copy_to_host(self._h, request, pos.ctypes.data, nrm.ctypes.data,
+                                                       cell.ctypes.data, tris.ctypes.data), None, "copy")
+        return TriangleMesh(pos, nrm, tris, cell, int(mi.invalid_quads), mi)
+
+    def release(self, request: int) -> None:
+        load_library().s2m_server_release(self._h, request)
+
+    def drain(self, timeout_s: float = 3600.0) -> None:
+        _check(load_library().s2m_server_drain(self._h, timeout_s), None, "drain")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        load_library().s2m_server_get_stats(self._h, ctypes.byref(st))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self._h:
+            load_library().s2m_server_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def mesh_device(sdf, state: AppState, stream: int = 0) -> DeviceMesh:
     """Run the whole pipeline on the GPU; the mesh stays in device memory."""
     compiled = sdf.compile() if isinstance(sdf, Sdf3DShader) else sdf
@@ -522,6 +623,13 @@ def generate(sdf, state: AppState | None = None, stream: int = 0) -> TriangleMes
         return dm.to_host(stream)
     finally:
         dm.close()
+
+
+def measure_sfu_peak(stream: int = 0) -> float:
+    """Measured SFU (MUFU) issue rate of the current GPU, Gop/s."""
+    g = ctypes.c_double()
+    _check(load_library().s2m_measure_sfu_peak(ctypes.byref(g), ctypes.c_void_p(stream)), None, "sfu probe")
+    return g.value
 
 
 def measure_fp32_peak(stream: int = 0) -> float:

@@ -489,9 +489,16 @@ void job_sizes(const HostJob &h, size_t &zero_bytes, size_t &data_bytes) {
 
 }  // namespace
 
+// Pinned host words the results of one launch are copied into (reused).
+struct PinnedBlock {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
 struct s2m_batch {
   std::vector<HostJob> jobs;
-  std::vector<void *> arenas;  // one per run; results of a run's jobs live in its arena
+  std::vector<void *> arenas;  // one per launch; results of a launch's jobs live in its arena
+  std::vector<PinnedBlock> pinned_free;
   uint64_t budget = 0;
   int blocks_per_sm = 0;
   double last_ms = 0;
@@ -500,8 +507,31 @@ struct s2m_batch {
 
 namespace {
 
-// Run jobs `idx` in one persistent launch (new arena).  Returns S2M_OK or an error.
-int run_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, char *err, size_t errlen) {
+// One persistent launch in flight.
+struct Wave {
+  std::vector<int> idx;
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PinnedBlock res;  // S2BatchResult[idx.size()] then S2BatchCtl
+};
+
+int take_pinned(s2m_batch *b, size_t bytes, PinnedBlock &out) {
+  for (size_t i = 0; i < b->pinned_free.size(); ++i)
+    if (b->pinned_free[i].bytes >= bytes) {
+      out = b->pinned_free[i];
+      b->pinned_free.erase(b->pinned_free.begin() + long(i));
+      return S2M_OK;
+    }
+  out.bytes = std::max<size_t>(bytes, 1 << 18);
+  if (cudaHostAlloc(&out.p, out.bytes, cudaHostAllocDefault) != cudaSuccess) return S2M_E_OOM;
+  return S2M_OK;
+}
+
+// Enqueue jobs `idx` as one persistent launch on `st` (arena from the
+// stream-ordered allocator; nothing waits for the device).
+int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave &w, char *err, size_t errlen) {
   std::vector<size_t> zb(idx.size()), db(idx.size());
   size_t ztot = 0, dtot = 0;
   for (size_t i = 0; i < idx.size(); ++i) {
@@ -517,13 +547,18 @@ int run_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, char *e
   const size_t ctl_bytes = al(sizeof(S2BatchCtl));
   const size_t total = ztot + ctl_bytes + dtot + prog_bytes + jobs_bytes + segs_bytes + res_bytes;
   char *arena = nullptr;
-  cudaError_t e = cudaMalloc(&arena, total);
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&arena), total, st);
   if (e != cudaSuccess) {
+    cudaGetLastError();
     set_err(err, errlen, std::string("batch arena (") + std::to_string(total) + " bytes): " + cudaGetErrorString(e));
     return S2M_E_OOM;
   }
   b->arenas.push_back(arena);
   const int run_id = int(b->arenas.size()) - 1;
+  w.idx = idx;
+  w.arena = arena;
+  w.arena_bytes = total;
+  w.st = st;
 
   // host images of the job table, segments and programs
   std::vector<S2BatchJob> dj(idx.size());
@@ -639,17 +674,43 @@ int run_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, char *e
   S2B_CUDA(cudaEventRecord(e1, st));
   s2m_batch_results<<<unsigned((idx.size() + 127) / 128), 128, 0, st>>>(d_jobs, int(idx.size()), d_res);
   S2B_CUDA(cudaGetLastError());
-  std::vector<S2BatchResult> res(idx.size());
-  S2BatchCtl hctl;
-  S2B_CUDA(cudaMemcpyAsync(res.data(), d_res, idx.size() * sizeof(S2BatchResult), cudaMemcpyDeviceToHost, st));
-  S2B_CUDA(cudaMemcpyAsync(&hctl, d_ctl, sizeof(hctl), cudaMemcpyDeviceToHost, st));
-  S2B_CUDA(cudaStreamSynchronize(st));
+  const size_t rbytes = idx.size() * sizeof(S2BatchResult);
+  if (take_pinned(b, rbytes + sizeof(S2BatchCtl), w.res) != S2M_OK) {
+    set_err(err, errlen, "pinned result buffer");
+    return S2M_E_OOM;
+  }
+  S2B_CUDA(cudaMemcpyAsync(w.res.p, d_res, rbytes, cudaMemcpyDeviceToHost, st));
+  S2B_CUDA(cudaMemcpyAsync(static_cast<char *>(w.res.p) + rbytes, d_ctl, sizeof(S2BatchCtl), cudaMemcpyDeviceToHost,
+                           st));
+  w.e0 = e0;
+  w.e1 = e1;
+  S2B_CUDA(cudaEventRecord(w.e1, st));  // re-recorded after the copies: completion of the whole launch
+  return S2M_OK;
+#undef S2B_CUDA
+}
+
+bool wave_ready(const Wave &w) { return cudaEventQuery(w.e1) != cudaErrorNotReady; }
+
+// Wait for the launch and copy its results into the jobs.
+int finish_wave(s2m_batch *b, Wave &w, char *err, size_t errlen) {
+  cudaError_t e = cudaEventSynchronize(w.e1);
   float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  cudaEventElapsedTime(&ms, w.e0, w.e1);
+  cudaEventDestroy(w.e0);
+  cudaEventDestroy(w.e1);
+  w.e0 = w.e1 = nullptr;
+  if (e != cudaSuccess) {
+    set_err(err, errlen, std::string("batch launch: ") + cudaGetErrorString(e));
+    return S2M_E_CUDA;
+  }
   b->last_ms += ms;
   b->last_launches += 2;
+  const std::vector<int> &idx = w.idx;
+  const S2BatchResult *res = static_cast<const S2BatchResult *>(w.res.p);
+  const S2BatchCtl hctl = *reinterpret_cast<const S2BatchCtl *>(static_cast<const char *>(w.res.p) +
+                                                                 idx.size() * sizeof(S2BatchResult));
+  b->pinned_free.push_back(w.res);
+  w.res = PinnedBlock();
   if (hctl.err & S2_ERR_BATCH_WAIT) {
     set_err(err, errlen, "a batch stage wait hit its limit");
     return S2M_E_TIMEOUT;
@@ -664,7 +725,13 @@ int run_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, char *e
     h.ok = (h.err & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF | S2_ERR_LOOKBACK | S2_ERR_INDEX_OVF)) == 0;
   }
   return S2M_OK;
-#undef S2B_CUDA
+}
+
+int run_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, char *err, size_t errlen) {
+  Wave w;
+  int rc = launch_wave(b, idx, st, w, err, errlen);
+  if (rc != S2M_OK) return rc;
+  return finish_wave(b, w, err, errlen);
 }
 
 }  // namespace
@@ -839,8 +906,469 @@ int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, u
 
 void s2m_batch_free(s2m_batch *b) {
   if (!b) return;
-  for (void *a : b->arenas) cudaFree(a);
+  for (void *a : b->arenas) cudaFreeAsync(a, nullptr);
+  cudaStreamSynchronize(nullptr);
+  for (PinnedBlock &p : b->pinned_free) cudaFreeHost(p.p);
   delete b;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Serving: continuous batching.
+//
+// Requests (CSG programs, or compiled SDFs) are queued by any host thread.
+// The server thread admits queued requests while their device footprint fits
+// the memory budget and fewer than `max_inflight` persistent launches are
+// running, and launches each admitted group as one persistent kernel on its
+// own stream.  Requests that arrive while launches run are admitted as soon
+// as a slot and memory free up; the new launch then runs beside the one still
+// finishing, so their work overlaps on the device.  Compiled-SDF requests run
+// the per-job pipeline on a third stream from a second host thread.  A
+// request's latency is completion minus submission (host clock).
+
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <thread>
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct SReq {
+  uint64_t id = 0;
+  int kind = 0;  // 0 CSG program, 1 compiled SDF
+  std::vector<float> prog;
+  const s2m_sdf *sdf = nullptr;
+  s2m_params params{};
+  double t_submit = 0, t_done = 0;
+  int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+  int status = S2M_OK;
+  std::string msg;
+  uint64_t footprint = 0;
+  s2m_mesh_info info{};
+  int wave = -1;        // CSG: server wave holding the results
+  uint32_t job = 0;     // CSG: job index inside that wave's batch
+  s2m_mesh *mesh = nullptr;  // compiled SDF: the mesh handle
+  int attempts = 0;
+};
+
+struct SWave {
+  s2m_batch *b = nullptr;
+  Wave w;
+  std::vector<uint64_t> reqs;
+  int live = 0;        // requests of this wave whose results are still held
+  bool finished = false;
+  cudaStream_t st = nullptr;
+};
+
+uint64_t sdf_job_footprint(const s2m_params &p) {
+  const uint64_t N = p.resolution, n2 = N * N;
+  const uint64_t plane = (N + 1) * ((N + 32) / 32 * 32) * 4;
+  const uint64_t ring = std::min<uint64_t>(plane * 65, std::max<uint64_t>(2 * plane, 50000000ull));
+  return ring + n2 * (8 * 64 + 6 * 32 + 12 * 12 + 8 + 8) + (64u << 20);
+}
+
+}  // namespace
+
+struct s2m_server {
+  s2m_server_config cfg{};
+  std::mutex mu;
+  std::condition_variable cv, done_cv;
+  std::map<uint64_t, SReq> reqs;
+  std::deque<uint64_t> queue, sdf_queue;
+  std::vector<SWave> waves;
+  uint64_t next_id = 1;
+  uint64_t used_bytes = 0, peak_bytes = 0;
+  uint64_t submitted = 0, completed = 0, failed = 0, batches = 0;
+  double first_submit = 0, last_done = 0;
+  double voxels_done = 0;
+  std::vector<double> latencies_ms;
+  bool stop = false;
+  int inflight = 0;
+  cudaStream_t streams[2] = {nullptr, nullptr};
+  cudaStream_t sdf_stream = nullptr;
+  std::thread worker, sdf_worker;
+  int device = 0;
+};
+
+namespace {
+
+void server_release_locked(s2m_server *s, SReq &r) {
+  if (r.state != 2 && r.state != 3) return;
+  if (r.kind == 0 && r.wave >= 0) {
+    SWave &sw = s->waves[size_t(r.wave)];
+    if (--sw.live == 0 && sw.finished && sw.b) {
+      for (void *a : sw.b->arenas) cudaFreeAsync(a, sw.st);
+      sw.b->arenas.clear();
+      for (PinnedBlock &p : sw.b->pinned_free) cudaFreeHost(p.p);
+      sw.b->pinned_free.clear();
+      delete sw.b;
+      sw.b = nullptr;
+    }
+    r.wave = -1;
+  }
+  if (r.kind == 1 && r.mesh) {
+    s2m_mesh_free(r.mesh);
+    r.mesh = nullptr;
+  }
+  if (r.footprint) {
+    s->used_bytes -= std::min(s->used_bytes, r.footprint);
+    r.footprint = 0;
+  }
+}
+
+void server_complete_locked(s2m_server *s, SReq &r, int status, const std::string &msg) {
+  r.t_done = now_s();
+  r.status = status;
+  r.msg = msg;
+  if (status == S2M_OK) {
+    r.state = 2;
+    ++s->completed;
+    s->latencies_ms.push_back((r.t_done - r.t_submit) * 1e3);
+    s->voxels_done += double(r.info.cells);
+  } else {
+    r.state = 3;
+    ++s->failed;
+  }
+  s->last_done = r.t_done;
+  if (!s->cfg.keep_results) server_release_locked(s, r);
+}
+
+void server_loop(s2m_server *s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  char err[1024];
+  int next_stream = 0;
+  while (true) {
+    // 1. launches that finished
+    for (size_t wi = 0; wi < s->waves.size(); ++wi) {
+      SWave &sw = s->waves[wi];
+      if (sw.finished || !sw.b || !wave_ready(sw.w)) continue;
+      int rc = finish_wave(sw.b, sw.w, err, sizeof err);
+      sw.finished = true;
+      --s->inflight;
+      sw.live = 1;  // guard: the batch stays alive while its requests complete
+      for (size_t k = 0; k < sw.reqs.size(); ++k) {
+        SReq &r = s->reqs[sw.reqs[k]];
+        const HostJob &h = sw.b->jobs[k];
+        if (rc == S2M_OK && h.ok) {
+          s2m_batch_job_info(sw.b, uint32_t(k), &r.info);
+          r.wave = int(wi);
+          r.job = uint32_t(k);
+          ++sw.live;
+          server_complete_locked(s, r, S2M_OK, "");
+        } else if (rc == S2M_OK && r.attempts < 4 && !(h.err & (S2_ERR_LOOKBACK | S2_ERR_INDEX_OVF))) {
+          // buffers too small: queue again with the exact totals
+          const unsigned long long need_c = h.ncand + h.ncand / 16 + 4096;
+          const unsigned long long need_v = std::max<unsigned long long>(h.nverts + h.nverts / 16 + 4096, need_c);
+          r.params.max_vertices = need_v;
+          r.params.max_triangles = std::max<unsigned long long>(h.ntris + h.ntris / 16 + 4096, 2 * need_v + 4096);
+          s->used_bytes -= std::min(s->used_bytes, r.footprint);
+          r.footprint = 0;
+          r.state = 0;
+          s->queue.push_front(r.id);
+        } else {
+          server_complete_locked(s, r, rc == S2M_OK ? S2M_E_OVERFLOW : rc, rc == S2M_OK ? "overflow" : err);
+        }
+      }
+      if (--sw.live == 0 && sw.b) {
+        for (void *a : sw.b->arenas) cudaFreeAsync(a, sw.st);
+        sw.b->arenas.clear();
+        for (PinnedBlock &p : sw.b->pinned_free) cudaFreeHost(p.p);
+        sw.b->pinned_free.clear();
+        delete sw.b;
+        sw.b = nullptr;
+      }
+      s->done_cv.notify_all();
+    }
+    // 2. admission: a new launch when a slot is free
+    if (!s->queue.empty() && s->inflight < int(s->cfg.max_inflight)) {
+      s2m_batch *b = new s2m_batch();
+      std::vector<uint64_t> ids;
+      uint64_t add = 0;
+      while (!s->queue.empty() && ids.size() < s->cfg.max_batch_jobs) {
+        SReq &r = s->reqs[s->queue.front()];
+        uint32_t jid = 0;
+        if (s2m_batch_add_csg(b, r.prog.data(), uint32_t(r.prog.size()), &r.params, &jid, err, sizeof err) != S2M_OK) {
+          s->queue.pop_front();
+          server_complete_locked(s, r, S2M_E_INVALID, err);
+          continue;
+        }
+        const uint64_t fp = s2m_batch_job_footprint(b, jid);
+        if (s->cfg.memory_budget_bytes && fp > s->cfg.memory_budget_bytes) {
+          b->jobs.pop_back();
+          s->queue.pop_front();
+          server_complete_locked(s, r, S2M_E_OOM, "request larger than the memory budget");
+          continue;
+        }
+        if (s->cfg.memory_budget_bytes && s->used_bytes + add + fp > s->cfg.memory_budget_bytes) {
+          b->jobs.pop_back();
+          break;  // waits for memory: admitted when earlier requests release theirs
+        }
+        r.footprint = fp;
+        add += fp;
+        r.state = 1;
+        ++r.attempts;
+        ids.push_back(r.id);
+        s->queue.pop_front();
+      }
+      if (!ids.empty()) {
+        s->used_bytes += add;
+        s->peak_bytes = std::max(s->peak_bytes, s->used_bytes);
+        SWave sw;
+        sw.b = b;
+        sw.reqs = ids;
+        sw.st = s->streams[next_stream];
+        next_stream ^= 1;
+        std::vector<int> idx(ids.size());
+        for (size_t k = 0; k < ids.size(); ++k) idx[k] = int(k);
+        lk.unlock();
+        int rc = launch_wave(b, idx, sw.st, sw.w, err, sizeof err);
+        lk.lock();
+        if (rc != S2M_OK) {
+          for (uint64_t id : ids) server_complete_locked(s, s->reqs[id], rc, err);
+          delete b;
+        } else {
+          ++s->inflight;
+          ++s->batches;
+          s->waves.push_back(sw);
+        }
+        continue;
+      }
+      delete b;
+    }
+    if (s->stop && s->queue.empty() && s->inflight == 0) break;
+    s->cv.wait_for(lk, std::chrono::microseconds(200));
+  }
+}
+
+void server_sdf_loop(s2m_server *s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  char err[1024];
+  while (true) {
+    if (s->sdf_queue.empty()) {
+      if (s->stop) break;
+      s->cv.wait_for(lk, std::chrono::milliseconds(1));
+      continue;
+    }
+    uint64_t id = s->sdf_queue.front();
+    SReq &r0 = s->reqs[id];
+    if (s->cfg.memory_budget_bytes && s->used_bytes + r0.footprint > s->cfg.memory_budget_bytes &&
+        s->used_bytes > 0) {
+      s->cv.wait_for(lk, std::chrono::microseconds(200));
+      continue;
+    }
+    s->sdf_queue.pop_front();
+    s->used_bytes += r0.footprint;
+    s->peak_bytes = std::max(s->peak_bytes, s->used_bytes);
+    r0.state = 1;
+    const s2m_sdf *sdf = r0.sdf;
+    s2m_params p = r0.params;
+    lk.unlock();
+    s2m_mesh *m = nullptr;
+    int rc = s2m_mesh_create(sdf, &p, s->sdf_stream, &m, err, sizeof err);
+    lk.lock();
+    SReq &r = s->reqs[id];
+    if (rc == S2M_OK) {
+      r.mesh = m;
+      s2m_mesh_get_info(m, &r.info);
+    }
+    server_complete_locked(s, r, rc, rc == S2M_OK ? "" : err);
+    s->done_cv.notify_all();
+  }
+}
+
+double percentile(std::vector<double> v, double q) {
+  if (v.empty()) return 0;
+  std::sort(v.begin(), v.end());
+  double pos = q * double(v.size() - 1);
+  size_t i = size_t(pos);
+  double f = pos - double(i);
+  return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+int s2m_server_create(const s2m_server_config *cfg, s2m_server **out, char *err, size_t errlen) {
+  if (!out) return S2M_E_INVALID;
+  s2m_server *s = new s2m_server();
+  if (cfg) s->cfg = *cfg;
+  if (s->cfg.max_inflight == 0) s->cfg.max_inflight = 2;
+  if (s->cfg.max_batch_jobs == 0) s->cfg.max_batch_jobs = 1024;
+  cudaGetDevice(&s->device);
+  // keep freed arenas in the stream-ordered pool instead of returning them to the driver
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  for (int i = 0; i < 2; ++i)
+    if (cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking) != cudaSuccess) {
+      set_err(err, errlen, "cudaStreamCreate failed");
+      delete s;
+      return S2M_E_CUDA;
+    }
+  cudaStreamCreateWithFlags(&s->sdf_stream, cudaStreamNonBlocking);
+  s->worker = std::thread(server_loop, s);
+  s->sdf_worker = std::thread(server_sdf_loop, s);
+  *out = s;
+  return S2M_OK;
+}
+
+int s2m_server_submit_csg(s2m_server *s, const float *program, uint32_t len, const s2m_params *params,
+                          uint64_t *request_id, char *err, size_t errlen) {
+  if (!s || !program || !params) return S2M_E_INVALID;
+  std::string why;
+  if (!csg_validate(program, len, why)) {
+    set_err(err, errlen, "invalid CSG program: " + why);
+    return S2M_E_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  SReq r;
+  r.id = s->next_id++;
+  r.kind = 0;
+  r.prog.assign(program, program + len);
+  r.params = *params;
+  r.t_submit = now_s();
+  if (s->submitted == 0) s->first_submit = r.t_submit;
+  ++s->submitted;
+  s->queue.push_back(r.id);
+  if (request_id) *request_id = r.id;
+  s->reqs.emplace(r.id, std::move(r));
+  s->cv.notify_all();
+  return S2M_OK;
+}
+
+int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *params, uint64_t *request_id,
+                          char *err, size_t errlen) {
+  if (!s || !sdf || !params) return S2M_E_INVALID;
+  uint64_t fp = sdf_job_footprint(*params);
+  if (s->cfg.memory_budget_bytes && fp > s->cfg.memory_budget_bytes) {
+    set_err(err, errlen, "request larger than the memory budget");
+    return S2M_E_OOM;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  SReq r;
+  r.id = s->next_id++;
+  r.kind = 1;
+  r.sdf = sdf;
+  r.params = *params;
+  r.footprint = fp;
+  r.t_submit = now_s();
+  if (s->submitted == 0) s->first_submit = r.t_submit;
+  ++s->submitted;
+  s->sdf_queue.push_back(r.id);
+  if (request_id) *request_id = r.id;
+  s->reqs.emplace(r.id, std::move(r));
+  s->cv.notify_all();
+  return S2M_OK;
+}
+
+int s2m_server_wait(s2m_server *s, uint64_t id, double timeout_s, s2m_mesh_info *info, char *err, size_t errlen) {
+  if (!s) return S2M_E_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return S2M_E_INVALID;
+  const double deadline = now_s() + timeout_s;
+  while (it->second.state < 2) {
+    if (now_s() > deadline) return S2M_E_TIMEOUT;
+    s->done_cv.wait_for(lk, std::chrono::milliseconds(1));
+  }
+  if (info) *info = it->second.info;
+  if (it->second.status != S2M_OK) set_err(err, errlen, it->second.msg);
+  return it->second.status;
+}
+
+int s2m_server_copy_to_host(s2m_server *s, uint64_t id, float *pos, float *nrm, uint64_t *cell, uint32_t *tris) {
+  if (!s) return S2M_E_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end() || it->second.state != 2) return S2M_E_INVALID;
+  SReq &r = it->second;
+  if (r.kind == 1) return r.mesh ? s2m_mesh_copy_to_host(r.mesh, pos, nrm, cell, tris, s->sdf_stream) : S2M_E_INVALID;
+  if (r.wave < 0 || !s->waves[size_t(r.wave)].b) return S2M_E_INVALID;
+  return s2m_batch_job_copy_to_host(s->waves[size_t(r.wave)].b, r.job, pos, nrm, cell, tris,
+                                    s->waves[size_t(r.wave)].st);
+}
+
+int s2m_server_release(s2m_server *s, uint64_t id) {
+  if (!s) return S2M_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return S2M_E_INVALID;
+  server_release_locked(s, it->second);
+  s->cv.notify_all();
+  return S2M_OK;
+}
+
+int s2m_server_drain(s2m_server *s, double timeout_s) {
+  if (!s) return S2M_E_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  const double deadline = now_s() + timeout_s;
+  while (s->completed + s->failed < s->submitted) {
+    if (now_s() > deadline) return S2M_E_TIMEOUT;
+    s->done_cv.wait_for(lk, std::chrono::milliseconds(1));
+  }
+  return S2M_OK;
+}
+
+int s2m_server_get_stats(s2m_server *s, s2m_server_stats *out) {
+  if (!s || !out) return S2M_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->failed = s->failed;
+  out->batches = s->batches;
+  out->peak_bytes = s->peak_bytes;
+  out->p50_ms = percentile(s->latencies_ms, 0.50);
+  out->p99_ms = percentile(s->latencies_ms, 0.99);
+  double sum = 0;
+  for (double l : s->latencies_ms) sum += l;
+  out->mean_ms = s->latencies_ms.empty() ? 0 : sum / double(s->latencies_ms.size());
+  const double span = s->last_done - s->first_submit;
+  out->span_s = span;
+  out->meshes_per_s = span > 0 ? double(s->completed) / span : 0;
+  out->gvoxels_per_s = span > 0 ? s->voxels_done / span / 1e9 : 0;
+  return S2M_OK;
+}
+
+void s2m_server_free(s2m_server *s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv.notify_all();
+  }
+  if (s->worker.joinable()) s->worker.join();
+  if (s->sdf_worker.joinable()) s->sdf_worker.join();
+  for (auto &kv : s->reqs) {
+    kv.second.state = kv.second.state < 2 ? 3 : kv.second.state;
+    server_release_locked(s, kv.second);
+  }
+  for (SWave &sw : s->waves)
+    if (sw.b) {
+      for (void *a : sw.b->arenas) cudaFreeAsync(a, sw.st);
+      for (PinnedBlock &p : sw.b->pinned_free) cudaFreeHost(p.p);
+      delete sw.b;
+    }
+  for (int i = 0; i < 2; ++i)
+    if (s->streams[i]) {
+      cudaStreamSynchronize(s->streams[i]);
+      cudaStreamDestroy(s->streams[i]);
+    }
+  if (s->sdf_stream) cudaStreamDestroy(s->sdf_stream);
+  delete s;
 }
 
 }  // extern "C"

@@ -99,6 +99,7 @@ struct s2m_sdf {
 
 struct s2m_mesh {
   const s2m_sdf *sdf = nullptr;
+  cudaStream_t stream = nullptr;  // buffers are allocated and freed in this stream's order
   s2m_params params{};
   S2Job job{};
   int N = 0, D = 0, nzc = 0, nslabs = 0;
@@ -133,6 +134,10 @@ struct s2m_mesh {
   std::vector<double> ev_units;
   size_t ev_used = 0;
   s2m_profile prof{};
+  // CUDA graph of the whole pipeline, replayed by s2m_mesh_run_async
+  bool use_graph = false;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
 };
 
 namespace {
@@ -202,13 +207,35 @@ uint32_t reference_resolution(uint32_t r) {
   return r;
 }
 
+// Pinned 8-word read-back slots, carved from blocks that live for the process
+// (pinning and unpinning host memory per job would synchronise the device).
+std::mutex g_pinned_mu;
+std::vector<unsigned long long *> g_pinned_free;
+
+unsigned long long *take_pinned_slot() {
+  std::lock_guard<std::mutex> lock(g_pinned_mu);
+  if (g_pinned_free.empty()) {
+    unsigned long long *blk = nullptr;
+    if (cudaMallocHost(&blk, 512 * 64) != cudaSuccess) return nullptr;
+    for (int i = 0; i < 512; ++i) g_pinned_free.push_back(blk + 8 * i);
+  }
+  unsigned long long *p = g_pinned_free.back();
+  g_pinned_free.pop_back();
+  return p;
+}
+
+void give_pinned_slot(unsigned long long *p) {
+  std::lock_guard<std::mutex> lock(g_pinned_mu);
+  g_pinned_free.push_back(p);
+}
+
 void free_buffers(s2m_mesh *m) {
   void *ptrs[] = {m->ring, m->slab_ctrl, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
                   m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
                   m->jobctl};
   for (void *p : ptrs)
-    if (p) cudaFree(p);
-  if (m->h_read) cudaFreeHost(m->h_read);
+    if (p) cudaFreeAsync(p, m->stream);
+  if (m->h_read) give_pinned_slot(m->h_read);
   m->ring = nullptr; m->slab_ctrl = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
   m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
   m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
@@ -262,8 +289,14 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   return S2M_OK;
 }
 
+void drop_graph(s2m_mesh *m) {
+  if (m->graph) cudaGraphExecDestroy(m->graph);
+  m->graph = nullptr;
+}
+
 int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long vcap, unsigned long long tcap,
                   char *err, size_t errlen) {
+  drop_graph(m);
   free_buffers(m);
   const S2Job &j = m->job;
   const unsigned long long N = (unsigned long long)m->N;
@@ -277,23 +310,28 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   m->quad_tiles = (m->vcap + S2_Q_TILE - 1) / S2_Q_TILE;
   size_t ring_floats = size_t(j.ring) * size_t(j.plane);
-  S2_CUDA(cudaMalloc(&m->ring, ring_floats * sizeof(float)));
-  S2_CUDA(cudaMalloc(&m->slab_ctrl, m->slab_ctrl_words * 8));
-  S2_CUDA(cudaMalloc(&m->cand_key, m->cand_cap * 8));
-  S2_CUDA(cudaMalloc(&m->cand_val, m->cand_cap * 32));
-  S2_CUDA(cudaMalloc(&m->cand_pos, m->cand_cap * 12));
-  S2_CUDA(cudaMalloc(&m->cand_nrm, m->cand_cap * 12));
-  S2_CUDA(cudaMalloc(&m->cand_base, size_t(m->nslabs + 1) * 8));
-  S2_CUDA(cudaMalloc(&m->cand_status, m->vc_tiles * 8));
-  S2_CUDA(cudaMalloc(&m->pos, m->vcap * 12));
-  S2_CUDA(cudaMalloc(&m->nrm, m->vcap * 12));
-  S2_CUDA(cudaMalloc(&m->key, m->vcap * 8));
-  S2_CUDA(cudaMalloc(&m->tris, m->tcap * 12));
-  S2_CUDA(cudaMalloc(&m->rowcnt, N * N * 4));
-  S2_CUDA(cudaMalloc(&m->rowstart, (N * N + 1) * 4));
-  S2_CUDA(cudaMalloc(&m->scan_status, (m->scan_tiles + m->quad_tiles) * 8));
-  S2_CUDA(cudaMalloc(&m->jobctl, 8 * 8));
-  S2_CUDA(cudaMallocHost(&m->h_read, 8 * 8));
+  cudaStream_t st = m->stream;
+  S2_CUDA(cudaMallocAsync(&m->ring, ring_floats * sizeof(float), st));
+  S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_val, m->cand_cap * 32, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_pos, m->cand_cap * 12, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_nrm, m->cand_cap * 12, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_base, size_t(m->nslabs + 1) * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_status, m->vc_tiles * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->pos, m->vcap * 12, st));
+  S2_CUDA(cudaMallocAsync(&m->nrm, m->vcap * 12, st));
+  S2_CUDA(cudaMallocAsync(&m->key, m->vcap * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->tris, m->tcap * 12, st));
+  S2_CUDA(cudaMallocAsync(&m->rowcnt, N * N * 4, st));
+  S2_CUDA(cudaMallocAsync(&m->rowstart, (N * N + 1) * 4, st));
+  S2_CUDA(cudaMallocAsync(&m->scan_status, (m->scan_tiles + m->quad_tiles) * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->jobctl, 8 * 8, st));
+  m->h_read = take_pinned_slot();
+  if (!m->h_read) {
+    set_err(err, errlen, "pinned read-back slot");
+    return S2M_E_OOM;
+  }
   return S2M_OK;
 }
 
@@ -710,7 +748,30 @@ int s2m_wgsl_has_function(const char *wgsl, const char *fn) {
 
 int s2m_mesh_run_async(s2m_mesh *m, void *stream) {
   if (!m || !m->sdf) return S2M_E_INVALID;
-  cudaError_t e = enqueue(m, static_cast<cudaStream_t>(stream));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (m->use_graph && !m->profile) {
+    // capture the launch sequence once (per stream), then replay it: one
+    // launch call instead of one per kernel and memset
+    if (!m->graph || m->graph_stream != st) {
+      drop_graph(m);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = enqueue(m, st);
+        e = cudaStreamEndCapture(st, &g);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&m->graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        m->graph = nullptr;
+        return S2M_E_CUDA;
+      }
+      m->graph_stream = st;
+    }
+    return cudaGraphLaunch(m->graph, st) == cudaSuccess ? S2M_OK : S2M_E_CUDA;
+  }
+  cudaError_t e = enqueue(m, st);
   if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? S2M_E_OOM : S2M_E_CUDA;
   return S2M_OK;
 }
@@ -740,7 +801,18 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
   *out = nullptr;
   s2m_mesh *m = new s2m_mesh();
   m->sdf = sdf;
+  m->stream = static_cast<cudaStream_t>(stream);
   m->params = *params;
+  static std::once_flag pool_once;
+  std::call_once(pool_once, [] {
+    // freed mesh buffers stay in the stream-ordered pool for the next job
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
   if (!(m->params.eps > 0.0f)) m->params.eps = 1e-4f;
   int rc = setup_job(m, err, errlen);
   if (rc != S2M_OK) {
@@ -946,6 +1018,13 @@ int s2m_mesh_write(const s2m_mesh *m, const char *path, char *err, size_t errlen
   return s2m::write_mesh_file(path, pos.data(), nrm.data(), m->nverts, tris.data(), m->ntris, err, errlen);
 }
 
+int s2m_mesh_set_graph(s2m_mesh *m, int enable) {
+  if (!m) return S2M_E_INVALID;
+  m->use_graph = enable != 0;
+  if (!m->use_graph) drop_graph(m);
+  return S2M_OK;
+}
+
 int s2m_mesh_set_profiling(s2m_mesh *m, int enable) {
   if (!m) return S2M_E_INVALID;
   m->profile = enable != 0;
@@ -967,6 +1046,7 @@ int s2m_mesh_reset_profile(s2m_mesh *m) {
 void s2m_mesh_free(s2m_mesh *m) {
   if (!m) return;
   for (cudaEvent_t e : m->ev) cudaEventDestroy(e);
+  drop_graph(m);
   free_buffers(m);
   delete m;
 }
@@ -978,6 +1058,36 @@ int s2m_write_stl(const float *pos, const uint32_t *tris, uint64_t ntris, const 
 int s2m_write_ply(const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris, uint64_t ntris,
                   const char *path) {
   return s2m::write_ply(path, pos, nrm, nverts, tris, ntris) ? S2M_OK : S2M_E_IO;
+}
+
+int s2m_measure_sfu_peak(double *gops, void *stream) {
+  if (!gops) return S2M_E_INVALID;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int sms = device_sm_count();
+  const int blocks = sms * 8, iters = 4096;
+  float *out = nullptr;
+  if (cudaMallocAsync(&out, size_t(blocks) * 4, st) != cudaSuccess) return S2M_E_OOM;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, st);
+    s2m_sfu_probe<<<blocks, 256, 0, st>>>(out, iters, 0.5f);
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    double ops = double(blocks) * 256.0 * iters * 8.0;
+    if (rep > 0) best = std::max(best, ops / (double(ms) * 1e-3) / 1e9);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFreeAsync(out, st);
+  cudaStreamSynchronize(st);
+  if (cudaGetLastError() != cudaSuccess) return S2M_E_CUDA;
+  *gops = best;
+  return S2M_OK;
 }
 
 int s2m_measure_fp32_peak(double *gops, void *stream) {

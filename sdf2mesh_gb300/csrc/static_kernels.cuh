@@ -41,3 +41,19 @@ __global__ void __launch_bounds__(256) s2m_fp32_probe(float *out, int iters, int
   for (int c = 0; c < 8; ++c) s += x[c];
   if (s == 1234.5f) out[blockIdx.x] = s;  // keeps the chains live
 }
+
+// SFU issue-rate probe: 8 independent dependent chains of reciprocal square
+// root (one MUFU operation each) and one FP32 add per step.
+__global__ void __launch_bounds__(256) s2m_sfu_probe(float *out, int iters, float c) {
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = 1.0f + (float)(threadIdx.x + k) * 1e-3f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = rsqrtf(__fadd_rn(x[k], c));
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 1234.5f) out[blockIdx.x] = s;
+}

@@ -289,3 +289,19 @@ def test_qef_1024_watertight(lib):
     e.sort(axis=1)
     _, counts = np.unique(e[:, 0] * np.int64(1 << 32) + e[:, 1], return_counts=True)
     assert (counts == 2).all()
+
+
+def test_graph_replay_identical(lib):
+    """s2m_mesh_run_async replaying the captured CUDA graph gives the same bits."""
+    src, prm = workloads.csg64(seed=2)
+    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    dm = s2m.mesh_device(sdf, s2m.AppState(resolution=80, bounds=2.0))
+    first = dm.to_host()
+    dm.set_graph(True)
+    for _ in range(3):
+        dm.run_async()
+        dm.sync()
+    again = dm.to_host()
+    dm.close()
+    assert_bit_exact(again, oracle.mesh(oracle.CSG, prm, 80, 2.0), "graph replay")
+    assert np.array_equal(first.triangle_indices, again.triangle_indices)

@@ -1,0 +1,95 @@
+"""Serving: continuous batching (s2m_server_*).
+
+Requests submitted from several threads while others run on the GPU; each
+result must be the same alone and in the mix (bit for bit: the same rule and
+arithmetic run whatever the batch), admission must hold the memory budget."""
+from __future__ import annotations
+
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import sdf2mesh_gb300 as s2m
+from sdf2mesh_gb300 import workloads
+from tests.parity import assert_bit_exact
+from tests.test_gpu_batch import per_job_as_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def test_results_same_alone_and_in_the_mix(lib):
+    rng = workloads.SplitMix64(11)
+    specs = []
+    for seed in range(40):
+        _, prog = workloads.random_tree(seed)
+        N = workloads.log_uniform_resolution(rng, (32, 48, 64, 96, 128))
+        specs.append(("csg", prog, s2m.AppState(resolution=N, bounds=2.0, qef=(seed % 5 == 0))))
+    src, _ = workloads.mandelbulb(8.0, 6, 2.0, 0.003)
+    mb = s2m.Sdf3DShader.from_source(src, s2m.LANG_GLSL, "sdf").compile()
+    for N in (48, 64, 80):
+        specs.append(("sdf", mb, s2m.AppState(resolution=N, bounds=2.5)))
+    server = s2m.Server(memory_budget_bytes=2 << 30, max_inflight=2, max_batch_jobs=16)
+    ids = [None] * len(specs)
+
+    def submit(part):
+        for i in part:
+            kind, obj, st = specs[i]
+            ids[i] = server.submit_csg(obj, st) if kind == "csg" else server.submit_sdf(obj, st)
+            time.sleep(0.002 * (i % 3))
+
+    threads = [threading.Thread(target=submit, args=(range(k, len(specs), 3),)) for k in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    server.drain(600)
+    st = server.stats()
+    assert st["completed"] == len(specs) and st["failed"] == 0
+    assert st["batches"] >= 2 and st["p99_ms"] >= st["p50_ms"] > 0
+    for i, (kind, obj, state) in enumerate(specs):
+        got = server.mesh(ids[i])
+        if kind == "csg":
+            b = s2m.Batch()
+            j = b.add_csg(obj, state)
+            b.run()
+            alone = b.mesh(j)
+        else:
+            alone = s2m.generate(obj, state)
+        assert_bit_exact(got, per_job_as_oracle(alone), f"request {i} ({kind})")
+    server.close()
+
+
+def test_admission_under_budget(lib):
+    budget = 192 << 20
+    server = s2m.Server(memory_budget_bytes=budget, max_inflight=2, keep_results=False)
+    reqs = []
+    for seed in range(24):
+        _, prog = workloads.random_tree(seed)
+        reqs.append(server.submit_csg(prog, s2m.AppState(resolution=128, bounds=2.0)))
+    server.drain(600)
+    st = server.stats()
+    assert st["completed"] == 24 and st["failed"] == 0
+    assert 0 < st["peak_bytes"] <= budget
+    assert st["batches"] >= 3  # the budget forces several launches
+    # a request larger than the whole budget is refused, not queued forever
+    _, prog = workloads.random_tree(1)
+    rid = server.submit_csg(prog, s2m.AppState(resolution=1024, bounds=2.0))
+    with pytest.raises(s2m.S2MError) as e:
+        server.wait(rid, 60)
+    assert e.value.name == "OOM"
+    server.close()
+
+
+def test_server_overflow_requeue(lib):
+    """Requests whose guessed buffers overflow are re-queued with the exact sizes."""
+    _, prog = workloads.random_tree(2)
+    server = s2m.Server()
+    rid = server.submit_csg(prog, s2m.AppState(resolution=96, bounds=2.0, max_vertices=64, max_triangles=64))
+    got = server.mesh(rid)
+    b = s2m.Batch()
+    j = b.add_csg(prog, s2m.AppState(resolution=96, bounds=2.0))
+    b.run()
+    assert_bit_exact(got, per_job_as_oracle(b.mesh(j)), "requeued request")
+    server.close()
