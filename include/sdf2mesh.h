@@ -128,8 +128,12 @@ int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops);
    job (-1: not tuned yet): its name, and the measured ns per lattice point
    of each of the S2M_EVAL_VARIANTS variants.  No reference counterpart (the
    reference has one fixed kernel, dualcontour.wgsl:161-162). */
-#define S2M_EVAL_VARIANTS 6
+#define S2M_EVAL_VARIANTS 4
 int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point);
+/* Name, registers per thread and local (spill) bytes per thread of one
+   variant, as the tuner recorded them (0 before tuning). */
+int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_t namelen, int *registers,
+                              int *local_bytes);
 
 void s2m_sdf_free(s2m_sdf *sdf);
 
@@ -262,6 +266,14 @@ enum {
   S2M_CSG_UNION = 10, S2M_CSG_SUBTRACT = 11, S2M_CSG_INTERSECT = 12, S2M_CSG_SMOOTH_UNION = 13,
   S2M_CSG_SMOOTH_INTERSECTION = 14, S2M_CSG_SMOOTH_SUBTRACTION = 15
 };
+/* The CSG program of a .sdf3d source (raw or preprocessed) whose sdf3d is a
+   single expression over sdf3d_sphere / box / torus (at p or p - constant),
+   sdf3d_capsule (at p), min, max, negation and sdf_op_smooth_* with constant
+   arguments -- e.g. the batching workload's sources.  *len receives the
+   length; program (capacity floats) may be NULL to query it.  S2M_E_PARSE
+   with the reason for any other source (compile it with s2m_compile). */
+int s2m_csg_from_source(const char *source, float *program, uint32_t capacity, uint32_t *len, char *err,
+                        size_t errlen);
 typedef struct s2m_batch s2m_batch;
 int s2m_batch_create(s2m_batch **out, uint64_t memory_budget_bytes);
 int s2m_batch_add_csg(s2m_batch *b, const float *program, uint32_t len, const s2m_params *params,
@@ -305,6 +317,12 @@ int s2m_server_submit_csg(s2m_server *s, const float *program, uint32_t len, con
                           uint64_t *request_id, char *err, size_t errlen);
 int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *params, uint64_t *request_id,
                           char *err, size_t errlen);
+/* A request as source text, the reference's plugin surface: WGSL whose sdf3d
+   is a CSG expression (s2m_csg_from_source) runs on the batch interpreter;
+   any other source is compiled once (cached by its text) and runs the
+   per-job pipeline. */
+int s2m_server_submit_source(s2m_server *s, const char *source, int lang, const char *sdf_name,
+                             const s2m_params *params, uint64_t *request_id, char *err, size_t errlen);
 /* S2M_OK once the request completed, S2M_E_TIMEOUT if it has not yet, or its error. */
 int s2m_server_wait(s2m_server *s, uint64_t request_id, double timeout_s, s2m_mesh_info *info, char *err,
                     size_t errlen);

@@ -130,6 +130,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_sdf_op_counts": ([vp, dp, dp], i),
             "s2m_sdf_free": ([vp], None),
             "s2m_sdf_eval_variant": ([vp, ctypes.c_char_p, sz, dp], i),
+            "s2m_sdf_eval_variant_info": ([vp, i, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)], i),
             "s2m_wgsl_remove_function": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)], i),
             "s2m_wgsl_rename_function": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                           ctypes.POINTER(vp)], i),
@@ -149,6 +151,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_mesh_set_profiling": ([vp, i], i),
             "s2m_mesh_set_graph": ([vp, i], i),
             "s2m_measure_sfu_peak": ([dp, vp], i),
+            "s2m_csg_from_source": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(u32),
+                                     ctypes.c_char_p, sz], i),
             "s2m_batch_create": ([ctypes.POINTER(vp), u64], i),
             "s2m_batch_add_csg": ([vp, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(Params),
                                    ctypes.POINTER(u32), ctypes.c_char_p, sz], i),
@@ -162,6 +166,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_server_submit_csg": ([vp, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(Params),
                                        ctypes.POINTER(u64), ctypes.c_char_p, sz], i),
             "s2m_server_submit_sdf": ([vp, vp, ctypes.POINTER(Params), ctypes.POINTER(u64), ctypes.c_char_p, sz], i),
+            "s2m_server_submit_source": ([vp, ctypes.c_char_p, i, ctypes.c_char_p, ctypes.POINTER(Params),
+                                          ctypes.POINTER(u64), ctypes.c_char_p, sz], i),
             "s2m_server_wait": ([vp, u64, ctypes.c_double, ctypes.POINTER(MeshInfo), ctypes.c_char_p, sz], i),
             "s2m_server_copy_to_host": ([vp, u64, vp, vp, vp, vp], i),
             "s2m_server_release": ([vp, u64], i),
@@ -256,9 +262,20 @@ class CompiledSdf:
     def eval_variant(self):
         """(name, ns per lattice point of each variant) chosen by the autotuner; name is 'untuned' before the first job."""
         name = ctypes.create_string_buffer(64)
-        ns = (ctypes.c_double * 6)()
+        ns = (ctypes.c_double * 4)()
         load_library().s2m_sdf_eval_variant(self._h, name, 64, ns)
         return name.value.decode(), list(ns)
+
+    def eval_variants(self):
+        """Per variant: (name, ns per point, registers, local bytes) as the autotuner measured them."""
+        _, ns = self.eval_variant()
+        out = []
+        for v in range(len(ns)):
+            name = ctypes.create_string_buffer(64)
+            regs, loc = ctypes.c_int(), ctypes.c_int()
+            load_library().s2m_sdf_eval_variant_info(self._h, v, name, 64, ctypes.byref(regs), ctypes.byref(loc))
+            out.append((name.value.decode(), ns[v], regs.value, loc.value))
+        return out
 
     def close(self):
         if self._h:
@@ -310,6 +327,17 @@ class Sdf3DShader:
     def write_to_file(self, path: str) -> None:
         with open(path, "w") as f:
             f.write(self.source)
+
+    def csg_program(self) -> np.ndarray:
+        """The batch interpreter's CSG program of this source (raises for non-CSG sources)."""
+        L = load_library()
+        n = ctypes.c_uint32()
+        err = _errbuf()
+        _check(L.s2m_csg_from_source(self.source.encode(), None, 0, ctypes.byref(n), err, len(err)), err, "csg")
+        prog = np.empty(n.value, np.float32)
+        _check(L.s2m_csg_from_source(self.source.encode(), prog.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                     n.value, ctypes.byref(n), err, len(err)), err, "csg")
+        return prog
 
     def compile(self, fmad: bool = False) -> CompiledSdf:
         L = load_library()
@@ -561,6 +589,16 @@ class Server:
         err = _errbuf()
         _check(load_library().s2m_server_submit_sdf(self._h, sdf.handle, ctypes.byref(p), ctypes.byref(rid), err,
                                                      len(err)), err, "submit")
+        return int(rid.value)
+
+    def submit_source(self, source: str, state: AppState, lang: int = LANG_WGSL, sdf_name: str = "sdf") -> int:
+        """Submit .sdf3d / GLSL text: CSG expressions run on the interpreter, others compile once (cached)."""
+        p = state.params()
+        rid = ctypes.c_uint64()
+        err = _errbuf()
+        _check(load_library().s2m_server_submit_source(self._h, source.encode(), lang, sdf_name.encode(),
+                                                        ctypes.byref(p), ctypes.byref(rid), err, len(err)),
+               err, "submit")
         return int(rid.value)
 
     def wait(self, request: int, timeout_s: float = 600.0) -> MeshInfo:

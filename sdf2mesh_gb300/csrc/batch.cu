@@ -156,6 +156,145 @@ struct S2CsgSdf {
   __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
     s2_tetra_normal(*this, px, py, pz, eps, n);
   }
+
+  // W points (x, y, z[w]) per decoded opcode: the same arithmetic as
+  // operator(), applied to W independent stacks (instruction-level
+  // parallelism, one decode for W evaluations).
+  template <int W>
+  __device__ void eval_run(float x, float y, const float z[W], float out[W]) const {
+    float st[S2_CSG_STACK][W];
+    int sp = 0;
+    int i = 0;
+    while (i < len) {
+      const int op = (int)__ldg(prog + i);
+      const float *a = prog + i + 1;
+      switch (op) {
+        case S2M_CSG_SPHERE: {
+          const float cx = __ldg(a), cy = __ldg(a + 1), cz = __ldg(a + 2), r = __ldg(a + 3);
+          const float dx = __fsub_rn(x, cx), dy = __fsub_rn(y, cy);
+#pragma unroll
+          for (int w = 0; w < W; ++w) st[sp][w] = __fsub_rn(len3(dx, dy, __fsub_rn(z[w], cz)), r);
+          ++sp;
+          i += 5;
+          break;
+        }
+        case S2M_CSG_BOX: {
+          const float qx = __fsub_rn(fabsf(__fsub_rn(x, __ldg(a))), __fmul_rn(0.5f, __ldg(a + 3)));
+          const float qy = __fsub_rn(fabsf(__fsub_rn(y, __ldg(a + 1))), __fmul_rn(0.5f, __ldg(a + 4)));
+          const float cz = __ldg(a + 2), hz = __fmul_rn(0.5f, __ldg(a + 5));
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const float qz = __fsub_rn(fabsf(__fsub_rn(z[w], cz)), hz);
+            const float outside = len3(fmaxf(qx, 0.0f), fmaxf(qy, 0.0f), fmaxf(qz, 0.0f));
+            st[sp][w] = __fadd_rn(outside, fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f));
+          }
+          ++sp;
+          i += 7;
+          break;
+        }
+        case S2M_CSG_TORUS: {
+          const float dx = __fsub_rn(x, __ldg(a)), dy = __fsub_rn(y, __ldg(a + 1)), cz = __ldg(a + 2);
+          const float R = __ldg(a + 3), r = __ldg(a + 4);
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const float qx = __fsub_rn(len2(dx, __fsub_rn(z[w], cz)), R);
+            st[sp][w] = __fsub_rn(len2(qx, dy), r);
+          }
+          ++sp;
+          i += 6;
+          break;
+        }
+        case S2M_CSG_CAPSULE: {
+          const float ax = __ldg(a), ay = __ldg(a + 1), az = __ldg(a + 2);
+          const float bax = __fsub_rn(__ldg(a + 3), ax), bay = __fsub_rn(__ldg(a + 4), ay),
+                      baz = __fsub_rn(__ldg(a + 5), az), r = __ldg(a + 6);
+          const float pax = __fsub_rn(x, ax), pay = __fsub_rn(y, ay);
+          const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(bax, bax), __fmul_rn(bay, bay)), __fmul_rn(baz, baz));
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const float paz = __fsub_rn(z[w], az);
+            const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(pax, bax), __fmul_rn(pay, bay)), __fmul_rn(paz, baz));
+            const float h = clamp01(__fdiv_rn(d1, d2));
+            st[sp][w] = __fsub_rn(len3(__fsub_rn(pax, __fmul_rn(bax, h)), __fsub_rn(pay, __fmul_rn(bay, h)),
+                                       __fsub_rn(paz, __fmul_rn(baz, h))),
+                                  r);
+          }
+          ++sp;
+          i += 8;
+          break;
+        }
+        case S2M_CSG_PLANE: {
+          const float dxy = __fadd_rn(__fmul_rn(x, __ldg(a)), __fmul_rn(y, __ldg(a + 1)));
+          const float nz = __ldg(a + 2), d = __ldg(a + 3);
+#pragma unroll
+          for (int w = 0; w < W; ++w) st[sp][w] = __fsub_rn(__fadd_rn(dxy, __fmul_rn(z[w], nz)), d);
+          ++sp;
+          i += 5;
+          break;
+        }
+        case S2M_CSG_UNION:
+          --sp;
+#pragma unroll
+          for (int w = 0; w < W; ++w) st[sp - 1][w] = fminf(st[sp - 1][w], st[sp][w]);
+          i += 1;
+          break;
+        case S2M_CSG_SUBTRACT:
+          --sp;
+#pragma unroll
+          for (int w = 0; w < W; ++w) st[sp - 1][w] = fmaxf(st[sp - 1][w], -st[sp][w]);
+          i += 1;
+          break;
+        case S2M_CSG_INTERSECT:
+          --sp;
+#pragma unroll
+          for (int w = 0; w < W; ++w) st[sp - 1][w] = fmaxf(st[sp - 1][w], st[sp][w]);
+          i += 1;
+          break;
+        case S2M_CSG_SMOOTH_UNION: {
+          --sp;
+          const float k = __ldg(a);
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const float b = st[sp][w], d1 = st[sp - 1][w];
+            const float h = clamp01(__fadd_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
+            st[sp - 1][w] = __fsub_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
+          }
+          i += 2;
+          break;
+        }
+        case S2M_CSG_SMOOTH_INTERSECTION: {
+          --sp;
+          const float k = __ldg(a);
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const float b = st[sp][w], d1 = st[sp - 1][w];
+            const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
+            st[sp - 1][w] = __fadd_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
+          }
+          i += 2;
+          break;
+        }
+        case S2M_CSG_SMOOTH_SUBTRACTION: {
+          --sp;
+          const float k = __ldg(a);
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const float b = st[sp][w], d1 = st[sp - 1][w];
+            const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fadd_rn(b, d1)), k)));
+            st[sp - 1][w] = __fadd_rn(mix(b, -d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
+          }
+          i += 2;
+          break;
+        }
+        default:
+#pragma unroll
+          for (int w = 0; w < W; ++w) out[w] = __int_as_float(0x7fc00000);
+          return;
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < W; ++w) out[w] = st[sp - 1][w];
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -198,18 +337,32 @@ struct S2BatchResult {
   unsigned err, pad;
 };
 
+// Lattice points of one item: S2_B_EVAL_ITEM / 4 units, a unit being a run
+// of 4 planes (k0 .. k0 + 3) at one (y, x); consecutive threads take
+// consecutive x, so each plane's stores are coalesced.
+#define S2_B_EVAL_RUN 4
 __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned item) {
   const S2Job &j = J.job;
   const S2CsgSdf f{J.prog, J.prog_len};
-  const long long P = j.P, pp = P * P, total = pp * P;
+  const unsigned P = (unsigned)j.P, pp = P * P;  // P <= 4097: P * P < 2^32
+  const unsigned runs = (P + S2_B_EVAL_RUN - 1) / S2_B_EVAL_RUN;
+  const unsigned long long units = (unsigned long long)runs * pp;
 #pragma unroll 1
-  for (int r = 0; r < S2_B_EVAL_ITEM / 256; ++r) {
-    const long long idx = (long long)item * S2_B_EVAL_ITEM + r * 256 + threadIdx.x;
-    if (idx >= total) break;
-    const int k = (int)(idx / pp);
-    const long long rem = idx - (long long)k * pp;
-    const int y = (int)(rem / P), x = (int)(rem - (long long)y * P);
-    J.lattice[(long long)k * j.plane + (long long)y * j.pitch + x] = f(s2_coord(j, x), s2_coord(j, y), s2_coord(j, k));
+  for (int r = 0; r < S2_B_EVAL_ITEM / S2_B_EVAL_RUN / 256; ++r) {
+    const unsigned long long u = (unsigned long long)item * (S2_B_EVAL_ITEM / S2_B_EVAL_RUN) + r * 256 + threadIdx.x;
+    if (u >= units) break;
+    const unsigned run = (unsigned)(u / pp);
+    const unsigned c = (unsigned)(u - (unsigned long long)run * pp);
+    const unsigned y = s2_udiv(c, P, j.magic_p), x = c - y * P;
+    const int k0 = (int)(run * S2_B_EVAL_RUN);
+    float z[S2_B_EVAL_RUN], v[S2_B_EVAL_RUN];
+#pragma unroll
+    for (int w = 0; w < S2_B_EVAL_RUN; ++w) z[w] = s2_coord(j, min(k0 + w, j.P - 1));
+    f.eval_run<S2_B_EVAL_RUN>(s2_coord(j, (int)x), s2_coord(j, (int)y), z, v);
+    float *dst = J.lattice + (long long)k0 * j.plane + (long long)y * j.pitch + x;
+#pragma unroll
+    for (int w = 0; w < S2_B_EVAL_RUN; ++w)
+      if (k0 + w < j.P) dst[(long long)w * j.plane] = v[w];
   }
 }
 
@@ -619,7 +772,11 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
     // items per stage
     const unsigned long long P = (unsigned long long)h.job.P;
     const unsigned long long n2 = N * N;
-    J.nitems[S2_ST_EVAL] = unsigned((P * P * P + S2_B_EVAL_ITEM - 1) / S2_B_EVAL_ITEM);
+    {
+      const unsigned long long units = (P + S2_B_EVAL_RUN - 1) / S2_B_EVAL_RUN * P * P;
+      const unsigned long long per_item = S2_B_EVAL_ITEM / S2_B_EVAL_RUN;
+      J.nitems[S2_ST_EVAL] = unsigned((units + per_item - 1) / per_item);
+    }
     J.nitems[S2_ST_CELLS] = unsigned(std::max<size_t>(1, cell_tiles));
     J.nitems[S2_ST_VERT] = unsigned(std::min<unsigned long long>(128, std::max<unsigned long long>(1, n2 / 2048)));
     J.nitems[S2_ST_VCOMPACT] = unsigned(std::min<unsigned long long>(64, std::max<unsigned long long>(1, n2 / 8192)));
@@ -790,6 +947,8 @@ int s2m_batch_add_csg(s2m_batch *b, const float *program, uint32_t len, const s2
   j.lag = (params->flags & S2M_JOB_SLICE_LAG) ? 1 : 0;
   j.exact = (params->flags & S2M_JOB_EXACT_CORNERS) ? 1 : 0;
   j.qef = (params->flags & S2M_JOB_QEF) ? 1 : 0;
+  j.magic_n = uint32_t((1ull << 32) / uint64_t(j.N) + 1);
+  j.magic_p = uint32_t((1ull << 32) / uint64_t(j.P) + 1);
   h.nzc = j.lag ? int(N) - 1 : int(N);
   const unsigned long long n3 = (unsigned long long)N * N * N, n2 = (unsigned long long)N * N;
   h.cand_cap = std::min(n3, std::max<unsigned long long>(4096, 8 * n2));
@@ -996,6 +1155,9 @@ struct s2m_server {
   cudaStream_t sdf_stream = nullptr;
   std::thread worker, sdf_worker;
   int device = 0;
+  // sources that are not CSG programs, compiled once (keyed by language, name, text)
+  std::mutex compile_mu;
+  std::map<std::string, s2m_sdf *> compiled;
 };
 
 namespace {
@@ -1274,6 +1436,44 @@ int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *p
   return S2M_OK;
 }
 
+int s2m_server_submit_source(s2m_server *s, const char *source, int lang, const char *sdf_name,
+                             const s2m_params *params, uint64_t *request_id, char *err, size_t errlen) {
+  if (!s || !source || !params) return S2M_E_INVALID;
+  if (lang == S2M_LANG_WGSL) {
+    uint32_t n = 0;
+    if (s2m_csg_from_source(source, nullptr, 0, &n, nullptr, 0) == S2M_OK && n > 0) {
+      std::vector<float> prog(n);
+      if (s2m_csg_from_source(source, prog.data(), n, &n, err, errlen) == S2M_OK)
+        return s2m_server_submit_csg(s, prog.data(), n, params, request_id, err, errlen);
+    }
+  }
+  const std::string key = std::to_string(lang) + '\0' + (sdf_name ? sdf_name : "sdf") + '\0' + source;
+  s2m_sdf *sdf = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(s->compile_mu);
+    auto it = s->compiled.find(key);
+    if (it != s->compiled.end()) sdf = it->second;
+  }
+  if (!sdf) {
+    std::string text = source;
+    if (lang == S2M_LANG_WGSL) {
+      char *pre = nullptr;
+      if (s2m_preprocess_source(source, nullptr, &pre, err, errlen) != S2M_OK) return S2M_E_PARSE;
+      text = pre;
+      s2m_free_string(pre);
+    }
+    int rc = s2m_compile(text.c_str(), lang, sdf_name, 0, &sdf, err, errlen);
+    if (rc != S2M_OK) return rc;
+    std::lock_guard<std::mutex> lk(s->compile_mu);
+    auto ins = s->compiled.emplace(key, sdf);
+    if (!ins.second) {
+      s2m_sdf_free(sdf);
+      sdf = ins.first->second;
+    }
+  }
+  return s2m_server_submit_sdf(s, sdf, params, request_id, err, errlen);
+}
+
 int s2m_server_wait(s2m_server *s, uint64_t id, double timeout_s, s2m_mesh_info *info, char *err, size_t errlen) {
   if (!s) return S2M_E_INVALID;
   std::unique_lock<std::mutex> lk(s->mu);
@@ -1368,6 +1568,7 @@ void s2m_server_free(s2m_server *s) {
       cudaStreamDestroy(s->streams[i]);
     }
   if (s->sdf_stream) cudaStreamDestroy(s->sdf_stream);
+  for (auto &kv : s->compiled) s2m_sdf_free(kv.second);
   delete s;
 }
 

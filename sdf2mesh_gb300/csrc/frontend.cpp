@@ -2669,4 +2669,177 @@ FrontendResult translate(const std::string &source, Lang lang, const std::string
   return r;
 }
 
+// ---------------------------------------------------------------------------
+// CSG programs from .sdf3d sources.  A source whose sdf3d is one expression
+// over the library's primitives with constant arguments -- sdf3d_sphere,
+// sdf3d_box, sdf3d_torus (each at p or p - constant), sdf3d_capsule at p --
+// combined by min, max, negation and the sdf_op_smooth_* operators becomes
+// the postfix program the batch interpreter evaluates with the same
+// arithmetic (opcodes of include/sdf2mesh.h).
+
+namespace {
+
+struct CsgConv {
+  Func *sdf = nullptr;
+  std::vector<float> prog;
+  std::string why;
+
+  [[noreturn]] void no(const Expr *e, const std::string &m) {
+    throw CompileError(e ? e->line : 0, "not a CSG expression: " + m);
+  }
+  static float as_f32(double v) { return float(v); }
+
+  // A constant scalar: literal, negated literal, folded constant or const symbol.
+  float scalar(const Expr *e) {
+    if (e->k == Expr::Lit) return e->lit_b == B::F32 ? e->flit : as_f32(e->lit);
+    if (e->k == Expr::Unary && e->s == "-" && e->a.size() == 1) return -scalar(e->a[0]);
+    if (e->cst && e->cv.size() == 1) return as_f32(e->cv[0]);
+    if (e->k == Expr::Ref && e->sym && e->sym->cst && e->sym->cv.size() == 1) return as_f32(e->sym->cv[0]);
+    no(e, "argument is not a constant");
+  }
+  // A constant vector of n components: vecN(...) / vecNf(...) of constants (or a splat).
+  std::vector<float> vector(const Expr *e, int n) {
+    if (e->cst && int(e->cv.size()) == n) {
+      std::vector<float> r;
+      for (double v : e->cv) r.push_back(as_f32(v));
+      return r;
+    }
+    if (e->k == Expr::Call && e->is_ctor) {
+      if (int(e->a.size()) == n) {
+        std::vector<float> r;
+        for (const Expr *x : e->a) r.push_back(scalar(x));
+        return r;
+      }
+      if (e->a.size() == 1) return std::vector<float>(size_t(n), scalar(e->a[0]));
+    }
+    no(e, "argument is not a constant vector");
+  }
+  bool is_p(const Expr *e) const {
+    return e->k == Expr::Ref && e->sym && e->sym->k == Sym::Param && e->s == sdf->params[0].name;
+  }
+  // p -> (0,0,0);  p - c -> c
+  std::vector<float> centre(const Expr *e) {
+    if (is_p(e)) return {0.0f, 0.0f, 0.0f};
+    if (e->k == Expr::Binary && e->s == "-" && e->a.size() == 2 && is_p(e->a[0])) return vector(e->a[1], 3);
+    no(e, "primitive not evaluated at p or p - constant");
+  }
+  void put(float v) { prog.push_back(v); }
+  void put(const std::vector<float> &v) { prog.insert(prog.end(), v.begin(), v.end()); }
+
+  void expr(const Expr *e) {
+    if (e->k != Expr::Call || e->is_ctor) no(e, "expected a call");
+    const std::string &f = e->s;
+    const size_t na = e->a.size();
+    if ((f == "min" || f == "max") && na == 2) {
+      expr(e->a[0]);
+      if (f == "max" && e->a[1]->k == Expr::Unary && e->a[1]->s == "-") {
+        expr(e->a[1]->a[0]);
+        put(float(S2M_CSG_SUBTRACT));
+      } else {
+        expr(e->a[1]);
+        put(float(f == "min" ? S2M_CSG_UNION : S2M_CSG_INTERSECT));
+      }
+      return;
+    }
+    if ((f == "sdf_op_smooth_union" || f == "sdf_op_smooth_intersection" || f == "sdf_op_smooth_subtraction") &&
+        na == 3) {
+      expr(e->a[0]);
+      expr(e->a[1]);
+      put(float(f == "sdf_op_smooth_union" ? S2M_CSG_SMOOTH_UNION
+                                            : f == "sdf_op_smooth_intersection" ? S2M_CSG_SMOOTH_INTERSECTION
+                                                                                 : S2M_CSG_SMOOTH_SUBTRACTION));
+      put(scalar(e->a[2]));
+      return;
+    }
+    if (f == "sdf3d_sphere" && na == 2) {
+      put(float(S2M_CSG_SPHERE));
+      put(centre(e->a[0]));
+      put(scalar(e->a[1]));
+      return;
+    }
+    if (f == "sdf3d_box" && na == 2) {
+      put(float(S2M_CSG_BOX));
+      put(centre(e->a[0]));
+      put(vector(e->a[1], 3));
+      return;
+    }
+    if (f == "sdf3d_torus" && na == 2) {
+      put(float(S2M_CSG_TORUS));
+      put(centre(e->a[0]));
+      put(vector(e->a[1], 2));
+      return;
+    }
+    if (f == "sdf3d_capsule" && na == 4) {
+      if (!is_p(e->a[0])) no(e, "capsule not evaluated at p");
+      put(float(S2M_CSG_CAPSULE));
+      put(vector(e->a[1], 3));
+      put(vector(e->a[2], 3));
+      put(scalar(e->a[3]));
+      return;
+    }
+    no(e, "unsupported call " + f);
+  }
+};
+
+std::string squash_ws(const std::string &t) {
+  std::string o;
+  for (char ch : t)
+    if (!std::isspace((unsigned char)ch)) o.push_back(ch);
+  return o;
+}
+
+// The library function `name`, if the source defines it, must be the
+// library's own text (the program's opcodes stand for the library formulas).
+bool library_function_intact(const std::string &src_sq, const std::string &name) {
+  const std::string key = "fn" + name + "(";
+  size_t at = src_sq.find(key);
+  if (at == std::string::npos) return true;
+  if (src_sq.find(key, at + 1) != std::string::npos) return false;
+  for (const char *mod : {"sdf3d::primitives", "sdf::op"}) {
+    std::string lib = squash_ws(builtin_module_source(mod));
+    size_t la = lib.find(key);
+    if (la == std::string::npos) continue;
+    size_t lb = lib.find("fn", la + 2);
+    std::string fn = lib.substr(la, lb == std::string::npos ? std::string::npos : lb - la);
+    return src_sq.compare(at, fn.size(), fn) == 0;
+  }
+  return true;
+}
+
+}  // namespace
+
+bool csg_from_source(const std::string &source, std::vector<float> &prog, std::string &why) {
+  Module M;
+  try {
+    std::vector<Tok> toks = lex(source, Lang::WGSL);
+    Parser(M, toks, Lang::WGSL).parse_module();
+    Func *sdf = find_fn(M, "sdf3d", 1);
+    if (!sdf) throw CompileError(0, "no fn sdf3d(p: vec3f) -> f32");
+    Sema S(M);
+    for (Global *g : M.globals) S.resolve_global(g);
+    for (Func *f : M.funcs) S.check_function(f);
+    const std::string sq = squash_ws(source);
+    for (const char *lib : {"sdf3d_sphere", "sdf3d_box", "sdf3d_torus", "sdf3d_capsule", "sdf_op_smooth_union",
+                            "sdf_op_smooth_intersection", "sdf_op_smooth_subtraction"})
+      if (!library_function_intact(sq, lib))
+        throw CompileError(0, std::string("not a CSG expression: ") + lib + " is not the library function");
+    const Stmt *body = sdf->body;
+    const Stmt *ret = nullptr;
+    for (const Stmt *st : body->body) {
+      if (st->k == Stmt::Empty) continue;
+      if (st->k != Stmt::Return || ret) throw CompileError(st->line, "not a CSG expression: sdf3d must be one return");
+      ret = st;
+    }
+    if (!ret || !ret->val) throw CompileError(sdf->line, "not a CSG expression: sdf3d has no return value");
+    CsgConv C;
+    C.sdf = sdf;
+    C.expr(ret->val);
+    prog.swap(C.prog);
+    return true;
+  } catch (const CompileError &e) {
+    why = (e.line > 0 ? "line " + std::to_string(e.line) + ": " : std::string()) + e.what();
+    return false;
+  }
+}
+
 }  // namespace s2m

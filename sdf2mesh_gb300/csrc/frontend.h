@@ -44,6 +44,12 @@ std::string preprocess_sdf3d_text(const std::string &src, const std::string &sel
 // is generated when the source has none.
 FrontendResult translate(const std::string &source, Lang lang, const std::string &sdf_name);
 
+// The batch interpreter's postfix CSG program (opcodes S2M_CSG_*) of a
+// preprocessed .sdf3d source whose sdf3d is one expression over the
+// library's primitives and operators with constant arguments; false (and
+// why) for any other source.
+bool csg_from_source(const std::string &source, std::vector<float> &prog, std::string &why);
+
 // Text helpers with the behaviour of shadertoy.rs:248-352.
 bool wgsl_remove_function(const std::string &wgsl, const std::string &function_name,
                           std::string &out);

@@ -80,8 +80,8 @@ struct EvalVariant {
   const char *name;
   int run;
 };
-constexpr EvalVariant kEvalVariants[] = {{"s2m_eval_b2r4", 4}, {"s2m_eval_b3r4", 4}, {"s2m_eval_b4r4", 4},
-                                         {"s2m_eval_b4r1", 1}, {"s2m_eval_b6r4", 4}, {"s2m_eval_b8r4", 4}};
+constexpr EvalVariant kEvalVariants[] = {
+    {"s2m_eval_b2r4", 4}, {"s2m_eval_b3r4", 4}, {"s2m_eval_b4r4", 4}, {"s2m_eval_b3p4", 4}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -91,10 +91,17 @@ struct s2m_sdf {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_eval[kNumEvalVariants] = {};
   cudaKernel_t k_cells = nullptr, k_vertices = nullptr;
+  // precision mode: a second module with the QEF vertex kernel, built on the
+  // first QEF job (most SDFs never need it, and it compiles slowly)
+  std::mutex qef_mu;
+  cudaLibrary_t qef_lib = nullptr;
+  cudaKernel_t k_vertices_qef = nullptr;
   // autotuned evaluation variant (-1: not tuned yet) and its timings (ns per point)
   mutable std::mutex tune_mu;
   mutable int eval_variant = -1;
   mutable double tune_ns[kNumEvalVariants] = {};
+  mutable int tune_regs[kNumEvalVariants] = {};
+  mutable int tune_local[kNumEvalVariants] = {};  // local (spill/stack) bytes per thread
 };
 
 struct s2m_mesh {
@@ -137,7 +144,7 @@ struct s2m_mesh {
   // CUDA graph of the whole pipeline, replayed by s2m_mesh_run_async
   bool use_graph = false;
   cudaGraphExec_t graph = nullptr;
-  cudaStream_t graph_stream = nullptr;
+  cudaStream_t capture_stream = nullptr;  // private stream the graph is captured on
 };
 
 namespace {
@@ -145,9 +152,13 @@ namespace {
 // ---------------------------------------------------------------------------
 // NVRTC
 
-int compile_module(s2m_sdf *s, char *err, size_t errlen) {
+// NVRTC: the lowered SDF with the pipeline's device sources into a CUBIN for
+// sm_103a, loaded as a library.  `qef` builds the precision-mode vertex
+// kernel alone.
+int nvrtc_build(const s2m_sdf *s, bool qef, cudaLibrary_t *lib, char *err, size_t errlen) {
   std::string src;
   src += "// sdf2mesh_gb300 per-SDF module\n";
+  if (qef) src += "#define S2M_QEF_MODULE 1\n";
   src += kS2mDeviceH;
   src += kS2mLookbackCuh;
   src += kS2mPreludeCuh;
@@ -159,8 +170,8 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
     set_err(err, errlen, "nvrtcCreateProgram failed");
     return S2M_E_NVRTC;
   }
-  std::vector<const char *> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device",
-                                    "-lineinfo", "--extra-device-vectorization"};
+  std::vector<const char *> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device"};
+  if (std::getenv("S2M_NVRTC_LINEINFO")) opts.push_back("-lineinfo");
   opts.push_back((s->flags & S2M_COMPILE_FMAD) ? "--fmad=true" : "--fmad=false");
   nvrtcResult rc = nvrtcCompileProgram(prog, int(opts.size()), opts.data());
   if (rc != NVRTC_SUCCESS) {
@@ -177,11 +188,17 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
   std::vector<char> cubin(cubin_n);
   nvrtcGetCUBIN(prog, cubin.data());
   nvrtcDestroyProgram(&prog);
-  cudaError_t ce = cudaLibraryLoadData(&s->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  cudaError_t ce = cudaLibraryLoadData(lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (ce != cudaSuccess) {
     set_err(err, errlen, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce));
     return ce == cudaErrorNoDevice || ce == cudaErrorInsufficientDriver ? S2M_E_NO_DEVICE : S2M_E_CUDA;
   }
+  return S2M_OK;
+}
+
+int compile_module(s2m_sdf *s, char *err, size_t errlen) {
+  int rc = nvrtc_build(s, false, &s->lib, err, errlen);
+  if (rc != S2M_OK) return rc;
   for (int v = 0; v < kNumEvalVariants; ++v)
     if (cudaLibraryGetKernel(&s->k_eval[v], s->lib, kEvalVariants[v].name) != cudaSuccess) {
       set_err(err, errlen, std::string("kernel missing from the compiled module: ") + kEvalVariants[v].name);
@@ -190,6 +207,20 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
   if (cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess ||
       cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "kernels missing from the compiled module");
+    return S2M_E_CUDA;
+  }
+  return S2M_OK;
+}
+
+// The QEF vertex kernel of an SDF, built once on its first precision-mode job.
+int ensure_qef_module(const s2m_sdf *cs, char *err, size_t errlen) {
+  s2m_sdf *s = const_cast<s2m_sdf *>(cs);
+  std::lock_guard<std::mutex> lock(s->qef_mu);
+  if (s->k_vertices_qef) return S2M_OK;
+  int rc = nvrtc_build(s, true, &s->qef_lib, err, errlen);
+  if (rc != S2M_OK) return rc;
+  if (cudaLibraryGetKernel(&s->k_vertices_qef, s->qef_lib, "s2m_vertices") != cudaSuccess) {
+    set_err(err, errlen, "QEF vertex kernel missing from the compiled module");
     return S2M_E_CUDA;
   }
   return S2M_OK;
@@ -273,6 +304,8 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   j.lag = (p.flags & S2M_JOB_SLICE_LAG) ? 1 : 0;
   j.exact = (p.flags & S2M_JOB_EXACT_CORNERS) ? 1 : 0;
   j.qef = (p.flags & S2M_JOB_QEF) ? 1 : 0;
+  j.magic_n = uint32_t((1ull << 32) / uint64_t(j.N) + 1);
+  j.magic_p = uint32_t((1ull << 32) / uint64_t(j.P) + 1);
   m->nzc = j.lag ? int(N) - 1 : int(N);
   // Slab depth: the ring of D + 1 lattice planes is sized to stay resident in
   // the 126 MB L2 between the evaluation and the cell pass.
@@ -463,7 +496,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   int nslabs = m->nslabs;
   void *vargs[] = {&jj, &cand, &nslabs};
   const unsigned vx_grid = unsigned(sms) * 16;
-  S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)m->sdf->k_vertices, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));
+  const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
+  S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));
   const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
   S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs), cudaGetLastError()));
   const unsigned scan_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->scan_tiles, size_t(sms) * 8)));
@@ -487,7 +521,7 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   }
   const S2Job &j = m->job;
   const long long pts = (long long)j.P * j.P;
-  int nk = std::min(j.ring, 8);
+  int nk = std::min(j.ring, 16);
   // small jobs: too little work per launch to rank the variants; keep the default
   if (double(pts) * nk < 2.0e6) {
     sdf->eval_variant = 0;
@@ -517,6 +551,13 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
     }
     double ns = double(ms_best) * 1e6 / (double(pts) * nk);
     sdf->tune_ns[v] = ns;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, (const void *)sdf->k_eval[v]) == cudaSuccess) {
+      sdf->tune_regs[v] = fa.numRegs;
+      sdf->tune_local[v] = int(fa.localSizeBytes);
+    } else {
+      cudaGetLastError();
+    }
     if (ns < best) {
       best = ns;
       best_v = v;
@@ -639,6 +680,28 @@ int s2m_preprocess_source(const char *source, const char *base_dir, char **out, 
   return S2M_OK;
 }
 
+int s2m_csg_from_source(const char *source, float *program, uint32_t capacity, uint32_t *len, char *err,
+                        size_t errlen) {
+  if (!source || !len) {
+    set_err(err, errlen, "null argument");
+    return S2M_E_INVALID;
+  }
+  std::vector<float> prog;
+  std::string why;
+  const std::string pre = s2m::preprocess_sdf3d_text(source, "", "", nullptr);
+  if (!s2m::csg_from_source(pre, prog, why)) {
+    set_err(err, errlen, why);
+    return S2M_E_PARSE;
+  }
+  *len = uint32_t(prog.size());
+  if (program && capacity >= prog.size()) std::memcpy(program, prog.data(), prog.size() * sizeof(float));
+  else if (program) {
+    set_err(err, errlen, "program needs " + std::to_string(prog.size()) + " floats");
+    return S2M_E_OVERFLOW;
+  }
+  return S2M_OK;
+}
+
 int s2m_translate(const char *source, int lang, const char *sdf_name, char **out, double *fp32_ops,
                   double *sfu_ops, char *err, size_t errlen) {
   if (!source) return S2M_E_INVALID;
@@ -712,6 +775,15 @@ int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double 
   return v;
 }
 
+int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_t namelen, int *registers,
+                              int *local_bytes) {
+  if (!sdf || variant < 0 || variant >= kNumEvalVariants) return S2M_E_INVALID;
+  if (name && namelen) set_err(name, namelen, kEvalVariants[variant].name);
+  if (registers) *registers = sdf->tune_regs[variant];
+  if (local_bytes) *local_bytes = sdf->tune_local[variant];
+  return S2M_OK;
+}
+
 int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
   if (!sdf) return S2M_E_INVALID;
   if (fp32_ops) *fp32_ops = sdf->fp32_ops;
@@ -722,6 +794,7 @@ int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
 void s2m_sdf_free(s2m_sdf *sdf) {
   if (!sdf) return;
   if (sdf->lib) cudaLibraryUnload(sdf->lib);
+  if (sdf->qef_lib) cudaLibraryUnload(sdf->qef_lib);
   delete sdf;
 }
 
@@ -750,24 +823,26 @@ int s2m_mesh_run_async(s2m_mesh *m, void *stream) {
   if (!m || !m->sdf) return S2M_E_INVALID;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (m->use_graph && !m->profile) {
-    // capture the launch sequence once (per stream), then replay it: one
-    // launch call instead of one per kernel and memset
-    if (!m->graph || m->graph_stream != st) {
-      drop_graph(m);
+    // capture the launch sequence once, on a private stream (the legacy
+    // default stream cannot be captured), then replay it on the caller's
+    // stream: one launch call instead of one per kernel and memset
+    if (!m->graph) {
+      if (!m->capture_stream && cudaStreamCreateWithFlags(&m->capture_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return S2M_E_CUDA;
       cudaGraph_t g = nullptr;
-      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      cudaError_t e = cudaStreamBeginCapture(m->capture_stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
-        cudaError_t e2 = enqueue(m, st);
-        e = cudaStreamEndCapture(st, &g);
+        cudaError_t e2 = enqueue(m, m->capture_stream);
+        e = cudaStreamEndCapture(m->capture_stream, &g);
         if (e2 != cudaSuccess) e = e2;
       }
       if (e == cudaSuccess) e = cudaGraphInstantiate(&m->graph, g, 0);
       if (g) cudaGraphDestroy(g);
       if (e != cudaSuccess) {
+        cudaGetLastError();
         m->graph = nullptr;
         return S2M_E_CUDA;
       }
-      m->graph_stream = st;
     }
     return cudaGraphLaunch(m->graph, st) == cudaSuccess ? S2M_OK : S2M_E_CUDA;
   }
@@ -815,6 +890,7 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
   });
   if (!(m->params.eps > 0.0f)) m->params.eps = 1e-4f;
   int rc = setup_job(m, err, errlen);
+  if (rc == S2M_OK && m->job.qef) rc = ensure_qef_module(sdf, err, errlen);
   if (rc != S2M_OK) {
     delete m;
     return rc;
@@ -895,6 +971,11 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
     return S2M_E_INVALID;
   }
   out->resolution = uint32_t(m.N);
+  if (m.job.qef && !sdf->k_vertices_qef) {
+    set_err(err, errlen, "precision mode needs the SDF's QEF module, which loading allocates: run one "
+                         "s2m_mesh_create with S2M_JOB_QEF for this SDF first");
+    return S2M_E_INVALID;
+  }
   unsigned char *base = nullptr;
   rc = noalloc_scratch(&base, err, errlen);
   if (rc != S2M_OK) return rc;
@@ -1048,6 +1129,7 @@ void s2m_mesh_free(s2m_mesh *m) {
   for (cudaEvent_t e : m->ev) cudaEventDestroy(e);
   drop_graph(m);
   free_buffers(m);
+  if (m->capture_stream) cudaStreamDestroy(m->capture_stream);
   delete m;
 }
 

@@ -26,10 +26,19 @@ struct S2Cell {
 
 __device__ __forceinline__ S2Cell s2_cell_of(const S2Job &j, long long c, int zc0) {
   S2Cell r;
-  r.x = (int)(c % j.N);
-  long long q = c / j.N;
-  r.y = (int)(q % j.N);
-  r.z = zc0 + (int)(q / j.N);
+  if (c < 0x100000000ll) {
+    const unsigned cu = (unsigned)c, n = (unsigned)j.N;
+    const unsigned q = s2_udiv(cu, n, j.magic_n);
+    r.x = (int)(cu - q * n);
+    const unsigned z = s2_udiv(q, n, j.magic_n);
+    r.y = (int)(q - z * n);
+    r.z = zc0 + (int)z;
+  } else {
+    r.x = (int)(c % j.N);
+    long long q = c / j.N;
+    r.y = (int)(q % j.N);
+    r.z = zc0 + (int)(q / j.N);
+  }
   return r;
 }
 

@@ -33,35 +33,47 @@ struct S2UserSdf {
 // the occupancy the compiler must allow (__launch_bounds__ minimum blocks),
 // which trades registers against latency hiding; the runtime's autotuner
 // times them per SDF and keeps the fastest.
-template <int RUN>
+template <int RUN, bool PAIR>
 __device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restrict__ ring, int k0, int nk) {
-  long long idx = (long long)blockIdx.x * S2_EVAL_BLOCK + threadIdx.x;
-  long long pts = (long long)job.P * job.P;
+  const unsigned idx = blockIdx.x * S2_EVAL_BLOCK + threadIdx.x;  // P * P < 2^32
+  const unsigned pts = (unsigned)job.P * (unsigned)job.P;
   if (idx >= pts) return;
-  int i = (int)(idx % job.P);
-  int jy = (int)(idx / job.P);
+  const int jy = (int)s2_udiv(idx, (unsigned)job.P, job.magic_p);
+  const int i = (int)(idx - (unsigned)jy * (unsigned)job.P);
   float x = s2_coord(job, i), y = s2_coord(job, jy);
   int kb = k0 + (int)blockIdx.y * RUN;
   int ke = min(kb + RUN, k0 + nk);
   long long row = (long long)jy * job.pitch + i;
+  int k = kb;
+  if (PAIR) {
+    // two independent evaluations per iteration: instruction-level parallelism
 #pragma unroll 1
-  for (int k = kb; k < ke; ++k) {
+    for (; k + 1 < ke; k += 2) {
+      const float f0 = s2m_user_sdf(x, y, s2_coord(job, k));
+      const float f1 = s2m_user_sdf(x, y, s2_coord(job, k + 1));
+      ring[(long long)(k % job.ring) * job.plane + row] = f0;
+      ring[(long long)((k + 1) % job.ring) * job.plane + row] = f1;
+    }
+  }
+#pragma unroll 1
+  for (; k < ke; ++k) {
     float z = s2_coord(job, k);
     ring[(long long)(k % job.ring) * job.plane + row] = s2m_user_sdf(x, y, z);
   }
 }
 
-#define S2_EVAL_VARIANT(NAME, MINB, RUN)                                                          \
+#define S2_EVAL_VARIANT(NAME, MINB, RUN, PAIR)                                                    \
   extern "C" __global__ void __launch_bounds__(S2_EVAL_BLOCK, MINB)                               \
-  NAME(S2Job job, float *__restrict__ ring, int k0, int nk) { s2_eval_planes<RUN>(job, ring, k0, nk); }
+  NAME(S2Job job, float *__restrict__ ring, int k0, int nk) { s2_eval_planes<RUN, PAIR>(job, ring, k0, nk); }
 // Keep this table in step with kEvalVariants in runtime.cu.
-S2_EVAL_VARIANT(s2m_eval_b2r4, 2, 4)
-S2_EVAL_VARIANT(s2m_eval_b3r4, 3, 4)
-S2_EVAL_VARIANT(s2m_eval_b4r4, 4, 4)
-S2_EVAL_VARIANT(s2m_eval_b4r1, 4, 1)
-S2_EVAL_VARIANT(s2m_eval_b6r4, 6, 4)
-S2_EVAL_VARIANT(s2m_eval_b8r4, 8, 4)
+#ifndef S2M_QEF_MODULE
+S2_EVAL_VARIANT(s2m_eval_b2r4, 2, 4, false)
+S2_EVAL_VARIANT(s2m_eval_b3r4, 3, 4, false)
+S2_EVAL_VARIANT(s2m_eval_b4r4, 4, 4, false)
+S2_EVAL_VARIANT(s2m_eval_b3p4, 3, 4, true)
+#endif
 
+#ifndef S2M_QEF_MODULE
 // Cell pass of one slab (cell slices zc0 .. zc1 - 1): classify every cell and
 // append the candidates, in (z, y, x) order, to the job's candidate list at
 // cand.base[slab] + (look-back prefix over tiles), each with its 8 lattice
@@ -118,6 +130,8 @@ s2m_cells(S2Job job, S2Slab slab, S2Cand cand, int zc0, int zc1, int slab_index)
   }
 }
 
+#endif  // S2M_QEF_MODULE
+
 // Vertices of every candidate of the job, one candidate per thread (dense:
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
 // final key and writes cand.pos / cand.nrm for cells with a vertex.
@@ -136,7 +150,12 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
     float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     float pos[3], nrm[3];
     const S2UserSdf sdf;
-    unsigned long long key = job.qef ? s2_vertex_qef(sdf, job, c, v, pos, nrm) : s2_vertex(sdf, job, c, v, pos, nrm);
+#ifdef S2M_QEF_MODULE
+    // precision-mode module (compiled on the first QEF job of this SDF)
+    unsigned long long key = s2_vertex_qef(sdf, job, c, v, pos, nrm);
+#else
+    unsigned long long key = s2_vertex(sdf, job, c, v, pos, nrm);
+#endif
     cand.key[o] = key;
     if (key >> 63) {
       cand.pos[3 * o] = pos[0];

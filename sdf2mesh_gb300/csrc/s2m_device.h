@@ -22,7 +22,19 @@ struct S2Job {
   int lag;                 // 1: labels are z + 1 (reference slice lag)
   int exact;               // 1: re-evaluate off-lattice corners of every cell
   int qef;                 // 1: precision mode (lattice corners, QEF vertex, FP64 solve)
+  unsigned magic_n;        // floor(2^32 / N) + 1: division by N of 32-bit indices
+  unsigned magic_p;        // floor(2^32 / P) + 1
 };
+
+// Division of a 32-bit index by d (2 <= d < 2^31) with the precomputed
+// magic = floor(2^32 / d) + 1: the high product overestimates the quotient by
+// at most one, and the remainder's sign tells which.
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+__device__ __forceinline__ unsigned s2_udiv(unsigned c, unsigned d, unsigned magic) {
+  unsigned q = __umulhi(c, magic);
+  return ((int)(c - q * d) < 0) ? q - 1u : q;
+}
+#endif
 
 // Per-slab buffers of the cell pass.
 struct S2Slab {

@@ -205,3 +205,29 @@ def test_standard_normal_marker(lib):
               "               sdf3d(p + h.yyx) - sdf3d(p - h.yyx));\n}\n"
               "fn sdf3d(p: vec3f) -> f32 { return sdf3d_sphere(p, 0.5); }\n")
     assert "S2M_STD_NORMAL" not in lower(custom)[0]
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_csg_program_from_source(lib, oracle_lib, seed):
+    """The batching workload's .sdf3d sources convert to exactly the programs
+    the oracle evaluates, and the program evaluates like the source."""
+    src, prog = workloads.random_tree(seed)
+    got = s2m.Sdf3DShader.from_source(src).csg_program()
+    assert np.array_equal(got, np.asarray(prog, np.float32))
+
+
+def test_csg_program_rejects_other_sources(lib):
+    for src in (workloads.csg64()[0],
+                "use sdf3d::*;\nfn sdf3d(p: vec3f) -> f32 { return sdf3d_sphere(p * 2.0, 0.5); }\n",
+                "use sdf3d::*;\nfn sdf3d(p: vec3f) -> f32 { return sdf3d_sphere(p, p.x); }\n",
+                "fn sdf3d_sphere(p: vec3f, r: f32) -> f32 { return length(p) - 2.0 * r; }\n"
+                "fn sdf3d(p: vec3f) -> f32 { return sdf3d_sphere(p, 0.5); }\n"):
+        with pytest.raises(s2m.S2MError) as e:
+            s2m.Sdf3DShader.from_source(src).csg_program()
+        assert e.value.name == "PARSE"
+    prog = s2m.Sdf3DShader.from_source(
+        "use sdf3d::*;\nuse sdf::op;\nfn sdf3d(p: vec3f) -> f32 {\n"
+        "  return sdf_op_smooth_subtraction(sdf3d_box(p, vec3f(1.0)), max(sdf3d_torus(p - vec3(0.1, 0.0, 0.0), "
+        "vec2(0.5, 0.1)), -sdf3d_capsule(p, vec3(-1.0), vec3(1.0), 0.2)), 0.05);\n}\n").csg_program()
+    assert prog.tolist() == [1, 0, 0, 0, 1, 1, 1, 2, np.float32(0.1), 0, 0, 0.5, np.float32(0.1),
+                             3, -1, -1, -1, 1, 1, 1, np.float32(0.2), 11, 15, np.float32(0.05)]

@@ -93,3 +93,25 @@ def test_server_overflow_requeue(lib):
     b.run()
     assert_bit_exact(got, per_job_as_oracle(b.mesh(j)), "requeued request")
     server.close()
+
+
+def test_submit_source_routes_and_matches(lib):
+    """Requests as source text: CSG-shaped .sdf3d runs on the interpreter,
+    GLSL compiles once (cached) -- each result equals the per-job pipeline's
+    mesh of the same source."""
+    server = s2m.Server()
+    reqs = []
+    for seed in (2, 3, 7):
+        src, _ = workloads.random_tree(seed)
+        st = s2m.AppState(resolution=64, bounds=2.0)
+        reqs.append((server.submit_source(src, st), src, s2m.LANG_WGSL, st))
+    mb, _ = workloads.mandelbulb(8.0, 5, 2.0, 0.003)
+    for N in (40, 56):
+        st = s2m.AppState(resolution=N, bounds=2.5)
+        reqs.append((server.submit_source(mb, st, s2m.LANG_GLSL, "sdf"), mb, s2m.LANG_GLSL, st))
+    server.drain(600)
+    for rid, src, lang, st in reqs:
+        got = server.mesh(rid)
+        alone = s2m.generate(s2m.Sdf3DShader.from_source(src, lang, "sdf").compile(), st)
+        assert_bit_exact(got, per_job_as_oracle(alone), f"request {rid}")
+    server.close()
