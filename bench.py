@@ -209,6 +209,18 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def eval_traffic_per_point():
+    """DRAM bytes per lattice point of the evaluation kernel, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "s2m_eval_cells_csg64_512.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_point"):
+                return float(line.split("=")[1])
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -357,7 +369,12 @@ def ours(a):
         per_launch_ms = ms["eval_planes"] / n_eval
         t_fp32 = fp32_ops / fp32_peak
         t_sfu = sfu_ops / sfu_peak if sfu_peak > 0 else 0.0
-        common = {"kernel": "s2m_eval_*", "traffic": None, "ms_per_launch": per_launch_ms,
+        tpp = eval_traffic_per_point() if a.workload == "csg64_1024" else None
+        traffic = tpp * prof["eval_points"] / n_eval if tpp else None
+        common = {"kernel": "s2m_eval_*", "traffic": traffic, "traffic_source": (
+                      "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 512^3 case "
+                      "(profiles/s2m_eval_cells_csg64_512.md), scaled by points per launch") if traffic else None,
+                  "ms_per_launch": per_launch_ms,
                   "algorithmic": f"{fp32_ops:g} FP32 + {sfu_ops:g} SFU ops per lattice point x "
                                  f"{prof['eval_points'] / n_eval:.0f} points per launch",
                   "fp32_gops": eval_gops, "fp32_peak_gops": fp32_peak, "sfu_gops": eval_sfu,

@@ -43,6 +43,7 @@
 #define S2_CSG_STACK 32
 
 struct S2CsgSdf {
+  static constexpr bool kStdNormal = true;
   const float *prog;
   int len;
 
@@ -369,53 +370,15 @@ __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned ite
 // Classification tile `tile` of the job (the tickets of this stage come in
 // tile order, so the look-back only waits for tiles already taken).
 __device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned tile) {
-  __shared__ unsigned s_warp[32];
-  __shared__ unsigned long long s_excl;
-  const S2Job &job = J.job;
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const long long ncells = (long long)J.nzc * job.N * job.N;
+  const long long ncells = (long long)J.nzc * J.job.N * J.job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-  unsigned ballots[S2_CELL_CPT];
-#pragma unroll
-  for (int m = 0; m < S2_CELL_CPT; ++m) {
-    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
-    bool is_cand = c < ncells && s2_classify<true>(job, J.lattice, s2_cell_of(job, c, 0));
-    ballots[m] = __ballot_sync(S2_FULL, is_cand);
-    if (lane == 0) s_warp[m * 8 + warp] = __popc(ballots[m]);
-  }
-  __syncthreads();
-  if (warp == 0) {
-    unsigned tot = s2_warp_exclusive32(s_warp);
-    unsigned long long excl = s2_lookback(J.cell_status, tile, tot, J.mesh.err);
-    if (lane == 0) {
-      s_excl = excl;
-      if (tile == ntiles - 1) J.cand.base[1] = excl + tot;
-    }
-  }
-  __syncthreads();
-  const unsigned lt = s2_lanemask_lt();
-#pragma unroll
-  for (int m = 0; m < S2_CELL_CPT; ++m) {
-    if (!((ballots[m] >> lane) & 1u)) continue;
-    unsigned long long o = s_excl + s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
-    if (o >= J.cand.cap) {
-      atomicOr(J.mesh.err, S2_ERR_CAND_OVF);
-      continue;
-    }
-    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
-    S2Cell cell = s2_cell_of(job, c, 0);
-    float v[8];
-    s2_load_corners<true>(job, J.lattice, cell, v);
-    J.cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
-    float4 *dst = reinterpret_cast<float4 *>(J.cand.val + 8 * o);
-    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
-    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-  }
-  __syncthreads();  // s_warp / s_excl are reused by the block's next item
+  s2_cell_tile<true>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, tile, ntiles, ncells, 0, 0ull,
+                     J.cand.base + 1);
 }
 
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
   __shared__ unsigned s_chunk;
+  __shared__ S2WarpScratch s_ws[256 / 32];
   const S2Job &job = J.job;
   const S2CsgSdf f{J.prog, J.prog_len};
   const unsigned long long n = min(__ldcg(J.cand.base + 1), J.cand.cap);
@@ -427,17 +390,23 @@ __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
     __syncthreads();
     if (chunk >= nchunks) break;
     const unsigned long long o = (unsigned long long)chunk * S2_B_VERT_CHUNK + threadIdx.x;
-    if (o < n) {
-      unsigned long long k = __ldcg(J.cand.key + o);
-      S2Cell c;
-      c.x = (int)(k & 0xffffull);
-      c.y = (int)((k >> 16) & 0xffffull);
-      c.z = (int)((k >> 32) & 0xffffull);
+    const bool active = o < n;
+    unsigned long long k = active ? __ldcg(J.cand.key + o) : 0ull;
+    S2Cell c;
+    c.x = (int)(k & 0xffffull);
+    c.y = (int)((k >> 16) & 0xffffull);
+    c.z = (int)((k >> 32) & 0xffffull);
+    float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (active) {
       const float4 *src = reinterpret_cast<const float4 *>(J.cand.val + 8 * o);
       const float4 a = __ldcg(src), b = __ldcg(src + 1);
-      float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-      float pos[3], nrm[3];
-      const unsigned long long key = job.qef ? s2_vertex_qef(f, job, c, v, pos, nrm) : s2_vertex(f, job, c, v, pos, nrm);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    }
+    float pos[3], nrm[3];
+    unsigned long long key;
+    if (job.qef) key = active ? s2_vertex_qef(f, job, c, v, pos, nrm) : 0ull;
+    else key = s2_vertex_warp(f, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
+    if (active) {
       J.cand.key[o] = key;
       if (key >> 63) {
         J.cand.pos[3 * o] = pos[0];

@@ -83,6 +83,74 @@ __device__ __forceinline__ bool s2_classify(const S2Job &j, const float *__restr
   return false;
 }
 
+// Classification from values already loaded (same rule as s2_classify).
+__device__ __forceinline__ bool s2_classify_values(const S2Job &j, S2Cell c, const float v[8]) {
+  unsigned pos = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) pos |= (v[k] > 0.0f ? 1u : 0u) << k;
+  if (pos != 0u && pos != 0xffu) return true;
+  if (j.qef) return false;
+  const unsigned off = s2_off_mask(j, c);
+  if (!off) return false;
+  if (j.exact) return true;
+  bool near = false;
+#pragma unroll
+  for (int k = 1; k < 8; ++k) near |= ((off >> k) & 1u) && !(fabsf(v[k]) >= j.guard);
+  return near;
+}
+
+template <bool CG>
+__device__ __forceinline__ float4 s2_ld4(const float *p) {
+  return CG ? __ldcg(reinterpret_cast<const float4 *>(p)) : __ldg(reinterpret_cast<const float4 *>(p));
+}
+template <bool CG>
+__device__ __forceinline__ float s2_ld1(const float *p) {
+  return CG ? __ldcg(p) : __ldg(p);
+}
+
+// Four consecutive cells of the linear order starting at cell c0 (z, y, x):
+// their candidate bits (bit m for cell c0 + m, cells past `ncells` excluded)
+// and their corner values.  When N is a multiple of 4 the four cells share
+// a row and start at a multiple of 4, so each of the 4 corner rows is one
+// 16-byte load plus one scalar (8 loads for 4 cells instead of 32).
+template <bool CG>
+__device__ __forceinline__ unsigned s2_classify4(const S2Job &j, const float *__restrict__ ring, long long c0,
+                                                 long long ncells, int zc0, float v[4][8]) {
+  unsigned mask = 0;
+  if (c0 >= ncells) return 0u;
+  const S2Cell c = s2_cell_of(j, c0, zc0);
+  if ((j.N & 3) == 0 && c0 + 3 < ncells) {
+    const float *p0 = ring + (long long)(c.z % j.ring) * j.plane + (long long)c.y * j.pitch + c.x;
+    const float *p1 = ring + (long long)((c.z + 1) % j.ring) * j.plane + (long long)c.y * j.pitch + c.x;
+    const float *rows[4] = {p0, p0 + j.pitch, p1, p1 + j.pitch};  // (y, z) = 00, 10, 01, 11
+    float r[4][5];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 a = s2_ld4<CG>(rows[q]);
+      r[q][0] = a.x; r[q][1] = a.y; r[q][2] = a.z; r[q][3] = a.w;
+      r[q][4] = s2_ld1<CG>(rows[q] + 4);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      // corner index bx | by << 1 | bz << 2
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[m][k] = r[((k >> 1) & 1) | (((k >> 2) & 1) << 1)][m + (k & 1)];
+      S2Cell cm = c;
+      cm.x = c.x + m;
+      if (s2_classify_values(j, cm, v[m])) mask |= 1u << m;
+    }
+    return mask;
+  }
+#pragma unroll 1
+  for (int m = 0; m < 4; ++m) {
+    if (c0 + m >= ncells) break;
+    const S2Cell cm = s2_cell_of(j, c0 + m, zc0);
+    s2_load_corners<CG>(j, ring, cm, v[m]);
+    if (s2_classify_values(j, cm, v[m])) mask |= 1u << m;
+  }
+  return mask;
+}
+
 // sdf3d_normal.wgsl:4-10 as a loop with one sdf3d call site:
 // n = ((t0 + t1) + t2) + t3 with t_i = d_i * sdf3d(p + d_i * eps), the order
 // the library function adds in.
@@ -344,3 +412,199 @@ __device__ __forceinline__ unsigned long long s2_vertex_qef(const F &sdf, const 
   return key | (1ull << 63);
 }
 
+
+// One classification tile (S2_CELL_TILE cells, S2_CELL_BLOCK threads, 4
+// consecutive cells per thread): candidates appended in (z, y, x) order at
+// base + (look-back prefix over tiles), each with its 8 corner values; the
+// last tile stores the running total in *next_base.
+template <bool CG>
+__device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__restrict__ ring, const S2Cand &cand,
+                                             unsigned long long *status, unsigned *err, unsigned tile,
+                                             unsigned ntiles, long long ncells, int zc0, unsigned long long base,
+                                             unsigned long long *next_base) {
+  __shared__ unsigned s_warp[32];
+  __shared__ unsigned long long s_excl;
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const long long c0 = (long long)tile * S2_CELL_TILE + 4ll * tid;
+  float v[4][8];
+  const unsigned mask = s2_classify4<CG>(job, ring, c0, ncells, zc0, v);
+  const unsigned cnt = __popc(mask);
+  unsigned inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
+    if ((int)lane >= o) inc += t;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  if (tid < 32 && tid >= S2_CELL_BLOCK / 32) s_warp[tid] = 0u;
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned tot = s2_warp_exclusive32(s_warp);
+    const unsigned long long excl = s2_lookback(status, tile, tot, err);
+    if (lane == 0) {
+      s_excl = excl;
+      if (tile == ntiles - 1) *next_base = base + excl + tot;
+    }
+  }
+  __syncthreads();
+  unsigned long long o = base + s_excl + s_warp[warp] + (inc - cnt);
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    if (!((mask >> m) & 1u)) continue;
+    if (o >= cand.cap) {
+      atomicOr(err, S2_ERR_CAND_OVF);
+      ++o;
+      continue;
+    }
+    const S2Cell cell = s2_cell_of(job, c0 + m, zc0);
+    cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
+    float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
+    dst[0] = make_float4(v[m][0], v[m][1], v[m][2], v[m][3]);
+    dst[1] = make_float4(v[m][4], v[m][5], v[m][6], v[m][7]);
+    ++o;
+  }
+  __syncthreads();  // s_warp / s_excl are reused by the block's next tile
+}
+
+// ---------------------------------------------------------------------------
+// Vertices of the reference rule for a warp's 32 candidates at once.  The
+// evaluations a candidate needs -- its off-lattice corners, then the four
+// normal samples -- differ in number from lane to lane; here each warp lists
+// them in shared memory and evaluates the list 32 at a time, so every lane
+// evaluates the SDF on every pass.  Same coordinates, same arithmetic, same
+// order of the normal sum as s2_vertex: the same bits.  F::kStdNormal says
+// whether F's normal is the library's tetrahedral one (otherwise, and in
+// precision mode, the per-lane s2_vertex path runs).
+struct S2WarpScratch {
+  unsigned short req[32 * 8];
+  float val[32][8];
+  float lo[32][3], hi[32][3];
+  float pos[32][3];
+  float nv[32][4];
+};
+
+template <class F>
+__device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const S2Job &j, bool active, S2Cell c,
+                                                             float v[8], float pos[3], float nrm[3],
+                                                             S2WarpScratch &ws) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt = s2_lanemask_lt();
+  float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
+  float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
+  const unsigned off = active ? (s2_off_mask(j, c) & 0xfeu) : 0u;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ws.lo[lane][a] = mn[a];
+    ws.hi[lane][a] = mx[a];
+  }
+  // 1. off-lattice corners
+  unsigned cnt = __popc(off), inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
+    if ((int)lane >= o) inc += t;
+  }
+  const unsigned total = __shfl_sync(S2_FULL, inc, 31);
+  {
+    unsigned slot = inc - cnt, rem = off;
+    while (rem) {
+      const unsigned k = __ffs(rem) - 1;
+      rem &= rem - 1u;
+      ws.req[slot++] = (unsigned short)((lane << 3) | k);
+    }
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (unsigned r0 = 0; r0 < total; r0 += 32) {
+    const unsigned r = r0 + lane;
+    if (r < total) {
+      const unsigned q = ws.req[r], l = q >> 3, k = q & 7u;
+      const float x = (k & 1) ? ws.hi[l][0] : ws.lo[l][0];
+      const float y = (k & 2) ? ws.hi[l][1] : ws.lo[l][1];
+      const float z = (k & 4) ? ws.hi[l][2] : ws.lo[l][2];
+      ws.val[l][k] = sdf(x, y, z);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 1; k < 8; ++k)
+    if ((off >> k) & 1u) v[k] = ws.val[lane][k];
+  // 2. crossings and mass point (dualcontour.wgsl:86-131)
+  const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
+  const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
+  const int eax[12] = {2, 2, 2, 2, 1, 1, 1, 1, 0, 0, 0, 0};
+  const float eu[12] = {0, 0, 1, 1, 0, 0, 1, 1, 0, 0, 1, 1};
+  const float ev[12] = {0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 0, 1};
+  float avg[3] = {0.0f, 0.0f, 0.0f};
+  float count = 0.0f;
+#pragma unroll
+  for (int e = 0; e < 12; ++e) {
+    const float a = v[ea[e]], b = v[eb[e]];
+    if ((a > 0.0f) != (b > 0.0f)) {
+      const float t = __fdiv_rn(__fsub_rn(0.0f, a), __fsub_rn(b, a));
+      float w[3];
+      if (eax[e] == 2) { w[0] = eu[e]; w[1] = ev[e]; w[2] = t; }
+      else if (eax[e] == 1) { w[0] = eu[e]; w[1] = t; w[2] = ev[e]; }
+      else { w[0] = t; w[1] = eu[e]; w[2] = ev[e]; }
+      if (w[0] > 0.0f || w[1] > 0.0f || w[2] > 0.0f) {
+        avg[0] = __fadd_rn(avg[0], w[0]);
+        avg[1] = __fadd_rn(avg[1], w[1]);
+        avg[2] = __fadd_rn(avg[2], w[2]);
+        count = __fadd_rn(count, 1.0f);
+      }
+    }
+  }
+  const unsigned signs = (v[1] > 0.0f ? 1u : 0u) | (v[2] > 0.0f ? 2u : 0u) | (v[4] > 0.0f ? 4u : 0u) | (v[0] > 0.0f ? 8u : 0u);
+  const unsigned long long zl = (unsigned long long)(j.lag ? c.z + 1 : c.z);
+  const unsigned long long key = (unsigned long long)c.x | ((unsigned long long)c.y << 16) | (zl << 32) |
+                                 ((unsigned long long)signs << 48);
+  const bool has = active && count > 1.0f;
+  if (has) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float bsize = __fsub_rn(mx[a], mn[a]);
+      pos[a] = __fadd_rn(mn[a], __fdiv_rn(__fmul_rn(bsize, avg[a]), count));
+      ws.pos[lane][a] = pos[a];
+    }
+  }
+  // 3. the four tetrahedral normal samples of every vertex
+  const unsigned vb = __ballot_sync(S2_FULL, has);
+  const unsigned nreq = 4u * __popc(vb);
+  const unsigned myfirst = 4u * __popc(vb & lt);
+  if (has)
+    for (unsigned d = 0; d < 4; ++d) ws.req[myfirst + d] = (unsigned short)((lane << 3) | d);
+  __syncwarp();
+#pragma unroll 1
+  for (unsigned r0 = 0; r0 < nreq; r0 += 32) {
+    const unsigned r = r0 + lane;
+    if (r < nreq) {
+      const unsigned q = ws.req[r], l = q >> 3, d = q & 7u;
+      const float dx = (d == 0 || d == 3) ? 1.0f : -1.0f;
+      const float dy = (d >= 2) ? 1.0f : -1.0f;
+      const float dz = (d == 1 || d == 3) ? 1.0f : -1.0f;
+      ws.nv[l][d] = sdf(__fadd_rn(ws.pos[l][0], __fmul_rn(dx, j.eps)), __fadd_rn(ws.pos[l][1], __fmul_rn(dy, j.eps)),
+                        __fadd_rn(ws.pos[l][2], __fmul_rn(dz, j.eps)));
+    }
+  }
+  __syncwarp();
+  if (!has) return key;
+  float n[3];
+#pragma unroll
+  for (int d = 0; d < 4; ++d) {
+    const float dx = (d == 0 || d == 3) ? 1.0f : -1.0f;
+    const float dy = (d >= 2) ? 1.0f : -1.0f;
+    const float dz = (d == 1 || d == 3) ? 1.0f : -1.0f;
+    const float f = ws.nv[lane][d];
+    const float tx = __fmul_rn(dx, f), ty = __fmul_rn(dy, f), tz = __fmul_rn(dz, f);
+    if (d == 0) {
+      n[0] = tx; n[1] = ty; n[2] = tz;
+    } else {
+      n[0] = __fadd_rn(n[0], tx); n[1] = __fadd_rn(n[1], ty); n[2] = __fadd_rn(n[2], tz);
+    }
+  }
+  const float len = s2_len3(n);
+  nrm[0] = __fdiv_rn(n[0], len);
+  nrm[1] = __fdiv_rn(n[1], len);
+  nrm[2] = __fdiv_rn(n[2], len);
+  return key | (1ull << 63);
+}

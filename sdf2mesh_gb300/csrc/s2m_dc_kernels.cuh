@@ -16,6 +16,11 @@
 
 // The lowered user SDF as the evaluator of s2m_dc_core.cuh.
 struct S2UserSdf {
+#ifdef S2M_STD_NORMAL
+  static constexpr bool kStdNormal = true;
+#else
+  static constexpr bool kStdNormal = false;
+#endif
   __device__ __forceinline__ float operator()(float x, float y, float z) const { return s2m_user_sdf(x, y, z); }
   __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
 #ifdef S2M_STD_NORMAL
@@ -81,53 +86,14 @@ S2_EVAL_VARIANT(s2m_eval_b3p4, 3, 4, true)
 extern "C" __global__ void __launch_bounds__(S2_CELL_BLOCK)
 s2m_cells(S2Job job, S2Slab slab, S2Cand cand, int zc0, int zc1, int slab_index) {
   __shared__ unsigned s_tile;
-  __shared__ unsigned s_warp[32];
-  __shared__ unsigned long long s_excl;
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  if (tid == 0) s_tile = atomicAdd(slab.tile_counter, 1u);
+  if (threadIdx.x == 0) s_tile = atomicAdd(slab.tile_counter, 1u);
   __syncthreads();
   const unsigned tile = s_tile;
   const long long ncells = (long long)(zc1 - zc0) * job.N * job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
   if (tile >= ntiles) return;
-  const unsigned long long base = cand.base[slab_index];
-
-  unsigned ballots[S2_CELL_CPT];
-#pragma unroll
-  for (int m = 0; m < S2_CELL_CPT; ++m) {
-    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
-    bool is_cand = c < ncells && s2_classify(job, slab.ring, s2_cell_of(job, c, zc0));
-    ballots[m] = __ballot_sync(S2_FULL, is_cand);
-    if (lane == 0) s_warp[m * 8 + warp] = __popc(ballots[m]);
-  }
-  __syncthreads();
-  if (warp == 0) {
-    unsigned tot = s2_warp_exclusive32(s_warp);
-    unsigned long long excl = s2_lookback(slab.status, tile, tot, slab.err);
-    if (lane == 0) {
-      s_excl = excl;
-      if (tile == ntiles - 1) cand.base[slab_index + 1] = base + excl + tot;
-    }
-  }
-  __syncthreads();
-  const unsigned lt = s2_lanemask_lt();
-#pragma unroll
-  for (int m = 0; m < S2_CELL_CPT; ++m) {
-    if (!((ballots[m] >> lane) & 1u)) continue;
-    unsigned long long o = base + s_excl + s_warp[m * 8 + warp] + __popc(ballots[m] & lt);
-    if (o >= cand.cap) {
-      atomicOr(slab.err, S2_ERR_CAND_OVF);
-      continue;
-    }
-    long long c = (long long)tile * S2_CELL_TILE + m * S2_CELL_BLOCK + tid;
-    S2Cell cell = s2_cell_of(job, c, zc0);
-    float v[8];
-    s2_load_corners(job, slab.ring, cell, v);
-    cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
-    float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
-    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
-    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-  }
+  s2_cell_tile<false>(job, slab.ring, cand, slab.status, slab.err, tile, ntiles, ncells, zc0, cand.base[slab_index],
+                      cand.base + slab_index + 1);
 }
 
 #endif  // S2M_QEF_MODULE
@@ -137,25 +103,36 @@ s2m_cells(S2Job job, S2Slab slab, S2Cand cand, int zc0, int zc1, int slab_index)
 // final key and writes cand.pos / cand.nrm for cells with a vertex.
 extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
+  __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
-  for (unsigned long long o = (unsigned long long)blockIdx.x * S2_VX_BLOCK + threadIdx.x; o < n;
-       o += (unsigned long long)gridDim.x * S2_VX_BLOCK) {
-    unsigned long long k = cand.key[o];
+  const S2UserSdf sdf;
+  // grid-stride over warp-sized runs of candidates, all lanes together
+  const unsigned long long stride = (unsigned long long)gridDim.x * S2_VX_BLOCK;
+  for (unsigned long long base = (unsigned long long)blockIdx.x * S2_VX_BLOCK + (threadIdx.x & ~31u); base < n;
+       base += stride) {
+    const unsigned long long o = base + (threadIdx.x & 31u);
+    const bool active = o < n;
+    unsigned long long k = active ? cand.key[o] : 0ull;
     S2Cell c;
     c.x = (int)(k & 0xffffull);
     c.y = (int)((k >> 16) & 0xffffull);
     c.z = (int)((k >> 32) & 0xffffull);
-    const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
-    float4 a = src[0], b = src[1];
-    float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (active) {
+      const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
+      const float4 a = src[0], b = src[1];
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    }
     float pos[3], nrm[3];
-    const S2UserSdf sdf;
+    unsigned long long key;
 #ifdef S2M_QEF_MODULE
     // precision-mode module (compiled on the first QEF job of this SDF)
-    unsigned long long key = s2_vertex_qef(sdf, job, c, v, pos, nrm);
+    key = active ? s2_vertex_qef(sdf, job, c, v, pos, nrm) : 0ull;
 #else
-    unsigned long long key = s2_vertex(sdf, job, c, v, pos, nrm);
+    if (S2UserSdf::kStdNormal) key = s2_vertex_warp(sdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
+    else key = active ? s2_vertex(sdf, job, c, v, pos, nrm) : 0ull;
 #endif
+    if (!active) continue;
     cand.key[o] = key;
     if (key >> 63) {
       cand.pos[3 * o] = pos[0];

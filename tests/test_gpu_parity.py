@@ -305,3 +305,25 @@ def test_graph_replay_identical(lib):
     dm.close()
     assert_bit_exact(again, oracle.mesh(oracle.CSG, prm, 80, 2.0), "graph replay")
     assert np.array_equal(first.triangle_indices, again.triangle_indices)
+
+
+# Error of the binary32 reference rule against the same rule in binary64:
+# topology equal outside tie cells (a corner within 1e-6 of zero), common
+# vertices within REF_RULE_TOL_CELLS cell sizes.
+REF_RULE_TOL_CELLS = 5e-4  # measured 8.6e-5 on these cases
+
+
+@pytest.mark.parametrize("case", ["torus128", "csg128"])
+def test_reference_rule_against_fp64_oracle(lib, case):
+    if case == "torus128":
+        src, prm = workloads.torus()
+        kind = oracle.TORUS
+    else:
+        src, prm = workloads.csg64(seed=0)
+        kind = oracle.CSG
+    N = 128
+    gpu = run(s2m.Sdf3DShader.from_source(src).compile(), N)
+    ref = oracle.mesh(kind, prm, N, 2.0, precision=oracle.F64)
+    r = compare_with_ties(gpu, ref, kind, prm, N, 2.0, eps=1e-6, h=2.0 / (N - 1))
+    assert r["tri_diff_unexplained"] == 0, r
+    assert r["max_pos_err_cells"] < REF_RULE_TOL_CELLS, r
