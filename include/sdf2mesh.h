@@ -43,7 +43,11 @@ typedef enum {
   S2M_E_NO_DEVICE = 10    /* no CUDA device                                       */
 } s2m_status;
 
-typedef enum { S2M_LANG_WGSL = 0, S2M_LANG_GLSL = 1 } s2m_lang;
+/* S2M_LANG_SHADERTOY: ShaderToy-style GLSL as the site stores it (no version
+   line, uniforms or main), wrapped as shadertoy.rs:154-166 does; its inputs
+   (iTime, iResolution, iMouse ...) are constant zero.  The HTTP fetch of the
+   reference (--shadertoy-id) is not offered: files only. */
+typedef enum { S2M_LANG_WGSL = 0, S2M_LANG_GLSL = 1, S2M_LANG_SHADERTOY = 2 } s2m_lang;
 
 /* Compile flags. */
 #define S2M_COMPILE_FMAD 0x1u  /* allow FMA contraction: faster, no longer bit-exact

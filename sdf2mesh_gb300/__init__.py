@@ -27,13 +27,13 @@ import numpy as np
 __all__ = [
     "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate", "Batch", "Server",
     "load_library", "translate", "wgsl_remove_function", "wgsl_rename_function", "wgsl_has_function",
-    "LANG_WGSL", "LANG_GLSL", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "JOB_QEF", "COMPILE_FMAD",
+    "LANG_WGSL", "LANG_GLSL", "LANG_SHADERTOY", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "JOB_QEF", "COMPILE_FMAD",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libsdf2mesh_gb300.so")
 
-LANG_WGSL, LANG_GLSL = 0, 1
+LANG_WGSL, LANG_GLSL, LANG_SHADERTOY = 0, 1, 2
 COMPILE_FMAD = 0x1
 JOB_POW2_ROUNDING, JOB_SLICE_LAG, JOB_EXACT_CORNERS, JOB_QEF = 0x1, 0x2, 0x4, 0x8
 

@@ -59,7 +59,7 @@ struct S2CsgSdf {
     return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
   }
 
-  __device__ float operator()(float x, float y, float z) const {
+  __device__ __noinline__ float operator()(float x, float y, float z) const {
     float st[S2_CSG_STACK];
     int sp = 0;
     int i = 0;

@@ -39,6 +39,7 @@ void usage() {
                "  -i, --sdf <SDF>                Input SDF file\n"
                "      --shadertoy-id <ID>        Input ShaderToy shader ID (unavailable: no network)\n"
                "      --shadertoy-sdf <NAME>     ShaderToy SDF name [default: sdf]\n"
+               "      --shadertoy-file <FILE>    ShaderToy-style code from a file (inputs are zero)\n"
                "      --glsl <GLSL>              Input GLSL fragment shader\n"
                "      --glsl-sdf <NAME>          GLSL SDF name [default: sdf]\n"
                "  -0, --mesh <MESH>              Output mesh file (supports STL and PLY output)\n"
@@ -65,7 +66,8 @@ bool read_text(const std::string &path, std::string &out) {
 }  // namespace
 
 int main(int argc, char **argv) {
-  std::string sdf, glsl, glsl_sdf = "sdf", mesh, debug_wgsl, debug_cuda, shadertoy_id;
+  std::string sdf, glsl, glsl_sdf = "sdf", mesh, debug_wgsl, debug_cuda, shadertoy_id, shadertoy_file,
+      shadertoy_sdf = "sdf";
   unsigned long resolution = 256;
   double bounds = 2.0;
   bool exact_res = false, no_lag = false, fmad = false;
@@ -101,7 +103,11 @@ int main(int argc, char **argv) {
       if (!value(glsl_sdf)) return 2;
     } else if (a == "--shadertoy-id") {
       if (!value(shadertoy_id)) return 2;
-    } else if (a == "--shadertoy-sdf" || a == "--debug-png") {
+    } else if (a == "--shadertoy-sdf") {
+      if (!value(shadertoy_sdf)) return 2;
+    } else if (a == "--shadertoy-file") {
+      if (!value(shadertoy_file)) return 2;
+    } else if (a == "--debug-png") {
       if (!value(tmp)) return 2;
     } else if (a == "-0" || a == "--mesh") {
       if (!value(mesh)) return 2;
@@ -157,6 +163,14 @@ int main(int argc, char **argv) {
     }
     source = pre;
     s2m_free_string(pre);
+  } else if (!shadertoy_file.empty()) {
+    log("INFO", "Reading SDF from ShaderToy-style file " + shadertoy_file + "...");
+    if (!read_text(shadertoy_file, source)) {
+      log("ERROR", "could not read " + shadertoy_file);
+      return 1;
+    }
+    lang = S2M_LANG_SHADERTOY;
+    glsl_sdf = shadertoy_sdf;
   } else if (!glsl.empty()) {
     log("INFO", "Reading SDF from GLSL fragment shader " + glsl + "...");
     if (!read_text(glsl, source)) {

@@ -39,6 +39,9 @@ bool preprocess_sdf3d_file(const std::string &path, std::string &out, std::strin
 std::string preprocess_sdf3d_text(const std::string &src, const std::string &self_path,
                                   const std::string &base_dir, std::vector<std::string> *log);
 
+// ShaderToy-style code wrapped into a GLSL fragment shader (shadertoy.rs:154-166).
+std::string shadertoy_wrap(const std::string &code);
+
 // Parse, check and lower a complete source.  For GLSL, `sdf_name` is the
 // function with signature float(vec3) (shader.rs:89-98); a wrapper `sdf3d`
 // is generated when the source has none.

@@ -184,6 +184,19 @@ static void expand(const std::string &text, const std::string &self_path, const 
   }
 }
 
+// ShaderToy-style code as the site stores it (no version line, no uniform
+// declarations, no main): wrapped as shadertoy.rs:154-166 does before
+// conversion.  The inputs are the site's documented shader inputs; here they
+// are uniforms the frontend folds to zero (there is no render loop).
+std::string shadertoy_wrap(const std::string &code) {
+  std::string g = "#version 450 core\n";
+  g += "uniform vec3 iResolution;\nuniform float iTime;\nuniform float iTimeDelta;\nuniform int iFrame;\n";
+  g += "uniform vec4 iChannelTime;\nuniform vec4 iMouse;\nuniform vec4 iDate;\nuniform float iSampleRate;\n";
+  g += code;
+  g += "\nvoid main() {}\n";
+  return g;
+}
+
 std::string preprocess_sdf3d_text(const std::string &src, const std::string &self_path,
                                   const std::string &base_dir, std::vector<std::string> *log) {
   std::string out;

@@ -705,7 +705,8 @@ int s2m_csg_from_source(const char *source, float *program, uint32_t capacity, u
 int s2m_translate(const char *source, int lang, const char *sdf_name, char **out, double *fp32_ops,
                   double *sfu_ops, char *err, size_t errlen) {
   if (!source) return S2M_E_INVALID;
-  s2m::FrontendResult r = s2m::translate(source, lang == S2M_LANG_GLSL ? s2m::Lang::GLSL : s2m::Lang::WGSL,
+  const std::string text = lang == S2M_LANG_SHADERTOY ? s2m::shadertoy_wrap(source) : std::string(source);
+  s2m::FrontendResult r = s2m::translate(text, lang == S2M_LANG_WGSL ? s2m::Lang::WGSL : s2m::Lang::GLSL,
                                          sdf_name ? sdf_name : "sdf");
   if (!r.ok) {
     set_err(err, errlen, r.error);
@@ -721,7 +722,8 @@ int s2m_compile(const char *source, int lang, const char *sdf_name, uint32_t com
                 char *err, size_t errlen) {
   if (!source || !out) return S2M_E_INVALID;
   *out = nullptr;
-  s2m::FrontendResult r = s2m::translate(source, lang == S2M_LANG_GLSL ? s2m::Lang::GLSL : s2m::Lang::WGSL,
+  const std::string text = lang == S2M_LANG_SHADERTOY ? s2m::shadertoy_wrap(source) : std::string(source);
+  s2m::FrontendResult r = s2m::translate(text, lang == S2M_LANG_WGSL ? s2m::Lang::WGSL : s2m::Lang::GLSL,
                                          sdf_name ? sdf_name : "sdf");
   if (!r.ok) {
     set_err(err, errlen, r.error);
@@ -745,7 +747,7 @@ int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t 
                      char *err, size_t errlen) {
   if (!path || !out) return S2M_E_INVALID;
   std::string text;
-  if (lang == S2M_LANG_GLSL) {
+  if (lang != S2M_LANG_WGSL) {
     std::ifstream f(path, std::ios::binary);
     if (!f) {
       set_err(err, errlen, std::string("could not read ") + path);

@@ -413,10 +413,12 @@ __device__ __forceinline__ unsigned long long s2_vertex_qef(const F &sdf, const 
 }
 
 
-// One classification tile (S2_CELL_TILE cells, S2_CELL_BLOCK threads, 4
-// consecutive cells per thread): candidates appended in (z, y, x) order at
-// base + (look-back prefix over tiles), each with its 8 corner values; the
-// last tile stores the running total in *next_base.
+// One classification tile (S2_CELL_TILE cells, S2_CELL_BLOCK threads,
+// S2_CELL_CPT consecutive cells per thread in groups of 4): candidates
+// appended in (z, y, x) order at base + (look-back prefix over tiles), each
+// with its 8 corner values; the last tile stores the running total in
+// *next_base.  Large tiles keep the look-back short: all resident tiles start
+// together and each walks back over the aggregates of those still running.
 template <bool CG>
 __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__restrict__ ring, const S2Cand &cand,
                                              unsigned long long *status, unsigned *err, unsigned tile,
@@ -425,9 +427,13 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
   __shared__ unsigned s_warp[32];
   __shared__ unsigned long long s_excl;
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const long long c0 = (long long)tile * S2_CELL_TILE + 4ll * tid;
-  float v[4][8];
-  const unsigned mask = s2_classify4<CG>(job, ring, c0, ncells, zc0, v);
+  const long long c0 = (long long)tile * S2_CELL_TILE + (long long)S2_CELL_CPT * tid;
+  unsigned mask = 0;  // bit g * 4 + m: cell c0 + 4g + m
+#pragma unroll
+  for (int g = 0; g < S2_CELL_CPT / 4; ++g) {
+    float v[4][8];
+    mask |= s2_classify4<CG>(job, ring, c0 + 4 * g, ncells, zc0, v) << (4 * g);
+  }
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
 #pragma unroll
@@ -448,19 +454,22 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
   }
   __syncthreads();
   unsigned long long o = base + s_excl + s_warp[warp] + (inc - cnt);
-#pragma unroll
-  for (int m = 0; m < 4; ++m) {
-    if (!((mask >> m) & 1u)) continue;
+  unsigned rem = mask;
+  while (rem) {
+    const int m = __ffs(rem) - 1;
+    rem &= rem - 1u;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
       ++o;
       continue;
     }
     const S2Cell cell = s2_cell_of(job, c0 + m, zc0);
+    float v[8];
+    s2_load_corners<CG>(job, ring, cell, v);  // candidates are few: re-read their corners
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
     float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
-    dst[0] = make_float4(v[m][0], v[m][1], v[m][2], v[m][3]);
-    dst[1] = make_float4(v[m][4], v[m][5], v[m][6], v[m][7]);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
     ++o;
   }
   __syncthreads();  // s_warp / s_excl are reused by the block's next tile

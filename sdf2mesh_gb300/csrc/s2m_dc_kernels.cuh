@@ -14,6 +14,28 @@
 // reference's 8 values.  All arithmetic of the vertex rule uses explicitly
 // rounded binary32 intrinsics (no contraction, whatever the SDF's flags).
 
+// One out-of-line copy of the SDF for the vertex kernels: they evaluate it at
+// several call sites (off-lattice corners, normal samples, crossings), and
+// inlining each would multiply a large body beyond the instruction cache.
+__device__ __noinline__ float s2_user_sdf_call(float x, float y, float z) { return s2m_user_sdf(x, y, z); }
+
+struct S2UserSdfCall {
+#ifdef S2M_STD_NORMAL
+  static constexpr bool kStdNormal = true;
+#else
+  static constexpr bool kStdNormal = false;
+#endif
+  __device__ __forceinline__ float operator()(float x, float y, float z) const { return s2_user_sdf_call(x, y, z); }
+  __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
+#ifdef S2M_STD_NORMAL
+    s2_tetra_normal(*this, px, py, pz, eps, n);
+#else
+    s2v3 r = s2m_user_normal(s2mk(px, py, pz), eps);
+    n[0] = r.x; n[1] = r.y; n[2] = r.z;
+#endif
+  }
+};
+
 // The lowered user SDF as the evaluator of s2m_dc_core.cuh.
 struct S2UserSdf {
 #ifdef S2M_STD_NORMAL
@@ -105,7 +127,7 @@ extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
   __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
-  const S2UserSdf sdf;
+  const S2UserSdfCall sdf;
   // grid-stride over warp-sized runs of candidates, all lanes together
   const unsigned long long stride = (unsigned long long)gridDim.x * S2_VX_BLOCK;
   for (unsigned long long base = (unsigned long long)blockIdx.x * S2_VX_BLOCK + (threadIdx.x & ~31u); base < n;
@@ -129,7 +151,7 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
     // precision-mode module (compiled on the first QEF job of this SDF)
     key = active ? s2_vertex_qef(sdf, job, c, v, pos, nrm) : 0ull;
 #else
-    if (S2UserSdf::kStdNormal) key = s2_vertex_warp(sdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
+    if (S2UserSdfCall::kStdNormal) key = s2_vertex_warp(sdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
     else key = active ? s2_vertex(sdf, job, c, v, pos, nrm) : 0ull;
 #endif
     if (!active) continue;

@@ -85,7 +85,7 @@ struct S2MeshDev {
 #define S2_ERR_INDEX_OVF 0x10u    /* more than 2^32 - 2 vertices                */
 
 #define S2_CELL_BLOCK 256
-#define S2_CELL_CPT 4
+#define S2_CELL_CPT 16
 #define S2_CELL_TILE (S2_CELL_BLOCK * S2_CELL_CPT)
 #define S2_EVAL_BLOCK 256
 #define S2_EVAL_RUN 4

@@ -231,3 +231,18 @@ def test_csg_program_rejects_other_sources(lib):
         "vec2(0.5, 0.1)), -sdf3d_capsule(p, vec3(-1.0), vec3(1.0), 0.2)), 0.05);\n}\n").csg_program()
     assert prog.tolist() == [1, 0, 0, 0, 1, 1, 1, 2, np.float32(0.1), 0, 0, 0.5, np.float32(0.1),
                              3, -1, -1, -1, 1, 1, 1, np.float32(0.2), 11, 15, np.float32(0.05)]
+
+
+def test_shadertoy_style_file(lib, oracle_lib):
+    """ShaderToy-style code (no version line, uniforms or main; shadertoy.rs:154-166):
+    wrapped, inputs folded to zero, mainImage ignored."""
+    code = ("float sdSphere(vec3 p, float r) { return length(p) - r; }\n"
+            "float sdf(vec3 p) { return sdSphere(p, 0.5 + 0.25 * sin(iTime)) + 0.0 * iResolution.x; }\n"
+            "void mainImage(out vec4 fragColor, in vec2 fragCoord) {\n"
+            "  fragColor = vec4(sdf(vec3(fragCoord / iResolution.xy, 0.0)));\n}\n")
+    cuda, _, _ = s2m.translate(code, s2m.LANG_SHADERTOY, "sdf")
+    p = points(2000)
+    assert_same_bits(eval_host(cuda, p), oracle.evaluate(oracle.SPHERE, [0.5], p))
+    with pytest.raises(s2m.S2MError) as e:
+        s2m.translate(code, s2m.LANG_SHADERTOY, "missing")
+    assert e.value.name == "MISSING_SDF"
