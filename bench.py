@@ -211,7 +211,7 @@ class Clocks:
 
 def eval_traffic_per_point():
     """DRAM bytes per lattice point of the evaluation kernel, from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "s2m_eval_cells_csg64_512.md")
+    p = os.path.join(ROOT, "profiles", "s2m_eval_csg64_512.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_point"):
@@ -373,7 +373,7 @@ def ours(a):
         traffic = tpp * prof["eval_points"] / n_eval if tpp else None
         common = {"kernel": "s2m_eval_*", "traffic": traffic, "traffic_source": (
                       "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 512^3 case "
-                      "(profiles/s2m_eval_cells_csg64_512.md), scaled by points per launch") if traffic else None,
+                      "(profiles/s2m_eval_csg64_512.md), scaled by points per launch") if traffic else None,
                   "ms_per_launch": per_launch_ms,
                   "algorithmic": f"{fp32_ops:g} FP32 + {sfu_ops:g} SFU ops per lattice point x "
                                  f"{prof['eval_points'] / n_eval:.0f} points per launch",
