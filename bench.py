@@ -354,8 +354,16 @@ def ours(a):
         nl = prof["launches"][k]
         kernels[k] = {"launches_per_step": nl // a.steps, "ms_per_step": ms[k] / a.steps,
                       "share": ms[k] / max(1e-9, sum(ms.values()))}
+    # ops the evaluation kernel executes per point: the SDF as written, or, when the autotuner
+    # picked a run-of-4 variant, its run form (the x/y-only part once per 4 points)
+    variant = sdf.eval_variant()[0]
+    run_counts = sdf.run_op_counts()
+    per_point_scalar = (fp32_ops, sfu_ops)
+    if run_counts and "v4" in variant:
+        fp32_ops, sfu_ops = run_counts
     eval_gops = fp32_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
     eval_sfu = sfu_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
+    scalar_equiv_gops = per_point_scalar[0] * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
     # contouring passes: bytes they must move per job (state them in one place)
     V, T = nverts, ntris
     contour_bytes = (V * (32 + 32)            # vcompact: candidate read + vertex write (pos, nrm, key)
@@ -378,6 +386,9 @@ def ours(a):
                   "algorithmic": f"{fp32_ops:g} FP32 + {sfu_ops:g} SFU ops per lattice point x "
                                  f"{prof['eval_points'] / n_eval:.0f} points per launch",
                   "fp32_gops": eval_gops, "fp32_peak_gops": fp32_peak, "sfu_gops": eval_sfu,
+                  "variant": variant, "per_point_ops_as_written": {"fp32": per_point_scalar[0], "sfu": per_point_scalar[1]},
+                  "per_point_ops_executed": {"fp32": fp32_ops, "sfu": sfu_ops},
+                  "fp32_gops_as_written": scalar_equiv_gops,
                   "sfu_peak_gops": sfu_peak, "dominant_by_time": dom,
                   "peak_source": "measured in this run: s2m_fp32_probe (FP32 add/mul issue rate) and "
                                  "s2m_sfu_probe (MUFU rsqrt issue rate); MEASURED_PEAKS.json has neither"}

@@ -127,12 +127,16 @@ const char *s2m_sdf_cuda_source(const s2m_sdf *sdf);
 
 /* Algorithmic FP32 and SFU operations of one sdf3d evaluation. */
 int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops);
+/* Operations per point when the lattice kernel evaluates runs of 4 points
+   sharing x and y (the part that depends only on x and y runs once per run);
+   S2M_E_INVALID when the SDF has no run form (branches, loops). */
+int s2m_sdf_run_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops);
 
 /* Evaluation-kernel variant the autotuner chose for this SDF on its first
    job (-1: not tuned yet): its name, and the measured ns per lattice point
    of each of the S2M_EVAL_VARIANTS variants.  No reference counterpart (the
    reference has one fixed kernel, dualcontour.wgsl:161-162). */
-#define S2M_EVAL_VARIANTS 4
+#define S2M_EVAL_VARIANTS 5
 int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point);
 /* Name, registers per thread and local (spill) bytes per thread of one
    variant, as the tuner recorded them (0 before tuning). */

@@ -128,6 +128,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                   ctypes.c_char_p, sz], i),
             "s2m_sdf_cuda_source": ([vp], ctypes.c_char_p),
             "s2m_sdf_op_counts": ([vp, dp, dp], i),
+            "s2m_sdf_run_op_counts": ([vp, dp, dp], i),
             "s2m_sdf_free": ([vp], None),
             "s2m_sdf_eval_variant": ([vp, ctypes.c_char_p, sz, dp], i),
             "s2m_sdf_eval_variant_info": ([vp, i, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
@@ -254,6 +255,12 @@ class CompiledSdf:
     def cuda_source(self) -> str:
         return load_library().s2m_sdf_cuda_source(self._h).decode()
 
+    def run_op_counts(self):
+        """Ops per point in runs of 4 sharing x and y, or None when the SDF has no run form."""
+        fp, sfu = ctypes.c_double(), ctypes.c_double()
+        rc = load_library().s2m_sdf_run_op_counts(self._h, ctypes.byref(fp), ctypes.byref(sfu))
+        return (fp.value, sfu.value) if rc == 0 else None
+
     def op_counts(self):
         fp, sfu = ctypes.c_double(), ctypes.c_double()
         load_library().s2m_sdf_op_counts(self._h, ctypes.byref(fp), ctypes.byref(sfu))
@@ -262,7 +269,7 @@ class CompiledSdf:
     def eval_variant(self):
         """(name, ns per lattice point of each variant) chosen by the autotuner; name is 'untuned' before the first job."""
         name = ctypes.create_string_buffer(64)
-        ns = (ctypes.c_double * 4)()
+        ns = (ctypes.c_double * 5)()
         load_library().s2m_sdf_eval_variant(self._h, name, 64, ns)
         return name.value.decode(), list(ns)
 

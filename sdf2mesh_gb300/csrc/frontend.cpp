@@ -2525,6 +2525,262 @@ class Emitter {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Run-of-4 lowering.  The lattice kernel evaluates runs of 4 points that
+// share x and y and differ in z.  For a straight-line SDF (no branches or
+// loops, float scalars and vectors only), this emits
+//     s2m_user_sdf_run4(float x, float y, const s2x4 &z, s2x4 &out)
+// with vectors split into components and user functions inlined; every
+// scalar that depends only on p.x and p.y is computed once per run as a
+// float, every other one as an s2x4 (4 lanes, one per point).  Each lane runs
+// the same operations in the same order as s2m_user_sdf, so the values are
+// identical; the shared part is simply not repeated.  Anything else throws
+// RunBail and the SDF keeps only the per-point form.
+
+struct RunBail {};
+struct RVal {
+  std::string code;
+  bool var = false;  // depends on p.z
+};
+using RVec = std::vector<RVal>;
+
+class RunEmitter {
+ public:
+  std::ostringstream out;
+  int tmp = 0;
+  int depth = 0;
+  double fp_u = 0, fp_v = 0, sfu_u = 0, sfu_v = 0;  // ops per run (uniform once, varying per lane)
+  std::map<const Sym *, RVec> env;
+
+  [[noreturn]] static void bail() { throw RunBail{}; }
+
+  static Ty out_t(const Expr *e) { return e->want.b != B::Void ? e->want : concrete(e->t); }
+
+  RVal bind(const std::string &code, bool var, bool sfu = false) {
+    std::string n = "r" + std::to_string(tmp++);
+    out << "  const " << (var ? "s2x4 " : "float ") << n << " = " << code << ";\n";
+    double &c = sfu ? (var ? sfu_v : sfu_u) : (var ? fp_v : fp_u);
+    c += var ? 4.0 : 1.0;
+    return {n, var};
+  }
+
+  static RVec lit(const Ty &t, const std::vector<double> &cv) {
+    if (t.b != B::F32 || is_mat(t)) bail();
+    RVec r;
+    for (int i = 0; i < t.n; ++i) r.push_back({flit(float(cv.empty() ? 0.0 : (cv.size() == 1 ? cv[0] : cv[size_t(i)]))), false});
+    return r;
+  }
+
+  static RVec bcast(const RVec &v, size_t n) {
+    if (v.size() == n) return v;
+    if (v.size() != 1) bail();
+    return RVec(n, v[0]);
+  }
+
+  // fn(args...) lane-wise: the scalar builtin when every argument is uniform,
+  // its run form s2r_<name> otherwise.
+  RVal call(const std::string &name, const std::vector<RVal> &a, bool sfu) {
+    bool var = false;
+    std::string args;
+    for (size_t i = 0; i < a.size(); ++i) {
+      var = var || a[i].var;
+      args += (i ? ", " : "") + a[i].code;
+    }
+    return bind((var ? "s2r_" + name.substr(3) : name) + "(" + args + ")", var, sfu);
+  }
+
+  RVec componentwise(const std::string &fn, const std::vector<RVec> &args, bool sfu) {
+    size_t n = 1;
+    for (const RVec &a : args) n = std::max(n, a.size());
+    std::vector<RVec> b;
+    for (const RVec &a : args) b.push_back(bcast(a, n));
+    RVec r;
+    for (size_t i = 0; i < n; ++i) {
+      std::vector<RVal> ai;
+      for (const RVec &a : b) ai.push_back(a[i]);
+      r.push_back(call(fn, ai, sfu));
+    }
+    return r;
+  }
+
+  RVal arith(const std::string &op, const RVal &a, const RVal &b) {
+    return bind("(" + a.code + " " + op + " " + b.code + ")", a.var || b.var, op == "/");
+  }
+
+  // dot(a, b) summed left to right, as the prelude's s2_dot
+  RVal dot(const RVec &a, const RVec &b) {
+    if (a.size() != b.size()) bail();
+    RVal s = arith("*", a[0], b[0]);
+    for (size_t i = 1; i < a.size(); ++i) s = arith("+", s, arith("*", a[i], b[i]));
+    return s;
+  }
+
+  RVec expr(const Expr *e) {
+    const Ty t = out_t(e);
+    if (t.b != B::F32 || is_mat(t)) bail();
+    if (e->cst && (is_abstract(e->t) || e->k == Expr::Lit ||
+                   (e->k == Expr::Ref && e->sym && (e->sym->k == Sym::Const || e->sym->k == Sym::Global))))
+      return lit(t, e->cv);
+    const Ty nt = concrete(e->t);
+    if (nt.b != B::F32 || is_mat(nt)) bail();
+    switch (e->k) {
+      case Expr::Lit: return lit(nt, e->cv);
+      case Expr::Ref: {
+        if (e->sym->cst && (e->sym->k == Sym::Const || e->sym->k == Sym::Global)) return lit(nt, e->sym->cv);
+        auto it = env.find(e->sym);
+        if (it == env.end()) bail();
+        return it->second;
+      }
+      case Expr::Unary: {
+        if (e->s != "-") bail();
+        RVec a = expr(e->a[0]), r;
+        for (const RVal &c : a) r.push_back(bind("(-" + c.code + ")", c.var));
+        return r;
+      }
+      case Expr::Binary: {
+        const std::string &op = e->s;
+        if (op != "+" && op != "-" && op != "*" && op != "/") bail();
+        RVec a = expr(e->a[0]), b = expr(e->a[1]);
+        size_t n = std::max(a.size(), b.size());
+        a = bcast(a, n);
+        b = bcast(b, n);
+        RVec r;
+        for (size_t i = 0; i < n; ++i) r.push_back(arith(op, a[i], b[i]));
+        return r;
+      }
+      case Expr::Swz: {
+        RVec a = expr(e->a[0]), r;
+        for (int k : e->swz) {
+          if (k < 0 || size_t(k) >= a.size()) bail();
+          r.push_back(a[size_t(k)]);
+        }
+        return r;
+      }
+      case Expr::Call: {
+        if (e->is_ctor) {
+          RVec r;
+          for (const Expr *x : e->a) {
+            RVec v = expr(x);
+            r.insert(r.end(), v.begin(), v.end());
+          }
+          if (r.empty()) return lit(nt, {0.0});
+          if (r.size() == 1 && nt.n > 1) return RVec(size_t(nt.n), r[0]);
+          r.resize(size_t(nt.n));
+          return r;
+        }
+        if (e->fn) return inline_call(e);
+        return builtin(e);
+      }
+      default: bail();
+    }
+  }
+
+  RVec builtin(const Expr *e) {
+    const int id = int(e->lit);
+    std::vector<RVec> a;
+    for (const Expr *x : e->a) a.push_back(expr(x));
+    switch (id) {
+      case B_ABS: return componentwise("s2_abs", a, false);
+      case B_FLOOR: return componentwise("s2_floor", a, false);
+      case B_CEIL: return componentwise("s2_ceil", a, false);
+      case B_SQRT: return componentwise("s2_sqrt", a, true);
+      case B_MIN: return componentwise("s2_min", a, false);
+      case B_MAX: return componentwise("s2_max", a, false);
+      case B_CLAMP: return componentwise("s2_clamp", a, false);
+      case B_SATURATE: return componentwise("s2_saturate", a, false);
+      case B_MIX: return componentwise("s2_mix", a, false);
+      case B_SIN: return componentwise("s2_sin", a, true);
+      case B_COS: return componentwise("s2_cos", a, true);
+      case B_EXP: return componentwise("s2_exp", a, true);
+      case B_LOG: return componentwise("s2_log", a, true);
+      case B_POW: return componentwise("s2_pow", a, true);
+      case B_ATAN2: return componentwise("s2_atan2", a, true);
+      case B_LENGTH: {
+        if (a.size() != 1) bail();
+        if (a[0].size() == 1) return {call("s2_abs", {a[0][0]}, false)};
+        return {call("s2_sqrt", {dot(a[0], a[0])}, true)};
+      }
+      case B_DOT:
+        if (a.size() != 2) bail();
+        if (a[0].size() == 1) return {arith("*", a[0][0], a[1][0])};
+        return {dot(a[0], a[1])};
+      case B_DISTANCE: {
+        if (a.size() != 2 || a[0].size() != a[1].size()) bail();
+        RVec d;
+        for (size_t i = 0; i < a[0].size(); ++i) d.push_back(arith("-", a[0][i], a[1][i]));
+        if (d.size() == 1) return {call("s2_abs", {d[0]}, false)};
+        return {call("s2_sqrt", {dot(d, d)}, true)};
+      }
+      default: bail();
+    }
+  }
+
+  RVec inline_call(const Expr *e) {
+    const Func *f = e->fn;
+    if (++depth > 32) bail();
+    std::vector<RVec> args;
+    for (size_t i = 0; i < e->a.size(); ++i) {
+      if (f->params[i].out) bail();
+      args.push_back(expr(e->a[i]));
+    }
+    for (size_t i = 0; i < e->a.size(); ++i)
+      if (f->params[i].sym) env[f->params[i].sym] = args[i];
+    RVec ret;
+    bool done = false;
+    block(f->body, ret, done);
+    if (!done) bail();
+    --depth;
+    return ret;
+  }
+
+  void block(const Stmt *s, RVec &ret, bool &done) {
+    if (done) bail();  // statements after a return
+    switch (s->k) {
+      case Stmt::Block:
+        for (const Stmt *x : s->body) {
+          if (done) {
+            if (x->k == Stmt::Empty) continue;
+            bail();
+          }
+          block(x, ret, done);
+        }
+        return;
+      case Stmt::Empty: return;
+      case Stmt::Decl: {
+        const Sym *sym = s->sym;
+        if (sym->k == Sym::Const && sym->cst) return;
+        if (s->decl_t.b != B::F32 || is_mat(s->decl_t)) bail();
+        env[sym] = s->init ? expr(s->init) : lit(s->decl_t, {0.0});
+        return;
+      }
+      case Stmt::Assign: {
+        const Expr *l = s->lhs;
+        if (l->k != Expr::Ref || !l->sym || l->sym->k != Sym::Var) bail();
+        RVec r = expr(s->rhs);
+        if (s->op != "=") {
+          const std::string op = s->op.substr(0, s->op.size() - 1);
+          if (op != "+" && op != "-" && op != "*" && op != "/") bail();
+          RVec cur = env.at(l->sym);
+          size_t n = std::max(cur.size(), r.size());
+          cur = bcast(cur, n);
+          r = bcast(r, n);
+          RVec x;
+          for (size_t i = 0; i < n; ++i) x.push_back(arith(op, cur[i], r[i]));
+          r = x;
+        }
+        env[l->sym] = r;
+        return;
+      }
+      case Stmt::Return:
+        if (!s->val) bail();
+        ret = expr(s->val);
+        done = true;
+        return;
+      default: bail();
+    }
+  }
+};
+
 // Functions reachable from `root` in callee-first order; recursion is an error.
 void collect_calls(const Stmt *s, std::vector<const Expr *> &calls);
 void collect_calls(const Expr *e, std::vector<const Expr *> &calls) {
@@ -2652,6 +2908,23 @@ FrontendResult translate(const std::string &source, Lang lang, const std::string
                    src.compare(first, fn.size(), fn) == 0;
     }
     if (std_normal) E.out << "#define S2M_STD_NORMAL 1\n";
+    // run-of-4 form of sdf3d, when it is straight-line float code
+    try {
+      RunEmitter R;
+      RVec p = {{"x", false}, {"y", false}, {"z", true}};
+      R.env[sdf->params[0].sym] = p;
+      RVec ret;
+      bool done = false;
+      R.block(sdf->body, ret, done);
+      if (!done || ret.size() != 1) throw RunBail{};
+      E.out << "S2HD void s2m_user_sdf_run4(float x, float y, const s2x4 &z, s2x4 &out)\n{\n" << R.out.str();
+      if (ret[0].var) E.out << "  out = " << ret[0].code << ";\n";
+      else E.out << "  out = s2x4_splat(" << ret[0].code << ");\n";
+      E.out << "}\n#define S2M_HAS_RUN4 1\n";
+      r.run_fp32_ops = (R.fp_u + R.fp_v) / 4.0;
+      r.run_sfu_ops = (R.sfu_u + R.sfu_v) / 4.0;
+    } catch (const RunBail &) {
+    }
     r.cuda = E.out.str();
     for (auto &w : M.warnings) r.warnings.push_back(w);
     r.ok = true;

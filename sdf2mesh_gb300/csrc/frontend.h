@@ -24,6 +24,8 @@ struct FrontendResult {
   double fp32_ops = 0;                // algorithmic FP32 ops per sdf3d call
   double sfu_ops = 0;                 // sqrt / div / transcendental ops per call
   bool ops_exact = true;              // false when a loop bound was not static
+  double run_fp32_ops = 0;            // per point in runs of 4 sharing x, y (0: no run form)
+  double run_sfu_ops = 0;
 };
 
 // Built-in WGSL modules selected by `use <name>;` (shader.rs:12-20, 50-62).

@@ -81,12 +81,13 @@ struct EvalVariant {
   int run;
 };
 constexpr EvalVariant kEvalVariants[] = {
-    {"s2m_eval_b2r4", 4}, {"s2m_eval_b3r4", 4}, {"s2m_eval_b4r4", 4}, {"s2m_eval_b3p4", 4}};
+    {"s2m_eval_b2r4", 4}, {"s2m_eval_b3r4", 4}, {"s2m_eval_b4r4", 4}, {"s2m_eval_b2v4", 4}, {"s2m_eval_b3v4", 4}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
   std::string user_cuda;
   double fp32_ops = 0, sfu_ops = 0;
+  double run_fp32_ops = 0, run_sfu_ops = 0;  // per point in runs of 4 (0: no run form)
   uint32_t flags = 0;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_eval[kNumEvalVariants] = {};
@@ -733,6 +734,8 @@ int s2m_compile(const char *source, int lang, const char *sdf_name, uint32_t com
   s->user_cuda = r.cuda;
   s->fp32_ops = r.fp32_ops;
   s->sfu_ops = r.sfu_ops;
+  s->run_fp32_ops = r.run_fp32_ops;
+  s->run_sfu_ops = r.run_sfu_ops;
   s->flags = compile_flags;
   int rc = compile_module(s, err, errlen);
   if (rc != S2M_OK) {
@@ -767,6 +770,13 @@ int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t 
 }
 
 const char *s2m_sdf_cuda_source(const s2m_sdf *sdf) { return sdf ? sdf->user_cuda.c_str() : nullptr; }
+
+int s2m_sdf_run_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
+  if (!sdf) return S2M_E_INVALID;
+  if (fp32_ops) *fp32_ops = sdf->run_fp32_ops;
+  if (sfu_ops) *sfu_ops = sdf->run_sfu_ops;
+  return sdf->run_fp32_ops > 0 ? S2M_OK : S2M_E_INVALID;
+}
 
 int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point) {
   if (!sdf) return S2M_E_INVALID;

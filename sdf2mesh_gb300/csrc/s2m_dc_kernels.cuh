@@ -60,7 +60,7 @@ struct S2UserSdf {
 // the occupancy the compiler must allow (__launch_bounds__ minimum blocks),
 // which trades registers against latency hiding; the runtime's autotuner
 // times them per SDF and keeps the fastest.
-template <int RUN, bool PAIR>
+template <int RUN, bool VEC>
 __device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restrict__ ring, int k0, int nk) {
   const unsigned idx = blockIdx.x * S2_EVAL_BLOCK + threadIdx.x;  // P * P < 2^32
   const unsigned pts = (unsigned)job.P * (unsigned)job.P;
@@ -72,16 +72,20 @@ __device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restri
   int ke = min(kb + RUN, k0 + nk);
   long long row = (long long)jy * job.pitch + i;
   int k = kb;
-  if (PAIR) {
-    // two independent evaluations per iteration: instruction-level parallelism
+#ifdef S2M_HAS_RUN4
+  if (VEC) {
+    // 4 planes at once: the x/y-only part of the SDF once, the rest per lane
 #pragma unroll 1
-    for (; k + 1 < ke; k += 2) {
-      const float f0 = s2m_user_sdf(x, y, s2_coord(job, k));
-      const float f1 = s2m_user_sdf(x, y, s2_coord(job, k + 1));
-      ring[(long long)(k % job.ring) * job.plane + row] = f0;
-      ring[(long long)((k + 1) % job.ring) * job.plane + row] = f1;
+    for (; k + 3 < ke; k += 4) {
+      s2x4 z, f;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) z.v[w] = s2_coord(job, k + w);
+      s2m_user_sdf_run4(x, y, z, f);
+#pragma unroll
+      for (int w = 0; w < 4; ++w) ring[(long long)((k + w) % job.ring) * job.plane + row] = f.v[w];
     }
   }
+#endif
 #pragma unroll 1
   for (; k < ke; ++k) {
     float z = s2_coord(job, k);
@@ -97,7 +101,8 @@ __device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restri
 S2_EVAL_VARIANT(s2m_eval_b2r4, 2, 4, false)
 S2_EVAL_VARIANT(s2m_eval_b3r4, 3, 4, false)
 S2_EVAL_VARIANT(s2m_eval_b4r4, 4, 4, false)
-S2_EVAL_VARIANT(s2m_eval_b3p4, 3, 4, true)
+S2_EVAL_VARIANT(s2m_eval_b2v4, 2, 4, true)
+S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
 #endif
 
 #ifndef S2M_QEF_MODULE

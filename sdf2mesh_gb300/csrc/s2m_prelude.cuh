@@ -306,3 +306,39 @@ S2HD s2v3 s2_cross(const s2v3 &a, const s2v3 &b) {
 template <int N> S2HD s2vec<float, N> s2_reflect(const s2vec<float, N> &e1, const s2vec<float, N> &e2) {
   return e1 - 2.0f * s2_dot(e2, e1) * e2;
 }
+
+// ---------------------------------------------------------------------------
+// Runs of 4 points sharing x and y (s2m_user_sdf_run4): s2x4 holds the 4
+// lanes of a value that depends on z; values that do not are plain floats.
+// Every operation is the scalar one applied lane by lane.
+struct s2x4 {
+  float v[4];
+};
+S2HD s2x4 s2x4_splat(float a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = a; return r; }
+S2HD float s2_lane(float a, int) { return a; }
+S2HD float s2_lane(const s2x4 &a, int i) { return a.v[i]; }
+#define S2_X4_OP(op)                                                                       \
+  S2HD s2x4 operator op(const s2x4 &a, const s2x4 &b) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = a.v[i] op b.v[i]; return r; } \
+  S2HD s2x4 operator op(const s2x4 &a, float b) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = a.v[i] op b; return r; } \
+  S2HD s2x4 operator op(float a, const s2x4 &b) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = a op b.v[i]; return r; }
+S2_X4_OP(+)
+S2_X4_OP(-)
+S2_X4_OP(*)
+S2_X4_OP(/)
+#undef S2_X4_OP
+S2HD s2x4 operator-(const s2x4 &a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = -a.v[i]; return r; }
+#define S2_X4_F1(name) \
+  template <class A> S2HD s2x4 s2r_##name(const A &a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = s2_##name(s2_lane(a, i)); return r; }
+#define S2_X4_F2(name)                                                                       \
+  template <class A, class B> S2HD s2x4 s2r_##name(const A &a, const B &b) {                 \
+    s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = s2_##name(s2_lane(a, i), s2_lane(b, i)); return r; }
+#define S2_X4_F3(name)                                                                       \
+  template <class A, class B, class C> S2HD s2x4 s2r_##name(const A &a, const B &b, const C &c) { \
+    s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = s2_##name(s2_lane(a, i), s2_lane(b, i), s2_lane(c, i)); return r; }
+S2_X4_F1(abs) S2_X4_F1(floor) S2_X4_F1(ceil) S2_X4_F1(sqrt) S2_X4_F1(saturate) S2_X4_F1(sin) S2_X4_F1(cos)
+S2_X4_F1(exp) S2_X4_F1(log)
+S2_X4_F2(min) S2_X4_F2(max) S2_X4_F2(pow) S2_X4_F2(atan2)
+S2_X4_F3(clamp) S2_X4_F3(mix)
+#undef S2_X4_F1
+#undef S2_X4_F2
+#undef S2_X4_F3

@@ -246,3 +246,31 @@ def test_shadertoy_style_file(lib, oracle_lib):
     with pytest.raises(s2m.S2MError) as e:
         s2m.translate(code, s2m.LANG_SHADERTOY, "missing")
     assert e.value.name == "MISSING_SDF"
+
+
+
+@pytest.mark.parametrize("which", ["torus", "csg64", "tree3", "tree9", "capsules"])
+def test_run4_form_matches_per_point(lib, which):
+    """s2m_user_sdf_run4 (x/y-only part once per run of 4 z values) equals
+    s2m_user_sdf lane by lane, bit for bit; SDFs with loops have no run form."""
+    from tests.hostsdf import eval_run4_host
+    if which == "torus":
+        src = workloads.torus()[0]
+    elif which == "csg64":
+        src = workloads.csg64(seed=3)[0]
+    elif which == "capsules":
+        src = ("use sdf3d::*;\nuse sdf::op;\nfn sdf3d(p: vec3f) -> f32 {\n"
+               "  let q = abs(p) - vec3f(0.2);\n  var d = sdf3d_capsule(q, vec3f(0.0), vec3f(0.3, 0.1, 0.2), 0.1);\n"
+               "  d = sdf_op_smooth_subtraction(d, sdf3d_box(p, vec3(0.5, 0.4, 0.3)) * 0.5, 0.05);\n"
+               "  return mix(d, dot(p, vec3f(0.3, 0.4, -0.2)) / 2.0, 0.25);\n}\n")
+    else:
+        src = workloads.random_tree(int(which[4:]))[0]
+    cuda, _, _ = lower(src)
+    assert "S2M_HAS_RUN4" in cuda
+    rng = np.random.default_rng(5)
+    xy = rng.uniform(-1.2, 1.2, size=(500, 1, 2)).astype(np.float32).astype(np.float64)
+    z = rng.uniform(-1.2, 1.2, size=(500, 4, 1)).astype(np.float32).astype(np.float64)
+    pts = np.concatenate([np.broadcast_to(xy, (500, 4, 2)), z], axis=2).reshape(-1, 3)
+    assert_same_bits(eval_run4_host(cuda, pts), eval_host(cuda, pts))
+    mb = lower(workloads.mandelbulb()[0], s2m.LANG_GLSL, "sdf")[0]
+    assert "S2M_HAS_RUN4" not in mb

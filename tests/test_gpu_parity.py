@@ -208,7 +208,7 @@ def test_custom_normal_function(lib, oracle_lib):
     assert (np.sum(gpu.normals * radial, axis=1) > 0.999).all()
 
 
-@pytest.mark.parametrize("variant", range(4))
+@pytest.mark.parametrize("variant", range(5))
 def test_eval_variants_identical(lib, variant, monkeypatch):
     """Every evaluation-kernel variant the autotuner may pick gives the same bits."""
     src, prm = workloads.csg64(seed=1)
