@@ -6,11 +6,13 @@
 // src/mesh.rs:267-341, which run one z-slice per dispatch with a host
 // round-trip each):
 //   for each slab of D cell slices:
-//     s2m_eval_planes   lattice planes of the slab into an L2-sized ring (NVRTC)
-//     s2m_cells         classify cells, exact corners, vertices   (NVRTC)
-//     s2m_vcompact      ordered vertex compaction, row counts     (nvcc)
-//   s2m_rowscan         row starts of the sorted vertex list      (nvcc)
-//   s2m_quads           quads -> triangles, ordered               (nvcc)
+//     s2m_eval_*        lattice planes of the slab into an L2-sized ring (NVRTC)
+//     s2m_cells_mark / _offsets / _emit
+//                       classify cells, append candidates in order (nvcc)
+//   s2m_vertices        reference-rule (or QEF) vertices           (NVRTC)
+//   s2m_vcompact        ordered vertex compaction, row counts      (nvcc)
+//   s2m_rowscan         row starts of the sorted vertex list       (nvcc)
+//   s2m_quads           quads -> triangles, ordered                (nvcc)
 // Everything is stream-ordered; the host reads back a few counters at the end.
 #include <cuda_runtime.h>
 #include <nvrtc.h>
@@ -91,7 +93,7 @@ struct s2m_sdf {
   uint32_t flags = 0;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_eval[kNumEvalVariants] = {};
-  cudaKernel_t k_cells = nullptr, k_vertices = nullptr;
+  cudaKernel_t k_vertices = nullptr;
   // precision mode: a second module with the QEF vertex kernel, built on the
   // first QEF job (most SDFs never need it, and it compiles slowly)
   std::mutex qef_mu;
@@ -113,7 +115,9 @@ struct s2m_mesh {
   int N = 0, D = 0, nzc = 0, nslabs = 0;
   // workspace
   float *ring = nullptr;
-  unsigned long long *slab_ctrl = nullptr;  // [cell-tile status | tile counter]
+  unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
+  unsigned short *cell_masks = nullptr;      // per thread of a cell tile: candidate bits of its cells
+  unsigned *tile_cnt = nullptr;              // per cell tile: candidates
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -205,8 +209,7 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
       set_err(err, errlen, std::string("kernel missing from the compiled module: ") + kEvalVariants[v].name);
       return S2M_E_CUDA;
     }
-  if (cudaLibraryGetKernel(&s->k_cells, s->lib, "s2m_cells") != cudaSuccess ||
-      cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
+  if (cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
   }
@@ -262,13 +265,13 @@ void give_pinned_slot(unsigned long long *p) {
 }
 
 void free_buffers(s2m_mesh *m) {
-  void *ptrs[] = {m->ring, m->slab_ctrl, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
+  void *ptrs[] = {m->ring, m->slab_ctrl, m->cell_masks, m->tile_cnt, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
                   m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
                   m->jobctl};
   for (void *p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   if (m->h_read) give_pinned_slot(m->h_read);
-  m->ring = nullptr; m->slab_ctrl = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
+  m->ring = nullptr; m->slab_ctrl = nullptr; m->cell_masks = nullptr; m->tile_cnt = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
   m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
   m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
   m->jobctl = nullptr; m->h_read = nullptr;
@@ -347,6 +350,8 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   cudaStream_t st = m->stream;
   S2_CUDA(cudaMallocAsync(&m->ring, ring_floats * sizeof(float), st));
   S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->cell_masks, m->cell_tiles * S2_CELL_BLOCK * 2, st));
+  S2_CUDA(cudaMallocAsync(&m->tile_cnt, m->cell_tiles * 4, st));
   S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cand_val, m->cand_cap * 32, st));
   S2_CUDA(cudaMallocAsync(&m->cand_pos, m->cand_cap * 12, st));
@@ -439,12 +444,6 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   if ((e = cudaMemsetAsync(m->rowcnt, 0, N * N * 4, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->scan_status, 0, (m->scan_tiles + m->quad_tiles) * 8, st)) != cudaSuccess) return e;
 
-  S2Slab slab;
-  slab.ring = m->ring;
-  slab.status = m->slab_ctrl;
-  slab.tile_counter = reinterpret_cast<unsigned *>(m->slab_ctrl + m->cell_tiles);
-  slab.err = c.err;
-
   S2Cand cand;
   cand.key = m->cand_key;
   cand.val = m->cand_val;
@@ -486,12 +485,15 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     dim3 eg(eval_blocks, unsigned((nk + run - 1) / run));
     S2_LAUNCH(0, double(pts) * nk,
               cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
-    if ((e = cudaMemsetAsync(m->slab_ctrl, 0, m->slab_ctrl_words * 8, st)) != cudaSuccess) return e;
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
     unsigned cg = unsigned((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-    int si = s;
-    void *cargs[] = {&jj, &slab, &cand, &zc0, &zc1, &si};
-    S2_LAUNCH(1, ncells, cudaLaunchKernel((const void *)m->sdf->k_cells, dim3(cg), dim3(S2_CELL_BLOCK), cargs, 0, st));
+    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CELL_BLOCK, 0, st>>>(j, m->ring, m->cell_masks, m->tile_cnt, zc0, zc1),
+                          cudaGetLastError()));
+    S2_LAUNCH(1, 0, (s2m_cells_offsets<<<1, 1024, 0, st>>>(m->tile_cnt, cg, m->slab_ctrl, m->cand_base, s),
+                     cudaGetLastError()));
+    S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CELL_BLOCK, 0, st>>>(j, m->ring, m->cell_masks, m->slab_ctrl, cand, c.err,
+                                                                  zc0),
+                     cudaGetLastError()));
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
@@ -1001,6 +1003,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   size_t used = 0;
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
+            carve(base, used, m.cell_tiles * S2_CELL_BLOCK, &m.cell_masks) && carve(base, used, m.cell_tiles, &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
             carve(base, used, size_t(8), &m.jobctl);

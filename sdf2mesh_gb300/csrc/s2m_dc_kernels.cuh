@@ -10,7 +10,7 @@
 // A cell corner coincides with a lattice point except where, on some axis,
 // mn + size rounds differently from bmin + size * (pos + 1) ("off-lattice");
 // for cells that can carry a vertex, those corners are re-evaluated at the
-// reference coordinates (s2m_cells), so the vertex rule sees exactly the
+// reference coordinates (s2m_vertices), so the vertex rule sees exactly the
 // reference's 8 values.  All arithmetic of the vertex rule uses explicitly
 // rounded binary32 intrinsics (no contraction, whatever the SDF's flags).
 
@@ -105,25 +105,7 @@ S2_EVAL_VARIANT(s2m_eval_b2v4, 2, 4, true)
 S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
 #endif
 
-#ifndef S2M_QEF_MODULE
-// Cell pass of one slab (cell slices zc0 .. zc1 - 1): classify every cell and
-// append the candidates, in (z, y, x) order, to the job's candidate list at
-// cand.base[slab] + (look-back prefix over tiles), each with its 8 lattice
-// corner values.  The last tile publishes cand.base[slab + 1].
-extern "C" __global__ void __launch_bounds__(S2_CELL_BLOCK)
-s2m_cells(S2Job job, S2Slab slab, S2Cand cand, int zc0, int zc1, int slab_index) {
-  __shared__ unsigned s_tile;
-  if (threadIdx.x == 0) s_tile = atomicAdd(slab.tile_counter, 1u);
-  __syncthreads();
-  const unsigned tile = s_tile;
-  const long long ncells = (long long)(zc1 - zc0) * job.N * job.N;
-  const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-  if (tile >= ntiles) return;
-  s2_cell_tile<false>(job, slab.ring, cand, slab.status, slab.err, tile, ntiles, ncells, zc0, cand.base[slab_index],
-                      cand.base + slab_index + 1);
-}
 
-#endif  // S2M_QEF_MODULE
 
 // Vertices of every candidate of the job, one candidate per thread (dense:
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
