@@ -13,7 +13,10 @@ indices, all on the device.  A voxel is a cell; value = N^3 * steps / time.
                buffers, pipeline, count readback) + the mesh copied to pinned
                host memory + s2m_mesh_free
   roofline     the dominant kernel, from CUDA events around every launch of
-               the timed steps
+               the timed steps; for the evaluation, the SDF operations it
+               executed (with tile pruning: counted per tile by the tile pass)
+  full_evaluation  the same job with tile pruning off (every SDF operation at
+               every lattice point), timed the same way
   cpu_baseline the CPU oracle (restatement of the reference rule, OpenMP on all
                host cores) on a bounded window of slices of the same job
 
@@ -55,6 +58,7 @@ def parse():
     ap.add_argument("--resolution", type=int, default=None)
     ap.add_argument("--workload", default="csg64_1024", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-full-eval", action="store_true", help="skip the run without tile pruning")
     return ap.parse_args()
 
 
@@ -209,9 +213,13 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def eval_traffic_per_point():
-    """DRAM bytes per lattice point of the evaluation kernel, from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "s2m_eval_csg64_512.md")
+EVAL_PROFILE = {False: "s2m_eval_csg64_512.md", True: "s2m_evalp_csg64_512.md"}
+
+
+def eval_traffic_per_point(pruned=False):
+    """DRAM bytes per lattice point of the evaluation (pruned: tile pass + pruned
+    kernel), from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", EVAL_PROFILE[pruned])
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_point"):
@@ -250,9 +258,11 @@ def ours(a):
     t0 = time.perf_counter()
     _, bounds, qef, desc = WORKLOADS[a.workload]
     lang = s2m.LANG_GLSL if a.workload.startswith("mandelbulb") else s2m.LANG_WGSL
-    sdf = s2m.Sdf3DShader.from_source(src, lang, "sdf").compile()
+    shader = s2m.Sdf3DShader.from_source(src, lang, "sdf")
+    sdf = shader.compile()
     compile_s = time.perf_counter() - t0
     fp32_ops, sfu_ops = sdf.op_counts()
+    prune_comb, _ = sdf.prune_info()
 
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
@@ -270,36 +280,58 @@ def ours(a):
             dist.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(a.warmup):
-        mesh.run_async(sp)
-        mesh.sync(sp)
+    def timed(m, steps, warmup, clocks=None):
+        """Device time of `steps` runs of mesh m (CUDA events on its stream,
+        L2 flushed before each, outside the events), with per-kernel events."""
+        for _ in range(warmup):
+            m.run_async(sp)
+            m.sync(sp)
+        m.set_profiling(True)
+        m.reset_profile()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        barrier()
+        if clocks:
+            clocks.start()
+        w0 = time.perf_counter()
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+            m.run_async(sp)
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+            m.sync(sp)
+        barrier()
+        w = time.perf_counter() - w0
+        clk = clocks.stop() if clocks else None
+        m.set_profiling(False)
+        return sum(s.elapsed_time(e) for s, e in evs), m.profile(), w, clk
 
     # ---- device-timed steps -------------------------------------------------
-    mesh.set_profiling(True)
-    mesh.reset_profile()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
-    clocks = Clocks(local)
-    barrier()
-    clocks.start()
-    wall0 = time.perf_counter()
-    for i in range(a.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(i))
-            evs[i][0].record(stream)
-        mesh.run_async(sp)
-        with torch.cuda.stream(stream):
-            evs[i][1].record(stream)
-        mesh.sync(sp)
-    barrier()
-    wall = time.perf_counter() - wall0
-    clk = clocks.stop()
-    mesh.set_profiling(False)
-    step_ms = [s.elapsed_time(e) for s, e in evs]
-    tot_ms = sum(step_ms)
-    prof = mesh.profile()
+    tot_ms, prof, wall, clk = timed(mesh, a.steps, a.warmup, Clocks(local))
+    eval_ops = mesh.eval_ops()  # SDF operations the last run executed
     tot_ms = reduce_max(tot_ms, dev)
     voxels_step = float(N) ** 3
     value = voxels_step * a.steps * ws / (tot_ms * 1e-3) / 1e9
+
+    # ---- the same job without tile pruning (every operation at every point) --
+    full_eval = None
+    if prune_comb > 0 and not a.no_full_eval:
+        plain = shader.compile(prune=False)
+        fmesh = s2m.mesh_device(plain, state, sp)
+        f_ms, f_prof, _, _ = timed(fmesh, a.steps, max(1, min(a.warmup, 2)))
+        f_ms = reduce_max(f_ms, dev)
+        f_mi = fmesh.info()
+        if int(f_mi.nverts) != nverts or int(f_mi.ntris) != ntris:
+            raise RuntimeError("the full evaluation's mesh differs from the pruned one")
+        f_ops = fmesh.eval_ops()
+        full_eval = {"value": voxels_step * a.steps * ws / (f_ms * 1e-3) / 1e9, "unit": UNIT,
+                     "ms_per_step": f_ms / a.steps, "eval_variant": plain.eval_variant()[0],
+                     "eval_ms_per_step": f_prof["ms"]["eval_planes"] / a.steps,
+                     "fp32_ops_per_step": f_ops["fp32_ops"], "sfu_ops_per_step": f_ops["sfu_ops"],
+                     "mesh": "same vertex and triangle counts (bit-identity is a GPU test)"}
+        fmesh.close()
+        plain.close()
 
     # ---- end to end through the C ABI: create -> pinned host copy -> free ----
     host_pos = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
@@ -354,13 +386,13 @@ def ours(a):
         nl = prof["launches"][k]
         kernels[k] = {"launches_per_step": nl // a.steps, "ms_per_step": ms[k] / a.steps,
                       "share": ms[k] / max(1e-9, sum(ms.values()))}
-    # ops the evaluation kernel executes per point: the SDF as written, or, when the autotuner
-    # picked a run-of-4 variant, its run form (the x/y-only part once per 4 points)
+    # ops the evaluation executes per point: the SDF as written; with a run-of-4 variant its run
+    # form (the x/y-only part once per 4 points); with tile pruning the operations of the segments
+    # the tile pass left active, counted per tile (eval_ops of the last run)
     variant = sdf.eval_variant()[0]
-    run_counts = sdf.run_op_counts()
     per_point_scalar = (fp32_ops, sfu_ops)
-    if run_counts and "v4" in variant:
-        fp32_ops, sfu_ops = run_counts
+    pts_run = max(1.0, eval_ops["points"])
+    fp32_ops, sfu_ops = eval_ops["fp32_ops"] / pts_run, eval_ops["sfu_ops"] / pts_run
     eval_gops = fp32_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
     eval_sfu = sfu_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
     scalar_equiv_gops = per_point_scalar[0] * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
@@ -377,17 +409,22 @@ def ours(a):
         per_launch_ms = ms["eval_planes"] / n_eval
         t_fp32 = fp32_ops / fp32_peak
         t_sfu = sfu_ops / sfu_peak if sfu_peak > 0 else 0.0
-        tpp = eval_traffic_per_point() if a.workload == "csg64_1024" else None
+        tpp = eval_traffic_per_point(eval_ops["pruned"]) if a.workload == "csg64_1024" else None
         traffic = tpp * prof["eval_points"] / n_eval if tpp else None
-        common = {"kernel": "s2m_eval_*", "traffic": traffic, "traffic_source": (
+        common = {"kernel": "s2m_tiles + s2m_evalp_*" if eval_ops["pruned"] else "s2m_eval_*",
+                  "traffic": traffic, "traffic_source": (
                       "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 512^3 case "
-                      "(profiles/s2m_eval_csg64_512.md), scaled by points per launch") if traffic else None,
+                      f"(profiles/{EVAL_PROFILE[eval_ops['pruned']]}), scaled by points per launch")
+                  if traffic else None,
+                  "tile_pruning": eval_ops["pruned"],
                   "ms_per_launch": per_launch_ms,
                   "algorithmic": f"{fp32_ops:g} FP32 + {sfu_ops:g} SFU ops per lattice point x "
                                  f"{prof['eval_points'] / n_eval:.0f} points per launch",
                   "fp32_gops": eval_gops, "fp32_peak_gops": fp32_peak, "sfu_gops": eval_sfu,
                   "variant": variant, "per_point_ops_as_written": {"fp32": per_point_scalar[0], "sfu": per_point_scalar[1]},
                   "per_point_ops_executed": {"fp32": fp32_ops, "sfu": sfu_ops},
+                  "executed_ops_source": ("tile pass: active segments' operations x points of each tile"
+                                          if eval_ops["pruned"] else "frontend op count x points"),
                   "fp32_gops_as_written": scalar_equiv_gops,
                   "sfu_peak_gops": sfu_peak, "dominant_by_time": dom,
                   "peak_source": "measured in this run: s2m_fp32_probe (FP32 add/mul issue rate) and "
@@ -428,6 +465,7 @@ def ours(a):
                 "ms_per_step": e2e_tot / a.steps,
                 "path": "s2m_mesh_create + s2m_mesh_copy_to_host (pinned) + s2m_mesh_free; inputs are the "
                         "compiled SDF module and a 48-byte parameter block passed as kernel arguments"},
+        "full_evaluation": full_eval,
         "roofline": roof,
         "roofline_contouring": contour,
         "kernels": kernels,
@@ -438,6 +476,9 @@ def ours(a):
                  "candidate_cells": int(info.candidate_cells), "slab_depth": int(info.slab_depth)},
         "compile_s": compile_s,
         "eval_variant": sdf.eval_variant()[0],
+        "tile_pruning": {"combinators": prune_comb, "used": eval_ops["pruned"],
+                         "fp32_ops_per_point": fp32_ops, "sfu_ops_per_point": sfu_ops,
+                         "fp32_ops_per_point_as_written": per_point_scalar[0]},
         "eval_variants": [{"name": n, "ns_per_point": t, "registers": r, "local_bytes": l}
                           for n, t, r, l in sdf.eval_variants()],
         "triangles_per_s": ntris * a.steps * ws / (tot_ms * 1e-3),

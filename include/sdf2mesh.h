@@ -50,8 +50,11 @@ typedef enum {
 typedef enum { S2M_LANG_WGSL = 0, S2M_LANG_GLSL = 1, S2M_LANG_SHADERTOY = 2 } s2m_lang;
 
 /* Compile flags. */
-#define S2M_COMPILE_FMAD 0x1u  /* allow FMA contraction: faster, no longer bit-exact
-                                  with the reference rule's binary32 arithmetic     */
+#define S2M_COMPILE_FMAD 0x1u      /* allow FMA contraction: faster, no longer bit-exact
+                                      with the reference rule's binary32 arithmetic
+                                      (also turns tile pruning off)                  */
+#define S2M_COMPILE_NO_PRUNE 0x2u  /* evaluate every operation of the SDF at every
+                                      lattice point (no tile pruning)               */
 
 /* Job flags (s2m_params.flags). */
 #define S2M_JOB_POW2_ROUNDING 0x1u  /* round resolution up to a power of two as the
@@ -136,12 +139,27 @@ int s2m_sdf_run_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops)
    job (-1: not tuned yet): its name, and the measured ns per lattice point
    of each of the S2M_EVAL_VARIANTS variants.  No reference counterpart (the
    reference has one fixed kernel, dualcontour.wgsl:161-162). */
-#define S2M_EVAL_VARIANTS 5
+#define S2M_EVAL_VARIANTS 7
 int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point);
+/* Use `variant` for this SDF's later jobs instead of tuning (S2M_E_INVALID
+   when the module has no such variant, e.g. a pruned one without a pruning
+   form). */
+int s2m_sdf_set_eval_variant(s2m_sdf *sdf, int variant);
 /* Name, registers per thread and local (spill) bytes per thread of one
-   variant, as the tuner recorded them (0 before tuning). */
+   variant, as the tuner recorded them (0 before tuning).  Variants 5 and 6
+   are the tile-pruned ones; their ns per point is 0 when the SDF has no
+   pruning form. */
 int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_t namelen, int *registers,
                               int *local_bytes);
+
+/* Tile pruning (no reference counterpart).  For a straight-line SDF the
+   frontend also emits an interval evaluation over a tile of 8 x 8 x <= 8
+   lattice points.  Where it proves that a min, max or sdf::op smooth
+   operator returns one operand bit for bit at every point of the tile, the
+   other operand's exclusive operations are skipped there, so the lattice
+   values stay bit-identical.  *combinators: combinators that can prune (0:
+   no pruning form, or turned off by S2M_COMPILE_FMAD / _NO_PRUNE). */
+int s2m_sdf_prune_info(const s2m_sdf *sdf, int *combinators, int *words);
 
 void s2m_sdf_free(s2m_sdf *sdf);
 
@@ -174,6 +192,12 @@ int s2m_mesh_run_async(s2m_mesh *mesh, void *stream);
 int s2m_mesh_sync(s2m_mesh *mesh, void *stream, char *err, size_t errlen);
 
 int s2m_mesh_get_info(const s2m_mesh *mesh, s2m_mesh_info *info);
+
+/* SDF operations the last run's lattice evaluation executed: points
+   evaluated, FP32 and SFU operations in total (pruned runs: counted per tile
+   by the tile pass; others: the per-point counts times the points).
+   Returns 1 when the run was tile-pruned, 0 when not, < 0 on error. */
+int s2m_mesh_eval_ops(const s2m_mesh *mesh, double *points, double *fp32_ops, double *sfu_ops);
 
 /* Copy the mesh to caller-owned host buffers (any may be NULL):
    pos / nrm 3*nverts floats, cell nverts keys, tris 3*ntris indices. */

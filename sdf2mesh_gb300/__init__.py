@@ -27,7 +27,7 @@ import numpy as np
 __all__ = [
     "S2MError", "Sdf3DShader", "CompiledSdf", "AppState", "DeviceMesh", "TriangleMesh", "generate", "Batch", "Server",
     "load_library", "translate", "wgsl_remove_function", "wgsl_rename_function", "wgsl_has_function",
-    "LANG_WGSL", "LANG_GLSL", "LANG_SHADERTOY", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "JOB_QEF", "COMPILE_FMAD",
+    "LANG_WGSL", "LANG_GLSL", "LANG_SHADERTOY", "JOB_POW2_ROUNDING", "JOB_SLICE_LAG", "JOB_EXACT_CORNERS", "JOB_QEF", "COMPILE_FMAD", "COMPILE_NO_PRUNE",
 ]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -35,6 +35,8 @@ LIB_PATH = os.path.join(HERE, "_lib", "libsdf2mesh_gb300.so")
 
 LANG_WGSL, LANG_GLSL, LANG_SHADERTOY = 0, 1, 2
 COMPILE_FMAD = 0x1
+COMPILE_NO_PRUNE = 0x2
+EVAL_VARIANTS = 7
 JOB_POW2_ROUNDING, JOB_SLICE_LAG, JOB_EXACT_CORNERS, JOB_QEF = 0x1, 0x2, 0x4, 0x8
 
 S2M_OK = 0
@@ -129,6 +131,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_sdf_cuda_source": ([vp], ctypes.c_char_p),
             "s2m_sdf_op_counts": ([vp, dp, dp], i),
             "s2m_sdf_run_op_counts": ([vp, dp, dp], i),
+            "s2m_sdf_set_eval_variant": ([vp, i], i),
+            "s2m_sdf_prune_info": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], i),
+            "s2m_mesh_eval_ops": ([vp, dp, dp, dp], i),
             "s2m_sdf_free": ([vp], None),
             "s2m_sdf_eval_variant": ([vp, ctypes.c_char_p, sz, dp], i),
             "s2m_sdf_eval_variant_info": ([vp, i, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
@@ -269,9 +274,19 @@ class CompiledSdf:
     def eval_variant(self):
         """(name, ns per lattice point of each variant) chosen by the autotuner; name is 'untuned' before the first job."""
         name = ctypes.create_string_buffer(64)
-        ns = (ctypes.c_double * 5)()
+        ns = (ctypes.c_double * EVAL_VARIANTS)()
         load_library().s2m_sdf_eval_variant(self._h, name, 64, ns)
         return name.value.decode(), list(ns)
+
+    def set_eval_variant(self, variant: int) -> None:
+        """Use evaluation variant `variant` (0 .. EVAL_VARIANTS - 1) instead of tuning."""
+        _check(load_library().s2m_sdf_set_eval_variant(self._h, variant), None, f"eval variant {variant}")
+
+    def prune_info(self):
+        """(combinators that can prune, activity words per tile); (0, 0) without tile pruning."""
+        c, w = ctypes.c_int(), ctypes.c_int()
+        load_library().s2m_sdf_prune_info(self._h, ctypes.byref(c), ctypes.byref(w))
+        return c.value, w.value
 
     def eval_variants(self):
         """Per variant: (name, ns per point, registers, local bytes) as the autotuner measured them."""
@@ -346,12 +361,15 @@ class Sdf3DShader:
                                      n.value, ctypes.byref(n), err, len(err)), err, "csg")
         return prog
 
-    def compile(self, fmad: bool = False) -> CompiledSdf:
+    def compile(self, fmad: bool = False, prune: bool = True) -> CompiledSdf:
+        """NVRTC module for sm_103a.  fmad: FMA contraction (not bit-exact);
+        prune=False: no tile pruning (every operation at every point)."""
         L = load_library()
         h = ctypes.c_void_p()
         err = _errbuf()
+        flags = (COMPILE_FMAD if fmad else 0) | (0 if prune else COMPILE_NO_PRUNE)
         rc = L.s2m_compile(self.source.encode(), self.lang, self.sdf_name.encode(),
-                           COMPILE_FMAD if fmad else 0, ctypes.byref(h), err, len(err))
+                           flags, ctypes.byref(h), err, len(err))
         _check(rc, err, "compile")
         return CompiledSdf(h)
 
@@ -427,6 +445,12 @@ class DeviceMesh:
         return {"ms": {k: pr.ms[i] for i, k in enumerate(KERNEL_KINDS)},
                 "launches": {k: int(pr.launches[i]) for i, k in enumerate(KERNEL_KINDS)},
                 "eval_points": pr.eval_points, "cells": pr.cells}
+
+    def eval_ops(self) -> dict:
+        """SDF operations the last run's lattice evaluation executed."""
+        pts, fp, sfu = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        rc = load_library().s2m_mesh_eval_ops(self._h, ctypes.byref(pts), ctypes.byref(fp), ctypes.byref(sfu))
+        return {"pruned": rc == 1, "points": pts.value, "fp32_ops": fp.value, "sfu_ops": sfu.value}
 
     def reset_profile(self) -> None:
         _check(load_library().s2m_mesh_reset_profile(self._h), None, "profile")

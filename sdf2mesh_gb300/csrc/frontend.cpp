@@ -25,6 +25,7 @@
 #include <stdexcept>
 
 #include "frontend.h"
+#include "prune.h"
 #include "../../include/sdf2mesh.h"
 
 namespace s2m {
@@ -2781,6 +2782,288 @@ class RunEmitter {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Scalar expression graph of a straight-line SDF for tile pruning
+// (prune.h).  The traversal and the lowering of each builtin are those of
+// RunEmitter, so the graph performs the operations of s2m_user_sdf in the
+// same order.  A user function whose body lowers to exactly the arithmetic of
+// sdf::op's smooth union / intersection / subtraction of its three arguments
+// becomes one combinator node.
+
+struct PruneBail {};
+
+class PruneBuilder {
+ public:
+  PruneIR ir;
+  std::map<const Sym *, std::vector<int>> env;
+  int depth = 0;
+
+  [[noreturn]] static void bail() { throw PruneBail{}; }
+
+  int node(POp op, int a = -1, int b = -1, int c = -1) {
+    PNode n;
+    n.op = op;
+    n.a = a;
+    n.b = b;
+    n.c = c;
+    ir.nodes.push_back(n);
+    return int(ir.nodes.size()) - 1;
+  }
+  int cst(float v) {
+    uint32_t bits;
+    std::memcpy(&bits, &v, 4);
+    auto it = consts_.find(bits);
+    if (it != consts_.end()) return it->second;
+    const int id = node(POp::Const);
+    ir.nodes[size_t(id)].k = v;
+    consts_[bits] = id;
+    return id;
+  }
+
+  static Ty out_t(const Expr *e) { return e->want.b != B::Void ? e->want : concrete(e->t); }
+
+  std::vector<int> lit(const Ty &t, const std::vector<double> &cv) {
+    if (t.b != B::F32 || is_mat(t)) bail();
+    std::vector<int> r;
+    for (int i = 0; i < t.n; ++i)
+      r.push_back(cst(float(cv.empty() ? 0.0 : (cv.size() == 1 ? cv[0] : cv[size_t(i)]))));
+    return r;
+  }
+
+  static std::vector<int> bcast(const std::vector<int> &v, size_t n) {
+    if (v.size() == n) return v;
+    if (v.size() != 1) bail();
+    return std::vector<int>(n, v[0]);
+  }
+
+  std::vector<int> componentwise(POp op, const std::vector<std::vector<int>> &args) {
+    size_t n = 1;
+    for (const auto &a : args) n = std::max(n, a.size());
+    std::vector<std::vector<int>> b;
+    for (const auto &a : args) b.push_back(bcast(a, n));
+    std::vector<int> r;
+    for (size_t i = 0; i < n; ++i)
+      r.push_back(node(op, b[0][i], b.size() > 1 ? b[1][i] : -1, b.size() > 2 ? b[2][i] : -1));
+    return r;
+  }
+
+  int dot(const std::vector<int> &a, const std::vector<int> &b) {
+    if (a.size() != b.size()) bail();
+    int s = node(POp::Mul, a[0], b[0]);
+    for (size_t i = 1; i < a.size(); ++i) s = node(POp::Add, s, node(POp::Mul, a[i], b[i]));
+    return s;
+  }
+
+  std::vector<int> expr(const Expr *e) {
+    const Ty t = out_t(e);
+    if (t.b != B::F32 || is_mat(t)) bail();
+    if (e->cst && (is_abstract(e->t) || e->k == Expr::Lit ||
+                   (e->k == Expr::Ref && e->sym && (e->sym->k == Sym::Const || e->sym->k == Sym::Global))))
+      return lit(t, e->cv);
+    const Ty nt = concrete(e->t);
+    if (nt.b != B::F32 || is_mat(nt)) bail();
+    switch (e->k) {
+      case Expr::Lit: return lit(nt, e->cv);
+      case Expr::Ref: {
+        if (e->sym->cst && (e->sym->k == Sym::Const || e->sym->k == Sym::Global)) return lit(nt, e->sym->cv);
+        auto it = env.find(e->sym);
+        if (it == env.end()) bail();
+        return it->second;
+      }
+      case Expr::Unary: {
+        if (e->s != "-") bail();
+        std::vector<int> a = expr(e->a[0]), r;
+        for (int c : a) r.push_back(node(POp::Neg, c));
+        return r;
+      }
+      case Expr::Binary: {
+        const std::string &op = e->s;
+        POp o = op == "+" ? POp::Add : op == "-" ? POp::Sub : op == "*" ? POp::Mul : op == "/" ? POp::Div : POp::X;
+        if (o == POp::X) bail();
+        std::vector<int> a = expr(e->a[0]), b = expr(e->a[1]);
+        size_t n = std::max(a.size(), b.size());
+        a = bcast(a, n);
+        b = bcast(b, n);
+        std::vector<int> r;
+        for (size_t i = 0; i < n; ++i) r.push_back(node(o, a[i], b[i]));
+        return r;
+      }
+      case Expr::Swz: {
+        std::vector<int> a = expr(e->a[0]), r;
+        for (int k : e->swz) {
+          if (k < 0 || size_t(k) >= a.size()) bail();
+          r.push_back(a[size_t(k)]);
+        }
+        return r;
+      }
+      case Expr::Call: {
+        if (e->is_ctor) {
+          std::vector<int> r;
+          for (const Expr *x : e->a) {
+            std::vector<int> v = expr(x);
+            r.insert(r.end(), v.begin(), v.end());
+          }
+          if (r.empty()) return lit(nt, {0.0});
+          if (r.size() == 1 && nt.n > 1) return std::vector<int>(size_t(nt.n), r[0]);
+          r.resize(size_t(nt.n));
+          return r;
+        }
+        if (e->fn) return inline_call(e);
+        return builtin(e);
+      }
+      default: bail();
+    }
+  }
+
+  std::vector<int> builtin(const Expr *e) {
+    std::vector<std::vector<int>> a;
+    for (const Expr *x : e->a) a.push_back(expr(x));
+    switch (int(e->lit)) {
+      case B_ABS: return componentwise(POp::Abs, a);
+      case B_FLOOR: return componentwise(POp::Floor, a);
+      case B_CEIL: return componentwise(POp::Ceil, a);
+      case B_SQRT: return componentwise(POp::Sqrt, a);
+      case B_MIN: return componentwise(POp::Min, a);
+      case B_MAX: return componentwise(POp::Max, a);
+      case B_CLAMP: return componentwise(POp::Clamp, a);
+      case B_SATURATE: return componentwise(POp::Saturate, a);
+      case B_MIX: return componentwise(POp::Mix, a);
+      case B_SIN: return componentwise(POp::Sin, a);
+      case B_COS: return componentwise(POp::Cos, a);
+      case B_EXP: return componentwise(POp::Exp, a);
+      case B_LOG: return componentwise(POp::Log, a);
+      case B_POW: return componentwise(POp::Pow, a);
+      case B_ATAN2: return componentwise(POp::Atan2, a);
+      case B_LENGTH:
+        if (a.size() != 1) bail();
+        if (a[0].size() == 1) return {node(POp::Abs, a[0][0])};
+        return {node(POp::Sqrt, dot(a[0], a[0]))};
+      case B_DOT:
+        if (a.size() != 2) bail();
+        if (a[0].size() == 1) return {node(POp::Mul, a[0][0], a[1][0])};
+        return {dot(a[0], a[1])};
+      case B_DISTANCE: {
+        if (a.size() != 2 || a[0].size() != a[1].size()) bail();
+        std::vector<int> d;
+        for (size_t i = 0; i < a[0].size(); ++i) d.push_back(node(POp::Sub, a[0][i], a[1][i]));
+        if (d.size() == 1) return {node(POp::Abs, d[0])};
+        return {node(POp::Sqrt, dot(d, d))};
+      }
+      default: bail();
+    }
+  }
+
+  std::vector<int> inline_call(const Expr *e) {
+    const Func *f = e->fn;
+    if (++depth > 32) bail();
+    std::vector<std::vector<int>> args;
+    for (size_t i = 0; i < e->a.size(); ++i) {
+      if (f->params[i].out) bail();
+      args.push_back(expr(e->a[i]));
+    }
+    for (size_t i = 0; i < e->a.size(); ++i)
+      if (f->params[i].sym) env[f->params[i].sym] = args[i];
+    std::vector<int> ret;
+    bool done = false;
+    block(f->body, ret, done);
+    if (!done) bail();
+    --depth;
+    if (args.size() == 3 && ret.size() == 1 && args[0].size() == 1 && args[1].size() == 1 && args[2].size() == 1) {
+      const POp k = smooth_kind(ret[0], args[0][0], args[1][0], args[2][0]);
+      if (k != POp::X) return {node(k, args[0][0], args[1][0], args[2][0])};
+    }
+    return ret;
+  }
+
+  void block(const Stmt *s, std::vector<int> &ret, bool &done) {
+    if (done) bail();
+    switch (s->k) {
+      case Stmt::Block:
+        for (const Stmt *x : s->body) {
+          if (done) {
+            if (x->k == Stmt::Empty) continue;
+            bail();
+          }
+          block(x, ret, done);
+        }
+        return;
+      case Stmt::Empty: return;
+      case Stmt::Decl: {
+        const Sym *sym = s->sym;
+        if (sym->k == Sym::Const && sym->cst) return;
+        if (s->decl_t.b != B::F32 || is_mat(s->decl_t)) bail();
+        env[sym] = s->init ? expr(s->init) : lit(s->decl_t, {0.0});
+        return;
+      }
+      case Stmt::Assign: {
+        const Expr *l = s->lhs;
+        if (l->k != Expr::Ref || !l->sym || l->sym->k != Sym::Var) bail();
+        std::vector<int> r = expr(s->rhs);
+        if (s->op != "=") {
+          const std::string op = s->op.substr(0, s->op.size() - 1);
+          POp o = op == "+" ? POp::Add : op == "-" ? POp::Sub : op == "*" ? POp::Mul : op == "/" ? POp::Div : POp::X;
+          if (o == POp::X) bail();
+          std::vector<int> cur = env.at(l->sym);
+          size_t n = std::max(cur.size(), r.size());
+          cur = bcast(cur, n);
+          r = bcast(r, n);
+          std::vector<int> x;
+          for (size_t i = 0; i < n; ++i) x.push_back(node(o, cur[i], r[i]));
+          r = x;
+        }
+        env[l->sym] = r;
+        return;
+      }
+      case Stmt::Return:
+        if (!s->val) bail();
+        ret = expr(s->val);
+        done = true;
+        return;
+      default: bail();
+    }
+  }
+
+ private:
+  std::map<uint32_t, int> consts_;
+
+  bool is(int v, POp op) const { return v >= 0 && ir.nodes[size_t(v)].op == op; }
+  bool is2(int v, POp op, int a, int b) const {
+    return is(v, op) && ir.nodes[size_t(v)].a == a && ir.nodes[size_t(v)].b == b;
+  }
+  bool isc(int v, float x) const {
+    if (!is(v, POp::Const)) return false;
+    float k = ir.nodes[size_t(v)].k;
+    return std::memcmp(&k, &x, 4) == 0;
+  }
+  const PNode &at(int v) const { return ir.nodes[size_t(v)]; }
+
+  // r == mix(b, A2, h) OP (k * h) * (1 - h), h = clamp(t, 0, 1), t = 0.5 OPT (0.5 * (b OPD a)) / k
+  POp smooth_kind(int r, int a, int b, int k) const {
+    if (!is(r, POp::Sub) && !is(r, POp::Add)) return POp::X;
+    const int m = at(r).a, q = at(r).b;
+    if (!is(m, POp::Mix) || at(m).a != b) return POp::X;
+    const int h = at(m).c;
+    // q = (k * h) * (1 - h)
+    if (!is(q, POp::Mul) || !is2(at(q).a, POp::Mul, k, h) || !is(at(q).b, POp::Sub) || !isc(at(at(q).b).a, 1.0f) ||
+        at(at(q).b).b != h)
+      return POp::X;
+    if (!is(h, POp::Clamp) || !isc(at(h).b, 0.0f) || !isc(at(h).c, 1.0f)) return POp::X;
+    const int t = at(h).a;
+    if ((!is(t, POp::Add) && !is(t, POp::Sub)) || !isc(at(t).a, 0.5f)) return POp::X;
+    const int dv = at(t).b;
+    if (!is(dv, POp::Div) || at(dv).b != k) return POp::X;
+    const int hm = at(dv).a;
+    if (!is(hm, POp::Mul) || !isc(at(hm).a, 0.5f)) return POp::X;
+    const int df = at(hm).b;
+    const int a2 = at(m).b;
+    if (is(r, POp::Sub) && is(t, POp::Add) && a2 == a && is2(df, POp::Sub, b, a)) return POp::SmoothUnion;
+    if (is(r, POp::Add) && is(t, POp::Sub) && a2 == a && is2(df, POp::Sub, b, a)) return POp::SmoothIntersection;
+    if (is(r, POp::Add) && is(t, POp::Sub) && is(a2, POp::Neg) && at(a2).a == a && is2(df, POp::Add, b, a))
+      return POp::SmoothSubtraction;
+    return POp::X;
+  }
+};
+
 // Functions reachable from `root` in callee-first order; recursion is an error.
 void collect_calls(const Stmt *s, std::vector<const Expr *> &calls);
 void collect_calls(const Expr *e, std::vector<const Expr *> &calls) {
@@ -2924,6 +3207,25 @@ FrontendResult translate(const std::string &source, Lang lang, const std::string
       r.run_fp32_ops = (R.fp_u + R.fp_v) / 4.0;
       r.run_sfu_ops = (R.sfu_u + R.sfu_v) / 4.0;
     } catch (const RunBail &) {
+    }
+    // tile-pruning form of sdf3d, when it is straight-line float code with
+    // combinators worth skipping
+    try {
+      PruneBuilder PB;
+      const int X = PB.node(POp::X), Y = PB.node(POp::Y), Z = PB.node(POp::Z);
+      PB.env[sdf->params[0].sym] = {X, Y, Z};
+      std::vector<int> ret;
+      bool done = false;
+      PB.block(sdf->body, ret, done);
+      if (!done || ret.size() != 1) throw PruneBail{};
+      PB.ir.root = ret[0];
+      PruneCode pc = prune_codegen(PB.ir);
+      if (pc.ok) {
+        E.out << pc.cuda;
+        r.prune_combinators = pc.combinators;
+        r.prune_words = pc.words;
+      }
+    } catch (const PruneBail &) {
     }
     r.cuda = E.out.str();
     for (auto &w : M.warnings) r.warnings.push_back(w);

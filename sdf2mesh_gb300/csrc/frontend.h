@@ -26,6 +26,8 @@ struct FrontendResult {
   bool ops_exact = true;              // false when a loop bound was not static
   double run_fp32_ops = 0;            // per point in runs of 4 sharing x, y (0: no run form)
   double run_sfu_ops = 0;
+  int prune_combinators = 0;          // combinators the tile-pruning form can skip (0: no such form)
+  int prune_words = 0;                // 32-bit activity words per tile
 };
 
 // Built-in WGSL modules selected by `use <name>;` (shader.rs:12-20, 50-62).

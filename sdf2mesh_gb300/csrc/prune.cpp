@@ -1,0 +1,417 @@
+// prune.cpp -- segment analysis and code generation for tile pruning (see
+// prune.h for the idea and the soundness argument).
+//
+// Segments.  Operand `side` (0 = a, 1 = b) of an enabled combinator c opens
+// segment (c, side).  A node belongs to the innermost segment through which
+// every path from it to the result passes: the post-dominating combinator
+// operand edge.  Nodes are visited from the result backwards, and a node's
+// segment is the lowest common ancestor, in the segment tree, of what each
+// of its uses requires.  A node in segment S is needed only when S is
+// active, so the point code evaluates S's nodes inside one `if` on S's bit.
+//
+// Generated code:
+//   s2m_user_sdf_tile(X, Y, Z, m, fp, sfu)   intervals of the tile's coordinates
+//       -> activity bits m[] (2 per combinator: operand a needed, operand b
+//          needed) and the FP32 / SFU operations per point that remain;
+//   s2m_user_sdf_pruned(x, y, z, m)          the point value, evaluating only
+//       the active segments; bit-identical to s2m_user_sdf.
+#include "prune.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+
+namespace s2m {
+namespace {
+
+// A combinator side is worth a branch when its subgraph costs at least this
+// (FP32 ops + 4 per SFU op).
+constexpr double kMinSkipWeight = 6.0;
+constexpr int kMaxCombinators = 256;
+
+std::string lit(float v) {
+  if (std::isnan(v)) return "__int_as_float(0x7fc00000)";
+  if (std::isinf(v)) return v > 0 ? "__int_as_float(0x7f800000)" : "__int_as_float(0xff800000)";
+  char b[64];
+  std::snprintf(b, sizeof b, "%af", double(v));
+  return std::string("(") + b + ")";
+}
+
+bool is_comb(POp op) {
+  return op == POp::Min || op == POp::Max || op == POp::SmoothUnion || op == POp::SmoothIntersection ||
+         op == POp::SmoothSubtraction;
+}
+
+bool is_leaf(POp op) { return op == POp::X || op == POp::Y || op == POp::Z || op == POp::Const; }
+
+struct OpCost {
+  double fp = 0, sfu = 0;
+  double weight() const { return fp + 4.0 * sfu; }
+};
+
+OpCost node_cost(POp op) {
+  switch (op) {
+    // negation is an operand modifier on the GPU, free as in the frontend's count
+    case POp::X: case POp::Y: case POp::Z: case POp::Const: case POp::Neg: return {0, 0};
+    case POp::Add: case POp::Sub: case POp::Mul: case POp::Abs: case POp::Floor: case POp::Ceil:
+    case POp::Min: case POp::Max:
+      return {1, 0};
+    case POp::Clamp: case POp::Saturate: return {2, 0};
+    case POp::Mix: return {4, 0};
+    case POp::Div: case POp::Sqrt: case POp::Sin: case POp::Cos: case POp::Exp: case POp::Log: case POp::Pow:
+    case POp::Atan2:
+      return {0, 1};
+    case POp::SmoothUnion: case POp::SmoothIntersection: case POp::SmoothSubtraction: return {13, 1};
+  }
+  return {0, 0};
+}
+
+class Pruner {
+ public:
+  explicit Pruner(const PruneIR &ir) : ir_(ir), n_(int(ir.nodes.size())) {}
+
+  PruneCode run() {
+    PruneCode pc;
+    if (ir_.root < 0 || ir_.root >= n_) return pc;
+    mark_live();
+    // 1. every combinator enabled; 2. keep those with a side worth skipping
+    std::vector<int> cand;
+    for (int v = 0; v < n_; ++v)
+      if (live_[v] && is_comb(ir_.nodes[size_t(v)].op)) cand.push_back(v);
+    if (cand.empty()) return pc;
+    set_enabled(cand);
+    owners();
+    std::vector<double> sub = subtree_weights();
+    std::vector<std::pair<double, int>> keep;
+    for (size_t ci = 0; ci < combs_.size(); ++ci) {
+      double w = std::max(sub[size_t(seg(int(ci), 0))], sub[size_t(seg(int(ci), 1))]);
+      if (w >= kMinSkipWeight) keep.push_back({w, combs_[ci]});
+    }
+    if (keep.empty()) return pc;
+    if (int(keep.size()) > kMaxCombinators) {
+      std::stable_sort(keep.begin(), keep.end(), [](auto &x, auto &y) { return x.first > y.first; });
+      keep.resize(size_t(kMaxCombinators));
+    }
+    std::vector<int> en;
+    for (auto &k : keep) en.push_back(k.second);
+    std::sort(en.begin(), en.end());
+    set_enabled(en);
+    owners();
+    pc.combinators = int(combs_.size());
+    pc.words = (2 * pc.combinators + 31) / 32;
+    std::ostringstream o;
+    o << "// tile pruning: " << pc.combinators << " combinators, " << pc.words << " words of activity bits\n";
+    o << "#define S2M_HAS_PRUNE 1\n#define S2M_PRUNE_WORDS " << pc.words << "\n";
+    emit_tile(o, pc.words);
+    emit_point(o);
+    pc.cuda = o.str();
+    pc.ok = true;
+    return pc;
+  }
+
+ private:
+  const PruneIR &ir_;
+  int n_;
+  std::vector<char> live_;
+  std::vector<std::vector<std::pair<int, int>>> uses_;
+  std::vector<int> comb_of_;  // node -> enabled combinator index, or -1
+  std::vector<int> combs_;    // enabled combinator nodes, ascending
+  std::vector<int> owner_;    // node -> segment
+  std::vector<int> sparent_, sdepth_;
+
+  static int seg(int ci, int side) { return 1 + 2 * ci + side; }
+  const PNode &nd(int v) const { return ir_.nodes[size_t(v)]; }
+
+  void mark_live() {
+    live_.assign(size_t(n_), 0);
+    uses_.assign(size_t(n_), {});
+    live_[size_t(ir_.root)] = 1;
+    for (int v = n_ - 1; v >= 0; --v) {
+      if (!live_[size_t(v)]) continue;
+      const PNode &p = nd(v);
+      const int args[3] = {p.a, p.b, p.c};
+      for (int i = 0; i < 3; ++i)
+        if (args[i] >= 0) {
+          live_[size_t(args[i])] = 1;
+          uses_[size_t(args[i])].push_back({v, i});
+        }
+    }
+  }
+
+  void set_enabled(const std::vector<int> &en) {
+    combs_ = en;
+    comb_of_.assign(size_t(n_), -1);
+    for (size_t i = 0; i < en.size(); ++i) comb_of_[size_t(en[i])] = int(i);
+  }
+
+  int lca(int a, int b) const {
+    while (sdepth_[size_t(a)] > sdepth_[size_t(b)]) a = sparent_[size_t(a)];
+    while (sdepth_[size_t(b)] > sdepth_[size_t(a)]) b = sparent_[size_t(b)];
+    while (a != b) {
+      a = sparent_[size_t(a)];
+      b = sparent_[size_t(b)];
+    }
+    return a;
+  }
+
+  void owners() {
+    const size_t ns = 1 + 2 * combs_.size();
+    sparent_.assign(ns, -1);
+    sdepth_.assign(ns, 0);
+    owner_.assign(size_t(n_), -1);
+    for (int v = n_ - 1; v >= 0; --v) {
+      if (!live_[size_t(v)]) continue;
+      int o = -1;
+      if (v == ir_.root) o = 0;
+      for (auto &[u, pos] : uses_[size_t(v)]) {
+        const int cu = comb_of_[size_t(u)];
+        const int want = (cu >= 0 && pos < 2) ? seg(cu, pos) : owner_[size_t(u)];
+        o = o < 0 ? want : lca(o, want);
+      }
+      owner_[size_t(v)] = o;
+      const int cv = comb_of_[size_t(v)];
+      if (cv >= 0)
+        for (int side = 0; side < 2; ++side) {
+          sparent_[size_t(seg(cv, side))] = o;
+          sdepth_[size_t(seg(cv, side))] = sdepth_[size_t(o)] + 1;
+        }
+    }
+  }
+
+  // Weight of every segment including the segments nested in it.
+  std::vector<double> subtree_weights() const {
+    const size_t ns = sparent_.size();
+    std::vector<double> w(ns, 0.0);
+    for (int v = 0; v < n_; ++v)
+      if (live_[size_t(v)] && !is_leaf(nd(v).op)) w[size_t(owner_[size_t(v)])] += node_cost(nd(v).op).weight();
+    std::vector<int> order(ns);
+    for (size_t i = 0; i < ns; ++i) order[i] = int(i);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return sdepth_[size_t(a)] > sdepth_[size_t(b)]; });
+    for (int s : order)
+      if (sparent_[size_t(s)] >= 0) w[size_t(sparent_[size_t(s)])] += w[size_t(s)];
+    return w;
+  }
+
+  std::string val(int v) const {
+    const PNode &p = nd(v);
+    switch (p.op) {
+      case POp::X: return "x";
+      case POp::Y: return "y";
+      case POp::Z: return "z";
+      case POp::Const: return lit(p.k);
+      default: return "v" + std::to_string(v);
+    }
+  }
+
+  std::string ival(int v) const {
+    const PNode &p = nd(v);
+    switch (p.op) {
+      case POp::X: return "X";
+      case POp::Y: return "Y";
+      case POp::Z: return "Z";
+      case POp::Const: return "s2i_pt(" + lit(p.k) + ")";
+      default: return "i" + std::to_string(v);
+    }
+  }
+
+  // Point expression of a node (combinators: their full arithmetic).
+  std::string expr(int v) const {
+    const PNode &p = nd(v);
+    const std::string A = p.a >= 0 ? val(p.a) : "", B = p.b >= 0 ? val(p.b) : "", C = p.c >= 0 ? val(p.c) : "";
+    switch (p.op) {
+      case POp::Neg: return "(-" + A + ")";
+      case POp::Add: return "(" + A + " + " + B + ")";
+      case POp::Sub: return "(" + A + " - " + B + ")";
+      case POp::Mul: return "(" + A + " * " + B + ")";
+      case POp::Div: return "(" + A + " / " + B + ")";
+      case POp::Abs: return "s2_abs(" + A + ")";
+      case POp::Floor: return "s2_floor(" + A + ")";
+      case POp::Ceil: return "s2_ceil(" + A + ")";
+      case POp::Sqrt: return "s2_sqrt(" + A + ")";
+      case POp::Min: return "s2_min(" + A + ", " + B + ")";
+      case POp::Max: return "s2_max(" + A + ", " + B + ")";
+      case POp::Clamp: return "s2_clamp(" + A + ", " + B + ", " + C + ")";
+      case POp::Saturate: return "s2_saturate(" + A + ")";
+      case POp::Mix: return "s2_mix(" + A + ", " + B + ", " + C + ")";
+      case POp::Sin: return "s2_sin(" + A + ")";
+      case POp::Cos: return "s2_cos(" + A + ")";
+      case POp::Exp: return "s2_exp(" + A + ")";
+      case POp::Log: return "s2_log(" + A + ")";
+      case POp::Pow: return "s2_pow(" + A + ", " + B + ")";
+      case POp::Atan2: return "s2_atan2(" + A + ", " + B + ")";
+      case POp::SmoothUnion: return "s2_op_smooth_union(" + A + ", " + B + ", " + C + ")";
+      case POp::SmoothIntersection: return "s2_op_smooth_intersection(" + A + ", " + B + ", " + C + ")";
+      case POp::SmoothSubtraction: return "s2_op_smooth_subtraction(" + A + ", " + B + ", " + C + ")";
+      default: return "";
+    }
+  }
+
+  // Interval of a node; enabled combinators also store their decision in d<v>.
+  std::string iexpr(int v) const {
+    const PNode &p = nd(v);
+    const std::string A = p.a >= 0 ? ival(p.a) : "", B = p.b >= 0 ? ival(p.b) : "", C = p.c >= 0 ? ival(p.c) : "";
+    const std::string D = comb_of_[size_t(v)] >= 0 ? "&d" + std::to_string(v) : "nullptr";
+    switch (p.op) {
+      case POp::Neg: return "s2i_neg(" + A + ")";
+      case POp::Add: return "s2i_add(" + A + ", " + B + ")";
+      case POp::Sub: return "s2i_sub(" + A + ", " + B + ")";
+      case POp::Mul: return p.a == p.b ? "s2i_sq(" + A + ")" : "s2i_mul(" + A + ", " + B + ")";
+      case POp::Div: return "s2i_div(" + A + ", " + B + ")";
+      case POp::Abs: return "s2i_abs(" + A + ")";
+      case POp::Floor: return "s2i_floor(" + A + ")";
+      case POp::Ceil: return "s2i_ceil(" + A + ")";
+      case POp::Sqrt: return "s2i_sqrt(" + A + ")";
+      case POp::Min: return "s2i_min_sel(" + A + ", " + B + ", " + D + ")";
+      case POp::Max: return "s2i_max_sel(" + A + ", " + B + ", " + D + ")";
+      case POp::Clamp: return "s2i_clamp(" + A + ", " + B + ", " + C + ")";
+      case POp::Saturate: return "s2i_clamp(" + A + ", s2i_pt(0.0f), s2i_pt(1.0f))";
+      case POp::Mix: return "s2i_mix(" + A + ", " + B + ", " + C + ")";
+      case POp::Sin: case POp::Cos: return "s2i_unit(" + A + ")";
+      case POp::Atan2: return "s2i_angle(" + A + ", " + B + ")";
+      case POp::Exp: case POp::Log: case POp::Pow: return "s2i_unknown()";
+      case POp::SmoothUnion: return "s2i_smooth_union_sel(" + A + ", " + B + ", " + C + ", " + D + ")";
+      case POp::SmoothIntersection: return "s2i_smooth_intersection_sel(" + A + ", " + B + ", " + C + ", " + D + ")";
+      case POp::SmoothSubtraction: return "s2i_smooth_subtraction_sel(" + A + ", " + B + ", " + C + ", " + D + ")";
+      default: return ival(v);
+    }
+  }
+
+  static std::string bit_test(int bit) {
+    return "(m[" + std::to_string(bit >> 5) + "] & 0x" + [&] {
+      char b[16];
+      std::snprintf(b, sizeof b, "%xu", 1u << (bit & 31));
+      return std::string(b);
+    }() + ")";
+  }
+
+  void emit_tile(std::ostringstream &o, int words) const {
+    o << "S2HD void s2m_user_sdf_tile(const s2i X, const s2i Y, const s2i Z, unsigned *m, float *fp, float *sfu)\n{\n";
+    o << "  (void)X; (void)Y; (void)Z;\n";
+    for (int v : combs_) o << "  int d" << v << " = 0;\n";
+    for (int v = 0; v < n_; ++v) {
+      if (!live_[size_t(v)] || is_leaf(nd(v).op)) continue;
+      o << "  const s2i i" << v << " = " << iexpr(v) << ";\n";
+    }
+    // activity: parents (larger node index) before the segments nested in them
+    const size_t ns = 1 + 2 * combs_.size();
+    o << "  const bool s0 = true;\n";
+    for (int ci = int(combs_.size()) - 1; ci >= 0; --ci) {
+      const int v = combs_[size_t(ci)];
+      o << "  const bool s" << seg(ci, 0) << " = s" << owner_[size_t(v)] << " && d" << v << " != 2;\n";
+      o << "  const bool s" << seg(ci, 1) << " = s" << owner_[size_t(v)] << " && d" << v << " != 1;\n";
+    }
+    for (int w = 0; w < words; ++w) {
+      o << "  m[" << w << "] = 0u";
+      for (int b = 0; b < 32; ++b) {
+        const int s = 1 + 32 * w + b;
+        if (size_t(s) < ns) o << " | (s" << s << " ? 0x" << std::hex << (1u << b) << std::dec << "u : 0u)";
+      }
+      o << ";\n";
+    }
+    // operations per point that remain: each active segment's own nodes, and
+    // the arithmetic of every needed combinator that keeps both operands
+    std::vector<OpCost> sc(ns);
+    for (int v = 0; v < n_; ++v) {
+      if (!live_[size_t(v)] || is_leaf(nd(v).op) || comb_of_[size_t(v)] >= 0) continue;
+      OpCost c = node_cost(nd(v).op);
+      sc[size_t(owner_[size_t(v)])].fp += c.fp;
+      sc[size_t(owner_[size_t(v)])].sfu += c.sfu;
+    }
+    auto sum = [&](bool sfu) {
+      std::ostringstream e;
+      e << "0.0f";
+      for (size_t s = 0; s < ns; ++s) {
+        const double c = sfu ? sc[s].sfu : sc[s].fp;
+        if (c > 0) e << " + (s" << s << " ? " << c << ".0f : 0.0f)";
+      }
+      for (size_t ci = 0; ci < combs_.size(); ++ci) {
+        const int v = combs_[ci];
+        OpCost c = node_cost(nd(v).op);
+        const double x = sfu ? c.sfu : c.fp;
+        if (x > 0) e << " + (s" << owner_[size_t(v)] << " && d" << v << " == 0 ? " << x << ".0f : 0.0f)";
+      }
+      return e.str();
+    };
+    o << "  *fp = " << sum(false) << ";\n";
+    o << "  *sfu = " << sum(true) << ";\n";
+    o << "}\n";
+  }
+
+  // Point code.  Every node is placed in a region: the innermost operand-b
+  // segment enclosing its segment, or the top level.  A region's nodes are
+  // emitted in ascending order; a node whose segment is not the region
+  // itself (an operand-a segment inside it) is guarded by that segment's
+  // bit, consecutive nodes of one segment sharing one `if`.  A combinator is
+  // emitted where its index falls, without a guard of its own (when its
+  // segment is inactive its value is simply not used), as
+  //     if (b active) { <region of operand b>; v = a active ? op(a, b) : b; } else v = a;
+  // so a combinator that keeps operand a costs one test.  Operand-a
+  // segments are not nested blocks: a chain of combinators stays one level
+  // deep.
+  void emit_region(std::ostringstream &o, int R, const std::vector<std::vector<int>> &members,
+                   const std::string &ind) const {
+    int open = R;
+    auto close = [&]() {
+      if (open != R) o << ind << "}\n";
+      open = R;
+    };
+    for (int v : members[size_t(R)]) {
+      const int ci = comb_of_[size_t(v)];
+      if (ci >= 0) {
+        close();
+        const PNode &p = nd(v);
+        const int sa = seg(ci, 0), sb = seg(ci, 1);
+        const std::string A = val(p.a), B = val(p.b);
+        const std::string keepA = p.op == POp::SmoothSubtraction ? "(-" + A + ")" : A;
+        o << ind << "if " << bit_test(sb - 1) << " {\n";
+        emit_region(o, sb, members, ind + "  ");
+        o << ind << "  if " << bit_test(sa - 1) << " v" << v << " = " << expr(v) << ";\n";
+        o << ind << "  else v" << v << " = " << B << ";\n";
+        o << ind << "} else {\n" << ind << "  v" << v << " = " << keepA << ";\n" << ind << "}\n";
+        continue;
+      }
+      const int s = owner_[size_t(v)];
+      if (s != open) {
+        close();
+        if (s != R) o << ind << "if " << bit_test(s - 1) << " {\n";
+        open = s;
+      }
+      o << ind << (open != R ? "  " : "") << "v" << v << " = " << expr(v) << ";\n";
+    }
+    close();
+  }
+
+  // Region of each node: the innermost operand-b segment among its segment
+  // and the segment's ancestors (0: top level).
+  std::vector<std::vector<int>> regions() const {
+    const size_t ns = 1 + 2 * combs_.size();
+    std::vector<std::vector<int>> members(ns);
+    for (int v = 0; v < n_; ++v) {
+      if (!live_[size_t(v)] || is_leaf(nd(v).op)) continue;
+      int r = owner_[size_t(v)];
+      while (r != 0 && (r - 1) % 2 != 1) r = sparent_[size_t(r)];
+      members[size_t(r)].push_back(v);
+    }
+    return members;
+  }
+
+  void emit_point(std::ostringstream &o) const {
+    // Out of line on the device (S2M_PRUNED_FN): inlined into the lattice
+    // kernel's point loop, the branchy body let the compiler keep far more
+    // values live across iterations than the registers hold.
+    o << "S2M_PRUNED_FN float s2m_user_sdf_pruned(float x, float y, float z, const unsigned *m)\n{\n";
+    o << "  (void)x; (void)y; (void)z;\n";
+    for (int v = 0; v < n_; ++v)
+      if (live_[size_t(v)] && !is_leaf(nd(v).op)) o << "  float v" << v << ";\n";
+    emit_region(o, 0, regions(), "  ");
+    o << "  return " << val(ir_.root) << ";\n}\n";
+  }
+};
+
+}  // namespace
+
+PruneCode prune_codegen(const PruneIR &ir) { return Pruner(ir).run(); }
+
+}  // namespace s2m

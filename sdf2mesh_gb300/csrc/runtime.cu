@@ -76,23 +76,32 @@ int device_sm_count() {
 
 }  // namespace
 
-// Evaluation-kernel variants compiled into every SDF module (the table in
-// s2m_dc_kernels.cuh): name, z-run length.
+// Evaluation-kernel variants compiled into every SDF module (the tables in
+// s2m_dc_kernels.cuh): name, z-run length, whether it evaluates the run-of-4
+// form, and whether it is a tile-pruned variant (present only in modules of
+// SDFs with a pruning form).
 struct EvalVariant {
   const char *name;
   int run;
+  bool vec;
+  bool pruned;
 };
 constexpr EvalVariant kEvalVariants[] = {
-    {"s2m_eval_b2r4", 4}, {"s2m_eval_b3r4", 4}, {"s2m_eval_b4r4", 4}, {"s2m_eval_b2v4", 4}, {"s2m_eval_b3v4", 4}};
+    {"s2m_eval_b2r4", 4, false, false}, {"s2m_eval_b3r4", 4, false, false}, {"s2m_eval_b4r4", 4, false, false},
+    {"s2m_eval_b2v4", 4, true, false},  {"s2m_eval_b3v4", 4, true, false},  {"s2m_evalp_b8", 1, false, true},
+    {"s2m_evalp_b16", 1, false, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
   std::string user_cuda;
   double fp32_ops = 0, sfu_ops = 0;
   double run_fp32_ops = 0, run_sfu_ops = 0;  // per point in runs of 4 (0: no run form)
+  int prune_words = 0;                        // activity words per pruning tile (0: no pruning form)
+  int prune_combinators = 0;
   uint32_t flags = 0;
   cudaLibrary_t lib = nullptr;
-  cudaKernel_t k_eval[kNumEvalVariants] = {};
+  cudaKernel_t k_eval[kNumEvalVariants] = {};  // null: variant not in this module
+  cudaKernel_t k_tiles = nullptr;               // tile pass of the pruned variants
   cudaKernel_t k_vertices = nullptr;
   // precision mode: a second module with the QEF vertex kernel, built on the
   // first QEF job (most SDFs never need it, and it compiles slowly)
@@ -102,6 +111,7 @@ struct s2m_sdf {
   // autotuned evaluation variant (-1: not tuned yet) and its timings (ns per point)
   mutable std::mutex tune_mu;
   mutable int eval_variant = -1;
+  mutable int eval_variant_plain = -1;  // fastest variant without pruning (runs with no pruning buffers)
   mutable double tune_ns[kNumEvalVariants] = {};
   mutable int tune_regs[kNumEvalVariants] = {};
   mutable int tune_local[kNumEvalVariants] = {};  // local (spill/stack) bytes per thread
@@ -118,6 +128,8 @@ struct s2m_mesh {
   unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
   unsigned short *cell_masks = nullptr;      // per thread of a cell tile: candidate bits of its cells
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
+  // tile pruning: [ops FP32, ops SFU] (2 u64) then activity words of a slab's tiles
+  unsigned long long *prune_buf = nullptr;
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -139,6 +151,10 @@ struct s2m_mesh {
   uint64_t nverts = 0, ntris = 0, invalid = 0, ncand = 0;
   uint32_t errflags = 0;
   uint64_t launches = 0;
+  // SDF operations of the last run's lattice evaluation, and its points
+  bool last_pruned = false;
+  int last_variant = 0;
+  double eval_points = 0, eval_fp_ops = 0, eval_sfu_ops = 0;
   // optional per-kernel timing: an event pair around each launch
   bool profile = false;
   std::vector<cudaEvent_t> ev;
@@ -204,11 +220,24 @@ int nvrtc_build(const s2m_sdf *s, bool qef, cudaLibrary_t *lib, char *err, size_
 int compile_module(s2m_sdf *s, char *err, size_t errlen) {
   int rc = nvrtc_build(s, false, &s->lib, err, errlen);
   if (rc != S2M_OK) return rc;
-  for (int v = 0; v < kNumEvalVariants; ++v)
+  // Pruned variants are bit-exact only without FMA contraction (their
+  // interval bounds and the skipped arithmetic assume separately rounded
+  // operations), so an S2M_COMPILE_FMAD module does not use them.
+  const bool prune = s->prune_words > 0 && !(s->flags & (S2M_COMPILE_FMAD | S2M_COMPILE_NO_PRUNE));
+  for (int v = 0; v < kNumEvalVariants; ++v) {
+    if (kEvalVariants[v].pruned && !prune) {
+      s->k_eval[v] = nullptr;
+      continue;
+    }
     if (cudaLibraryGetKernel(&s->k_eval[v], s->lib, kEvalVariants[v].name) != cudaSuccess) {
       set_err(err, errlen, std::string("kernel missing from the compiled module: ") + kEvalVariants[v].name);
       return S2M_E_CUDA;
     }
+  }
+  if (prune && cudaLibraryGetKernel(&s->k_tiles, s->lib, "s2m_tiles") != cudaSuccess) {
+    set_err(err, errlen, "kernel missing from the compiled module: s2m_tiles");
+    return S2M_E_CUDA;
+  }
   if (cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
@@ -265,13 +294,13 @@ void give_pinned_slot(unsigned long long *p) {
 }
 
 void free_buffers(s2m_mesh *m) {
-  void *ptrs[] = {m->ring, m->slab_ctrl, m->cell_masks, m->tile_cnt, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
+  void *ptrs[] = {m->ring, m->slab_ctrl, m->cell_masks, m->tile_cnt, m->prune_buf, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
                   m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
                   m->jobctl};
   for (void *p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   if (m->h_read) give_pinned_slot(m->h_read);
-  m->ring = nullptr; m->slab_ctrl = nullptr; m->cell_masks = nullptr; m->tile_cnt = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
+  m->ring = nullptr; m->slab_ctrl = nullptr; m->cell_masks = nullptr; m->tile_cnt = nullptr; m->prune_buf = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
   m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
   m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
   m->jobctl = nullptr; m->h_read = nullptr;
@@ -326,6 +355,28 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   return S2M_OK;
 }
 
+// Tiles of slab planes k0 .. k0 + nk - 1 for the pruned variants: tzs planes
+// per tile (at most S2_PT_ZMAX, balanced), nzt tiles in z, none empty.
+struct PruneGeom {
+  int tzs = 0, nzt = 0;
+  long long ntiles = 0;
+};
+PruneGeom prune_geom(const S2Job &j, int nk) {
+  PruneGeom g;
+  const int parts = (nk + S2_PT_ZMAX - 1) / S2_PT_ZMAX;
+  g.tzs = (nk + parts - 1) / parts;
+  g.nzt = (nk + g.tzs - 1) / g.tzs;
+  const long long ntx = (j.P + S2_PT_XY - 1) / S2_PT_XY;
+  g.ntiles = ntx * ntx * g.nzt;
+  return g;
+}
+// Two operation counters, then the activity words of the largest slab
+// (nk <= D + 1 planes; the tile count grows with nk).
+size_t prune_buf_bytes(const s2m_mesh *m) {
+  const PruneGeom g = prune_geom(m->job, m->D + 1);
+  return 16 + size_t(g.ntiles) * size_t(m->sdf->prune_words) * 4;
+}
+
 void drop_graph(s2m_mesh *m) {
   if (m->graph) cudaGraphExecDestroy(m->graph);
   m->graph = nullptr;
@@ -352,6 +403,7 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cell_masks, m->cell_tiles * S2_CELL_BLOCK * 2, st));
   S2_CUDA(cudaMallocAsync(&m->tile_cnt, m->cell_tiles * 4, st));
+  if (m->sdf->k_tiles) S2_CUDA(cudaMallocAsync(&m->prune_buf, prune_buf_bytes(m), st));
   S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cand_val, m->cand_cap * 32, st));
   S2_CUDA(cudaMallocAsync(&m->cand_pos, m->cand_cap * 12, st));
@@ -472,8 +524,19 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
 
   const long long pts = (long long)j.P * j.P;
   const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
-  const int ev = m->sdf->eval_variant >= 0 ? m->sdf->eval_variant : 0;
+  int ev = m->sdf->eval_variant >= 0 ? m->sdf->eval_variant : 0;
+  // without pruning buffers (the no-allocation entry point) the fastest plain variant
+  if (kEvalVariants[ev].pruned && !m->prune_buf) ev = std::max(0, m->sdf->eval_variant_plain);
+  const bool pruned = kEvalVariants[ev].pruned;
   const int run = kEvalVariants[ev].run;
+  m->last_pruned = pruned;
+  m->last_variant = ev;
+  m->eval_points = 0;
+  m->eval_fp_ops = m->eval_sfu_ops = 0;
+  if (pruned) {
+    cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, 16, st);
+    if (e0 != cudaSuccess) return e0;
+  }
   for (int s = 0; s < m->nslabs; ++s) {
     int zc0 = s * m->D;
     int zc1 = std::min(m->nzc, zc0 + m->D);
@@ -481,10 +544,24 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     int nk = zc1 - k0 + 1;
     S2Job jj = j;
     float *ring = m->ring;
-    void *eargs[] = {&jj, &ring, &k0, &nk};
-    dim3 eg(eval_blocks, unsigned((nk + run - 1) / run));
-    S2_LAUNCH(0, double(pts) * nk,
-              cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
+    m->eval_points += double(pts) * nk;
+    if (pruned) {
+      PruneGeom g = prune_geom(j, nk);
+      unsigned long long *ops = m->prune_buf;
+      unsigned *bits = reinterpret_cast<unsigned *>(m->prune_buf + 2);
+      void *targs[] = {&jj, &bits, &ops, &k0, &nk, &g.tzs, &g.nzt};
+      S2_LAUNCH(0, 0, cudaLaunchKernel((const void *)m->sdf->k_tiles, dim3(unsigned((g.ntiles + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
+                                       dim3(S2_PT_BLOCK), targs, 0, st));
+      void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
+      S2_LAUNCH(0, double(pts) * nk,
+                cudaLaunchKernel((const void *)m->sdf->k_eval[ev], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK),
+                                 pargs, 0, st));
+    } else {
+      void *eargs[] = {&jj, &ring, &k0, &nk};
+      dim3 eg(eval_blocks, unsigned((nk + run - 1) / run));
+      S2_LAUNCH(0, double(pts) * nk,
+                cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
+    }
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
     unsigned cg = unsigned((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
     S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CELL_BLOCK, 0, st>>>(j, m->ring, m->cell_masks, m->tile_cnt, zc0, zc1),
@@ -510,16 +587,19 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   return cudaSuccess;
 }
 
-// Autotuner: time every evaluation variant on the job's first planes (into
-// the job's own ring, which the pipeline overwrites afterwards) and keep the
-// fastest for this SDF.  Runs once per SDF, on its first job.
+// Autotuner: time every evaluation variant of the module on up to 16 planes
+// through the middle of the job (into the job's own ring, which the pipeline
+// overwrites afterwards) and keep the fastest for this SDF.  A pruned variant
+// is timed with its tile pass.  Runs once per SDF, on its first job.
 int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   const s2m_sdf *sdf = m->sdf;
   std::lock_guard<std::mutex> lock(sdf->tune_mu);
   if (sdf->eval_variant >= 0) return S2M_OK;
   if (std::getenv("S2M_EVAL_VARIANT")) {
     int v = std::atoi(std::getenv("S2M_EVAL_VARIANT"));
-    sdf->eval_variant = (v >= 0 && v < kNumEvalVariants) ? v : 0;
+    if (v < 0 || v >= kNumEvalVariants || !sdf->k_eval[v]) v = 0;
+    sdf->eval_variant = v;
+    sdf->eval_variant_plain = kEvalVariants[v].pruned ? 0 : v;
     return S2M_OK;
   }
   const S2Job &j = m->job;
@@ -528,24 +608,41 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   // small jobs: too little work per launch to rank the variants; keep the default
   if (double(pts) * nk < 2.0e6) {
     sdf->eval_variant = 0;
+    sdf->eval_variant_plain = 0;
     return S2M_OK;
   }
+  int k0 = std::max(0, std::min(j.P - nk, j.P / 2 - nk / 2));
   cudaEvent_t a, b;
   S2_CUDA(cudaEventCreate(&a));
   S2_CUDA(cudaEventCreate(&b));
   const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
-  double best = 1e300;
-  int best_v = 0;
+  double best = 1e300, best_plain = 1e300;
+  int best_v = 0, best_plain_v = 0;
   for (int v = 0; v < kNumEvalVariants; ++v) {
+    if (!sdf->k_eval[v] || (kEvalVariants[v].pruned && !m->prune_buf)) {
+      sdf->tune_ns[v] = 0;
+      continue;
+    }
     float ms_best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
       S2Job jj = j;
       float *ring = m->ring;
-      int k0 = 0;
-      void *args[] = {&jj, &ring, &k0, &nk};
-      dim3 eg(eval_blocks, unsigned((nk + kEvalVariants[v].run - 1) / kEvalVariants[v].run));
       S2_CUDA(cudaEventRecord(a, st));
-      S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], eg, dim3(S2_EVAL_BLOCK), args, 0, st));
+      if (kEvalVariants[v].pruned) {
+        PruneGeom g = prune_geom(j, nk);
+        unsigned long long *ops = m->prune_buf;
+        unsigned *bits = reinterpret_cast<unsigned *>(m->prune_buf + 2);
+        void *targs[] = {&jj, &bits, &ops, &k0, &nk, &g.tzs, &g.nzt};
+        S2_CUDA(cudaLaunchKernel((const void *)sdf->k_tiles, dim3(unsigned((g.ntiles + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
+                                 dim3(S2_PT_BLOCK), targs, 0, st));
+        void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
+        S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK),
+                                 pargs, 0, st));
+      } else {
+        void *args[] = {&jj, &ring, &k0, &nk};
+        dim3 eg(eval_blocks, unsigned((nk + kEvalVariants[v].run - 1) / kEvalVariants[v].run));
+        S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], eg, dim3(S2_EVAL_BLOCK), args, 0, st));
+      }
       S2_CUDA(cudaEventRecord(b, st));
       S2_CUDA(cudaEventSynchronize(b));
       float ms = 0;
@@ -565,18 +662,34 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
       best = ns;
       best_v = v;
     }
+    if (!kEvalVariants[v].pruned && ns < best_plain) {
+      best_plain = ns;
+      best_plain_v = v;
+    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   sdf->eval_variant = best_v;
+  sdf->eval_variant_plain = best_plain_v;
   return S2M_OK;
 }
 
 int readback(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   S2_CUDA(cudaMemcpyAsync(m->h_read, m->jobctl, 4 * 8, cudaMemcpyDeviceToHost, st));
   S2_CUDA(cudaMemcpyAsync(m->h_read + 4, m->cand_base + m->nslabs, 8, cudaMemcpyDeviceToHost, st));
+  if (m->last_pruned) S2_CUDA(cudaMemcpyAsync(m->h_read + 5, m->prune_buf, 16, cudaMemcpyDeviceToHost, st));
   S2_CUDA(cudaStreamSynchronize(st));
   prof_collect(m);
+  if (m->last_pruned) {
+    m->eval_fp_ops = double(m->h_read[5]);
+    m->eval_sfu_ops = double(m->h_read[6]);
+  } else {
+    const bool run = kEvalVariants[m->last_variant].vec;
+    const double fp = run && m->sdf->run_fp32_ops > 0 ? m->sdf->run_fp32_ops : m->sdf->fp32_ops;
+    const double sfu = run && m->sdf->run_fp32_ops > 0 ? m->sdf->run_sfu_ops : m->sdf->sfu_ops;
+    m->eval_fp_ops = fp * m->eval_points;
+    m->eval_sfu_ops = sfu * m->eval_points;
+  }
   m->ntris = m->h_read[0];
   m->invalid = m->h_read[1];
   m->nverts = m->h_read[2];
@@ -738,6 +851,8 @@ int s2m_compile(const char *source, int lang, const char *sdf_name, uint32_t com
   s->sfu_ops = r.sfu_ops;
   s->run_fp32_ops = r.run_fp32_ops;
   s->run_sfu_ops = r.run_sfu_ops;
+  s->prune_words = r.prune_words;
+  s->prune_combinators = r.prune_combinators;
   s->flags = compile_flags;
   int rc = compile_module(s, err, errlen);
   if (rc != S2M_OK) {
@@ -789,6 +904,15 @@ int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double 
   return v;
 }
 
+int s2m_sdf_set_eval_variant(s2m_sdf *sdf, int variant) {
+  if (!sdf || variant < 0 || variant >= kNumEvalVariants || !sdf->k_eval[variant]) return S2M_E_INVALID;
+  std::lock_guard<std::mutex> lock(sdf->tune_mu);
+  sdf->eval_variant = variant;
+  if (!kEvalVariants[variant].pruned) sdf->eval_variant_plain = variant;
+  else if (sdf->eval_variant_plain < 0) sdf->eval_variant_plain = 0;
+  return S2M_OK;
+}
+
 int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_t namelen, int *registers,
                               int *local_bytes) {
   if (!sdf || variant < 0 || variant >= kNumEvalVariants) return S2M_E_INVALID;
@@ -796,6 +920,22 @@ int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_
   if (registers) *registers = sdf->tune_regs[variant];
   if (local_bytes) *local_bytes = sdf->tune_local[variant];
   return S2M_OK;
+}
+
+int s2m_sdf_prune_info(const s2m_sdf *sdf, int *combinators, int *words) {
+  if (!sdf) return S2M_E_INVALID;
+  const bool on = sdf->k_tiles != nullptr;
+  if (combinators) *combinators = on ? sdf->prune_combinators : 0;
+  if (words) *words = on ? sdf->prune_words : 0;
+  return S2M_OK;
+}
+
+int s2m_mesh_eval_ops(const s2m_mesh *m, double *points, double *fp32_ops, double *sfu_ops) {
+  if (!m) return S2M_E_INVALID;
+  if (points) *points = m->eval_points;
+  if (fp32_ops) *fp32_ops = m->eval_fp_ops;
+  if (sfu_ops) *sfu_ops = m->eval_sfu_ops;
+  return m->last_pruned ? 1 : 0;
 }
 
 int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {

@@ -105,6 +105,106 @@ S2_EVAL_VARIANT(s2m_eval_b2v4, 2, 4, true)
 S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
 #endif
 
+#if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
+// Tile pruning (the generated s2m_user_sdf_tile / s2m_user_sdf_pruned*).
+// A slab's planes k0 .. k0 + nk - 1 are cut into tiles of 8 x 8 points by
+// `tzs` planes (nzt tiles in z); tile t = (tz * nty + ty) * ntx + tx.
+
+struct S2PruneTile {
+  int i0, i1, j0, j1, kb, ke;  // inclusive point ranges
+};
+__device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long t, int k0, int nk, int tzs) {
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  S2PruneTile r;
+  const int tx = (int)(t % ntx);
+  const long long q = t / ntx;
+  const int ty = (int)(q % ntx);
+  const int tz = (int)(q / ntx);
+  r.i0 = tx * S2_PT_XY;
+  r.i1 = min(r.i0 + S2_PT_XY, job.P) - 1;
+  r.j0 = ty * S2_PT_XY;
+  r.j1 = min(r.j0 + S2_PT_XY, job.P) - 1;
+  r.kb = k0 + tz * tzs;
+  r.ke = min(r.kb + tzs, k0 + nk) - 1;
+  return r;
+}
+
+// One thread per tile: interval evaluation over the tile's coordinate box,
+// activity bits, and the SDF operations that remain (summed into ops[0] FP32,
+// ops[1] SFU, per lattice point evaluated).
+extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK)
+s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops, int k0, int nk, int tzs,
+          int nzt) {
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const long long ntiles = (long long)ntx * ntx * nzt;
+  const long long t = (long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
+  unsigned long long fp_ops = 0, sfu_ops = 0;
+  const S2PruneTile tl = s2_prune_tile(job, t < ntiles ? t : 0, k0, nk, tzs);
+  if (t < ntiles && tl.kb <= tl.ke) {
+    s2i X, Y, Z;
+    X.lo = s2_coord(job, tl.i0); X.hi = s2_coord(job, tl.i1);
+    Y.lo = s2_coord(job, tl.j0); Y.hi = s2_coord(job, tl.j1);
+    Z.lo = s2_coord(job, tl.kb); Z.hi = s2_coord(job, tl.ke);
+    unsigned m[S2M_PRUNE_WORDS];
+    float fp = 0.0f, sfu = 0.0f;
+    s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);
+#pragma unroll
+    for (int w = 0; w < S2M_PRUNE_WORDS; ++w) bits[t * S2M_PRUNE_WORDS + w] = m[w];
+    const unsigned long long npts =
+        (unsigned long long)(tl.i1 - tl.i0 + 1) * (unsigned long long)(tl.j1 - tl.j0 + 1) * (unsigned long long)(tl.ke - tl.kb + 1);
+    fp_ops = (unsigned long long)fp * npts;
+    sfu_ops = (unsigned long long)sfu * npts;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    fp_ops += __shfl_down_sync(0xffffffffu, fp_ops, o);
+    sfu_ops += __shfl_down_sync(0xffffffffu, sfu_ops, o);
+  }
+  if ((threadIdx.x & 31u) == 0 && (fp_ops | sfu_ops)) {
+    atomicAdd(ops, fp_ops);
+    atomicAdd(ops + 1, sfu_ops);
+  }
+}
+
+// Pruned lattice evaluation: one tile per warp, the lanes striding over the
+// tile's points.  The activity bits (in shared memory) are the same for the
+// whole warp, so the pruned function's branches never diverge.  Points past
+// the lattice edge (tiles are 8 x 8) evaluate a clamped point and store
+// nothing.
+__device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restrict__ ring,
+                                               const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) {
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const long long ntiles = (long long)ntx * ntx * nzt;
+  const long long t = (long long)blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5);
+  if (t >= ntiles) return;
+  const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, tzs);
+  if (tl.kb > tl.ke) return;
+  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_PRUNE_WORDS];
+  const int lane = (int)(threadIdx.x & 31u);
+  if (lane < S2M_PRUNE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
+  __syncwarp();
+  const unsigned *m = s_bits[threadIdx.x >> 5];
+  const int npts = S2_PT_XY * S2_PT_XY * (tl.ke - tl.kb + 1);
+#pragma unroll 1
+  for (int q = lane; q < npts; q += 32) {
+    const int i = tl.i0 + (q & (S2_PT_XY - 1));
+    const int j = tl.j0 + ((q >> 3) & (S2_PT_XY - 1));
+    const int k = tl.kb + (q >> 6);
+    const float f = s2m_user_sdf_pruned(s2_coord(job, min(i, tl.i1)), s2_coord(job, min(j, tl.j1)), s2_coord(job, k), m);
+    if (i <= tl.i1 && j <= tl.j1) ring[(long long)(k % job.ring) * job.plane + (long long)j * job.pitch + i] = f;
+  }
+}
+
+#define S2_EVALP_VARIANT(NAME, MINB)                                                              \
+  extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
+  NAME(S2Job job, float *__restrict__ ring, const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) { \
+    s2_eval_pruned(job, ring, bits, k0, nk, tzs, nzt);                                            \
+  }
+// Keep this table in step with kEvalVariants in runtime.cu.
+S2_EVALP_VARIANT(s2m_evalp_b8, 8)
+S2_EVALP_VARIANT(s2m_evalp_b16, 16)
+#endif
+
 
 
 // Vertices of every candidate of the job, one candidate per thread (dense:

@@ -89,6 +89,11 @@ struct S2MeshDev {
 #define S2_CELL_TILE (S2_CELL_BLOCK * S2_CELL_CPT)
 #define S2_EVAL_BLOCK 256
 #define S2_EVAL_RUN 4
+// Tile pruning: tiles of 8 x 8 lattice points in x and y and at most 8
+// planes in z; the pruned evaluation runs one tile per warp, 4 per block.
+#define S2_PT_XY 8
+#define S2_PT_ZMAX 8
+#define S2_PT_BLOCK 128
 #define S2_VX_BLOCK 128
 #define S2_VC_BLOCK 256
 #define S2_VC_CPT 4

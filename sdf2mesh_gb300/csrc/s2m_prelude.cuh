@@ -11,7 +11,11 @@
 
 #if defined(__CUDACC_RTC__) || defined(__CUDACC__)
 #define S2HD __host__ __device__ __forceinline__
+#define S2M_PRUNED_FN __host__ __device__ __noinline__
+#define S2I_FN __host__ __device__ __noinline__
 #else
+#define S2M_PRUNED_FN inline
+#define S2I_FN inline
 #include <cmath>
 #include <cstring>
 #define S2HD inline
@@ -257,6 +261,167 @@ S2_VEC1(s2_tanh) S2_VEC1(s2_saturate) S2_VEC1(s2_radians) S2_VEC1(s2_degrees)
 S2_VEC2(s2_pow) S2_VEC2(s2_atan2) S2_VEC2(s2_min) S2_VEC2(s2_max) S2_VEC2(s2_fmod_glsl)
 S2_VEC2(s2_fmod_wgsl) S2_VEC2(s2_imod)
 S2_VEC3(s2_clamp) S2_VEC3(s2_fma) S2_VEC3(s2_mix)
+
+// The sdf::op smooth operators, operation for operation as their WGSL text
+// (0.5 * (b - a) / k is (0.5 * (b - a)) / k; k * h * (1 - h) is (k * h) * (1 - h)).
+S2HD float s2_op_smooth_union(float a, float b, float k) {
+  const float h = s2_clamp(0.5f + 0.5f * (b - a) / k, 0.0f, 1.0f);
+  return s2_mix(b, a, h) - k * h * (1.0f - h);
+}
+S2HD float s2_op_smooth_intersection(float a, float b, float k) {
+  const float h = s2_clamp(0.5f - 0.5f * (b - a) / k, 0.0f, 1.0f);
+  return s2_mix(b, a, h) + k * h * (1.0f - h);
+}
+S2HD float s2_op_smooth_subtraction(float a, float b, float k) {
+  const float h = s2_clamp(0.5f - 0.5f * (b + a) / k, 0.0f, 1.0f);
+  return s2_mix(b, -a, h) + k * h * (1.0f - h);
+}
+
+// ---------------------------------------------------------------------------
+// Intervals for tile pruning.  [lo, hi] bounds the binary32 value that the
+// point code computes for every point of a tile: each operation below applies
+// the point code's own round-to-nearest operation to the endpoints (or, for
+// products and quotients, to the four corners), which is sound because the
+// exact operation is monotone in each argument there and rounding is
+// monotone.  An interval with a NaN endpoint is unknown: every comparison on
+// it is false, so no decision rests on it.  Results with an infinite
+// endpoint become unknown as well, so a known interval always bounds finite
+// values.  The larger helpers are out of line on the device (S2I_FN): the
+// tile function calls them once per node, and inlining them all made its
+// compilation slower than the rest of the module together.
+struct s2i {
+  float lo, hi;
+};
+S2HD s2i s2i_unknown() { s2i r; r.lo = r.hi = __int_as_float(0x7fc00000u); return r; }
+S2HD bool s2i_ok(s2i a) { return fabsf(a.lo) <= 3.40282347e38f && fabsf(a.hi) <= 3.40282347e38f; }
+S2HD s2i s2i_pt(float v) { s2i r; r.lo = v; r.hi = v; return r; }
+S2HD s2i s2i_fin(float lo, float hi) {
+  s2i r; r.lo = lo; r.hi = hi;
+  return s2i_ok(r) ? r : s2i_unknown();
+}
+S2HD float s2i_min4(float a, float b, float c, float d) { return fminf(fminf(a, b), fminf(c, d)); }
+S2HD float s2i_max4(float a, float b, float c, float d) { return fmaxf(fmaxf(a, b), fmaxf(c, d)); }
+S2HD s2i s2i_neg(s2i a) { return s2i_ok(a) ? s2i_fin(-a.hi, -a.lo) : s2i_unknown(); }
+S2HD s2i s2i_add(s2i a, s2i b) { return s2i_ok(a) && s2i_ok(b) ? s2i_fin(a.lo + b.lo, a.hi + b.hi) : s2i_unknown(); }
+S2HD s2i s2i_sub(s2i a, s2i b) { return s2i_ok(a) && s2i_ok(b) ? s2i_fin(a.lo - b.hi, a.hi - b.lo) : s2i_unknown(); }
+S2I_FN s2i s2i_mul(s2i a, s2i b) {
+  if (!s2i_ok(a) || !s2i_ok(b)) return s2i_unknown();
+  const float p = a.lo * b.lo, q = a.lo * b.hi, r = a.hi * b.lo, s = a.hi * b.hi;
+  return s2i_fin(s2i_min4(p, q, r, s), s2i_max4(p, q, r, s));
+}
+// x * x of one value (both factors equal at every point): never negative.
+S2I_FN s2i s2i_sq(s2i a) {
+  if (!s2i_ok(a)) return s2i_unknown();
+  const float l = a.lo * a.lo, h = a.hi * a.hi;
+  if (a.lo >= 0.0f) return s2i_fin(l, h);
+  if (a.hi <= 0.0f) return s2i_fin(h, l);
+  return s2i_fin(0.0f, fmaxf(l, h));
+}
+S2I_FN s2i s2i_div(s2i a, s2i b) {
+  if (!s2i_ok(a) || !s2i_ok(b) || !(b.lo > 0.0f || b.hi < 0.0f)) return s2i_unknown();
+  const float p = a.lo / b.lo, q = a.lo / b.hi, r = a.hi / b.lo, s = a.hi / b.hi;
+  return s2i_fin(s2i_min4(p, q, r, s), s2i_max4(p, q, r, s));
+}
+S2I_FN s2i s2i_abs(s2i a) {
+  if (!s2i_ok(a)) return s2i_unknown();
+  if (a.lo >= 0.0f) return a;
+  if (a.hi <= 0.0f) return s2i_fin(-a.hi, -a.lo);
+  return s2i_fin(0.0f, fmaxf(-a.lo, a.hi));
+}
+S2HD s2i s2i_floor(s2i a) { return s2i_ok(a) ? s2i_fin(floorf(a.lo), floorf(a.hi)) : s2i_unknown(); }
+S2HD s2i s2i_ceil(s2i a) { return s2i_ok(a) ? s2i_fin(ceilf(a.lo), ceilf(a.hi)) : s2i_unknown(); }
+S2I_FN s2i s2i_sqrt(s2i a) {
+  return s2i_ok(a) && a.lo >= 0.0f ? s2i_fin(sqrtf(a.lo), sqrtf(a.hi)) : s2i_unknown();
+}
+S2HD s2i s2i_min(s2i a, s2i b) {
+  return s2i_ok(a) && s2i_ok(b) ? s2i_fin(fminf(a.lo, b.lo), fminf(a.hi, b.hi)) : s2i_unknown();
+}
+S2HD s2i s2i_max(s2i a, s2i b) {
+  return s2i_ok(a) && s2i_ok(b) ? s2i_fin(fmaxf(a.lo, b.lo), fmaxf(a.hi, b.hi)) : s2i_unknown();
+}
+S2I_FN s2i s2i_clamp(s2i e, s2i lo, s2i hi) { return s2i_min(s2i_max(e, lo), hi); }
+S2I_FN s2i s2i_mix(s2i a, s2i b, s2i t) { return s2i_add(s2i_mul(a, s2i_sub(s2i_pt(1.0f), t)), s2i_mul(b, t)); }
+// sin / cos of a finite argument: within [-1, 1] (with a margin for the
+// implementation's rounding).  atan2: within [-pi, pi], likewise.
+S2HD s2i s2i_unit(s2i a) { return s2i_ok(a) ? s2i_fin(-1.0009765625f, 1.0009765625f) : s2i_unknown(); }
+S2HD s2i s2i_angle(s2i a, s2i b) {
+  return s2i_ok(a) && s2i_ok(b) ? s2i_fin(-3.1416015625f, 3.1416015625f) : s2i_unknown();
+}
+
+// Combinators.  *d = 1 when the result is operand a (for the smooth
+// subtraction: -a) bit for bit at every point, 2 when it is operand b, 0
+// otherwise; the interval returned bounds the result.
+//   min / max: strictly separated operands.
+//   smooth operators: the blend weight h clamps to exactly 1 (or +0) at every
+//   point, k > 0, and no operand can be a zero whose sign the blend
+//   arithmetic would change (mix adds b * (+0) or a * (+0), and the k term
+//   adds or subtracts +0).
+S2I_FN s2i s2i_min_sel(s2i a, s2i b, int *d) {
+  if (d) *d = 0;
+  if (!s2i_ok(a) || !s2i_ok(b)) return s2i_unknown();
+  if (a.hi < b.lo) { if (d) *d = 1; return a; }
+  if (b.hi < a.lo) { if (d) *d = 2; return b; }
+  return s2i_min(a, b);
+}
+S2I_FN s2i s2i_max_sel(s2i a, s2i b, int *d) {
+  if (d) *d = 0;
+  if (!s2i_ok(a) || !s2i_ok(b)) return s2i_unknown();
+  if (a.lo > b.hi) { if (d) *d = 1; return a; }
+  if (b.lo > a.hi) { if (d) *d = 2; return b; }
+  return s2i_max(a, b);
+}
+S2HD bool s2i_nonzero(s2i a) { return a.lo > 0.0f || a.hi < 0.0f; }
+// Smooth operators keeping both operands.  For any blend weight h in [0, 1],
+// r(h) = b (1 - h) + a h -/+ k h (1 - h) lies in [min(a, b) - k/4, max(a, b)]
+// (union; intersection mirrored), and r is quadratic in h with its extremum
+// at the unclamped weight h* = 0.5 +/- (b - a) / 2k, where it equals the
+// smooth min (max) <= min(a, b) (>= max(a, b)).  The computed h is within a
+// few ulps of clamp(h*), which moves r by k (h - h*)^2, and the binary32
+// evaluation adds at most a few ulps of |a| + |b| + k; `slack` covers both
+// with a wide margin.
+S2HD float s2i_mag(s2i a) { return fmaxf(fabsf(a.lo), fabsf(a.hi)); }
+S2HD float s2i_slack(s2i a, s2i b, s2i k) { return (s2i_mag(a) + s2i_mag(b) + k.hi) * 0x1p-20f; }
+S2HD s2i s2i_smooth_min_bound(s2i a, s2i b, s2i k) {
+  const float e = s2i_slack(a, b, k);
+  return s2i_fin(fminf(a.lo, b.lo) - 0.25f * k.hi - e, fminf(a.hi, b.hi) + e);
+}
+S2HD s2i s2i_smooth_max_bound(s2i a, s2i b, s2i k) {
+  const float e = s2i_slack(a, b, k);
+  return s2i_fin(fmaxf(a.lo, b.lo) - e, fmaxf(a.hi, b.hi) + 0.25f * k.hi + e);
+}
+S2I_FN s2i s2i_smooth_union_sel(s2i a, s2i b, s2i k, int *d) {
+  if (d) *d = 0;
+  const s2i t = s2i_add(s2i_pt(0.5f), s2i_div(s2i_mul(s2i_pt(0.5f), s2i_sub(b, a)), k));
+  if (s2i_ok(t) && k.lo > 0.0f) {
+    // h = 1: (b * (+0) + a) - (+0)        h = +0: (b + a * (+0)) - (+0)
+    if (t.lo >= 1.0f && (s2i_nonzero(a) || b.hi < 0.0f)) { if (d) *d = 1; return a; }
+    if (t.hi < 0.0f && (s2i_nonzero(b) || a.hi < 0.0f)) { if (d) *d = 2; return b; }
+  }
+  if (!s2i_ok(a) || !s2i_ok(b) || !s2i_ok(k) || !(k.lo > 0.0f)) return s2i_unknown();
+  return s2i_smooth_min_bound(a, b, k);
+}
+S2I_FN s2i s2i_smooth_intersection_sel(s2i a, s2i b, s2i k, int *d) {
+  if (d) *d = 0;
+  const s2i t = s2i_sub(s2i_pt(0.5f), s2i_div(s2i_mul(s2i_pt(0.5f), s2i_sub(b, a)), k));
+  if (s2i_ok(t) && k.lo > 0.0f) {
+    // h = 1: (b * (+0) + a) + (+0)        h = +0: (b + a * (+0)) + (+0)
+    if (t.lo >= 1.0f && s2i_nonzero(a)) { if (d) *d = 1; return a; }
+    if (t.hi < 0.0f && s2i_nonzero(b)) { if (d) *d = 2; return b; }
+  }
+  if (!s2i_ok(a) || !s2i_ok(b) || !s2i_ok(k) || !(k.lo > 0.0f)) return s2i_unknown();
+  return s2i_smooth_max_bound(a, b, k);
+}
+S2I_FN s2i s2i_smooth_subtraction_sel(s2i a, s2i b, s2i k, int *d) {
+  if (d) *d = 0;
+  const s2i t = s2i_sub(s2i_pt(0.5f), s2i_div(s2i_mul(s2i_pt(0.5f), s2i_add(b, a)), k));
+  if (s2i_ok(t) && k.lo > 0.0f) {
+    // h = 1: (b * (+0) + (-a)) + (+0)     h = +0: (b + (-a) * (+0)) + (+0)
+    if (t.lo >= 1.0f && s2i_nonzero(a)) { if (d) *d = 1; return s2i_neg(a); }
+    if (t.hi < 0.0f && s2i_nonzero(b)) { if (d) *d = 2; return b; }
+  }
+  if (!s2i_ok(a) || !s2i_ok(b) || !s2i_ok(k) || !(k.lo > 0.0f)) return s2i_unknown();
+  return s2i_smooth_max_bound(s2i_neg(a), b, k);
+}
 #undef S2_VEC1
 #undef S2_VEC2
 #undef S2_VEC3

@@ -36,7 +36,23 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
                 '    for (int w = 0; w < 4; ++w) z.v[w] = (float)xyz[3*(4*i+w)+2];\n'
                 '    s2m_user_sdf_run4((float)xyz[3*4*i], (float)xyz[3*4*i+1], z, f);\n'
                 '    for (int w = 0; w < 4; ++w) out[4*i+w] = f.v[w]; }\n  return 1;\n}\n'
-                '#else\nextern "C" int eval_run4(long, const double*, double*) { return 0; }\n#endif\n')
+                '#else\nextern "C" int eval_run4(long, const double*, double*) { return 0; }\n#endif\n'
+                '#ifdef S2M_HAS_PRUNE\n'
+                'extern "C" int prune_tiles(long ntiles, const float* box, int npts, const float* pts, unsigned* bits,\n'
+                '                           float* ops, float* full, float* pruned) {\n'
+                '  for (long t = 0; t < ntiles; ++t) {\n'
+                '    s2i X, Y, Z; X.lo = box[6*t]; X.hi = box[6*t+1]; Y.lo = box[6*t+2]; Y.hi = box[6*t+3];\n'
+                '    Z.lo = box[6*t+4]; Z.hi = box[6*t+5];\n'
+                '    unsigned m[S2M_PRUNE_WORDS]; float fp, sfu;\n'
+                '    s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);\n'
+                '    for (int w = 0; w < S2M_PRUNE_WORDS; ++w) bits[t * S2M_PRUNE_WORDS + w] = m[w];\n'
+                '    ops[2*t] = fp; ops[2*t+1] = sfu;\n'
+                '    for (int p = 0; p < npts; ++p) { const float* q = pts + 3 * (t * npts + p);\n'
+                '      full[t * npts + p] = s2m_user_sdf(q[0], q[1], q[2]);\n'
+                '      pruned[t * npts + p] = s2m_user_sdf_pruned(q[0], q[1], q[2], m); }\n'
+                '  }\n  return S2M_PRUNE_WORDS;\n}\n'
+                '#else\nextern "C" int prune_tiles(long, const float*, int, const float*, unsigned*, float*, float*,\n'
+                '                           float*) { return 0; }\n#endif\n')
     so = os.path.join(d, "sdf.so")
     subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
                     src, "-o", so], check=True, capture_output=True)
@@ -44,6 +60,7 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
     L.eval_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
     L.normal_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
     L.eval_run4.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
+    L.prune_tiles.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 5
     _cache[key] = L
     return L
 
@@ -64,3 +81,44 @@ def eval_run4_host(cuda_src: str, xyz: np.ndarray):
     if not L.eval_run4(pts.shape[0], pts.ctypes.data, out.ctypes.data):
         return None
     return out
+
+
+def lattice_tiles(N: int, bounds: float, tiles=None, T: int = 8):
+    """Tiles of T^3 lattice points (clipped at the lattice edge) of an N-cell
+    job: their coordinate boxes (6 floats) and their points (padded to T^3
+    by repeating), computed in binary32 as the kernels do: bmin + size * i
+    with size = (B/2 - (-B/2)) / (N - 1), the reference's cell size."""
+    P = N + 1
+    half = np.float32(np.float32(bounds) * np.float32(0.5))
+    bmin = np.float32(np.float32(0.0) - half)
+    ext = np.float32(np.float32(0.0) + half) - bmin
+    size = np.float32(ext / np.float32(N - 1))
+    def coord(i):
+        return (bmin + size * np.asarray(i, np.float32)).astype(np.float32)
+    if tiles is None:
+        nt = (P + T - 1) // T
+        tiles = [(a, b, c) for a in range(nt) for b in range(nt) for c in range(nt)]
+    boxes, pts = [], []
+    for (a, b, c) in tiles:
+        ii = np.arange(a * T, min(a * T + T, P)); jj = np.arange(b * T, min(b * T + T, P))
+        kk = np.arange(c * T, min(c * T + T, P))
+        g = np.stack(np.meshgrid(coord(ii), coord(jj), coord(kk), indexing="ij"), -1).reshape(-1, 3)
+        boxes.append([coord(ii[0]), coord(ii[-1]), coord(jj[0]), coord(jj[-1]), coord(kk[0]), coord(kk[-1])])
+        pts.append(np.resize(g, (T ** 3, 3)))
+    return np.array(boxes, np.float32), np.array(pts, np.float32)
+
+
+def prune_host(cuda_src: str, boxes: np.ndarray, pts: np.ndarray):
+    """Run the tile function and the pruned point function on the host:
+    (words per tile or 0, ops per tile [fp, sfu], full values, pruned values)."""
+    L = compile_host(cuda_src)
+    nt, npts = len(boxes), pts.shape[1]
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    pts = np.ascontiguousarray(pts, np.float32)
+    bits = np.zeros((nt, 64), np.uint32)
+    ops = np.zeros((nt, 2), np.float32)
+    full = np.zeros((nt, npts), np.float32)
+    pruned = np.zeros((nt, npts), np.float32)
+    w = L.prune_tiles(nt, boxes.ctypes.data, npts, pts.ctypes.data, bits.ctypes.data, ops.ctypes.data,
+                      full.ctypes.data, pruned.ctypes.data)
+    return w, ops, full, pruned

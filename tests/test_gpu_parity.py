@@ -208,14 +208,20 @@ def test_custom_normal_function(lib, oracle_lib):
     assert (np.sum(gpu.normals * radial, axis=1) > 0.999).all()
 
 
-@pytest.mark.parametrize("variant", range(5))
-def test_eval_variants_identical(lib, variant, monkeypatch):
-    """Every evaluation-kernel variant the autotuner may pick gives the same bits."""
+@pytest.fixture(scope="module")
+def csg64_seed1(lib):
     src, prm = workloads.csg64(seed=1)
-    monkeypatch.setenv("S2M_EVAL_VARIANT", str(variant))
-    sdf = s2m.Sdf3DShader.from_source(src).compile()
+    return s2m.Sdf3DShader.from_source(src).compile(), prm
+
+
+@pytest.mark.parametrize("variant", range(s2m.EVAL_VARIANTS))
+def test_eval_variants_identical(csg64_seed1, variant):
+    """Every evaluation-kernel variant the autotuner may pick (5 and 6: tile
+    pruned) gives the same bits."""
+    sdf, prm = csg64_seed1
+    sdf.set_eval_variant(variant)
     gpu = run(sdf, 96)
-    assert sdf.eval_variant()[0] != "untuned"
+    assert sdf.eval_variant()[0] == sdf.eval_variants()[variant][0]
     assert_bit_exact(gpu, oracle.mesh(oracle.CSG, prm, 96, 2.0), f"variant {variant}")
 
 
@@ -225,7 +231,7 @@ def test_autotuner_picks_a_variant(lib):
     assert sdf.eval_variant()[0] == "untuned"
     run(sdf, 512)  # large enough for the tuner to time (>= 2e6 points per trial)
     name, ns = sdf.eval_variant()
-    assert name.startswith("s2m_eval_") and all(x > 0 for x in ns)
+    assert name.startswith("s2m_eval") and all(x > 0 for x in ns)
 
 
 # ---------------------------------------------------------------------------

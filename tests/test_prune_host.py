@@ -1,0 +1,126 @@
+"""Tile pruning on the CPU: the frontend's generated tile function and pruned
+point function, compiled for the host, against the full per-point function.
+For every tile, each pruned value must be bit-identical to the full value:
+the proof obligations of each pruning decision (interval bounds under
+round-to-nearest, operand separation, signed zeros) are checked here on
+lattice tiles of real jobs, including the tiles clipped at the lattice edge."""
+import numpy as np
+import pytest
+
+import sdf2mesh_gb300 as s2m
+from sdf2mesh_gb300 import workloads
+
+from hostsdf import lattice_tiles, prune_host
+
+
+def lowered(src, lang=s2m.LANG_WGSL, name="sdf"):
+    if lang == s2m.LANG_WGSL:
+        src = s2m.Sdf3DShader.from_source(src).source
+    return s2m.translate(src, lang, name)
+
+
+def check(cu, N, bounds=2.0, tiles=None, seed=0, count=None):
+    if count is not None:
+        rng = np.random.default_rng(seed)
+        nt = (N + 1 + 7) // 8
+        tiles = [tuple(int(v) for v in rng.integers(0, nt, 3)) for _ in range(count)]
+    boxes, pts = lattice_tiles(N, bounds, tiles)
+    w, ops, full, pruned = prune_host(cu, boxes, pts)
+    assert w > 0, "no pruning form"
+    bad = full.view(np.uint32) != pruned.view(np.uint32)
+    assert not bad.any(), f"{int(bad.sum())} pruned values differ, e.g. tile {np.argwhere(bad)[0]}"
+    return ops
+
+
+def test_csg64_every_tile_n48(lib):
+    cu, fp, sfu = lowered(workloads.csg64()[0])
+    ops = check(cu, 48)
+    assert ops[:, 0].max() <= fp and ops[:, 1].max() <= sfu
+    assert ops[:, 0].mean() < 0.5 * fp  # most tiles skip most spheres
+
+
+@pytest.mark.parametrize("N", [256, 1024])
+def test_csg64_random_tiles(lib, N):
+    cu, fp, sfu = lowered(workloads.csg64()[0])
+    ops = check(cu, N, count=400, seed=N)
+    assert ops[:, 0].mean() < 0.1 * fp
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_trees(lib, seed):
+    cu, _, _ = lowered(workloads.random_tree(seed)[0])
+    if "S2M_HAS_PRUNE" not in cu:
+        pytest.skip("tree without a combinator worth pruning")
+    check(cu, 64, count=300, seed=seed)
+    check(cu, 256, count=300, seed=seed + 100)
+
+
+SMOOTH_OPS = """use sdf3d::primitives;
+use sdf::op;
+fn sdf3d(p: vec3f) -> f32 {
+    let a = sdf3d_sphere(p - vec3f(0.3, 0.0, 0.0), 0.4);
+    let b = sdf3d_box(p + vec3f(0.3, 0.1, 0.0), vec3f(0.5, 0.6, 0.4));
+    let c = sdf3d_torus(p - vec3f(0.0, 0.2, 0.1), vec2f(0.4, 0.1));
+    let u = sdf_op_smooth_union(a, b, 0.05);
+    let i = sdf_op_smooth_intersection(u, c - 0.2, 0.03);
+    return min(sdf_op_smooth_subtraction(sdf3d_sphere(p, 0.25), i, 0.04), max(c, -a));
+}
+"""
+
+
+@pytest.mark.parametrize("N", [33, 128])
+def test_smooth_operators_and_min_max(lib, N):
+    cu, _, _ = lowered(SMOOTH_OPS)
+    assert "S2M_HAS_PRUNE" in cu
+    check(cu, N, count=500, seed=N)
+
+
+# Operands that are exactly +-0 on whole planes of the lattice (p.x * 0.0,
+# coordinates that are 0.0 at the centre), blend widths that are zero or
+# negative, and a square root of a negative value (NaN): every decision must
+# either be proven or not taken.
+EDGE = """use sdf3d::primitives;
+use sdf::op;
+fn sdf3d(p: vec3f) -> f32 {
+    let s = sdf3d_sphere(p, 0.5);
+    let z0 = p.x * 0.0;
+    let a = sdf_op_smooth_union(z0, sdf3d_sphere(p - vec3f(0.9, 0.9, 0.9), 0.1), 0.05);
+    let b = sdf_op_smooth_union(s, sdf3d_box(p, vec3f(0.3, 0.3, 0.3)), 0.0);
+    let c = sdf_op_smooth_intersection(-z0, sdf3d_sphere(p + vec3f(0.8, 0.0, 0.0), 0.1), -0.1);
+    let d = min(sqrt(p.y), sdf3d_torus(p, vec2f(0.5, 0.2)));
+    let e = max(p.z, -sdf3d_sphere(p - vec3f(0.0, 0.0, 0.7), 0.2));
+    return min(min(a, b), min(min(c, d), e));
+}
+"""
+
+
+@pytest.mark.parametrize("N", [16, 64])
+def test_edge_cases(lib, N):
+    cu, _, _ = lowered(EDGE)
+    assert "S2M_HAS_PRUNE" in cu
+    check(cu, N)  # every tile
+
+
+def test_user_function_with_library_arithmetic_is_a_combinator(lib):
+    """A user function whose body is sdf::op's smooth union arithmetic is
+    recognised by its arithmetic, not its name."""
+    src = """use sdf3d::primitives;
+fn blend(a: f32, b: f32, k: f32) -> f32 {
+    let h = clamp(0.5 + 0.5 * (b - a) / k, 0.0, 1.0);
+    return mix(b, a, h) - k * h * (1.0 - h);
+}
+fn sdf3d(p: vec3f) -> f32 {
+    return blend(sdf3d_sphere(p - vec3f(0.5, 0.0, 0.0), 0.3), sdf3d_sphere(p + vec3f(0.5, 0.0, 0.0), 0.3), 0.1);
+}
+"""
+    cu, _, _ = lowered(src)
+    assert "s2_op_smooth_union(" in cu
+    check(cu, 64, count=200)
+
+
+def test_no_pruning_form_without_combinators_or_with_loops(lib):
+    cu, _, _ = lowered(workloads.torus()[0] if isinstance(workloads.torus(), tuple) else workloads.torus())
+    assert "S2M_HAS_PRUNE" not in cu
+    mb = workloads.mandelbulb()
+    cu, _, _ = lowered(mb[0] if isinstance(mb, tuple) else mb, s2m.LANG_GLSL, "sdf")
+    assert "S2M_HAS_PRUNE" not in cu
