@@ -139,14 +139,14 @@ int s2m_sdf_run_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops)
    job (-1: not tuned yet): its name, and the measured ns per lattice point
    of each of the S2M_EVAL_VARIANTS variants.  No reference counterpart (the
    reference has one fixed kernel, dualcontour.wgsl:161-162). */
-#define S2M_EVAL_VARIANTS 7
+#define S2M_EVAL_VARIANTS 8
 int s2m_sdf_eval_variant(const s2m_sdf *sdf, char *name, size_t namelen, double *ns_per_point);
 /* Use `variant` for this SDF's later jobs instead of tuning (S2M_E_INVALID
    when the module has no such variant, e.g. a pruned one without a pruning
    form). */
 int s2m_sdf_set_eval_variant(s2m_sdf *sdf, int variant);
 /* Name, registers per thread and local (spill) bytes per thread of one
-   variant, as the tuner recorded them (0 before tuning).  Variants 5 and 6
+   variant, as the tuner recorded them (0 before tuning).  Variants 5 to 7
    are the tile-pruned ones; their ns per point is 0 when the SDF has no
    pruning form. */
 int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_t namelen, int *registers,

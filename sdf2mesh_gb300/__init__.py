@@ -36,7 +36,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libsdf2mesh_gb300.so")
 LANG_WGSL, LANG_GLSL, LANG_SHADERTOY = 0, 1, 2
 COMPILE_FMAD = 0x1
 COMPILE_NO_PRUNE = 0x2
-EVAL_VARIANTS = 7
+EVAL_VARIANTS = 8
 JOB_POW2_ROUNDING, JOB_SLICE_LAG, JOB_EXACT_CORNERS, JOB_QEF = 0x1, 0x2, 0x4, 0x8
 
 S2M_OK = 0

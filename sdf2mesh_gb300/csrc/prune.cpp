@@ -104,7 +104,16 @@ class Pruner {
     std::ostringstream o;
     o << "// tile pruning: " << pc.combinators << " combinators, " << pc.words << " words of activity bits\n";
     o << "#define S2M_HAS_PRUNE 1\n#define S2M_PRUNE_WORDS " << pc.words << "\n";
+    var_.assign(size_t(n_), 0);
+    for (int v = 0; v < n_; ++v) {
+      const PNode &p = nd(v);
+      var_[size_t(v)] = p.op == POp::Z || (p.a >= 0 && var_[size_t(p.a)]) || (p.b >= 0 && var_[size_t(p.b)]) ||
+                        (p.c >= 0 && var_[size_t(p.c)]);
+    }
     emit_tile(o, pc.words);
+    run4_ = false;
+    emit_point(o);
+    run4_ = true;
     emit_point(o);
     pc.cuda = o.str();
     pc.ok = true;
@@ -120,6 +129,8 @@ class Pruner {
   std::vector<int> combs_;    // enabled combinator nodes, ascending
   std::vector<int> owner_;    // node -> segment
   std::vector<int> sparent_, sdepth_;
+  std::vector<char> var_;  // depends on z (one value per point of a run of 4)
+  bool run4_ = false;      // emitting the run-of-4 form
 
   static int seg(int ci, int side) { return 1 + 2 * ci + side; }
   const PNode &nd(int v) const { return ir_.nodes[size_t(v)]; }
@@ -216,8 +227,15 @@ class Pruner {
     }
   }
 
-  // Point expression of a node (combinators: their full arithmetic).
+  // Point expression of a node (combinators: their full arithmetic).  In the
+  // run-of-4 form a node that varies with z is an s2x4 and its builtins are
+  // the lane-wise s2r_ forms (the same operations per lane).
   std::string expr(int v) const {
+    std::string e = expr_scalar(v);
+    if (run4_ && var_[size_t(v)] && e.compare(0, 3, "s2_") == 0) e = "s2r_" + e.substr(3);
+    return e;
+  }
+  std::string expr_scalar(int v) const {
     const PNode &p = nd(v);
     const std::string A = p.a >= 0 ? val(p.a) : "", B = p.b >= 0 ? val(p.b) : "", C = p.c >= 0 ? val(p.c) : "";
     switch (p.op) {
@@ -363,7 +381,7 @@ class Pruner {
         close();
         const PNode &p = nd(v);
         const int sa = seg(ci, 0), sb = seg(ci, 1);
-        const std::string A = val(p.a), B = val(p.b);
+        const std::string A = as_var(p.a, var_[size_t(v)]), B = as_var(p.b, var_[size_t(v)]);
         const std::string keepA = p.op == POp::SmoothSubtraction ? "(-" + A + ")" : A;
         o << ind << "if " << bit_test(sb - 1) << " {\n";
         emit_region(o, sb, members, ind + "  ");
@@ -397,16 +415,25 @@ class Pruner {
     return members;
   }
 
+  // A value as an s2x4 where one is wanted (a uniform value is splat).
+  std::string as_var(int v, bool want) const {
+    return run4_ && want && !var_[size_t(v)] ? "s2x4_splat(" + val(v) + ")" : val(v);
+  }
+
   void emit_point(std::ostringstream &o) const {
     // Out of line on the device (S2M_PRUNED_FN): inlined into the lattice
     // kernel's point loop, the branchy body let the compiler keep far more
     // values live across iterations than the registers hold.
-    o << "S2M_PRUNED_FN float s2m_user_sdf_pruned(float x, float y, float z, const unsigned *m)\n{\n";
+    if (run4_)
+      o << "S2M_PRUNED_FN s2x4 s2m_user_sdf_pruned_run4(float x, float y, s2x4 z, const unsigned *m)\n{\n";
+    else
+      o << "S2M_PRUNED_FN float s2m_user_sdf_pruned(float x, float y, float z, const unsigned *m)\n{\n";
     o << "  (void)x; (void)y; (void)z;\n";
     for (int v = 0; v < n_; ++v)
-      if (live_[size_t(v)] && !is_leaf(nd(v).op)) o << "  float v" << v << ";\n";
+      if (live_[size_t(v)] && !is_leaf(nd(v).op))
+        o << (run4_ && var_[size_t(v)] ? "  s2x4 v" : "  float v") << v << ";\n";
     emit_region(o, 0, regions(), "  ");
-    o << "  return " << val(ir_.root) << ";\n}\n";
+    o << "  return " << (run4_ ? as_var(ir_.root, true) : val(ir_.root)) << ";\n}\n";
   }
 };
 

@@ -89,7 +89,7 @@ struct EvalVariant {
 constexpr EvalVariant kEvalVariants[] = {
     {"s2m_eval_b2r4", 4, false, false}, {"s2m_eval_b3r4", 4, false, false}, {"s2m_eval_b4r4", 4, false, false},
     {"s2m_eval_b2v4", 4, true, false},  {"s2m_eval_b3v4", 4, true, false},  {"s2m_evalp_b8", 1, false, true},
-    {"s2m_evalp_b16", 1, false, true}};
+    {"s2m_evalp_b16", 1, false, true},  {"s2m_evalp_b8v4", 4, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -128,8 +128,12 @@ struct s2m_mesh {
   unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
   unsigned short *cell_masks = nullptr;      // per thread of a cell tile: candidate bits of its cells
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
-  // tile pruning: [ops FP32, ops SFU] (2 u64) then activity words of a slab's tiles
+  // tile pruning: [ops FP32, ops SFU] (2 u64), the tile base of every slab
+  // (nslabs + 1 u64), then the activity words of `prune_chunk` slabs' tiles
   unsigned long long *prune_buf = nullptr;
+  std::vector<unsigned long long> slab_tile_base;  // host copy
+  int prune_chunk = 0;
+  size_t prune_bits_off = 0;  // bytes from prune_buf to the activity words
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -355,8 +359,17 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   return S2M_OK;
 }
 
+// Planes k0 .. k0 + nk - 1 that slab s evaluates.
+void slab_planes(const s2m_mesh *m, int s, int &k0, int &nk) {
+  const int zc0 = s * m->D;
+  const int zc1 = std::min(m->nzc, zc0 + m->D);
+  k0 = s == 0 ? 0 : zc0 + 1;
+  nk = zc1 - k0 + 1;
+}
+
 // Tiles of slab planes k0 .. k0 + nk - 1 for the pruned variants: tzs planes
-// per tile (at most S2_PT_ZMAX, balanced), nzt tiles in z, none empty.
+// per tile (at most S2_PT_ZMAX, balanced), nzt tiles in z, none empty (the
+// device computes the same in s2_tile_depth).
 struct PruneGeom {
   int tzs = 0, nzt = 0;
   long long ntiles = 0;
@@ -370,11 +383,58 @@ PruneGeom prune_geom(const S2Job &j, int nk) {
   g.ntiles = ntx * ntx * g.nzt;
   return g;
 }
-// Two operation counters, then the activity words of the largest slab
-// (nk <= D + 1 planes; the tile count grows with nk).
-size_t prune_buf_bytes(const s2m_mesh *m) {
-  const PruneGeom g = prune_geom(m->job, m->D + 1);
-  return 16 + size_t(g.ntiles) * size_t(m->sdf->prune_words) * 4;
+
+// The tile pass runs over chunks of prune_chunk slabs, one launch each; the
+// activity words of a chunk stay within kPruneBitsBudget (all slabs of the
+// job at once up to well beyond 1024^3).
+constexpr size_t kPruneBitsBudget = size_t(256) << 20;
+size_t prune_layout(s2m_mesh *m) {
+  const int ns = m->nslabs;
+  m->slab_tile_base.assign(size_t(ns) + 1, 0ull);
+  unsigned long long max_slab = 1;
+  for (int s = 0; s < ns; ++s) {
+    int k0, nk;
+    slab_planes(m, s, k0, nk);
+    const unsigned long long t = (unsigned long long)prune_geom(m->job, nk).ntiles;
+    m->slab_tile_base[size_t(s) + 1] = m->slab_tile_base[size_t(s)] + t;
+    max_slab = std::max(max_slab, t);
+  }
+  const size_t words = size_t(m->sdf->prune_words);
+  m->prune_chunk = int(std::max<size_t>(1, std::min<size_t>(size_t(std::max(ns, 1)),
+                                                            kPruneBitsBudget / (max_slab * words * 4))));
+  unsigned long long chunk_tiles = 0;
+  for (int s = 0; s < ns; s += m->prune_chunk) {
+    const int e = std::min(ns, s + m->prune_chunk);
+    chunk_tiles = std::max(chunk_tiles, m->slab_tile_base[size_t(e)] - m->slab_tile_base[size_t(s)]);
+  }
+  m->prune_bits_off = (16 + 8 * (size_t(ns) + 1) + 15) / 16 * 16;
+  return m->prune_bits_off + size_t(chunk_tiles) * words * 4;
+}
+
+// Tile pass over slabs [s_begin, s_end) and the pruned evaluation of slab s.
+cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t st) {
+  S2Job jj = m->job;
+  unsigned *bits = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(m->prune_buf) + m->prune_bits_off);
+  unsigned long long *ops = m->prune_buf;
+  const unsigned long long *base = m->prune_buf + 2;
+  int D = m->D, nzc = m->nzc;
+  const unsigned long long n = m->slab_tile_base[size_t(s_end)] - m->slab_tile_base[size_t(s_begin)];
+  void *targs[] = {&jj, &bits, &ops, &base, &s_begin, &s_end, &D, &nzc};
+  return cudaLaunchKernel((const void *)m->sdf->k_tiles, dim3(unsigned((n + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
+                          dim3(S2_PT_BLOCK), targs, 0, st);
+}
+cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaStream_t st) {
+  S2Job jj = m->job;
+  float *ring = m->ring;
+  int k0, nk;
+  slab_planes(m, s, k0, nk);
+  PruneGeom g = prune_geom(m->job, nk);
+  const unsigned *bits =
+      reinterpret_cast<const unsigned *>(reinterpret_cast<const char *>(m->prune_buf) + m->prune_bits_off) +
+      (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
+  void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
+  return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
+                          0, st);
 }
 
 void drop_graph(s2m_mesh *m) {
@@ -403,7 +463,12 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cell_masks, m->cell_tiles * S2_CELL_BLOCK * 2, st));
   S2_CUDA(cudaMallocAsync(&m->tile_cnt, m->cell_tiles * 4, st));
-  if (m->sdf->k_tiles) S2_CUDA(cudaMallocAsync(&m->prune_buf, prune_buf_bytes(m), st));
+  if (m->sdf->k_tiles && m->nslabs > 0) {
+    S2_CUDA(cudaMallocAsync(&m->prune_buf, prune_layout(m), st));
+    // pageable source: the call returns once the words are staged
+    S2_CUDA(cudaMemcpyAsync(m->prune_buf + 2, m->slab_tile_base.data(), m->slab_tile_base.size() * 8,
+                            cudaMemcpyHostToDevice, st));
+  }
   S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cand_val, m->cand_cap * 32, st));
   S2_CUDA(cudaMallocAsync(&m->cand_pos, m->cand_cap * 12, st));
@@ -546,16 +611,9 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     float *ring = m->ring;
     m->eval_points += double(pts) * nk;
     if (pruned) {
-      PruneGeom g = prune_geom(j, nk);
-      unsigned long long *ops = m->prune_buf;
-      unsigned *bits = reinterpret_cast<unsigned *>(m->prune_buf + 2);
-      void *targs[] = {&jj, &bits, &ops, &k0, &nk, &g.tzs, &g.nzt};
-      S2_LAUNCH(0, 0, cudaLaunchKernel((const void *)m->sdf->k_tiles, dim3(unsigned((g.ntiles + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
-                                       dim3(S2_PT_BLOCK), targs, 0, st));
-      void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
-      S2_LAUNCH(0, double(pts) * nk,
-                cudaLaunchKernel((const void *)m->sdf->k_eval[ev], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK),
-                                 pargs, 0, st));
+      const int cb = s - s % m->prune_chunk;
+      if (s == cb) S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
+      S2_LAUNCH(0, double(pts) * nk, launch_evalp(m, ev, s, cb, st));
     } else {
       void *eargs[] = {&jj, &ring, &k0, &nk};
       dim3 eg(eval_blocks, unsigned((nk + run - 1) / run));
@@ -587,10 +645,12 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   return cudaSuccess;
 }
 
-// Autotuner: time every evaluation variant of the module on up to 16 planes
-// through the middle of the job (into the job's own ring, which the pipeline
-// overwrites afterwards) and keep the fastest for this SDF.  A pruned variant
-// is timed with its tile pass.  Runs once per SDF, on its first job.
+// Autotuner: time every evaluation variant of the module on the slabs at a
+// quarter, a half and three quarters of the job (into the job's own ring,
+// which the pipeline overwrites afterwards) and keep the fastest for this
+// SDF.  A pruned variant is timed with its tile pass.  Runs once per SDF, on
+// its first job.  (One window through the middle of a CSG scene is where
+// pruning saves least; quartiles are closer to the whole job.)
 int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   const s2m_sdf *sdf = m->sdf;
   std::lock_guard<std::mutex> lock(sdf->tune_mu);
@@ -604,14 +664,23 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   }
   const S2Job &j = m->job;
   const long long pts = (long long)j.P * j.P;
-  int nk = std::min(j.ring, 16);
+  std::vector<int> trial;
+  for (int q = 1; q <= 3 && m->nslabs > 0; ++q) {
+    const int s = std::min(m->nslabs - 1, m->nslabs * q / 4);
+    if (trial.empty() || trial.back() != s) trial.push_back(s);
+  }
+  double trial_pts = 0;
+  for (int s : trial) {
+    int k0, nk;
+    slab_planes(m, s, k0, nk);
+    trial_pts += double(pts) * nk;
+  }
   // small jobs: too little work per launch to rank the variants; keep the default
-  if (double(pts) * nk < 2.0e6) {
+  if (trial_pts < 6.0e6) {
     sdf->eval_variant = 0;
     sdf->eval_variant_plain = 0;
     return S2M_OK;
   }
-  int k0 = std::max(0, std::min(j.P - nk, j.P / 2 - nk / 2));
   cudaEvent_t a, b;
   S2_CUDA(cudaEventCreate(&a));
   S2_CUDA(cudaEventCreate(&b));
@@ -625,23 +694,20 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
     }
     float ms_best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
-      S2Job jj = j;
-      float *ring = m->ring;
       S2_CUDA(cudaEventRecord(a, st));
-      if (kEvalVariants[v].pruned) {
-        PruneGeom g = prune_geom(j, nk);
-        unsigned long long *ops = m->prune_buf;
-        unsigned *bits = reinterpret_cast<unsigned *>(m->prune_buf + 2);
-        void *targs[] = {&jj, &bits, &ops, &k0, &nk, &g.tzs, &g.nzt};
-        S2_CUDA(cudaLaunchKernel((const void *)sdf->k_tiles, dim3(unsigned((g.ntiles + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
-                                 dim3(S2_PT_BLOCK), targs, 0, st));
-        void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
-        S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK),
-                                 pargs, 0, st));
-      } else {
-        void *args[] = {&jj, &ring, &k0, &nk};
-        dim3 eg(eval_blocks, unsigned((nk + kEvalVariants[v].run - 1) / kEvalVariants[v].run));
-        S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], eg, dim3(S2_EVAL_BLOCK), args, 0, st));
+      for (int s : trial) {
+        if (kEvalVariants[v].pruned) {
+          S2_CUDA(launch_tiles(m, s, s + 1, st));
+          S2_CUDA(launch_evalp(m, v, s, s, st));
+        } else {
+          S2Job jj = j;
+          float *ring = m->ring;
+          int k0, nk;
+          slab_planes(m, s, k0, nk);
+          void *args[] = {&jj, &ring, &k0, &nk};
+          dim3 eg(eval_blocks, unsigned((nk + kEvalVariants[v].run - 1) / kEvalVariants[v].run));
+          S2_CUDA(cudaLaunchKernel((const void *)sdf->k_eval[v], eg, dim3(S2_EVAL_BLOCK), args, 0, st));
+        }
       }
       S2_CUDA(cudaEventRecord(b, st));
       S2_CUDA(cudaEventSynchronize(b));
@@ -649,7 +715,7 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
       S2_CUDA(cudaEventElapsedTime(&ms, a, b));
       if (rep > 0) ms_best = std::min(ms_best, ms);
     }
-    double ns = double(ms_best) * 1e6 / (double(pts) * nk);
+    double ns = double(ms_best) * 1e6 / trial_pts;
     sdf->tune_ns[v] = ns;
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, (const void *)sdf->k_eval[v]) == cudaSuccess) {

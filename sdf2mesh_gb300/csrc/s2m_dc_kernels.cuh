@@ -106,9 +106,23 @@ S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
 #endif
 
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
-// Tile pruning (the generated s2m_user_sdf_tile / s2m_user_sdf_pruned*).
-// A slab's planes k0 .. k0 + nk - 1 are cut into tiles of 8 x 8 points by
-// `tzs` planes (nzt tiles in z); tile t = (tz * nty + ty) * ntx + tx.
+// Tile pruning (the generated s2m_user_sdf_tile / s2m_user_sdf_pruned).
+// Slab s evaluates planes k0 .. k0 + nk - 1 (k0 = 0 for the first slab, else
+// s * D + 1; the last plane is min(nzc, (s + 1) * D)).  Its planes are cut
+// into tiles of 8 x 8 points by `tzs` planes (at most S2_PT_ZMAX, balanced),
+// nzt tiles in z; tile t = (tz * nty + ty) * ntx + tx.  slab_base[s] is the
+// index of slab s's first tile among all tiles of the job.
+
+__device__ __forceinline__ void s2_slab_planes(int s, int D, int nzc, int &k0, int &nk) {
+  const int zc0 = s * D;
+  const int zc1 = min(nzc, zc0 + D);
+  k0 = s == 0 ? 0 : zc0 + 1;
+  nk = zc1 - k0 + 1;
+}
+__device__ __forceinline__ int s2_tile_depth(int nk) {
+  const int parts = (nk + S2_PT_ZMAX - 1) / S2_PT_ZMAX;
+  return (nk + parts - 1) / parts;
+}
 
 struct S2PruneTile {
   int i0, i1, j0, j1, kb, ke;  // inclusive point ranges
@@ -129,18 +143,27 @@ __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long
   return r;
 }
 
-// One thread per tile: interval evaluation over the tile's coordinate box,
-// activity bits, and the SDF operations that remain (summed into ops[0] FP32,
-// ops[1] SFU, per lattice point evaluated).
+// The tile pass of slabs s_begin .. s_end - 1 in one launch, one thread per
+// tile: interval evaluation over the tile's coordinate box, activity bits
+// (tile g of the job at bits[(g - slab_base[s_begin]) * W]), and the SDF
+// operations that remain (summed into ops[0] FP32, ops[1] SFU, per lattice
+// point).  One launch covers many slabs so that the grid fills the GPU.
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK)
-s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops, int k0, int nk, int tzs,
-          int nzt) {
-  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const long long ntiles = (long long)ntx * ntx * nzt;
-  const long long t = (long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
+s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops,
+          const unsigned long long *__restrict__ slab_base, int s_begin, int s_end, int D, int nzc) {
+  const unsigned long long b0 = slab_base[s_begin], b1 = slab_base[s_end];
+  const unsigned long long g = b0 + (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
   unsigned long long fp_ops = 0, sfu_ops = 0;
-  const S2PruneTile tl = s2_prune_tile(job, t < ntiles ? t : 0, k0, nk, tzs);
-  if (t < ntiles && tl.kb <= tl.ke) {
+  if (g < b1) {
+    int lo = s_begin, hi = s_end - 1;  // the slab of tile g: largest s with slab_base[s] <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (slab_base[mid] <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    int k0, nk;
+    s2_slab_planes(lo, D, nzc, k0, nk);
+    const S2PruneTile tl = s2_prune_tile(job, (long long)(g - slab_base[lo]), k0, nk, s2_tile_depth(nk));
     s2i X, Y, Z;
     X.lo = s2_coord(job, tl.i0); X.hi = s2_coord(job, tl.i1);
     Y.lo = s2_coord(job, tl.j0); Y.hi = s2_coord(job, tl.j1);
@@ -148,10 +171,11 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
     unsigned m[S2M_PRUNE_WORDS];
     float fp = 0.0f, sfu = 0.0f;
     s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);
+    unsigned *dst = bits + (g - b0) * S2M_PRUNE_WORDS;
 #pragma unroll
-    for (int w = 0; w < S2M_PRUNE_WORDS; ++w) bits[t * S2M_PRUNE_WORDS + w] = m[w];
-    const unsigned long long npts =
-        (unsigned long long)(tl.i1 - tl.i0 + 1) * (unsigned long long)(tl.j1 - tl.j0 + 1) * (unsigned long long)(tl.ke - tl.kb + 1);
+    for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
+    const unsigned long long npts = (unsigned long long)(tl.i1 - tl.i0 + 1) * (unsigned long long)(tl.j1 - tl.j0 + 1) *
+                                    (unsigned long long)max(0, tl.ke - tl.kb + 1);
     fp_ops = (unsigned long long)fp * npts;
     sfu_ops = (unsigned long long)sfu * npts;
   }
@@ -167,10 +191,13 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
 }
 
 // Pruned lattice evaluation: one tile per warp, the lanes striding over the
-// tile's points.  The activity bits (in shared memory) are the same for the
-// whole warp, so the pruned function's branches never diverge.  Points past
-// the lattice edge (tiles are 8 x 8) evaluate a clamped point and store
-// nothing.
+// tile's points (RUN4: over runs of 4 planes sharing x and y, which share
+// the bit tests and the x/y-only arithmetic; a run past the tile's last
+// plane repeats that plane and stores only its own planes).  The activity
+// bits (in shared memory) are the same for the whole warp, so the pruned
+// function's branches never diverge.  Points past the lattice edge (tiles
+// are 8 x 8) evaluate a clamped point and store nothing.
+template <bool RUN4>
 __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restrict__ ring,
                                                const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) {
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
@@ -184,7 +211,28 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   if (lane < S2M_PRUNE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
   __syncwarp();
   const unsigned *m = s_bits[threadIdx.x >> 5];
-  const int npts = S2_PT_XY * S2_PT_XY * (tl.ke - tl.kb + 1);
+  const int nz = tl.ke - tl.kb + 1;
+  if (RUN4) {
+    const int nruns = S2_PT_XY * S2_PT_XY * ((nz + 3) >> 2);
+#pragma unroll 1
+    for (int q = lane; q < nruns; q += 32) {
+      const int i = tl.i0 + (q & (S2_PT_XY - 1));
+      const int j = tl.j0 + ((q >> 3) & (S2_PT_XY - 1));
+      const int k = tl.kb + 4 * (q >> 6);
+      s2x4 z;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) z.v[w] = s2_coord(job, min(k + w, tl.ke));
+      const s2x4 f = s2m_user_sdf_pruned_run4(s2_coord(job, min(i, tl.i1)), s2_coord(job, min(j, tl.j1)), z, m);
+      if (i <= tl.i1 && j <= tl.j1) {
+        float *col = ring + (long long)j * job.pitch + i;
+#pragma unroll
+        for (int w = 0; w < 4; ++w)
+          if (k + w <= tl.ke) col[(long long)((k + w) % job.ring) * job.plane] = f.v[w];
+      }
+    }
+    return;
+  }
+  const int npts = S2_PT_XY * S2_PT_XY * nz;
 #pragma unroll 1
   for (int q = lane; q < npts; q += 32) {
     const int i = tl.i0 + (q & (S2_PT_XY - 1));
@@ -195,14 +243,15 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   }
 }
 
-#define S2_EVALP_VARIANT(NAME, MINB)                                                              \
+#define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
   NAME(S2Job job, float *__restrict__ ring, const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) { \
-    s2_eval_pruned(job, ring, bits, k0, nk, tzs, nzt);                                            \
+    s2_eval_pruned<RUN4>(job, ring, bits, k0, nk, tzs, nzt);                                      \
   }
 // Keep this table in step with kEvalVariants in runtime.cu.
-S2_EVALP_VARIANT(s2m_evalp_b8, 8)
-S2_EVALP_VARIANT(s2m_evalp_b16, 16)
+S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
+S2_EVALP_VARIANT(s2m_evalp_b16, 16, false)
+S2_EVALP_VARIANT(s2m_evalp_b8v4, 8, true)
 #endif
 
 

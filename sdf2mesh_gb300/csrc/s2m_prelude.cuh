@@ -503,7 +503,8 @@ S2HD s2x4 operator-(const s2x4 &a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] 
 S2_X4_F1(abs) S2_X4_F1(floor) S2_X4_F1(ceil) S2_X4_F1(sqrt) S2_X4_F1(saturate) S2_X4_F1(sin) S2_X4_F1(cos)
 S2_X4_F1(exp) S2_X4_F1(log)
 S2_X4_F2(min) S2_X4_F2(max) S2_X4_F2(pow) S2_X4_F2(atan2)
-S2_X4_F3(clamp) S2_X4_F3(mix)
+S2_X4_F3(clamp) S2_X4_F3(mix) S2_X4_F3(op_smooth_union) S2_X4_F3(op_smooth_intersection)
+S2_X4_F3(op_smooth_subtraction)
 #undef S2_X4_F1
 #undef S2_X4_F2
 #undef S2_X4_F3

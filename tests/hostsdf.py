@@ -39,7 +39,7 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
                 '#else\nextern "C" int eval_run4(long, const double*, double*) { return 0; }\n#endif\n'
                 '#ifdef S2M_HAS_PRUNE\n'
                 'extern "C" int prune_tiles(long ntiles, const float* box, int npts, const float* pts, unsigned* bits,\n'
-                '                           float* ops, float* full, float* pruned) {\n'
+                '                           float* ops, float* full, float* pruned, float* full4, float* pruned4) {\n'
                 '  for (long t = 0; t < ntiles; ++t) {\n'
                 '    s2i X, Y, Z; X.lo = box[6*t]; X.hi = box[6*t+1]; Y.lo = box[6*t+2]; Y.hi = box[6*t+3];\n'
                 '    Z.lo = box[6*t+4]; Z.hi = box[6*t+5];\n'
@@ -50,9 +50,14 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
                 '    for (int p = 0; p < npts; ++p) { const float* q = pts + 3 * (t * npts + p);\n'
                 '      full[t * npts + p] = s2m_user_sdf(q[0], q[1], q[2]);\n'
                 '      pruned[t * npts + p] = s2m_user_sdf_pruned(q[0], q[1], q[2], m); }\n'
+                '    for (int p = 0; p + 3 < npts; p += 4) { const float* q = pts + 3 * (t * npts + p);\n'
+                '      s2x4 z; for (int w = 0; w < 4; ++w) z.v[w] = q[3 * w + 2];\n'
+                '      s2x4 f = s2m_user_sdf_pruned_run4(q[0], q[1], z, m);\n'
+                '      for (int w = 0; w < 4; ++w) { full4[t * npts + p + w] = s2m_user_sdf(q[0], q[1], z.v[w]);\n'
+                '        pruned4[t * npts + p + w] = f.v[w]; } }\n'
                 '  }\n  return S2M_PRUNE_WORDS;\n}\n'
                 '#else\nextern "C" int prune_tiles(long, const float*, int, const float*, unsigned*, float*, float*,\n'
-                '                           float*) { return 0; }\n#endif\n')
+                '                           float*, float*, float*) { return 0; }\n#endif\n')
     so = os.path.join(d, "sdf.so")
     subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
                     src, "-o", so], check=True, capture_output=True)
@@ -60,7 +65,7 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
     L.eval_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
     L.normal_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
     L.eval_run4.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
-    L.prune_tiles.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 5
+    L.prune_tiles.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 7
     _cache[key] = L
     return L
 
@@ -109,8 +114,10 @@ def lattice_tiles(N: int, bounds: float, tiles=None, T: int = 8):
 
 
 def prune_host(cuda_src: str, boxes: np.ndarray, pts: np.ndarray):
-    """Run the tile function and the pruned point function on the host:
-    (words per tile or 0, ops per tile [fp, sfu], full values, pruned values)."""
+    """Run the tile function and the pruned point functions on the host:
+    (words per tile or 0, ops per tile [fp, sfu], full values, pruned values,
+    and the same for the run-of-4 form on groups of 4 consecutive points with
+    the first one's x and y)."""
     L = compile_host(cuda_src)
     nt, npts = len(boxes), pts.shape[1]
     boxes = np.ascontiguousarray(boxes, np.float32)
@@ -119,6 +126,8 @@ def prune_host(cuda_src: str, boxes: np.ndarray, pts: np.ndarray):
     ops = np.zeros((nt, 2), np.float32)
     full = np.zeros((nt, npts), np.float32)
     pruned = np.zeros((nt, npts), np.float32)
+    full4 = np.zeros((nt, npts), np.float32)
+    pruned4 = np.zeros((nt, npts), np.float32)
     w = L.prune_tiles(nt, boxes.ctypes.data, npts, pts.ctypes.data, bits.ctypes.data, ops.ctypes.data,
-                      full.ctypes.data, pruned.ctypes.data)
-    return w, ops, full, pruned
+                      full.ctypes.data, pruned.ctypes.data, full4.ctypes.data, pruned4.ctypes.data)
+    return w, ops, full, pruned, full4, pruned4

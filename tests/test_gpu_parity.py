@@ -216,7 +216,7 @@ def csg64_seed1(lib):
 
 @pytest.mark.parametrize("variant", range(s2m.EVAL_VARIANTS))
 def test_eval_variants_identical(csg64_seed1, variant):
-    """Every evaluation-kernel variant the autotuner may pick (5 and 6: tile
+    """Every evaluation-kernel variant the autotuner may pick (5 to 7: tile
     pruned) gives the same bits."""
     sdf, prm = csg64_seed1
     sdf.set_eval_variant(variant)

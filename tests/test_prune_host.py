@@ -25,10 +25,12 @@ def check(cu, N, bounds=2.0, tiles=None, seed=0, count=None):
         nt = (N + 1 + 7) // 8
         tiles = [tuple(int(v) for v in rng.integers(0, nt, 3)) for _ in range(count)]
     boxes, pts = lattice_tiles(N, bounds, tiles)
-    w, ops, full, pruned = prune_host(cu, boxes, pts)
+    w, ops, full, pruned, full4, pruned4 = prune_host(cu, boxes, pts)
     assert w > 0, "no pruning form"
     bad = full.view(np.uint32) != pruned.view(np.uint32)
     assert not bad.any(), f"{int(bad.sum())} pruned values differ, e.g. tile {np.argwhere(bad)[0]}"
+    bad4 = full4.view(np.uint32) != pruned4.view(np.uint32)
+    assert not bad4.any(), f"{int(bad4.sum())} run-of-4 pruned values differ, e.g. {np.argwhere(bad4)[0]}"
     return ops
 
 
