@@ -78,18 +78,20 @@ int device_sm_count() {
 
 // Evaluation-kernel variants compiled into every SDF module (the tables in
 // s2m_dc_kernels.cuh): name, z-run length, whether it evaluates the run-of-4
-// form, and whether it is a tile-pruned variant (present only in modules of
-// SDFs with a pruning form).
+// form, whether it is a tile-pruned variant (present only in modules of SDFs
+// with a pruning form), and whether it is the persistent chunked form.
 struct EvalVariant {
   const char *name;
   int run;
   bool vec;
   bool pruned;
+  bool chunked;
 };
 constexpr EvalVariant kEvalVariants[] = {
-    {"s2m_eval_b2r4", 4, false, false}, {"s2m_eval_b3r4", 4, false, false}, {"s2m_eval_b4r4", 4, false, false},
-    {"s2m_eval_b2v4", 4, true, false},  {"s2m_eval_b3v4", 4, true, false},  {"s2m_evalp_b8", 1, false, true},
-    {"s2m_evalp_b16", 1, false, true},  {"s2m_evalp_b8v4", 4, true, true}};
+    {"s2m_eval_b2r4", 4, false, false, false}, {"s2m_eval_b3r4", 4, false, false, false},
+    {"s2m_eval_b4r4", 4, false, false, false}, {"s2m_eval_b2v4", 4, true, false, false},
+    {"s2m_eval_b3v4", 4, true, false, false},  {"s2m_evalp_b8", 1, false, true, false},
+    {"s2m_evalpc_b2", 1, false, true, true},   {"s2m_evalpc_b2v4", 4, true, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -126,13 +128,17 @@ struct s2m_mesh {
   // workspace
   float *ring = nullptr;
   unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
-  unsigned short *cell_masks = nullptr;      // per thread of a cell tile: candidate bits of its cells
+  uint2 *pt_bits = nullptr;                  // sign / near-zero bits of a slab's lattice points
+  unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
+  unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
-  // tile pruning: [ops FP32, ops SFU] (2 u64), the tile base of every slab
-  // (nslabs + 1 u64), then the activity words of `prune_chunk` slabs' tiles
+  // tile pruning: [ops FP32, ops SFU] (2 u64), a tile-chunk counter per slab
+  // (u32), the tile base of every slab (nslabs + 1 u64), then the activity
+  // words of `prune_chunk` slabs' tiles
   unsigned long long *prune_buf = nullptr;
   std::vector<unsigned long long> slab_tile_base;  // host copy
   int prune_chunk = 0;
+  size_t prune_base_off = 0;  // bytes from prune_buf to the slab tile bases
   size_t prune_bits_off = 0;  // bytes from prune_buf to the activity words
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
@@ -298,13 +304,14 @@ void give_pinned_slot(unsigned long long *p) {
 }
 
 void free_buffers(s2m_mesh *m) {
-  void *ptrs[] = {m->ring, m->slab_ctrl, m->cell_masks, m->tile_cnt, m->prune_buf, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
+  void *ptrs[] = {m->ring, m->slab_ctrl, m->pt_bits, m->offx, m->cell_words, m->tile_cnt, m->prune_buf, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
                   m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
                   m->jobctl};
   for (void *p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   if (m->h_read) give_pinned_slot(m->h_read);
-  m->ring = nullptr; m->slab_ctrl = nullptr; m->cell_masks = nullptr; m->tile_cnt = nullptr; m->prune_buf = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
+  m->ring = nullptr; m->slab_ctrl = nullptr; m->pt_bits = nullptr; m->offx = nullptr; m->cell_words = nullptr;
+  m->tile_cnt = nullptr; m->prune_buf = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
   m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
   m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
   m->jobctl = nullptr; m->h_read = nullptr;
@@ -407,16 +414,21 @@ size_t prune_layout(s2m_mesh *m) {
     const int e = std::min(ns, s + m->prune_chunk);
     chunk_tiles = std::max(chunk_tiles, m->slab_tile_base[size_t(e)] - m->slab_tile_base[size_t(s)]);
   }
-  m->prune_bits_off = (16 + 8 * (size_t(ns) + 1) + 15) / 16 * 16;
+  m->prune_base_off = (16 + 4 * size_t(ns) + 15) / 16 * 16;
+  m->prune_bits_off = (m->prune_base_off + 8 * (size_t(ns) + 1) + 15) / 16 * 16;
   return m->prune_bits_off + size_t(chunk_tiles) * words * 4;
 }
+unsigned long long *prune_bases(const s2m_mesh *m) {
+  return reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(m->prune_buf) + m->prune_base_off);
+}
+unsigned *prune_counters(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
 // Tile pass over slabs [s_begin, s_end) and the pruned evaluation of slab s.
 cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t st) {
   S2Job jj = m->job;
   unsigned *bits = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(m->prune_buf) + m->prune_bits_off);
   unsigned long long *ops = m->prune_buf;
-  const unsigned long long *base = m->prune_buf + 2;
+  const unsigned long long *base = prune_bases(m);
   int D = m->D, nzc = m->nzc;
   const unsigned long long n = m->slab_tile_base[size_t(s_end)] - m->slab_tile_base[size_t(s_begin)];
   void *targs[] = {&jj, &bits, &ops, &base, &s_begin, &s_end, &D, &nzc};
@@ -432,9 +444,34 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   const unsigned *bits =
       reinterpret_cast<const unsigned *>(reinterpret_cast<const char *>(m->prune_buf) + m->prune_bits_off) +
       (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
+  if (kEvalVariants[v].chunked) {
+    unsigned *counter = prune_counters(m) + s;
+    void *cargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m->sdf->k_eval[v], S2_PTP_BLOCK, 0) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    const long long chunks = (g.ntiles + S2_PTP_BLOCK / 32 - 1) / (S2_PTP_BLOCK / 32);
+    const unsigned grid = unsigned(std::max<long long>(1, std::min<long long>(chunks, (long long)device_sm_count() * per_sm)));
+    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(grid), dim3(S2_PTP_BLOCK), cargs, 0, st);
+  }
   void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
                           0, st);
+}
+
+// Classification buffers: words of 32 cells per slab (tiles of S2_CW_BLOCK
+// words), and the point bits of a slab's D + 1 planes.
+size_t cell_word_tiles(const s2m_mesh *m) {
+  const size_t WN = size_t((m->N + 31) / 32);
+  return (size_t(m->D) * size_t(m->N) * WN + S2_CW_BLOCK - 1) / S2_CW_BLOCK;
+}
+size_t pt_bits_words(const s2m_mesh *m) {
+  const size_t P = size_t(m->job.P), WP = (P + 31) / 32;
+  return (size_t(m->D) + 1) * P * WP;
 }
 
 void drop_graph(s2m_mesh *m) {
@@ -448,11 +485,10 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   free_buffers(m);
   const S2Job &j = m->job;
   const unsigned long long N = (unsigned long long)m->N;
-  const unsigned long long cells_per_slab = (unsigned long long)m->D * N * N;
   m->cand_cap = std::max<unsigned long long>(1024, std::min(cand_cap, N * N * N));
   m->vcap = std::max<unsigned long long>(1024, std::min(vcap, N * N * N));
   m->tcap = std::max<unsigned long long>(2048, tcap);
-  m->cell_tiles = (cells_per_slab + S2_CELL_TILE - 1) / S2_CELL_TILE;
+  m->cell_tiles = cell_word_tiles(m);
   m->vc_tiles = (m->cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
   m->slab_ctrl_words = m->cell_tiles + 1;
   m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
@@ -461,12 +497,14 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   cudaStream_t st = m->stream;
   S2_CUDA(cudaMallocAsync(&m->ring, ring_floats * sizeof(float), st));
   S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->cell_masks, m->cell_tiles * S2_CELL_BLOCK * 2, st));
+  S2_CUDA(cudaMallocAsync(&m->pt_bits, pt_bits_words(m) * sizeof(uint2), st));
+  S2_CUDA(cudaMallocAsync(&m->offx, size_t((j.N + 31) / 32) * 4, st));
+  S2_CUDA(cudaMallocAsync(&m->cell_words, m->cell_tiles * S2_CW_BLOCK * 4, st));
   S2_CUDA(cudaMallocAsync(&m->tile_cnt, m->cell_tiles * 4, st));
   if (m->sdf->k_tiles && m->nslabs > 0) {
     S2_CUDA(cudaMallocAsync(&m->prune_buf, prune_layout(m), st));
     // pageable source: the call returns once the words are staged
-    S2_CUDA(cudaMemcpyAsync(m->prune_buf + 2, m->slab_tile_base.data(), m->slab_tile_base.size() * 8,
+    S2_CUDA(cudaMemcpyAsync(prune_bases(m), m->slab_tile_base.data(), m->slab_tile_base.size() * 8,
                             cudaMemcpyHostToDevice, st));
   }
   S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
@@ -598,10 +636,11 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->last_variant = ev;
   m->eval_points = 0;
   m->eval_fp_ops = m->eval_sfu_ops = 0;
-  if (pruned) {
-    cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, 16, st);
+  if (pruned) {  // operation counters and the slabs' tile-chunk counters
+    cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }
+  S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
   for (int s = 0; s < m->nslabs; ++s) {
     int zc0 = s * m->D;
     int zc1 = std::min(m->nzc, zc0 + m->D);
@@ -621,13 +660,20 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                 cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
     }
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
-    unsigned cg = unsigned((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CELL_BLOCK, 0, st>>>(j, m->ring, m->cell_masks, m->tile_cnt, zc0, zc1),
+    const unsigned long long np = (unsigned long long)(zc1 - zc0 + 1);
+    const unsigned long long bit_threads = np * (unsigned long long)j.P * (unsigned long long)((j.P + 31) / 32) * 32ull;
+    S2_LAUNCH(1, 0, (s2m_cells_bits<<<unsigned((bit_threads + 255) / 256), 256, 0, st>>>(j, m->ring, m->pt_bits, zc0,
+                                                                                          int(np)),
+                     cudaGetLastError()));
+    const unsigned long long nwords = (unsigned long long)(zc1 - zc0) * N * ((N + 31) / 32);
+    const unsigned cg = unsigned((nwords + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
+    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->pt_bits, m->offx, m->cell_words, m->tile_cnt,
+                                                                    zc0, zc1),
                           cudaGetLastError()));
     S2_LAUNCH(1, 0, (s2m_cells_offsets<<<1, 1024, 0, st>>>(m->tile_cnt, cg, m->slab_ctrl, m->cand_base, s),
                      cudaGetLastError()));
-    S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CELL_BLOCK, 0, st>>>(j, m->ring, m->cell_masks, m->slab_ctrl, cand, c.err,
-                                                                  zc0),
+    S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->ring, m->cell_words, m->slab_ctrl, cand, c.err,
+                                                               zc0, zc1),
                      cudaGetLastError()));
   }
   S2Job jj = j;
@@ -694,6 +740,7 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
     }
     float ms_best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
+      if (kEvalVariants[v].pruned) S2_CUDA(cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st));
       S2_CUDA(cudaEventRecord(a, st));
       for (int s : trial) {
         if (kEvalVariants[v].pruned) {
@@ -1202,14 +1249,14 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
 
   const S2Job &j = m.job;
   const unsigned long long N = (unsigned long long)m.N;
-  const unsigned long long cells_per_slab = (unsigned long long)m.D * N * N;
-  m.cell_tiles = (cells_per_slab + S2_CELL_TILE - 1) / S2_CELL_TILE;
+  m.cell_tiles = cell_word_tiles(&m);
   m.slab_ctrl_words = m.cell_tiles + 1;
   m.scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   size_t used = 0;
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
-            carve(base, used, m.cell_tiles * S2_CELL_BLOCK, &m.cell_masks) && carve(base, used, m.cell_tiles, &m.tile_cnt) &&
+            carve(base, used, pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
+            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles, &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
             carve(base, used, size_t(8), &m.jobctl);

@@ -190,27 +190,17 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
   }
 }
 
-// Pruned lattice evaluation: one tile per warp, the lanes striding over the
-// tile's points (RUN4: over runs of 4 planes sharing x and y, which share
-// the bit tests and the x/y-only arithmetic; a run past the tile's last
-// plane repeats that plane and stores only its own planes).  The activity
-// bits (in shared memory) are the same for the whole warp, so the pruned
-// function's branches never diverge.  Points past the lattice edge (tiles
-// are 8 x 8) evaluate a clamped point and store nothing.
+// Pruned evaluation of one tile by one warp: the lanes stride over the
+// tile's points (RUN4: over runs of 4 planes sharing x and y, which share the
+// bit tests and the x/y-only arithmetic; a run past the tile's last plane
+// repeats that plane and stores only its own planes).  `m` (shared memory)
+// holds the tile's activity bits, the same for the whole warp, so the pruned
+// function's branches never diverge.  Points past the lattice edge (tiles are
+// 8 x 8) evaluate a clamped point and store nothing.
 template <bool RUN4>
-__device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restrict__ ring,
-                                               const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) {
-  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const long long ntiles = (long long)ntx * ntx * nzt;
-  const long long t = (long long)blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5);
-  if (t >= ntiles) return;
-  const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, tzs);
-  if (tl.kb > tl.ke) return;
-  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_PRUNE_WORDS];
+__device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict__ ring, const S2PruneTile &tl,
+                                             const unsigned *m) {
   const int lane = (int)(threadIdx.x & 31u);
-  if (lane < S2M_PRUNE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
-  __syncwarp();
-  const unsigned *m = s_bits[threadIdx.x >> 5];
   const int nz = tl.ke - tl.kb + 1;
   if (RUN4) {
     const int nruns = S2_PT_XY * S2_PT_XY * ((nz + 3) >> 2);
@@ -243,15 +233,73 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   }
 }
 
+// One tile per warp, 4 warps per block, tile t = block * 4 + warp.
+template <bool RUN4>
+__device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restrict__ ring,
+                                               const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) {
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const long long ntiles = (long long)ntx * ntx * nzt;
+  const long long t = (long long)blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5);
+  if (t >= ntiles) return;
+  const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, tzs);
+  if (tl.kb > tl.ke) return;
+  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_PRUNE_WORDS];
+  const int lane = (int)(threadIdx.x & 31u);
+  if (lane < S2M_PRUNE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
+  __syncwarp();
+  s2_eval_tile<RUN4>(job, ring, tl, s_bits[threadIdx.x >> 5]);
+}
+
+// Persistent form: each block takes chunks of S2_PTP_BLOCK / 32 consecutive
+// tiles (one per warp) from the slab's counter until none are left.  All the
+// warps of a block then work on neighbouring tiles, whose active segments are
+// much alike, so they run the same parts of the (large) pruned function and
+// share the instruction cache; with one tile per 4-warp block, an SM's warps
+// come from tiles all over the slab.
+template <bool RUN4>
+__device__ __forceinline__ void s2_eval_pruned_chunks(const S2Job &job, float *__restrict__ ring,
+                                                      const unsigned *__restrict__ bits, int k0, int nk, int tzs,
+                                                      int nzt, unsigned *__restrict__ counter) {
+  constexpr int kWarps = S2_PTP_BLOCK / 32;
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const long long ntiles = (long long)ntx * ntx * nzt;
+  __shared__ unsigned s_chunk;
+  __shared__ unsigned s_bits[kWarps][S2M_PRUNE_WORDS];
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
+  for (;;) {
+    if (threadIdx.x == 0) s_chunk = atomicAdd(counter, 1u);
+    __syncthreads();
+    const long long first = (long long)s_chunk * kWarps;
+    __syncthreads();
+    if (first >= ntiles) break;
+    const long long t = first + warp;
+    if (t < ntiles) {
+      const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, tzs);
+      if (tl.kb <= tl.ke) {
+        if (lane < S2M_PRUNE_WORDS) s_bits[warp][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
+        __syncwarp();
+        s2_eval_tile<RUN4>(job, ring, tl, s_bits[warp]);
+        __syncwarp();
+      }
+    }
+  }
+}
+
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
   NAME(S2Job job, float *__restrict__ ring, const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) { \
     s2_eval_pruned<RUN4>(job, ring, bits, k0, nk, tzs, nzt);                                      \
   }
+#define S2_EVALPC_VARIANT(NAME, MINB, RUN4)                                                       \
+  extern "C" __global__ void __launch_bounds__(S2_PTP_BLOCK, MINB)                                \
+  NAME(S2Job job, float *__restrict__ ring, const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt, \
+       unsigned *counter) {                                                                       \
+    s2_eval_pruned_chunks<RUN4>(job, ring, bits, k0, nk, tzs, nzt, counter);                      \
+  }
 // Keep this table in step with kEvalVariants in runtime.cu.
 S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
-S2_EVALP_VARIANT(s2m_evalp_b16, 16, false)
-S2_EVALP_VARIANT(s2m_evalp_b8v4, 8, true)
+S2_EVALPC_VARIANT(s2m_evalpc_b2, 2, false)
+S2_EVALPC_VARIANT(s2m_evalpc_b2v4, 2, true)
 #endif
 
 

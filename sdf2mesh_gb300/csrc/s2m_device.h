@@ -87,6 +87,7 @@ struct S2MeshDev {
 #define S2_CELL_BLOCK 256
 #define S2_CELL_CPT 16
 #define S2_CELL_TILE (S2_CELL_BLOCK * S2_CELL_CPT)
+#define S2_CW_BLOCK 256          /* words of 32 cells per classification tile */
 #define S2_EVAL_BLOCK 256
 #define S2_EVAL_RUN 4
 // Tile pruning: tiles of 8 x 8 lattice points in x and y and at most 8
@@ -94,6 +95,7 @@ struct S2MeshDev {
 #define S2_PT_XY 8
 #define S2_PT_ZMAX 8
 #define S2_PT_BLOCK 128
+#define S2_PTP_BLOCK 512          /* persistent pruned evaluation: 16 warps, 16 tiles per chunk */
 #define S2_VX_BLOCK 128
 #define S2_VC_BLOCK 256
 #define S2_VC_CPT 4

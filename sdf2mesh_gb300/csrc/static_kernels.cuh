@@ -6,35 +6,107 @@
 #include "s2m_workers.cuh"
 #include "s2m_dc_core.cuh"
 
-// Classification of one slab in three passes that never wait on one another
-// (a single pass with a look-back makes every resident tile wait for the
-// aggregates of the others):
-//   s2m_cells_mark     candidate bits of S2_CELL_CPT cells per thread, tile counts
+// Classification of one slab, bit-parallel over 32 cells along x, in passes
+// that never wait on one another:
+//   s2m_cells_bits     per lattice point of the slab's planes, a sign bit
+//                      (v > 0) and a near-zero bit (!(|v| >= guard)), 32
+//                      points per word pair; each point is read once
+//   s2m_cells_mark     per word of 32 cells, the candidate bits from the
+//                      corner bits of the 4 point rows around it (a few dozen
+//                      bitwise operations for 32 cells), and the tile counts
 //   s2m_cells_offsets  exclusive scan of the tile counts (one block)
 //   s2m_cells_emit     the candidates of each tile, in (z, y, x) order
-__global__ void __launch_bounds__(S2_CELL_BLOCK) s2m_cells_mark(S2Job job, const float *__restrict__ ring,
-                                                                unsigned short *__restrict__ masks,
-                                                                unsigned *__restrict__ tile_cnt, int zc0, int zc1) {
-  __shared__ unsigned s_warp[S2_CELL_BLOCK / 32];
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, tile = blockIdx.x;
-  const long long ncells = (long long)(zc1 - zc0) * job.N * job.N;
-  const long long c0 = (long long)tile * S2_CELL_TILE + (long long)S2_CELL_CPT * tid;
-  unsigned mask = 0;
+// The rule is s2_classify_values' (s2m_dc_core.cuh): a cell is a candidate
+// when its 8 lattice corners do not share a sign, or (reference rule) when a
+// corner whose reference coordinates are off the lattice is near zero (every
+// cell with such a corner when S2M_JOB_EXACT_CORNERS).
+
+// Off-lattice bit of every cell column x: bit x % 32 of word x / 32 is
+// s2_off_lattice(x + 1).
+__global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict__ offx) {
+  const int x = (int)(blockIdx.x * 256u + threadIdx.x);
+  const unsigned b = __ballot_sync(S2_FULL, x < job.N && s2_off_lattice(job, x + 1));
+  if ((threadIdx.x & 31u) == 0 && x < job.N) offx[x >> 5] = b;
+}
+
+// Planes zc0 .. zc0 + np - 1 (slot p = plane zc0 + p): bits[(p * P + y) * WP + w]
+// holds points x = 32 w .. 32 w + 31 of row y (bits past the lattice are 0).
+__global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__restrict__ ring,
+                                                      uint2 *__restrict__ bits, int zc0, int np) {
+  const int WP = (job.P + 31) >> 5;
+  const long long wi = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;  // the warp's word
+  if (wi >= (long long)np * job.P * WP) return;                           // whole warps
+  const int w = (int)(wi % WP);
+  const long long r = wi / WP;
+  const int y = (int)(r % job.P);
+  const int p = (int)(r / job.P);
+  const int x = w * 32 + (int)(threadIdx.x & 31u);
+  const bool in = x < job.P;
+  const float v = in ? __ldg(ring + (long long)((zc0 + p) % job.ring) * job.plane + (long long)y * job.pitch + x) : 0.0f;
+  const unsigned pos = __ballot_sync(S2_FULL, in && v > 0.0f);
+  const unsigned near = __ballot_sync(S2_FULL, in && !(fabsf(v) >= job.guard));
+  if ((threadIdx.x & 31u) == 0) bits[wi] = make_uint2(pos, near);
+}
+
+// Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.
+__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, const uint2 *__restrict__ bits,
+                                                            const unsigned *__restrict__ offx,
+                                                            unsigned *__restrict__ words,
+                                                            unsigned *__restrict__ tile_cnt, int zc0, int zc1) {
+  __shared__ unsigned s_warp[S2_CW_BLOCK / 32];
+  const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5;
+  const long long nw = (long long)(zc1 - zc0) * job.N * WN;
+  const long long l = (long long)blockIdx.x * S2_CW_BLOCK + threadIdx.x;
+  unsigned cand = 0;
+  if (l < nw) {
+    const int w = (int)(l % WN);
+    const long long r = l / WN;
+    const int y = (int)(r % job.N);
+    const int dz = (int)(r / job.N);
+    // corner k = bx | by << 1 | bz << 2 lies in point row q = by | bz << 1
+    // (k = 2 q + bx); bx = 1 takes the row's bits shifted by one point
+    unsigned pb[8], nb[8];
 #pragma unroll
-  for (int g = 0; g < S2_CELL_CPT / 4; ++g) {
-    float v[4][8];
-    mask |= s2_classify4<false>(job, ring, c0 + 4 * g, ncells, zc0, v) << (4 * g);
+    for (int q = 0; q < 4; ++q) {
+      const long long base = ((long long)(dz + (q >> 1)) * job.P + (y + (q & 1))) * WP + w;
+      const uint2 lo = bits[base];
+      const uint2 hi = w + 1 < WP ? bits[base + 1] : make_uint2(0u, 0u);
+      pb[2 * q] = lo.x;
+      pb[2 * q + 1] = __funnelshift_r(lo.x, hi.x, 1);
+      nb[2 * q] = lo.y;
+      nb[2 * q + 1] = __funnelshift_r(lo.y, hi.y, 1);
+    }
+    unsigned all = ~0u, any = 0u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      all &= pb[k];
+      any |= pb[k];
+    }
+    cand = any & ~all;
+    if (!job.qef) {
+      const unsigned ox = offx[w];
+      const unsigned oy = s2_off_lattice(job, y + 1) ? ~0u : 0u;
+      const unsigned oz = s2_off_lattice(job, zc0 + dz + 1) ? ~0u : 0u;
+      if (job.exact) {
+        cand |= ox | oy | oz;
+      } else {
+#pragma unroll
+        for (int k = 1; k < 8; ++k)
+          cand |= nb[k] & (((k & 1) ? ox : 0u) | ((k & 2) ? oy : 0u) | ((k & 4) ? oz : 0u));
+      }
+    }
+    if (w == WN - 1 && (job.N & 31)) cand &= (1u << (job.N & 31)) - 1u;
+    words[l] = cand;
   }
-  masks[(size_t)tile * S2_CELL_BLOCK + tid] = (unsigned short)mask;
-  unsigned cnt = __popc(mask);
+  unsigned cnt = __popc(cand);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(S2_FULL, cnt, o);
-  if (lane == 0) s_warp[warp] = cnt;
+  if ((threadIdx.x & 31u) == 0) s_warp[threadIdx.x >> 5] = cnt;
   __syncthreads();
-  if (tid == 0) {
+  if (threadIdx.x == 0) {
     unsigned t = 0;
-    for (int w = 0; w < S2_CELL_BLOCK / 32; ++w) t += s_warp[w];
-    tile_cnt[tile] = t;
+    for (int i = 0; i < S2_CW_BLOCK / 32; ++i) t += s_warp[i];
+    tile_cnt[blockIdx.x] = t;
   }
 }
 
@@ -79,13 +151,18 @@ __global__ void __launch_bounds__(1024) s2m_cells_offsets(const unsigned *__rest
   if (tid == 0) base[slab_index + 1] = s_carry;
 }
 
-__global__ void __launch_bounds__(S2_CELL_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
-                                                                const unsigned short *__restrict__ masks,
-                                                                const unsigned long long *__restrict__ tile_off,
-                                                                S2Cand cand, unsigned *err, int zc0) {
+// The candidates of each tile in order: key (x | y << 16 | z << 32) and the
+// 8 lattice corner values.
+__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
+                                                            const unsigned *__restrict__ words,
+                                                            const unsigned long long *__restrict__ tile_off,
+                                                            S2Cand cand, unsigned *err, int zc0, int zc1) {
   __shared__ unsigned s_warp[32];
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, tile = blockIdx.x;
-  const unsigned mask = masks[(size_t)tile * S2_CELL_BLOCK + tid];
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const int WN = (job.N + 31) >> 5;
+  const long long nw = (long long)(zc1 - zc0) * job.N * WN;
+  const long long l = (long long)blockIdx.x * S2_CW_BLOCK + tid;
+  const unsigned mask = l < nw ? words[l] : 0u;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
 #pragma unroll
@@ -94,23 +171,27 @@ __global__ void __launch_bounds__(S2_CELL_BLOCK) s2m_cells_emit(S2Job job, const
     if ((int)lane >= o) inc += t;
   }
   if (lane == 31) s_warp[warp] = inc;
-  if (tid < 32 && tid >= S2_CELL_BLOCK / 32) s_warp[tid] = 0u;
+  if (tid < 32 && tid >= S2_CW_BLOCK / 32) s_warp[tid] = 0u;
   __syncthreads();
   if (warp == 0) s2_warp_exclusive32(s_warp);
   __syncthreads();
   if (!mask) return;
-  unsigned long long o = tile_off[tile] + s_warp[warp] + (inc - cnt);
-  const long long c0 = (long long)tile * S2_CELL_TILE + (long long)S2_CELL_CPT * tid;
+  unsigned long long o = tile_off[blockIdx.x] + s_warp[warp] + (inc - cnt);
+  const int w = (int)(l % WN);
+  const long long r = l / WN;
+  S2Cell cell;
+  cell.y = (int)(r % job.N);
+  cell.z = zc0 + (int)(r / job.N);
   unsigned rem = mask;
   while (rem) {
-    const int m = __ffs(rem) - 1;
+    const int b = __ffs(rem) - 1;
     rem &= rem - 1u;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
       ++o;
       continue;
     }
-    const S2Cell cell = s2_cell_of(job, c0 + m, zc0);
+    cell.x = 32 * w + b;
     float v[8];
     s2_load_corners<false>(job, ring, cell, v);
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
