@@ -13,6 +13,8 @@
 //   s2m_user_sdf_tile(X, Y, Z, m, fp, sfu)   intervals of the tile's coordinates
 //       -> activity bits m[] (2 per combinator: operand a needed, operand b
 //          needed) and the FP32 / SFU operations per point that remain;
+//   s2m_user_sdf_tile_in(X, Y, Z, pm, m, ...)  the same for a tile inside a
+//       box whose bits pm are known: only pm's active segments are evaluated;
 //   s2m_user_sdf_pruned(x, y, z, m)          the point value, evaluating only
 //       the active segments; bit-identical to s2m_user_sdf.
 #include "prune.h"
@@ -21,6 +23,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <sstream>
 
 namespace s2m {
@@ -110,7 +113,8 @@ class Pruner {
       var_[size_t(v)] = p.op == POp::Z || (p.a >= 0 && var_[size_t(p.a)]) || (p.b >= 0 && var_[size_t(p.b)]) ||
                         (p.c >= 0 && var_[size_t(p.c)]);
     }
-    emit_tile(o, pc.words);
+    emit_tile(o, pc.words, false);
+    emit_tile(o, pc.words, true);
     run4_ = false;
     emit_point(o);
     run4_ = true;
@@ -304,13 +308,27 @@ class Pruner {
     }() + ")";
   }
 
-  void emit_tile(std::ostringstream &o, int words) const {
-    o << "S2HD void s2m_user_sdf_tile(const s2i X, const s2i Y, const s2i Z, unsigned *m, float *fp, float *sfu)\n{\n";
+  // The tile function.  `guarded`: the form for a tile inside a larger box
+  // whose activity bits pm are known.  A segment inactive there is inactive
+  // in the tile, and a combinator with one operand inactive there keeps the
+  // other one, so only the nodes of segments active in pm are evaluated.
+  void emit_tile(std::ostringstream &o, int words, bool guarded) const {
+    if (guarded)
+      o << "S2I_FN void s2m_user_sdf_tile_in(const s2i X, const s2i Y, const s2i Z, const unsigned *pm, unsigned *m, "
+           "float *fp, float *sfu)\n{\n";
+    else
+      o << "S2I_FN void s2m_user_sdf_tile(const s2i X, const s2i Y, const s2i Z, unsigned *m, float *fp, float *sfu)\n{\n";
     o << "  (void)X; (void)Y; (void)Z;\n";
     for (int v : combs_) o << "  int d" << v << " = 0;\n";
-    for (int v = 0; v < n_; ++v) {
-      if (!live_[size_t(v)] || is_leaf(nd(v).op)) continue;
-      o << "  const s2i i" << v << " = " << iexpr(v) << ";\n";
+    if (!guarded) {
+      for (int v = 0; v < n_; ++v) {
+        if (!live_[size_t(v)] || is_leaf(nd(v).op)) continue;
+        o << "  const s2i i" << v << " = " << iexpr(v) << ";\n";
+      }
+    } else {
+      for (int v = 0; v < n_; ++v)
+        if (live_[size_t(v)] && !is_leaf(nd(v).op)) o << "  s2i i" << v << ";\n";
+      emit_tile_region(o, 0, regions(), "  ");
     }
     // activity: parents (larger node index) before the segments nested in them
     const size_t ns = 1 + 2 * combs_.size();
@@ -357,19 +375,17 @@ class Pruner {
     o << "}\n";
   }
 
-  // Point code.  Every node is placed in a region: the innermost operand-b
-  // segment enclosing its segment, or the top level.  A region's nodes are
-  // emitted in ascending order; a node whose segment is not the region
-  // itself (an operand-a segment inside it) is guarded by that segment's
-  // bit, consecutive nodes of one segment sharing one `if`.  A combinator is
-  // emitted where its index falls, without a guard of its own (when its
-  // segment is inactive its value is simply not used), as
-  //     if (b active) { <region of operand b>; v = a active ? op(a, b) : b; } else v = a;
-  // so a combinator that keeps operand a costs one test.  Operand-a
-  // segments are not nested blocks: a chain of combinators stays one level
-  // deep.
-  void emit_region(std::ostringstream &o, int R, const std::vector<std::vector<int>> &members,
-                   const std::string &ind) const {
+  // The guarded tile function's body, in the regions of the point code: a
+  // combinator is
+  //   if (b active in pm) { <region of b>; i = a active in pm ? sel(a, b) : b; }
+  //   else if (a active in pm) i = a;
+  // and the nodes of an operand-a segment inside a region are guarded by
+  // that segment's bit in pm.
+  static std::string ptest(int bit) {
+    return "(pm[" + std::to_string(bit >> 5) + "] >> " + std::to_string(bit & 31) + " & 1u)";
+  }
+  void emit_tile_region(std::ostringstream &o, int R, const std::vector<std::vector<int>> &members,
+                        const std::string &ind) const {
     int open = R;
     auto close = [&]() {
       if (open != R) o << ind << "}\n";
@@ -381,13 +397,106 @@ class Pruner {
         close();
         const PNode &p = nd(v);
         const int sa = seg(ci, 0), sb = seg(ci, 1);
-        const std::string A = as_var(p.a, var_[size_t(v)]), B = as_var(p.b, var_[size_t(v)]);
-        const std::string keepA = p.op == POp::SmoothSubtraction ? "(-" + A + ")" : A;
-        o << ind << "if " << bit_test(sb - 1) << " {\n";
-        emit_region(o, sb, members, ind + "  ");
-        o << ind << "  if " << bit_test(sa - 1) << " v" << v << " = " << expr(v) << ";\n";
-        o << ind << "  else v" << v << " = " << B << ";\n";
-        o << ind << "} else {\n" << ind << "  v" << v << " = " << keepA << ";\n" << ind << "}\n";
+        const std::string keepA = p.op == POp::SmoothSubtraction ? "s2i_neg(" + ival(p.a) + ")" : ival(p.a);
+        o << ind << "if " << ptest(sb - 1) << " {\n";
+        emit_tile_region(o, sb, members, ind + "  ");
+        o << ind << "  if " << ptest(sa - 1) << " i" << v << " = " << iexpr(v) << ";\n";
+        o << ind << "  else { i" << v << " = " << ival(p.b) << "; d" << v << " = 2; }\n";
+        o << ind << "} else if " << ptest(sa - 1) << " {\n";
+        o << ind << "  i" << v << " = " << keepA << "; d" << v << " = 1;\n" << ind << "}\n";
+        continue;
+      }
+      const int s = owner_[size_t(v)];
+      if (s != open) {
+        close();
+        if (s != R) o << ind << "if " << ptest(s - 1) << " {\n";
+        open = s;
+      }
+      o << ind << (open != R ? "  " : "") << "i" << v << " = " << iexpr(v) << ";\n";
+    }
+    close();
+  }
+
+  // Point code.  Every node is placed in a region: the innermost operand-b
+  // segment enclosing its segment, or the top level.  A region's nodes are
+  // emitted in ascending order; a node whose segment is not the region
+  // itself (an operand-a segment inside it) is guarded by that segment's
+  // bit, consecutive nodes of one segment sharing one `if`.  A combinator is
+  // emitted where its index falls, without a guard of its own (when its
+  // segment is inactive its value is simply not used), as
+  //     if (b active) { <region of operand b>; v = a active ? op(a, b) : b; } else v = a;
+  // so a combinator that keeps operand a costs one test.  Operand-a
+  // segments are not nested blocks: a chain of combinators stays one level
+  // deep.
+  void emit_combinator(std::ostringstream &o, int v, const std::vector<std::vector<int>> &members,
+                       const std::string &ind) const {
+    const int ci = comb_of_[size_t(v)];
+    const PNode &p = nd(v);
+    const int sa = seg(ci, 0), sb = seg(ci, 1);
+    const std::string A = as_var(p.a, var_[size_t(v)]), B = as_var(p.b, var_[size_t(v)]);
+    const std::string keepA = p.op == POp::SmoothSubtraction ? "(-" + A + ")" : A;
+    o << ind << "if " << bit_test(sb - 1) << " {\n";
+    emit_region(o, sb, members, ind + "  ");
+    o << ind << "  if " << bit_test(sa - 1) << " v" << v << " = " << expr(v) << ";\n";
+    o << ind << "  else v" << v << " = " << B << ";\n";
+    o << ind << "} else {\n" << ind << "  v" << v << " = " << keepA << ";\n" << ind << "}\n";
+  }
+
+  // A chain: consecutive members of a region, each combinator the operand a
+  // of the next and used nowhere else (c = op(op(op(x, b1), b2), b3) ...).
+  // Its combinators are emitted in chunks of kChainChunk under one test of
+  // their operand-b bits: when none is set, every combinator of the chunk
+  // keeps operand a and the chunk's result is its input.  (Not for the smooth
+  // subtraction, whose "keep a" is -a.)
+  static constexpr int kChainChunk = 8;
+  bool chain_link(int prev, int v) const {
+    const int ci = comb_of_[size_t(v)];
+    if (ci < 0 || nd(v).op == POp::SmoothSubtraction) return false;
+    if (prev < 0) return true;
+    return nd(v).a == prev && uses_[size_t(prev)].size() == 1;
+  }
+
+  void emit_region(std::ostringstream &o, int R, const std::vector<std::vector<int>> &members,
+                   const std::string &ind) const {
+    int open = R;
+    auto close = [&]() {
+      if (open != R) o << ind << "}\n";
+      open = R;
+    };
+    const std::vector<int> &mem = members[size_t(R)];
+    for (size_t idx = 0; idx < mem.size(); ++idx) {
+      const int v = mem[idx];
+      const int ci = comb_of_[size_t(v)];
+      if (ci >= 0) {
+        close();
+        size_t end = idx + 1;  // the chain starting at v: mem[idx, end)
+        if (chain_link(-1, v))
+          while (end < mem.size() && chain_link(mem[end - 1], mem[end])) ++end;
+        if (end - idx < 4) {
+          emit_combinator(o, v, members, ind);
+          continue;
+        }
+        for (size_t c0 = idx; c0 < end; c0 += kChainChunk) {
+          const size_t c1 = std::min(end, c0 + size_t(kChainChunk));
+          std::map<int, unsigned> words;  // operand-b bits of the chunk by word
+          for (size_t k = c0; k < c1; ++k) {
+            const int bit = seg(comb_of_[size_t(mem[k])], 1) - 1;
+            words[bit >> 5] |= 1u << (bit & 31);
+          }
+          std::ostringstream test;
+          for (auto &[w, msk] : words) {
+            char hx[16];
+            std::snprintf(hx, sizeof hx, "%xu", msk);
+            test << (test.tellp() > 0 ? " | " : "") << "(m[" << w << "] & 0x" << hx << ")";
+          }
+          const int last = mem[c1 - 1];
+          o << ind << "if (" << test.str() << ") {\n";
+          for (size_t k = c0; k < c1; ++k) emit_combinator(o, mem[k], members, ind + "  ");
+          o << ind << "} else {\n";
+          o << ind << "  v" << last << " = " << as_var(nd(mem[c0]).a, var_[size_t(last)]) << ";\n";
+          o << ind << "}\n";
+        }
+        idx = end - 1;
         continue;
       }
       const int s = owner_[size_t(v)];

@@ -103,7 +103,8 @@ struct s2m_sdf {
   uint32_t flags = 0;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_eval[kNumEvalVariants] = {};  // null: variant not in this module
-  cudaKernel_t k_tiles = nullptr;               // tile pass of the pruned variants
+  cudaKernel_t k_tiles = nullptr;               // tile pass of the pruned variants (tiles,
+  cudaKernel_t k_tiles_coarse = nullptr;        // and the boxes of 4 x 4 tiles first)
   cudaKernel_t k_vertices = nullptr;
   // precision mode: a second module with the QEF vertex kernel, built on the
   // first QEF job (most SDFs never need it, and it compiles slowly)
@@ -133,13 +134,16 @@ struct s2m_mesh {
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
   // tile pruning: [ops FP32, ops SFU] (2 u64), a tile-chunk counter per slab
-  // (u32), the tile base of every slab (nslabs + 1 u64), then the activity
-  // words of `prune_chunk` slabs' tiles
+  // (u32), the first tile and the first coarse box of every slab (2 x
+  // nslabs + 1 u64), then the activity words of `prune_chunk` slabs' coarse
+  // boxes and tiles
   unsigned long long *prune_buf = nullptr;
-  std::vector<unsigned long long> slab_tile_base;  // host copy
+  std::vector<unsigned long long> slab_tile_base, slab_coarse_base;  // host copies
   int prune_chunk = 0;
-  size_t prune_base_off = 0;  // bytes from prune_buf to the slab tile bases
-  size_t prune_bits_off = 0;  // bytes from prune_buf to the activity words
+  size_t prune_base_off = 0;   // bytes from prune_buf to the slab tile bases
+  size_t prune_cbase_off = 0;  // ... to the slab coarse-box bases
+  size_t prune_sbits_off = 0;  // ... to the coarse boxes' activity words
+  size_t prune_bits_off = 0;   // ... to the tiles' activity words
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -244,8 +248,9 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
       return S2M_E_CUDA;
     }
   }
-  if (prune && cudaLibraryGetKernel(&s->k_tiles, s->lib, "s2m_tiles") != cudaSuccess) {
-    set_err(err, errlen, "kernel missing from the compiled module: s2m_tiles");
+  if (prune && (cudaLibraryGetKernel(&s->k_tiles, s->lib, "s2m_tiles") != cudaSuccess ||
+                cudaLibraryGetKernel(&s->k_tiles_coarse, s->lib, "s2m_tiles_coarse") != cudaSuccess)) {
+    set_err(err, errlen, "kernel missing from the compiled module: s2m_tiles / s2m_tiles_coarse");
     return S2M_E_CUDA;
   }
   if (cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
@@ -391,47 +396,64 @@ PruneGeom prune_geom(const S2Job &j, int nk) {
   return g;
 }
 
-// The tile pass runs over chunks of prune_chunk slabs, one launch each; the
+// The tile pass runs over chunks of prune_chunk slabs, two launches each; the
 // activity words of a chunk stay within kPruneBitsBudget (all slabs of the
 // job at once up to well beyond 1024^3).
 constexpr size_t kPruneBitsBudget = size_t(256) << 20;
 size_t prune_layout(s2m_mesh *m) {
   const int ns = m->nslabs;
   m->slab_tile_base.assign(size_t(ns) + 1, 0ull);
+  m->slab_coarse_base.assign(size_t(ns) + 1, 0ull);
+  const long long ntx = (m->job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const long long ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
   unsigned long long max_slab = 1;
   for (int s = 0; s < ns; ++s) {
     int k0, nk;
     slab_planes(m, s, k0, nk);
-    const unsigned long long t = (unsigned long long)prune_geom(m->job, nk).ntiles;
-    m->slab_tile_base[size_t(s) + 1] = m->slab_tile_base[size_t(s)] + t;
-    max_slab = std::max(max_slab, t);
+    const PruneGeom g = prune_geom(m->job, nk);
+    m->slab_tile_base[size_t(s) + 1] = m->slab_tile_base[size_t(s)] + (unsigned long long)g.ntiles;
+    m->slab_coarse_base[size_t(s) + 1] = m->slab_coarse_base[size_t(s)] + (unsigned long long)(ncx * ncx * g.nzt);
+    max_slab = std::max(max_slab, (unsigned long long)g.ntiles);
   }
   const size_t words = size_t(m->sdf->prune_words);
   m->prune_chunk = int(std::max<size_t>(1, std::min<size_t>(size_t(std::max(ns, 1)),
                                                             kPruneBitsBudget / (max_slab * words * 4))));
-  unsigned long long chunk_tiles = 0;
+  unsigned long long chunk_tiles = 0, chunk_coarse = 0;
   for (int s = 0; s < ns; s += m->prune_chunk) {
     const int e = std::min(ns, s + m->prune_chunk);
     chunk_tiles = std::max(chunk_tiles, m->slab_tile_base[size_t(e)] - m->slab_tile_base[size_t(s)]);
+    chunk_coarse = std::max(chunk_coarse, m->slab_coarse_base[size_t(e)] - m->slab_coarse_base[size_t(s)]);
   }
-  m->prune_base_off = (16 + 4 * size_t(ns) + 15) / 16 * 16;
-  m->prune_bits_off = (m->prune_base_off + 8 * (size_t(ns) + 1) + 15) / 16 * 16;
+  auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+  m->prune_base_off = up16(16 + 4 * size_t(ns));
+  m->prune_cbase_off = up16(m->prune_base_off + 8 * (size_t(ns) + 1));
+  m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
+  m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * words * 4);
   return m->prune_bits_off + size_t(chunk_tiles) * words * 4;
 }
-unsigned long long *prune_bases(const s2m_mesh *m) {
-  return reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(m->prune_buf) + m->prune_base_off);
+template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
+  return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
 }
+unsigned long long *prune_bases(const s2m_mesh *m) { return prune_at<unsigned long long>(m, m->prune_base_off); }
 unsigned *prune_counters(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
-// Tile pass over slabs [s_begin, s_end) and the pruned evaluation of slab s.
+// Tile pass over slabs [s_begin, s_end) (coarse boxes, then tiles) and the
+// pruned evaluation of slab s.
 cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t st) {
   S2Job jj = m->job;
-  unsigned *bits = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(m->prune_buf) + m->prune_bits_off);
+  unsigned *sbits = prune_at<unsigned>(m, m->prune_sbits_off);
+  unsigned *bits = prune_at<unsigned>(m, m->prune_bits_off);
   unsigned long long *ops = m->prune_buf;
-  const unsigned long long *base = prune_bases(m);
+  const unsigned long long *tbase = prune_at<unsigned long long>(m, m->prune_base_off);
+  const unsigned long long *cbase = prune_at<unsigned long long>(m, m->prune_cbase_off);
   int D = m->D, nzc = m->nzc;
+  const unsigned long long nc = m->slab_coarse_base[size_t(s_end)] - m->slab_coarse_base[size_t(s_begin)];
+  void *cargs[] = {&jj, &sbits, &cbase, &s_begin, &s_end, &D, &nzc};
+  cudaError_t e = cudaLaunchKernel((const void *)m->sdf->k_tiles_coarse,
+                                   dim3(unsigned((nc + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), cargs, 0, st);
+  if (e != cudaSuccess) return e;
   const unsigned long long n = m->slab_tile_base[size_t(s_end)] - m->slab_tile_base[size_t(s_begin)];
-  void *targs[] = {&jj, &bits, &ops, &base, &s_begin, &s_end, &D, &nzc};
+  void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc};
   return cudaLaunchKernel((const void *)m->sdf->k_tiles, dim3(unsigned((n + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
                           dim3(S2_PT_BLOCK), targs, 0, st);
 }
@@ -441,9 +463,8 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   int k0, nk;
   slab_planes(m, s, k0, nk);
   PruneGeom g = prune_geom(m->job, nk);
-  const unsigned *bits =
-      reinterpret_cast<const unsigned *>(reinterpret_cast<const char *>(m->prune_buf) + m->prune_bits_off) +
-      (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
+  const unsigned *bits = prune_at<unsigned>(m, m->prune_bits_off) +
+                        (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
   if (kEvalVariants[v].chunked) {
     unsigned *counter = prune_counters(m) + s;
     void *cargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
@@ -506,6 +527,8 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
     // pageable source: the call returns once the words are staged
     S2_CUDA(cudaMemcpyAsync(prune_bases(m), m->slab_tile_base.data(), m->slab_tile_base.size() * 8,
                             cudaMemcpyHostToDevice, st));
+    S2_CUDA(cudaMemcpyAsync(prune_at<unsigned long long>(m, m->prune_cbase_off), m->slab_coarse_base.data(),
+                            m->slab_coarse_base.size() * 8, cudaMemcpyHostToDevice, st));
   }
   S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cand_val, m->cand_cap * 32, st));
@@ -660,11 +683,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                 cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
     }
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
-    const unsigned long long np = (unsigned long long)(zc1 - zc0 + 1);
-    const unsigned long long bit_threads = np * (unsigned long long)j.P * (unsigned long long)((j.P + 31) / 32) * 32ull;
-    S2_LAUNCH(1, 0, (s2m_cells_bits<<<unsigned((bit_threads + 255) / 256), 256, 0, st>>>(j, m->ring, m->pt_bits, zc0,
-                                                                                          int(np)),
-                     cudaGetLastError()));
+    const dim3 bits_grid(unsigned((j.P + 31) / 32), unsigned((j.P + 7) / 8), unsigned(zc1 - zc0 + 1));
+    S2_LAUNCH(1, 0, (s2m_cells_bits<<<bits_grid, 256, 0, st>>>(j, m->ring, m->pt_bits, zc0), cudaGetLastError()));
     const unsigned long long nwords = (unsigned long long)(zc1 - zc0) * N * ((N + 31) / 32);
     const unsigned cg = unsigned((nwords + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
     S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->pt_bits, m->offx, m->cell_words, m->tile_cnt,

@@ -143,34 +143,89 @@ __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long
   return r;
 }
 
-// The tile pass of slabs s_begin .. s_end - 1 in one launch, one thread per
-// tile: interval evaluation over the tile's coordinate box, activity bits
-// (tile g of the job at bits[(g - slab_base[s_begin]) * W]), and the SDF
-// operations that remain (summed into ops[0] FP32, ops[1] SFU, per lattice
-// point).  One launch covers many slabs so that the grid fills the GPU.
-extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK)
+// The tile pass of slabs s_begin .. s_end - 1, in two launches of one thread
+// per box, each covering many slabs so that the grid fills the GPU:
+//   s2m_tiles_coarse  boxes of 4 x 4 tiles (32 x 32 points by the tile depth):
+//                     the full interval evaluation -> sbits
+//   s2m_tiles         each tile inside its coarse box: only the segments
+//                     active in the box are evaluated -> bits, and the SDF
+//                     operations that remain (ops[0] FP32, ops[1] SFU, per
+//                     lattice point)
+// Coarse box c of the job is at sbits[(c - cbase[s_begin]) * W], tile g at
+// bits[(g - tbase[s_begin]) * W]; cbase / tbase hold each slab's first index.
+__device__ __forceinline__ int s2_find_slab(const unsigned long long *base, int s_begin, int s_end,
+                                            unsigned long long g) {
+  int lo = s_begin, hi = s_end - 1;  // largest s with base[s] <= g
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
+s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long long *__restrict__ cbase, int s_begin,
+                 int s_end, int D, int nzc) {
+  const unsigned long long b0 = cbase[s_begin];
+  const unsigned long long c = b0 + (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
+  if (c >= cbase[s_end]) return;
+  const int s = s2_find_slab(cbase, s_begin, s_end, c);
+  int k0, nk;
+  s2_slab_planes(s, D, nzc, k0, nk);
+  const int tzs = s2_tile_depth(nk);
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
+  const long long lc = (long long)(c - cbase[s]);
+  const int cx = (int)(lc % ncx);
+  const long long q = lc / ncx;
+  const int cy = (int)(q % ncx);
+  const int tz = (int)(q / ncx);
+  const int span = S2_PT_XY * S2_PT_COARSE;
+  const int i0 = cx * span, i1 = min(i0 + span, job.P) - 1;
+  const int j0 = cy * span, j1 = min(j0 + span, job.P) - 1;
+  const int kb = k0 + tz * tzs, ke = min(kb + tzs, k0 + nk) - 1;
+  s2i X, Y, Z;
+  X.lo = s2_coord(job, i0); X.hi = s2_coord(job, i1);
+  Y.lo = s2_coord(job, j0); Y.hi = s2_coord(job, j1);
+  Z.lo = s2_coord(job, kb); Z.hi = s2_coord(job, max(kb, ke));
+  unsigned m[S2M_PRUNE_WORDS];
+  float fp, sfu;
+  s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);
+  unsigned *dst = sbits + (c - b0) * S2M_PRUNE_WORDS;
+#pragma unroll
+  for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
+}
+
+extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops,
-          const unsigned long long *__restrict__ slab_base, int s_begin, int s_end, int D, int nzc) {
-  const unsigned long long b0 = slab_base[s_begin], b1 = slab_base[s_end];
+          const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
+          const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc) {
+  const unsigned long long b0 = tbase[s_begin], b1 = tbase[s_end];
   const unsigned long long g = b0 + (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
   unsigned long long fp_ops = 0, sfu_ops = 0;
   if (g < b1) {
-    int lo = s_begin, hi = s_end - 1;  // the slab of tile g: largest s with slab_base[s] <= g
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (slab_base[mid] <= g) lo = mid;
-      else hi = mid - 1;
-    }
+    const int s = s2_find_slab(tbase, s_begin, s_end, g);
     int k0, nk;
-    s2_slab_planes(lo, D, nzc, k0, nk);
-    const S2PruneTile tl = s2_prune_tile(job, (long long)(g - slab_base[lo]), k0, nk, s2_tile_depth(nk));
+    s2_slab_planes(s, D, nzc, k0, nk);
+    const long long t = (long long)(g - tbase[s]);
+    const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, s2_tile_depth(nk));
+    const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+    const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
+    const int tx = (int)(t % ntx);
+    const long long q = t / ntx;
+    const int ty = (int)(q % ntx);
+    const int tz = (int)(q / ntx);
+    const unsigned long long c =
+        cbase[s] + ((unsigned long long)tz * ncx + ty / S2_PT_COARSE) * ncx + tx / S2_PT_COARSE;
+    const unsigned *pm = sbits + (c - cbase[s_begin]) * S2M_PRUNE_WORDS;
     s2i X, Y, Z;
     X.lo = s2_coord(job, tl.i0); X.hi = s2_coord(job, tl.i1);
     Y.lo = s2_coord(job, tl.j0); Y.hi = s2_coord(job, tl.j1);
-    Z.lo = s2_coord(job, tl.kb); Z.hi = s2_coord(job, tl.ke);
+    Z.lo = s2_coord(job, tl.kb); Z.hi = s2_coord(job, max(tl.kb, tl.ke));
     unsigned m[S2M_PRUNE_WORDS];
     float fp = 0.0f, sfu = 0.0f;
-    s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);
+    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu);
     unsigned *dst = bits + (g - b0) * S2M_PRUNE_WORDS;
 #pragma unroll
     for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];

@@ -31,24 +31,46 @@ __global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict_
 
 // Planes zc0 .. zc0 + np - 1 (slot p = plane zc0 + p): bits[(p * P + y) * WP + w]
 // holds points x = 32 w .. 32 w + 31 of row y (bits past the lattice are 0).
+// Grid (WP, ceil(P / 8), np), 8 warps per block, one row word per warp (no
+// index division).
 __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__restrict__ ring,
-                                                      uint2 *__restrict__ bits, int zc0, int np) {
+                                                      uint2 *__restrict__ bits, int zc0) {
   const int WP = (job.P + 31) >> 5;
-  const long long wi = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;  // the warp's word
-  if (wi >= (long long)np * job.P * WP) return;                           // whole warps
-  const int w = (int)(wi % WP);
-  const long long r = wi / WP;
-  const int y = (int)(r % job.P);
-  const int p = (int)(r / job.P);
+  const int w = (int)blockIdx.x, p = (int)blockIdx.z;
+  const int y = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  if (y >= job.P) return;  // whole warps
   const int x = w * 32 + (int)(threadIdx.x & 31u);
   const bool in = x < job.P;
   const float v = in ? __ldg(ring + (long long)((zc0 + p) % job.ring) * job.plane + (long long)y * job.pitch + x) : 0.0f;
   const unsigned pos = __ballot_sync(S2_FULL, in && v > 0.0f);
   const unsigned near = __ballot_sync(S2_FULL, in && !(fabsf(v) >= job.guard));
-  if ((threadIdx.x & 31u) == 0) bits[wi] = make_uint2(pos, near);
+  if ((threadIdx.x & 31u) == 0) bits[((long long)p * job.P + y) * WP + w] = make_uint2(pos, near);
 }
 
 // Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.
+// Its coordinates from the block's first word (one 64-bit division per
+// block; 32-bit ones per thread).
+struct S2CellWord {
+  int w, y, dz;
+};
+__device__ __forceinline__ S2CellWord s2_cell_word(const S2Job &job, int WN) {
+  __shared__ unsigned long long s_row0;
+  __shared__ int s_w0;
+  const unsigned long long l0 = (unsigned long long)blockIdx.x * S2_CW_BLOCK;
+  if (threadIdx.x == 0) {
+    s_row0 = l0 / (unsigned long long)WN;
+    s_w0 = (int)(l0 - s_row0 * (unsigned long long)WN);
+  }
+  __syncthreads();
+  const unsigned q = (unsigned)s_w0 + threadIdx.x;  // < WN + S2_CW_BLOCK
+  const unsigned row = (unsigned)s_row0 + q / (unsigned)WN;  // < slab depth * N < 2^32
+  S2CellWord c;
+  c.w = (int)(q % (unsigned)WN);
+  c.y = (int)(row % (unsigned)job.N);
+  c.dz = (int)(row / (unsigned)job.N);
+  return c;
+}
+
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, const uint2 *__restrict__ bits,
                                                             const unsigned *__restrict__ offx,
                                                             unsigned *__restrict__ words,
@@ -57,12 +79,10 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, const u
   const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5;
   const long long nw = (long long)(zc1 - zc0) * job.N * WN;
   const long long l = (long long)blockIdx.x * S2_CW_BLOCK + threadIdx.x;
+  const S2CellWord cw = s2_cell_word(job, WN);
   unsigned cand = 0;
   if (l < nw) {
-    const int w = (int)(l % WN);
-    const long long r = l / WN;
-    const int y = (int)(r % job.N);
-    const int dz = (int)(r / job.N);
+    const int w = cw.w, y = cw.y, dz = cw.dz;
     // corner k = bx | by << 1 | bz << 2 lies in point row q = by | bz << 1
     // (k = 2 q + bx); bx = 1 takes the row's bits shifted by one point
     unsigned pb[8], nb[8];
@@ -152,7 +172,9 @@ __global__ void __launch_bounds__(1024) s2m_cells_offsets(const unsigned *__rest
 }
 
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
-// 8 lattice corner values.
+// 8 lattice corner values.  A warp takes its words with candidates one at a
+// time, lane l writing the cell of bit l: the corner loads of a word's cells
+// are then coalesced rows, and every lane works.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
@@ -162,6 +184,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
   const int WN = (job.N + 31) >> 5;
   const long long nw = (long long)(zc1 - zc0) * job.N * WN;
   const long long l = (long long)blockIdx.x * S2_CW_BLOCK + tid;
+  const S2CellWord cw = s2_cell_word(job, WN);
   const unsigned mask = l < nw ? words[l] : 0u;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
@@ -175,30 +198,28 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
   __syncthreads();
   if (warp == 0) s2_warp_exclusive32(s_warp);
   __syncthreads();
-  if (!mask) return;
-  unsigned long long o = tile_off[blockIdx.x] + s_warp[warp] + (inc - cnt);
-  const int w = (int)(l % WN);
-  const long long r = l / WN;
-  S2Cell cell;
-  cell.y = (int)(r % job.N);
-  cell.z = zc0 + (int)(r / job.N);
-  unsigned rem = mask;
-  while (rem) {
-    const int b = __ffs(rem) - 1;
-    rem &= rem - 1u;
+  const unsigned long long first = tile_off[blockIdx.x] + s_warp[warp] + (inc - cnt);
+  unsigned todo = __ballot_sync(S2_FULL, mask != 0u);
+  while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1u;
+    const unsigned m = __shfl_sync(S2_FULL, mask, src);
+    const unsigned long long o = __shfl_sync(S2_FULL, first, src) + __popc(m & ((1u << lane) - 1u));
+    S2Cell cell;
+    cell.x = 32 * __shfl_sync(S2_FULL, cw.w, src) + (int)lane;
+    cell.y = __shfl_sync(S2_FULL, cw.y, src);
+    cell.z = zc0 + __shfl_sync(S2_FULL, cw.dz, src);
+    if (!((m >> lane) & 1u)) continue;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
-      ++o;
       continue;
     }
-    cell.x = 32 * w + b;
     float v[8];
     s2_load_corners<false>(job, ring, cell, v);
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
     float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
     dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-    ++o;
   }
 }
 

@@ -56,6 +56,19 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
                 '      for (int w = 0; w < 4; ++w) { full4[t * npts + p + w] = s2m_user_sdf(q[0], q[1], z.v[w]);\n'
                 '        pruned4[t * npts + p + w] = f.v[w]; } }\n'
                 '  }\n  return S2M_PRUNE_WORDS;\n}\n'
+                'extern "C" void prune_tiles_in(long ntiles, const float* pbox, const float* box, int npts,\n'
+                '                               const float* pts, float* ops, float* pruned) {\n'
+                '  for (long t = 0; t < ntiles; ++t) {\n'
+                '    s2i X, Y, Z; X.lo = pbox[6*t]; X.hi = pbox[6*t+1]; Y.lo = pbox[6*t+2]; Y.hi = pbox[6*t+3];\n'
+                '    Z.lo = pbox[6*t+4]; Z.hi = pbox[6*t+5];\n'
+                '    unsigned pm[S2M_PRUNE_WORDS], m[S2M_PRUNE_WORDS]; float fp, sfu;\n'
+                '    s2m_user_sdf_tile(X, Y, Z, pm, &fp, &sfu);\n'
+                '    X.lo = box[6*t]; X.hi = box[6*t+1]; Y.lo = box[6*t+2]; Y.hi = box[6*t+3]; Z.lo = box[6*t+4]; Z.hi = box[6*t+5];\n'
+                '    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu);\n'
+                '    ops[2*t] = fp; ops[2*t+1] = sfu;\n'
+                '    for (int p = 0; p < npts; ++p) { const float* q = pts + 3 * (t * npts + p);\n'
+                '      pruned[t * npts + p] = s2m_user_sdf_pruned(q[0], q[1], q[2], m); }\n'
+                '  }\n}\n'
                 '#else\nextern "C" int prune_tiles(long, const float*, int, const float*, unsigned*, float*, float*,\n'
                 '                           float*, float*, float*) { return 0; }\n#endif\n')
     so = os.path.join(d, "sdf.so")
@@ -66,6 +79,8 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
     L.normal_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
     L.eval_run4.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
     L.prune_tiles.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 7
+    if hasattr(L, "prune_tiles_in"):
+        L.prune_tiles_in.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
     _cache[key] = L
     return L
 
@@ -88,7 +103,7 @@ def eval_run4_host(cuda_src: str, xyz: np.ndarray):
     return out
 
 
-def lattice_tiles(N: int, bounds: float, tiles=None, T: int = 8):
+def lattice_tiles(N: int, bounds: float, tiles=None, T: int = 8, with_parents: bool = False):
     """Tiles of T^3 lattice points (clipped at the lattice edge) of an N-cell
     job: their coordinate boxes (6 floats) and their points (padded to T^3
     by repeating), computed in binary32 as the kernels do: bmin + size * i
@@ -103,13 +118,19 @@ def lattice_tiles(N: int, bounds: float, tiles=None, T: int = 8):
     if tiles is None:
         nt = (P + T - 1) // T
         tiles = [(a, b, c) for a in range(nt) for b in range(nt) for c in range(nt)]
-    boxes, pts = [], []
+    boxes, pts, parents = [], [], []
+    C = 4 * T  # coarse boxes of 4 x 4 tiles (the tile pass's first level)
     for (a, b, c) in tiles:
         ii = np.arange(a * T, min(a * T + T, P)); jj = np.arange(b * T, min(b * T + T, P))
         kk = np.arange(c * T, min(c * T + T, P))
         g = np.stack(np.meshgrid(coord(ii), coord(jj), coord(kk), indexing="ij"), -1).reshape(-1, 3)
         boxes.append([coord(ii[0]), coord(ii[-1]), coord(jj[0]), coord(jj[-1]), coord(kk[0]), coord(kk[-1])])
+        pi0, pj0 = (a * T) // C * C, (b * T) // C * C
+        parents.append([coord(pi0), coord(min(pi0 + C, P) - 1), coord(pj0), coord(min(pj0 + C, P) - 1),
+                        coord(kk[0]), coord(kk[-1])])
         pts.append(np.resize(g, (T ** 3, 3)))
+    if with_parents:
+        return np.array(boxes, np.float32), np.array(pts, np.float32), np.array(parents, np.float32)
     return np.array(boxes, np.float32), np.array(pts, np.float32)
 
 
@@ -131,3 +152,18 @@ def prune_host(cuda_src: str, boxes: np.ndarray, pts: np.ndarray):
     w = L.prune_tiles(nt, boxes.ctypes.data, npts, pts.ctypes.data, bits.ctypes.data, ops.ctypes.data,
                       full.ctypes.data, pruned.ctypes.data, full4.ctypes.data, pruned4.ctypes.data)
     return w, ops, full, pruned, full4, pruned4
+
+
+def prune_host_in(cuda_src: str, parents: np.ndarray, boxes: np.ndarray, pts: np.ndarray):
+    """The two-level tile pass on the host: bits of each parent box, then the
+    tile's bits from them (s2m_user_sdf_tile_in); (ops per tile, pruned values)."""
+    L = compile_host(cuda_src)
+    nt, npts = len(boxes), pts.shape[1]
+    parents = np.ascontiguousarray(parents, np.float32)
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    pts = np.ascontiguousarray(pts, np.float32)
+    ops = np.zeros((nt, 2), np.float32)
+    pruned = np.zeros((nt, npts), np.float32)
+    L.prune_tiles_in(nt, parents.ctypes.data, boxes.ctypes.data, npts, pts.ctypes.data, ops.ctypes.data,
+                     pruned.ctypes.data)
+    return ops, pruned

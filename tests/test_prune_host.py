@@ -10,7 +10,7 @@ import pytest
 import sdf2mesh_gb300 as s2m
 from sdf2mesh_gb300 import workloads
 
-from hostsdf import lattice_tiles, prune_host
+from hostsdf import lattice_tiles, prune_host, prune_host_in
 
 
 def lowered(src, lang=s2m.LANG_WGSL, name="sdf"):
@@ -24,13 +24,18 @@ def check(cu, N, bounds=2.0, tiles=None, seed=0, count=None):
         rng = np.random.default_rng(seed)
         nt = (N + 1 + 7) // 8
         tiles = [tuple(int(v) for v in rng.integers(0, nt, 3)) for _ in range(count)]
-    boxes, pts = lattice_tiles(N, bounds, tiles)
+    boxes, pts, parents = lattice_tiles(N, bounds, tiles, with_parents=True)
     w, ops, full, pruned, full4, pruned4 = prune_host(cu, boxes, pts)
     assert w > 0, "no pruning form"
     bad = full.view(np.uint32) != pruned.view(np.uint32)
     assert not bad.any(), f"{int(bad.sum())} pruned values differ, e.g. tile {np.argwhere(bad)[0]}"
     bad4 = full4.view(np.uint32) != pruned4.view(np.uint32)
     assert not bad4.any(), f"{int(bad4.sum())} run-of-4 pruned values differ, e.g. {np.argwhere(bad4)[0]}"
+    # two-level tile pass: the tile's bits from its coarse box's bits
+    ops_in, pruned_in = prune_host_in(cu, parents, boxes, pts)
+    bad_in = full.view(np.uint32) != pruned_in.view(np.uint32)
+    assert not bad_in.any(), f"{int(bad_in.sum())} values differ with two-level bits, e.g. {np.argwhere(bad_in)[0]}"
+    assert (ops_in[:, 0] <= ops[:, 0] + 0.5).all()  # a coarse decision is never undone
     return ops
 
 
