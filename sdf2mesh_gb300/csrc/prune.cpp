@@ -231,6 +231,9 @@ class Pruner {
     }
   }
 
+  // The scalar pruned code calls the out-of-line smooth operators.
+  std::string call_sfx() const { return run4_ ? "" : "_call"; }
+
   // Point expression of a node (combinators: their full arithmetic).  In the
   // run-of-4 form a node that varies with z is an s2x4 and its builtins are
   // the lane-wise s2r_ forms (the same operations per lane).
@@ -263,9 +266,9 @@ class Pruner {
       case POp::Log: return "s2_log(" + A + ")";
       case POp::Pow: return "s2_pow(" + A + ", " + B + ")";
       case POp::Atan2: return "s2_atan2(" + A + ", " + B + ")";
-      case POp::SmoothUnion: return "s2_op_smooth_union(" + A + ", " + B + ", " + C + ")";
-      case POp::SmoothIntersection: return "s2_op_smooth_intersection(" + A + ", " + B + ", " + C + ")";
-      case POp::SmoothSubtraction: return "s2_op_smooth_subtraction(" + A + ", " + B + ", " + C + ")";
+      case POp::SmoothUnion: return "s2_op_smooth_union" + call_sfx() + "(" + A + ", " + B + ", " + C + ")";
+      case POp::SmoothIntersection: return "s2_op_smooth_intersection" + call_sfx() + "(" + A + ", " + B + ", " + C + ")";
+      case POp::SmoothSubtraction: return "s2_op_smooth_subtraction" + call_sfx() + "(" + A + ", " + B + ", " + C + ")";
       default: return "";
     }
   }
@@ -384,6 +387,23 @@ class Pruner {
   static std::string ptest(int bit) {
     return "(pm[" + std::to_string(bit >> 5) + "] >> " + std::to_string(bit & 31) + " & 1u)";
   }
+  void emit_tile_combinator(std::ostringstream &o, int v, const std::vector<std::vector<int>> &members,
+                            const std::string &ind) const {
+    const int ci = comb_of_[size_t(v)];
+    const PNode &p = nd(v);
+    const int sa = seg(ci, 0), sb = seg(ci, 1);
+    const std::string keepA = p.op == POp::SmoothSubtraction ? "s2i_neg(" + ival(p.a) + ")" : ival(p.a);
+    o << ind << "if " << ptest(sb - 1) << " {\n";
+    emit_tile_region(o, sb, members, ind + "  ");
+    o << ind << "  if " << ptest(sa - 1) << " i" << v << " = " << iexpr(v) << ";\n";
+    o << ind << "  else { i" << v << " = " << ival(p.b) << "; d" << v << " = 2; }\n";
+    o << ind << "} else if " << ptest(sa - 1) << " {\n";
+    o << ind << "  i" << v << " = " << keepA << "; d" << v << " = 1;\n" << ind << "}\n";
+  }
+
+  // Chains as in the point code: a chunk whose operand-b bits are all clear
+  // in pm keeps operand a throughout (d = 1 for each combinator; one that is
+  // not needed has d unused, and d = 1 leaves its operands inactive).
   void emit_tile_region(std::ostringstream &o, int R, const std::vector<std::vector<int>> &members,
                         const std::string &ind) const {
     int open = R;
@@ -391,19 +411,35 @@ class Pruner {
       if (open != R) o << ind << "}\n";
       open = R;
     };
-    for (int v : members[size_t(R)]) {
+    const std::vector<int> &mem = members[size_t(R)];
+    for (size_t idx = 0; idx < mem.size(); ++idx) {
+      const int v = mem[idx];
       const int ci = comb_of_[size_t(v)];
       if (ci >= 0) {
         close();
-        const PNode &p = nd(v);
-        const int sa = seg(ci, 0), sb = seg(ci, 1);
-        const std::string keepA = p.op == POp::SmoothSubtraction ? "s2i_neg(" + ival(p.a) + ")" : ival(p.a);
-        o << ind << "if " << ptest(sb - 1) << " {\n";
-        emit_tile_region(o, sb, members, ind + "  ");
-        o << ind << "  if " << ptest(sa - 1) << " i" << v << " = " << iexpr(v) << ";\n";
-        o << ind << "  else { i" << v << " = " << ival(p.b) << "; d" << v << " = 2; }\n";
-        o << ind << "} else if " << ptest(sa - 1) << " {\n";
-        o << ind << "  i" << v << " = " << keepA << "; d" << v << " = 1;\n" << ind << "}\n";
+        size_t end = idx + 1;
+        if (chain_link(-1, v))
+          while (end < mem.size() && chain_link(mem[end - 1], mem[end])) ++end;
+        if (end - idx < 4) {
+          emit_tile_combinator(o, v, members, ind);
+          continue;
+        }
+        for (size_t c0 = idx; c0 < end; c0 += kChainChunk) {
+          const size_t c1 = std::min(end, c0 + size_t(kChainChunk));
+          std::ostringstream test;
+          for (auto &[w, msk] : chunk_b_words(mem, c0, c1)) {
+            char hx[16];
+            std::snprintf(hx, sizeof hx, "%xu", msk);
+            test << (test.tellp() > 0 ? " | " : "") << "(pm[" << w << "] & 0x" << hx << ")";
+          }
+          o << ind << "if (" << test.str() << ") {\n";
+          for (size_t k = c0; k < c1; ++k) emit_tile_combinator(o, mem[k], members, ind + "  ");
+          o << ind << "} else {\n";
+          o << ind << "  i" << mem[c1 - 1] << " = " << ival(nd(mem[c0]).a) << ";\n";
+          for (size_t k = c0; k < c1; ++k) o << ind << "  d" << mem[k] << " = 1;\n";
+          o << ind << "}\n";
+        }
+        idx = end - 1;
         continue;
       }
       const int s = owner_[size_t(v)];
@@ -449,6 +485,15 @@ class Pruner {
   // keeps operand a and the chunk's result is its input.  (Not for the smooth
   // subtraction, whose "keep a" is -a.)
   static constexpr int kChainChunk = 8;
+  // operand-b bits of the combinators mem[c0, c1), by word
+  std::map<int, unsigned> chunk_b_words(const std::vector<int> &mem, size_t c0, size_t c1) const {
+    std::map<int, unsigned> words;
+    for (size_t k = c0; k < c1; ++k) {
+      const int bit = seg(comb_of_[size_t(mem[k])], 1) - 1;
+      words[bit >> 5] |= 1u << (bit & 31);
+    }
+    return words;
+  }
   bool chain_link(int prev, int v) const {
     const int ci = comb_of_[size_t(v)];
     if (ci < 0 || nd(v).op == POp::SmoothSubtraction) return false;
@@ -478,13 +523,8 @@ class Pruner {
         }
         for (size_t c0 = idx; c0 < end; c0 += kChainChunk) {
           const size_t c1 = std::min(end, c0 + size_t(kChainChunk));
-          std::map<int, unsigned> words;  // operand-b bits of the chunk by word
-          for (size_t k = c0; k < c1; ++k) {
-            const int bit = seg(comb_of_[size_t(mem[k])], 1) - 1;
-            words[bit >> 5] |= 1u << (bit & 31);
-          }
           std::ostringstream test;
-          for (auto &[w, msk] : words) {
+          for (auto &[w, msk] : chunk_b_words(mem, c0, c1)) {
             char hx[16];
             std::snprintf(hx, sizeof hx, "%xu", msk);
             test << (test.tellp() > 0 ? " | " : "") << "(m[" << w << "] & 0x" << hx << ")";

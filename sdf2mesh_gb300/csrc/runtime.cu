@@ -683,7 +683,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                 cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
     }
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
-    const dim3 bits_grid(unsigned((j.P + 31) / 32), unsigned((j.P + 7) / 8), unsigned(zc1 - zc0 + 1));
+    const dim3 bits_grid(unsigned((j.P + 7) / 8), unsigned(zc1 - zc0 + 1));
     S2_LAUNCH(1, 0, (s2m_cells_bits<<<bits_grid, 256, 0, st>>>(j, m->ring, m->pt_bits, zc0), cudaGetLastError()));
     const unsigned long long nwords = (unsigned long long)(zc1 - zc0) * N * ((N + 31) / 32);
     const unsigned cg = unsigned((nwords + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
@@ -698,7 +698,12 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
-  void *vargs[] = {&jj, &cand, &nslabs};
+  // the lattice evaluation's tile bits, when every slab's are still resident
+  const unsigned *tbits = (pruned && m->prune_chunk >= m->nslabs && !j.qef) ? prune_at<unsigned>(m, m->prune_bits_off)
+                                                                             : nullptr;
+  const unsigned long long *tbase = m->prune_buf ? prune_at<unsigned long long>(m, m->prune_base_off) : nullptr;
+  int D = m->D, nzc = m->nzc;
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc};
   const unsigned vx_grid = unsigned(sms) * 16;
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));

@@ -484,6 +484,15 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
 // order of the normal sum as s2_vertex: the same bits.  F::kStdNormal says
 // whether F's normal is the library's tetrahedral one (otherwise, and in
 // precision mode, the per-lane s2_vertex path runs).
+// The SDF at a point requested by lane l of the warp (s2_vertex_warp
+// evaluates other lanes' requests): plain evaluators ignore l; an evaluator
+// with per-lane state (the tile-pruned one) overloads this.
+template <class F>
+__device__ __forceinline__ float s2_sdf_for(const F &f, unsigned l, float x, float y, float z) {
+  (void)l;
+  return f(x, y, z);
+}
+
 struct S2WarpScratch {
   unsigned short req[32 * 8];
   float val[32][8];
@@ -531,7 +540,7 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
       const float x = (k & 1) ? ws.hi[l][0] : ws.lo[l][0];
       const float y = (k & 2) ? ws.hi[l][1] : ws.lo[l][1];
       const float z = (k & 4) ? ws.hi[l][2] : ws.lo[l][2];
-      ws.val[l][k] = sdf(x, y, z);
+      ws.val[l][k] = s2_sdf_for(sdf, l, x, y, z);
     }
   }
   __syncwarp();
@@ -591,8 +600,8 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
       const float dx = (d == 0 || d == 3) ? 1.0f : -1.0f;
       const float dy = (d >= 2) ? 1.0f : -1.0f;
       const float dz = (d == 1 || d == 3) ? 1.0f : -1.0f;
-      ws.nv[l][d] = sdf(__fadd_rn(ws.pos[l][0], __fmul_rn(dx, j.eps)), __fadd_rn(ws.pos[l][1], __fmul_rn(dy, j.eps)),
-                        __fadd_rn(ws.pos[l][2], __fmul_rn(dz, j.eps)));
+      ws.nv[l][d] = s2_sdf_for(sdf, l, __fadd_rn(ws.pos[l][0], __fmul_rn(dx, j.eps)),
+                               __fadd_rn(ws.pos[l][1], __fmul_rn(dy, j.eps)), __fadd_rn(ws.pos[l][2], __fmul_rn(dz, j.eps)));
     }
   }
   __syncwarp();

@@ -153,6 +153,24 @@ __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long
 //                     lattice point)
 // Coarse box c of the job is at sbits[(c - cbase[s_begin]) * W], tile g at
 // bits[(g - tbase[s_begin]) * W]; cbase / tbase hold each slab's first index.
+// Coordinate range of a tile's box along one axis: lattice indices a .. b,
+// widened by a margin.  The boxes reach one lattice point past the tile's
+// points in +x, +y and -z, and the margin (more than the normal epsilon plus
+// thousands of ulps of the coordinates) covers every point the vertex kernel
+// evaluates for the cells whose tile this is (cell x in [i0, i1] spans points
+// x .. x + 1; cell z with plane z + 1 in the tile spans z .. z + 1): the
+// off-lattice corners mn + size and the normal samples p +/- eps around a
+// vertex inside its cell.  So the bits serve both the lattice evaluation and
+// the vertices.
+__device__ __forceinline__ s2i s2_prune_box(const S2Job &job, int a, int b) {
+  const float mg = __fadd_rn(__fmul_rn(fabsf(job.eps), 1.0625f),
+                             __fmul_rn(__fadd_rn(fabsf(job.bmin), fabsf(job.size)), 0x1p-12f));
+  s2i r;
+  r.lo = __fsub_rn(s2_coord(job, a), mg);
+  r.hi = __fadd_rn(s2_coord(job, b), mg);
+  return r;
+}
+
 __device__ __forceinline__ int s2_find_slab(const unsigned long long *base, int s_begin, int s_end,
                                             unsigned long long g) {
   int lo = s_begin, hi = s_end - 1;  // largest s with base[s] <= g
@@ -185,10 +203,7 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   const int i0 = cx * span, i1 = min(i0 + span, job.P) - 1;
   const int j0 = cy * span, j1 = min(j0 + span, job.P) - 1;
   const int kb = k0 + tz * tzs, ke = min(kb + tzs, k0 + nk) - 1;
-  s2i X, Y, Z;
-  X.lo = s2_coord(job, i0); X.hi = s2_coord(job, i1);
-  Y.lo = s2_coord(job, j0); Y.hi = s2_coord(job, j1);
-  Z.lo = s2_coord(job, kb); Z.hi = s2_coord(job, max(kb, ke));
+  const s2i X = s2_prune_box(job, i0, i1 + 1), Y = s2_prune_box(job, j0, j1 + 1), Z = s2_prune_box(job, kb - 1, max(kb, ke));
   unsigned m[S2M_PRUNE_WORDS];
   float fp, sfu;
   s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);
@@ -219,10 +234,8 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
     const unsigned long long c =
         cbase[s] + ((unsigned long long)tz * ncx + ty / S2_PT_COARSE) * ncx + tx / S2_PT_COARSE;
     const unsigned *pm = sbits + (c - cbase[s_begin]) * S2M_PRUNE_WORDS;
-    s2i X, Y, Z;
-    X.lo = s2_coord(job, tl.i0); X.hi = s2_coord(job, tl.i1);
-    Y.lo = s2_coord(job, tl.j0); Y.hi = s2_coord(job, tl.j1);
-    Z.lo = s2_coord(job, tl.kb); Z.hi = s2_coord(job, max(tl.kb, tl.ke));
+    const s2i X = s2_prune_box(job, tl.i0, tl.i1 + 1), Y = s2_prune_box(job, tl.j0, tl.j1 + 1),
+              Z = s2_prune_box(job, tl.kb - 1, max(tl.kb, tl.ke));
     unsigned m[S2M_PRUNE_WORDS];
     float fp = 0.0f, sfu = 0.0f;
     s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu);
@@ -359,13 +372,54 @@ S2_EVALPC_VARIANT(s2m_evalpc_b2v4, 2, true)
 
 
 
+#if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
+// The SDF for the vertex kernel with the lattice evaluation's tile bits:
+// lane l's requests use the bits of lane l's cell (the tile boxes cover the
+// corners and normal samples of their cells), or the full SDF when it has
+// none.
+struct S2UserSdfPruned {
+  static constexpr bool kStdNormal = S2UserSdfCall::kStdNormal;
+  const unsigned *const *mp;  // per lane of the block
+  __device__ __forceinline__ float operator()(float x, float y, float z) const { return s2_user_sdf_call(x, y, z); }
+  __device__ __forceinline__ float at(unsigned l, float x, float y, float z) const {
+    const unsigned *m = mp[(threadIdx.x & ~31u) + l];
+    return m ? s2m_user_sdf_pruned(x, y, z, m) : s2_user_sdf_call(x, y, z);
+  }
+};
+__device__ __forceinline__ float s2_sdf_for(const S2UserSdfPruned &f, unsigned l, float x, float y, float z) {
+  return f.at(l, x, y, z);
+}
+
+// The activity bits of the tile of cell c (all slabs' tiles in one buffer).
+__device__ __forceinline__ const unsigned *s2_cell_bits(const S2Job &job, S2Cell c, const unsigned *tbits,
+                                                        const unsigned long long *tbase, int D, int nzc) {
+  const int s = c.z / D;
+  int k0, nk;
+  s2_slab_planes(s, D, nzc, k0, nk);
+  const int tz = (c.z + 1 - k0) / s2_tile_depth(nk);
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const unsigned long long t = ((unsigned long long)tz * ntx + c.y / S2_PT_XY) * ntx + c.x / S2_PT_XY;
+  return tbits + (tbase[s] + t - tbase[0]) * S2M_PRUNE_WORDS;
+}
+#endif
+
 // Vertices of every candidate of the job, one candidate per thread (dense:
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
-// final key and writes cand.pos / cand.nrm for cells with a vertex.
+// final key and writes cand.pos / cand.nrm for cells with a vertex.  With
+// tbits (tile pruning, every slab's bits resident), the SDF evaluations use
+// the bits of each cell's tile.
 extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
-s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
+s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
+             int nzc) {
   __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
+#if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
+  __shared__ const unsigned *s_mp[S2_VX_BLOCK];
+  S2UserSdfPruned psdf;
+  psdf.mp = s_mp;
+#else
+  (void)tbits; (void)tbase; (void)D; (void)nzc;
+#endif
   const S2UserSdfCall sdf;
   // grid-stride over warp-sized runs of candidates, all lanes together
   const unsigned long long stride = (unsigned long long)gridDim.x * S2_VX_BLOCK;
@@ -390,6 +444,14 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs) {
     // precision-mode module (compiled on the first QEF job of this SDF)
     key = active ? s2_vertex_qef(sdf, job, c, v, pos, nrm) : 0ull;
 #else
+#ifdef S2M_HAS_PRUNE
+    if (S2UserSdfCall::kStdNormal && tbits) {
+      s_mp[threadIdx.x] = active ? s2_cell_bits(job, c, tbits, tbase, D, nzc) : nullptr;
+      __syncwarp();
+      key = s2_vertex_warp(psdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
+      __syncwarp();
+    } else
+#endif
     if (S2UserSdfCall::kStdNormal) key = s2_vertex_warp(sdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
     else key = active ? s2_vertex(sdf, job, c, v, pos, nrm) : 0ull;
 #endif

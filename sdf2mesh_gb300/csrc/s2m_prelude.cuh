@@ -276,6 +276,15 @@ S2HD float s2_op_smooth_subtraction(float a, float b, float k) {
   const float h = s2_clamp(0.5f - 0.5f * (b + a) / k, 0.0f, 1.0f);
   return s2_mix(b, -a, h) + k * h * (1.0f - h);
 }
+// Out-of-line copies for the pruned code: one body each instead of one per
+// combinator keeps its code (and instruction-cache footprint) small.
+S2M_PRUNED_FN float s2_op_smooth_union_call(float a, float b, float k) { return s2_op_smooth_union(a, b, k); }
+S2M_PRUNED_FN float s2_op_smooth_intersection_call(float a, float b, float k) {
+  return s2_op_smooth_intersection(a, b, k);
+}
+S2M_PRUNED_FN float s2_op_smooth_subtraction_call(float a, float b, float k) {
+  return s2_op_smooth_subtraction(a, b, k);
+}
 
 // ---------------------------------------------------------------------------
 // Intervals for tile pruning.  [lo, hi] bounds the binary32 value that the

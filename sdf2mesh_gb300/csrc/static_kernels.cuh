@@ -31,20 +31,26 @@ __global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict_
 
 // Planes zc0 .. zc0 + np - 1 (slot p = plane zc0 + p): bits[(p * P + y) * WP + w]
 // holds points x = 32 w .. 32 w + 31 of row y (bits past the lattice are 0).
-// Grid (WP, ceil(P / 8), np), 8 warps per block, one row word per warp (no
-// index division).
+// Grid (ceil(P / 8), np), 8 warps per block, one row per warp: the warp walks
+// the row's words (a 128-byte load and two ballots each).
 __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__restrict__ ring,
                                                       uint2 *__restrict__ bits, int zc0) {
   const int WP = (job.P + 31) >> 5;
-  const int w = (int)blockIdx.x, p = (int)blockIdx.z;
-  const int y = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  const int p = (int)blockIdx.y;
+  const int y = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5);
   if (y >= job.P) return;  // whole warps
-  const int x = w * 32 + (int)(threadIdx.x & 31u);
-  const bool in = x < job.P;
-  const float v = in ? __ldg(ring + (long long)((zc0 + p) % job.ring) * job.plane + (long long)y * job.pitch + x) : 0.0f;
-  const unsigned pos = __ballot_sync(S2_FULL, in && v > 0.0f);
-  const unsigned near = __ballot_sync(S2_FULL, in && !(fabsf(v) >= job.guard));
-  if ((threadIdx.x & 31u) == 0) bits[((long long)p * job.P + y) * WP + w] = make_uint2(pos, near);
+  const int lane = (int)(threadIdx.x & 31u);
+  const float *row = ring + (long long)((zc0 + p) % job.ring) * job.plane + (long long)y * job.pitch;
+  uint2 *dst = bits + ((long long)p * job.P + y) * WP;
+#pragma unroll 4
+  for (int w = 0; w < WP; ++w) {
+    const int x = w * 32 + lane;
+    const bool in = x < job.P;
+    const float v = in ? __ldg(row + x) : 0.0f;
+    const unsigned pos = __ballot_sync(S2_FULL, in && v > 0.0f);
+    const unsigned near = __ballot_sync(S2_FULL, in && !(fabsf(v) >= job.guard));
+    if (lane == 0) dst[w] = make_uint2(pos, near);
+  }
 }
 
 // Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.

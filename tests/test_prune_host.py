@@ -121,7 +121,7 @@ fn sdf3d(p: vec3f) -> f32 {
 }
 """
     cu, _, _ = lowered(src)
-    assert "s2_op_smooth_union(" in cu
+    assert "s2_op_smooth_union_call(" in cu
     check(cu, 64, count=200)
 
 
