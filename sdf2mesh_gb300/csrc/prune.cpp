@@ -231,13 +231,21 @@ class Pruner {
     }
   }
 
-  // The scalar pruned code calls the out-of-line smooth operators.
-  std::string call_sfx() const { return run4_ ? "" : "_call"; }
+  // The pruned code calls the out-of-line smooth operators.
+  std::string call_sfx() const { return "_call"; }
 
   // Point expression of a node (combinators: their full arithmetic).  In the
   // run-of-4 form a node that varies with z is an s2x4 and its builtins are
   // the lane-wise s2r_ forms (the same operations per lane).
   std::string expr(int v) const {
+    const PNode &p = nd(v);
+    if (run4_ && var_[size_t(v)] &&
+        (p.op == POp::SmoothUnion || p.op == POp::SmoothIntersection || p.op == POp::SmoothSubtraction)) {
+      const char *f = p.op == POp::SmoothUnion ? "s2r_op_smooth_union_call"
+                      : p.op == POp::SmoothIntersection ? "s2r_op_smooth_intersection_call"
+                                                        : "s2r_op_smooth_subtraction_call";
+      return std::string(f) + "(" + as_var(p.a, true) + ", " + as_var(p.b, true) + ", " + as_var(p.c, true) + ")";
+    }
     std::string e = expr_scalar(v);
     if (run4_ && var_[size_t(v)] && e.compare(0, 3, "s2_") == 0) e = "s2r_" + e.substr(3);
     return e;

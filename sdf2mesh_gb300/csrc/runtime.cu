@@ -91,7 +91,7 @@ constexpr EvalVariant kEvalVariants[] = {
     {"s2m_eval_b2r4", 4, false, false, false}, {"s2m_eval_b3r4", 4, false, false, false},
     {"s2m_eval_b4r4", 4, false, false, false}, {"s2m_eval_b2v4", 4, true, false, false},
     {"s2m_eval_b3v4", 4, true, false, false},  {"s2m_evalp_b8", 1, false, true, false},
-    {"s2m_evalpc_b2", 1, false, true, true},   {"s2m_evalpc_b2v4", 4, true, true, true}};
+    {"s2m_evalp_b8v4", 4, true, true, false},  {"s2m_evalpc_b2", 1, false, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -129,7 +129,7 @@ struct s2m_mesh {
   // workspace
   float *ring = nullptr;
   unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
-  uint2 *pt_bits = nullptr;                  // sign / near-zero bits of a slab's lattice points
+  unsigned *pt_bits = nullptr;               // sign, then near-zero bits of the ring's lattice points
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
@@ -371,6 +371,18 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   return S2M_OK;
 }
 
+// Point bits of the ring (two arrays of ring * P * ceil(P / 32) words).
+size_t pt_bits_words(const s2m_mesh *m) {  // one of the two arrays (S2PointBits)
+  const size_t P = size_t(m->job.P), WP = (P + 31) / 32;
+  return size_t(m->job.ring) * P * WP;
+}
+S2PointBits point_bits(const s2m_mesh *m) {
+  S2PointBits pb;
+  pb.pos = m->pt_bits;
+  pb.near = m->pt_bits + pt_bits_words(m);
+  return pb;
+}
+
 // Planes k0 .. k0 + nk - 1 that slab s evaluates.
 void slab_planes(const s2m_mesh *m, int s, int &k0, int &nk) {
   const int zc0 = s * m->D;
@@ -465,9 +477,10 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   PruneGeom g = prune_geom(m->job, nk);
   const unsigned *bits = prune_at<unsigned>(m, m->prune_bits_off) +
                         (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
+  S2PointBits pb = point_bits(m);
   if (kEvalVariants[v].chunked) {
     unsigned *counter = prune_counters(m) + s;
-    void *cargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
+    void *cargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m->sdf->k_eval[v], S2_PTP_BLOCK, 0) !=
             cudaSuccess ||
@@ -479,7 +492,7 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
     const unsigned grid = unsigned(std::max<long long>(1, std::min<long long>(chunks, (long long)device_sm_count() * per_sm)));
     return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(grid), dim3(S2_PTP_BLOCK), cargs, 0, st);
   }
-  void *pargs[] = {&jj, &ring, &bits, &k0, &nk, &g.tzs, &g.nzt};
+  void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
                           0, st);
 }
@@ -489,10 +502,6 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
 size_t cell_word_tiles(const s2m_mesh *m) {
   const size_t WN = size_t((m->N + 31) / 32);
   return (size_t(m->D) * size_t(m->N) * WN + S2_CW_BLOCK - 1) / S2_CW_BLOCK;
-}
-size_t pt_bits_words(const s2m_mesh *m) {
-  const size_t P = size_t(m->job.P), WP = (P + 31) / 32;
-  return (size_t(m->D) + 1) * P * WP;
 }
 
 void drop_graph(s2m_mesh *m) {
@@ -518,7 +527,9 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   cudaStream_t st = m->stream;
   S2_CUDA(cudaMallocAsync(&m->ring, ring_floats * sizeof(float), st));
   S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->pt_bits, pt_bits_words(m) * sizeof(uint2), st));
+  S2_CUDA(cudaMallocAsync(&m->pt_bits, 2 * pt_bits_words(m) * 4, st));
+  // the words' bits past the lattice edge are never written and must read 0
+  S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, 2 * pt_bits_words(m) * 4, st));
   S2_CUDA(cudaMallocAsync(&m->offx, size_t((j.N + 31) / 32) * 4, st));
   S2_CUDA(cudaMallocAsync(&m->cell_words, m->cell_tiles * S2_CW_BLOCK * 4, st));
   S2_CUDA(cudaMallocAsync(&m->tile_cnt, m->cell_tiles * 4, st));
@@ -664,6 +675,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     if (e0 != cudaSuccess) return e0;
   }
   S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
+  const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
     int zc0 = s * m->D;
     int zc1 = std::min(m->nzc, zc0 + m->D);
@@ -683,11 +695,12 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                 cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
     }
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
-    const dim3 bits_grid(unsigned((j.P + 7) / 8), unsigned(zc1 - zc0 + 1));
-    S2_LAUNCH(1, 0, (s2m_cells_bits<<<bits_grid, 256, 0, st>>>(j, m->ring, m->pt_bits, zc0), cudaGetLastError()));
+    if (!pruned)  // the pruned evaluation writes the point bits of its planes itself
+      S2_LAUNCH(1, 0, (s2m_cells_bits<<<dim3(unsigned((j.P + 7) / 8), unsigned(nk)), 256, 0, st>>>(j, m->ring, pb, k0),
+                       cudaGetLastError()));
     const unsigned long long nwords = (unsigned long long)(zc1 - zc0) * N * ((N + 31) / 32);
     const unsigned cg = unsigned((nwords + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
-    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->pt_bits, m->offx, m->cell_words, m->tile_cnt,
+    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
                                                                     zc0, zc1),
                           cudaGetLastError()));
     S2_LAUNCH(1, 0, (s2m_cells_offsets<<<1, 1024, 0, st>>>(m->tile_cnt, cg, m->slab_ctrl, m->cand_base, s),
@@ -1280,7 +1293,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   size_t used = 0;
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
-            carve(base, used, pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
+            carve(base, used, 2 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
             carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles, &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&

@@ -258,52 +258,87 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
   }
 }
 
-// Pruned evaluation of one tile by one warp: the lanes stride over the
-// tile's points (RUN4: over runs of 4 planes sharing x and y, which share the
-// bit tests and the x/y-only arithmetic; a run past the tile's last plane
-// repeats that plane and stores only its own planes).  `m` (shared memory)
-// holds the tile's activity bits, the same for the whole warp, so the pruned
-// function's branches never diverge.  Points past the lattice edge (tiles are
-// 8 x 8) evaluate a clamped point and store nothing.
-template <bool RUN4>
-__device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict__ ring, const S2PruneTile &tl,
-                                             const unsigned *m) {
+// Point bits of one warp-wide step of a tile: the 32 lanes hold 8 points
+// along x times 4 rows from `y0` in the plane at ring slot `slot`, so each
+// ballot holds one byte (8 points) per row.  Lanes 0-3 store the sign bytes
+// of rows y0 .. y0 + 3, lanes 4-7 the near-zero bytes.
+__device__ __forceinline__ void s2_tile_bits(const S2Job &job, S2PointBits pb, const S2PruneTile &tl, int y0,
+                                             int slot, bool store, float f) {
+  const unsigned pos = __ballot_sync(S2_FULL, store && f > 0.0f);
+  const unsigned near = __ballot_sync(S2_FULL, store && !(fabsf(f) >= job.guard));
   const int lane = (int)(threadIdx.x & 31u);
-  const int nz = tl.ke - tl.kb + 1;
+  const int r = lane & 3, y = y0 + r;
+  if (lane < 8 && y <= tl.j1) {
+    const int WP = (job.P + 31) >> 5;
+    unsigned char *base = reinterpret_cast<unsigned char *>(lane < 4 ? pb.pos : pb.near);
+    base[(((long long)slot * job.P + y) * WP) * 4 + (tl.i0 >> 3)] =
+        (unsigned char)(((lane < 4 ? pos : near) >> (8 * r)) & 0xffu);
+  }
+}
+
+// Pruned evaluation of one tile by one warp, writing the values and their
+// point bits.  Lane l takes x = i0 + l % 8 and the rows j0 + l / 8 and
+// j0 + l / 8 + 4, and walks the tile's planes (RUN4: runs of 4 planes, which
+// share the bit tests and the x/y-only arithmetic; a run past the tile's last
+// plane repeats that plane and stores only its own planes).  `m` (shared
+// memory) holds the tile's activity bits, the same for the whole warp, so the
+// pruned function's branches never diverge and every lane takes part in the
+// ballots.  Points past the lattice edge (tiles are 8 x 8) evaluate a
+// clamped point and store nothing.
+template <bool RUN4>
+__device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
+                                             const S2PruneTile &tl, const unsigned *m) {
+  const int lane = (int)(threadIdx.x & 31u);
+  const int i = tl.i0 + (lane & 7), ja = tl.j0 + (lane >> 3);
+  const float x = s2_coord(job, min(i, tl.i1));
+  const float y0 = s2_coord(job, min(ja, tl.j1)), y1 = s2_coord(job, min(ja + 4, tl.j1));
+  const bool xin = i <= tl.i1;
+  float *const col = ring + (long long)min(i, tl.i1);
+  int slot = tl.kb % job.ring;  // the tile spans at most S2_PT_ZMAX <= ring planes
   if (RUN4) {
-    const int nruns = S2_PT_XY * S2_PT_XY * ((nz + 3) >> 2);
 #pragma unroll 1
-    for (int q = lane; q < nruns; q += 32) {
-      const int i = tl.i0 + (q & (S2_PT_XY - 1));
-      const int j = tl.j0 + ((q >> 3) & (S2_PT_XY - 1));
-      const int k = tl.kb + 4 * (q >> 6);
+    for (int k = tl.kb; k <= tl.ke; k += 4) {
       s2x4 z;
 #pragma unroll
       for (int w = 0; w < 4; ++w) z.v[w] = s2_coord(job, min(k + w, tl.ke));
-      const s2x4 f = s2m_user_sdf_pruned_run4(s2_coord(job, min(i, tl.i1)), s2_coord(job, min(j, tl.j1)), z, m);
-      if (i <= tl.i1 && j <= tl.j1) {
-        float *col = ring + (long long)j * job.pitch + i;
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        const int j = ja + 4 * h;
+        const bool store = xin && j <= tl.j1;
+        const s2x4 f = s2m_user_sdf_pruned_run4(x, h ? y1 : y0, z, m);
+        int sw = slot;
 #pragma unroll
-        for (int w = 0; w < 4; ++w)
-          if (k + w <= tl.ke) col[(long long)((k + w) % job.ring) * job.plane] = f.v[w];
+        for (int w = 0; w < 4; ++w) {
+          if (k + w <= tl.ke) {  // the same on every lane
+            if (store) col[(long long)sw * job.plane + (long long)j * job.pitch] = f.v[w];
+            s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, sw, store, f.v[w]);
+          }
+          if (++sw == job.ring) sw = 0;
+        }
       }
+      slot += 4;
+      if (slot >= job.ring) slot -= job.ring;
     }
     return;
   }
-  const int npts = S2_PT_XY * S2_PT_XY * nz;
 #pragma unroll 1
-  for (int q = lane; q < npts; q += 32) {
-    const int i = tl.i0 + (q & (S2_PT_XY - 1));
-    const int j = tl.j0 + ((q >> 3) & (S2_PT_XY - 1));
-    const int k = tl.kb + (q >> 6);
-    const float f = s2m_user_sdf_pruned(s2_coord(job, min(i, tl.i1)), s2_coord(job, min(j, tl.j1)), s2_coord(job, k), m);
-    if (i <= tl.i1 && j <= tl.j1) ring[(long long)(k % job.ring) * job.plane + (long long)j * job.pitch + i] = f;
+  for (int k = tl.kb; k <= tl.ke; ++k) {
+    const float z = s2_coord(job, k);
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      const int j = ja + 4 * h;
+      const bool store = xin && j <= tl.j1;
+      const float f = s2m_user_sdf_pruned(x, h ? y1 : y0, z, m);
+      if (store) col[(long long)slot * job.plane + (long long)j * job.pitch] = f;
+      s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store, f);
+    }
+    if (++slot == job.ring) slot = 0;
   }
 }
 
 // One tile per warp, 4 warps per block, tile t = block * 4 + warp.
 template <bool RUN4>
-__device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restrict__ ring,
+__device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
                                                const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) {
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const long long ntiles = (long long)ntx * ntx * nzt;
@@ -315,7 +350,7 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   const int lane = (int)(threadIdx.x & 31u);
   if (lane < S2M_PRUNE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
   __syncwarp();
-  s2_eval_tile<RUN4>(job, ring, tl, s_bits[threadIdx.x >> 5]);
+  s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
 }
 
 // Persistent form: each block takes chunks of S2_PTP_BLOCK / 32 consecutive
@@ -325,7 +360,7 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
 // share the instruction cache; with one tile per 4-warp block, an SM's warps
 // come from tiles all over the slab.
 template <bool RUN4>
-__device__ __forceinline__ void s2_eval_pruned_chunks(const S2Job &job, float *__restrict__ ring,
+__device__ __forceinline__ void s2_eval_pruned_chunks(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
                                                       const unsigned *__restrict__ bits, int k0, int nk, int tzs,
                                                       int nzt, unsigned *__restrict__ counter) {
   constexpr int kWarps = S2_PTP_BLOCK / 32;
@@ -346,7 +381,7 @@ __device__ __forceinline__ void s2_eval_pruned_chunks(const S2Job &job, float *_
       if (tl.kb <= tl.ke) {
         if (lane < S2M_PRUNE_WORDS) s_bits[warp][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
         __syncwarp();
-        s2_eval_tile<RUN4>(job, ring, tl, s_bits[warp]);
+        s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[warp]);
         __syncwarp();
       }
     }
@@ -355,19 +390,20 @@ __device__ __forceinline__ void s2_eval_pruned_chunks(const S2Job &job, float *_
 
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
-  NAME(S2Job job, float *__restrict__ ring, const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt) { \
-    s2_eval_pruned<RUN4>(job, ring, bits, k0, nk, tzs, nzt);                                      \
+  NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
+       int tzs, int nzt) {                                                                        \
+    s2_eval_pruned<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt);                                  \
   }
 #define S2_EVALPC_VARIANT(NAME, MINB, RUN4)                                                       \
   extern "C" __global__ void __launch_bounds__(S2_PTP_BLOCK, MINB)                                \
-  NAME(S2Job job, float *__restrict__ ring, const unsigned *__restrict__ bits, int k0, int nk, int tzs, int nzt, \
-       unsigned *counter) {                                                                       \
-    s2_eval_pruned_chunks<RUN4>(job, ring, bits, k0, nk, tzs, nzt, counter);                      \
+  NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
+       int tzs, int nzt, unsigned *counter) {                                                     \
+    s2_eval_pruned_chunks<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt, counter);                  \
   }
 // Keep this table in step with kEvalVariants in runtime.cu.
 S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
+S2_EVALP_VARIANT(s2m_evalp_b8v4, 8, true)
 S2_EVALPC_VARIANT(s2m_evalpc_b2, 2, false)
-S2_EVALPC_VARIANT(s2m_evalpc_b2v4, 2, true)
 #endif
 
 

@@ -59,6 +59,16 @@ struct S2Cand {
   unsigned *tile_counter;         // s2m_vcompact
 };
 
+// Sign (v > 0) and near-zero (!(|v| >= guard)) bits of lattice points,
+// indexed by ring slot like the lattice values: word ((k % ring) * P + y) *
+// WP + x / 32 (WP = ceil(P / 32)) holds bit x % 32 of plane k, row y; in
+// little-endian bytes, byte x / 8 holds bit x % 8.  Bits past the lattice
+// edge are 0.
+struct S2PointBits {
+  unsigned *pos;
+  unsigned *near;
+};
+
 // Mesh outputs and the cross-slab counters.
 struct S2MeshDev {
   float *pos;                     // 3 * vcap

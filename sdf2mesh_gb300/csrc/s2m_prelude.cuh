@@ -514,6 +514,14 @@ S2_X4_F1(exp) S2_X4_F1(log)
 S2_X4_F2(min) S2_X4_F2(max) S2_X4_F2(pow) S2_X4_F2(atan2)
 S2_X4_F3(clamp) S2_X4_F3(mix) S2_X4_F3(op_smooth_union) S2_X4_F3(op_smooth_intersection)
 S2_X4_F3(op_smooth_subtraction)
+// Out-of-line run forms of the smooth operators for the pruned code.
+S2M_PRUNED_FN s2x4 s2r_op_smooth_union_call(s2x4 a, s2x4 b, s2x4 k) { return s2r_op_smooth_union(a, b, k); }
+S2M_PRUNED_FN s2x4 s2r_op_smooth_intersection_call(s2x4 a, s2x4 b, s2x4 k) {
+  return s2r_op_smooth_intersection(a, b, k);
+}
+S2M_PRUNED_FN s2x4 s2r_op_smooth_subtraction_call(s2x4 a, s2x4 b, s2x4 k) {
+  return s2r_op_smooth_subtraction(a, b, k);
+}
 #undef S2_X4_F1
 #undef S2_X4_F2
 #undef S2_X4_F3

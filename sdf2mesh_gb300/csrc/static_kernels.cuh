@@ -8,9 +8,10 @@
 
 // Classification of one slab, bit-parallel over 32 cells along x, in passes
 // that never wait on one another:
-//   s2m_cells_bits     per lattice point of the slab's planes, a sign bit
+//   s2m_cells_bits     per lattice point of the slab's new planes, a sign bit
 //                      (v > 0) and a near-zero bit (!(|v| >= guard)), 32
-//                      points per word pair; each point is read once
+//                      points per word, each point read once (the pruned
+//                      evaluation writes these bits itself)
 //   s2m_cells_mark     per word of 32 cells, the candidate bits from the
 //                      corner bits of the 4 point rows around it (a few dozen
 //                      bitwise operations for 32 cells), and the tile counts
@@ -29,19 +30,19 @@ __global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict_
   if ((threadIdx.x & 31u) == 0 && x < job.N) offx[x >> 5] = b;
 }
 
-// Planes zc0 .. zc0 + np - 1 (slot p = plane zc0 + p): bits[(p * P + y) * WP + w]
-// holds points x = 32 w .. 32 w + 31 of row y (bits past the lattice are 0).
-// Grid (ceil(P / 8), np), 8 warps per block, one row per warp: the warp walks
-// the row's words (a 128-byte load and two ballots each).
-__global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__restrict__ ring,
-                                                      uint2 *__restrict__ bits, int zc0) {
+// Point bits of planes k0 .. k0 + gridDim.y - 1 (for evaluation variants
+// that do not write them themselves).  Grid (ceil(P / 8), planes), 8 warps
+// per block, one row per warp: the warp walks the row's words (a 128-byte
+// load and two ballots each).
+__global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__restrict__ ring, S2PointBits pb,
+                                                      int k0) {
   const int WP = (job.P + 31) >> 5;
-  const int p = (int)blockIdx.y;
+  const int slot = (k0 + (int)blockIdx.y) % job.ring;
   const int y = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5);
   if (y >= job.P) return;  // whole warps
   const int lane = (int)(threadIdx.x & 31u);
-  const float *row = ring + (long long)((zc0 + p) % job.ring) * job.plane + (long long)y * job.pitch;
-  uint2 *dst = bits + ((long long)p * job.P + y) * WP;
+  const float *row = ring + (long long)slot * job.plane + (long long)y * job.pitch;
+  const long long o = ((long long)slot * job.P + y) * WP;
 #pragma unroll 4
   for (int w = 0; w < WP; ++w) {
     const int x = w * 32 + lane;
@@ -49,7 +50,10 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
     const float v = in ? __ldg(row + x) : 0.0f;
     const unsigned pos = __ballot_sync(S2_FULL, in && v > 0.0f);
     const unsigned near = __ballot_sync(S2_FULL, in && !(fabsf(v) >= job.guard));
-    if (lane == 0) dst[w] = make_uint2(pos, near);
+    if (lane == 0) {
+      pb.pos[o + w] = pos;
+      pb.near[o + w] = near;
+    }
   }
 }
 
@@ -77,7 +81,7 @@ __device__ __forceinline__ S2CellWord s2_cell_word(const S2Job &job, int WN) {
   return c;
 }
 
-__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, const uint2 *__restrict__ bits,
+__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2PointBits pb,
                                                             const unsigned *__restrict__ offx,
                                                             unsigned *__restrict__ words,
                                                             unsigned *__restrict__ tile_cnt, int zc0, int zc1) {
@@ -91,22 +95,24 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, const u
     const int w = cw.w, y = cw.y, dz = cw.dz;
     // corner k = bx | by << 1 | bz << 2 lies in point row q = by | bz << 1
     // (k = 2 q + bx); bx = 1 takes the row's bits shifted by one point
-    unsigned pb[8], nb[8];
+    unsigned pbit[8], nbit[8];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const long long base = ((long long)(dz + (q >> 1)) * job.P + (y + (q & 1))) * WP + w;
-      const uint2 lo = bits[base];
-      const uint2 hi = w + 1 < WP ? bits[base + 1] : make_uint2(0u, 0u);
-      pb[2 * q] = lo.x;
-      pb[2 * q + 1] = __funnelshift_r(lo.x, hi.x, 1);
-      nb[2 * q] = lo.y;
-      nb[2 * q + 1] = __funnelshift_r(lo.y, hi.y, 1);
+      const int slot = (zc0 + dz + (q >> 1)) % job.ring;
+      const long long base = ((long long)slot * job.P + (y + (q & 1))) * WP + w;
+      const bool more = w + 1 < WP;
+      const unsigned plo = __ldg(pb.pos + base), phi = more ? __ldg(pb.pos + base + 1) : 0u;
+      const unsigned nlo = __ldg(pb.near + base), nhi = more ? __ldg(pb.near + base + 1) : 0u;
+      pbit[2 * q] = plo;
+      pbit[2 * q + 1] = __funnelshift_r(plo, phi, 1);
+      nbit[2 * q] = nlo;
+      nbit[2 * q + 1] = __funnelshift_r(nlo, nhi, 1);
     }
     unsigned all = ~0u, any = 0u;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      all &= pb[k];
-      any |= pb[k];
+      all &= pbit[k];
+      any |= pbit[k];
     }
     cand = any & ~all;
     if (!job.qef) {
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, const u
       } else {
 #pragma unroll
         for (int k = 1; k < 8; ++k)
-          cand |= nb[k] & (((k & 1) ? ox : 0u) | ((k & 2) ? oy : 0u) | ((k & 4) ? oz : 0u));
+          cand |= nbit[k] & (((k & 1) ? ox : 0u) | ((k & 2) ? oy : 0u) | ((k & 4) ? oz : 0u));
       }
     }
     if (w == WN - 1 && (job.N & 31)) cand &= (1u << (job.N & 31)) - 1u;
