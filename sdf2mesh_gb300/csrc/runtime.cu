@@ -78,20 +78,18 @@ int device_sm_count() {
 
 // Evaluation-kernel variants compiled into every SDF module (the tables in
 // s2m_dc_kernels.cuh): name, z-run length, whether it evaluates the run-of-4
-// form, whether it is a tile-pruned variant (present only in modules of SDFs
-// with a pruning form), and whether it is the persistent chunked form.
+// form, and whether it is a tile-pruned variant (present only in modules of
+// SDFs with a pruning form).
 struct EvalVariant {
   const char *name;
   int run;
   bool vec;
   bool pruned;
-  bool chunked;
 };
 constexpr EvalVariant kEvalVariants[] = {
-    {"s2m_eval_b2r4", 4, false, false, false}, {"s2m_eval_b3r4", 4, false, false, false},
-    {"s2m_eval_b4r4", 4, false, false, false}, {"s2m_eval_b2v4", 4, true, false, false},
-    {"s2m_eval_b3v4", 4, true, false, false},  {"s2m_evalp_b8", 1, false, true, false},
-    {"s2m_evalp_b8v4", 4, true, true, false},  {"s2m_evalpc_b2", 1, false, true, true}};
+    {"s2m_eval_b2r4", 4, false, false}, {"s2m_eval_b3r4", 4, false, false}, {"s2m_eval_b4r4", 4, false, false},
+    {"s2m_eval_b2v4", 4, true, false},  {"s2m_eval_b3v4", 4, true, false},  {"s2m_evalp_b8", 1, false, true},
+    {"s2m_evalp_b12", 1, false, true},  {"s2m_evalp_b8v4", 4, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -133,10 +131,9 @@ struct s2m_mesh {
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
-  // tile pruning: [ops FP32, ops SFU] (2 u64), a tile-chunk counter per slab
-  // (u32), the first tile and the first coarse box of every slab (2 x
-  // nslabs + 1 u64), then the activity words of `prune_chunk` slabs' coarse
-  // boxes and tiles
+  // tile pruning: [ops FP32, ops SFU] (2 u64), the first tile and the first
+  // coarse box of every slab (2 x nslabs + 1 u64), then the activity words
+  // of `prune_chunk` slabs' coarse boxes and tiles
   unsigned long long *prune_buf = nullptr;
   std::vector<unsigned long long> slab_tile_base, slab_coarse_base;  // host copies
   int prune_chunk = 0;
@@ -437,7 +434,7 @@ size_t prune_layout(s2m_mesh *m) {
     chunk_coarse = std::max(chunk_coarse, m->slab_coarse_base[size_t(e)] - m->slab_coarse_base[size_t(s)]);
   }
   auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-  m->prune_base_off = up16(16 + 4 * size_t(ns));
+  m->prune_base_off = 16;
   m->prune_cbase_off = up16(m->prune_base_off + 8 * (size_t(ns) + 1));
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * words * 4);
@@ -447,7 +444,6 @@ template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
 }
 unsigned long long *prune_bases(const s2m_mesh *m) { return prune_at<unsigned long long>(m, m->prune_base_off); }
-unsigned *prune_counters(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
 // Tile pass over slabs [s_begin, s_end) (coarse boxes, then tiles) and the
 // pruned evaluation of slab s.
@@ -478,20 +474,6 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   const unsigned *bits = prune_at<unsigned>(m, m->prune_bits_off) +
                         (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
   S2PointBits pb = point_bits(m);
-  if (kEvalVariants[v].chunked) {
-    unsigned *counter = prune_counters(m) + s;
-    void *cargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m->sdf->k_eval[v], S2_PTP_BLOCK, 0) !=
-            cudaSuccess ||
-        per_sm < 1) {
-      cudaGetLastError();
-      per_sm = 1;
-    }
-    const long long chunks = (g.ntiles + S2_PTP_BLOCK / 32 - 1) / (S2_PTP_BLOCK / 32);
-    const unsigned grid = unsigned(std::max<long long>(1, std::min<long long>(chunks, (long long)device_sm_count() * per_sm)));
-    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(grid), dim3(S2_PTP_BLOCK), cargs, 0, st);
-  }
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
                           0, st);
@@ -532,7 +514,7 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, 2 * pt_bits_words(m) * 4, st));
   S2_CUDA(cudaMallocAsync(&m->offx, size_t((j.N + 31) / 32) * 4, st));
   S2_CUDA(cudaMallocAsync(&m->cell_words, m->cell_tiles * S2_CW_BLOCK * 4, st));
-  S2_CUDA(cudaMallocAsync(&m->tile_cnt, m->cell_tiles * 4, st));
+  S2_CUDA(cudaMallocAsync(&m->tile_cnt, (m->cell_tiles + 1) * 4, st));  // + the finished-block counter
   if (m->sdf->k_tiles && m->nslabs > 0) {
     S2_CUDA(cudaMallocAsync(&m->prune_buf, prune_layout(m), st));
     // pageable source: the call returns once the words are staged
@@ -670,10 +652,11 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->last_variant = ev;
   m->eval_points = 0;
   m->eval_fp_ops = m->eval_sfu_ops = 0;
-  if (pruned) {  // operation counters and the slabs' tile-chunk counters
+  if (pruned) {  // operation counters
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }
+  if ((e = cudaMemsetAsync(m->tile_cnt + m->cell_tiles, 0, 4, st)) != cudaSuccess) return e;
   S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
   const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
@@ -701,10 +684,9 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     const unsigned long long nwords = (unsigned long long)(zc1 - zc0) * N * ((N + 31) / 32);
     const unsigned cg = unsigned((nwords + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
     S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
-                                                                    zc0, zc1),
+                                                                    m->tile_cnt + m->cell_tiles, m->slab_ctrl,
+                                                                    m->cand_base, s, zc0, zc1),
                           cudaGetLastError()));
-    S2_LAUNCH(1, 0, (s2m_cells_offsets<<<1, 1024, 0, st>>>(m->tile_cnt, cg, m->slab_ctrl, m->cand_base, s),
-                     cudaGetLastError()));
     S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->ring, m->cell_words, m->slab_ctrl, cand, c.err,
                                                                zc0, zc1),
                      cudaGetLastError()));
@@ -1294,7 +1276,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
             carve(base, used, 2 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
-            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles, &m.tile_cnt) &&
+            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles + 1, &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
             carve(base, used, size_t(8), &m.jobctl);

@@ -353,57 +353,16 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
 }
 
-// Persistent form: each block takes chunks of S2_PTP_BLOCK / 32 consecutive
-// tiles (one per warp) from the slab's counter until none are left.  All the
-// warps of a block then work on neighbouring tiles, whose active segments are
-// much alike, so they run the same parts of the (large) pruned function and
-// share the instruction cache; with one tile per 4-warp block, an SM's warps
-// come from tiles all over the slab.
-template <bool RUN4>
-__device__ __forceinline__ void s2_eval_pruned_chunks(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
-                                                      const unsigned *__restrict__ bits, int k0, int nk, int tzs,
-                                                      int nzt, unsigned *__restrict__ counter) {
-  constexpr int kWarps = S2_PTP_BLOCK / 32;
-  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const long long ntiles = (long long)ntx * ntx * nzt;
-  __shared__ unsigned s_chunk;
-  __shared__ unsigned s_bits[kWarps][S2M_PRUNE_WORDS];
-  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
-  for (;;) {
-    if (threadIdx.x == 0) s_chunk = atomicAdd(counter, 1u);
-    __syncthreads();
-    const long long first = (long long)s_chunk * kWarps;
-    __syncthreads();
-    if (first >= ntiles) break;
-    const long long t = first + warp;
-    if (t < ntiles) {
-      const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, tzs);
-      if (tl.kb <= tl.ke) {
-        if (lane < S2M_PRUNE_WORDS) s_bits[warp][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
-        __syncwarp();
-        s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[warp]);
-        __syncwarp();
-      }
-    }
-  }
-}
-
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
   NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
        int tzs, int nzt) {                                                                        \
     s2_eval_pruned<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt);                                  \
   }
-#define S2_EVALPC_VARIANT(NAME, MINB, RUN4)                                                       \
-  extern "C" __global__ void __launch_bounds__(S2_PTP_BLOCK, MINB)                                \
-  NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
-       int tzs, int nzt, unsigned *counter) {                                                     \
-    s2_eval_pruned_chunks<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt, counter);                  \
-  }
 // Keep this table in step with kEvalVariants in runtime.cu.
 S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
+S2_EVALP_VARIANT(s2m_evalp_b12, 12, false)
 S2_EVALP_VARIANT(s2m_evalp_b8v4, 8, true)
-S2_EVALPC_VARIANT(s2m_evalpc_b2, 2, false)
 #endif
 
 

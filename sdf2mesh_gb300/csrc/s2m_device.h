@@ -106,7 +106,6 @@ struct S2MeshDev {
 #define S2_PT_ZMAX 8
 #define S2_PT_BLOCK 128
 #define S2_PT_COARSE 4            /* tiles per coarse box of the tile pass, along x and y */
-#define S2_PTP_BLOCK 512          /* persistent pruned evaluation: 16 warps, 16 tiles per chunk */
 #define S2_VX_BLOCK 128
 #define S2_VC_BLOCK 256
 #define S2_VC_CPT 4

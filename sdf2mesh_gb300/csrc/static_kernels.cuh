@@ -15,12 +15,56 @@
 //   s2m_cells_mark     per word of 32 cells, the candidate bits from the
 //                      corner bits of the 4 point rows around it (a few dozen
 //                      bitwise operations for 32 cells), and the tile counts
-//   s2m_cells_offsets  exclusive scan of the tile counts (one block)
+//                      (the last block to finish scans them into offsets)
 //   s2m_cells_emit     the candidates of each tile, in (z, y, x) order
 // The rule is s2_classify_values' (s2m_dc_core.cuh): a cell is a candidate
 // when its 8 lattice corners do not share a sign, or (reference rule) when a
 // corner whose reference coordinates are off the lattice is near zero (every
 // cell with such a corner when S2M_JOB_EXACT_CORNERS).
+
+// tile_off[t] = cand.base[slab] + (candidates of tiles < t); cand.base[slab + 1]
+// = the slab's running total.  Run by one block of NT threads, any tile
+// count; the counts are read from L2 (other blocks wrote them).
+template <int NT>
+__device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned ntiles,
+                                              unsigned long long *__restrict__ tile_off, unsigned long long *base,
+                                              int slab_index) {
+  __shared__ unsigned long long s_warp[32];
+  __shared__ unsigned long long s_carry;
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  if (tid == 0) s_carry = __ldcg(base + slab_index);
+  if (tid < 32) s_warp[tid] = 0ull;
+  __syncthreads();
+  for (unsigned t0 = 0; t0 < ntiles; t0 += NT) {
+    const unsigned t = t0 + tid;
+    const unsigned long long v = t < ntiles ? __ldcg(tile_cnt + t) : 0ull;
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long x = __shfl_up_sync(S2_FULL, inc, o);
+      if ((int)lane >= o) inc += x;
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      const unsigned long long w = s_warp[lane];
+      unsigned long long wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long x = __shfl_up_sync(S2_FULL, wi, o);
+        if ((int)lane >= o) wi += x;
+      }
+      s_warp[lane] = wi - w;
+    }
+    __syncthreads();
+    const unsigned long long carry = s_carry;
+    if (t < ntiles) tile_off[t] = carry + s_warp[warp] + inc - v;
+    __syncthreads();
+    if (tid == NT - 1) s_carry = carry + s_warp[NT / 32 - 1] + inc;  // last thread's inclusive total
+    __syncthreads();
+  }
+  if (tid == 0) base[slab_index + 1] = s_carry;
+}
 
 // Off-lattice bit of every cell column x: bit x % 32 of word x / 32 is
 // s2_off_lattice(x + 1).
@@ -81,10 +125,15 @@ __device__ __forceinline__ S2CellWord s2_cell_word(const S2Job &job, int WN) {
   return c;
 }
 
+// The last block to finish (a fence, then an atomic count of finished blocks)
+// also scans the tile counts into the slab's candidate offsets (tile_off,
+// base[slab + 1]), so no separate launch is needed; `done` returns to 0.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2PointBits pb,
                                                             const unsigned *__restrict__ offx,
-                                                            unsigned *__restrict__ words,
-                                                            unsigned *__restrict__ tile_cnt, int zc0, int zc1) {
+                                                            unsigned *__restrict__ words, unsigned *tile_cnt,
+                                                            unsigned *done, unsigned long long *__restrict__ tile_off,
+                                                            unsigned long long *base, int slab_index, int zc0,
+                                                            int zc1) {
   __shared__ unsigned s_warp[S2_CW_BLOCK / 32];
   const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5;
   const long long nw = (long long)(zc1 - zc0) * job.N * WN;
@@ -135,52 +184,19 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(S2_FULL, cnt, o);
   if ((threadIdx.x & 31u) == 0) s_warp[threadIdx.x >> 5] = cnt;
   __syncthreads();
+  __shared__ bool s_last;
   if (threadIdx.x == 0) {
     unsigned t = 0;
     for (int i = 0; i < S2_CW_BLOCK / 32; ++i) t += s_warp[i];
     tile_cnt[blockIdx.x] = t;
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
   }
-}
-
-// tile_off[t] = cand.base[slab] + (candidates of tiles < t); cand.base[slab + 1]
-// = the slab's running total.  One block of 1024 threads, any tile count.
-__global__ void __launch_bounds__(1024) s2m_cells_offsets(const unsigned *__restrict__ tile_cnt, unsigned ntiles,
-                                                          unsigned long long *__restrict__ tile_off,
-                                                          unsigned long long *base, int slab_index) {
-  __shared__ unsigned long long s_warp[32];
-  __shared__ unsigned long long s_carry;
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  if (tid == 0) s_carry = base[slab_index];
   __syncthreads();
-  for (unsigned t0 = 0; t0 < ntiles; t0 += 1024) {
-    const unsigned t = t0 + tid;
-    const unsigned long long v = t < ntiles ? tile_cnt[t] : 0ull;
-    unsigned long long inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long x = __shfl_up_sync(S2_FULL, inc, o);
-      if ((int)lane >= o) inc += x;
-    }
-    if (lane == 31) s_warp[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-      const unsigned long long w = s_warp[lane];
-      unsigned long long wi = w;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long x = __shfl_up_sync(S2_FULL, wi, o);
-        if ((int)lane >= o) wi += x;
-      }
-      s_warp[lane] = wi - w;
-    }
-    __syncthreads();
-    const unsigned long long carry = s_carry;
-    if (t < ntiles) tile_off[t] = carry + s_warp[warp] + inc - v;
-    __syncthreads();
-    if (tid == 1023) s_carry = carry + s_warp[31] + inc;  // last thread's inclusive total
-    __syncthreads();
-  }
-  if (tid == 0) base[slab_index + 1] = s_carry;
+  if (!s_last) return;
+  __threadfence();
+  s2_scan_tiles<S2_CW_BLOCK>(tile_cnt, gridDim.x, tile_off, base, slab_index);
+  if (threadIdx.x == 0) *done = 0u;
 }
 
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the

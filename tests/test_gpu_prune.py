@@ -19,7 +19,7 @@ from tests.test_prune_host import EDGE, SMOOTH_OPS
 
 pytestmark = pytest.mark.gpu
 
-PRUNED = (5, 6, 7)  # s2m_evalp_b8, s2m_evalp_b8v4, s2m_evalpc_b2 (persistent)
+PRUNED = (5, 6, 7)  # s2m_evalp_b8, s2m_evalp_b12, s2m_evalp_b8v4
 PLAIN = 1        # s2m_eval_b3r4
 
 
