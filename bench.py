@@ -5,6 +5,10 @@ Workload (one "step"): the CSG SDF -- a rounded box (half-size 0.7, radius
 torus (0.5, 0.1) -- meshed at 1024^3 cells over [-1, 1]^3: grid evaluation,
 sign changes, crossings, mass-point vertices with normals, quads -> triangle
 indices, all on the device.  A voxel is a cell; value = N^3 * steps / time.
+The lattice evaluation is tile-pruned when the autotuner finds that faster:
+per tile, the operands of min / max / smooth operators that an interval
+pass proves cannot change any point's binary32 value are skipped, and the
+mesh is bit-identical to the full evaluation (a GPU test).
 
   value        device time per step (CUDA events on the launching stream),
                mesh buffers resident, L2 flushed between steps (outside the
@@ -460,7 +464,9 @@ def ours(a):
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "flushed between steps (256 MiB write, outside the timed events)",
                    "precision": ("precision mode: lattice corners, QEF vertex, FP32 compensated sums, FP64 solve"
-                                 if qef else "reference rule in binary32, no FMA contraction, IEEE div/sqrt")},
+                                 if qef else "reference rule in binary32, no FMA contraction, IEEE div/sqrt"),
+                   "evaluation": ("tile-pruned (exact: bit-identical to every operation at every point)"
+                                  if eval_ops["pruned"] else "every SDF operation at every lattice point")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_tot / a.steps,
                 "path": "s2m_mesh_create + s2m_mesh_copy_to_host (pinned) + s2m_mesh_free; inputs are the "

@@ -122,3 +122,18 @@ def test_operators_and_edge_cases(lib, name, src, N):
 def test_fmad_turns_pruning_off(lib):
     src, _ = workloads.csg64(seed=0)
     assert s2m.Sdf3DShader.from_source(src).compile(fmad=True).prune_info() == (0, 0)
+
+
+@pytest.mark.parametrize("mode", ["qef", "exact_corners", "reference_cli"])
+def test_job_modes_pruned_equals_full(csg64, mode):
+    """Precision mode, exact off-lattice corners and the reference CLI's
+    rounding and slice lag run the same lattice through the pruned kernels."""
+    pruned, plain, _ = csg64
+    kw = {"qef": dict(qef=True), "exact_corners": dict(exact_corners=True),
+          "reference_cli": dict(reference_rounding=True, slice_lag=True)}[mode]
+    N = 150
+    full, _ = mesh(plain, N, PLAIN, **kw)
+    for v in PRUNED:
+        got, ops = mesh(pruned, N, v, **kw)
+        assert ops["pruned"]
+        same_mesh(got, full, f"{mode} variant {v}")
