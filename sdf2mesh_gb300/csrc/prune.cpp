@@ -10,9 +10,10 @@
 // active, so the point code evaluates S's nodes inside one `if` on S's bit.
 //
 // Generated code:
-//   s2m_user_sdf_tile(X, Y, Z, m, fp, sfu)   intervals of the tile's coordinates
-//       -> activity bits m[] (2 per combinator: operand a needed, operand b
-//          needed) and the FP32 / SFU operations per point that remain;
+//   s2m_user_sdf_tile(X, Y, Z, m, fp, sfu, root)   intervals of the tile's
+//       coordinates -> activity bits m[] (2 per combinator: operand a needed,
+//       operand b needed), the FP32 / SFU operations per point that remain,
+//       and the interval of the SDF's value;
 //   s2m_user_sdf_tile_in(X, Y, Z, pm, m, ...)  the same for a tile inside a
 //       box whose bits pm are known: only pm's active segments are evaluated;
 //   s2m_user_sdf_pruned(x, y, z, m)          the point value, evaluating only
@@ -326,9 +327,10 @@ class Pruner {
   void emit_tile(std::ostringstream &o, int words, bool guarded) const {
     if (guarded)
       o << "S2I_FN void s2m_user_sdf_tile_in(const s2i X, const s2i Y, const s2i Z, const unsigned *pm, unsigned *m, "
-           "float *fp, float *sfu)\n{\n";
+           "float *fp, float *sfu, s2i *root)\n{\n";
     else
-      o << "S2I_FN void s2m_user_sdf_tile(const s2i X, const s2i Y, const s2i Z, unsigned *m, float *fp, float *sfu)\n{\n";
+      o << "S2I_FN void s2m_user_sdf_tile(const s2i X, const s2i Y, const s2i Z, unsigned *m, float *fp, float *sfu, "
+           "s2i *root)\n{\n";
     o << "  (void)X; (void)Y; (void)Z;\n";
     for (int v : combs_) o << "  int d" << v << " = 0;\n";
     if (!guarded) {
@@ -383,6 +385,7 @@ class Pruner {
     };
     o << "  *fp = " << sum(false) << ";\n";
     o << "  *sfu = " << sum(true) << ";\n";
+    o << "  *root = " << ival(ir_.root) << ";\n";  // bounds the SDF's value at every point of the box
     o << "}\n";
   }
 

@@ -426,7 +426,7 @@ size_t prune_layout(s2m_mesh *m) {
   }
   const size_t words = size_t(m->sdf->prune_words);
   m->prune_chunk = int(std::max<size_t>(1, std::min<size_t>(size_t(std::max(ns, 1)),
-                                                            kPruneBitsBudget / (max_slab * words * 4))));
+                                                            kPruneBitsBudget / (max_slab * (words + 1) * 4))));
   unsigned long long chunk_tiles = 0, chunk_coarse = 0;
   for (int s = 0; s < ns; s += m->prune_chunk) {
     const int e = std::min(ns, s + m->prune_chunk);
@@ -438,7 +438,7 @@ size_t prune_layout(s2m_mesh *m) {
   m->prune_cbase_off = up16(m->prune_base_off + 8 * (size_t(ns) + 1));
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * words * 4);
-  return m->prune_bits_off + size_t(chunk_tiles) * words * 4;
+  return m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4;  // + each tile's flag word
 }
 template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
@@ -471,8 +471,9 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   int k0, nk;
   slab_planes(m, s, k0, nk);
   PruneGeom g = prune_geom(m->job, nk);
-  const unsigned *bits = prune_at<unsigned>(m, m->prune_bits_off) +
-                        (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]) * size_t(m->sdf->prune_words);
+  const unsigned *bits = prune_at<unsigned>(m, m->prune_bits_off) + (m->slab_tile_base[size_t(s)] -
+                                                                     m->slab_tile_base[size_t(chunk_begin)]) *
+                                                                        (size_t(m->sdf->prune_words) + 1);
   S2PointBits pb = point_bits(m);
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,

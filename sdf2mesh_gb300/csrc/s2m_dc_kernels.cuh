@@ -127,6 +127,17 @@ __device__ __forceinline__ int s2_tile_depth(int nk) {
 struct S2PruneTile {
   int i0, i1, j0, j1, kb, ke;  // inclusive point ranges
 };
+
+// A tile's record: S2M_PRUNE_WORDS activity words, then a flag word.  Flag
+// S2_TILE_DECIDED: the interval of the SDF's value over the tile's box lies
+// at or beyond +guard (with S2_TILE_POSITIVE) or -guard, so every point's
+// sign bit is known and its near-zero bit is 0 -- all that classification
+// reads -- and the points are not evaluated.  Their lattice values are
+// written as NaN; the vertex kernel evaluates any such corner of a candidate
+// cell exactly (s2_fill_unknown_corners), so the mesh does not change.
+#define S2M_TILE_WORDS (S2M_PRUNE_WORDS + 1)
+#define S2_TILE_DECIDED 1u
+#define S2_TILE_POSITIVE 2u
 __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long t, int k0, int nk, int tzs) {
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   S2PruneTile r;
@@ -206,7 +217,8 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   const s2i X = s2_prune_box(job, i0, i1 + 1), Y = s2_prune_box(job, j0, j1 + 1), Z = s2_prune_box(job, kb - 1, max(kb, ke));
   unsigned m[S2M_PRUNE_WORDS];
   float fp, sfu;
-  s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);
+  s2i root;
+  s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu, &root);
   unsigned *dst = sbits + (c - b0) * S2M_PRUNE_WORDS;
 #pragma unroll
   for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
@@ -238,10 +250,16 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
               Z = s2_prune_box(job, tl.kb - 1, max(tl.kb, tl.ke));
     unsigned m[S2M_PRUNE_WORDS];
     float fp = 0.0f, sfu = 0.0f;
-    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu);
-    unsigned *dst = bits + (g - b0) * S2M_PRUNE_WORDS;
+    s2i root;
+    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu, &root);
+    unsigned flag = 0u;
+    if (root.lo >= job.guard) flag = S2_TILE_DECIDED | S2_TILE_POSITIVE;  // false for an unknown (NaN) interval
+    else if (root.hi <= -job.guard) flag = S2_TILE_DECIDED;
+    if (flag) fp = sfu = 0.0f;  // nothing of the SDF is evaluated there
+    unsigned *dst = bits + (g - b0) * S2M_TILE_WORDS;
 #pragma unroll
     for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
+    dst[S2M_PRUNE_WORDS] = flag;
     const unsigned long long npts = (unsigned long long)(tl.i1 - tl.i0 + 1) * (unsigned long long)(tl.j1 - tl.j0 + 1) *
                                     (unsigned long long)max(0, tl.ke - tl.kb + 1);
     fp_ops = (unsigned long long)fp * npts;
@@ -263,9 +281,9 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
 // ballot holds one byte (8 points) per row.  Lanes 0-3 store the sign bytes
 // of rows y0 .. y0 + 3, lanes 4-7 the near-zero bytes.
 __device__ __forceinline__ void s2_tile_bits(const S2Job &job, S2PointBits pb, const S2PruneTile &tl, int y0,
-                                             int slot, bool store, float f) {
-  const unsigned pos = __ballot_sync(S2_FULL, store && f > 0.0f);
-  const unsigned near = __ballot_sync(S2_FULL, store && !(fabsf(f) >= job.guard));
+                                             int slot, bool is_pos, bool is_near) {
+  const unsigned pos = __ballot_sync(S2_FULL, is_pos);
+  const unsigned near = __ballot_sync(S2_FULL, is_near);
   const int lane = (int)(threadIdx.x & 31u);
   const int r = lane & 3, y = y0 + r;
   if (lane < 8 && y <= tl.j1) {
@@ -290,6 +308,25 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
                                              const S2PruneTile &tl, const unsigned *m) {
   const int lane = (int)(threadIdx.x & 31u);
   const int i = tl.i0 + (lane & 7), ja = tl.j0 + (lane >> 3);
+  const unsigned flag = m[S2M_PRUNE_WORDS];
+  if (flag & S2_TILE_DECIDED) {  // the same on the whole warp
+    const float nan = __int_as_float(0x7fc00000);
+    const bool pos = (flag & S2_TILE_POSITIVE) != 0u;
+    float *const col = ring + (long long)min(i, tl.i1);
+    int slot = tl.kb % job.ring;
+#pragma unroll 1
+    for (int k = tl.kb; k <= tl.ke; ++k) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int j = ja + 4 * h;
+        const bool store = i <= tl.i1 && j <= tl.j1;
+        if (store) col[(long long)slot * job.plane + (long long)j * job.pitch] = nan;
+        s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store && pos, false);
+      }
+      if (++slot == job.ring) slot = 0;
+    }
+    return;
+  }
   const float x = s2_coord(job, min(i, tl.i1));
   const float y0 = s2_coord(job, min(ja, tl.j1)), y1 = s2_coord(job, min(ja + 4, tl.j1));
   const bool xin = i <= tl.i1;
@@ -311,7 +348,8 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
         for (int w = 0; w < 4; ++w) {
           if (k + w <= tl.ke) {  // the same on every lane
             if (store) col[(long long)sw * job.plane + (long long)j * job.pitch] = f.v[w];
-            s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, sw, store, f.v[w]);
+            s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, sw, store && f.v[w] > 0.0f,
+                         store && !(fabsf(f.v[w]) >= job.guard));
           }
           if (++sw == job.ring) sw = 0;
         }
@@ -330,7 +368,7 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
       const bool store = xin && j <= tl.j1;
       const float f = s2m_user_sdf_pruned(x, h ? y1 : y0, z, m);
       if (store) col[(long long)slot * job.plane + (long long)j * job.pitch] = f;
-      s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store, f);
+      s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store && f > 0.0f, store && !(fabsf(f) >= job.guard));
     }
     if (++slot == job.ring) slot = 0;
   }
@@ -346,9 +384,9 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   if (t >= ntiles) return;
   const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, tzs);
   if (tl.kb > tl.ke) return;
-  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_PRUNE_WORDS];
+  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_TILE_WORDS];
   const int lane = (int)(threadIdx.x & 31u);
-  if (lane < S2M_PRUNE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_PRUNE_WORDS + lane);
+  if (lane < S2M_TILE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + t * S2M_TILE_WORDS + lane);
   __syncwarp();
   s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
 }
@@ -394,9 +432,21 @@ __device__ __forceinline__ const unsigned *s2_cell_bits(const S2Job &job, S2Cell
   const int tz = (c.z + 1 - k0) / s2_tile_depth(nk);
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const unsigned long long t = ((unsigned long long)tz * ntx + c.y / S2_PT_XY) * ntx + c.x / S2_PT_XY;
-  return tbits + (tbase[s] + t - tbase[0]) * S2M_PRUNE_WORDS;
+  return tbits + (tbase[s] + t - tbase[0]) * S2M_TILE_WORDS;
 }
 #endif
+
+// Lattice corners left unknown (NaN) by a decided tile of the pruned
+// evaluation: evaluated here at their lattice coordinates, exactly as the
+// lattice pass would have.  (A corner whose SDF value is NaN is evaluated
+// again, to the same NaN.)
+__device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell c, float v[8]) {
+#pragma unroll 1
+  for (int k = 0; k < 8; ++k)
+    if (v[k] != v[k])
+      v[k] = s2_user_sdf_call(s2_coord(job, c.x + (k & 1)), s2_coord(job, c.y + ((k >> 1) & 1)),
+                              s2_coord(job, c.z + ((k >> 2) & 1)));
+}
 
 // Vertices of every candidate of the job, one candidate per thread (dense:
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
@@ -432,6 +482,7 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
       const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
       const float4 a = src[0], b = src[1];
       v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+      s2_fill_unknown_corners(job, c, v);
     }
     float pos[3], nrm[3];
     unsigned long long key;

@@ -39,12 +39,14 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
                 '#else\nextern "C" int eval_run4(long, const double*, double*) { return 0; }\n#endif\n'
                 '#ifdef S2M_HAS_PRUNE\n'
                 'extern "C" int prune_tiles(long ntiles, const float* box, int npts, const float* pts, unsigned* bits,\n'
-                '                           float* ops, float* full, float* pruned, float* full4, float* pruned4) {\n'
+                '                           float* ops, float* full, float* pruned, float* full4, float* pruned4,\n'
+                '                           float* rootb) {\n'
                 '  for (long t = 0; t < ntiles; ++t) {\n'
                 '    s2i X, Y, Z; X.lo = box[6*t]; X.hi = box[6*t+1]; Y.lo = box[6*t+2]; Y.hi = box[6*t+3];\n'
                 '    Z.lo = box[6*t+4]; Z.hi = box[6*t+5];\n'
-                '    unsigned m[S2M_PRUNE_WORDS]; float fp, sfu;\n'
-                '    s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu);\n'
+                '    unsigned m[S2M_PRUNE_WORDS]; float fp, sfu; s2i root;\n'
+                '    s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu, &root);\n'
+                '    rootb[2*t] = root.lo; rootb[2*t+1] = root.hi;\n'
                 '    for (int w = 0; w < S2M_PRUNE_WORDS; ++w) bits[t * S2M_PRUNE_WORDS + w] = m[w];\n'
                 '    ops[2*t] = fp; ops[2*t+1] = sfu;\n'
                 '    for (int p = 0; p < npts; ++p) { const float* q = pts + 3 * (t * npts + p);\n'
@@ -57,20 +59,21 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
                 '        pruned4[t * npts + p + w] = f.v[w]; } }\n'
                 '  }\n  return S2M_PRUNE_WORDS;\n}\n'
                 'extern "C" void prune_tiles_in(long ntiles, const float* pbox, const float* box, int npts,\n'
-                '                               const float* pts, float* ops, float* pruned) {\n'
+                '                               const float* pts, float* ops, float* pruned, float* rootb) {\n'
                 '  for (long t = 0; t < ntiles; ++t) {\n'
                 '    s2i X, Y, Z; X.lo = pbox[6*t]; X.hi = pbox[6*t+1]; Y.lo = pbox[6*t+2]; Y.hi = pbox[6*t+3];\n'
                 '    Z.lo = pbox[6*t+4]; Z.hi = pbox[6*t+5];\n'
-                '    unsigned pm[S2M_PRUNE_WORDS], m[S2M_PRUNE_WORDS]; float fp, sfu;\n'
-                '    s2m_user_sdf_tile(X, Y, Z, pm, &fp, &sfu);\n'
+                '    unsigned pm[S2M_PRUNE_WORDS], m[S2M_PRUNE_WORDS]; float fp, sfu; s2i root;\n'
+                '    s2m_user_sdf_tile(X, Y, Z, pm, &fp, &sfu, &root);\n'
                 '    X.lo = box[6*t]; X.hi = box[6*t+1]; Y.lo = box[6*t+2]; Y.hi = box[6*t+3]; Z.lo = box[6*t+4]; Z.hi = box[6*t+5];\n'
-                '    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu);\n'
+                '    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu, &root);\n'
+                '    rootb[2*t] = root.lo; rootb[2*t+1] = root.hi;\n'
                 '    ops[2*t] = fp; ops[2*t+1] = sfu;\n'
                 '    for (int p = 0; p < npts; ++p) { const float* q = pts + 3 * (t * npts + p);\n'
                 '      pruned[t * npts + p] = s2m_user_sdf_pruned(q[0], q[1], q[2], m); }\n'
                 '  }\n}\n'
                 '#else\nextern "C" int prune_tiles(long, const float*, int, const float*, unsigned*, float*, float*,\n'
-                '                           float*, float*, float*) { return 0; }\n#endif\n')
+                '                           float*, float*, float*, float*) { return 0; }\n#endif\n')
     so = os.path.join(d, "sdf.so")
     subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
                     src, "-o", so], check=True, capture_output=True)
@@ -78,9 +81,9 @@ def compile_host(cuda_src: str) -> ctypes.CDLL:
     L.eval_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
     L.normal_points.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
     L.eval_run4.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
-    L.prune_tiles.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 7
+    L.prune_tiles.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 8
     if hasattr(L, "prune_tiles_in"):
-        L.prune_tiles_in.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+        L.prune_tiles_in.argtypes = [ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4
     _cache[key] = L
     return L
 
@@ -149,14 +152,16 @@ def prune_host(cuda_src: str, boxes: np.ndarray, pts: np.ndarray):
     pruned = np.zeros((nt, npts), np.float32)
     full4 = np.zeros((nt, npts), np.float32)
     pruned4 = np.zeros((nt, npts), np.float32)
+    root = np.zeros((nt, 2), np.float32)
     w = L.prune_tiles(nt, boxes.ctypes.data, npts, pts.ctypes.data, bits.ctypes.data, ops.ctypes.data,
-                      full.ctypes.data, pruned.ctypes.data, full4.ctypes.data, pruned4.ctypes.data)
-    return w, ops, full, pruned, full4, pruned4
+                      full.ctypes.data, pruned.ctypes.data, full4.ctypes.data, pruned4.ctypes.data, root.ctypes.data)
+    return w, ops, full, pruned, full4, pruned4, root
 
 
 def prune_host_in(cuda_src: str, parents: np.ndarray, boxes: np.ndarray, pts: np.ndarray):
     """The two-level tile pass on the host: bits of each parent box, then the
-    tile's bits from them (s2m_user_sdf_tile_in); (ops per tile, pruned values)."""
+    tile's bits from them (s2m_user_sdf_tile_in); (ops per tile, pruned values,
+    the interval of the SDF's value over each tile)."""
     L = compile_host(cuda_src)
     nt, npts = len(boxes), pts.shape[1]
     parents = np.ascontiguousarray(parents, np.float32)
@@ -164,6 +169,7 @@ def prune_host_in(cuda_src: str, parents: np.ndarray, boxes: np.ndarray, pts: np
     pts = np.ascontiguousarray(pts, np.float32)
     ops = np.zeros((nt, 2), np.float32)
     pruned = np.zeros((nt, npts), np.float32)
+    root = np.zeros((nt, 2), np.float32)
     L.prune_tiles_in(nt, parents.ctypes.data, boxes.ctypes.data, npts, pts.ctypes.data, ops.ctypes.data,
-                     pruned.ctypes.data)
-    return ops, pruned
+                     pruned.ctypes.data, root.ctypes.data)
+    return ops, pruned, root

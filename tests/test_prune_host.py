@@ -25,14 +25,23 @@ def check(cu, N, bounds=2.0, tiles=None, seed=0, count=None):
         nt = (N + 1 + 7) // 8
         tiles = [tuple(int(v) for v in rng.integers(0, nt, 3)) for _ in range(count)]
     boxes, pts, parents = lattice_tiles(N, bounds, tiles, with_parents=True)
-    w, ops, full, pruned, full4, pruned4 = prune_host(cu, boxes, pts)
+    w, ops, full, pruned, full4, pruned4, root = prune_host(cu, boxes, pts)
     assert w > 0, "no pruning form"
     bad = full.view(np.uint32) != pruned.view(np.uint32)
     assert not bad.any(), f"{int(bad.sum())} pruned values differ, e.g. tile {np.argwhere(bad)[0]}"
     bad4 = full4.view(np.uint32) != pruned4.view(np.uint32)
     assert not bad4.any(), f"{int(bad4.sum())} run-of-4 pruned values differ, e.g. {np.argwhere(bad4)[0]}"
+    # the interval of the SDF's value bounds every point of the tile (a
+    # "decided" tile's points are never evaluated); NaN intervals are unknown
+    known = np.isfinite(root).all(axis=1)
+    fin = np.isfinite(full)
+    assert ((full >= root[:, :1]) | ~fin | ~known[:, None]).all(), "value below its tile's interval"
+    assert ((full <= root[:, 1:]) | ~fin | ~known[:, None]).all(), "value above its tile's interval"
+    assert (fin | ~known[:, None]).all(), "a known interval must bound finite values"
     # two-level tile pass: the tile's bits from its coarse box's bits
-    ops_in, pruned_in = prune_host_in(cu, parents, boxes, pts)
+    ops_in, pruned_in, root_in = prune_host_in(cu, parents, boxes, pts)
+    known_in = np.isfinite(root_in).all(axis=1)
+    assert ((full >= root_in[:, :1]) & (full <= root_in[:, 1:]) | ~known_in[:, None]).all()
     bad_in = full.view(np.uint32) != pruned_in.view(np.uint32)
     assert not bad_in.any(), f"{int(bad_in.sum())} values differ with two-level bits, e.g. {np.argwhere(bad_in)[0]}"
     assert (ops_in[:, 0] <= ops[:, 0] + 0.5).all()  # a coarse decision is never undone
