@@ -81,10 +81,11 @@ class Pruner {
     if (ir_.root < 0 || ir_.root >= n_) return pc;
     mark_live();
     // 1. every combinator enabled; 2. keep those with a side worth skipping
+    // (With no combinator worth a branch the form is still emitted: the
+    // tile's value interval alone decides the tiles far from the surface.)
     std::vector<int> cand;
     for (int v = 0; v < n_; ++v)
       if (live_[v] && is_comb(ir_.nodes[size_t(v)].op)) cand.push_back(v);
-    if (cand.empty()) return pc;
     set_enabled(cand);
     owners();
     std::vector<double> sub = subtree_weights();
@@ -93,7 +94,6 @@ class Pruner {
       double w = std::max(sub[size_t(seg(int(ci), 0))], sub[size_t(seg(int(ci), 1))]);
       if (w >= kMinSkipWeight) keep.push_back({w, combs_[ci]});
     }
-    if (keep.empty()) return pc;
     if (int(keep.size()) > kMaxCombinators) {
       std::stable_sort(keep.begin(), keep.end(), [](auto &x, auto &y) { return x.first > y.first; });
       keep.resize(size_t(kMaxCombinators));
@@ -104,7 +104,7 @@ class Pruner {
     set_enabled(en);
     owners();
     pc.combinators = int(combs_.size());
-    pc.words = (2 * pc.combinators + 31) / 32;
+    pc.words = std::max(1, (2 * pc.combinators + 31) / 32);
     std::ostringstream o;
     o << "// tile pruning: " << pc.combinators << " combinators, " << pc.words << " words of activity bits\n";
     o << "#define S2M_HAS_PRUNE 1\n#define S2M_PRUNE_WORDS " << pc.words << "\n";

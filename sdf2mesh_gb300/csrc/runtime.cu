@@ -78,18 +78,21 @@ int device_sm_count() {
 
 // Evaluation-kernel variants compiled into every SDF module (the tables in
 // s2m_dc_kernels.cuh): name, z-run length, whether it evaluates the run-of-4
-// form, and whether it is a tile-pruned variant (present only in modules of
-// SDFs with a pruning form).
+// form, whether it is a tile-pruned variant (present only in modules of SDFs
+// with a pruning form), and whether its warps take tiles from a counter
+// (persistent launch).
 struct EvalVariant {
   const char *name;
   int run;
   bool vec;
   bool pruned;
+  bool dynamic;
 };
 constexpr EvalVariant kEvalVariants[] = {
-    {"s2m_eval_b2r4", 4, false, false}, {"s2m_eval_b3r4", 4, false, false}, {"s2m_eval_b4r4", 4, false, false},
-    {"s2m_eval_b2v4", 4, true, false},  {"s2m_eval_b3v4", 4, true, false},  {"s2m_evalp_b8", 1, false, true},
-    {"s2m_evalp_b12", 1, false, true},  {"s2m_evalp_b8v4", 4, true, true}};
+    {"s2m_eval_b2r4", 4, false, false, false}, {"s2m_eval_b3r4", 4, false, false, false},
+    {"s2m_eval_b4r4", 4, false, false, false}, {"s2m_eval_b2v4", 4, true, false, false},
+    {"s2m_eval_b3v4", 4, true, false, false},  {"s2m_evalp_b8", 1, false, true, false},
+    {"s2m_evalpd_b8", 1, false, true, true},   {"s2m_evalpd_b12", 1, false, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -131,9 +134,10 @@ struct s2m_mesh {
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
-  // tile pruning: [ops FP32, ops SFU] (2 u64), the first tile and the first
-  // coarse box of every slab (2 x nslabs + 1 u64), then the activity words
-  // of `prune_chunk` slabs' coarse boxes and tiles
+  // tile pruning: [ops FP32, ops SFU] (2 u64), a tile counter per slab (u32,
+  // the persistent variants), the first tile and the first coarse box of
+  // every slab (2 x nslabs + 1 u64), then the activity words of
+  // `prune_chunk` slabs' coarse boxes and tiles
   unsigned long long *prune_buf = nullptr;
   std::vector<unsigned long long> slab_tile_base, slab_coarse_base;  // host copies
   int prune_chunk = 0;
@@ -434,7 +438,7 @@ size_t prune_layout(s2m_mesh *m) {
     chunk_coarse = std::max(chunk_coarse, m->slab_coarse_base[size_t(e)] - m->slab_coarse_base[size_t(s)]);
   }
   auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-  m->prune_base_off = 16;
+  m->prune_base_off = up16(16 + 4 * size_t(ns));
   m->prune_cbase_off = up16(m->prune_base_off + 8 * (size_t(ns) + 1));
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * words * 4);
@@ -444,6 +448,7 @@ template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
 }
 unsigned long long *prune_bases(const s2m_mesh *m) { return prune_at<unsigned long long>(m, m->prune_base_off); }
+unsigned *prune_counters(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
 // Tile pass over slabs [s_begin, s_end) (coarse boxes, then tiles) and the
 // pruned evaluation of slab s.
@@ -475,6 +480,20 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
                                                                      m->slab_tile_base[size_t(chunk_begin)]) *
                                                                         (size_t(m->sdf->prune_words) + 1);
   S2PointBits pb = point_bits(m);
+  if (kEvalVariants[v].dynamic) {
+    unsigned *counter = prune_counters(m) + s;
+    void *dargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m->sdf->k_eval[v], S2_PT_BLOCK, 0) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 4;
+    }
+    const long long blocks = std::min<long long>((g.ntiles + 3) / 4, (long long)device_sm_count() * per_sm);
+    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned(std::max<long long>(1, blocks))),
+                            dim3(S2_PT_BLOCK), dargs, 0, st);
+  }
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
                           0, st);
@@ -653,7 +672,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->last_variant = ev;
   m->eval_points = 0;
   m->eval_fp_ops = m->eval_sfu_ops = 0;
-  if (pruned) {  // operation counters
+  if (pruned) {  // operation counters and the slabs' tile counters
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }

@@ -391,6 +391,40 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
 }
 
+// Persistent form: every warp takes tiles one at a time from the slab's
+// counter until none are left.  A decided tile costs a few instructions per
+// point and a tile on the surface up to a hundred times more; taken per warp,
+// the fast tiles do not hold a block's other warps, and no warp waits at the
+// end of a fixed share.
+template <bool RUN4>
+__device__ __forceinline__ void s2_eval_pruned_dyn(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
+                                                   const unsigned *__restrict__ bits, int k0, int nk, int tzs,
+                                                   int nzt, unsigned *__restrict__ counter) {
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const long long ntiles = (long long)ntx * ntx * nzt;
+  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_TILE_WORDS];
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
+#pragma unroll 1
+  for (;;) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1u);
+    t = __shfl_sync(S2_FULL, t, 0);
+    if ((long long)t >= ntiles) break;
+    const S2PruneTile tl = s2_prune_tile(job, (long long)t, k0, nk, tzs);
+    if (tl.kb > tl.ke) continue;
+    if (lane < S2M_TILE_WORDS) s_bits[warp][lane] = __ldg(bits + (unsigned long long)t * S2M_TILE_WORDS + lane);
+    __syncwarp();
+    s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[warp]);
+    __syncwarp();
+  }
+}
+
+#define S2_EVALPD_VARIANT(NAME, MINB, RUN4)                                                       \
+  extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
+  NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
+       int tzs, int nzt, unsigned *counter) {                                                     \
+    s2_eval_pruned_dyn<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt, counter);                     \
+  }
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
   NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
@@ -399,8 +433,8 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   }
 // Keep this table in step with kEvalVariants in runtime.cu.
 S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
-S2_EVALP_VARIANT(s2m_evalp_b12, 12, false)
-S2_EVALP_VARIANT(s2m_evalp_b8v4, 8, true)
+S2_EVALPD_VARIANT(s2m_evalpd_b8, 8, false)
+S2_EVALPD_VARIANT(s2m_evalpd_b12, 12, false)
 #endif
 
 

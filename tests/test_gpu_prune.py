@@ -19,7 +19,7 @@ from tests.test_prune_host import EDGE, SMOOTH_OPS
 
 pytestmark = pytest.mark.gpu
 
-PRUNED = (5, 6, 7)  # s2m_evalp_b8, s2m_evalp_b12, s2m_evalp_b8v4
+PRUNED = (5, 6, 7)  # s2m_evalp_b8, s2m_evalpd_b8, s2m_evalpd_b12 (persistent)
 PLAIN = 1        # s2m_eval_b3r4
 
 
@@ -99,8 +99,7 @@ def test_slab_depths(csg64, depth):
 def test_random_trees_pruned(lib, seed):
     src, prog = workloads.random_tree(seed)
     pruned, plain = pair(src)
-    if pruned.prune_info()[0] == 0:
-        pytest.skip("tree without a combinator worth pruning")
+    assert pruned.prune_info()[1] > 0  # every straight-line SDF has the tile form
     N = [48, 64, 96, 40][seed % 4]
     got, _ = mesh(pruned, N, PRUNED[0])
     assert_bit_exact(got, oracle.mesh(oracle.TREE, prog, N, 2.0), f"tree {seed} pruned")
@@ -137,3 +136,17 @@ def test_job_modes_pruned_equals_full(csg64, mode):
         got, ops = mesh(pruned, N, v, **kw)
         assert ops["pruned"]
         same_mesh(got, full, f"{mode} variant {v}")
+
+
+@pytest.mark.parametrize("kind", ["torus", "sphere"])
+def test_tile_form_without_combinators(lib, kind):
+    """No combinator to prune: only the decided tiles far from the surface
+    skip evaluation, and the mesh is bit-identical."""
+    src = getattr(workloads, kind)()[0]
+    pruned, plain = pair(src)
+    assert pruned.prune_info() == (0, 1)
+    full, ops_full = mesh(plain, 200, PLAIN)
+    for v in PRUNED:
+        got, ops = mesh(pruned, 200, v)
+        same_mesh(got, full, f"{kind} variant {v}")
+        assert ops["fp32_ops"] < 0.5 * ops_full["fp32_ops"]

@@ -134,9 +134,13 @@ fn sdf3d(p: vec3f) -> f32 {
     check(cu, 64, count=200)
 
 
-def test_no_pruning_form_without_combinators_or_with_loops(lib):
-    cu, _, _ = lowered(workloads.torus()[0] if isinstance(workloads.torus(), tuple) else workloads.torus())
-    assert "S2M_HAS_PRUNE" not in cu
-    mb = workloads.mandelbulb()
-    cu, _, _ = lowered(mb[0] if isinstance(mb, tuple) else mb, s2m.LANG_GLSL, "sdf")
+def test_tile_form_without_combinators_and_none_with_loops(lib):
+    """A straight-line SDF without combinators still gets the tile form (its
+    value interval decides the tiles far from the surface); one with loops
+    gets none."""
+    cu, _, _ = lowered(workloads.torus()[0])
+    assert "S2M_HAS_PRUNE" in cu and "tile pruning: 0 combinators" in cu
+    ops = check(cu, 48)
+    assert (ops[:, 0] >= 0).all()
+    cu, _, _ = lowered(workloads.mandelbulb()[0], s2m.LANG_GLSL, "sdf")
     assert "S2M_HAS_PRUNE" not in cu
