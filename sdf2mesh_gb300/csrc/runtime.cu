@@ -79,20 +79,20 @@ int device_sm_count() {
 // Evaluation-kernel variants compiled into every SDF module (the tables in
 // s2m_dc_kernels.cuh): name, z-run length, whether it evaluates the run-of-4
 // form, whether it is a tile-pruned variant (present only in modules of SDFs
-// with a pruning form), and whether its warps take tiles from a counter
-// (persistent launch).
+// with a pruning form), and whether it evaluates only the tile pass's list of
+// undecided tiles (after s2m_fill_decided).
 struct EvalVariant {
   const char *name;
   int run;
   bool vec;
   bool pruned;
-  bool dynamic;
+  bool listed;
 };
 constexpr EvalVariant kEvalVariants[] = {
     {"s2m_eval_b2r4", 4, false, false, false}, {"s2m_eval_b3r4", 4, false, false, false},
     {"s2m_eval_b4r4", 4, false, false, false}, {"s2m_eval_b2v4", 4, true, false, false},
     {"s2m_eval_b3v4", 4, true, false, false},  {"s2m_evalp_b8", 1, false, true, false},
-    {"s2m_evalpd_b8", 1, false, true, true},   {"s2m_evalpd_b12", 1, false, true, true}};
+    {"s2m_evalpl_b8", 1, false, true, true},   {"s2m_evalpl_b8v4", 4, true, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
 struct s2m_sdf {
@@ -134,10 +134,10 @@ struct s2m_mesh {
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
-  // tile pruning: [ops FP32, ops SFU] (2 u64), a tile counter per slab (u32,
-  // the persistent variants), the first tile and the first coarse box of
-  // every slab (2 x nslabs + 1 u64), then the activity words of
-  // `prune_chunk` slabs' coarse boxes and tiles
+  // tile pruning: [ops FP32, ops SFU] (2 u64), the length of each slab's list
+  // of undecided tiles (u32), the first tile and the first coarse box of
+  // every slab (2 x nslabs + 1 u64), then for `prune_chunk` slabs the
+  // activity words of the coarse boxes and the tiles, and the tile lists
   unsigned long long *prune_buf = nullptr;
   std::vector<unsigned long long> slab_tile_base, slab_coarse_base;  // host copies
   int prune_chunk = 0;
@@ -145,6 +145,7 @@ struct s2m_mesh {
   size_t prune_cbase_off = 0;  // ... to the slab coarse-box bases
   size_t prune_sbits_off = 0;  // ... to the coarse boxes' activity words
   size_t prune_bits_off = 0;   // ... to the tiles' activity words
+  size_t prune_list_off = 0;   // ... to the lists of undecided tiles
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -442,13 +443,14 @@ size_t prune_layout(s2m_mesh *m) {
   m->prune_cbase_off = up16(m->prune_base_off + 8 * (size_t(ns) + 1));
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * words * 4);
-  return m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4;  // + each tile's flag word
+  m->prune_list_off = up16(m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4);  // + each tile's flag word
+  return m->prune_list_off + size_t(chunk_tiles) * 4;
 }
 template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
 }
 unsigned long long *prune_bases(const s2m_mesh *m) { return prune_at<unsigned long long>(m, m->prune_base_off); }
-unsigned *prune_counters(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
+unsigned *prune_list_counts(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
 // Tile pass over slabs [s_begin, s_end) (coarse boxes, then tiles) and the
 // pruned evaluation of slab s.
@@ -466,7 +468,9 @@ cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t
                                    dim3(unsigned((nc + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), cargs, 0, st);
   if (e != cudaSuccess) return e;
   const unsigned long long n = m->slab_tile_base[size_t(s_end)] - m->slab_tile_base[size_t(s_begin)];
-  void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc};
+  unsigned *list = prune_at<unsigned>(m, m->prune_list_off);
+  unsigned *counts = prune_list_counts(m);
+  void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc, &list, &counts};
   return cudaLaunchKernel((const void *)m->sdf->k_tiles, dim3(unsigned((n + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
                           dim3(S2_PT_BLOCK), targs, 0, st);
 }
@@ -480,19 +484,18 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
                                                                      m->slab_tile_base[size_t(chunk_begin)]) *
                                                                         (size_t(m->sdf->prune_words) + 1);
   S2PointBits pb = point_bits(m);
-  if (kEvalVariants[v].dynamic) {
-    unsigned *counter = prune_counters(m) + s;
-    void *dargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt, &counter};
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m->sdf->k_eval[v], S2_PT_BLOCK, 0) !=
-            cudaSuccess ||
-        per_sm < 1) {
-      cudaGetLastError();
-      per_sm = 4;
-    }
-    const long long blocks = std::min<long long>((g.ntiles + 3) / 4, (long long)device_sm_count() * per_sm);
-    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned(std::max<long long>(1, blocks))),
-                            dim3(S2_PT_BLOCK), dargs, 0, st);
+  if (kEvalVariants[v].listed) {
+    const int W1 = m->sdf->prune_words + 1;
+    const dim3 fg(unsigned((m->job.P + 255) / 256), unsigned((m->job.P + 7) / 8), unsigned(nk));
+    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, ring, pb, bits, W1, k0, g.tzs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
+                           (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
+    const unsigned *count = prune_list_counts(m) + s;
+    void *largs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &list, &count};
+    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK),
+                            largs, 0, st);
   }
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
@@ -672,7 +675,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->last_variant = ev;
   m->eval_points = 0;
   m->eval_fp_ops = m->eval_sfu_ops = 0;
-  if (pruned) {  // operation counters and the slabs' tile counters
+  if (pruned) {  // operation counters and the slabs' list lengths
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }

@@ -227,7 +227,8 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops,
           const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
-          const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc) {
+          const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc,
+          unsigned *__restrict__ list, unsigned *__restrict__ list_count) {
   const unsigned long long b0 = tbase[s_begin], b1 = tbase[s_end];
   const unsigned long long g = b0 + (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
   unsigned long long fp_ops = 0, sfu_ops = 0;
@@ -260,6 +261,10 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
 #pragma unroll
     for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
     dst[S2M_PRUNE_WORDS] = flag;
+    if (!flag) {  // the slab's list of tiles to evaluate (in any order)
+      const unsigned i = atomicAdd(list_count + s, 1u);
+      list[(tbase[s] - b0) + i] = (unsigned)t;
+    }
     const unsigned long long npts = (unsigned long long)(tl.i1 - tl.i0 + 1) * (unsigned long long)(tl.j1 - tl.j0 + 1) *
                                     (unsigned long long)max(0, tl.ke - tl.kb + 1);
     fp_ops = (unsigned long long)fp * npts;
@@ -391,39 +396,31 @@ __device__ __forceinline__ void s2_eval_pruned(const S2Job &job, float *__restri
   s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
 }
 
-// Persistent form: every warp takes tiles one at a time from the slab's
-// counter until none are left.  A decided tile costs a few instructions per
-// point and a tile on the surface up to a hundred times more; taken per warp,
-// the fast tiles do not hold a block's other warps, and no warp waits at the
-// end of a fixed share.
+// The listed form: only the slab's undecided tiles (the tile pass's list),
+// one per warp; s2m_fill_decided has written the decided ones.  Every warp
+// then has real work, so the blocks are about equally long.
 template <bool RUN4>
-__device__ __forceinline__ void s2_eval_pruned_dyn(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
-                                                   const unsigned *__restrict__ bits, int k0, int nk, int tzs,
-                                                   int nzt, unsigned *__restrict__ counter) {
-  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const long long ntiles = (long long)ntx * ntx * nzt;
+__device__ __forceinline__ void s2_eval_pruned_listed(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
+                                                      const unsigned *__restrict__ bits, int k0, int nk, int tzs,
+                                                      const unsigned *__restrict__ list,
+                                                      const unsigned *__restrict__ list_count) {
+  const unsigned i = blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5);
+  if (i >= __ldg(list_count)) return;  // whole warps
+  const unsigned t = __ldg(list + i);
+  const S2PruneTile tl = s2_prune_tile(job, (long long)t, k0, nk, tzs);
+  if (tl.kb > tl.ke) return;
   __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_TILE_WORDS];
-  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
-#pragma unroll 1
-  for (;;) {
-    unsigned t = 0;
-    if (lane == 0) t = atomicAdd(counter, 1u);
-    t = __shfl_sync(S2_FULL, t, 0);
-    if ((long long)t >= ntiles) break;
-    const S2PruneTile tl = s2_prune_tile(job, (long long)t, k0, nk, tzs);
-    if (tl.kb > tl.ke) continue;
-    if (lane < S2M_TILE_WORDS) s_bits[warp][lane] = __ldg(bits + (unsigned long long)t * S2M_TILE_WORDS + lane);
-    __syncwarp();
-    s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[warp]);
-    __syncwarp();
-  }
+  const int lane = (int)(threadIdx.x & 31u);
+  if (lane < S2M_TILE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + (unsigned long long)t * S2M_TILE_WORDS + lane);
+  __syncwarp();
+  s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
 }
 
-#define S2_EVALPD_VARIANT(NAME, MINB, RUN4)                                                       \
+#define S2_EVALPL_VARIANT(NAME, MINB, RUN4)                                                       \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
   NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
-       int tzs, int nzt, unsigned *counter) {                                                     \
-    s2_eval_pruned_dyn<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt, counter);                     \
+       int tzs, const unsigned *__restrict__ list, const unsigned *__restrict__ list_count) {     \
+    s2_eval_pruned_listed<RUN4>(job, ring, pb, bits, k0, nk, tzs, list, list_count);              \
   }
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
@@ -433,8 +430,8 @@ __device__ __forceinline__ void s2_eval_pruned_dyn(const S2Job &job, float *__re
   }
 // Keep this table in step with kEvalVariants in runtime.cu.
 S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
-S2_EVALPD_VARIANT(s2m_evalpd_b8, 8, false)
-S2_EVALPD_VARIANT(s2m_evalpd_b12, 12, false)
+S2_EVALPL_VARIANT(s2m_evalpl_b8, 8, false)
+S2_EVALPL_VARIANT(s2m_evalpl_b8v4, 8, true)
 #endif
 
 

@@ -101,6 +101,33 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
   }
 }
 
+// The points of a slab's decided tiles (the pruned evaluation's tile pass
+// proved |f| >= guard there with a known sign): NaN values, and the known
+// point bits (sign from the tile's flag word, near-zero 0).  Planes
+// k0 .. k0 + gridDim.z - 1; one thread per 8 points (a tile's width) of a
+// row: grid (ceil(P / 256), ceil(P / 8), planes), no index division.
+__global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, float *__restrict__ ring, S2PointBits pb,
+                                                        const unsigned *__restrict__ tiles, int tile_words, int k0,
+                                                        int tzs) {
+  const int no = (job.P + 7) >> 3;  // 8-point groups per row = tiles along x
+  const int o = (int)blockIdx.x * 32 + (int)(threadIdx.x & 31u);
+  const int y = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+  if (o >= no || y >= job.P) return;
+  const int k = k0 + (int)blockIdx.z;
+  const unsigned long long t = ((unsigned long long)(blockIdx.z / (unsigned)tzs) * no + (y >> 3)) * no + o;
+  const unsigned flag = __ldg(tiles + t * tile_words + (tile_words - 1));
+  if (!(flag & 1u)) return;  // S2_TILE_DECIDED; its points are evaluated
+  const int slot = k % job.ring;
+  const int x0 = o * 8, n = min(8, job.P - x0);
+  float *dst = ring + (long long)slot * job.plane + (long long)y * job.pitch + x0;
+  const float nan = __int_as_float(0x7fc00000);
+  for (int i = 0; i < n; ++i) dst[i] = nan;
+  const int WP = (job.P + 31) >> 5;
+  const long long byte = (((long long)slot * job.P + y) * WP) * 4 + o;
+  reinterpret_cast<unsigned char *>(pb.pos)[byte] = (flag & 2u) ? (unsigned char)((1u << n) - 1u) : 0u;  // S2_TILE_POSITIVE
+  reinterpret_cast<unsigned char *>(pb.near)[byte] = 0u;
+}
+
 // Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.
 // Its coordinates from the block's first word (one 64-bit division per
 // block; 32-bit ones per thread).

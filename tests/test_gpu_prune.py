@@ -19,7 +19,7 @@ from tests.test_prune_host import EDGE, SMOOTH_OPS
 
 pytestmark = pytest.mark.gpu
 
-PRUNED = (5, 6, 7)  # s2m_evalp_b8, s2m_evalpd_b8, s2m_evalpd_b12 (persistent)
+PRUNED = (5, 6, 7)  # s2m_evalp_b8, s2m_evalpl_b8, s2m_evalpl_b8v4 (undecided tiles listed)
 PLAIN = 1        # s2m_eval_b3r4
 
 
