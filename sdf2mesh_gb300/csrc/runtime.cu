@@ -358,13 +358,26 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   j.magic_n = uint32_t((1ull << 32) / uint64_t(j.N) + 1);
   j.magic_p = uint32_t((1ull << 32) / uint64_t(j.P) + 1);
   m->nzc = j.lag ? int(N) - 1 : int(N);
-  // Slab depth: the ring of D + 1 lattice planes is sized to stay resident in
-  // the 126 MB L2 between the evaluation and the cell pass.
+  // Slab depth.  Full evaluation: the ring of D + 1 lattice planes is sized
+  // to stay resident in the 126 MB L2 between the evaluation and the point
+  // bits pass.  An SDF with a tile form: the pruned evaluation writes the
+  // point bits itself and classification reads only those (and the
+  // candidates' corners), so the ring need not fit in L2; deep slabs (a ring
+  // of up to 4 GB, slabs of equal depth) amortise each slab's evaluation
+  // tail, where its last heavy tiles run at low occupancy (a 1024^3 CSG job:
+  // 16.3 ms with 10-plane slabs, 7.9 ms with 512).
   int D = int(p.slab_depth);
   if (D <= 0) {
-    double plane_bytes = double(j.plane) * 4.0;
-    D = int(48.0e6 / plane_bytes) - 1;
-    D = std::max(1, std::min(D, 64));
+    const double plane_bytes = double(j.plane) * 4.0;
+    if (m->sdf && m->sdf->k_tiles) {
+      const int dmax = std::max(1, int(std::min(4.0e9 / plane_bytes, 1.0e9)) - 1);
+      const int nz = std::max(1, m->nzc);
+      const int ns = (nz + dmax - 1) / dmax;
+      D = (nz + ns - 1) / ns;
+    } else {
+      D = int(48.0e6 / plane_bytes) - 1;
+      D = std::max(1, std::min(D, 64));
+    }
   }
   D = std::max(1, std::min(D, std::max(1, m->nzc)));
   m->D = D;
