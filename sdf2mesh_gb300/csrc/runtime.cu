@@ -130,7 +130,7 @@ struct s2m_mesh {
   // workspace
   float *ring = nullptr;
   unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
-  unsigned *pt_bits = nullptr;               // sign, then near-zero bits of the ring's lattice points
+  unsigned *pt_bits = nullptr;               // sign, near-zero, then unknown-value bits of the ring's lattice points
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
   unsigned *tile_cnt = nullptr;              // per cell tile: candidates
@@ -386,8 +386,8 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   return S2M_OK;
 }
 
-// Point bits of the ring (two arrays of ring * P * ceil(P / 32) words).
-size_t pt_bits_words(const s2m_mesh *m) {  // one of the two arrays (S2PointBits)
+// Point bits of the ring (three arrays of ring * P * ceil(P / 32) words).
+size_t pt_bits_words(const s2m_mesh *m) {  // one of the three arrays (S2PointBits)
   const size_t P = size_t(m->job.P), WP = (P + 31) / 32;
   return size_t(m->job.ring) * P * WP;
 }
@@ -395,6 +395,7 @@ S2PointBits point_bits(const s2m_mesh *m) {
   S2PointBits pb;
   pb.pos = m->pt_bits;
   pb.near = m->pt_bits + pt_bits_words(m);
+  pb.unk = m->pt_bits + 2 * pt_bits_words(m);
   return pb;
 }
 
@@ -500,7 +501,7 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   if (kEvalVariants[v].listed) {
     const int W1 = m->sdf->prune_words + 1;
     const dim3 fg(unsigned((m->job.P + 255) / 256), unsigned((m->job.P + 7) / 8), unsigned(nk));
-    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, ring, pb, bits, W1, k0, g.tzs);
+    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, g.tzs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
@@ -545,9 +546,9 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   cudaStream_t st = m->stream;
   S2_CUDA(cudaMallocAsync(&m->ring, ring_floats * sizeof(float), st));
   S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->pt_bits, 2 * pt_bits_words(m) * 4, st));
+  S2_CUDA(cudaMallocAsync(&m->pt_bits, 3 * pt_bits_words(m) * 4, st));
   // the words' bits past the lattice edge are never written and must read 0
-  S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, 2 * pt_bits_words(m) * 4, st));
+  S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, 3 * pt_bits_words(m) * 4, st));
   S2_CUDA(cudaMallocAsync(&m->offx, size_t((j.N + 31) / 32) * 4, st));
   S2_CUDA(cudaMallocAsync(&m->cell_words, m->cell_tiles * S2_CW_BLOCK * 4, st));
   S2_CUDA(cudaMallocAsync(&m->tile_cnt, (m->cell_tiles + 1) * 4, st));  // + the finished-block counter
@@ -723,8 +724,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                                                                     m->tile_cnt + m->cell_tiles, m->slab_ctrl,
                                                                     m->cand_base, s, zc0, zc1),
                           cudaGetLastError()));
-    S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->ring, m->cell_words, m->slab_ctrl, cand, c.err,
-                                                               zc0, zc1),
+    S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
+                                                               m->cell_words, m->slab_ctrl, cand, c.err, zc0, zc1),
                      cudaGetLastError()));
   }
   S2Job jj = j;
@@ -1311,7 +1312,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   size_t used = 0;
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
-            carve(base, used, 2 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
+            carve(base, used, 3 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
             carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles + 1, &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&

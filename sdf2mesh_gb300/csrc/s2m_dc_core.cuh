@@ -509,13 +509,24 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
   const unsigned lt = s2_lanemask_lt();
   float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
   float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
-  const unsigned off = active ? (s2_off_mask(j, c) & 0xfeu) : 0u;
+  // Corners evaluated here: the off-lattice ones (at the cell's reference
+  // coordinates) and those the lattice pass left unknown (NaN, decided tiles
+  // of the pruned evaluation).  An unknown corner that is on the lattice has
+  // reference coordinates equal to its lattice coordinates, so both kinds are
+  // evaluated at the cell's bounds.
+  unsigned off = 0u;
+  if (active) {
+    off = s2_off_mask(j, c) & 0xfeu;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (v[k] != v[k]) off |= 1u << k;
+  }
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     ws.lo[lane][a] = mn[a];
     ws.hi[lane][a] = mx[a];
   }
-  // 1. off-lattice corners
+  // 1. off-lattice and unknown corners
   unsigned cnt = __popc(off), inc = cnt;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -545,7 +556,7 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
   }
   __syncwarp();
 #pragma unroll
-  for (int k = 1; k < 8; ++k)
+  for (int k = 0; k < 8; ++k)
     if ((off >> k) & 1u) v[k] = ws.val[lane][k];
   // 2. crossings and mass point (dualcontour.wgsl:86-131)
   const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};

@@ -132,9 +132,10 @@ struct S2PruneTile {
 // S2_TILE_DECIDED: the interval of the SDF's value over the tile's box lies
 // at or beyond +guard (with S2_TILE_POSITIVE) or -guard, so every point's
 // sign bit is known and its near-zero bit is 0 -- all that classification
-// reads -- and the points are not evaluated.  Their lattice values are
-// written as NaN; the vertex kernel evaluates any such corner of a candidate
-// cell exactly (s2_fill_unknown_corners), so the mesh does not change.
+// reads -- and the points are not evaluated.  Their values are not written:
+// their unknown-value bits (S2PointBits::unk) are set instead, the candidate
+// records get NaN for such corners, and the vertex kernel evaluates those
+// exactly, so the mesh does not change.
 #define S2M_TILE_WORDS (S2M_PRUNE_WORDS + 1)
 #define S2_TILE_DECIDED 1u
 #define S2_TILE_POSITIVE 2u
@@ -284,18 +285,20 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
 // Point bits of one warp-wide step of a tile: the 32 lanes hold 8 points
 // along x times 4 rows from `y0` in the plane at ring slot `slot`, so each
 // ballot holds one byte (8 points) per row.  Lanes 0-3 store the sign bytes
-// of rows y0 .. y0 + 3, lanes 4-7 the near-zero bytes.
+// of rows y0 .. y0 + 3, lanes 4-7 the near-zero bytes, lanes 8-11 the
+// unknown-value bytes.
 __device__ __forceinline__ void s2_tile_bits(const S2Job &job, S2PointBits pb, const S2PruneTile &tl, int y0,
-                                             int slot, bool is_pos, bool is_near) {
+                                             int slot, bool is_pos, bool is_near, bool is_unk) {
   const unsigned pos = __ballot_sync(S2_FULL, is_pos);
   const unsigned near = __ballot_sync(S2_FULL, is_near);
+  const unsigned unk = __ballot_sync(S2_FULL, is_unk);
   const int lane = (int)(threadIdx.x & 31u);
   const int r = lane & 3, y = y0 + r;
-  if (lane < 8 && y <= tl.j1) {
+  if (lane < 12 && y <= tl.j1) {
     const int WP = (job.P + 31) >> 5;
-    unsigned char *base = reinterpret_cast<unsigned char *>(lane < 4 ? pb.pos : pb.near);
+    unsigned char *base = reinterpret_cast<unsigned char *>(lane < 4 ? pb.pos : lane < 8 ? pb.near : pb.unk);
     base[(((long long)slot * job.P + y) * WP) * 4 + (tl.i0 >> 3)] =
-        (unsigned char)(((lane < 4 ? pos : near) >> (8 * r)) & 0xffu);
+        (unsigned char)(((lane < 4 ? pos : lane < 8 ? near : unk) >> (8 * r)) & 0xffu);
   }
 }
 
@@ -314,10 +317,8 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
   const int lane = (int)(threadIdx.x & 31u);
   const int i = tl.i0 + (lane & 7), ja = tl.j0 + (lane >> 3);
   const unsigned flag = m[S2M_PRUNE_WORDS];
-  if (flag & S2_TILE_DECIDED) {  // the same on the whole warp
-    const float nan = __int_as_float(0x7fc00000);
+  if (flag & S2_TILE_DECIDED) {  // the same on the whole warp: bits only, no values
     const bool pos = (flag & S2_TILE_POSITIVE) != 0u;
-    float *const col = ring + (long long)min(i, tl.i1);
     int slot = tl.kb % job.ring;
 #pragma unroll 1
     for (int k = tl.kb; k <= tl.ke; ++k) {
@@ -325,8 +326,7 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
       for (int h = 0; h < 2; ++h) {
         const int j = ja + 4 * h;
         const bool store = i <= tl.i1 && j <= tl.j1;
-        if (store) col[(long long)slot * job.plane + (long long)j * job.pitch] = nan;
-        s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store && pos, false);
+        s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store && pos, false, store);
       }
       if (++slot == job.ring) slot = 0;
     }
@@ -354,7 +354,7 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
           if (k + w <= tl.ke) {  // the same on every lane
             if (store) col[(long long)sw * job.plane + (long long)j * job.pitch] = f.v[w];
             s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, sw, store && f.v[w] > 0.0f,
-                         store && !(fabsf(f.v[w]) >= job.guard));
+                         store && !(fabsf(f.v[w]) >= job.guard), false);
           }
           if (++sw == job.ring) sw = 0;
         }
@@ -373,7 +373,7 @@ __device__ __forceinline__ void s2_eval_tile(const S2Job &job, float *__restrict
       const bool store = xin && j <= tl.j1;
       const float f = s2m_user_sdf_pruned(x, h ? y1 : y0, z, m);
       if (store) col[(long long)slot * job.plane + (long long)j * job.pitch] = f;
-      s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store && f > 0.0f, store && !(fabsf(f) >= job.guard));
+      s2_tile_bits(job, pb, tl, tl.j0 + 4 * h, slot, store && f > 0.0f, store && !(fabsf(f) >= job.guard), false);
     }
     if (++slot == job.ring) slot = 0;
   }
@@ -470,7 +470,8 @@ __device__ __forceinline__ const unsigned *s2_cell_bits(const S2Job &job, S2Cell
 // Lattice corners left unknown (NaN) by a decided tile of the pruned
 // evaluation: evaluated here at their lattice coordinates, exactly as the
 // lattice pass would have.  (A corner whose SDF value is NaN is evaluated
-// again, to the same NaN.)
+// again, to the same NaN.)  For the precision mode and SDFs with their own
+// normal; s2_vertex_warp evaluates them with its other requests.
 __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell c, float v[8]) {
 #pragma unroll 1
   for (int k = 0; k < 8; ++k)
@@ -513,7 +514,10 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
       const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
       const float4 a = src[0], b = src[1];
       v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-      s2_fill_unknown_corners(job, c, v);
+#ifndef S2M_QEF_MODULE
+      if (!S2UserSdfCall::kStdNormal)  // s2_vertex_warp evaluates unknown corners with its requests
+#endif
+        s2_fill_unknown_corners(job, c, v);
     }
     float pos[3], nrm[3];
     unsigned long long key;

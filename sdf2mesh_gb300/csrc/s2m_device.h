@@ -63,10 +63,13 @@ struct S2Cand {
 // indexed by ring slot like the lattice values: word ((k % ring) * P + y) *
 // WP + x / 32 (WP = ceil(P / 32)) holds bit x % 32 of plane k, row y; in
 // little-endian bytes, byte x / 8 holds bit x % 8.  Bits past the lattice
-// edge are 0.
+// edge are 0.  `unk` (pruned evaluation only): the point lies in a decided
+// tile, so its sign and near bits are known but its value was not computed
+// and the ring holds no value for it.
 struct S2PointBits {
   unsigned *pos;
   unsigned *near;
+  unsigned *unk;
 };
 
 // Mesh outputs and the cross-slab counters.

@@ -102,11 +102,11 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
 }
 
 // The points of a slab's decided tiles (the pruned evaluation's tile pass
-// proved |f| >= guard there with a known sign): NaN values, and the known
-// point bits (sign from the tile's flag word, near-zero 0).  Planes
-// k0 .. k0 + gridDim.z - 1; one thread per 8 points (a tile's width) of a
-// row: grid (ceil(P / 256), ceil(P / 8), planes), no index division.
-__global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, float *__restrict__ ring, S2PointBits pb,
+// proved |f| >= guard there with a known sign): the known point bits (sign
+// from the tile's flag word, near-zero 0, unknown value 1); no values.
+// Planes k0 .. k0 + gridDim.z - 1; one thread per 8 points (a tile's width)
+// of a row: grid (ceil(P / 256), ceil(P / 8), planes), no index division.
+__global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits pb,
                                                         const unsigned *__restrict__ tiles, int tile_words, int k0,
                                                         int tzs) {
   const int no = (job.P + 7) >> 3;  // 8-point groups per row = tiles along x
@@ -119,13 +119,11 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, float *__rest
   if (!(flag & 1u)) return;  // S2_TILE_DECIDED; its points are evaluated
   const int slot = k % job.ring;
   const int x0 = o * 8, n = min(8, job.P - x0);
-  float *dst = ring + (long long)slot * job.plane + (long long)y * job.pitch + x0;
-  const float nan = __int_as_float(0x7fc00000);
-  for (int i = 0; i < n; ++i) dst[i] = nan;
   const int WP = (job.P + 31) >> 5;
   const long long byte = (((long long)slot * job.P + y) * WP) * 4 + o;
   reinterpret_cast<unsigned char *>(pb.pos)[byte] = (flag & 2u) ? (unsigned char)((1u << n) - 1u) : 0u;  // S2_TILE_POSITIVE
   reinterpret_cast<unsigned char *>(pb.near)[byte] = 0u;
+  reinterpret_cast<unsigned char *>(pb.unk)[byte] = (unsigned char)((1u << n) - 1u);
 }
 
 // Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.
@@ -227,10 +225,12 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
 }
 
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
-// 8 lattice corner values.  A warp takes its words with candidates one at a
+// 8 lattice corner values (NaN where the point's unknown-value bit is set: a
+// decided tile of the pruned evaluation wrote no value there).  A warp takes its words with candidates one at a
 // time, lane l writing the cell of bit l: the corner loads of a word's cells
 // are then coalesced rows, and every lane works.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
+                                                            const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
                                                             S2Cand cand, unsigned *err, int zc0, int zc1) {
@@ -271,6 +271,17 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     }
     float v[8];
     s2_load_corners<false>(job, ring, cell, v);
+    if (unk) {  // corners of decided tiles: no value in the ring
+      const int WP = (job.P + 31) >> 5, w = cell.x >> 5;
+      const bool more = w + 1 < WP;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
+        const long long base = ((long long)((cell.z + (q >> 1)) % job.ring) * job.P + (cell.y + (q & 1))) * WP + w;
+        const unsigned lo = __ldg(unk + base), hi = more ? __ldg(unk + base + 1) : 0u;
+        if ((lo >> lane) & 1u) v[2 * q] = __int_as_float(0x7fc00000);
+        if ((__funnelshift_r(lo, hi, 1) >> lane) & 1u) v[2 * q + 1] = __int_as_float(0x7fc00000);
+      }
+    }
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
     float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
