@@ -153,6 +153,14 @@ struct s2m_mesh {
   unsigned long long cand_cap = 0;
   unsigned long long *cand_base = nullptr;    // nslabs + 1
   unsigned long long *cand_status = nullptr;  // vc_tiles
+  // vertex work in tile order (s2m_vtile_*), with tile pruning when every
+  // slab's tile bits stay resident: [part_base 2 u64 | tile counts (vt_tiles)
+  // + done counter | block totals (vt_blocks) | block offsets (vt_blocks u64)
+  // | tile and rank per candidate (u64) | permutation (u32)]
+  unsigned char *vt_buf = nullptr;
+  unsigned long long vt_tiles = 0;
+  unsigned vt_blocks = 0;
+  size_t vt_cnt_off = 0, vt_part_off = 0, vt_poff_off = 0, vt_rank_off = 0, vt_perm_off = 0;
   // outputs and job counters
   float *pos = nullptr, *nrm = nullptr;
   unsigned long long *key = nullptr;
@@ -313,7 +321,7 @@ void give_pinned_slot(unsigned long long *p) {
 void free_buffers(s2m_mesh *m) {
   void *ptrs[] = {m->ring, m->slab_ctrl, m->pt_bits, m->offx, m->cell_words, m->tile_cnt, m->prune_buf, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
                   m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
-                  m->jobctl};
+                  m->jobctl, m->vt_buf};
   for (void *p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   if (m->h_read) give_pinned_slot(m->h_read);
@@ -321,7 +329,7 @@ void free_buffers(s2m_mesh *m) {
   m->tile_cnt = nullptr; m->prune_buf = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
   m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
   m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
-  m->jobctl = nullptr; m->h_read = nullptr;
+  m->jobctl = nullptr; m->h_read = nullptr; m->vt_buf = nullptr;
 }
 
 int setup_job(s2m_mesh *m, char *err, size_t errlen) {
@@ -566,6 +574,17 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   S2_CUDA(cudaMallocAsync(&m->cand_nrm, m->cand_cap * 12, st));
   S2_CUDA(cudaMallocAsync(&m->cand_base, size_t(m->nslabs + 1) * 8, st));
   S2_CUDA(cudaMallocAsync(&m->cand_status, m->vc_tiles * 8, st));
+  if (m->prune_buf && m->prune_chunk >= m->nslabs && m->cand_cap < (1ull << 32)) {
+    auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+    m->vt_tiles = m->slab_tile_base[size_t(m->nslabs)] - m->slab_tile_base[0];
+    m->vt_blocks = unsigned((m->vt_tiles + S2_VT_TILE - 1) / S2_VT_TILE);
+    m->vt_cnt_off = 16;
+    m->vt_part_off = up16(m->vt_cnt_off + 4 * (size_t(m->vt_tiles) + 1));
+    m->vt_poff_off = up16(m->vt_part_off + 4 * size_t(m->vt_blocks));
+    m->vt_rank_off = up16(m->vt_poff_off + 8 * size_t(m->vt_blocks));
+    m->vt_perm_off = up16(m->vt_rank_off + 8 * size_t(m->cand_cap));
+    S2_CUDA(cudaMallocAsync(&m->vt_buf, m->vt_perm_off + 4 * size_t(m->cand_cap), st));
+  }
   S2_CUDA(cudaMallocAsync(&m->pos, m->vcap * 12, st));
   S2_CUDA(cudaMallocAsync(&m->nrm, m->vcap * 12, st));
   S2_CUDA(cudaMallocAsync(&m->key, m->vcap * 8, st));
@@ -735,7 +754,26 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                                                                              : nullptr;
   const unsigned long long *tbase = m->prune_buf ? prune_at<unsigned long long>(m, m->prune_base_off) : nullptr;
   int D = m->D, nzc = m->nzc;
-  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc};
+  const unsigned *perm = nullptr;
+  if (tbits && m->vt_buf) {  // candidates grouped by tile for the vertex kernel
+    unsigned *tcnt = reinterpret_cast<unsigned *>(m->vt_buf + m->vt_cnt_off);
+    unsigned *part = reinterpret_cast<unsigned *>(m->vt_buf + m->vt_part_off);
+    unsigned long long *pbase = reinterpret_cast<unsigned long long *>(m->vt_buf);
+    unsigned long long *poff = reinterpret_cast<unsigned long long *>(m->vt_buf + m->vt_poff_off);
+    unsigned long long *rank = reinterpret_cast<unsigned long long *>(m->vt_buf + m->vt_rank_off);
+    unsigned *vperm = reinterpret_cast<unsigned *>(m->vt_buf + m->vt_perm_off);
+    if ((e = cudaMemsetAsync(m->vt_buf, 0, m->vt_part_off, st)) != cudaSuccess) return e;
+    const unsigned cgrid = unsigned(sms) * 8;
+    S2_LAUNCH(2, 0, (s2m_vtile_count<<<cgrid, 256, 0, st>>>(j, cand, nslabs, tbase, D, nzc, tcnt, rank),
+                     cudaGetLastError()));
+    S2_LAUNCH(2, 0, (s2m_vtile_scan<<<m->vt_blocks, 256, 0, st>>>(tcnt, m->vt_tiles, part, poff, pbase,
+                                                                  tcnt + m->vt_tiles),
+                     cudaGetLastError()));
+    S2_LAUNCH(2, 0, (s2m_vtile_scatter<<<cgrid, 256, 0, st>>>(cand, nslabs, tcnt, poff, rank, vperm),
+                     cudaGetLastError()));
+    perm = vperm;
+  }
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm};
   const unsigned vx_grid = unsigned(sms) * 16;
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));

@@ -24,6 +24,35 @@ struct S2Cell {
   int x, y, z;
 };
 
+// Slab s evaluates lattice planes k0 .. k0 + nk - 1 (k0 = 0 for the first
+// slab, else s * D + 1; the last plane is min(nzc, (s + 1) * D)).  The tile
+// pruning cuts them into tiles of S2_PT_XY x S2_PT_XY points by
+// s2_tile_depth(nk) planes.
+__device__ __forceinline__ void s2_slab_planes(int s, int D, int nzc, int &k0, int &nk) {
+  const int zc0 = s * D;
+  const int zc1 = min(nzc, zc0 + D);
+  k0 = s == 0 ? 0 : zc0 + 1;
+  nk = zc1 - k0 + 1;
+}
+__device__ __forceinline__ int s2_tile_depth(int nk) {
+  const int parts = (nk + S2_PT_ZMAX - 1) / S2_PT_ZMAX;
+  return (nk + parts - 1) / parts;
+}
+// Index, among all tiles of the job, of the pruning tile whose box covers
+// cell c (its corners and normal samples): the tile of the cell's lattice
+// point (x, y, z + 1), whose box reaches one point further in +x, +y and -z.
+// tbase[s] is slab s's first tile.
+__device__ __forceinline__ unsigned long long s2_cell_prune_tile(const S2Job &job, S2Cell c,
+                                                                 const unsigned long long *tbase, int D, int nzc) {
+  const int s = c.z / D;
+  int k0, nk;
+  s2_slab_planes(s, D, nzc, k0, nk);
+  const int tz = (c.z + 1 - k0) / s2_tile_depth(nk);
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const unsigned long long t = ((unsigned long long)tz * ntx + c.y / S2_PT_XY) * ntx + c.x / S2_PT_XY;
+  return tbase[s] + t - tbase[0];
+}
+
 __device__ __forceinline__ S2Cell s2_cell_of(const S2Job &j, long long c, int zc0) {
   S2Cell r;
   if (c < 0x100000000ll) {

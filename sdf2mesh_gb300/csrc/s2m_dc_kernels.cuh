@@ -111,18 +111,8 @@ S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
 // s * D + 1; the last plane is min(nzc, (s + 1) * D)).  Its planes are cut
 // into tiles of 8 x 8 points by `tzs` planes (at most S2_PT_ZMAX, balanced),
 // nzt tiles in z; tile t = (tz * nty + ty) * ntx + tx.  slab_base[s] is the
-// index of slab s's first tile among all tiles of the job.
-
-__device__ __forceinline__ void s2_slab_planes(int s, int D, int nzc, int &k0, int &nk) {
-  const int zc0 = s * D;
-  const int zc1 = min(nzc, zc0 + D);
-  k0 = s == 0 ? 0 : zc0 + 1;
-  nk = zc1 - k0 + 1;
-}
-__device__ __forceinline__ int s2_tile_depth(int nk) {
-  const int parts = (nk + S2_PT_ZMAX - 1) / S2_PT_ZMAX;
-  return (nk + parts - 1) / parts;
-}
+// index of slab s's first tile among all tiles of the job.  (s2_slab_planes,
+// s2_tile_depth and s2_cell_prune_tile are in s2m_dc_core.cuh.)
 
 struct S2PruneTile {
   int i0, i1, j0, j1, kb, ke;  // inclusive point ranges
@@ -457,13 +447,7 @@ __device__ __forceinline__ float s2_sdf_for(const S2UserSdfPruned &f, unsigned l
 // The activity bits of the tile of cell c (all slabs' tiles in one buffer).
 __device__ __forceinline__ const unsigned *s2_cell_bits(const S2Job &job, S2Cell c, const unsigned *tbits,
                                                         const unsigned long long *tbase, int D, int nzc) {
-  const int s = c.z / D;
-  int k0, nk;
-  s2_slab_planes(s, D, nzc, k0, nk);
-  const int tz = (c.z + 1 - k0) / s2_tile_depth(nk);
-  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const unsigned long long t = ((unsigned long long)tz * ntx + c.y / S2_PT_XY) * ntx + c.x / S2_PT_XY;
-  return tbits + (tbase[s] + t - tbase[0]) * S2M_TILE_WORDS;
+  return tbits + s2_cell_prune_tile(job, c, tbase, D, nzc) * S2M_TILE_WORDS;
 }
 #endif
 
@@ -484,10 +468,12 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
 // final key and writes cand.pos / cand.nrm for cells with a vertex.  With
 // tbits (tile pruning, every slab's bits resident), the SDF evaluations use
-// the bits of each cell's tile.
+// the bits of each cell's tile, and `perm` (when given) lists the candidates
+// grouped by tile (s2m_vtile_*), so that a warp's evaluations take one path
+// through the pruned SDF.
 extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
-             int nzc) {
+             int nzc, const unsigned *perm) {
   __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
@@ -502,8 +488,9 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
   const unsigned long long stride = (unsigned long long)gridDim.x * S2_VX_BLOCK;
   for (unsigned long long base = (unsigned long long)blockIdx.x * S2_VX_BLOCK + (threadIdx.x & ~31u); base < n;
        base += stride) {
-    const unsigned long long o = base + (threadIdx.x & 31u);
-    const bool active = o < n;
+    const unsigned long long i = base + (threadIdx.x & 31u);
+    const bool active = i < n;
+    const unsigned long long o = active && perm ? (unsigned long long)perm[i] : i;
     unsigned long long k = active ? cand.key[o] : 0ull;
     S2Cell c;
     c.x = (int)(k & 0xffffull);

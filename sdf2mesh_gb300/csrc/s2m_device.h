@@ -107,6 +107,7 @@ struct S2MeshDev {
 // planes in z; the pruned evaluation runs one tile per warp, 4 per block.
 #define S2_PT_XY 8
 #define S2_PT_ZMAX 8
+#define S2_VT_TILE 2048  // per-tile candidate counts scanned per block of s2m_vtile_scan (256 threads x 8)
 #define S2_PT_BLOCK 128
 #define S2_PT_COARSE 4            /* tiles per coarse box of the tile pass, along x and y */
 #define S2_VX_BLOCK 128

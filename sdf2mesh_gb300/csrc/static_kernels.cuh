@@ -289,6 +289,91 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
   }
 }
 
+// Vertex work in tile order (tile pruning).  The vertex kernel evaluates the
+// SDF with the activity bits of each candidate's tile; lanes of a warp whose
+// candidates lie in different tiles take different paths through the pruned
+// SDF, one after the other.  Candidates are listed in (z, y, x) order, so 32
+// consecutive ones span several tiles.  A counting sort by tile gives the
+// vertex kernel a permutation that groups them:
+//   s2m_vtile_count    each candidate's tile and its rank among the tile's
+//   s2m_vtile_scan     exclusive scan of the per-tile counts
+//   s2m_vtile_scatter  perm[first of the tile + rank] = candidate
+// The mesh does not depend on the order: a candidate's vertex is a function
+// of its cell and its tile's bits alone.
+__global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, int nslabs,
+                                                       const unsigned long long *__restrict__ tbase, int D, int nzc,
+                                                       unsigned *tcnt, unsigned long long *__restrict__ trank) {
+  const unsigned long long n = min(cand.base[nslabs], cand.cap);
+  for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * 256u) {
+    const unsigned long long k = cand.key[i];
+    S2Cell c;
+    c.x = (int)(k & 0xffffull);
+    c.y = (int)((k >> 16) & 0xffffull);
+    c.z = (int)((k >> 32) & 0xffffull);
+    const unsigned long long t = s2_cell_prune_tile(job, c, tbase, D, nzc);
+    trank[i] = (t << 16) | atomicAdd(tcnt + t, 1u);  // a tile covers at most 8 x 8 x 8 cells
+  }
+}
+
+// tcnt[0 .. T) becomes each tile's first position within its block of
+// S2_VT_TILE tiles; part_cnt[b] = block b's total.  The last block to finish
+// scans the totals into part_off (part_base[0] = 0 on entry); `done` returns
+// to 0.
+__global__ void __launch_bounds__(256) s2m_vtile_scan(unsigned *tcnt, unsigned long long T, unsigned *part_cnt,
+                                                      unsigned long long *part_off, unsigned long long *part_base,
+                                                      unsigned *done) {
+  __shared__ unsigned s_warp[32];
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const unsigned long long b0 = (unsigned long long)blockIdx.x * S2_VT_TILE + 8ull * tid;
+  unsigned v[8], sum = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    v[q] = b0 + q < T ? tcnt[b0 + q] : 0u;
+    sum += v[q];
+  }
+  unsigned inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
+    if ((int)lane >= o) inc += t;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  if (tid < 32 && tid >= 8) s_warp[tid] = 0u;
+  __syncthreads();
+  if (warp == 0) s2_warp_exclusive32(s_warp);
+  __syncthreads();
+  unsigned run = s_warp[warp] + inc - sum;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (b0 + q < T) tcnt[b0 + q] = run;
+    run += v[q];
+  }
+  __shared__ bool s_last;
+  if (tid == 255) {
+    part_cnt[blockIdx.x] = run;  // the block's total
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  s2_scan_tiles<256>(part_cnt, gridDim.x, part_off, part_base, 0);
+  if (tid == 0) *done = 0u;
+}
+
+__global__ void __launch_bounds__(256) s2m_vtile_scatter(S2Cand cand, int nslabs, const unsigned *__restrict__ tcnt,
+                                                         const unsigned long long *__restrict__ part_off,
+                                                         const unsigned long long *__restrict__ trank,
+                                                         unsigned *__restrict__ perm) {
+  const unsigned long long n = min(cand.base[nslabs], cand.cap);
+  for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * 256u) {
+    const unsigned long long tr = trank[i], t = tr >> 16;
+    perm[part_off[t / S2_VT_TILE] + tcnt[t] + (tr & 0xffffull)] = (unsigned)i;
+  }
+}
+
 __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand cand, S2MeshDev mesh, int nslabs) {
   s2_vcompact_worker(job, cand, mesh, nslabs, blockIdx.x == 0);
 }
