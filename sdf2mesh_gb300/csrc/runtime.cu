@@ -508,7 +508,8 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   S2PointBits pb = point_bits(m);
   if (kEvalVariants[v].listed) {
     const int W1 = m->sdf->prune_words + 1;
-    const dim3 fg(unsigned((m->job.P + 255) / 256), unsigned((m->job.P + 7) / 8), unsigned(nk));
+    const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
+    const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(nk));
     s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, g.tzs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

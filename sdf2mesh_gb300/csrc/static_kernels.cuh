@@ -101,29 +101,36 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
   }
 }
 
-// The points of a slab's decided tiles (the pruned evaluation's tile pass
-// proved |f| >= guard there with a known sign): the known point bits (sign
-// from the tile's flag word, near-zero 0, unknown value 1); no values.
-// Planes k0 .. k0 + gridDim.z - 1; one thread per 8 points (a tile's width)
-// of a row: grid (ceil(P / 256), ceil(P / 8), planes), no index division.
+// The point bits of a slab's planes k0 .. k0 + gridDim.y - 1 in its decided
+// tiles (the pruned evaluation's tile pass proved |f| >= guard there with a
+// known sign): sign from the tile's flag word, near-zero 0, unknown value 1;
+// no values.  One thread per 32-point word of a row (4 tiles along x), grid
+// (ceil(P * WP / 256), planes): every word of the planes is written, the
+// undecided tiles' bytes as 0, which s2m_evalpl_* overwrites afterwards.
 __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits pb,
                                                         const unsigned *__restrict__ tiles, int tile_words, int k0,
                                                         int tzs) {
-  const int no = (job.P + 7) >> 3;  // 8-point groups per row = tiles along x
-  const int o = (int)blockIdx.x * 32 + (int)(threadIdx.x & 31u);
-  const int y = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
-  if (o >= no || y >= job.P) return;
-  const int k = k0 + (int)blockIdx.z;
-  const unsigned long long t = ((unsigned long long)(blockIdx.z / (unsigned)tzs) * no + (y >> 3)) * no + o;
-  const unsigned flag = __ldg(tiles + t * tile_words + (tile_words - 1));
-  if (!(flag & 1u)) return;  // S2_TILE_DECIDED; its points are evaluated
-  const int slot = k % job.ring;
-  const int x0 = o * 8, n = min(8, job.P - x0);
   const int WP = (job.P + 31) >> 5;
-  const long long byte = (((long long)slot * job.P + y) * WP) * 4 + o;
-  reinterpret_cast<unsigned char *>(pb.pos)[byte] = (flag & 2u) ? (unsigned char)((1u << n) - 1u) : 0u;  // S2_TILE_POSITIVE
-  reinterpret_cast<unsigned char *>(pb.near)[byte] = 0u;
-  reinterpret_cast<unsigned char *>(pb.unk)[byte] = (unsigned char)((1u << n) - 1u);
+  const int q = (int)(blockIdx.x * 256u + threadIdx.x);  // word (y, w) of the plane
+  if (q >= job.P * WP) return;
+  const int y = q / WP, w = q - y * WP;
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const unsigned long long trow = ((unsigned long long)(blockIdx.y / (unsigned)tzs) * ntx + y / S2_PT_XY) * ntx;
+  unsigned pos = 0u, unk = 0u;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const int tx = 4 * w + b;
+    if (tx >= ntx) break;
+    const unsigned flag = __ldg(tiles + (trow + tx) * tile_words + (tile_words - 1));
+    if (!(flag & 1u)) continue;  // S2_TILE_DECIDED
+    const unsigned bits = (1u << min(8, job.P - 8 * tx)) - 1u;
+    unk |= bits << (8 * b);
+    if (flag & 2u) pos |= bits << (8 * b);  // S2_TILE_POSITIVE
+  }
+  const long long o = ((long long)((k0 + (int)blockIdx.y) % job.ring) * job.P + y) * WP + w;
+  pb.pos[o] = pos;
+  pb.near[o] = 0u;
+  pb.unk[o] = unk;
 }
 
 // Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.
