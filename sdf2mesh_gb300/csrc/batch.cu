@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
         case S2_ST_VERT: s2b_stage_vertices(J); break;
         case S2_ST_VCOMPACT: s2_vcompact_worker(J.job, J.cand, J.mesh, 1, item == 0); break;
         case S2_ST_ROWS: s2_rowscan_worker(J.mesh, (unsigned long long)J.job.N * J.job.N); break;
-        case S2_ST_QUADS: s2_quads_worker(J.job, J.mesh, J.scan_tiles, item == 0); break;
+        case S2_ST_QUADS: s2_quads_worker<false>(J.job, J.mesh, J.scan_tiles, item == 0); break;
       }
     }
     __syncthreads();

@@ -464,7 +464,7 @@ size_t prune_layout(s2m_mesh *m) {
   m->prune_base_off = up16(16 + 4 * size_t(ns));
   m->prune_cbase_off = up16(m->prune_base_off + 8 * (size_t(ns) + 1));
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
-  m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * words * 4);
+  m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * (words + 1) * 4);  // + each box's flag word
   m->prune_list_off = up16(m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4);  // + each tile's flag word
   return m->prune_list_off + size_t(chunk_tiles) * 4;
 }

@@ -148,13 +148,18 @@ __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long
 // The tile pass of slabs s_begin .. s_end - 1, in two launches of one thread
 // per box, each covering many slabs so that the grid fills the GPU:
 //   s2m_tiles_coarse  boxes of 4 x 4 tiles (32 x 32 points by the tile depth):
-//                     the full interval evaluation -> sbits
+//                     the full interval evaluation -> sbits and the box's
+//                     flag word
 //   s2m_tiles         each tile inside its coarse box: only the segments
 //                     active in the box are evaluated -> bits, and the SDF
 //                     operations that remain (ops[0] FP32, ops[1] SFU, per
-//                     lattice point)
-// Coarse box c of the job is at sbits[(c - cbase[s_begin]) * W], tile g at
-// bits[(g - tbase[s_begin]) * W]; cbase / tbase hold each slab's first index.
+//                     lattice point).  A tile of a decided box is decided
+//                     with it (the box's interval bounds every point of the
+//                     tile's box) and takes the box's bits, without an
+//                     evaluation of its own.
+// Coarse box c of the job is at sbits[(c - cbase[s_begin]) * S2M_TILE_WORDS],
+// tile g at bits[(g - tbase[s_begin]) * S2M_TILE_WORDS]; cbase / tbase hold
+// each slab's first index.
 // Coordinate range of a tile's box along one axis: lattice indices a .. b,
 // widened by a margin.  The boxes reach one lattice point past the tile's
 // points in +x, +y and -z, and the margin (more than the normal epsilon plus
@@ -184,6 +189,14 @@ __device__ __forceinline__ int s2_find_slab(const unsigned long long *base, int 
   return lo;
 }
 
+// S2_TILE_DECIDED (| S2_TILE_POSITIVE) when a box's root interval lies at or
+// beyond +-guard; 0 otherwise, and for an unknown (NaN) interval.
+__device__ __forceinline__ unsigned s2_root_flag(const S2Job &job, s2i root) {
+  if (root.lo >= job.guard) return S2_TILE_DECIDED | S2_TILE_POSITIVE;
+  if (root.hi <= -job.guard) return S2_TILE_DECIDED;
+  return 0u;
+}
+
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long long *__restrict__ cbase, int s_begin,
                  int s_end, int D, int nzc) {
@@ -210,9 +223,10 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   float fp, sfu;
   s2i root;
   s2m_user_sdf_tile(X, Y, Z, m, &fp, &sfu, &root);
-  unsigned *dst = sbits + (c - b0) * S2M_PRUNE_WORDS;
+  unsigned *dst = sbits + (c - b0) * S2M_TILE_WORDS;
 #pragma unroll
   for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
+  dst[S2M_PRUNE_WORDS] = s2_root_flag(job, root);
 }
 
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
@@ -237,16 +251,20 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
     const int tz = (int)(q / ntx);
     const unsigned long long c =
         cbase[s] + ((unsigned long long)tz * ncx + ty / S2_PT_COARSE) * ncx + tx / S2_PT_COARSE;
-    const unsigned *pm = sbits + (c - cbase[s_begin]) * S2M_PRUNE_WORDS;
-    const s2i X = s2_prune_box(job, tl.i0, tl.i1 + 1), Y = s2_prune_box(job, tl.j0, tl.j1 + 1),
-              Z = s2_prune_box(job, tl.kb - 1, max(tl.kb, tl.ke));
+    const unsigned *pm = sbits + (c - cbase[s_begin]) * S2M_TILE_WORDS;
     unsigned m[S2M_PRUNE_WORDS];
     float fp = 0.0f, sfu = 0.0f;
-    s2i root;
-    s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu, &root);
-    unsigned flag = 0u;
-    if (root.lo >= job.guard) flag = S2_TILE_DECIDED | S2_TILE_POSITIVE;  // false for an unknown (NaN) interval
-    else if (root.hi <= -job.guard) flag = S2_TILE_DECIDED;
+    unsigned flag = pm[S2M_PRUNE_WORDS];
+    if (flag) {
+#pragma unroll
+      for (int w = 0; w < S2M_PRUNE_WORDS; ++w) m[w] = pm[w];
+    } else {
+      const s2i X = s2_prune_box(job, tl.i0, tl.i1 + 1), Y = s2_prune_box(job, tl.j0, tl.j1 + 1),
+                Z = s2_prune_box(job, tl.kb - 1, max(tl.kb, tl.ke));
+      s2i root;
+      s2m_user_sdf_tile_in(X, Y, Z, pm, m, &fp, &sfu, &root);
+      flag = s2_root_flag(job, root);
+    }
     if (flag) fp = sfu = 0.0f;  // nothing of the SDF is evaluated there
     unsigned *dst = bits + (g - b0) * S2M_TILE_WORDS;
 #pragma unroll

@@ -145,16 +145,26 @@ __device__ __forceinline__ void s2_rowscan_worker(const S2MeshDev &mesh, unsigne
 
 
 
+// Loads of the vertex keys and row starts: NC (a kernel launched after the
+// ones that wrote them) through the read-only cache, where neighbouring
+// vertices' searches of the same rows hit; else from L2 (the persistent
+// batch kernel, where they were written earlier in the same launch).
+template <bool NC, class T>
+__device__ __forceinline__ T s2_ldq(const T *p) {
+  return NC ? __ldg(p) : s2_ldcg(p);
+}
+
 // Index of the vertex of cell (x, y, z label) or S2_NO_VERTEX: the row of
 // (z, y) is a contiguous run of the vertex list sorted by x, as the sorted
 // VertexList the reference binary-searches (mesh.rs:326-331).
+template <bool NC>
 __device__ __forceinline__ unsigned s2_find(const S2MeshDev &m, int N, int x, int y, int z) {
   unsigned long long r = (unsigned long long)z * N + y;
-  unsigned lo = s2_ldcg(m.rowstart + r), hi = s2_ldcg(m.rowstart + r + 1);
+  unsigned lo = s2_ldq<NC>(m.rowstart + r), hi = s2_ldq<NC>(m.rowstart + r + 1);
   if (hi > m.vcap) hi = (unsigned)m.vcap;
   while (lo < hi) {
     unsigned mid = (lo + hi) >> 1;
-    int kx = (int)(s2_ldcg(m.key + mid) & 0xffffull);
+    int kx = (int)(s2_ldq<NC>(m.key + mid) & 0xffffull);
     if (kx < x) lo = mid + 1;
     else if (kx > x) hi = mid;
     else return mid;
@@ -171,6 +181,7 @@ struct S2Quads {
   unsigned invalid;  // quads dropped
 };
 
+template <bool NC>
 __device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, unsigned v, unsigned long long key) {
   S2Quads r;
   r.valid = 0;
@@ -185,14 +196,15 @@ __device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, un
     else r.invalid++;
   };
   if (b0 != b3 && y > 0 && z > 0)
-    put(0, s2_find(m, N, x, y - 1, z - 1), s2_find(m, N, x, y, z - 1), v, s2_find(m, N, x, y - 1, z), b0);
+    put(0, s2_find<NC>(m, N, x, y - 1, z - 1), s2_find<NC>(m, N, x, y, z - 1), v, s2_find<NC>(m, N, x, y - 1, z), b0);
   if (b1 != b3 && x > 0 && z > 0)
-    put(1, s2_find(m, N, x - 1, y, z - 1), s2_find(m, N, x, y, z - 1), v, s2_find(m, N, x - 1, y, z), !b1);
+    put(1, s2_find<NC>(m, N, x - 1, y, z - 1), s2_find<NC>(m, N, x, y, z - 1), v, s2_find<NC>(m, N, x - 1, y, z), !b1);
   if (b2 != b3 && x > 0 && y > 0)
-    put(2, s2_find(m, N, x - 1, y - 1, z), s2_find(m, N, x, y - 1, z), v, s2_find(m, N, x - 1, y, z), b2);
+    put(2, s2_find<NC>(m, N, x - 1, y - 1, z), s2_find<NC>(m, N, x, y - 1, z), v, s2_find<NC>(m, N, x - 1, y, z), b2);
   return r;
 }
 
+template <bool NC>
 __device__ __forceinline__ void s2_quads_worker(const S2Job &job, const S2MeshDev &mesh, unsigned scan_tiles,
                                                 bool leader) {
   __shared__ unsigned s_tile;
@@ -223,7 +235,7 @@ __device__ __forceinline__ void s2_quads_worker(const S2Job &job, const S2MeshDe
       qd[m].valid = 0;
       ntri[m] = 0;
       if (v < V) {
-        qd[m] = s2_vertex_quads(mesh, job.N, (unsigned)v, s2_ldcg(mesh.key + v));
+        qd[m] = s2_vertex_quads<NC>(mesh, job.N, (unsigned)v, s2_ldq<NC>(mesh.key + v));
         ntri[m] = 2u * __popc(qd[m].valid);
         invalid += qd[m].invalid;
       }

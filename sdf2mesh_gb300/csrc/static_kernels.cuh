@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(S2_SCAN_BLOCK) s2m_rowscan(S2MeshDev mesh, uns
 }
 
 __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads(S2Job job, S2MeshDev mesh, unsigned scan_tiles) {
-  s2_quads_worker(job, mesh, scan_tiles, blockIdx.x == 0);
+  s2_quads_worker<true>(job, mesh, scan_tiles, blockIdx.x == 0);
 }
 
 // FP32 issue-rate probe: 8 independent dependent chains per thread of
