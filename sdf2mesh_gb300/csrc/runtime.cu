@@ -527,10 +527,13 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
 
 // Classification buffers: words of 32 cells per slab (tiles of S2_CW_BLOCK
 // words), and the point bits of a slab's D + 1 planes.
-size_t cell_word_tiles(const s2m_mesh *m) {
+// Classification tiles: S2_CW_BLOCK words of 32 cells of one cell plane, nbp
+// per plane, D planes per slab.
+unsigned cell_tiles_per_plane(const s2m_mesh *m) {
   const size_t WN = size_t((m->N + 31) / 32);
-  return (size_t(m->D) * size_t(m->N) * WN + S2_CW_BLOCK - 1) / S2_CW_BLOCK;
+  return unsigned((size_t(m->N) * WN + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
 }
+size_t cell_word_tiles(const s2m_mesh *m) { return size_t(m->D) * cell_tiles_per_plane(m); }
 
 void drop_graph(s2m_mesh *m) {
   if (m->graph) cudaGraphExecDestroy(m->graph);
@@ -738,14 +741,15 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     if (!pruned)  // the pruned evaluation writes the point bits of its planes itself
       S2_LAUNCH(1, 0, (s2m_cells_bits<<<dim3(unsigned((j.P + 7) / 8), unsigned(nk)), 256, 0, st>>>(j, m->ring, pb, k0),
                        cudaGetLastError()));
-    const unsigned long long nwords = (unsigned long long)(zc1 - zc0) * N * ((N + 31) / 32);
-    const unsigned cg = unsigned((nwords + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
-    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<cg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
+    const unsigned nbp = cell_tiles_per_plane(m);
+    const unsigned ncp = unsigned(zc1 - zc0);
+    const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
+    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<mg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
                                                                     m->tile_cnt + m->cell_tiles, m->slab_ctrl,
                                                                     m->cand_base, s, zc0, zc1),
                           cudaGetLastError()));
-    S2_LAUNCH(1, 0, (s2m_cells_emit<<<cg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
-                                                               m->cell_words, m->slab_ctrl, cand, c.err, zc0, zc1),
+    S2_LAUNCH(1, 0, (s2m_cells_emit<<<eg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
+                                                               m->cell_words, m->slab_ctrl, cand, c.err, zc0),
                      cudaGetLastError()));
   }
   S2Job jj = j;

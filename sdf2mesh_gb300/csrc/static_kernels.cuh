@@ -23,9 +23,10 @@
 // cell with such a corner when S2M_JOB_EXACT_CORNERS).
 
 // tile_off[t] = cand.base[slab] + (candidates of tiles < t); cand.base[slab + 1]
-// = the slab's running total.  Run by one block of NT threads, any tile
-// count; the counts are read from L2 (other blocks wrote them).
-template <int NT>
+// = the slab's running total.  Run by one block of NT threads, CPT
+// consecutive counts per thread and step, any tile count; the counts are
+// read from L2 (other blocks wrote them).
+template <int NT, int CPT>
 __device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned ntiles,
                                               unsigned long long *__restrict__ tile_off, unsigned long long *base,
                                               int slab_index) {
@@ -35,10 +36,16 @@ __device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned
   if (tid == 0) s_carry = __ldcg(base + slab_index);
   if (tid < 32) s_warp[tid] = 0ull;
   __syncthreads();
-  for (unsigned t0 = 0; t0 < ntiles; t0 += NT) {
-    const unsigned t = t0 + tid;
-    const unsigned long long v = t < ntiles ? __ldcg(tile_cnt + t) : 0ull;
-    unsigned long long inc = v;
+  for (unsigned t0 = 0; t0 < ntiles; t0 += NT * CPT) {
+    const unsigned tb = t0 + tid * CPT;
+    unsigned v[CPT];
+    unsigned long long sum = 0ull;
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      v[q] = tb + q < ntiles ? __ldcg(tile_cnt + tb + q) : 0u;
+      sum += v[q];
+    }
+    unsigned long long inc = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const unsigned long long x = __shfl_up_sync(S2_FULL, inc, o);
@@ -58,9 +65,14 @@ __device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned
     }
     __syncthreads();
     const unsigned long long carry = s_carry;
-    if (t < ntiles) tile_off[t] = carry + s_warp[warp] + inc - v;
+    unsigned long long run = carry + s_warp[warp] + inc - sum;
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      if (tb + q < ntiles) tile_off[tb + q] = run;
+      run += v[q];
+    }
     __syncthreads();
-    if (tid == NT - 1) s_carry = carry + s_warp[NT / 32 - 1] + inc;  // last thread's inclusive total
+    if (tid == NT - 1) s_carry = run;  // the last thread's running total
     __syncthreads();
   }
   if (tid == 0) base[slab_index + 1] = s_carry;
@@ -133,121 +145,121 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
   pb.unk[o] = unk;
 }
 
-// Word l of cells (z = zc0 + dz, y, x = 32 w ..): l = (dz * N + y) * WN + w.
-// Its coordinates from the block's first word (one 64-bit division per
-// block; 32-bit ones per thread).
-struct S2CellWord {
-  int w, y, dz;
-};
-__device__ __forceinline__ S2CellWord s2_cell_word(const S2Job &job, int WN) {
-  __shared__ unsigned long long s_row0;
-  __shared__ int s_w0;
-  const unsigned long long l0 = (unsigned long long)blockIdx.x * S2_CW_BLOCK;
-  if (threadIdx.x == 0) {
-    s_row0 = l0 / (unsigned long long)WN;
-    s_w0 = (int)(l0 - s_row0 * (unsigned long long)WN);
-  }
-  __syncthreads();
-  const unsigned q = (unsigned)s_w0 + threadIdx.x;  // < WN + S2_CW_BLOCK
-  const unsigned row = (unsigned)s_row0 + q / (unsigned)WN;  // < slab depth * N < 2^32
-  S2CellWord c;
-  c.w = (int)(q % (unsigned)WN);
-  c.y = (int)(row % (unsigned)job.N);
-  c.dz = (int)(row / (unsigned)job.N);
-  return c;
-}
-
-// The last block to finish (a fence, then an atomic count of finished blocks)
-// also scans the tile counts into the slab's candidate offsets (tile_off,
-// base[slab + 1]), so no separate launch is needed; `done` returns to 0.
+// Cell words and tiles of a slab: word yw = y * WN + w of cell plane dz
+// holds the cells (x = 32 w .., y, z = zc0 + dz), at words[dz * N * WN + yw].
+// Tile t = dz * nbp + b (nbp = ceil(N * WN / S2_CW_BLOCK) tiles per plane)
+// holds the plane's words b * S2_CW_BLOCK ..; tile order is (z, y, x) order.
+//
+// s2m_cells_mark: grid (nbp, ceil(planes / S2_MARK_PLANES)); a thread takes
+// one word position over S2_MARK_PLANES cell planes, so each point row it
+// reads serves the planes above and below it.  The last block to finish (a
+// fence, then an atomic count of finished blocks) also scans the tile counts
+// into the slab's candidate offsets (tile_off, base[slab + 1]), so no
+// separate launch is needed; `done` returns to 0.
+#define S2_MARK_PLANES 4
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2PointBits pb,
                                                             const unsigned *__restrict__ offx,
                                                             unsigned *__restrict__ words, unsigned *tile_cnt,
                                                             unsigned *done, unsigned long long *__restrict__ tile_off,
                                                             unsigned long long *base, int slab_index, int zc0,
                                                             int zc1) {
-  __shared__ unsigned s_warp[S2_CW_BLOCK / 32];
-  const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5;
-  const long long nw = (long long)(zc1 - zc0) * job.N * WN;
-  const long long l = (long long)blockIdx.x * S2_CW_BLOCK + threadIdx.x;
-  const S2CellWord cw = s2_cell_word(job, WN);
-  unsigned cand = 0;
-  if (l < nw) {
-    const int w = cw.w, y = cw.y, dz = cw.dz;
-    // corner k = bx | by << 1 | bz << 2 lies in point row q = by | bz << 1
-    // (k = 2 q + bx); bx = 1 takes the row's bits shifted by one point
-    unsigned pbit[8], nbit[8];
+  __shared__ unsigned s_cnt[S2_MARK_PLANES][S2_CW_BLOCK / 32];
+  const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5, NW = job.N * WN;
+  const int yw = (int)(blockIdx.x * S2_CW_BLOCK + threadIdx.x);
+  const int dz0 = (int)blockIdx.y * S2_MARK_PLANES;
+  const int ncp = min(S2_MARK_PLANES, zc1 - zc0 - dz0);  // cell planes of this block, >= 1
+  unsigned cand[S2_MARK_PLANES];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int slot = (zc0 + dz + (q >> 1)) % job.ring;
-      const long long base = ((long long)slot * job.P + (y + (q & 1))) * WP + w;
-      const bool more = w + 1 < WP;
-      const unsigned plo = __ldg(pb.pos + base), phi = more ? __ldg(pb.pos + base + 1) : 0u;
-      const unsigned nlo = __ldg(pb.near + base), nhi = more ? __ldg(pb.near + base + 1) : 0u;
-      pbit[2 * q] = plo;
-      pbit[2 * q + 1] = __funnelshift_r(plo, phi, 1);
-      nbit[2 * q] = nlo;
-      nbit[2 * q + 1] = __funnelshift_r(nlo, nhi, 1);
-    }
-    unsigned all = ~0u, any = 0u;
+  for (int i = 0; i < S2_MARK_PLANES; ++i) cand[i] = 0u;
+  if (yw < NW) {
+    const int y = yw / WN, w = yw - y * WN;
+    const bool more = w + 1 < WP;
+    const bool nearrule = !job.qef && !job.exact;
+    const unsigned ox = job.qef ? 0u : offx[w];
+    const unsigned oy = (!job.qef && s2_off_lattice(job, y + 1)) ? ~0u : 0u;
+    // per point plane p: AND and OR of its 4 corner words, and (reference
+    // rule) the near-zero corners that count when the plane is a cell's
+    // bottom (tb: corners k = 1, 2, 3) or top (tt: k = 4 .. 7).  Corner k =
+    // bx | by << 1 | bz << 2; bx = 1 takes the row's bits shifted by one.
+    unsigned andp[S2_MARK_PLANES + 1], orp[S2_MARK_PLANES + 1], tb[S2_MARK_PLANES + 1], tt[S2_MARK_PLANES + 1];
+    int slot = (zc0 + dz0) % job.ring;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      all &= pbit[k];
-      any |= pbit[k];
-    }
-    cand = any & ~all;
-    if (!job.qef) {
-      const unsigned ox = offx[w];
-      const unsigned oy = s2_off_lattice(job, y + 1) ? ~0u : 0u;
-      const unsigned oz = s2_off_lattice(job, zc0 + dz + 1) ? ~0u : 0u;
-      if (job.exact) {
-        cand |= ox | oy | oz;
-      } else {
-#pragma unroll
-        for (int k = 1; k < 8; ++k)
-          cand |= nbit[k] & (((k & 1) ? ox : 0u) | ((k & 2) ? oy : 0u) | ((k & 4) ? oz : 0u));
+    for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+      andp[p] = ~0u;
+      orp[p] = 0u;
+      tb[p] = tt[p] = 0u;
+      if (p > ncp) continue;
+      const long long r0 = ((long long)slot * job.P + y) * WP + w, r1 = r0 + WP;
+      const unsigned p0 = __ldg(pb.pos + r0), p1 = __ldg(pb.pos + r1);
+      const unsigned p0s = __funnelshift_r(p0, more ? __ldg(pb.pos + r0 + 1) : 0u, 1);
+      const unsigned p1s = __funnelshift_r(p1, more ? __ldg(pb.pos + r1 + 1) : 0u, 1);
+      andp[p] = p0 & p0s & p1 & p1s;
+      orp[p] = p0 | p0s | p1 | p1s;
+      if (nearrule) {
+        const unsigned n0 = __ldg(pb.near + r0), n1 = __ldg(pb.near + r1);
+        const unsigned n0s = __funnelshift_r(n0, more ? __ldg(pb.near + r0 + 1) : 0u, 1);
+        const unsigned n1s = __funnelshift_r(n1, more ? __ldg(pb.near + r1 + 1) : 0u, 1);
+        const unsigned oz = s2_off_lattice(job, zc0 + dz0 + p) ? ~0u : 0u;
+        tb[p] = (n0s & ox) | (n1 & oy) | (n1s & (ox | oy));
+        tt[p] = (n0 & oz) | (n0s & (ox | oz)) | (n1 & (oy | oz)) | (n1s & (ox | oy | oz));
       }
+      if (++slot == job.ring) slot = 0;
     }
-    if (w == WN - 1 && (job.N & 31)) cand &= (1u << (job.N & 31)) - 1u;
-    words[l] = cand;
-  }
-  unsigned cnt = __popc(cand);
+    const unsigned edge = (w == WN - 1 && (job.N & 31)) ? (1u << (job.N & 31)) - 1u : ~0u;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(S2_FULL, cnt, o);
-  if ((threadIdx.x & 31u) == 0) s_warp[threadIdx.x >> 5] = cnt;
+    for (int i = 0; i < S2_MARK_PLANES; ++i) {
+      if (i >= ncp) break;
+      unsigned c = (orp[i] | orp[i + 1]) & ~(andp[i] & andp[i + 1]);
+      if (nearrule) c |= tb[i] | tt[i + 1];
+      else if (!job.qef) c |= ox | oy | (s2_off_lattice(job, zc0 + dz0 + i + 1) ? ~0u : 0u);
+      c &= edge;
+      words[(long long)(dz0 + i) * NW + yw] = c;
+      cand[i] = c;
+    }
+  }
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < S2_MARK_PLANES; ++i) {
+    unsigned cnt = __popc(cand[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(S2_FULL, cnt, o);
+    if (lane == 0) s_cnt[i][warp] = cnt;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < ncp) {
+    unsigned t = 0;
+    for (int k = 0; k < S2_CW_BLOCK / 32; ++k) t += s_cnt[threadIdx.x][k];
+    tile_cnt[(unsigned long long)(dz0 + (int)threadIdx.x) * gridDim.x + blockIdx.x] = t;
+    __threadfence();
+  }
   __syncthreads();
   __shared__ bool s_last;
-  if (threadIdx.x == 0) {
-    unsigned t = 0;
-    for (int i = 0; i < S2_CW_BLOCK / 32; ++i) t += s_warp[i];
-    tile_cnt[blockIdx.x] = t;
-    __threadfence();
-    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
-  }
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x * gridDim.y - 1;
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  s2_scan_tiles<S2_CW_BLOCK>(tile_cnt, gridDim.x, tile_off, base, slab_index);
+  s2_scan_tiles<S2_CW_BLOCK, 16>(tile_cnt, (unsigned)(zc1 - zc0) * gridDim.x, tile_off, base, slab_index);
   if (threadIdx.x == 0) *done = 0u;
 }
 
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
 // 8 lattice corner values (NaN where the point's unknown-value bit is set: a
-// decided tile of the pruned evaluation wrote no value there).  A warp takes its words with candidates one at a
-// time, lane l writing the cell of bit l: the corner loads of a word's cells
-// are then coalesced rows, and every lane works.
+// decided tile of the pruned evaluation wrote no value there).  Grid (nbp,
+// cell planes), block = tile.  A warp takes its words with candidates one at
+// a time, lane l writing the cell of bit l: the corner loads of a word's
+// cells are then coalesced rows, and every lane works.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
                                                             const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
-                                                            S2Cand cand, unsigned *err, int zc0, int zc1) {
+                                                            S2Cand cand, unsigned *err, int zc0) {
   __shared__ unsigned s_warp[32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const int WN = (job.N + 31) >> 5;
-  const long long nw = (long long)(zc1 - zc0) * job.N * WN;
-  const long long l = (long long)blockIdx.x * S2_CW_BLOCK + tid;
-  const S2CellWord cw = s2_cell_word(job, WN);
-  const unsigned mask = l < nw ? words[l] : 0u;
+  const int WN = (job.N + 31) >> 5, NW = job.N * WN;
+  const int yw = (int)(blockIdx.x * S2_CW_BLOCK + tid);
+  const int dz = (int)blockIdx.y;
+  const unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
+  const int wy = yw / WN, wx = yw - wy * WN;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
 #pragma unroll
@@ -260,7 +272,8 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
   __syncthreads();
   if (warp == 0) s2_warp_exclusive32(s_warp);
   __syncthreads();
-  const unsigned long long first = tile_off[blockIdx.x] + s_warp[warp] + (inc - cnt);
+  const unsigned long long first =
+      tile_off[(unsigned long long)dz * gridDim.x + blockIdx.x] + s_warp[warp] + (inc - cnt);
   unsigned todo = __ballot_sync(S2_FULL, mask != 0u);
   while (todo) {
     const int src = __ffs(todo) - 1;
@@ -268,9 +281,9 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     const unsigned m = __shfl_sync(S2_FULL, mask, src);
     const unsigned long long o = __shfl_sync(S2_FULL, first, src) + __popc(m & ((1u << lane) - 1u));
     S2Cell cell;
-    cell.x = 32 * __shfl_sync(S2_FULL, cw.w, src) + (int)lane;
-    cell.y = __shfl_sync(S2_FULL, cw.y, src);
-    cell.z = zc0 + __shfl_sync(S2_FULL, cw.dz, src);
+    cell.x = 32 * __shfl_sync(S2_FULL, wx, src) + (int)lane;
+    cell.y = __shfl_sync(S2_FULL, wy, src);
+    cell.z = zc0 + dz;
     if (!((m >> lane) & 1u)) continue;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
@@ -365,7 +378,7 @@ __global__ void __launch_bounds__(256) s2m_vtile_scan(unsigned *tcnt, unsigned l
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  s2_scan_tiles<256>(part_cnt, gridDim.x, part_off, part_base, 0);
+  s2_scan_tiles<256, 4>(part_cnt, gridDim.x, part_off, part_base, 0);
   if (tid == 0) *done = 0u;
 }
 
