@@ -245,21 +245,22 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
 // 8 lattice corner values (NaN where the point's unknown-value bit is set: a
 // decided tile of the pruned evaluation wrote no value there).  Grid (nbp,
-// cell planes), block = tile.  A warp takes its words with candidates one at
-// a time, lane l writing the cell of bit l: the corner loads of a word's
-// cells are then coalesced rows, and every lane works.
+// cell planes), block = tile.  Each warp first lists the candidates of its 32
+// words in shared memory (word lane << 5 | bit, in (y, x) order), then writes
+// them 32 at a time, one per lane: most words hold one or two candidates, so
+// this keeps every lane busy.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
                                                             const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
                                                             S2Cand cand, unsigned *err, int zc0) {
   __shared__ unsigned s_warp[32];
+  __shared__ unsigned short s_list[S2_CW_BLOCK / 32][32 * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const int WN = (job.N + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + tid);
   const int dz = (int)blockIdx.y;
   const unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
-  const int wy = yw / WN, wx = yw - wy * WN;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
 #pragma unroll
@@ -267,24 +268,33 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
     if ((int)lane >= o) inc += t;
   }
+  const unsigned total = __shfl_sync(S2_FULL, inc, 31);
+  {
+    unsigned r = inc - cnt, rem = mask;
+    while (rem) {
+      const unsigned bit = __ffs(rem) - 1u;
+      rem &= rem - 1u;
+      s_list[warp][r++] = (unsigned short)((lane << 5) | bit);
+    }
+  }
   if (lane == 31) s_warp[warp] = inc;
   if (tid < 32 && tid >= S2_CW_BLOCK / 32) s_warp[tid] = 0u;
   __syncthreads();
   if (warp == 0) s2_warp_exclusive32(s_warp);
   __syncthreads();
-  const unsigned long long first =
-      tile_off[(unsigned long long)dz * gridDim.x + blockIdx.x] + s_warp[warp] + (inc - cnt);
-  unsigned todo = __ballot_sync(S2_FULL, mask != 0u);
-  while (todo) {
-    const int src = __ffs(todo) - 1;
-    todo &= todo - 1u;
-    const unsigned m = __shfl_sync(S2_FULL, mask, src);
-    const unsigned long long o = __shfl_sync(S2_FULL, first, src) + __popc(m & ((1u << lane) - 1u));
+  const unsigned long long first = tile_off[(unsigned long long)dz * gridDim.x + blockIdx.x] + s_warp[warp];
+  const int WP = (job.P + 31) >> 5;
+#pragma unroll 1
+  for (unsigned r = lane; r < total; r += 32u) {
+    const unsigned e = s_list[warp][r];
+    const int ywc = (int)(blockIdx.x * S2_CW_BLOCK + (warp << 5) + (e >> 5));
+    const int wy = ywc / WN, w = ywc - wy * WN;
+    const unsigned bit = e & 31u;
     S2Cell cell;
-    cell.x = 32 * __shfl_sync(S2_FULL, wx, src) + (int)lane;
-    cell.y = __shfl_sync(S2_FULL, wy, src);
+    cell.x = 32 * w + (int)bit;
+    cell.y = wy;
     cell.z = zc0 + dz;
-    if (!((m >> lane) & 1u)) continue;
+    const unsigned long long o = first + r;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
       continue;
@@ -292,14 +302,13 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     float v[8];
     s2_load_corners<false>(job, ring, cell, v);
     if (unk) {  // corners of decided tiles: no value in the ring
-      const int WP = (job.P + 31) >> 5, w = cell.x >> 5;
       const bool more = w + 1 < WP;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
         const long long base = ((long long)((cell.z + (q >> 1)) % job.ring) * job.P + (cell.y + (q & 1))) * WP + w;
         const unsigned lo = __ldg(unk + base), hi = more ? __ldg(unk + base + 1) : 0u;
-        if ((lo >> lane) & 1u) v[2 * q] = __int_as_float(0x7fc00000);
-        if ((__funnelshift_r(lo, hi, 1) >> lane) & 1u) v[2 * q + 1] = __int_as_float(0x7fc00000);
+        if ((lo >> bit) & 1u) v[2 * q] = __int_as_float(0x7fc00000);
+        if ((__funnelshift_r(lo, hi, 1) >> bit) & 1u) v[2 * q + 1] = __int_as_float(0x7fc00000);
       }
     }
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
