@@ -152,7 +152,7 @@ struct s2m_mesh {
   float *cand_val = nullptr, *cand_pos = nullptr, *cand_nrm = nullptr;
   unsigned long long cand_cap = 0;
   unsigned long long *cand_base = nullptr;    // nslabs + 1
-  unsigned long long *cand_status = nullptr;  // vc_tiles
+  unsigned long long *cand_status = nullptr;  // vc_ctrl_words(vc_tiles): s2m_vc_scan's base pair, counts, offsets
   // vertex work in tile order (s2m_vtile_*), with tile pruning when every
   // slab's tile bits stay resident: [part_base 2 u64 | tile counts (vt_tiles)
   // + done counter | block totals (vt_blocks) | block offsets (vt_blocks u64)
@@ -527,6 +527,12 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
 
 // Classification buffers: words of 32 cells per slab (tiles of S2_CW_BLOCK
 // words), and the point bits of a slab's D + 1 planes.
+// Vertex compaction control (u64 words): [base pair | per-tile vertex counts
+// (u32) | per-tile first vertex]; the first vc_ctrl_offsets words are zeroed
+// per job.
+size_t vc_ctrl_offsets(size_t vc_tiles) { return 2 + (vc_tiles + 1) / 2; }
+size_t vc_ctrl_words(size_t vc_tiles) { return vc_ctrl_offsets(vc_tiles) + vc_tiles; }
+
 // Classification tiles: S2_CW_BLOCK words of 32 cells of one cell plane, nbp
 // per plane, D planes per slab.
 unsigned cell_tiles_per_plane(const s2m_mesh *m) {
@@ -577,7 +583,7 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   S2_CUDA(cudaMallocAsync(&m->cand_pos, m->cand_cap * 12, st));
   S2_CUDA(cudaMallocAsync(&m->cand_nrm, m->cand_cap * 12, st));
   S2_CUDA(cudaMallocAsync(&m->cand_base, size_t(m->nslabs + 1) * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->cand_status, m->vc_tiles * 8, st));
+  S2_CUDA(cudaMallocAsync(&m->cand_status, vc_ctrl_words(m->vc_tiles) * 8, st));
   if (m->prune_buf && m->prune_chunk >= m->nslabs && m->cand_cap < (1ull << 32)) {
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
     m->vt_tiles = m->slab_tile_base[size_t(m->nslabs)] - m->slab_tile_base[0];
@@ -671,7 +677,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(m->jobctl, 0, 8 * 8, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->cand_base, 0, size_t(m->nslabs + 1) * 8, st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(m->cand_status, 0, m->vc_tiles * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->cand_status, 0, vc_ctrl_offsets(m->vc_tiles) * 8, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->rowcnt, 0, N * N * 4, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->scan_status, 0, (m->scan_tiles + m->quad_tiles) * 8, st)) != cudaSuccess) return e;
 
@@ -778,12 +784,16 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                      cudaGetLastError()));
     perm = vperm;
   }
-  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm};
+  unsigned long long *vc_base = m->cand_status;
+  unsigned *vc_cnt = reinterpret_cast<unsigned *>(m->cand_status + 2);
+  unsigned long long *vc_off = m->cand_status + vc_ctrl_offsets(m->vc_tiles);
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt};
   const unsigned vx_grid = unsigned(sms) * 16;
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));
+  S2_LAUNCH(3, 0, (s2m_vc_scan<<<1, 256, 0, st>>>(cand, nslabs, vc_cnt, vc_off, vc_base, md), cudaGetLastError()));
   const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
-  S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs), cudaGetLastError()));
+  S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs, vc_off), cudaGetLastError()));
   const unsigned scan_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->scan_tiles, size_t(sms) * 8)));
   S2_LAUNCH(4, 0, (s2m_rowscan<<<scan_grid, S2_SCAN_BLOCK, 0, st>>>(md, N * N), cudaGetLastError()));
   const unsigned q_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->quad_tiles, size_t(sms) * 8)));
@@ -1365,11 +1375,12 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
     return S2M_E_INVALID;
   }
   // The rest holds the candidate list and its scan words: 64 bytes per
-  // candidate plus one scan word per S2_VC_TILE candidates and one quad
-  // scan word per S2_Q_TILE vertices (vertices never outnumber candidates).
+  // candidate plus 12 bytes of compaction counts and offsets per S2_VC_TILE
+  // candidates and one quad scan word per S2_Q_TILE vertices (vertices never
+  // outnumber candidates).
   size_t left = size_t(S2M_NOALLOC_SCRATCH_BYTES) - used;
-  const double per_cand = 64.0 + 8.0 / S2_VC_TILE + 8.0 / S2_Q_TILE;
-  unsigned long long cap = (unsigned long long)((double(left) - 8 * 256.0 - 8.0 * double(m.scan_tiles)) / per_cand);
+  const double per_cand = 64.0 + 12.0 / S2_VC_TILE + 8.0 / S2_Q_TILE;
+  unsigned long long cap = (unsigned long long)((double(left) - 9 * 256.0 - 8.0 * double(m.scan_tiles)) / per_cand);
   cap = cap / 1024 * 1024;
   m.cand_cap = cap;
   m.vc_tiles = (cap + S2_VC_TILE - 1) / S2_VC_TILE;
@@ -1378,7 +1389,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   m.quad_tiles = (m.vcap + S2_Q_TILE - 1) / S2_Q_TILE;
   ok = carve(base, used, size_t(cap), &m.cand_key) && carve(base, used, size_t(cap) * 8, &m.cand_val) &&
        carve(base, used, size_t(cap) * 3, &m.cand_pos) && carve(base, used, size_t(cap) * 3, &m.cand_nrm) &&
-       carve(base, used, size_t(m.vc_tiles), &m.cand_status) &&
+       carve(base, used, vc_ctrl_words(m.vc_tiles), &m.cand_status) &&
        carve(base, used, size_t(m.scan_tiles + m.quad_tiles), &m.scan_status);
   if (!ok || cap == 0) {
     set_err(err, errlen, "no-allocation scratch layout failed");

@@ -488,10 +488,11 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // tbits (tile pruning, every slab's bits resident), the SDF evaluations use
 // the bits of each cell's tile, and `perm` (when given) lists the candidates
 // grouped by tile (s2m_vtile_*), so that a warp's evaluations take one path
-// through the pruned SDF.
+// through the pruned SDF.  vc_cnt[t] counts the vertices of candidates
+// t * S2_VC_TILE .. (t + 1) * S2_VC_TILE - 1 (for s2m_vc_scan).
 extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
-             int nzc, const unsigned *perm) {
+             int nzc, const unsigned *perm, unsigned *vc_cnt) {
   __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
@@ -541,6 +542,12 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
     if (S2UserSdfCall::kStdNormal) key = s2_vertex_warp(sdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
     else key = active ? s2_vertex(sdf, job, c, v, pos, nrm) : 0ull;
 #endif
+    {  // one atomic per group of lanes whose candidates share a compaction tile
+      const bool has = active && (key >> 63) != 0ull;
+      const unsigned long long vt = has ? o / S2_VC_TILE : ~0ull;
+      const unsigned peers = __match_any_sync(0xffffffffu, vt);
+      if (has && (unsigned)(__ffs(peers) - 1) == (threadIdx.x & 31u)) atomicAdd(vc_cnt + vt, (unsigned)__popc(peers));
+    }
     if (!active) continue;
     cand.key[o] = key;
     if (key >> 63) {

@@ -154,27 +154,36 @@ __device__ __forceinline__ T s2_ldq(const T *p) {
   return NC ? __ldg(p) : s2_ldcg(p);
 }
 
-// Index of the vertex of cell (x, y, z label) or S2_NO_VERTEX: the row of
+// The vertices of cells (x - 1, y, z label) and (x, y, z label): the row of
 // (z, y) is a contiguous run of the vertex list sorted by x, as the sorted
-// VertexList the reference binary-searches (mesh.rs:326-331).
+// VertexList the reference binary-searches (mesh.rs:326-331); one
+// lower-bound search for x gives both.  S2_NO_VERTEX where there is none.
+struct S2RowHit {
+  unsigned xm1, x;
+};
 template <bool NC>
-__device__ __forceinline__ unsigned s2_find(const S2MeshDev &m, int N, int x, int y, int z) {
-  unsigned long long r = (unsigned long long)z * N + y;
-  unsigned lo = s2_ldq<NC>(m.rowstart + r), hi = s2_ldq<NC>(m.rowstart + r + 1);
-  if (hi > m.vcap) hi = (unsigned)m.vcap;
+__device__ __forceinline__ S2RowHit s2_row_find(const S2MeshDev &m, int N, int x, int y, int z) {
+  const unsigned long long r = (unsigned long long)z * N + y;
+  const unsigned start = s2_ldq<NC>(m.rowstart + r);
+  unsigned end = s2_ldq<NC>(m.rowstart + r + 1);
+  if (end > m.vcap) end = (unsigned)m.vcap;
+  unsigned lo = start, hi = end;
   while (lo < hi) {
-    unsigned mid = (lo + hi) >> 1;
-    int kx = (int)(s2_ldq<NC>(m.key + mid) & 0xffffull);
-    if (kx < x) lo = mid + 1;
-    else if (kx > x) hi = mid;
-    else return mid;
+    const unsigned mid = (lo + hi) >> 1;
+    if ((int)(s2_ldq<NC>(m.key + mid) & 0xffffull) < x) lo = mid + 1;
+    else hi = mid;
   }
-  return S2_NO_VERTEX;
+  S2RowHit h;
+  h.x = (lo < end && (int)(s2_ldq<NC>(m.key + lo) & 0xffffull) == x) ? lo : S2_NO_VERTEX;
+  h.xm1 = (lo > start && (int)(s2_ldq<NC>(m.key + lo - 1) & 0xffffull) == x - 1) ? lo - 1 : S2_NO_VERTEX;
+  return h;
 }
 
 // Quads of one vertex (mesh.rs:280-321): x, y and z edges in that order,
 // each a Quad(...).swap(flag) split into triangles (q2, q1, q0), (q0, q3, q2)
-// (lib.rs:531-546); a quad with a missing vertex is dropped (invalid).
+// (lib.rs:531-546); a quad with a missing vertex is dropped (invalid).  The
+// six neighbouring cells lie in three rows and the vertex's own row, where
+// cell (x - 1, y, z) can only be vertex v - 1.
 struct S2Quads {
   unsigned q[3][4];
   unsigned valid;    // bit per quad
@@ -189,18 +198,25 @@ __device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, un
   const int x = (int)(key & 0xffffull), y = (int)((key >> 16) & 0xffffull), z = (int)((key >> 32) & 0xffffull);
   const unsigned s = (unsigned)((key >> 48) & 0xfull);
   const bool b0 = s & 1u, b1 = s & 2u, b2 = s & 4u, b3 = s & 8u;
+  const bool want0 = b0 != b3 && y > 0 && z > 0, want1 = b1 != b3 && x > 0 && z > 0, want2 = b2 != b3 && x > 0 && y > 0;
   auto put = [&](int qi, unsigned a, unsigned b, unsigned c, unsigned d, bool swap) {
     if (swap) { unsigned t = a; a = d; d = t; t = b; b = c; c = t; }
     r.q[qi][0] = a; r.q[qi][1] = b; r.q[qi][2] = c; r.q[qi][3] = d;
     if (a != S2_NO_VERTEX && b != S2_NO_VERTEX && c != S2_NO_VERTEX && d != S2_NO_VERTEX) r.valid |= 1u << qi;
     else r.invalid++;
   };
-  if (b0 != b3 && y > 0 && z > 0)
-    put(0, s2_find<NC>(m, N, x, y - 1, z - 1), s2_find<NC>(m, N, x, y, z - 1), v, s2_find<NC>(m, N, x, y - 1, z), b0);
-  if (b1 != b3 && x > 0 && z > 0)
-    put(1, s2_find<NC>(m, N, x - 1, y, z - 1), s2_find<NC>(m, N, x, y, z - 1), v, s2_find<NC>(m, N, x - 1, y, z), !b1);
-  if (b2 != b3 && x > 0 && y > 0)
-    put(2, s2_find<NC>(m, N, x - 1, y - 1, z), s2_find<NC>(m, N, x, y - 1, z), v, s2_find<NC>(m, N, x - 1, y, z), b2);
+  const S2RowHit none = {S2_NO_VERTEX, S2_NO_VERTEX};
+  const S2RowHit ra = (want0 || want2) ? s2_row_find<NC>(m, N, x, y - 1, z) : none;      // (., y - 1, z)
+  const S2RowHit rb = (want0 || want1) ? s2_row_find<NC>(m, N, x, y, z - 1) : none;      // (., y, z - 1)
+  const S2RowHit rc = want0 ? s2_row_find<NC>(m, N, x, y - 1, z - 1) : none;             // (., y - 1, z - 1)
+  unsigned own = S2_NO_VERTEX;                                                           // (x - 1, y, z)
+  if ((want1 || want2) && v > 0) {
+    const unsigned long long kp = s2_ldq<NC>(m.key + v - 1);
+    if (((kp ^ key) & 0x0000ffffffff0000ull) == 0ull && (int)(kp & 0xffffull) == x - 1) own = v - 1;
+  }
+  if (want0) put(0, rc.x, rb.x, v, ra.x, b0);
+  if (want1) put(1, rb.xm1, rb.x, v, own, !b1);
+  if (want2) put(2, ra.xm1, ra.x, v, own, b2);
   return r;
 }
 

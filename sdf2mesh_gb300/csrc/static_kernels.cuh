@@ -403,8 +403,66 @@ __global__ void __launch_bounds__(256) s2m_vtile_scatter(S2Cand cand, int nslabs
   }
 }
 
-__global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand cand, S2MeshDev mesh, int nslabs) {
-  s2_vcompact_worker(job, cand, mesh, nslabs, blockIdx.x == 0);
+// Vertex compaction of the per-job pipeline in two wait-free passes.  The
+// vertex kernel counts each tile's vertices (tiles of S2_VC_TILE candidates,
+// vc_cnt); s2m_vc_scan (one block) turns the counts into each tile's first
+// vertex (vc_off) and the job's vertex total (vc_base[1], mesh.vtotal;
+// vc_base[0] = 0 on entry); s2m_vcompact then writes every tile's vertices
+// in order, as s2_vcompact_worker does with its look-back (which the
+// persistent batch kernel keeps).
+__global__ void __launch_bounds__(256) s2m_vc_scan(S2Cand cand, int nslabs, const unsigned *vc_cnt,
+                                                   unsigned long long *vc_off, unsigned long long *vc_base,
+                                                   S2MeshDev mesh) {
+  const unsigned long long ncand = min(cand.base[nslabs], cand.cap);
+  const unsigned ntiles = (unsigned)((ncand + S2_VC_TILE - 1) / S2_VC_TILE);
+  s2_scan_tiles<256, 16>(vc_cnt, ntiles, vc_off, vc_base, 0);
+  if (threadIdx.x == 0) *mesh.vtotal = vc_base[1];  // written by this thread in the scan
+}
+
+__global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand cand, S2MeshDev mesh, int nslabs,
+                                                          const unsigned long long *__restrict__ vc_off) {
+  __shared__ unsigned s_warp[32];
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const unsigned long long ncand = min(cand.base[nslabs], cand.cap);
+  const unsigned ntiles = (unsigned)((ncand + S2_VC_TILE - 1) / S2_VC_TILE);
+  const unsigned lt = s2_lanemask_lt();
+  for (unsigned tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    unsigned long long keys[S2_VC_CPT];
+    unsigned ballots[S2_VC_CPT];
+#pragma unroll
+    for (int m = 0; m < S2_VC_CPT; ++m) {
+      const unsigned long long o = (unsigned long long)tile * S2_VC_TILE + m * S2_VC_BLOCK + tid;
+      keys[m] = o < ncand ? cand.key[o] : 0ull;
+      ballots[m] = __ballot_sync(S2_FULL, (keys[m] >> 63) != 0ull);
+      if (lane == 0) s_warp[m * (S2_VC_BLOCK / 32) + warp] = __popc(ballots[m]);
+    }
+    __syncthreads();
+    if (warp == 0) s2_warp_exclusive32(s_warp);
+    __syncthreads();
+    const unsigned long long first = vc_off[tile];
+#pragma unroll
+    for (int m = 0; m < S2_VC_CPT; ++m) {
+      if (!((ballots[m] >> lane) & 1u)) continue;
+      const unsigned long long o = (unsigned long long)tile * S2_VC_TILE + m * S2_VC_BLOCK + tid;
+      const unsigned long long v = first + s_warp[m * (S2_VC_BLOCK / 32) + warp] + __popc(ballots[m] & lt);
+      const unsigned long long key = keys[m] & ~(1ull << 63);
+      const unsigned y = (unsigned)((key >> 16) & 0xffffu), zl = (unsigned)((key >> 32) & 0xffffu);
+      atomicAdd(mesh.rowcnt + (unsigned long long)zl * job.N + y, 1u);
+      if (v >= 0xFFFFFFFEull) atomicOr(mesh.err, S2_ERR_INDEX_OVF);
+      if (v >= mesh.vcap) {
+        atomicOr(mesh.err, S2_ERR_VERT_OVF);
+        continue;
+      }
+      mesh.key[v] = key;
+      mesh.pos[3 * v] = cand.pos[3 * o];
+      mesh.pos[3 * v + 1] = cand.pos[3 * o + 1];
+      mesh.pos[3 * v + 2] = cand.pos[3 * o + 2];
+      mesh.nrm[3 * v] = cand.nrm[3 * o];
+      mesh.nrm[3 * v + 1] = cand.nrm[3 * o + 1];
+      mesh.nrm[3 * v + 2] = cand.nrm[3 * o + 2];
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(S2_SCAN_BLOCK) s2m_rowscan(S2MeshDev mesh, unsigned long long R) {
