@@ -509,8 +509,8 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   if (kEvalVariants[v].listed) {
     const int W1 = m->sdf->prune_words + 1;
     const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
-    const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(nk));
-    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, g.tzs);
+    const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
+    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +

@@ -116,18 +116,19 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
 // The point bits of a slab's planes k0 .. k0 + gridDim.y - 1 in its decided
 // tiles (the pruned evaluation's tile pass proved |f| >= guard there with a
 // known sign): sign from the tile's flag word, near-zero 0, unknown value 1;
-// no values.  One thread per 32-point word of a row (4 tiles along x), grid
-// (ceil(P * WP / 256), planes): every word of the planes is written, the
-// undecided tiles' bytes as 0, which s2m_evalpl_* overwrites afterwards.
+// no values.  One thread per 32-point word of a row (4 tiles along x) and
+// per layer of tiles (tzs planes, nk planes in all), grid (ceil(P * WP /
+// 256), layers): every word of the planes is written, the undecided tiles'
+// bytes as 0, which s2m_evalpl_* overwrites afterwards.
 __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits pb,
                                                         const unsigned *__restrict__ tiles, int tile_words, int k0,
-                                                        int tzs) {
+                                                        int nk, int tzs) {
   const int WP = (job.P + 31) >> 5;
   const int q = (int)(blockIdx.x * 256u + threadIdx.x);  // word (y, w) of the plane
   if (q >= job.P * WP) return;
   const int y = q / WP, w = q - y * WP;
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const unsigned long long trow = ((unsigned long long)(blockIdx.y / (unsigned)tzs) * ntx + y / S2_PT_XY) * ntx;
+  const unsigned long long trow = ((unsigned long long)blockIdx.y * ntx + y / S2_PT_XY) * ntx;
   unsigned pos = 0u, unk = 0u;
 #pragma unroll
   for (int b = 0; b < 4; ++b) {
@@ -139,10 +140,18 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
     unk |= bits << (8 * b);
     if (flag & 2u) pos |= bits << (8 * b);  // S2_TILE_POSITIVE
   }
-  const long long o = ((long long)((k0 + (int)blockIdx.y) % job.ring) * job.P + y) * WP + w;
-  pb.pos[o] = pos;
-  pb.near[o] = 0u;
-  pb.unk[o] = unk;
+  const int kb = k0 + (int)blockIdx.y * tzs, ke = min(kb + tzs, k0 + nk);
+  const long long plane = (long long)job.P * WP;
+  long long o = ((long long)(kb % job.ring) * job.P + y) * WP + w;
+  const long long wrap = (long long)job.ring * plane;
+#pragma unroll 1
+  for (int k = kb; k < ke; ++k) {
+    pb.pos[o] = pos;
+    pb.near[o] = 0u;
+    pb.unk[o] = unk;
+    o += plane;
+    if (o >= wrap) o -= wrap;
+  }
 }
 
 // Cell words and tiles of a slab: word yw = y * WN + w of cell plane dz
@@ -182,28 +191,48 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
     // bottom (tb: corners k = 1, 2, 3) or top (tt: k = 4 .. 7).  Corner k =
     // bx | by << 1 | bz << 2; bx = 1 takes the row's bits shifted by one.
     unsigned andp[S2_MARK_PLANES + 1], orp[S2_MARK_PLANES + 1], tb[S2_MARK_PLANES + 1], tt[S2_MARK_PLANES + 1];
-    int slot = (zc0 + dz0) % job.ring;
+    // all loads first (planes past ncp repeat the last one, unused), so that
+    // they are in flight together
+    long long rb[S2_MARK_PLANES + 1];
+    {
+      int slot = (zc0 + dz0) % job.ring;
+#pragma unroll
+      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+        rb[p] = ((long long)slot * job.P + y) * WP + w;
+        if (p < ncp && ++slot == job.ring) slot = 0;
+      }
+    }
+    const int dw = more ? 1 : 0;
+    unsigned pw[S2_MARK_PLANES + 1][4], nw[S2_MARK_PLANES + 1][4];
 #pragma unroll
     for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-      andp[p] = ~0u;
-      orp[p] = 0u;
-      tb[p] = tt[p] = 0u;
-      if (p > ncp) continue;
-      const long long r0 = ((long long)slot * job.P + y) * WP + w, r1 = r0 + WP;
-      const unsigned p0 = __ldg(pb.pos + r0), p1 = __ldg(pb.pos + r1);
-      const unsigned p0s = __funnelshift_r(p0, more ? __ldg(pb.pos + r0 + 1) : 0u, 1);
-      const unsigned p1s = __funnelshift_r(p1, more ? __ldg(pb.pos + r1 + 1) : 0u, 1);
+      pw[p][0] = __ldg(pb.pos + rb[p]);
+      pw[p][1] = __ldg(pb.pos + rb[p] + dw);
+      pw[p][2] = __ldg(pb.pos + rb[p] + WP);
+      pw[p][3] = __ldg(pb.pos + rb[p] + WP + dw);
+      if (nearrule) {
+        nw[p][0] = __ldg(pb.near + rb[p]);
+        nw[p][1] = __ldg(pb.near + rb[p] + dw);
+        nw[p][2] = __ldg(pb.near + rb[p] + WP);
+        nw[p][3] = __ldg(pb.near + rb[p] + WP + dw);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+      const unsigned p0 = pw[p][0], p1 = pw[p][2];
+      const unsigned p0s = __funnelshift_r(p0, more ? pw[p][1] : 0u, 1);
+      const unsigned p1s = __funnelshift_r(p1, more ? pw[p][3] : 0u, 1);
       andp[p] = p0 & p0s & p1 & p1s;
       orp[p] = p0 | p0s | p1 | p1s;
+      tb[p] = tt[p] = 0u;
       if (nearrule) {
-        const unsigned n0 = __ldg(pb.near + r0), n1 = __ldg(pb.near + r1);
-        const unsigned n0s = __funnelshift_r(n0, more ? __ldg(pb.near + r0 + 1) : 0u, 1);
-        const unsigned n1s = __funnelshift_r(n1, more ? __ldg(pb.near + r1 + 1) : 0u, 1);
+        const unsigned n0 = nw[p][0], n1 = nw[p][2];
+        const unsigned n0s = __funnelshift_r(n0, more ? nw[p][1] : 0u, 1);
+        const unsigned n1s = __funnelshift_r(n1, more ? nw[p][3] : 0u, 1);
         const unsigned oz = s2_off_lattice(job, zc0 + dz0 + p) ? ~0u : 0u;
         tb[p] = (n0s & ox) | (n1 & oy) | (n1s & (ox | oy));
         tt[p] = (n0 & oz) | (n0s & (ox | oz)) | (n1 & (oy | oz)) | (n1s & (ox | oy | oz));
       }
-      if (++slot == job.ring) slot = 0;
     }
     const unsigned edge = (w == WN - 1 && (job.N & 31)) ? (1u << (job.N & 31)) - 1u : ~0u;
 #pragma unroll
