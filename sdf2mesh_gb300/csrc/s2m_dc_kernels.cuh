@@ -490,7 +490,7 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // grouped by tile (s2m_vtile_*), so that a warp's evaluations take one path
 // through the pruned SDF.  vc_cnt[t] counts the vertices of candidates
 // t * S2_VC_TILE .. (t + 1) * S2_VC_TILE - 1 (for s2m_vc_scan).
-extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK)
+extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK, 8)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
              int nzc, const unsigned *perm, unsigned *vc_cnt) {
   __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
