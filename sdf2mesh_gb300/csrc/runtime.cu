@@ -489,7 +489,8 @@ cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t
   cudaError_t e = cudaLaunchKernel((const void *)m->sdf->k_tiles_coarse,
                                    dim3(unsigned((nc + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), cargs, 0, st);
   if (e != cudaSuccess) return e;
-  const unsigned long long n = m->slab_tile_base[size_t(s_end)] - m->slab_tile_base[size_t(s_begin)];
+  // 16 threads per coarse box, one per tile of its 4 x 4 (s2m_tiles)
+  const unsigned long long n = nc * S2_PT_COARSE * S2_PT_COARSE;
   unsigned *list = prune_at<unsigned>(m, m->prune_list_off);
   unsigned *counts = prune_list_counts(m);
   void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc, &list, &counts};

@@ -234,23 +234,32 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
           const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
           const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc,
           unsigned *__restrict__ list, unsigned *__restrict__ list_count) {
-  const unsigned long long b0 = tbase[s_begin], b1 = tbase[s_end];
-  const unsigned long long g = b0 + (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
+  // Thread q takes tile q % 16 (4 x 4 along x, y) of coarse box q / 16, so a
+  // warp's tiles share two boxes' bits and take at most two paths.
+  const unsigned long long b0 = tbase[s_begin];
+  const unsigned long long q = (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
+  const unsigned long long c = cbase[s_begin] + (q >> 4);
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
+  int tx = 0, ty = 0, tz = 0, s = s_begin;
+  bool live = c < cbase[s_end];
+  if (live) {
+    s = s2_find_slab(cbase, s_begin, s_end, c);
+    const long long lc = (long long)(c - cbase[s]);
+    const int cx = (int)(lc % ncx);
+    const long long r = lc / ncx;
+    tx = cx * S2_PT_COARSE + (int)(q & 3u);
+    ty = (int)(r % ncx) * S2_PT_COARSE + (int)((q >> 2) & 3u);
+    tz = (int)(r / ncx);
+    live = tx < ntx && ty < ntx;
+  }
   unsigned long long fp_ops = 0, sfu_ops = 0;
-  if (g < b1) {
-    const int s = s2_find_slab(tbase, s_begin, s_end, g);
+  if (live) {
     int k0, nk;
     s2_slab_planes(s, D, nzc, k0, nk);
-    const long long t = (long long)(g - tbase[s]);
+    const long long t = ((long long)tz * ntx + ty) * ntx + tx;
+    const unsigned long long g = tbase[s] + (unsigned long long)t;
     const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, s2_tile_depth(nk));
-    const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-    const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
-    const int tx = (int)(t % ntx);
-    const long long q = t / ntx;
-    const int ty = (int)(q % ntx);
-    const int tz = (int)(q / ntx);
-    const unsigned long long c =
-        cbase[s] + ((unsigned long long)tz * ncx + ty / S2_PT_COARSE) * ncx + tx / S2_PT_COARSE;
     const unsigned *pm = sbits + (c - cbase[s_begin]) * S2M_TILE_WORDS;
     unsigned m[S2M_PRUNE_WORDS];
     float fp = 0.0f, sfu = 0.0f;
