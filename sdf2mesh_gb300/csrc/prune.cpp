@@ -138,6 +138,9 @@ class Pruner {
   bool run4_ = false;      // emitting the run-of-4 form
 
   static int seg(int ci, int side) { return 1 + 2 * ci + side; }
+  static bool is_smooth(POp op) {
+    return op == POp::SmoothUnion || op == POp::SmoothIntersection || op == POp::SmoothSubtraction;
+  }
   const PNode &nd(int v) const { return ir_.nodes[size_t(v)]; }
 
   void mark_live() {
@@ -481,11 +484,15 @@ class Pruner {
     const PNode &p = nd(v);
     const int sa = seg(ci, 0), sb = seg(ci, 1);
     const std::string A = as_var(p.a, var_[size_t(v)]), B = as_var(p.b, var_[size_t(v)]);
-    const std::string keepA = p.op == POp::SmoothSubtraction ? "(-" + A + ")" : A;
+    // a decided smooth operator's result is its kept operand with -0 made +0
+    // (s2_canon; the operator's arithmetic at h = 1 or 0)
+    const bool smooth = is_smooth(p.op);
+    const std::string keepA = smooth ? "s2_canon(" + (p.op == POp::SmoothSubtraction ? "(-" + A + ")" : A) + ")" : A;
+    const std::string keepB = smooth ? "s2_canon(" + B + ")" : B;
     o << ind << "if " << bit_test(sb - 1) << " {\n";
     emit_region(o, sb, members, ind + "  ");
     o << ind << "  if " << bit_test(sa - 1) << " v" << v << " = " << expr(v) << ";\n";
-    o << ind << "  else v" << v << " = " << B << ";\n";
+    o << ind << "  else v" << v << " = " << keepB << ";\n";
     o << ind << "} else {\n" << ind << "  v" << v << " = " << keepA << ";\n" << ind << "}\n";
   }
 
@@ -541,10 +548,13 @@ class Pruner {
             test << (test.tellp() > 0 ? " | " : "") << "(m[" << w << "] & 0x" << hx << ")";
           }
           const int last = mem[c1 - 1];
+          bool smooth = false;  // the chunk's kept input passes a smooth operator: s2_canon
+          for (size_t k = c0; k < c1; ++k) smooth = smooth || is_smooth(nd(mem[k]).op);
+          const std::string in = as_var(nd(mem[c0]).a, var_[size_t(last)]);
           o << ind << "if (" << test.str() << ") {\n";
           for (size_t k = c0; k < c1; ++k) emit_combinator(o, mem[k], members, ind + "  ");
           o << ind << "} else {\n";
-          o << ind << "  v" << last << " = " << as_var(nd(mem[c0]).a, var_[size_t(last)]) << ";\n";
+          o << ind << "  v" << last << " = " << (smooth ? "s2_canon(" + in + ")" : in) << ";\n";
           o << ind << "}\n";
         }
         idx = end - 1;

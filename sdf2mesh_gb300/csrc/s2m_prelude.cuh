@@ -219,6 +219,15 @@ S2HD int s2_max(int a, int b) { return a > b ? a : b; }
 S2HD unsigned s2_min(unsigned a, unsigned b) { return a < b ? a : b; }
 S2HD unsigned s2_max(unsigned a, unsigned b) { return a > b ? a : b; }
 S2HD float s2_clamp(float e, float lo, float hi) { return fminf(fmaxf(e, lo), hi); }
+// x + (+0): -0 becomes +0, every other value is unchanged (the pruned code's
+// result of a decided smooth operator).
+S2HD float s2_canon(float x) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(x, 0.0f);
+#else
+  return x + 0.0f;
+#endif
+}
 S2HD int s2_clamp(int e, int lo, int hi) { return s2_min(s2_max(e, lo), hi); }
 S2HD unsigned s2_clamp(unsigned e, unsigned lo, unsigned hi) { return s2_min(s2_max(e, lo), hi); }
 S2HD float s2_saturate(float e) { return fminf(fmaxf(e, 0.0f), 1.0f); }
@@ -380,31 +389,49 @@ S2I_FN s2i s2i_max_sel(s2i a, s2i b, int *d) {
   return s2i_max(a, b);
 }
 S2HD bool s2i_nonzero(s2i a) { return a.lo > 0.0f || a.hi < 0.0f; }
-// Smooth operators keeping both operands.  For any blend weight h in [0, 1],
-// r(h) = b (1 - h) + a h -/+ k h (1 - h) lies in [min(a, b) - k/4, max(a, b)]
-// (union; intersection mirrored), and r is quadratic in h with its extremum
-// at the unclamped weight h* = 0.5 +/- (b - a) / 2k, where it equals the
-// smooth min (max) <= min(a, b) (>= max(a, b)).  The computed h is within a
-// few ulps of clamp(h*), which moves r by k (h - h*)^2, and the binary32
-// evaluation adds at most a few ulps of |a| + |b| + k; `slack` covers both
+// Smooth operators keeping both operands.  r(h) = b (1 - h) + a h -/+
+// k h (1 - h) is quadratic in the blend weight h, with its extremum at the
+// unclamped weight h* = 0.5 +/- (b - a) / 2k.  The computed h is within a few
+// ulps of clamp(h*), which moves r by k (h - h*)^2, and the binary32
+// evaluation adds at most a few ulps of |a| + |b| + k: `slack` covers both
 // with a wide margin.
 S2HD float s2i_mag(s2i a) { return fmaxf(fabsf(a.lo), fabsf(a.hi)); }
 S2HD float s2i_slack(s2i a, s2i b, s2i k) { return (s2i_mag(a) + s2i_mag(b) + k.hi) * 0x1p-20f; }
+// Bounds of the smooth minimum and maximum where neither operand is proven
+// to win.  With d = |a - b| / k, smin(a, b) = min(a, b) - k/4 (1 - d)^2 for
+// d < 1 and min(a, b) beyond: non-decreasing in a and in b (its partial
+// derivatives are h and 1 - h) and non-increasing in k; smax(a, b) =
+// -smin(-a, -b) likewise in a and b, non-decreasing in k.  So the exact
+// range over the box of the operands is the formula at its corners.  The
+// binary32 formula (8 operations) is within E = 2^-20 (|a| + |b| + k) of the
+// exact one, so a corner value moved outward by 2 E bounds the binary32
+// value at every point of the box.  (A single bound of -k/4 below min(a, b)
+// lets the error grow by k/4 per link of a long chain of smooth unions.)
 S2HD s2i s2i_smooth_min_bound(s2i a, s2i b, s2i k) {
-  const float e = s2i_slack(a, b, k);
-  return s2i_fin(fminf(a.lo, b.lo) - 0.25f * k.hi - e, fminf(a.hi, b.hi) + e);
+  const float e = 2.0f * s2i_slack(a, b, k);
+  return s2i_fin(s2_op_smooth_union(a.lo, b.lo, k.hi) - e, s2_op_smooth_union(a.hi, b.hi, k.lo) + e);
 }
 S2HD s2i s2i_smooth_max_bound(s2i a, s2i b, s2i k) {
-  const float e = s2i_slack(a, b, k);
-  return s2i_fin(fmaxf(a.lo, b.lo) - e, fmaxf(a.hi, b.hi) + 0.25f * k.hi + e);
+  const float e = 2.0f * s2i_slack(a, b, k);
+  return s2i_fin(s2_op_smooth_intersection(a.lo, b.lo, k.lo) - e, s2_op_smooth_intersection(a.hi, b.hi, k.hi) + e);
 }
+// A decided smooth operator returns its kept operand through s2_canon (x +
+// +0: -0 becomes +0, every other value is unchanged), which reproduces the
+// operator's arithmetic at h = 1 or h = +0 bit for bit where the conditions
+// below hold.  (b * (+0) is +0 for b > 0; the terms k h (1 - h) are +0.)
+//   union         h = 1: (b * (+0) + a) - (+0)    = s2_canon(a) if a != 0 or b > 0
+//                 h = 0: (b + a * (+0)) - (+0)    = s2_canon(b) if b != 0 or a > 0
+//   intersection  h = 1: (b * (+0) + a) + (+0)    = s2_canon(a)
+//                 h = 0: (b + a * (+0)) + (+0)    = s2_canon(b)
+//   subtraction   h = 1: (b * (+0) + (-a)) + (+0) = s2_canon(-a)
+//                 h = 0: (b + (-a) * (+0)) + (+0) = s2_canon(b)
+// (Operands are finite: intervals with a non-finite end are unknown.)
 S2I_FN s2i s2i_smooth_union_sel(s2i a, s2i b, s2i k, int *d) {
   if (d) *d = 0;
   const s2i t = s2i_add(s2i_pt(0.5f), s2i_div(s2i_mul(s2i_pt(0.5f), s2i_sub(b, a)), k));
   if (s2i_ok(t) && k.lo > 0.0f) {
-    // h = 1: (b * (+0) + a) - (+0)        h = +0: (b + a * (+0)) - (+0)
-    if (t.lo >= 1.0f && (s2i_nonzero(a) || b.hi < 0.0f)) { if (d) *d = 1; return a; }
-    if (t.hi < 0.0f && (s2i_nonzero(b) || a.hi < 0.0f)) { if (d) *d = 2; return b; }
+    if (t.lo >= 1.0f && (s2i_nonzero(a) || b.lo > 0.0f)) { if (d) *d = 1; return a; }
+    if (t.hi < 0.0f && (s2i_nonzero(b) || a.lo > 0.0f)) { if (d) *d = 2; return b; }
   }
   if (!s2i_ok(a) || !s2i_ok(b) || !s2i_ok(k) || !(k.lo > 0.0f)) return s2i_unknown();
   return s2i_smooth_min_bound(a, b, k);
@@ -413,9 +440,8 @@ S2I_FN s2i s2i_smooth_intersection_sel(s2i a, s2i b, s2i k, int *d) {
   if (d) *d = 0;
   const s2i t = s2i_sub(s2i_pt(0.5f), s2i_div(s2i_mul(s2i_pt(0.5f), s2i_sub(b, a)), k));
   if (s2i_ok(t) && k.lo > 0.0f) {
-    // h = 1: (b * (+0) + a) + (+0)        h = +0: (b + a * (+0)) + (+0)
-    if (t.lo >= 1.0f && s2i_nonzero(a)) { if (d) *d = 1; return a; }
-    if (t.hi < 0.0f && s2i_nonzero(b)) { if (d) *d = 2; return b; }
+    if (t.lo >= 1.0f) { if (d) *d = 1; return a; }
+    if (t.hi < 0.0f) { if (d) *d = 2; return b; }
   }
   if (!s2i_ok(a) || !s2i_ok(b) || !s2i_ok(k) || !(k.lo > 0.0f)) return s2i_unknown();
   return s2i_smooth_max_bound(a, b, k);
@@ -424,9 +450,8 @@ S2I_FN s2i s2i_smooth_subtraction_sel(s2i a, s2i b, s2i k, int *d) {
   if (d) *d = 0;
   const s2i t = s2i_sub(s2i_pt(0.5f), s2i_div(s2i_mul(s2i_pt(0.5f), s2i_add(b, a)), k));
   if (s2i_ok(t) && k.lo > 0.0f) {
-    // h = 1: (b * (+0) + (-a)) + (+0)     h = +0: (b + (-a) * (+0)) + (+0)
-    if (t.lo >= 1.0f && s2i_nonzero(a)) { if (d) *d = 1; return s2i_neg(a); }
-    if (t.hi < 0.0f && s2i_nonzero(b)) { if (d) *d = 2; return b; }
+    if (t.lo >= 1.0f) { if (d) *d = 1; return s2i_neg(a); }
+    if (t.hi < 0.0f) { if (d) *d = 2; return b; }
   }
   if (!s2i_ok(a) || !s2i_ok(b) || !s2i_ok(k) || !(k.lo > 0.0f)) return s2i_unknown();
   return s2i_smooth_max_bound(s2i_neg(a), b, k);
@@ -501,6 +526,7 @@ S2_X4_OP(*)
 S2_X4_OP(/)
 #undef S2_X4_OP
 S2HD s2x4 operator-(const s2x4 &a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = -a.v[i]; return r; }
+S2HD s2x4 s2_canon(const s2x4 &a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = s2_canon(a.v[i]); return r; }
 #define S2_X4_F1(name) \
   template <class A> S2HD s2x4 s2r_##name(const A &a) { s2x4 r; for (int i = 0; i < 4; ++i) r.v[i] = s2_##name(s2_lane(a, i)); return r; }
 #define S2_X4_F2(name)                                                                       \

@@ -117,6 +117,40 @@ def test_edge_cases(lib, N):
     check(cu, N)  # every tile
 
 
+# A decided smooth operator whose kept operand is +-0: the pruned code
+# returns it through s2_canon (-0 -> +0), which must match the operator's own
+# arithmetic at h = 1 or h = 0 bit for bit.  Each SDF returns the operator's
+# value itself, so the sign of a zero reaches the comparison.  z0 is +0 for
+# x >= 0 and -0 for x < 0; `far` is positive except near one corner.
+_ZERO_PRE = """use sdf3d::primitives;
+use sdf::op;
+fn sdf3d(p: vec3f) -> f32 {
+    let z0 = p.x * 0.0;
+    let far = sdf3d_sphere(p - vec3f(0.9, 0.9, 0.9), 0.05);
+    return %s;
+}
+"""
+SIGNED_ZERO_KEEPS = [
+    "sdf_op_smooth_union(z0, far, 0.05)",                       # keep a = +-0, b > 0
+    "sdf_op_smooth_union(far, -z0, 0.05)",                      # keep b = -+0, a > 0
+    "sdf_op_smooth_intersection(z0, -far - 1.0, 0.05)",         # keep a, b < 0
+    "sdf_op_smooth_intersection(-far - 1.0, -z0, 0.05)",        # keep b, a < 0
+    "sdf_op_smooth_subtraction(z0, -far - 1.0, 0.05)",          # keep -a
+    "sdf_op_smooth_subtraction(far + 1.0, -z0, 0.05)",          # keep b
+    "sdf_op_smooth_union(sdf_op_smooth_union(z0, far, 0.05), far + 0.5, 0.05)",  # canonical chain input
+]
+
+
+@pytest.mark.parametrize("expr", SIGNED_ZERO_KEEPS)
+@pytest.mark.parametrize("N", [16, 33])
+def test_smooth_keep_of_signed_zero(lib, expr, N):
+    cu, fp, _ = lowered(_ZERO_PRE % expr)
+    assert "S2M_HAS_PRUNE" in cu
+    ops = check(cu, N)  # every tile, bitwise
+    # the decision is taken somewhere (the operand that is not kept is pruned)
+    assert ops[:, 0].min() < fp
+
+
 def test_user_function_with_library_arithmetic_is_a_combinator(lib):
     """A user function whose body is sdf::op's smooth union arithmetic is
     recognised by its arithmetic, not its name."""
