@@ -274,17 +274,18 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
 // 8 lattice corner values (NaN where the point's unknown-value bit is set: a
 // decided tile of the pruned evaluation wrote no value there).  Grid (nbp,
-// cell planes), block = tile.  Each warp first lists the candidates of its 32
-// words in shared memory (word lane << 5 | bit, in (y, x) order), then writes
-// them 32 at a time, one per lane: most words hold one or two candidates, so
-// this keeps every lane busy.
+// cell planes), block = tile.  The block first lists the candidates of its
+// words in shared memory (word << 5 | bit, in (y, x) order), then writes
+// them one per thread: a word holds one or two candidates at most places of
+// the surface, and a warp's 32 words (a row at N = 1024) a handful, so the
+// block-wide list keeps the threads busy.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
                                                             const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
                                                             S2Cand cand, unsigned *err, int zc0) {
   __shared__ unsigned s_warp[32];
-  __shared__ unsigned short s_list[S2_CW_BLOCK / 32][32 * 32];
+  __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const int WN = (job.N + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + tid);
@@ -297,26 +298,27 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
     if ((int)lane >= o) inc += t;
   }
-  const unsigned total = __shfl_sync(S2_FULL, inc, 31);
-  {
-    unsigned r = inc - cnt, rem = mask;
-    while (rem) {
-      const unsigned bit = __ffs(rem) - 1u;
-      rem &= rem - 1u;
-      s_list[warp][r++] = (unsigned short)((lane << 5) | bit);
-    }
-  }
   if (lane == 31) s_warp[warp] = inc;
   if (tid < 32 && tid >= S2_CW_BLOCK / 32) s_warp[tid] = 0u;
   __syncthreads();
   if (warp == 0) s2_warp_exclusive32(s_warp);
   __syncthreads();
-  const unsigned long long first = tile_off[(unsigned long long)dz * gridDim.x + blockIdx.x] + s_warp[warp];
+  const unsigned total = s_warp[31];  // slots past the block's warps are 0: slot 31 gets the total
+  {
+    unsigned r = s_warp[warp] + inc - cnt, rem = mask;
+    while (rem) {
+      const unsigned bit = __ffs(rem) - 1u;
+      rem &= rem - 1u;
+      s_list[r++] = (unsigned short)((tid << 5) | bit);
+    }
+  }
+  __syncthreads();
+  const unsigned long long first = tile_off[(unsigned long long)dz * gridDim.x + blockIdx.x];
   const int WP = (job.P + 31) >> 5;
 #pragma unroll 1
-  for (unsigned r = lane; r < total; r += 32u) {
-    const unsigned e = s_list[warp][r];
-    const int ywc = (int)(blockIdx.x * S2_CW_BLOCK + (warp << 5) + (e >> 5));
+  for (unsigned r = tid; r < total; r += S2_CW_BLOCK) {
+    const unsigned e = s_list[r];
+    const int ywc = (int)(blockIdx.x * S2_CW_BLOCK + (e >> 5));
     const int wy = ywc / WN, w = ywc - wy * WN;
     const unsigned bit = e & 31u;
     S2Cell cell;
@@ -468,11 +470,22 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand ca
     __syncthreads();
     if (warp == 0) s2_warp_exclusive32(s_warp);
     __syncthreads();
-    const unsigned long long first = vc_off[tile];
+    // every load of the tile's vertices first, so that they are in flight together
+    float pn[S2_VC_CPT][6];
 #pragma unroll
     for (int m = 0; m < S2_VC_CPT; ++m) {
       if (!((ballots[m] >> lane) & 1u)) continue;
       const unsigned long long o = (unsigned long long)tile * S2_VC_TILE + m * S2_VC_BLOCK + tid;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        pn[m][c] = __ldg(cand.pos + 3 * o + c);
+        pn[m][3 + c] = __ldg(cand.nrm + 3 * o + c);
+      }
+    }
+    const unsigned long long first = vc_off[tile];
+#pragma unroll
+    for (int m = 0; m < S2_VC_CPT; ++m) {
+      if (!((ballots[m] >> lane) & 1u)) continue;
       const unsigned long long v = first + s_warp[m * (S2_VC_BLOCK / 32) + warp] + __popc(ballots[m] & lt);
       const unsigned long long key = keys[m] & ~(1ull << 63);
       const unsigned y = (unsigned)((key >> 16) & 0xffffu), zl = (unsigned)((key >> 32) & 0xffffu);
@@ -483,12 +496,11 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand ca
         continue;
       }
       mesh.key[v] = key;
-      mesh.pos[3 * v] = cand.pos[3 * o];
-      mesh.pos[3 * v + 1] = cand.pos[3 * o + 1];
-      mesh.pos[3 * v + 2] = cand.pos[3 * o + 2];
-      mesh.nrm[3 * v] = cand.nrm[3 * o];
-      mesh.nrm[3 * v + 1] = cand.nrm[3 * o + 1];
-      mesh.nrm[3 * v + 2] = cand.nrm[3 * o + 2];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        mesh.pos[3 * v + c] = pn[m][c];
+        mesh.nrm[3 * v + c] = pn[m][3 + c];
+      }
     }
     __syncthreads();
   }
