@@ -233,6 +233,23 @@ def eval_traffic_per_point(pruned=False):
     return None
 
 
+JOB_PROFILE = "job_csg64_1024.md"
+
+
+def job_profile():
+    """Warp instructions and DRAM bytes per job of the pruned evaluation phase
+    (CSG at 1024^3), from the committed ncu summary of one job."""
+    out = {}
+    try:
+        for line in open(os.path.join(ROOT, "profiles", JOB_PROFILE)):
+            for key in ("eval_inst_per_job", "eval_dram_bytes_per_job"):
+                if line.startswith(key):
+                    out[key] = float(line.split("=")[1])
+    except OSError:
+        pass
+    return out
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -433,12 +450,39 @@ def ours(a):
                   "sfu_peak_gops": sfu_peak, "dominant_by_time": dom,
                   "peak_source": "measured in this run: s2m_fp32_probe (FP32 add/mul issue rate) and "
                                  "s2m_sfu_probe (MUFU rsqrt issue rate); MEASURED_PEAKS.json has neither"}
+        jp = job_profile() if (eval_ops["pruned"] and a.workload == "csg64_1024" and N == 1024) else {}
         if t_sfu > t_fp32:
             roof = {"bound": "sfu", "achieved": eval_sfu, "peak": sfu_peak, "unit": "Gop/s",
                     "frac": eval_sfu / sfu_peak, **common}
         else:
             roof = {"bound": "fp32", "achieved": eval_gops, "peak": fp32_peak, "unit": "Gop/s",
                     "frac": eval_gops / fp32_peak, **common}
+        if jp.get("eval_inst_per_job"):
+            # Tile pruning leaves under one FP32 operation per lattice point: the phase is
+            # bound by instruction issue (interval code, tests of the activity bits, IEEE
+            # division and square-root sequences, point-bit stores), so its roofline is the
+            # issue rate: warp instructions per second against 4 per SM and clock.
+            sms = torch.cuda.get_device_properties(dev).multi_processor_count
+            mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+            t_job = ms["eval_planes"] / a.steps * 1e-3
+            if mhz and t_job > 0:
+                issue_peak = sms * 4 * mhz * 1e6 / 1e9
+                achieved = jp["eval_inst_per_job"] / t_job / 1e9
+                fp32_view = {"bound": roof["bound"], "achieved": roof["achieved"], "peak": roof["peak"],
+                             "unit": roof["unit"], "frac": roof["frac"]}
+                roof = {**common, "bound": "issue", "achieved": achieved, "peak": issue_peak,
+                        "unit": "G warp-instructions/s", "frac": achieved / issue_peak,
+                        "kernel": "s2m_tiles_coarse + s2m_tiles + s2m_fill_decided + s2m_evalpl_* (one job)",
+                        "traffic": jp.get("eval_dram_bytes_per_job"),
+                        "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the phase's "
+                                          f"launches in one job (profiles/{JOB_PROFILE})",
+                        "instructions_per_job": jp["eval_inst_per_job"],
+                        "instructions_source": f"ncu smsp__inst_executed.sum of the phase's launches in one "
+                                               f"job (profiles/{JOB_PROFILE})",
+                        "achieved_unit_time": "CUDA events of the phase per step",
+                        "peak_source": f"{sms} SMs x 4 warp schedulers x {mhz:.0f} MHz (median SM clock "
+                                       "sampled during the timed steps)",
+                        "fp32_view": fp32_view}
     else:
         roof = {"bound": "hbm", "kernel": dom, "achieved": contour_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": (contour_gbs or 0) / pk["hbm_gbs"], "peak_source": pk_kind, "traffic": None}
