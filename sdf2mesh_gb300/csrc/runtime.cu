@@ -518,8 +518,10 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
                            (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
     const unsigned *count = prune_list_counts(m) + s;
     void *largs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &list, &count};
-    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK),
-                            largs, 0, st);
+    // warps stride over the list (its length is on the device): 16 blocks per SM
+    const long long lblocks = std::min<long long>((g.ntiles + 3) / 4, (long long)device_sm_count() * 16);
+    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned(lblocks)), dim3(S2_PT_BLOCK), largs, 0,
+                            st);
   }
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
   return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,

@@ -421,16 +421,20 @@ __device__ __forceinline__ void s2_eval_pruned_listed(const S2Job &job, float *_
                                                       const unsigned *__restrict__ bits, int k0, int nk, int tzs,
                                                       const unsigned *__restrict__ list,
                                                       const unsigned *__restrict__ list_count) {
-  const unsigned i = blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5);
-  if (i >= __ldg(list_count)) return;  // whole warps
-  const unsigned t = __ldg(list + i);
-  const S2PruneTile tl = s2_prune_tile(job, (long long)t, k0, nk, tzs);
-  if (tl.kb > tl.ke) return;
+  // The list's length is known only on the device: the grid is sized for the
+  // GPU (a few blocks per SM), and its warps stride over the list.
   __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_TILE_WORDS];
   const int lane = (int)(threadIdx.x & 31u);
-  if (lane < S2M_TILE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + (unsigned long long)t * S2M_TILE_WORDS + lane);
-  __syncwarp();
-  s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
+  const unsigned n = __ldg(list_count), stride = gridDim.x * (S2_PT_BLOCK / 32);
+  for (unsigned i = blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5); i < n; i += stride) {  // whole warps
+    const unsigned t = __ldg(list + i);
+    const S2PruneTile tl = s2_prune_tile(job, (long long)t, k0, nk, tzs);
+    if (tl.kb > tl.ke) continue;
+    __syncwarp();  // the previous tile's bits are no longer read
+    if (lane < S2M_TILE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + (unsigned long long)t * S2M_TILE_WORDS + lane);
+    __syncwarp();
+    s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
+  }
 }
 
 #define S2_EVALPL_VARIANT(NAME, MINB, RUN4)                                                       \
