@@ -485,11 +485,17 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand ca
     const unsigned long long first = vc_off[tile];
 #pragma unroll
     for (int m = 0; m < S2_VC_CPT; ++m) {
-      if (!((ballots[m] >> lane) & 1u)) continue;
+      // one count per row and warp: the warp's vertices are in (z, y, x) order,
+      // so a row's vertices are neighbours
+      const bool has = (ballots[m] >> lane) & 1u;
+      const unsigned long long row = has ? ((keys[m] >> 32) & 0xffffull) * (unsigned long long)job.N +
+                                               ((keys[m] >> 16) & 0xffffull)
+                                         : ~0ull;
+      const unsigned peers = __match_any_sync(S2_FULL, row);
+      if (has && (unsigned)(__ffs(peers) - 1) == lane) atomicAdd(mesh.rowcnt + row, (unsigned)__popc(peers));
+      if (!has) continue;
       const unsigned long long v = first + s_warp[m * (S2_VC_BLOCK / 32) + warp] + __popc(ballots[m] & lt);
       const unsigned long long key = keys[m] & ~(1ull << 63);
-      const unsigned y = (unsigned)((key >> 16) & 0xffffu), zl = (unsigned)((key >> 32) & 0xffffu);
-      atomicAdd(mesh.rowcnt + (unsigned long long)zl * job.N + y, 1u);
       if (v >= 0xFFFFFFFEull) atomicOr(mesh.err, S2_ERR_INDEX_OVF);
       if (v >= mesh.vcap) {
         atomicOr(mesh.err, S2_ERR_VERT_OVF);
