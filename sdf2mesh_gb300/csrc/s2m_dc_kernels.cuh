@@ -279,8 +279,17 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
 #pragma unroll
     for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
     dst[S2M_PRUNE_WORDS] = flag;
-    if (!flag) {  // the slab's list of tiles to evaluate (in any order)
-      const unsigned i = atomicAdd(list_count + s, 1u);
+    // the slab's list of tiles to evaluate (in any order): one atomic per slab
+    // and warp, since every thread of a slab adds to the same counter
+    const unsigned am = __activemask();
+    const unsigned und = __ballot_sync(am, !flag);
+    if (!flag) {
+      const unsigned peers = __match_any_sync(und, s);
+      const int leader = __ffs(peers) - 1;
+      unsigned first = 0;
+      if ((int)(threadIdx.x & 31u) == leader) first = atomicAdd(list_count + s, (unsigned)__popc(peers));
+      first = __shfl_sync(peers, first, leader);
+      const unsigned i = first + (unsigned)__popc(peers & s2_lanemask_lt());
       list[(tbase[s] - b0) + i] = (unsigned)t;
     }
     const unsigned long long npts = (unsigned long long)(tl.i1 - tl.i0 + 1) * (unsigned long long)(tl.j1 - tl.j0 + 1) *

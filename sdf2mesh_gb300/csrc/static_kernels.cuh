@@ -372,7 +372,15 @@ __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, i
     c.y = (int)((k >> 16) & 0xffffull);
     c.z = (int)((k >> 32) & 0xffffull);
     const unsigned long long t = s2_cell_prune_tile(job, c, tbase, D, nzc);
-    trank[i] = (t << 16) | atomicAdd(tcnt + t, 1u);  // a tile covers at most 8 x 8 x 8 cells
+    // one atomic per tile and warp (a warp's candidates share a few tiles)
+    const unsigned am = __activemask();
+    const unsigned peers = __match_any_sync(am, t);
+    const int leader = __ffs(peers) - 1;
+    unsigned first = 0;
+    if ((int)(threadIdx.x & 31u) == leader) first = atomicAdd(tcnt + t, (unsigned)__popc(peers));
+    first = __shfl_sync(peers, first, leader);
+    const unsigned rank = first + (unsigned)__popc(peers & s2_lanemask_lt());
+    trank[i] = (t << 16) | rank;  // a tile covers at most 8 x 8 x 8 cells
   }
 }
 
