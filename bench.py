@@ -217,7 +217,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-EVAL_PROFILE = {False: "s2m_eval_csg64_512.md", True: "s2m_evalp_csg64_512.md"}
+EVAL_PROFILE = {False: "s2m_eval_csg64_512.md", True: "job_csg64_1024.md"}
 
 
 def eval_traffic_per_point(pruned=False):
@@ -434,8 +434,8 @@ def ours(a):
         traffic = tpp * prof["eval_points"] / n_eval if tpp else None
         common = {"kernel": "s2m_tiles + s2m_evalp_*" if eval_ops["pruned"] else "s2m_eval_*",
                   "traffic": traffic, "traffic_source": (
-                      "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 512^3 case "
-                      f"(profiles/{EVAL_PROFILE[eval_ops['pruned']]}), scaled by points per launch")
+                      "ncu dram__bytes_read.sum + dram__bytes_write.sum per lattice point from "
+                      f"profiles/{EVAL_PROFILE[eval_ops['pruned']]}, scaled by points per launch")
                   if traffic else None,
                   "tile_pruning": eval_ops["pruned"],
                   "ms_per_launch": per_launch_ms,
