@@ -448,7 +448,8 @@ size_t prune_layout(s2m_mesh *m) {
     slab_planes(m, s, k0, nk);
     const PruneGeom g = prune_geom(m->job, nk);
     m->slab_tile_base[size_t(s) + 1] = m->slab_tile_base[size_t(s)] + (unsigned long long)g.ntiles;
-    m->slab_coarse_base[size_t(s) + 1] = m->slab_coarse_base[size_t(s)] + (unsigned long long)(ncx * ncx * g.nzt);
+    m->slab_coarse_base[size_t(s) + 1] =
+        m->slab_coarse_base[size_t(s)] + (unsigned long long)(ncx * ncx * ((g.nzt + S2_PT_COARSE_Z - 1) / S2_PT_COARSE_Z));
     max_slab = std::max(max_slab, (unsigned long long)g.ntiles);
   }
   const size_t words = size_t(m->sdf->prune_words);
@@ -489,8 +490,8 @@ cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t
   cudaError_t e = cudaLaunchKernel((const void *)m->sdf->k_tiles_coarse,
                                    dim3(unsigned((nc + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), cargs, 0, st);
   if (e != cudaSuccess) return e;
-  // 16 threads per coarse box, one per tile of its 4 x 4 (s2m_tiles)
-  const unsigned long long n = nc * S2_PT_COARSE * S2_PT_COARSE;
+  // one thread per tile slot of each coarse box (s2m_tiles)
+  const unsigned long long n = nc * S2_PT_COARSE * S2_PT_COARSE * S2_PT_COARSE_Z;
   unsigned *list = prune_at<unsigned>(m, m->prune_list_off);
   unsigned *counts = prune_list_counts(m);
   void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc, &list, &counts};

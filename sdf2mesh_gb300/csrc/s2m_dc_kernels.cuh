@@ -147,9 +147,9 @@ __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long
 
 // The tile pass of slabs s_begin .. s_end - 1, in two launches of one thread
 // per box, each covering many slabs so that the grid fills the GPU:
-//   s2m_tiles_coarse  boxes of 4 x 4 tiles (32 x 32 points by the tile depth):
-//                     the full interval evaluation -> sbits and the box's
-//                     flag word
+//   s2m_tiles_coarse  boxes of 4 x 4 tiles by 2 layers of tiles (32 x 32
+//                     points by twice the tile depth): the full interval
+//                     evaluation -> sbits and the box's flag word
 //   s2m_tiles         each tile inside its coarse box: only the segments
 //                     active in the box are evaluated -> bits, and the SDF
 //                     operations that remain (ops[0] FP32, ops[1] SFU, per
@@ -213,11 +213,11 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   const int cx = (int)(lc % ncx);
   const long long q = lc / ncx;
   const int cy = (int)(q % ncx);
-  const int tz = (int)(q / ncx);
+  const int cz = (int)(q / ncx);
   const int span = S2_PT_XY * S2_PT_COARSE;
   const int i0 = cx * span, i1 = min(i0 + span, job.P) - 1;
   const int j0 = cy * span, j1 = min(j0 + span, job.P) - 1;
-  const int kb = k0 + tz * tzs, ke = min(kb + tzs, k0 + nk) - 1;
+  const int kb = k0 + cz * S2_PT_COARSE_Z * tzs, ke = min(kb + S2_PT_COARSE_Z * tzs, k0 + nk) - 1;
   const s2i X = s2_prune_box(job, i0, i1 + 1), Y = s2_prune_box(job, j0, j1 + 1), Z = s2_prune_box(job, kb - 1, max(kb, ke));
   unsigned m[S2M_PRUNE_WORDS];
   float fp, sfu;
@@ -234,24 +234,30 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
           const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
           const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc,
           unsigned *__restrict__ list, unsigned *__restrict__ list_count) {
-  // Thread q takes tile q % 16 (4 x 4 along x, y) of coarse box q / 16, so a
-  // warp's tiles share two boxes' bits and take at most two paths.
+  // Thread q takes tile q % 32 (4 x 4 along x, y, by 2 layers along z) of
+  // coarse box q / 32, so a warp's tiles share one box's bits and take one
+  // path through the interval code.
+  constexpr unsigned kPerBox = S2_PT_COARSE * S2_PT_COARSE * S2_PT_COARSE_Z;
   const unsigned long long b0 = tbase[s_begin];
   const unsigned long long q = (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
-  const unsigned long long c = cbase[s_begin] + (q >> 4);
+  const unsigned long long c = cbase[s_begin] + q / kPerBox;
+  const unsigned sub = (unsigned)(q % kPerBox);
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
   int tx = 0, ty = 0, tz = 0, s = s_begin;
   bool live = c < cbase[s_end];
   if (live) {
     s = s2_find_slab(cbase, s_begin, s_end, c);
+    int k0s, nks;
+    s2_slab_planes(s, D, nzc, k0s, nks);
+    const int tzs = s2_tile_depth(nks), nzt = (nks + tzs - 1) / tzs;
     const long long lc = (long long)(c - cbase[s]);
     const int cx = (int)(lc % ncx);
     const long long r = lc / ncx;
-    tx = cx * S2_PT_COARSE + (int)(q & 3u);
-    ty = (int)(r % ncx) * S2_PT_COARSE + (int)((q >> 2) & 3u);
-    tz = (int)(r / ncx);
-    live = tx < ntx && ty < ntx;
+    tx = cx * S2_PT_COARSE + (int)(sub & 3u);
+    ty = (int)(r % ncx) * S2_PT_COARSE + (int)((sub >> 2) & 3u);
+    tz = (int)(r / ncx) * S2_PT_COARSE_Z + (int)(sub >> 4);
+    live = tx < ntx && ty < ntx && tz < nzt;
   }
   unsigned long long fp_ops = 0, sfu_ops = 0;
   if (live) {

@@ -110,6 +110,7 @@ struct S2MeshDev {
 #define S2_VT_TILE 2048  // per-tile candidate counts scanned per block of s2m_vtile_scan (256 threads x 8)
 #define S2_PT_BLOCK 128
 #define S2_PT_COARSE 4            /* tiles per coarse box of the tile pass, along x and y */
+#define S2_PT_COARSE_Z 2          /* ... and layers of tiles along z */
 #define S2_VX_BLOCK 128
 #define S2_VC_BLOCK 256
 #define S2_VC_CPT 4
