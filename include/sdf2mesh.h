@@ -79,7 +79,10 @@ typedef struct {
   float bounds;           /* edge of the centred cube [-B/2, B/2]^3        */
   float eps;              /* normal epsilon (reference: 1e-4)              */
   uint32_t flags;         /* S2M_JOB_*                                     */
-  uint32_t slab_depth;    /* cell slices per slab; 0 = automatic           */
+  uint32_t slab_depth;    /* cell slices per slab; 0 = automatic: a ring of
+                             lattice planes that fits in L2 (full
+                             evaluation), or slabs of equal depth from a
+                             ring of up to 4 GB (SDFs with a tile form)     */
   uint32_t reserved;
   uint64_t max_vertices;  /* initial vertex capacity; 0 = automatic        */
   uint64_t max_triangles; /* initial triangle capacity; 0 = automatic      */
