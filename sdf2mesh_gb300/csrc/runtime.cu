@@ -692,8 +692,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   cand.nrm = m->cand_nrm;
   cand.cap = m->cand_cap;
   cand.base = m->cand_base;
-  cand.status = m->cand_status;
-  cand.tile_counter = c.counters + 0;
+  cand.status = nullptr;  // the per-job compaction is wait-free (s2m_vc_scan, s2m_vcompact)
+  cand.tile_counter = nullptr;
 
   S2MeshDev md;
   md.pos = m->pos;

@@ -55,8 +55,8 @@ struct S2Cand {
   float *nrm;                     // 3 per candidate
   unsigned long long cap;         // capacity of the arrays
   unsigned long long *base;       // nslabs + 1 running offsets (exact even on overflow)
-  unsigned long long *status;     // look-back words of s2m_vcompact tiles
-  unsigned *tile_counter;         // s2m_vcompact
+  unsigned long long *status;     // look-back words of s2_vcompact_worker's tiles (batch engine)
+  unsigned *tile_counter;         // s2_vcompact_worker's tile counter (batch engine)
 };
 
 // Sign (v > 0) and near-zero (!(|v| >= guard)) bits of lattice points,
