@@ -7,7 +7,7 @@
 //     void f.normal(float x, float y, float z, float eps, float n[3]) const;
 //                                                           // sdf3d_normal, not normalised
 // NVRTC instantiates it with the lowered user SDF (s2m_dc_kernels.cuh); the
-// batch engine with its CSG program interpreter (s2m_batch.cuh).
+// batch engine with its CSG program interpreter (batch.cu).
 // All arithmetic of the rule is explicitly rounded binary32 / binary64.
 #pragma once
 
