@@ -160,8 +160,10 @@ int s2m_sdf_eval_variant_info(const s2m_sdf *sdf, int variant, char *name, size_
    lattice points.  Where it proves that a min, max or sdf::op smooth
    operator returns one operand bit for bit at every point of the tile, the
    other operand's exclusive operations are skipped there, so the lattice
-   values stay bit-identical.  *combinators: combinators that can prune (0:
-   no pruning form, or turned off by S2M_COMPILE_FMAD / _NO_PRUNE). */
+   values stay bit-identical.  *combinators: combinators that can prune;
+   *words: activity words per tile (0: no tile form, or turned off by
+   S2M_COMPILE_FMAD / _NO_PRUNE; a straight-line SDF without combinators
+   still has a tile form, with 0 combinators and 1 word). */
 int s2m_sdf_prune_info(const s2m_sdf *sdf, int *combinators, int *words);
 
 void s2m_sdf_free(s2m_sdf *sdf);

@@ -1096,11 +1096,28 @@ struct SWave {
   cudaStream_t st = nullptr;
 };
 
-uint64_t sdf_job_footprint(const s2m_params &p) {
-  const uint64_t N = p.resolution, n2 = N * N;
-  const uint64_t plane = (N + 1) * ((N + 32) / 32 * 32) * 4;
-  const uint64_t ring = std::min<uint64_t>(plane * 65, std::max<uint64_t>(2 * plane, 50000000ull));
-  return ring + n2 * (8 * 64 + 6 * 32 + 12 * 12 + 8 + 8) + (64u << 20);
+// Device bytes of one per-job mesh (s2m_mesh_create), for admission.  The
+// lattice ring follows the slab depth that setup_job picks: the given one,
+// an L2-sized ring (<= 65 planes) for full evaluation, or slabs of equal
+// depth from a ring of up to 4 GB for an SDF with a tile form; the point
+// bits are 3 bits per point of the ring.
+uint64_t sdf_job_footprint(const s2m_sdf *sdf, const s2m_params &p) {
+  const uint64_t N = p.resolution, n2 = N * N, P = N + 1;
+  const uint64_t plane = P * ((N + 32) / 32 * 32) * 4;
+  int words = 0;
+  const bool tile_form = s2m_sdf_prune_info(sdf, nullptr, &words) == S2M_OK && words > 0;
+  uint64_t planes;
+  if (p.slab_depth) {
+    planes = std::min<uint64_t>(p.slab_depth, N) + 1;
+  } else if (tile_form) {
+    const uint64_t dmax = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(4.0e9 / double(plane)), 1000000000ull) - 1);
+    const uint64_t ns = (std::max<uint64_t>(N, 1) + dmax - 1) / dmax;
+    planes = (N + ns - 1) / ns + 1;
+  } else {
+    planes = std::min<uint64_t>(65, std::max<uint64_t>(2, 50000000ull / plane));
+  }
+  const uint64_t ring = planes * plane, bits = 3 * planes * P * ((P + 31) / 32) * 4;
+  return ring + bits + n2 * (8 * 64 + 6 * 32 + 12 * 12 + 8 + 8) + (64u << 20);
 }
 
 }  // namespace
@@ -1383,7 +1400,7 @@ int s2m_server_submit_csg(s2m_server *s, const float *program, uint32_t len, con
 int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *params, uint64_t *request_id,
                           char *err, size_t errlen) {
   if (!s || !sdf || !params) return S2M_E_INVALID;
-  uint64_t fp = sdf_job_footprint(*params);
+  uint64_t fp = sdf_job_footprint(sdf, *params);
   if (s->cfg.memory_budget_bytes && fp > s->cfg.memory_budget_bytes) {
     set_err(err, errlen, "request larger than the memory budget");
     return S2M_E_OOM;
