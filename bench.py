@@ -16,15 +16,27 @@ mesh is bit-identical to the full evaluation (a GPU test).
   e2e          the C-ABI call a user makes per job: s2m_mesh_create (device
                buffers, pipeline, count readback) + the mesh copied to pinned
                host memory + s2m_mesh_free
-  roofline     the dominant kernel, from CUDA events around every launch of
-               the timed steps; for the evaluation, the SDF operations it
-               executed (with tile pruning: counted per tile by the tile pass)
+  roofline     the phase that takes the most device time (CUDA events around
+               every launch of the timed steps): its algorithmic bytes (or, for
+               the evaluation, the SDF operations it executed) per launch over
+               its event time per launch
   full_evaluation  the same job with tile pruning off (every SDF operation at
                every lattice point), timed the same way
-  cpu_baseline the CPU oracle (restatement of the reference rule, OpenMP on all
-               host cores) on a bounded window of slices of the same job
+  cpu_baseline the CPU oracle (restatement of the reference rule) on a bounded
+               window of slices of the same job, on all host cores and on one
 
---impl reference times that CPU implementation alone (the reference itself
+The same line also carries compact results of the other configurations, each
+measured in this run:
+  mandelbulb_2048  the power-8 Mandelbulb (8 iterations, bounds 2.5) at
+               2048^3, reference rule and precision mode
+  batch256     256 seeded random CSG trees in one persistent launch, beside
+               the plain per-job pipeline on the same jobs (modules compiled
+               beforehand)
+  serve        a Poisson request stream at several rates through the
+               continuous-batching server, beside the plain per-job pipeline
+               with the same compiled modules
+
+--impl reference times the CPU implementation alone (the reference itself
 is Rust + wgpu and cannot run here) and prints the same line.
 N > 1 GPUs (torchrun): independent replicas, one job per rank, no collective
 on the data path ("replicas only").
@@ -32,8 +44,10 @@ on the data path ("replicas only").
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -49,6 +63,7 @@ BOUNDS = 2.0
 METRIC = "Gvoxels/s at 1024^3"
 UNIT = "Gvoxels/s"
 CPU_SAMPLE_SLICES = 16     # cpu_baseline: cell slices [504, 520) of the 1024^3 job
+CPU_SAMPLE_SLICES_1T = 2   # ... on one host thread: [504, 506)
 REF_STEP_SLICES = 4        # --impl reference: cell slices per step
 CPU_Z0 = 504
 
@@ -63,6 +78,8 @@ def parse():
     ap.add_argument("--workload", default="csg64_1024", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-full-eval", action="store_true", help="skip the run without tile pruning")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the mandelbulb_2048 / batch256 / serve sub-results of the headline line")
     return ap.parse_args()
 
 
@@ -84,6 +101,7 @@ WORKLOADS = {
                                          "QEF vertex, FP32 compensated sums, FP64 solve"),
 }
 _ACTIVE = {"name": "csg64_1024"}
+MANDEL_DESC = "Mandelbulb power 8, 8 iterations, bailout 2, offset 0.003 (GLSL), bounds 2.5"
 
 
 def reduce_max(value: float, device=None) -> float:
@@ -217,45 +235,195 @@ class Clocks:
                 "samples": len(sm)}
 
 
-EVAL_PROFILE = {False: "s2m_eval_csg64_512.md", True: "job_csg64_1024.md"}
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return {"hbm_gbs": 6800.0}, "fallback (6.8 TB/s, no MEASURED_PEAKS.json)"
 
 
-def eval_traffic_per_point(pruned=False):
-    """DRAM bytes per lattice point of the evaluation (pruned: tile pass + pruned
-    kernel), from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", EVAL_PROFILE[pruned])
-    try:
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_point"):
-                return float(line.split("=")[1])
-    except OSError:
-        pass
-    return None
+PHASE_PROFILE = "phases_csg64_1024.md"
 
 
-JOB_PROFILE = "job_csg64_1024.md"
-
-
-def job_profile():
-    """Warp instructions and DRAM bytes per job of the pruned evaluation phase
-    (CSG at 1024^3), from the committed ncu summary of one job."""
+def phase_traffic():
+    """DRAM bytes per 1024^3 CSG job of each pipeline phase, from the committed
+    ncu summary of one job (profiles/phases_csg64_1024.md: lines
+    `traffic_<phase> = <bytes>`)."""
     out = {}
     try:
-        for line in open(os.path.join(ROOT, "profiles", JOB_PROFILE)):
-            for key in ("eval_inst_per_job", "eval_dram_bytes_per_job"):
-                if line.startswith(key):
-                    out[key] = float(line.split("=")[1])
+        for line in open(os.path.join(ROOT, "profiles", PHASE_PROFILE)):
+            if line.startswith("traffic_") and "=" in line:
+                k, v = line.split("=", 1)
+                out[k.strip()[len("traffic_"):]] = float(v)
     except OSError:
         pass
     return out
 
 
-def peaks():
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f), "measured"
-    return {"hbm_gbs": 6800.0}, "fallback"
+def phase_bytes(phase, N, C, V, T, pruned):
+    """Algorithmic DRAM bytes of one job's phase (what it must read and write at
+    least): 2 point bits (sign, near-zero) per lattice point for classification
+    (plus the 4-byte values when the lattice is materialised), 8-byte keys and
+    32 bytes of corner values per candidate, 28 bytes per vertex (position,
+    normal, cell key), 12 bytes per triangle."""
+    P3 = float(N + 1) ** 3
+    if phase == "cells":
+        return 2.0 * P3 / 8.0 + (0.0 if pruned else 4.0 * P3) + C * (8 + 32) + C * 32
+    if phase == "vertices":
+        return C * (8 + 32) + C * (8 + 24)
+    if phase == "vcompact":
+        return C * 8 + V * (24 + 28)
+    if phase == "rowscan":
+        return 8.0 * N * N
+    if phase == "quads":
+        return V * 8 + T * 12
+    return 0.0
+
+
+def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=None, e2e_steps=None):
+    """Device time of `steps` runs of one job (CUDA events on its stream, L2
+    flushed before each outside the events, per-kernel events on), then the
+    same job end to end through the C ABI: s2m_mesh_create + the reference's
+    TriangleMesh (positions, normals, triangle indices) copied to pinned host
+    memory + s2m_mesh_free."""
+    import torch
+    sp = stream.cuda_stream
+    mesh = s2m.mesh_device(sdf, state, sp)
+    info = mesh.info()
+    nverts, ntris = int(info.nverts), int(info.ntris)
+    for _ in range(warmup):
+        mesh.run_async(sp)
+        mesh.sync(sp)
+    mesh.set_profiling(True)
+    mesh.reset_profile()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    barrier()
+    if clocks:
+        clocks.start()
+    w0 = time.perf_counter()
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+        mesh.run_async(sp)
+        with torch.cuda.stream(stream):
+            evs[i][1].record(stream)
+        mesh.sync(sp)
+    barrier()
+    wall = time.perf_counter() - w0
+    clk = clocks.stop() if clocks else None
+    mesh.set_profiling(False)
+    dev_ms = sum(s.elapsed_time(e) for s, e in evs)
+    prof = mesh.profile()
+    ops = mesh.eval_ops()
+    launches = int(info.kernel_launches)
+    out = {"mesh": mesh, "info": info, "nverts": nverts, "ntris": ntris, "dev_ms": dev_ms, "prof": prof,
+           "eval_ops": ops, "wall": wall, "clocks": clk, "launches_per_step": launches}
+    # ---- end to end through the C ABI: create -> pinned host copy -> free ----
+    host_pos = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
+    host_nrm = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
+    host_tri = torch.empty(3 * ntris + 3, dtype=torch.int32, pin_memory=True)
+    p = state.params()
+    err = ctypes.create_string_buffer(4096)
+    e2e_ms = []
+    barrier()
+    for i in range(e2e_steps or steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        h = ctypes.c_void_p()
+        rc = L.s2m_mesh_create(sdf.handle, ctypes.byref(p), ctypes.c_void_p(sp), ctypes.byref(h), err, len(err))
+        if rc != 0:
+            raise RuntimeError(err.value.decode())
+        mi = s2m.MeshInfo()
+        L.s2m_mesh_get_info(h, ctypes.byref(mi))
+        if mi.nverts != nverts or mi.ntris != ntris:
+            raise RuntimeError("e2e mesh differs from the timed mesh")
+        rc = L.s2m_mesh_copy_to_host(h, host_pos.data_ptr(), host_nrm.data_ptr(), None,
+                                     host_tri.data_ptr(), ctypes.c_void_p(sp))
+        L.s2m_mesh_free(h)
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+        if rc != 0:
+            raise RuntimeError("copy to host failed")
+    barrier()
+    out["e2e_ms"] = sum(e2e_ms)
+    out["e2e_steps"] = len(e2e_ms)
+    out["d2h"] = nverts * (12 + 12) + ntris * 12
+    return out
+
+
+def kernels_table(prof, steps):
+    ms = prof["ms"]
+    tot = max(1e-9, sum(ms.values()))
+    return {k: {"launches_per_step": prof["launches"][k] // steps, "ms_per_step": ms[k] / steps,
+                "share": ms[k] / tot} for k in ms}
+
+
+def eval_roofline(s2m, sp, sdf, r, steps):
+    """Roofline of the evaluation phase: the SDF operations it executed (with tile
+    pruning: counted per tile by the tile pass; else the frontend's count per
+    point as written) against the measured FP32 or SFU issue rate."""
+    prof, ops = r["prof"], r["eval_ops"]
+    ms = prof["ms"]["eval_planes"]
+    n_eval = max(1, prof["launches"]["eval_planes"])
+    pts = max(1.0, ops["points"])
+    fp32_pp, sfu_pp = ops["fp32_ops"] / pts, ops["sfu_ops"] / pts
+    fp32_peak = s2m.measure_fp32_peak(sp)
+    sfu_peak = s2m.measure_sfu_peak(sp)
+    fp32_gops = fp32_pp * prof["eval_points"] / (ms * 1e-3) / 1e9
+    sfu_gops = sfu_pp * prof["eval_points"] / (ms * 1e-3) / 1e9
+    sfu_bound = sfu_pp / max(1e-9, sfu_peak) > fp32_pp / max(1e-9, fp32_peak)
+    return {"bound": "sfu" if sfu_bound else "fp32", "kernel": "s2m_tiles + s2m_evalpl_*" if ops["pruned"]
+            else "s2m_eval_*", "achieved": sfu_gops if sfu_bound else fp32_gops,
+            "peak": sfu_peak if sfu_bound else fp32_peak, "unit": "Gop/s",
+            "frac": (sfu_gops / sfu_peak) if sfu_bound else (fp32_gops / fp32_peak),
+            "fp32_frac": fp32_gops / fp32_peak, "sfu_frac": sfu_gops / sfu_peak,
+            "ms_per_launch": ms / n_eval,
+            "algorithmic": f"{fp32_pp:g} FP32 + {sfu_pp:g} SFU ops per lattice point x "
+                           f"{prof['eval_points'] / n_eval:.0f} points per launch",
+            "ops_source": ("tile pass: active segments' operations x points of each tile" if ops["pruned"]
+                           else "frontend op count per point as written (loops at their full trip count: an upper "
+                                "bound of what points that bail out early execute)"),
+            "peak_source": "measured in this run: s2m_fp32_probe (FP32 add/mul issue rate) and s2m_sfu_probe "
+                           "(MUFU rsqrt issue rate)",
+            "traffic": None}
+
+
+def dominant_roofline(s2m, sp, sdf, r, N, steps, pk, pk_kind, traffic_per_job=None):
+    """The phase with the most device time: evaluation against its op roofline,
+    any other phase against HBM with its algorithmic bytes."""
+    prof = r["prof"]
+    ms = prof["ms"]
+    dom = max(ms, key=lambda k: ms[k])
+    C, V, T = float(r["info"].candidate_cells), float(r["nverts"]), float(r["ntris"])
+    pruned = bool(r["eval_ops"]["pruned"])
+    if dom == "eval_planes":
+        roof = eval_roofline(s2m, sp, sdf, r, steps)
+    else:
+        nl = max(1, prof["launches"][dom])
+        per_launch_ms = ms[dom] / nl
+        launches_per_job = nl / steps
+        b = phase_bytes(dom, N, C, V, T, pruned) / launches_per_job
+        achieved = b / (per_launch_ms * 1e-3) / 1e9
+        tr = (traffic_per_job or {}).get(dom)
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "peak_source": pk_kind,
+                "algorithmic_bytes_per_launch": b, "ms_per_launch": per_launch_ms,
+                "algorithmic": "point bits 2 per lattice point, candidates 8 B key + 32 B corners written and "
+                               "corners read, vertices 28 B, triangles 12 B (per phase as it must move them)",
+                "traffic": tr / launches_per_job if tr else None,
+                "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the phase's launches in "
+                                  f"one job (profiles/{PHASE_PROFILE})" if tr else None}
+    roof["dominant_by_time"] = dom
+    # contouring as a whole (every phase after the evaluation), per 8(d)
+    cont_ms = sum(ms[k] for k in ms if k != "eval_planes") / steps
+    cont_b = sum(phase_bytes(k, N, C, V, T, pruned) for k in ("cells", "vertices", "vcompact", "rowscan", "quads"))
+    return roof, {"bound": "hbm", "ms_per_job": cont_ms, "bytes_per_job": cont_b,
+                  "achieved": cont_b / (cont_ms * 1e-3) / 1e9 if cont_ms > 0 else None, "peak": pk["hbm_gbs"],
+                  "unit": "GB/s", "frac": (cont_b / (cont_ms * 1e-3) / 1e9) / pk["hbm_gbs"] if cont_ms > 0 else None,
+                  "peak_source": pk_kind}
 
 
 def ours(a):
@@ -282,17 +450,16 @@ def ours(a):
     shader = s2m.Sdf3DShader.from_source(src, lang, "sdf")
     sdf = shader.compile()
     compile_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sdf_warm = shader.compile()  # the same source again: the on-disk module cache
+    compile_warm_s = time.perf_counter() - t0
+    sdf_warm.close()
     fp32_ops, sfu_ops = sdf.op_counts()
     prune_comb, _ = sdf.prune_info()
 
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
     state = s2m.AppState(resolution=N, bounds=bounds, qef=qef)
-    mesh = s2m.mesh_device(sdf, state, sp)
-    info = mesh.info()
-    nverts, ntris = int(info.nverts), int(info.ntris)
-    launches_per_step = int(info.kernel_launches)
-
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > 126 MB L2
 
     def barrier():
@@ -301,204 +468,73 @@ def ours(a):
             dist.barrier()
         torch.cuda.synchronize()
 
-    def timed(m, steps, warmup, clocks=None):
-        """Device time of `steps` runs of mesh m (CUDA events on its stream,
-        L2 flushed before each, outside the events), with per-kernel events."""
-        for _ in range(warmup):
-            m.run_async(sp)
-            m.sync(sp)
-        m.set_profiling(True)
-        m.reset_profile()
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        barrier()
-        if clocks:
-            clocks.start()
-        w0 = time.perf_counter()
-        for i in range(steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(float(i))
-                evs[i][0].record(stream)
-            m.run_async(sp)
-            with torch.cuda.stream(stream):
-                evs[i][1].record(stream)
-            m.sync(sp)
-        barrier()
-        w = time.perf_counter() - w0
-        clk = clocks.stop() if clocks else None
-        m.set_profiling(False)
-        return sum(s.elapsed_time(e) for s, e in evs), m.profile(), w, clk
-
-    # ---- device-timed steps -------------------------------------------------
-    tot_ms, prof, wall, clk = timed(mesh, a.steps, a.warmup, Clocks(local))
-    eval_ops = mesh.eval_ops()  # SDF operations the last run executed
-    tot_ms = reduce_max(tot_ms, dev)
+    # ---- device-timed steps, then end to end -------------------------------
+    r = time_job(s2m, L, sdf, state, stream, flush, a.steps, a.warmup, barrier, Clocks(local))
+    mesh, info, nverts, ntris = r["mesh"], r["info"], r["nverts"], r["ntris"]
+    tot_ms = reduce_max(r["dev_ms"], dev)
     voxels_step = float(N) ** 3
     value = voxels_step * a.steps * ws / (tot_ms * 1e-3) / 1e9
+    e2e_tot = reduce_max(r["e2e_ms"], dev)
+    e2e_value = voxels_step * r["e2e_steps"] * ws / (e2e_tot * 1e-3) / 1e9
 
     # ---- the same job without tile pruning (every operation at every point) --
     full_eval = None
     if prune_comb > 0 and not a.no_full_eval:
         plain = shader.compile(prune=False)
         fmesh = s2m.mesh_device(plain, state, sp)
-        f_ms, f_prof, _, _ = timed(fmesh, a.steps, max(1, min(a.warmup, 2)))
-        f_ms = reduce_max(f_ms, dev)
+        for _ in range(2):
+            fmesh.run_async(sp)
+            fmesh.sync(sp)
+        fmesh.set_profiling(True)
+        barrier()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for i in range(3):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+            fmesh.run_async(sp)
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+            fmesh.sync(sp)
+        f_ms = reduce_max(sum(s.elapsed_time(e) for s, e in evs), dev)
+        f_prof = fmesh.profile()
         f_mi = fmesh.info()
         if int(f_mi.nverts) != nverts or int(f_mi.ntris) != ntris:
             raise RuntimeError("the full evaluation's mesh differs from the pruned one")
-        f_ops = fmesh.eval_ops()
-        full_eval = {"value": voxels_step * a.steps * ws / (f_ms * 1e-3) / 1e9, "unit": UNIT,
-                     "ms_per_step": f_ms / a.steps, "eval_variant": plain.eval_variant()[0],
-                     "eval_ms_per_step": f_prof["ms"]["eval_planes"] / a.steps,
-                     "fp32_ops_per_step": f_ops["fp32_ops"], "sfu_ops_per_step": f_ops["sfu_ops"],
+        full_eval = {"value": voxels_step * 3 * ws / (f_ms * 1e-3) / 1e9, "unit": UNIT, "steps": 3,
+                     "ms_per_step": f_ms / 3, "eval_variant": plain.eval_variant()[0],
+                     "eval_ms_per_step": f_prof["ms"]["eval_planes"] / 3,
                      "mesh": "same vertex and triangle counts (bit-identity is a GPU test)"}
         fmesh.close()
         plain.close()
 
-    # ---- end to end through the C ABI: create -> pinned host copy -> free ----
-    host_pos = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
-    host_nrm = torch.empty(3 * nverts + 3, dtype=torch.float32, pin_memory=True)
-    host_tri = torch.empty(3 * ntris + 3, dtype=torch.int32, pin_memory=True)
-    p = state.params()
-    err = ctypes.create_string_buffer(4096)
-    e2e_ms = []
-    d2h = 0
-    barrier()
-    for i in range(a.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(i))
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        h = ctypes.c_void_p()
-        rc = L.s2m_mesh_create(sdf.handle, ctypes.byref(p), ctypes.c_void_p(sp), ctypes.byref(h), err, len(err))
-        if rc != 0:
-            raise RuntimeError(err.value.decode())
-        mi = s2m.MeshInfo()
-        L.s2m_mesh_get_info(h, ctypes.byref(mi))
-        if mi.nverts != nverts or mi.ntris != ntris:
-            raise RuntimeError("e2e mesh differs from the timed mesh")
-        # the reference's TriangleMesh: vertices (position, normal) and triangle indices
-        rc = L.s2m_mesh_copy_to_host(h, host_pos.data_ptr(), host_nrm.data_ptr(), None,
-                                     host_tri.data_ptr(), ctypes.c_void_p(sp))
-        L.s2m_mesh_free(h)
-        e2e_ms.append((time.perf_counter() - t) * 1e3)
-        if rc != 0:
-            raise RuntimeError("copy to host failed")
-        d2h = nverts * (12 + 12) + ntris * 12
-    barrier()
-    e2e_tot = sum(e2e_ms)
-    e2e_tot = reduce_max(e2e_tot, dev)
-    e2e_value = voxels_step * a.steps * ws / (e2e_tot * 1e-3) / 1e9
-
     if rank != 0:
+        mesh.close()
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel -------------------------------------
-    ms = prof["ms"]
-    dom = max(ms, key=lambda k: ms[k])
-    fp32_peak = s2m.measure_fp32_peak(sp)  # Gop/s, one FP32 add or mul per lane per cycle
     pk, pk_kind = peaks()
-    n_eval = max(1, prof["launches"]["eval_planes"])
-    roof = {}
-    kernels = {}
-    for k in ms:
-        nl = prof["launches"][k]
-        kernels[k] = {"launches_per_step": nl // a.steps, "ms_per_step": ms[k] / a.steps,
-                      "share": ms[k] / max(1e-9, sum(ms.values()))}
-    # ops the evaluation executes per point: the SDF as written; with a run-of-4 variant its run
-    # form (the x/y-only part once per 4 points); with tile pruning the operations of the segments
-    # the tile pass left active, counted per tile (eval_ops of the last run)
-    variant = sdf.eval_variant()[0]
-    per_point_scalar = (fp32_ops, sfu_ops)
-    pts_run = max(1.0, eval_ops["points"])
-    fp32_ops, sfu_ops = eval_ops["fp32_ops"] / pts_run, eval_ops["sfu_ops"] / pts_run
-    eval_gops = fp32_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
-    eval_sfu = sfu_ops * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
-    scalar_equiv_gops = per_point_scalar[0] * prof["eval_points"] / (ms["eval_planes"] * 1e-3) / 1e9
-    # contouring passes: bytes they must move per job (state them in one place)
-    V, T = nverts, ntris
-    contour_bytes = (V * (32 + 32)            # vcompact: candidate read + vertex write (pos, nrm, key)
-                     + 8.0 * N * N            # rowcnt + rowstart
-                     + V * 8 + T * 12)        # quads: key read + triangle indices
-    contour_ms = (ms["vcompact"] + ms["rowscan"] + ms["quads"]) / a.steps
-    contour_gbs = contour_bytes / (contour_ms * 1e-3) / 1e9 if contour_ms > 0 else None
-    if dom in ("eval_planes", "cells", "vertices"):
-        # evaluation: bound by FP32 issue or by the SFU, whichever the SDF's op mix hits first
-        sfu_peak = s2m.measure_sfu_peak(sp)
-        per_launch_ms = ms["eval_planes"] / n_eval
-        t_fp32 = fp32_ops / fp32_peak
-        t_sfu = sfu_ops / sfu_peak if sfu_peak > 0 else 0.0
-        tpp = eval_traffic_per_point(eval_ops["pruned"]) if a.workload == "csg64_1024" else None
-        traffic = tpp * prof["eval_points"] / n_eval if tpp else None
-        common = {"kernel": "s2m_tiles + s2m_evalp_*" if eval_ops["pruned"] else "s2m_eval_*",
-                  "traffic": traffic, "traffic_source": (
-                      "ncu dram__bytes_read.sum + dram__bytes_write.sum per lattice point from "
-                      f"profiles/{EVAL_PROFILE[eval_ops['pruned']]}, scaled by points per launch")
-                  if traffic else None,
-                  "tile_pruning": eval_ops["pruned"],
-                  "ms_per_launch": per_launch_ms,
-                  "algorithmic": f"{fp32_ops:g} FP32 + {sfu_ops:g} SFU ops per lattice point x "
-                                 f"{prof['eval_points'] / n_eval:.0f} points per launch",
-                  "fp32_gops": eval_gops, "fp32_peak_gops": fp32_peak, "sfu_gops": eval_sfu,
-                  "variant": variant, "per_point_ops_as_written": {"fp32": per_point_scalar[0], "sfu": per_point_scalar[1]},
-                  "per_point_ops_executed": {"fp32": fp32_ops, "sfu": sfu_ops},
-                  "executed_ops_source": ("tile pass: active segments' operations x points of each tile"
-                                          if eval_ops["pruned"] else "frontend op count x points"),
-                  "fp32_gops_as_written": scalar_equiv_gops,
-                  "sfu_peak_gops": sfu_peak, "dominant_by_time": dom,
-                  "peak_source": "measured in this run: s2m_fp32_probe (FP32 add/mul issue rate) and "
-                                 "s2m_sfu_probe (MUFU rsqrt issue rate); MEASURED_PEAKS.json has neither"}
-        jp = job_profile() if (eval_ops["pruned"] and a.workload == "csg64_1024" and N == 1024) else {}
-        if t_sfu > t_fp32:
-            roof = {"bound": "sfu", "achieved": eval_sfu, "peak": sfu_peak, "unit": "Gop/s",
-                    "frac": eval_sfu / sfu_peak, **common}
-        else:
-            roof = {"bound": "fp32", "achieved": eval_gops, "peak": fp32_peak, "unit": "Gop/s",
-                    "frac": eval_gops / fp32_peak, **common}
-        if jp.get("eval_inst_per_job"):
-            # Tile pruning leaves under one FP32 operation per lattice point: the phase is
-            # bound by instruction issue (interval code, tests of the activity bits, IEEE
-            # division and square-root sequences, point-bit stores), so its roofline is the
-            # issue rate: warp instructions per second against 4 per SM and clock.
-            sms = torch.cuda.get_device_properties(dev).multi_processor_count
-            mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
-            t_job = ms["eval_planes"] / a.steps * 1e-3
-            if mhz and t_job > 0:
-                issue_peak = sms * 4 * mhz * 1e6 / 1e9
-                achieved = jp["eval_inst_per_job"] / t_job / 1e9
-                fp32_view = {"bound": roof["bound"], "achieved": roof["achieved"], "peak": roof["peak"],
-                             "unit": roof["unit"], "frac": roof["frac"]}
-                roof = {**common, "bound": "issue", "achieved": achieved, "peak": issue_peak,
-                        "unit": "G warp-instructions/s", "frac": achieved / issue_peak,
-                        "kernel": "s2m_tiles_coarse + s2m_tiles + s2m_fill_decided + s2m_evalpl_* (one job)",
-                        "traffic": jp.get("eval_dram_bytes_per_job"),
-                        "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the phase's "
-                                          f"launches in one job (profiles/{JOB_PROFILE})",
-                        "instructions_per_job": jp["eval_inst_per_job"],
-                        "instructions_source": f"ncu smsp__inst_executed.sum of the phase's launches in one "
-                                               f"job (profiles/{JOB_PROFILE})",
-                        "achieved_unit_time": "CUDA events of the phase per step",
-                        "peak_source": f"{sms} SMs x 4 warp schedulers x {mhz:.0f} MHz (median SM clock "
-                                       "sampled during the timed steps)",
-                        "fp32_view": fp32_view}
-    else:
-        roof = {"bound": "hbm", "kernel": dom, "achieved": contour_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": (contour_gbs or 0) / pk["hbm_gbs"], "peak_source": pk_kind, "traffic": None}
-    contour = {"bound": "hbm", "achieved": contour_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
-               "frac": (contour_gbs or 0) / pk["hbm_gbs"], "peak_source": f"{pk_kind} (MEASURED_PEAKS hbm_gbs)",
-               "bytes_per_job": contour_bytes}
+    roof, contour = dominant_roofline(s2m, sp, sdf, r, N, a.steps, pk, pk_kind,
+                                      phase_traffic() if (a.workload == "csg64_1024" and N == 1024) else None)
+    eval_view = eval_roofline(s2m, sp, sdf, r, a.steps)
 
     cpu = None
     if not a.no_cpu_baseline:
         n = min(CPU_SAMPLE_SLICES if a.workload == "csg64_1024" else 4, N)
         z0 = max(0, min(CPU_Z0, N - n))
         dt, _ = cpu_sample(n, z0, N)
+        n1 = min(CPU_SAMPLE_SLICES_1T, N)
+        dt1, _ = cpu_sample(n1, z0, N, threads=1)
         cpu = {"value": n * N * N / dt / 1e9, "unit": UNIT, "cores": host_threads(), "kind": "port",
                "sample": f"CPU oracle (reference rule, binary32, OpenMP) on cell slices [{z0}, {z0 + n}) "
-                         f"of the {N}^3 job: {n * N * N} voxels in {dt:.2f} s"}
+                         f"of the {N}^3 job: {n * N * N} voxels in {dt:.2f} s",
+               "one_thread": {"value": n1 * N * N / dt1 / 1e9, "unit": UNIT, "cores": 1,
+                              "sample": f"cell slices [{z0}, {z0 + n1}): {n1 * N * N} voxels in {dt1:.2f} s"}}
 
+    eval_ops = r["eval_ops"]
+    pts_run = max(1.0, eval_ops["points"])
     metric = METRIC if a.workload == "csg64_1024" and N == 1024 else f"Gvoxels/s at {N}^3 ({a.workload})"
     line = {
         "metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
@@ -511,39 +547,80 @@ def ours(a):
                                  if qef else "reference rule in binary32, no FMA contraction, IEEE div/sqrt"),
                    "evaluation": ("tile-pruned (exact: bit-identical to every operation at every point)"
                                   if eval_ops["pruned"] else "every SDF operation at every lattice point")},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_tot / a.steps,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": r["d2h"],
+                "ms_per_step": e2e_tot / r["e2e_steps"],
                 "path": "s2m_mesh_create + s2m_mesh_copy_to_host (pinned: positions, normals, triangle indices, "
                         "the reference's TriangleMesh) + s2m_mesh_free; inputs are the "
                         "compiled SDF module and a 48-byte parameter block passed as kernel arguments"},
-        "full_evaluation": full_eval,
         "roofline": roof,
         "roofline_contouring": contour,
-        "kernels": kernels,
+        "roofline_evaluation": eval_view,
+        "kernels": kernels_table(r["prof"], a.steps),
+        "full_evaluation": full_eval,
         "cpu_baseline": cpu,
-        "clocks": clk,
-        "gpu_launches": launches_per_step * a.steps,
+        "clocks": r["clocks"],
+        "gpu_launches": r["launches_per_step"] * a.steps,
         "mesh": {"vertices": nverts, "triangles": ntris, "invalid_quads": int(info.invalid_quads),
                  "candidate_cells": int(info.candidate_cells), "slab_depth": int(info.slab_depth)},
-        "compile_s": compile_s,
+        "compile_s": {"cold": compile_s, "warm": compile_warm_s},
         "eval_variant": sdf.eval_variant()[0],
         "tile_pruning": {"combinators": prune_comb, "used": eval_ops["pruned"],
-                         "fp32_ops_per_point": fp32_ops, "sfu_ops_per_point": sfu_ops,
-                         "fp32_ops_per_point_as_written": per_point_scalar[0]},
-        "eval_variants": [{"name": n, "ns_per_point": t, "registers": r, "local_bytes": l}
-                          for n, t, r, l in sdf.eval_variants()],
+                         "fp32_ops_per_point": eval_ops["fp32_ops"] / pts_run,
+                         "sfu_ops_per_point": eval_ops["sfu_ops"] / pts_run,
+                         "fp32_ops_per_point_as_written": fp32_ops},
+        "eval_variants": [{"name": n, "ns_per_point": t, "registers": rg, "local_bytes": lb}
+                          for n, t, rg, lb in sdf.eval_variants()],
         "triangles_per_s": ntris * a.steps * ws / (tot_ms * 1e-3),
-        "wall_s_timed": wall,
+        "wall_s_timed": r["wall"],
     }
-    print(json.dumps(line), flush=True)
     mesh.close()
+    if ws == 1 and not a.no_extras and a.workload == "csg64_1024":
+        line["mandelbulb_2048"] = sub_mandelbulb(s2m, L, stream, flush, barrier, pk, pk_kind)
+        line["batch256"] = sub_batch(s2m)
+        line["serve"] = sub_serve(s2m)
+    print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
 
 
 # ---------------------------------------------------------------------------
-# Batching and serving workloads (spec changes (2) and (3)).
+# The other configurations, as compact sub-results of the headline line.
+
+
+def sub_mandelbulb(s2m, L, stream, flush, barrier, pk, pk_kind, N=2048, B=2.5, steps=3, warmup=3):
+    """Mandelbulb 2048^3 (bounds 2.5): the reference rule and precision mode, each
+    device-timed and end to end, with the evaluation's SFU / FP32 fractions."""
+    from sdf2mesh_gb300 import workloads
+    src, _ = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
+    t = time.perf_counter()
+    sdf = s2m.Sdf3DShader.from_source(src, s2m.LANG_GLSL, "sdf").compile()
+    out = {"sdf": MANDEL_DESC, "resolution": N, "unit": UNIT, "steps": steps, "warmup": warmup,
+           "compile_s": time.perf_counter() - t}
+    sp = stream.cuda_stream
+    for mode, qef in (("reference_rule", False), ("precision", True)):
+        clk = Clocks(0)
+        r = time_job(s2m, L, sdf, s2m.AppState(resolution=N, bounds=B, qef=qef), stream, flush, steps, warmup,
+                     barrier, clk, e2e_steps=2)
+        roof, _ = dominant_roofline(s2m, sp, sdf, r, N, steps, pk, pk_kind)
+        ev = eval_roofline(s2m, sp, sdf, r, steps)
+        out[mode] = {
+            "value": float(N) ** 3 * steps / (r["dev_ms"] * 1e-3) / 1e9, "ms_per_step": r["dev_ms"] / steps,
+            "e2e": {"value": float(N) ** 3 * r["e2e_steps"] / (r["e2e_ms"] * 1e-3) / 1e9,
+                    "ms_per_step": r["e2e_ms"] / r["e2e_steps"], "d2h_bytes_per_step": r["d2h"],
+                    "h2d_bytes_per_step": 0},
+            "roofline": {k: roof[k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac",
+                                              "dominant_by_time") if k in roof},
+            "evaluation": {"sfu_frac": ev["sfu_frac"], "fp32_frac": ev["fp32_frac"], "bound": ev["bound"],
+                           "ops_source": ev["ops_source"]},
+            "kernels": {k: round(v["ms_per_step"], 3) for k, v in kernels_table(r["prof"], steps).items()},
+            "launches_per_step": r["launches_per_step"],
+            "mesh": {"vertices": r["nverts"], "triangles": r["ntris"],
+                     "invalid_quads": int(r["info"].invalid_quads), "slab_depth": int(r["info"].slab_depth)},
+            "clocks": r["clocks"]}
+        r["mesh"].close()
+    sdf.close()
+    return out
 
 
 def batch_jobs(n=256, seed=4):
@@ -555,6 +632,14 @@ def batch_jobs(n=256, seed=4):
         N = workloads.log_uniform_resolution(rng)
         jobs.append((src, prog, N))
     return jobs
+
+
+def compile_all(s2m, sources):
+    """Compile distinct sources on all host threads (NVRTC releases the GIL)."""
+    uniq = list(dict.fromkeys(sources))
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(16, host_threads()))) as ex:
+        mods = dict(zip(uniq, ex.map(lambda s: s2m.Sdf3DShader.from_source(*s).compile(), uniq)))
+    return mods
 
 
 def plain_per_job(jobs, precompiled=None):
@@ -571,12 +656,10 @@ def plain_per_job(jobs, precompiled=None):
     return (time.perf_counter() - t) / len(jobs)
 
 
-def batch_arm(a):
+def sub_batch(s2m, steps=3, warmup=3):
+    """256 random CSG trees in one persistent launch, beside the plain per-job
+    pipeline on the same jobs with every module compiled (and tuned) beforehand."""
     import torch
-    torch.cuda.set_device(0)
-    import sdf2mesh_gb300 as s2m
-    from sdf2mesh_gb300 import build as b
-    b.build()
     jobs = batch_jobs()
     voxels = float(sum(N ** 3 for _, _, N in jobs))
 
@@ -591,60 +674,145 @@ def batch_arm(a):
         bt.close()
         return dt, ms, launches
 
-    for _ in range(a.warmup):
+    for _ in range(warmup):
         one()
     torch.cuda.synchronize()
     clocks = Clocks(0)
     clocks.start()
-    res = [one() for _ in range(a.steps)]
+    res = [one() for _ in range(steps)]
     clk = clocks.stop()
-    wall = sum(r[0] for r in res)
-    dev_ms = sum(r[1] for r in res)
-    launches = res[0][2]
-    # plain per-job pipeline on a bounded sample of the same jobs (first 32)
-    sample = jobs[:32]
-    plain_compile = plain_per_job(sample)
-    pre = [s2m.Sdf3DShader.from_source(src).compile() for src, _, _ in sample]
-    plain_per_job(sample[:4], pre[:4])  # warm (autotune, pools)
-    plain_mesh = plain_per_job(sample, pre)
-    sample_vox = float(sum(N ** 3 for _, _, N in sample)) / len(sample)
-    mps = len(jobs) * a.steps / wall
-    line = {
-        "metric": "meshes/s (batch of 256 CSG jobs)", "value": mps, "unit": "meshes/s", "n_gpus": 1,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": wall / a.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batch256", "jobs": len(jobs), "sdf": WORKLOADS["batch256"][3], "bounds": 2.0,
-                   "path": "s2m_batch_run: one persistent launch over a device work queue, CSG interpreter"},
-        "gvoxels_per_s": voxels * a.steps / wall / 1e9,
-        "device_ms_per_step": dev_ms / a.steps,
-        "gpu_launches": launches * a.steps,
-        "plain_per_job": {"meshes_per_s_with_compile": 1.0 / plain_compile, "meshes_per_s_precompiled": 1.0 / plain_mesh,
-                          "sample": "first 32 jobs of the same list, mean voxels per job %.3g vs %.3g in the batch"
-                                    % (sample_vox, voxels / len(jobs)),
-                          "speedup_vs_with_compile": mps / (1.0 / plain_compile),
-                          "speedup_vs_precompiled_same_mix": (voxels / len(jobs) / sample_vox) * mps / (1.0 / plain_mesh)},
-        "e2e": {"value": mps, "unit": "meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "clocks": clk,
-    }
-    print(json.dumps(line), flush=True)
+    wall = sum(x[0] for x in res)
+    mps = len(jobs) * steps / wall
+    mods = compile_all(s2m, [(src, s2m.LANG_WGSL, "sdf") for src, _, _ in jobs])
+    pre = [mods[(src, s2m.LANG_WGSL, "sdf")] for src, _, _ in jobs]
+    plain_per_job(jobs, pre)  # warm: autotuner, pools
+    plain_s = plain_per_job(jobs, pre)
+    for m in mods.values():
+        m.close()
+    return {"metric": "meshes/s (256 CSG jobs per step, one persistent launch)", "value": mps, "unit": "meshes/s",
+            "steps": steps, "warmup": warmup, "ms_per_step": wall / steps * 1e3,
+            "gvoxels_per_s": voxels * steps / wall / 1e9, "device_ms_per_step": sum(x[1] for x in res) / steps,
+            "launches_per_step": res[0][2],
+            "plain_per_job_precompiled": {"meshes_per_s": 1.0 / plain_s, "gvoxels_per_s": voxels / len(jobs) / plain_s
+                                          / 1e9, "path": "s2m_mesh_create + s2m_mesh_free per job, same 256 jobs, "
+                                                         "modules compiled and tuned beforehand"},
+            "speedup_vs_precompiled_same_mix": mps * plain_s, "clocks": clk}
 
 
-def serve_requests(rate, n, seed):
-    """Poisson arrivals at `rate` req/s: 90% random CSG trees, 10% Mandelbulbs."""
-    import math
+def serve_requests(n, seed=2000):
+    """Request contents: 90% random CSG trees, 10% Mandelbulbs, resolution
+    round(exp U(ln 64, ln 1024)); arrival gaps Exp(1) (scaled by 1/rate)."""
     from sdf2mesh_gb300 import workloads
     rng = workloads.SplitMix64(seed)
-    t = 0.0
     reqs = []
-    for i in range(n):
-        t += -math.log(1.0 - rng.u01()) / rate
+    t = 0.0
+    for _ in range(n):
+        t += -math.log(1.0 - rng.u01())
         N = int(round(math.exp(rng.uniform(math.log(64), math.log(1024)))))
         if rng.u01() < 0.1:
-            reqs.append((t, "mandelbulb", None, None, N))
+            reqs.append((t, "mandelbulb", None, N))
         else:
-            src, prog = workloads.random_tree(int(rng.next() % 100000))
-            reqs.append((t, "csg", src, prog, N))
+            src, _ = workloads.random_tree(int(rng.next() % 100000))
+            reqs.append((t, "csg", src, N))
     return reqs
+
+
+def run_serve_sweep(s2m, rates, nreq, reqs=None):
+    """Each rate: the same seeded requests, arrivals at `rate` req/s, through
+    (1) the continuous-batching server (requests as .sdf3d / GLSL text) and (2)
+    the plain per-job pipeline, one request at a time in arrival order, with
+    every module compiled beforehand (the same cache the server holds)."""
+    from sdf2mesh_gb300 import workloads
+    mb_src, _ = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
+    reqs = reqs or serve_requests(nreq)
+
+    def state(kind, N):
+        return s2m.AppState(resolution=N, bounds=2.5 if kind == "mandelbulb" else 2.0)
+
+    def key(kind, src):
+        return (mb_src, s2m.LANG_GLSL, "sdf") if kind == "mandelbulb" else (src, s2m.LANG_WGSL, "sdf")
+
+    mods = compile_all(s2m, [key(k, s) for _, k, s, _ in reqs])
+    pre = [mods[key(k, s)] for _, k, s, _ in reqs]
+    # warm both paths once: autotuner per module, pools, the server's source cache
+    server = s2m.Server(memory_budget_bytes=120 << 30, max_inflight=2, max_batch_jobs=64, keep_results=False)
+    for (_, kind, src, N) in reqs:
+        k = key(kind, src)
+        server.submit_source(k[0], state(kind, N), k[1], k[2])
+    server.drain(3600)
+    for k, (_, kind, src, N) in enumerate(reqs):
+        s2m.mesh_device(pre[k], state(kind, N)).close()
+
+    def paced(t0, rate):
+        for r in reqs:
+            d = t0 + r[0] / rate - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            yield r
+
+    table = []
+    for rate in rates:
+        server.reset_stats()
+        t0 = time.perf_counter()
+        for (_, kind, src, N) in paced(t0, rate):
+            k = key(kind, src)
+            server.submit_source(k[0], state(kind, N), k[1], k[2])
+        server.drain(3600)
+        sst = server.stats()
+        lat = []
+        t0 = time.perf_counter()
+        for i, (t, kind, src, N) in enumerate(paced(t0, rate)):
+            s2m.mesh_device(pre[i], state(kind, N)).close()
+            lat.append((time.perf_counter() - t0 - t / rate) * 1e3)
+        span = time.perf_counter() - t0
+        lat.sort()
+        plain = {"meshes_per_s": len(reqs) / span, "p50_ms": lat[len(lat) // 2],
+                 "p99_ms": lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]}
+        table.append({"rate": rate, "served": {"meshes_per_s": sst["meshes_per_s"], "p50_ms": sst["p50_ms"],
+                                               "p99_ms": sst["p99_ms"], "launches": sst["batches"],
+                                               "gvoxels_per_s": sst["gvoxels_per_s"],
+                                               "peak_gb": sst["peak_bytes"] / 1e9},
+                      "plain_per_job_precompiled": plain,
+                      "speedup_vs_precompiled": sst["meshes_per_s"] / plain["meshes_per_s"]})
+    server.close()
+    for m in mods.values():
+        m.close()
+    return table
+
+
+def sub_serve(s2m, rates=(10, 30, 100, 300, 1000, 2000), nreq=48):
+    table = run_serve_sweep(s2m, list(rates), nreq)
+    return {"metric": "served meshes/s and latency vs the plain per-job pipeline (same compiled modules)",
+            "requests_per_rate": nreq, "sdf": WORKLOADS["serve"][3],
+            "sweep": [{"rate": t["rate"], "meshes_per_s": t["served"]["meshes_per_s"],
+                       "p50_ms": t["served"]["p50_ms"], "p99_ms": t["served"]["p99_ms"],
+                       "plain_meshes_per_s": t["plain_per_job_precompiled"]["meshes_per_s"],
+                       "plain_p50_ms": t["plain_per_job_precompiled"]["p50_ms"],
+                       "plain_p99_ms": t["plain_per_job_precompiled"]["p99_ms"],
+                       "speedup_vs_precompiled": t["speedup_vs_precompiled"]} for t in table]}
+
+
+# ---------------------------------------------------------------------------
+# Stand-alone lines of the other configurations (--workload batch256 / serve).
+
+
+def batch_arm(a):
+    import torch
+    torch.cuda.set_device(0)
+    import sdf2mesh_gb300 as s2m
+    from sdf2mesh_gb300 import build as b
+    b.build()
+    r = sub_batch(s2m, steps=a.steps, warmup=a.warmup)
+    line = {"metric": r["metric"], "value": r["value"], "unit": "meshes/s", "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch256", "jobs": 256, "sdf": WORKLOADS["batch256"][3], "bounds": 2.0,
+                       "path": "s2m_batch_run: one persistent launch over a device work queue, CSG interpreter"},
+            "gpu_launches": r["launches_per_step"] * a.steps,
+            "e2e": {"value": r["value"], "unit": "meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            **{k: r[k] for k in ("gvoxels_per_s", "device_ms_per_step", "plain_per_job_precompiled",
+                                 "speedup_vs_precompiled_same_mix", "clocks")}}
+    print(json.dumps(line), flush=True)
 
 
 def serve_arm(a):
@@ -652,90 +820,21 @@ def serve_arm(a):
     torch.cuda.set_device(0)
     import sdf2mesh_gb300 as s2m
     from sdf2mesh_gb300 import build as b
-    from sdf2mesh_gb300 import workloads
     b.build()
-    mb_src, _ = workloads.mandelbulb(8.0, 8, 2.0, 0.003)
     rates = [10, 30, 100, 300, 1000, 2000]
-    nreq = 48
-    table = []
-
-    def paced(reqs, t0):
-        for r in reqs:
-            d = t0 + r[0] - time.perf_counter()
-            if d > 0:
-                time.sleep(d)
-            yield r
-
-    def state(kind, N):
-        return s2m.AppState(resolution=N, bounds=2.5 if kind == "mandelbulb" else 2.0)
-
-    for rate in rates:
-        reqs = serve_requests(rate, nreq, seed=rate)
-        # served: requests are source text (the plugin surface); CSG-shaped sources run on the
-        # batch interpreter, the Mandelbulb GLSL compiles once and is cached
-        server = s2m.Server(memory_budget_bytes=120 << 30, max_inflight=2, max_batch_jobs=64, keep_results=False)
-        t0 = time.perf_counter()
-        for (t, kind, src, prog, N) in paced(reqs, t0):
-            if kind == "csg":
-                server.submit_source(src, state(kind, N))
-            else:
-                server.submit_source(mb_src, state(kind, N), s2m.LANG_GLSL, "sdf")
-        server.drain(3600)
-        sst = server.stats()
-        server.close()
-
-        def plain(precompiled):
-            lat = []
-            t0 = time.perf_counter()
-            for k, (t, kind, src, prog, N) in enumerate(paced(reqs, t0)):
-                if precompiled is not None:
-                    sdf = precompiled[k]
-                elif kind == "csg":
-                    sdf = s2m.Sdf3DShader.from_source(src).compile()
-                else:
-                    sdf = s2m.Sdf3DShader.from_source(mb_src, s2m.LANG_GLSL, "sdf").compile()
-                m = s2m.mesh_device(sdf, state(kind, N))
-                m.close()
-                if precompiled is None:
-                    sdf.close()
-                lat.append((time.perf_counter() - t0 - t) * 1e3)
-            span = time.perf_counter() - t0
-            lat.sort()
-            return {"meshes_per_s": len(reqs) / span, "p50_ms": lat[len(lat) // 2],
-                    "p99_ms": lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]}
-
-        # plain per-job pipeline: one request at a time in arrival order, compiling its source
-        p_compile = plain(None)
-        # the same with every module compiled before the clock starts
-        mods = {}
-        pre = []
-        for (t, kind, src, prog, N) in reqs:
-            key = mb_src if kind == "mandelbulb" else src
-            if key not in mods:
-                mods[key] = (s2m.Sdf3DShader.from_source(mb_src, s2m.LANG_GLSL, "sdf") if kind == "mandelbulb"
-                             else s2m.Sdf3DShader.from_source(src)).compile()
-            pre.append(mods[key])
-        p_pre = plain(pre)
-        for m in mods.values():
-            m.close()
-        table.append({"rate": rate, "served": {"meshes_per_s": sst["meshes_per_s"], "p50_ms": sst["p50_ms"],
-                                               "p99_ms": sst["p99_ms"], "launches": sst["batches"],
-                                               "gvoxels_per_s": sst["gvoxels_per_s"],
-                                               "peak_gb": sst["peak_bytes"] / 1e9},
-                      "plain_per_job": p_compile, "plain_per_job_precompiled": p_pre,
-                      "speedup": sst["meshes_per_s"] / p_compile["meshes_per_s"],
-                      "speedup_vs_precompiled": sst["meshes_per_s"] / p_pre["meshes_per_s"]})
-        print(json.dumps(table[-1]), file=sys.stderr, flush=True)
+    table = run_serve_sweep(s2m, rates, 48)
+    for t in table:
+        print(json.dumps(t), file=sys.stderr, flush=True)
     top = table[-1]
     line = {
         "metric": "served meshes/s (Poisson stream, 2000 req/s offered)", "value": top["served"]["meshes_per_s"],
-        "unit": "meshes/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
+        "unit": "meshes/s", "n_gpus": 1, "steps": len(rates), "warmup": 1,
         "ms_per_step": 1e3 / max(1e-9, top["served"]["meshes_per_s"]), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "serve", "requests_per_rate": nreq, "rates": rates, "sdf": WORKLOADS["serve"][3],
+        "config": {"workload": "serve", "requests_per_rate": 48, "rates": rates, "sdf": WORKLOADS["serve"][3],
                    "served": "s2m_server_submit_source: requests are .sdf3d / GLSL text",
-                   "plain_per_job": "one request at a time in arrival order: NVRTC compile of its source + "
-                                    "s2m_mesh_create (and, beside it, the same with modules compiled beforehand)"},
+                   "plain_per_job": "one request at a time in arrival order: s2m_mesh_create with the modules "
+                                    "compiled beforehand"},
         "p50_ms": top["served"]["p50_ms"], "p99_ms": top["served"]["p99_ms"],
         "sweep": table,
         "e2e": {"value": top["served"]["meshes_per_s"], "unit": "meshes/s", "h2d_bytes_per_step": 0,

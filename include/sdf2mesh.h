@@ -4,8 +4,7 @@
  *
  * The reference (WilstonOreo/sdf2mesh) has no FFI: its boundary is a Rust
  * binary and a wgpu module.  Each entry point below names the reference code
- * it stands in for (paths relative to the reference sources); INTEGRATION.md
- * shows the binding a host program adds.
+ * it stands in for (paths relative to the reference sources).
  *
  * Conventions
  *   - Every function returns an s2m_status (0 = S2M_OK) unless noted; on
@@ -198,6 +197,14 @@ int s2m_mesh_sync(s2m_mesh *mesh, void *stream, char *err, size_t errlen);
 
 int s2m_mesh_get_info(const s2m_mesh *mesh, s2m_mesh_info *info);
 
+/* Device bytes s2m_mesh_create allocates for this job on its first attempt
+   (lattice ring, point bits, tile records, candidate, vertex and triangle
+   buffers), computed by the same job setup and buffer plan without
+   allocating anything.  A job whose initial capacities overflow is re-run
+   with the exact totals and then holds more.  No reference counterpart (the
+   reference's memory is two storage textures per slice, texture.rs:15-48). */
+int s2m_mesh_footprint(const s2m_sdf *sdf, const s2m_params *params, uint64_t *bytes);
+
 /* SDF operations the last run's lattice evaluation executed: points
    evaluated, FP32 and SFU operations in total (pruned runs: counted per tile
    by the tile pass; others: the per-point counts times the points).
@@ -227,6 +234,13 @@ typedef struct {
   double cells;            /* cells classified by kind-1 launches         */
 } s2m_profile;
 int s2m_mesh_set_profiling(s2m_mesh *mesh, int enable);
+/* Bound of every device-side wait of this mesh's runs (the look-back of the
+   ordered compactions), in seconds of the GPU's global timer; default 2 s.
+   A wait that runs out raises an error flag instead of spinning on: the run
+   finishes with S2M_E_TIMEOUT and the context stays usable.  The reference
+   has no device waits; it panics on a failed readback (main.rs:184, 196,
+   texture.rs:110). */
+int s2m_mesh_set_wait_limit(s2m_mesh *mesh, double seconds);
 /* Replay the mesh's launch sequence as a CUDA graph in s2m_mesh_run_async
    (captured on the first run on a stream; not while profiling). */
 int s2m_mesh_set_graph(s2m_mesh *mesh, int enable);
@@ -258,8 +272,11 @@ int s2m_mesh_reset_profile(s2m_mesh *mesh);
    overlaps (other host threads, or other streams without ordering between
    them) race; serialise them.  The first call on a device looks up the
    array's device address (cudaGetSymbolAddress) with that device current;
-   make that first call before any stream capture.  The call synchronises
-   `stream` (it reads the counts back). */
+   make that first call before any stream capture.  The address is kept for
+   the life of the process: after cudaDeviceReset (or a release of the
+   device's primary context) the array lives at a new address and the kept
+   one is stale, so do not call this entry point again in that process.  The
+   call synchronises `stream` (it reads the counts back). */
 #define S2M_NOALLOC_SCRATCH_BYTES (64u << 20)
 #define S2M_NOALLOC_MAX_RESOLUTION 256u
 typedef struct {
@@ -324,6 +341,11 @@ int s2m_batch_job_copy_to_host(const s2m_batch *b, uint32_t job, float *pos, flo
                                uint32_t *tris, void *stream);
 /* Device time of the last run's persistent launches, their count, jobs in the batch. */
 int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, uint32_t *njobs);
+/* Bounds of the persistent kernel's device waits, in seconds of the GPU's
+   global timer: a job stage waiting for the job's previous stage (default
+   30 s) and the look-back of its ordered compactions (default 2 s).  A wait
+   that runs out makes s2m_batch_run return S2M_E_TIMEOUT. */
+int s2m_batch_set_wait_limit(s2m_batch *b, double stage_seconds, double lookback_seconds);
 void s2m_batch_free(s2m_batch *b);
 
 /* ---- serving: continuous batching ---------------------------------------
@@ -368,12 +390,26 @@ int s2m_server_copy_to_host(s2m_server *s, uint64_t request_id, float *pos, floa
 int s2m_server_release(s2m_server *s, uint64_t request_id);
 int s2m_server_drain(s2m_server *s, double timeout_s);
 int s2m_server_get_stats(s2m_server *s, s2m_server_stats *out);
+/* Start a new measurement window (counts, latencies, span, peak bytes); the
+   compiled-source cache and resident results stay.  S2M_E_INVALID while
+   requests are still in flight (drain first). */
+int s2m_server_reset_stats(s2m_server *s);
 void s2m_server_free(s2m_server *s);
 
 /* ---- host writers (mesh.rs:8-141) -------------------------------------- */
 
 /* ASCII STL with Rust `{}` float text, facet normal (v2-v0) x (v1-v0). */
 int s2m_write_stl(const float *pos, const uint32_t *tris, uint64_t ntris, const char *path);
+/* Binary STL (80-byte header, u32 count, 50 bytes per facet: the same facet
+   normal (v2-v0) x (v1-v0) as the ASCII writer, lib.rs:181-185, three
+   vertices, a zero attribute word), written from all host threads.  Not in
+   the reference, whose ASCII STL runs to GBs at 2048^3 (README.md:96);
+   stands beside write_stl_to_file (mesh.rs:167-180).  S2M_E_IO also for more
+   than 2^32 - 1 triangles. */
+int s2m_write_stl_binary(const float *pos, const uint32_t *tris, uint64_t ntris, const char *path);
+/* s2m_mesh_write's binary STL form: the mesh copied to host memory, then
+   s2m_write_stl_binary. */
+int s2m_mesh_write_stl_binary(const s2m_mesh *mesh, const char *path, char *err, size_t errlen);
 /* ASCII PLY with per-vertex normals. */
 int s2m_write_ply(const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris,
                   uint64_t ntris, const char *path);

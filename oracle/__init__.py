@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libs2m_oracle.so")
 
-SPHERE, TORUS, CSG, MANDELBULB, TREE = 0, 1, 2, 3, 4
+SPHERE, TORUS, CSG, MANDELBULB, TREE, MARTIN_CUBE, P_KEY = 0, 1, 2, 3, 4, 5, 6
 F32, F64 = 0, 1
 FLAG_SLICE_LAG = 1
 FLAG_QEF = 2

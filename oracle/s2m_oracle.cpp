@@ -57,6 +57,13 @@ template <class T> T sdf_box(V3<T> p, V3<T> b) {
   V3<T> mq = {m_max(q.x, T(0)), m_max(q.y, T(0)), m_max(q.z, T(0))};
   return length3(mq) + m_min(m_max(q.x, m_max(q.y, q.z)), T(0));
 }
+// sdf3d_primitives.wgsl:13-17: d = abs(vec2(length(p.xz), p.y)) - vec2(r, h);
+// min(max(d.x, d.y), 0) + length(max(d, vec2f())).
+template <class T> T sdf_cylinder(V3<T> p, T h, T r) {
+  T dx = m_abs(length2(p.x, p.z)) - r;
+  T dy = m_abs(p.y) - h;
+  return m_min(m_max(dx, dy), T(0)) + length2(m_max(dx, T(0)), m_max(dy, T(0)));
+}
 // sdf3d_primitives.wgsl:19-25
 template <class T> T sdf_capsule(V3<T> p, V3<T> a, V3<T> b, T r) {
   V3<T> pa = p - a;
@@ -102,8 +109,110 @@ template <class T> struct Sdf {
       case ORACLE_SDF_CSG: return csg(p);
       case ORACLE_SDF_MANDELBULB: return mandelbulb(p);
       case ORACLE_SDF_TREE: return tree(p);
+      case ORACLE_SDF_MARTIN_CUBE: return martin_cube(p);
+      case ORACLE_SDF_P_KEY: return p_key(p);
     }
     return T(0);
+  }
+
+  // WGSL `const` declarations are abstract floats: a constant expression such
+  // as C*0.2 is folded in binary64 and rounded once when it meets an f32
+  // operand (the WGSL conversion rules as naga applies them).
+  static T ac(double v) { return T(v); }
+  static V3<T> sw_yxz(V3<T> p) { return {p.y, p.x, p.z}; }
+  static V3<T> sw_xzy(V3<T> p) { return {p.x, p.z, p.y}; }
+  static V3<T> sw_zyx(V3<T> p) { return {p.z, p.y, p.x}; }
+  static V3<T> v3(double a, double b, double c) { return {ac(a), ac(b), ac(c)}; }
+
+  // The letter arc of examples/martin_cube.sdf3d:9-27 and examples/p_key.sdf3d:9-27
+  // (the same function over a size constant S: C or KEY_SIZE).
+  static T letter_arc(V3<T> p, T ra, T rb, double S) {
+    V3<T> pp = sw_yxz(p);
+    pp.x = m_abs(pp.x - ac(S * 0.2));
+    pp.y = pp.y + ac(S * 0.25);
+    const V3<T> h = v3(0.0, S * 0.15, 0.0);
+    const V3<T> nh = {-h.x, -h.y, -h.z};
+    const V3<T> c = {clampT(pp.x, nh.x, h.x), clampT(pp.y, nh.y, h.y), clampT(pp.z, nh.z, h.z)};
+    const V3<T> q = pp - c;
+    const T scx = T(1), scy = T(0);
+    T k = T(0);
+    if (T(0) > scx * q.y) k = q.x * scx + q.y * scy;  // dot(q.xy, sc)
+    else k = length2(q.x, q.y);
+    return m_sqrt(dot3(q, q) + ra * ra - T(2) * ra * k) - rb;
+  }
+
+  // examples/martin_cube.sdf3d: a smooth cube with the letters M A R T I N
+  // carved into its faces (capsule segments and an arc).
+  static T mc_segment(V3<T> p, V3<T> a, V3<T> b) { return sdf_capsule(p, a, b, ac(0.12)); }  // :30-32
+  static T mc_letter_m(V3<T> p) {  // :34-47
+    const double C = 1.0;
+    V3<T> q = sw_yxz(p);
+    q.y = q.y * T(-1);
+    return m_min(m_min(mc_segment(q, v3(-C * 0.45, -C * 0.5, C), v3(-C * 0.45, C * 0.5, C)),
+                       mc_segment(q, v3(-C * 0.45, -C * 0.5, C), v3(0.0, 0.0, C))),
+                 m_min(mc_segment(q, v3(0.0, 0.0, C), v3(C * 0.45, -C * 0.5, C)),
+                       mc_segment(q, v3(C * 0.45, -C * 0.5, C), v3(C * 0.45, C * 0.5, C))));
+  }
+  static T mc_letter_a(V3<T> p) {  // :50-61
+    const double C = 1.0;
+    V3<T> q = sw_zyx(p);
+    q = V3<T>{-q.y, -q.x, q.z};
+    return m_min(m_min(mc_segment(q, v3(0.0, -C * 0.5, -C), v3(-C * 0.4, C * 0.5, -C)),
+                       mc_segment(q, v3(0.0, -C * 0.5, -C), v3(C * 0.4, C * 0.5, -C))),
+                 mc_segment(q, v3(-C * 0.2, C * 0.1, -C), v3(C * 0.2, C * 0.1, -C)));
+  }
+  static T mc_letter_r(V3<T> p) {  // :64-75
+    const double C = 1.0;
+    V3<T> q = p;
+    q.y = q.y * T(-1);
+    q.x = q.x - ac(C * 0.15);
+    return m_min(letter_arc(sw_xzy(q) - v3(0.0, 0.0, C), ac(C * 0.3), ac(0.12), C),
+                 m_min(mc_segment(q, v3(-C * 0.4, C, C * 0.5), v3(-C * 0.4, C, -C * 0.5)),
+                       mc_segment(q, v3(-C * 0.15, C, -C * 0.1), v3(C * 0.15, C, -C * 0.5))));
+  }
+  static T mc_letter_t(V3<T> p) {  // :79-84
+    const double C = 1.0;
+    return m_min(mc_segment(p, v3(C, 0.0, C * 0.5), v3(C, 0.0, -C * 0.5)),
+                 mc_segment(p, v3(C, -C * 0.4, C * 0.5), v3(C, C * 0.4, C * 0.5)));
+  }
+  static T mc_letter_i(V3<T> p) {  // :88-92
+    const double C = 1.0;
+    V3<T> q = sw_yxz(p);
+    q.x = q.x * T(-1);
+    return mc_segment(q, v3(-C, 0.0, C * 0.5), v3(-C, 0.0, -C * 0.5));
+  }
+  static T mc_letter_n(V3<T> p) {  // :96-107
+    const double C = 1.0;
+    V3<T> q = sw_xzy(p);
+    return m_min(mc_segment(q, v3(-C * 0.4, -C, C * 0.5), v3(-C * 0.4, -C, -C * 0.5)),
+                 m_min(mc_segment(q, v3(C * 0.4, -C, C * 0.5), v3(C * 0.4, -C, -C * 0.5)),
+                       mc_segment(q, v3(-C * 0.4, -C, -C * 0.5), v3(C * 0.4, -C, C * 0.5))));
+  }
+  static T martin_cube(V3<T> p) {  // :109-120
+    const T cube = op_smooth_intersection(sdf_box(p, v3(1.0, 1.0, 1.0)), sdf_sphere(p, ac(1.0 * 1.40)), ac(0.02));
+    const T letter = m_min(m_min(mc_letter_m(p), mc_letter_a(p)),
+                           m_min(m_min(mc_letter_r(p), mc_letter_t(p)), m_min(mc_letter_i(p), mc_letter_n(p))));
+    return op_smooth_subtraction(letter, cube, ac(0.02));
+  }
+
+  // examples/p_key.sdf3d: a key plate with a raised cylinder and the letter P.
+  static T pk_letter_p(V3<T> p) {  // :33-41
+    const double K = 15.0;
+    V3<T> q = p;
+    q.y = q.y * T(-1);
+    q.x = q.x - ac(K * 0.15);
+    return m_min(letter_arc(sw_xzy(q), ac(K * 0.3), ac(1.0), K),
+                 sdf_capsule(q, v3(-K * 0.4, 0.0, K * 0.5), v3(-K * 0.4, 0.0, -K * 0.5), ac(1.0)));
+  }
+  static T p_key(V3<T> p) {  // :43-53
+    const double K = 15.0, E = 2.0, H = 1.5, L = 1.0;
+    const V3<T> s = sw_xzy(p) * ac(2.5);
+    const V3<T> yzx = {p.y, p.z, p.x};
+    return op_smooth_subtraction(
+        pk_letter_p(s - v3(0.0, E * 2.5 + L, 0.0)),
+        op_smooth_union(sdf_box(p, v3(K, K, H)), sdf_cylinder(yzx - v3(0.0, (E + H) * 0.5, 0.0), ac(E - H), ac(K * 0.35)),
+                        ac(K * 0.15)),
+        ac(0.0));
   }
 
   // Large-scale CSG workload: max(box(p, vec3(b)) - round, -S(p)) unioned by
@@ -156,6 +265,7 @@ template <class T> struct Sdf {
   //   2 torus   cx cy cz R r         -> sdf3d_torus(p - c, vec2(R, r))
   //   3 capsule ax ay az bx by bz r  -> sdf3d_capsule(p, a, b, r)
   //   4 plane   nx ny nz d           -> dot(p, n) - d
+  //   5 cylinder cx cy cz h r        -> sdf3d_cylinder(p - c, h, r)   (oracle only)
   //  10 union   (a b -> min(a, b))
   //  11 subtract(a b -> max(a, -b))
   //  12 intersect (a b -> max(a, b))
@@ -174,6 +284,7 @@ template <class T> struct Sdf {
         case 2: stack[sp++] = sdf_torus(p - V3<T>{a[0], a[1], a[2]}, V2<T>{a[3], a[4]}); i += 5; break;
         case 3: stack[sp++] = sdf_capsule(p, V3<T>{a[0], a[1], a[2]}, V3<T>{a[3], a[4], a[5]}, a[6]); i += 7; break;
         case 4: stack[sp++] = dot3(p, V3<T>{a[0], a[1], a[2]}) - a[3]; i += 4; break;
+        case 5: stack[sp++] = sdf_cylinder(p - V3<T>{a[0], a[1], a[2]}, a[3], a[4]); i += 5; break;
         case 10: { T b = stack[--sp]; stack[sp - 1] = m_min(stack[sp - 1], b); } break;
         case 11: { T b = stack[--sp]; stack[sp - 1] = m_max(stack[sp - 1], -b); } break;
         case 12: { T b = stack[--sp]; stack[sp - 1] = m_max(stack[sp - 1], b); } break;

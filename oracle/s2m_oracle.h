@@ -45,7 +45,9 @@ enum {
   ORACLE_SDF_CSG = 2,        /* params: box_full, box_round, torus_R, torus_r, k,
                                 n, then n x (cx, cy, cz, radius)                    */
   ORACLE_SDF_MANDELBULB = 3, /* params: power, iterations, bailout, offset          */
-  ORACLE_SDF_TREE = 4        /* params: postfix CSG program, see s2m_oracle.cpp     */
+  ORACLE_SDF_TREE = 4,       /* params: postfix CSG program, see s2m_oracle.cpp     */
+  ORACLE_SDF_MARTIN_CUBE = 5,/* no params: the reference's examples/martin_cube.sdf3d */
+  ORACLE_SDF_P_KEY = 6       /* no params: the reference's examples/p_key.sdf3d       */
 };
 
 enum { ORACLE_F32 = 0, ORACLE_F64 = 1 };

@@ -146,16 +146,21 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_mesh_run_async": ([vp, vp], i),
             "s2m_mesh_sync": ([vp, vp, ctypes.c_char_p, sz], i),
             "s2m_mesh_get_info": ([vp, ctypes.POINTER(MeshInfo)], i),
+            "s2m_mesh_footprint": ([vp, ctypes.POINTER(Params), ctypes.POINTER(u64)], i),
             "s2m_mesh_copy_to_host": ([vp, vp, vp, vp, vp, vp], i),
             "s2m_mesh_write": ([vp, ctypes.c_char_p, ctypes.c_char_p, sz], i),
             "s2m_mesh_free": ([vp], None),
             "s2m_write_stl": ([vp, vp, u64, ctypes.c_char_p], i),
+            "s2m_write_stl_binary": ([vp, vp, u64, ctypes.c_char_p], i),
+            "s2m_mesh_write_stl_binary": ([vp, ctypes.c_char_p, ctypes.c_char_p, sz], i),
             "s2m_write_ply": ([vp, vp, u64, vp, u64, ctypes.c_char_p], i),
             "s2m_measure_fp32_peak": ([dp, vp], i),
             "s2m_mesh_noalloc": ([vp, ctypes.POINTER(Params), ctypes.POINTER(NoallocMesh), vp, ctypes.c_char_p, sz],
                                  i),
             "s2m_mesh_set_profiling": ([vp, i], i),
             "s2m_mesh_set_graph": ([vp, i], i),
+            "s2m_mesh_set_wait_limit": ([vp, ctypes.c_double], i),
+            "s2m_batch_set_wait_limit": ([vp, ctypes.c_double, ctypes.c_double], i),
             "s2m_measure_sfu_peak": ([dp, vp], i),
             "s2m_csg_from_source": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(u32),
                                      ctypes.c_char_p, sz], i),
@@ -179,6 +184,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_server_release": ([vp, u64], i),
             "s2m_server_drain": ([vp, ctypes.c_double], i),
             "s2m_server_get_stats": ([vp, ctypes.POINTER(ServerStats)], i),
+            "s2m_server_reset_stats": ([vp], i),
             "s2m_server_free": ([vp], None),
             "s2m_mesh_get_profile": ([vp, ctypes.POINTER(Profile)], i),
             "s2m_mesh_reset_profile": ([vp], i),
@@ -434,6 +440,10 @@ class DeviceMesh:
         """Replay the pipeline as a CUDA graph in run_async."""
         _check(load_library().s2m_mesh_set_graph(self._h, 1 if enable else 0), None, "graph")
 
+    def set_wait_limit(self, seconds: float) -> None:
+        """Bound of each device-side wait of this mesh's runs (default 2 s)."""
+        _check(load_library().s2m_mesh_set_wait_limit(self._h, float(seconds)), None, "wait limit")
+
     def set_profiling(self, enable: bool = True) -> None:
         """Record CUDA events around every kernel of later runs."""
         _check(load_library().s2m_mesh_set_profiling(self._h, 1 if enable else 0), None, "profiling")
@@ -509,6 +519,13 @@ class TriangleMesh:
         _check(load_library().s2m_write_stl(pos.ctypes.data, tris.ctypes.data, len(tris), os.fspath(path).encode()),
                None, f"write {path}")
 
+    def write_stl_binary_to_file(self, path: str) -> None:
+        """Binary STL: same facets and normals as the ASCII writer, 50 bytes each."""
+        pos = np.ascontiguousarray(self.positions, np.float32)
+        tris = np.ascontiguousarray(self.triangle_indices, np.uint32)
+        _check(load_library().s2m_write_stl_binary(pos.ctypes.data, tris.ctypes.data, len(tris),
+                                                   os.fspath(path).encode()), None, f"write {path}")
+
     def write_ply_to_file(self, path: str) -> None:
         pos = np.ascontiguousarray(self.positions, np.float32)
         nrm = np.ascontiguousarray(self.normals, np.float32)
@@ -551,6 +568,11 @@ class Batch:
 
     def footprint(self, job: int) -> int:
         return int(load_library().s2m_batch_job_footprint(self._h, job))
+
+    def set_wait_limit(self, stage_seconds: float, lookback_seconds: float = 2.0) -> None:
+        """Bounds of the persistent kernel's device waits (defaults 30 s and 2 s)."""
+        _check(load_library().s2m_batch_set_wait_limit(self._h, float(stage_seconds), float(lookback_seconds)),
+               None, "wait limit")
 
     def run(self, stream: int = 0) -> None:
         err = _errbuf()
@@ -661,6 +683,10 @@ class Server:
         load_library().s2m_server_get_stats(self._h, ctypes.byref(st))
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
 
+    def reset_stats(self) -> None:
+        """A new measurement window (after drain); compiled sources stay cached."""
+        _check(load_library().s2m_server_reset_stats(self._h), None, "reset stats")
+
     def close(self):
         if self._h:
             load_library().s2m_server_free(self._h)
@@ -683,6 +709,15 @@ def mesh_device(sdf, state: AppState, stream: int = 0) -> DeviceMesh:
     rc = L.s2m_mesh_create(compiled.handle, ctypes.byref(p), ctypes.c_void_p(stream), ctypes.byref(h), err, len(err))
     _check(rc, err, "mesh")
     return DeviceMesh(h, compiled)
+
+
+def mesh_footprint(sdf, state: AppState) -> int:
+    """Device bytes s2m_mesh_create allocates for this job (its first attempt)."""
+    compiled = sdf.compile() if isinstance(sdf, Sdf3DShader) else sdf
+    p = state.params()
+    b = ctypes.c_uint64()
+    _check(load_library().s2m_mesh_footprint(compiled.handle, ctypes.byref(p), ctypes.byref(b)), None, "footprint")
+    return int(b.value)
 
 
 def generate(sdf, state: AppState | None = None, stream: int = 0) -> TriangleMesh:

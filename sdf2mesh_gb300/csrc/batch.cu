@@ -373,7 +373,7 @@ __device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned ti
   const long long ncells = (long long)J.nzc * J.job.N * J.job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
   s2_cell_tile<true>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, tile, ntiles, ncells, 0, 0ull,
-                     J.cand.base + 1);
+                     J.cand.base + 1, J.mesh.wait_ns);
 }
 
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
@@ -420,9 +420,16 @@ __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
   }
 }
 
+// Test hook of the batch kernel (the `hold` argument): job 0's row-scan items
+// never count as done, so its quad items' stage wait runs out (a flag that
+// nothing sets); they then skip their work and the launch reports
+// S2_ERR_BATCH_WAIT.
+#define S2_HOLD_BATCH_ROWS 0x2u
+
 __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__restrict__ jobs,
                                                         const S2BatchSeg *__restrict__ segs, int nsegs,
-                                                        unsigned long long total, S2BatchCtl *ctl) {
+                                                        unsigned long long total, S2BatchCtl *ctl,
+                                                        unsigned long long stage_wait_ns, unsigned hold) {
   __shared__ unsigned long long s_ticket;
   __shared__ int s_ok;
   const unsigned tid = threadIdx.x;
@@ -443,18 +450,17 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
     if (tid == 0) {
       int ok = 1;
       if (sg.stage > 0) {
-        // wait for every item of the previous stage of this job (lower tickets)
-        // bounded by time: 30 s of the GPU's global timer
+        // wait for every item of the previous stage of this job (lower tickets),
+        // bounded by time: stage_wait_ns of the GPU's global timer
         const unsigned need = J.nitems[sg.stage - 1];
         unsigned long long t0 = 0;
         for (unsigned spins = 0;; ++spins) {
           unsigned d;
           asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(d) : "l"(J.done + sg.stage - 1) : "memory");
           if (d >= need) break;
-          unsigned long long now;
-          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+          const unsigned long long now = s2_globaltimer();
           if (spins == 0) t0 = now;
-          if (now - t0 > 30000000000ull) {
+          if (now - t0 > stage_wait_ns) {
             atomicOr(&ctl->err, S2_ERR_BATCH_WAIT);
             ok = 0;
             break;
@@ -476,7 +482,7 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
       }
     }
     __syncthreads();
-    if (tid == 0) {
+    if (tid == 0 && !((hold & S2_HOLD_BATCH_ROWS) && sg.job == 0 && sg.stage == S2_ST_ROWS)) {
       __threadfence();
       atomicAdd(J.done + sg.stage, 1u);
     }
@@ -625,9 +631,19 @@ struct s2m_batch {
   int blocks_per_sm = 0;
   double last_ms = 0;
   uint64_t last_launches = 0;
+  // bounds of the persistent kernel's device waits (GPU global timer ns): a
+  // stage waiting for its job's previous stage, and the look-backs
+  unsigned long long stage_wait_ns = 30000000000ull;
+  unsigned long long lookback_wait_ns = S2_WAIT_NS;
 };
 
 namespace {
+
+// S2M_TEST_HOLD (tests only): S2_HOLD_* bits of the kernels' test hooks.
+unsigned test_hold() {
+  const char *e = std::getenv("S2M_TEST_HOLD");
+  return e ? unsigned(std::strtoul(e, nullptr, 0)) : 0u;
+}
 
 // One persistent launch in flight.
 struct Wave {
@@ -733,6 +749,7 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
     J.cand.cap = h.cand_cap;
     J.mesh.vcap = h.vcap;
     J.mesh.tcap = h.tcap;
+    J.mesh.wait_ns = b->lookback_wait_ns;
     J.scan_tiles = unsigned(scan_tiles);
     std::memcpy(progs.data() + poff, h.prog.data(), h.prog.size() * 4);
     J.prog = reinterpret_cast<const float *>(arena + ztot + ctl_bytes + dtot + poff);
@@ -795,7 +812,8 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
   S2B_CUDA(cudaEventCreate(&e0));
   S2B_CUDA(cudaEventCreate(&e1));
   S2B_CUDA(cudaEventRecord(e0, st));
-  s2m_batch_kernel<<<grid, 256, 0, st>>>(d_jobs, d_segs, int(segs.size()), ticket, d_ctl);
+  s2m_batch_kernel<<<grid, 256, 0, st>>>(d_jobs, d_segs, int(segs.size()), ticket, d_ctl, b->stage_wait_ns,
+                                         test_hold());
   S2B_CUDA(cudaGetLastError());
   S2B_CUDA(cudaEventRecord(e1, st));
   s2m_batch_results<<<unsigned((idx.size() + 127) / 128), 128, 0, st>>>(d_jobs, int(idx.size()), d_res);
@@ -1032,6 +1050,14 @@ int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, u
   return S2M_OK;
 }
 
+int s2m_batch_set_wait_limit(s2m_batch *b, double stage_seconds, double lookback_seconds) {
+  if (!b || !(stage_seconds > 0.0) || !(lookback_seconds > 0.0) || stage_seconds > 3600.0 || lookback_seconds > 3600.0)
+    return S2M_E_INVALID;
+  b->stage_wait_ns = (unsigned long long)(stage_seconds * 1e9);
+  b->lookback_wait_ns = (unsigned long long)(lookback_seconds * 1e9);
+  return S2M_OK;
+}
+
 void s2m_batch_free(s2m_batch *b) {
   if (!b) return;
   for (void *a : b->arenas) cudaFreeAsync(a, nullptr);
@@ -1096,28 +1122,20 @@ struct SWave {
   cudaStream_t st = nullptr;
 };
 
-// Device bytes of one per-job mesh (s2m_mesh_create), for admission.  The
-// lattice ring follows the slab depth that setup_job picks: the given one,
-// an L2-sized ring (<= 65 planes) for full evaluation, or slabs of equal
-// depth from a ring of up to 4 GB for an SDF with a tile form; the point
-// bits are 3 bits per point of the ring.
+}  // namespace
+
+namespace s2m {
+// Device bytes s2m_mesh_create allocates for a job (runtime.cu): its own job
+// setup and buffer plan, so admission follows the resolution rounding, the
+// slab depth, the tile-pruning buffers and caller-set capacities.
+uint64_t mesh_job_footprint(const s2m_sdf *sdf, const s2m_params &params);
+}  // namespace s2m
+
+namespace {
+// Admission footprint of a compiled-SDF request: the job's buffer plan plus
+// 64 MiB for the autotuner's first run and pool rounding.
 uint64_t sdf_job_footprint(const s2m_sdf *sdf, const s2m_params &p) {
-  const uint64_t N = p.resolution, n2 = N * N, P = N + 1;
-  const uint64_t plane = P * ((N + 32) / 32 * 32) * 4;
-  int words = 0;
-  const bool tile_form = s2m_sdf_prune_info(sdf, nullptr, &words) == S2M_OK && words > 0;
-  uint64_t planes;
-  if (p.slab_depth) {
-    planes = std::min<uint64_t>(p.slab_depth, N) + 1;
-  } else if (tile_form) {
-    const uint64_t dmax = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(4.0e9 / double(plane)), 1000000000ull) - 1);
-    const uint64_t ns = (std::max<uint64_t>(N, 1) + dmax - 1) / dmax;
-    planes = (N + ns - 1) / ns + 1;
-  } else {
-    planes = std::min<uint64_t>(65, std::max<uint64_t>(2, 50000000ull / plane));
-  }
-  const uint64_t ring = planes * plane, bits = 3 * planes * P * ((P + 31) / 32) * 4;
-  return ring + bits + n2 * (8 * 64 + 6 * 32 + 12 * 12 + 8 + 8) + (64u << 20);
+  return s2m::mesh_job_footprint(sdf, p) + (64ull << 20);
 }
 
 }  // namespace
@@ -1526,6 +1544,18 @@ int s2m_server_get_stats(s2m_server *s, s2m_server_stats *out) {
   out->span_s = span;
   out->meshes_per_s = span > 0 ? double(s->completed) / span : 0;
   out->gvoxels_per_s = span > 0 ? s->voxels_done / span / 1e9 : 0;
+  return S2M_OK;
+}
+
+int s2m_server_reset_stats(s2m_server *s) {
+  if (!s) return S2M_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->completed + s->failed < s->submitted) return S2M_E_INVALID;  // drain first
+  s->submitted = s->completed = s->failed = s->batches = 0;
+  s->peak_bytes = s->used_bytes;
+  s->first_submit = s->last_done = 0;
+  s->voxels_done = 0;
+  s->latencies_ms.clear();
   return S2M_OK;
 }
 

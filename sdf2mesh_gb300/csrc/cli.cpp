@@ -4,7 +4,7 @@
 //
 //   sdf2mesh (--sdf|-i FILE.sdf3d | --glsl FILE [--glsl-sdf NAME]) --mesh|-0 OUT.{stl,ply}
 //            [--resolution|-r N (256)] [--bounds|-b B (2.0)] [--debug-wgsl FILE]
-//            [--debug-cuda FILE] [--exact-resolution] [--no-slice-lag] [--fmad]
+//            [--debug-cuda FILE] [--exact-resolution] [--no-slice-lag] [--fmad] [--binary-stl]
 //
 // As in the reference, a resolution that is not a power of two is rounded up
 // (main.rs:141-148) and slices are emitted with the reference's one-slice lag
@@ -51,6 +51,7 @@ void usage() {
                "      --exact-resolution         Do not round the resolution to a power of two\n"
                "      --no-slice-lag             Emit every slice at its own index\n"
                "      --fmad                     Allow FMA contraction in the SDF (faster, not bit-exact)\n"
+               "      --binary-stl               Write the STL in binary form (50 bytes per facet)\n"
                "  -h, --help                     Print help\n");
 }
 
@@ -70,7 +71,7 @@ int main(int argc, char **argv) {
       shadertoy_sdf = "sdf";
   unsigned long resolution = 256;
   double bounds = 2.0;
-  bool exact_res = false, no_lag = false, fmad = false;
+  bool exact_res = false, no_lag = false, fmad = false, binary_stl = false;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
     std::string v;
@@ -137,6 +138,8 @@ int main(int argc, char **argv) {
       no_lag = true;
     } else if (a == "--fmad") {
       fmad = true;
+    } else if (a == "--binary-stl") {
+      binary_stl = true;
     } else {
       std::fprintf(stderr, "error: unexpected argument '%s'\n", a.c_str());
       usage();
@@ -228,7 +231,8 @@ int main(int argc, char **argv) {
   std::snprintf(line, sizeof line, "Meshed %u^3 cells in %.3f s (%.2f Gvoxels/s)", info.resolution, secs,
                 double(info.cells) / secs / 1e9);
   log("INFO", line);
-  rc = s2m_mesh_write(m, mesh.c_str(), err, sizeof err);
+  rc = binary_stl ? s2m_mesh_write_stl_binary(m, mesh.c_str(), err, sizeof err)
+                  : s2m_mesh_write(m, mesh.c_str(), err, sizeof err);
   int status = 0;
   if (rc != S2M_OK) {
     log("ERROR", std::string("Could not write mesh to ") + mesh + ": " + err);

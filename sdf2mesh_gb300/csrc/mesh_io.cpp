@@ -5,7 +5,11 @@
 // threads and written in order.
 #include "mesh_io.h"
 
+#include <fcntl.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
 #include <charconv>
 #include <cmath>
 #include <cstdio>
@@ -112,6 +116,74 @@ bool write_stl(const char *path, const float *pos, const uint32_t *tris, uint64_
   });
   ok = ok && std::fputs("endsolid\n", fp) >= 0;
   return std::fclose(fp) == 0 && ok;
+}
+
+// Binary STL: an 80-byte header, the triangle count (u32), then 50 bytes per
+// triangle -- the facet normal (v2 - v0) x (v1 - v0) as in lib.rs:181-185,
+// the three vertices (12 little-endian f32) and a zero attribute word.  The
+// file size is known up front, so every host thread formats its own ranges
+// of triangles and writes them at their offsets (pwrite); nothing waits on
+// another thread's text.
+bool write_stl_binary(const char *path, const float *pos, const uint32_t *tris, uint64_t ntris) {
+  if (ntris > 0xFFFFFFFFull) return false;
+  const int fd = ::open(path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  if (fd < 0) return false;
+  unsigned char head[84] = {0};
+  static const char kTitle[] = "binary STL, sdf2mesh_gb300 dual contouring";
+  std::memcpy(head, kTitle, sizeof kTitle - 1);
+  const uint32_t n32 = uint32_t(ntris);
+  for (int b = 0; b < 4; ++b) head[80 + b] = (unsigned char)((n32 >> (8 * b)) & 0xffu);
+  bool ok = ::pwrite(fd, head, sizeof head, 0) == ssize_t(sizeof head);
+  const uint64_t chunk = 1u << 16;
+  const uint64_t nchunks = (ntris + chunk - 1) / chunk;
+  std::atomic<uint64_t> next{0};
+  std::atomic<bool> good{ok};
+  auto put_f32 = [](unsigned char *o, float v) {
+    uint32_t u;
+    std::memcpy(&u, &v, 4);
+    o[0] = (unsigned char)(u & 0xffu);
+    o[1] = (unsigned char)((u >> 8) & 0xffu);
+    o[2] = (unsigned char)((u >> 16) & 0xffu);
+    o[3] = (unsigned char)(u >> 24);
+  };
+  auto worker = [&] {
+    std::vector<unsigned char> buf(size_t(chunk) * 50);
+    for (;;) {
+      const uint64_t c = next.fetch_add(1);
+      if (c >= nchunks || !good.load()) return;
+      const uint64_t a = c * chunk, b = std::min(ntris, a + chunk);
+      unsigned char *o = buf.data();
+      for (uint64_t t = a; t < b; ++t, o += 50) {
+        const float *v0 = pos + 3 * size_t(tris[3 * t]);
+        const float *v1 = pos + 3 * size_t(tris[3 * t + 1]);
+        const float *v2 = pos + 3 * size_t(tris[3 * t + 2]);
+        const float ux = v2[0] - v0[0], uy = v2[1] - v0[1], uz = v2[2] - v0[2];
+        const float wx = v1[0] - v0[0], wy = v1[1] - v0[1], wz = v1[2] - v0[2];
+        const float n[3] = {uy * wz - uz * wy, uz * wx - ux * wz, ux * wy - uy * wx};
+        for (int k = 0; k < 3; ++k) put_f32(o + 4 * k, n[k]);
+        const float *vs[3] = {v0, v1, v2};
+        for (int v = 0; v < 3; ++v)
+          for (int k = 0; k < 3; ++k) put_f32(o + 12 + 12 * v + 4 * k, vs[v][k]);
+        o[48] = o[49] = 0;
+      }
+      const size_t bytes = size_t(b - a) * 50;
+      size_t done = 0;
+      while (done < bytes) {
+        const ssize_t w = ::pwrite(fd, buf.data() + done, bytes - done, off_t(84 + 50 * a + done));
+        if (w <= 0) {
+          good = false;
+          return;
+        }
+        done += size_t(w);
+      }
+    }
+  };
+  const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (unsigned i = 0; i < std::min<uint64_t>(nt, std::max<uint64_t>(1, nchunks)); ++i) th.emplace_back(worker);
+  for (auto &t : th) t.join();
+  ok = good.load();
+  return ::close(fd) == 0 && ok;
 }
 
 bool write_ply(const char *path, const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris,

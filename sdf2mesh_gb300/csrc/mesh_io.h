@@ -9,6 +9,9 @@ namespace s2m {
 // Rust `{}` Display of an f32 into buf (>= 64 bytes); returns the length.
 int format_f32(float v, char *buf);
 bool write_stl(const char *path, const float *pos, const uint32_t *tris, uint64_t ntris);
+// Binary STL (not in the reference, whose ASCII files run to GBs at 2048^3,
+// README.md:96): same facets and normals, written from all host threads.
+bool write_stl_binary(const char *path, const float *pos, const uint32_t *tris, uint64_t ntris);
 bool write_ply(const char *path, const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris,
                uint64_t ntris);
 // mesh.rs:182-196: "STL" / "PLY" by case-insensitive extension.

@@ -186,6 +186,8 @@ struct s2m_mesh {
   std::vector<double> ev_units;
   size_t ev_used = 0;
   s2m_profile prof{};
+  // bound of each device wait of a run (look-backs), GPU global timer ns
+  unsigned long long wait_ns = S2_WAIT_NS;
   // CUDA graph of the whole pipeline, replayed by s2m_mesh_run_async
   bool use_graph = false;
   cudaGraphExec_t graph = nullptr;
@@ -550,10 +552,21 @@ void drop_graph(s2m_mesh *m) {
   m->graph = nullptr;
 }
 
-int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long vcap, unsigned long long tcap,
-                  char *err, size_t errlen) {
-  drop_graph(m);
-  free_buffers(m);
+// Bytes of every device buffer of a job, in allocation order.  plan_buffers
+// fixes the capacities and layouts on the mesh; alloc_buffers allocates
+// exactly this plan, and the server's admission sums it (mesh_job_footprint),
+// so the two cannot drift apart.
+struct BufPlan {
+  size_t ring, slab_ctrl, pt_bits, offx, cell_words, tile_cnt, prune, cand_key, cand_val, cand_pos, cand_nrm,
+      cand_base, cand_status, vt, pos, nrm, key, tris, rowcnt, rowstart, scan_status, jobctl;
+  size_t total() const {
+    return ring + slab_ctrl + pt_bits + offx + cell_words + tile_cnt + prune + cand_key + cand_val + cand_pos +
+           cand_nrm + cand_base + cand_status + vt + pos + nrm + key + tris + rowcnt + rowstart + scan_status +
+           jobctl;
+  }
+};
+
+BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long vcap, unsigned long long tcap) {
   const S2Job &j = m->job;
   const unsigned long long N = (unsigned long long)m->N;
   m->cand_cap = std::max<unsigned long long>(1024, std::min(cand_cap, N * N * N));
@@ -564,31 +577,24 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   m->slab_ctrl_words = m->cell_tiles + 1;
   m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   m->quad_tiles = (m->vcap + S2_Q_TILE - 1) / S2_Q_TILE;
-  size_t ring_floats = size_t(j.ring) * size_t(j.plane);
-  cudaStream_t st = m->stream;
-  S2_CUDA(cudaMallocAsync(&m->ring, ring_floats * sizeof(float), st));
-  S2_CUDA(cudaMallocAsync(&m->slab_ctrl, m->slab_ctrl_words * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->pt_bits, 3 * pt_bits_words(m) * 4, st));
-  // the words' bits past the lattice edge are never written and must read 0
-  S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, 3 * pt_bits_words(m) * 4, st));
-  S2_CUDA(cudaMallocAsync(&m->offx, size_t((j.N + 31) / 32) * 4, st));
-  S2_CUDA(cudaMallocAsync(&m->cell_words, m->cell_tiles * S2_CW_BLOCK * 4, st));
-  S2_CUDA(cudaMallocAsync(&m->tile_cnt, (m->cell_tiles + 1) * 4, st));  // + the finished-block counter
-  if (m->sdf->k_tiles && m->nslabs > 0) {
-    S2_CUDA(cudaMallocAsync(&m->prune_buf, prune_layout(m), st));
-    // pageable source: the call returns once the words are staged
-    S2_CUDA(cudaMemcpyAsync(prune_bases(m), m->slab_tile_base.data(), m->slab_tile_base.size() * 8,
-                            cudaMemcpyHostToDevice, st));
-    S2_CUDA(cudaMemcpyAsync(prune_at<unsigned long long>(m, m->prune_cbase_off), m->slab_coarse_base.data(),
-                            m->slab_coarse_base.size() * 8, cudaMemcpyHostToDevice, st));
-  }
-  S2_CUDA(cudaMallocAsync(&m->cand_key, m->cand_cap * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->cand_val, m->cand_cap * 32, st));
-  S2_CUDA(cudaMallocAsync(&m->cand_pos, m->cand_cap * 12, st));
-  S2_CUDA(cudaMallocAsync(&m->cand_nrm, m->cand_cap * 12, st));
-  S2_CUDA(cudaMallocAsync(&m->cand_base, size_t(m->nslabs + 1) * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->cand_status, vc_ctrl_words(m->vc_tiles) * 8, st));
-  if (m->prune_buf && m->prune_chunk >= m->nslabs && m->cand_cap < (1ull << 32)) {
+  BufPlan b{};
+  b.ring = size_t(j.ring) * size_t(j.plane) * sizeof(float);
+  b.slab_ctrl = m->slab_ctrl_words * 8;
+  b.pt_bits = 3 * pt_bits_words(m) * 4;
+  b.offx = size_t((j.N + 31) / 32) * 4;
+  b.cell_words = m->cell_tiles * S2_CW_BLOCK * 4;
+  b.tile_cnt = (m->cell_tiles + 1) * 4;  // + the finished-block counter
+  const bool prune = m->sdf->k_tiles && m->nslabs > 0;
+  b.prune = prune ? prune_layout(m) : 0;
+  b.cand_key = m->cand_cap * 8;
+  b.cand_val = m->cand_cap * 32;
+  b.cand_pos = m->cand_cap * 12;
+  b.cand_nrm = m->cand_cap * 12;
+  b.cand_base = size_t(m->nslabs + 1) * 8;
+  b.cand_status = vc_ctrl_words(m->vc_tiles) * 8;
+  b.vt = 0;
+  m->vt_tiles = 0;
+  if (prune && m->prune_chunk >= m->nslabs && m->cand_cap < (1ull << 32)) {
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
     m->vt_tiles = m->slab_tile_base[size_t(m->nslabs)] - m->slab_tile_base[0];
     m->vt_blocks = unsigned((m->vt_tiles + S2_VT_TILE - 1) / S2_VT_TILE);
@@ -597,16 +603,84 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
     m->vt_poff_off = up16(m->vt_part_off + 4 * size_t(m->vt_blocks));
     m->vt_rank_off = up16(m->vt_poff_off + 8 * size_t(m->vt_blocks));
     m->vt_perm_off = up16(m->vt_rank_off + 8 * size_t(m->cand_cap));
-    S2_CUDA(cudaMallocAsync(&m->vt_buf, m->vt_perm_off + 4 * size_t(m->cand_cap), st));
+    b.vt = m->vt_perm_off + 4 * size_t(m->cand_cap);
   }
-  S2_CUDA(cudaMallocAsync(&m->pos, m->vcap * 12, st));
-  S2_CUDA(cudaMallocAsync(&m->nrm, m->vcap * 12, st));
-  S2_CUDA(cudaMallocAsync(&m->key, m->vcap * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->tris, m->tcap * 12, st));
-  S2_CUDA(cudaMallocAsync(&m->rowcnt, N * N * 4, st));
-  S2_CUDA(cudaMallocAsync(&m->rowstart, (N * N + 1) * 4, st));
-  S2_CUDA(cudaMallocAsync(&m->scan_status, (m->scan_tiles + m->quad_tiles) * 8, st));
-  S2_CUDA(cudaMallocAsync(&m->jobctl, 8 * 8, st));
+  b.pos = m->vcap * 12;
+  b.nrm = m->vcap * 12;
+  b.key = m->vcap * 8;
+  b.tris = m->tcap * 12;
+  b.rowcnt = N * N * 4;
+  b.rowstart = (N * N + 1) * 4;
+  b.scan_status = (m->scan_tiles + m->quad_tiles) * 8;
+  b.jobctl = 8 * 8;
+  return b;
+}
+
+// Initial capacities of a job's candidate, vertex and triangle arrays (the
+// pipeline regrows them to the exact totals when they overflow).
+void initial_caps(const s2m_mesh *m, const s2m_params &p, unsigned long long &cand_cap, unsigned long long &vcap,
+                  unsigned long long &tcap) {
+  const unsigned long long N = (unsigned long long)m->N;
+  const unsigned long long N3 = N * N * N;
+  cand_cap = std::min(N3, std::max<unsigned long long>(65536, 8 * N * N));
+  vcap = p.max_vertices ? p.max_vertices : std::min(N3, std::max<unsigned long long>(65536, 6 * N * N));
+  tcap = p.max_triangles ? p.max_triangles : std::max<unsigned long long>(131072, 2 * vcap + 4096);
+  if (p.max_vertices) cand_cap = std::min(N3, std::max<unsigned long long>(1024, p.max_vertices));
+}
+
+// Host hook for failure tests: when S2M_TEST_FAIL_ALLOC=k is set, the k-th
+// device allocation of the process (counting from 1) reports
+// cudaErrorMemoryAllocation without allocating.
+std::atomic<long long> g_alloc_count{0};
+cudaError_t mesh_malloc(void **p, size_t bytes, cudaStream_t st) {
+  static const long long fail_at = [] {
+    const char *e = std::getenv("S2M_TEST_FAIL_ALLOC");
+    return e ? std::atoll(e) : 0ll;
+  }();
+  if (fail_at > 0 && ++g_alloc_count == fail_at) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocAsync(p, bytes, st);
+}
+
+int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long vcap, unsigned long long tcap,
+                  char *err, size_t errlen) {
+  drop_graph(m);
+  free_buffers(m);
+  const BufPlan b = plan_buffers(m, cand_cap, vcap, tcap);
+  cudaStream_t st = m->stream;
+  S2_CUDA(mesh_malloc((void **)&m->ring, b.ring, st));
+  S2_CUDA(mesh_malloc((void **)&m->slab_ctrl, b.slab_ctrl, st));
+  S2_CUDA(mesh_malloc((void **)&m->pt_bits, b.pt_bits, st));
+  // the words' bits past the lattice edge are never written and must read 0
+  S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, b.pt_bits, st));
+  S2_CUDA(mesh_malloc((void **)&m->offx, b.offx, st));
+  S2_CUDA(mesh_malloc((void **)&m->cell_words, b.cell_words, st));
+  S2_CUDA(mesh_malloc((void **)&m->tile_cnt, b.tile_cnt, st));
+  if (b.prune) {
+    S2_CUDA(mesh_malloc((void **)&m->prune_buf, b.prune, st));
+    // pageable source: the call returns once the words are staged
+    S2_CUDA(cudaMemcpyAsync(prune_bases(m), m->slab_tile_base.data(), m->slab_tile_base.size() * 8,
+                            cudaMemcpyHostToDevice, st));
+    S2_CUDA(cudaMemcpyAsync(prune_at<unsigned long long>(m, m->prune_cbase_off), m->slab_coarse_base.data(),
+                            m->slab_coarse_base.size() * 8, cudaMemcpyHostToDevice, st));
+  }
+  S2_CUDA(mesh_malloc((void **)&m->cand_key, b.cand_key, st));
+  S2_CUDA(mesh_malloc((void **)&m->cand_val, b.cand_val, st));
+  S2_CUDA(mesh_malloc((void **)&m->cand_pos, b.cand_pos, st));
+  S2_CUDA(mesh_malloc((void **)&m->cand_nrm, b.cand_nrm, st));
+  S2_CUDA(mesh_malloc((void **)&m->cand_base, b.cand_base, st));
+  S2_CUDA(mesh_malloc((void **)&m->cand_status, b.cand_status, st));
+  if (b.vt) S2_CUDA(mesh_malloc((void **)&m->vt_buf, b.vt, st));
+  S2_CUDA(mesh_malloc((void **)&m->pos, b.pos, st));
+  S2_CUDA(mesh_malloc((void **)&m->nrm, b.nrm, st));
+  S2_CUDA(mesh_malloc((void **)&m->key, b.key, st));
+  S2_CUDA(mesh_malloc((void **)&m->tris, b.tris, st));
+  S2_CUDA(mesh_malloc((void **)&m->rowcnt, b.rowcnt, st));
+  S2_CUDA(mesh_malloc((void **)&m->rowstart, b.rowstart, st));
+  S2_CUDA(mesh_malloc((void **)&m->scan_status, b.scan_status, st));
+  S2_CUDA(mesh_malloc((void **)&m->jobctl, b.jobctl, st));
   m->h_read = take_pinned_slot();
   if (!m->h_read) {
     set_err(err, errlen, "pinned read-back slot");
@@ -710,6 +784,10 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   md.ntris = c.ntris;
   md.invalid = c.invalid;
   md.err = c.err;
+  md.wait_ns = m->wait_ns;
+  md.hold = 0;
+  if (const char *h = std::getenv("S2M_TEST_HOLD")) md.hold = unsigned(std::strtoul(h, nullptr, 0));  // tests only
+  md.pad = 0;
 
   const long long pts = (long long)j.P * j.P;
   const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
@@ -926,6 +1004,23 @@ int readback(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
 }
 
 }  // namespace
+
+namespace s2m {
+// Device bytes that s2m_mesh_create allocates for this job at its first
+// attempt: the same job setup (resolution rounding, slab depth, tile
+// layout) and the same buffer plan, without allocating.  0 for a job that
+// setup rejects.  Used by the server's admission (batch.cu).
+uint64_t mesh_job_footprint(const s2m_sdf *sdf, const s2m_params &params) {
+  s2m_mesh m;
+  m.sdf = sdf;
+  m.params = params;
+  if (!(m.params.eps > 0.0f)) m.params.eps = 1e-4f;
+  if (setup_job(&m, nullptr, 0) != S2M_OK) return 0;
+  unsigned long long cand_cap, vcap, tcap;
+  initial_caps(&m, m.params, cand_cap, vcap, tcap);
+  return uint64_t(plan_buffers(&m, cand_cap, vcap, tcap).total());
+}
+}  // namespace s2m
 
 // ===========================================================================
 // Meshing without device allocation: the pipeline's scratch in one fixed
@@ -1278,11 +1373,8 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
   }
   const unsigned long long N = (unsigned long long)m->N;
   const unsigned long long N3 = N * N * N;
-  unsigned long long cand_cap = std::min(N3, std::max<unsigned long long>(65536, 8 * N * N));
-  unsigned long long vcap = params->max_vertices ? params->max_vertices
-                                                 : std::min(N3, std::max<unsigned long long>(65536, 6 * N * N));
-  unsigned long long tcap = params->max_triangles ? params->max_triangles : std::max<unsigned long long>(131072, 2 * vcap + 4096);
-  if (params->max_vertices) cand_cap = std::min(N3, std::max<unsigned long long>(1024, params->max_vertices));
+  unsigned long long cand_cap, vcap, tcap;
+  initial_caps(m, *params, cand_cap, vcap, tcap);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   for (int attempt = 0; attempt < 5; ++attempt) {
     rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen);
@@ -1440,6 +1532,12 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   return S2M_OK;
 }
 
+int s2m_mesh_footprint(const s2m_sdf *sdf, const s2m_params *params, uint64_t *bytes) {
+  if (!sdf || !params || !bytes) return S2M_E_INVALID;
+  *bytes = s2m::mesh_job_footprint(sdf, *params);
+  return *bytes ? S2M_OK : S2M_E_INVALID;
+}
+
 int s2m_mesh_get_info(const s2m_mesh *m, s2m_mesh_info *info) {
   if (!m || !info) return S2M_E_INVALID;
   std::memset(info, 0, sizeof(*info));
@@ -1482,6 +1580,13 @@ int s2m_mesh_write(const s2m_mesh *m, const char *path, char *err, size_t errlen
   return s2m::write_mesh_file(path, pos.data(), nrm.data(), m->nverts, tris.data(), m->ntris, err, errlen);
 }
 
+int s2m_mesh_set_wait_limit(s2m_mesh *m, double seconds) {
+  if (!m || !(seconds > 0.0) || seconds > 3600.0) return S2M_E_INVALID;
+  m->wait_ns = (unsigned long long)(seconds * 1e9);
+  drop_graph(m);  // a captured graph holds the old bound
+  return S2M_OK;
+}
+
 int s2m_mesh_set_graph(s2m_mesh *m, int enable) {
   if (!m) return S2M_E_INVALID;
   m->use_graph = enable != 0;
@@ -1518,6 +1623,27 @@ void s2m_mesh_free(s2m_mesh *m) {
 
 int s2m_write_stl(const float *pos, const uint32_t *tris, uint64_t ntris, const char *path) {
   return s2m::write_stl(path, pos, tris, ntris) ? S2M_OK : S2M_E_IO;
+}
+
+int s2m_write_stl_binary(const float *pos, const uint32_t *tris, uint64_t ntris, const char *path) {
+  if ((!pos && ntris) || (!tris && ntris) || !path) return S2M_E_INVALID;
+  return s2m::write_stl_binary(path, pos, tris, ntris) ? S2M_OK : S2M_E_IO;
+}
+
+int s2m_mesh_write_stl_binary(const s2m_mesh *m, const char *path, char *err, size_t errlen) {
+  if (!m || !path) return S2M_E_INVALID;
+  std::vector<float> pos(m->nverts * 3);
+  std::vector<uint32_t> tris(m->ntris * 3);
+  int rc = s2m_mesh_copy_to_host(m, pos.data(), nullptr, nullptr, tris.data(), nullptr);
+  if (rc != S2M_OK) {
+    set_err(err, errlen, "device to host copy failed");
+    return rc;
+  }
+  if (!s2m::write_stl_binary(path, pos.data(), tris.data(), m->ntris)) {
+    set_err(err, errlen, std::string("could not write ") + path);
+    return S2M_E_IO;
+  }
+  return S2M_OK;
 }
 
 int s2m_write_ply(const float *pos, const float *nrm, uint64_t nverts, const uint32_t *tris, uint64_t ntris,

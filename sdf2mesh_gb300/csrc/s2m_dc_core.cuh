@@ -452,7 +452,7 @@ template <bool CG>
 __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__restrict__ ring, const S2Cand &cand,
                                              unsigned long long *status, unsigned *err, unsigned tile,
                                              unsigned ntiles, long long ncells, int zc0, unsigned long long base,
-                                             unsigned long long *next_base) {
+                                             unsigned long long *next_base, unsigned long long wait_ns) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned long long s_excl;
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -475,7 +475,7 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
   __syncthreads();
   if (warp == 0) {
     const unsigned tot = s2_warp_exclusive32(s_warp);
-    const unsigned long long excl = s2_lookback(status, tile, tot, err);
+    const unsigned long long excl = s2_lookback(status, tile, tot, err, wait_ns);
     if (lane == 0) {
       s_excl = excl;
       if (tile == ntiles - 1) *next_base = base + excl + tot;

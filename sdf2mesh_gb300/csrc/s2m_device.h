@@ -89,7 +89,15 @@ struct S2MeshDev {
   unsigned long long *invalid;    // out: invalid quads (mesh.rs:275-277)
   unsigned long long *ncand;      // out: candidates over all slabs
   unsigned *err;
+  unsigned long long wait_ns;     // bound of each device wait (look-back), GPU global timer ns
+  unsigned hold;                  // test hook: S2_HOLD_* (0 in normal runs)
+  unsigned pad;
 };
+
+// Test hooks (S2MeshDev::hold): a flag that nothing sets, so that a bounded
+// device wait runs out and the run reports S2M_E_TIMEOUT.  Only the waiting
+// is affected; every write stays bounds-checked.
+#define S2_HOLD_QUADS_TILE0 0x1u  /* tile 0 of the quad pass never publishes its prefix */
 
 #define S2_ERR_LOOKBACK 0x1u      /* a look-back wait hit its iteration limit   */
 #define S2_ERR_CAND_OVF 0x2u      /* candidate arrays too small                 */

@@ -5,16 +5,24 @@
 // status words (32 at a time, one per lane) until it meets an inclusive
 // prefix.  Tiles take their ids from an atomic counter when they start, so a
 // tile only ever waits for tiles that are already running; every wait is
-// still bounded: after S2_SPIN_LIMIT polls the tile raises S2_ERR_LOOKBACK in
-// the job's error word and continues, and every write that uses the offset is
-// bounds-checked against its buffer's capacity.
+// still bounded in time: once the GPU's global timer has advanced by the
+// job's wait limit (S2MeshDev::wait_ns, default S2_WAIT_NS) since the tile
+// began to wait, it raises S2_ERR_LOOKBACK in the job's error word and
+// continues, and every write that uses the offset is bounds-checked against
+// its buffer's capacity.
 #pragma once
 
 #define S2_LB_AGG 1ull
 #define S2_LB_PRE 2ull
 #define S2_LB_MASK ((1ull << 62) - 1ull)
-#define S2_SPIN_LIMIT (1u << 22)
+#define S2_WAIT_NS 2000000000ull /* default bound of one device wait: 2 s */
 #define S2_FULL 0xffffffffu
+
+__device__ __forceinline__ unsigned long long s2_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ void s2_st_release(unsigned long long *p, unsigned long long v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
@@ -39,7 +47,8 @@ __device__ __forceinline__ float s2_ldcg(const float *p) { return __ldcg(p); }
 // Called by all 32 lanes of one warp; returns the exclusive prefix of
 // `aggregate` over tiles 0 .. tile-1 (the same value in every lane).
 __device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *status, unsigned tile,
-                                                          unsigned long long aggregate, unsigned *err) {
+                                                          unsigned long long aggregate, unsigned *err,
+                                                          unsigned long long wait_ns) {
   const unsigned lane = threadIdx.x & 31u;
   if (tile == 0) {
     if (lane == 0) s2_st_release(status, (S2_LB_PRE << 62) | aggregate);
@@ -48,7 +57,7 @@ __device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *st
   if (lane == 0) s2_st_release(status + tile, (S2_LB_AGG << 62) | aggregate);
   unsigned long long excl = 0;
   long long base = (long long)tile - 1;
-  unsigned spins = 0;
+  unsigned long long t0 = 0;
   for (;;) {
     long long idx = base - (long long)lane;
     unsigned long long w = idx >= 0 ? s2_ld_acquire(status + idx) : (S2_LB_PRE << 62);
@@ -58,7 +67,10 @@ __device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *st
     unsigned first = pmask ? (unsigned)(__ffs(pmask) - 1) : 32u;
     unsigned need = first >= 31u ? S2_FULL : ((2u << first) - 1u);
     if (zmask & need) {
-      if (++spins > S2_SPIN_LIMIT) {
+      // the same timer value in every lane (broadcast), so the warp leaves together
+      const unsigned long long now = __shfl_sync(S2_FULL, s2_globaltimer(), 0);
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > wait_ns) {
         if (lane == 0) atomicOr(err, S2_ERR_LOOKBACK);
         break;
       }

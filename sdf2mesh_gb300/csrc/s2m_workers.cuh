@@ -42,7 +42,7 @@ __device__ __forceinline__ void s2_vcompact_worker(const S2Job &job, const S2Can
     __syncthreads();
     if (warp == 0) {
       unsigned tot = s2_warp_exclusive32(s_warp);
-      unsigned long long excl = s2_lookback(cand.status, tile, tot, mesh.err);
+      unsigned long long excl = s2_lookback(cand.status, tile, tot, mesh.err, mesh.wait_ns);
       if (lane == 0) {
         s_excl = excl;
         if (tile == ntiles - 1) *mesh.vtotal = excl + tot;
@@ -126,7 +126,7 @@ __device__ __forceinline__ void s2_rowscan_worker(const S2MeshDev &mesh, unsigne
     }
     unsigned pre = s2_block_exclusive(sum, s_warp, &s_total);
     if (warp == 0) {
-      unsigned long long excl = s2_lookback(mesh.scan_status, tile, s_total, mesh.err);
+      unsigned long long excl = s2_lookback(mesh.scan_status, tile, s_total, mesh.err, mesh.wait_ns);
       if (lane == 0) {
         s_excl = excl;
         if (tile == ntiles - 1) mesh.rowstart[R] = (unsigned)(excl + s_total);
@@ -272,7 +272,10 @@ __device__ __forceinline__ void s2_quads_worker(const S2Job &job, const S2MeshDe
     }
     __syncthreads();
     if (warp == 0) {
-      unsigned long long excl = s2_lookback(status, tile, s_total, mesh.err);
+      // S2_HOLD_QUADS_TILE0 (tests): tile 0 keeps its status word at 0, so every
+      // later tile's look-back waits until its limit
+      const bool hold = tile == 0 && (mesh.hold & S2_HOLD_QUADS_TILE0);
+      unsigned long long excl = hold ? 0ull : s2_lookback(status, tile, s_total, mesh.err, mesh.wait_ns);
       if (lane == 0) {
         s_excl = excl;
         if (tile == ntiles - 1) *mesh.ntris = excl + s_total;

@@ -1,9 +1,12 @@
-"""Extract the reference's own test vectors into tests/golden/.
+"""Extract the reference's own test vectors and example inputs into tests/golden/.
 
 The reference's only tests (src/shadertoy.rs:354-453) pin its WGSL text
 surgery: `remove_function` (:357-392) and `rename_function` (:394-401).  This
 script reads those tests as text from a reference checkout and writes their
-inputs and expected facts to wgsl_surgery.json.  Run from the repository root:
+inputs and expected facts to wgsl_surgery.json.  It also stores the example
+SDF files the reference ships as its inputs (examples/*.sdf3d, *.frag) in
+reference_examples.json, so that the GPU tests can mesh them where no
+reference checkout exists.  Run from the repository root:
 
     python tests/golden/make_golden.py /path/to/sdf2mesh
 """
@@ -45,7 +48,18 @@ def main(ref_root):
     with open(os.path.join(here, "wgsl_surgery.json"), "w") as f:
         json.dump(out, f, indent=1)
         f.write("\n")
+    examples = {}
+    for name in ("torus.sdf3d", "martin_cube.sdf3d", "p_key.sdf3d", "mandelmesh.frag"):
+        with open(os.path.join(ref_root, "examples", name)) as f:
+            examples[name] = f.read()
+    with open(os.path.join(here, "reference_examples.json"), "w") as f:
+        json.dump({"source": "examples/ (WilstonOreo/sdf2mesh), the reference's example inputs",
+                   "files": examples}, f, indent=1)
+        f.write("\n")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("S2M_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout>  (or set S2M_REFERENCE_DIR)")
+    main(ref)

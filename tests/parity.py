@@ -137,3 +137,87 @@ def reference_quads(cell_xyz, signs):
             if not (p < V and keys[p] == k):
                 missing.append(cc)
     return tris, int(invalid.sum()), np.array(missing, np.int64).reshape(-1, 3)
+
+
+def reference_quads_chunked(cell_xyz, signs, chunk=1 << 21):
+    """reference_quads over vertex chunks (same triangles in the same order),
+    for vertex lists of tens of millions: the per-quad arrays stay chunk-sized.
+    Returns (triangles, invalid quad count, missing cells)."""
+    c = np.asarray(cell_xyz, np.int64)
+    keys = c[:, 0] | (c[:, 1] << 16) | (c[:, 2] << 32)
+    V = len(keys)
+    s_all = np.asarray(signs, np.int64)
+    NONE = np.int64(0xFFFFFFFF)
+
+    def find(xx, yy, zz):
+        k = xx | (yy << 16) | (zz << 32)
+        pos = np.searchsorted(keys, k)
+        ok = (pos < V) & (keys[np.minimum(pos, V - 1)] == k)
+        return np.where(ok, pos, NONE)
+
+    tris_out, invalid_total, missing = [], 0, []
+    for a in range(0, V, chunk):
+        b = min(V, a + chunk)
+        x, y, z = c[a:b, 0], c[a:b, 1], c[a:b, 2]
+        s = s_all[a:b]
+        b0, b1, b2, b3 = (s & 1) != 0, (s & 2) != 0, (s & 4) != 0, (s & 8) != 0
+        idx = np.arange(a, b, dtype=np.int64)
+        n = b - a
+        quads = np.full((n, 3, 4), NONE, np.int64)
+        active = np.zeros((n, 3), bool)
+        swap = np.zeros((n, 3), bool)
+        m = (b0 != b3) & (y > 0) & (z > 0)
+        quads[m, 0] = np.stack([find(x[m], y[m] - 1, z[m] - 1), find(x[m], y[m], z[m] - 1), idx[m],
+                                find(x[m], y[m] - 1, z[m])], 1)
+        active[:, 0], swap[:, 0] = m, b0
+        m = (b1 != b3) & (x > 0) & (z > 0)
+        quads[m, 1] = np.stack([find(x[m] - 1, y[m], z[m] - 1), find(x[m], y[m], z[m] - 1), idx[m],
+                                find(x[m] - 1, y[m], z[m])], 1)
+        active[:, 1], swap[:, 1] = m, ~b1
+        m = (b2 != b3) & (x > 0) & (y > 0)
+        quads[m, 2] = np.stack([find(x[m] - 1, y[m] - 1, z[m]), find(x[m], y[m] - 1, z[m]), idx[m],
+                                find(x[m] - 1, y[m], z[m])], 1)
+        active[:, 2], swap[:, 2] = m, b2
+        quads = np.where(swap[..., None], quads[..., ::-1], quads)
+        valid = active & (quads != NONE).all(-1)
+        invalid = active & ~valid
+        invalid_total += int(invalid.sum())
+        q = quads[valid]
+        tris_out.append(np.stack([q[:, [2, 1, 0]], q[:, [0, 3, 2]]], 1).reshape(-1, 3).astype(np.uint32))
+        for vi, qi in zip(*np.nonzero(invalid)):
+            xx, yy, zz = c[a + vi]
+            cand = {0: [(xx, yy - 1, zz - 1), (xx, yy, zz - 1), (xx, yy - 1, zz)],
+                    1: [(xx - 1, yy, zz - 1), (xx, yy, zz - 1), (xx - 1, yy, zz)],
+                    2: [(xx - 1, yy - 1, zz), (xx, yy - 1, zz), (xx - 1, yy, zz)]}[int(qi)]
+            for cc in cand:
+                k = cc[0] | (cc[1] << 16) | (cc[2] << 32)
+                p = np.searchsorted(keys, k)
+                if not (p < V and keys[p] == k):
+                    missing.append(cc)
+    tris = np.concatenate(tris_out) if tris_out else np.zeros((0, 3), np.uint32)
+    return tris, invalid_total, np.array(missing, np.int64).reshape(-1, 3)
+
+
+def compare_window_with_ties(gsel, ref, kind, params, resolution, bounds, eps, h, slice_lag=False):
+    """The GPU's vertices of a window of slices (a TriangleMesh-like object with
+    cell_xyz, signs, positions) against the oracle's mesh of the same window:
+    vertex cells and sign words equal outside tie cells (a reference corner
+    with |f| <= eps).  Returns the counts and the largest position difference
+    (in cells) of the common vertices that are not tie cells."""
+    gk = keys_of(gsel.cell_xyz)
+    rk = keys_of(ref.cell)
+    gset, rset = set(gk.tolist()), set(rk.tolist())
+    only = gset ^ rset
+    ties = tie_cells(kind, params, resolution, bounds, list(only), eps, slice_lag)
+    assert only <= ties, f"{len(only - ties)} vertex cells differ outside tie cells, e.g. {sorted(only - ties)[:5]}"
+    common = np.array(sorted(gset & rset), np.uint64)
+    gi = np.searchsorted(gk, common)
+    ri = np.searchsorted(rk, common)
+    sign_diff = set(common[gsel.signs[gi] != ref.signs[ri]].tolist())
+    sd_ties = tie_cells(kind, params, resolution, bounds, list(sign_diff), eps, slice_lag)
+    assert sign_diff <= sd_ties, f"{len(sign_diff - sd_ties)} sign words differ outside tie cells"
+    err = np.abs(gsel.positions[gi].astype(np.float64) - np.asarray(ref.pos, np.float64)[ri]).max(axis=1) / h
+    flips = ties | sd_ties
+    near = np.array([int(k) not in flips for k in common.tolist()], bool)
+    return {"vertices": len(common), "tie_cells": len(flips | only), "vertex_only_one_side": len(only),
+            "max_pos_err_cells": float(err[near].max()) if near.any() else 0.0, "errs": err[near]}

@@ -66,3 +66,19 @@ def test_cli_glsl(lib, tmp_path):
     assert r.returncode == 0, r.stderr
     text = out.read_text()
     assert text.startswith("solid\n") and text.endswith("endsolid\n") and text.count("endfacet") > 1000
+
+
+@pytest.mark.gpu
+def test_cli_binary_stl(lib, oracle_lib, tmp_path):
+    """--binary-stl: the same facets as the ASCII file, in the binary form."""
+    import oracle
+    from tests.test_stl_binary import numpy_stl_binary
+    src = tmp_path / "torus.sdf3d"
+    src.write_text(TORUS)
+    out = tmp_path / "mesh.stl"
+    r = run("-i", os.fspath(src), "-0", os.fspath(out), "-r", "128", "--binary-stl")
+    assert r.returncode == 0, r.stderr
+    ref = oracle.mesh(oracle.TORUS, [0.5, 0.2], 128, 2.0, slice_lag=True)
+    data = out.read_bytes()
+    assert int.from_bytes(data[80:84], "little") == ref.ntris
+    assert data[84:] == numpy_stl_binary(ref.pos, ref.tris)

@@ -21,7 +21,9 @@ from tests.hostsdf import compile_host, eval_host
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_EXAMPLES = "/root/reference/examples"
+# A checkout of the reference sources, when one is at hand (S2M_REFERENCE_DIR);
+# the tests that read its example files as text skip without it.
+REF_EXAMPLES = os.path.join(os.environ.get("S2M_REFERENCE_DIR", ""), "examples")
 
 
 def lower(src, lang=s2m.LANG_WGSL, name="sdf"):
@@ -101,26 +103,62 @@ def test_normal_is_tetrahedral_sum(lib):
     assert np.array_equal(out.view(np.uint32), acc.astype(np.float32).view(np.uint32))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
-@pytest.mark.parametrize("name", ["torus.sdf3d", "martin_cube.sdf3d", "p_key.sdf3d"])
-def test_reference_examples_lower_and_run(lib, name):
-    sh = s2m.Sdf3DShader.from_path(os.path.join(REF_EXAMPLES, name))
+def reference_example(name):
+    """An example input the reference ships (examples/<name>), from the fixture
+    tests/golden/make_golden.py extracted."""
+    with open(os.path.join(GOLDEN, "reference_examples.json")) as f:
+        return json.load(f)["files"][name]
+
+
+@pytest.mark.skipif(not os.environ.get("S2M_REFERENCE_DIR") or not os.path.isdir(REF_EXAMPLES),
+                    reason="no reference checkout (S2M_REFERENCE_DIR)")
+def test_example_fixture_matches_checkout():
+    for name in ("torus.sdf3d", "martin_cube.sdf3d", "p_key.sdf3d", "mandelmesh.frag"):
+        assert open(os.path.join(REF_EXAMPLES, name)).read() == reference_example(name), name
+
+
+@pytest.mark.parametrize("name,kind,B", [("torus.sdf3d", oracle.TORUS, 2.0),
+                                         ("martin_cube.sdf3d", oracle.MARTIN_CUBE, 3.0),
+                                         ("p_key.sdf3d", oracle.P_KEY, 40.0)])
+def test_reference_examples_lower_bit_exact(lib, oracle_lib, name, kind, B):
+    """The reference's example files (swizzle assignment, `const` folding in
+    binary64, `if`, `var`, compound assignment, capsule, cylinder and the
+    smooth operators) lower to code that evaluates bit for bit like the
+    oracle's restatement of the same file."""
+    sh = s2m.Sdf3DShader.from_source(reference_example(name))
     cuda, fp32, _ = s2m.translate(sh.source)
     assert fp32 > 0
-    B = 40.0 if name == "p_key.sdf3d" else 2.0
-    v = eval_host(cuda, points(3000, lo=-B / 2, hi=B / 2))
-    assert np.isfinite(v).all()
+    p = points(20000, lo=-B / 2, hi=B / 2)
+    v = eval_host(cuda, p)
     assert (v < 0).any() and (v > 0).any(), "the surface crosses the box"
+    prm = [0.5, 0.2] if kind == oracle.TORUS else []
+    assert_same_bits(v, oracle.evaluate(kind, prm, p))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
 def test_reference_mandelmesh_glsl(lib, oracle_lib):
     """examples/mandelmesh.frag: 5 iterations, power 8, bailout 2, offset 0.003."""
-    text = open(os.path.join(REF_EXAMPLES, "mandelmesh.frag")).read()
+    text = reference_example("mandelmesh.frag")
     cuda, _, _ = s2m.translate(text, s2m.LANG_GLSL, "sdf")
     p = points(3000, lo=-1.25, hi=1.25)
     ref = oracle.evaluate(oracle.MANDELBULB, [8.0, 5, 2.0, 0.003], p)
     assert_same_bits(eval_host(cuda, p), ref)
+
+
+def test_cylinder_lowering_bit_exact(lib, oracle_lib):
+    """sdf3d_cylinder (sdf3d_primitives.wgsl:13-17) against the oracle."""
+    src = ("use sdf3d::*;\nfn sdf3d(p: vec3f) -> f32 {\n"
+           "  return sdf3d_cylinder(p - vec3f(0.125, -0.25, 0.0625), 0.5, 0.375);\n}\n")
+    cuda, _, _ = lower(src)
+    p = points(20000)
+    assert_same_bits(eval_host(cuda, p), oracle.evaluate(oracle.TREE, [5, 0.125, -0.25, 0.0625, 0.5, 0.375], p))
+
+
+def test_csg64_fixture_reproduced():
+    """The 1024^3 workload's source is checked in (tests/golden/csg64_seed0.sdf3d);
+    the generator still writes exactly that text."""
+    src, _ = workloads.csg64(seed=0)
+    with open(os.path.join(GOLDEN, "csg64_seed0.sdf3d")) as f:
+        assert f.read() == src
 
 
 def test_glsl_missing_function(lib):
