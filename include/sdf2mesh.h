@@ -130,6 +130,15 @@ int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t 
 /* The lowered CUDA C of a compiled SDF (for --debug-cuda); owned by sdf. */
 const char *s2m_sdf_cuda_source(const s2m_sdf *sdf);
 
+/* How the SDF's module was built: wall seconds of the NVRTC stage, the NVRTC
+   programs it was split into (compiled on parallel host threads), and how
+   many of them came from the on-disk module cache ($S2M_CACHE_DIR, empty to
+   turn it off; default $XDG_CACHE_HOME or $HOME/.cache, sdf2mesh_gb300/),
+   whose files hold the whole program text beside the CUBIN so that a hit is
+   an exact match.  The reference compiles its shader per run
+   (shader.rs:220-225). */
+int s2m_sdf_compile_info(const s2m_sdf *sdf, double *seconds, int *programs, int *cache_hits);
+
 /* Algorithmic FP32 and SFU operations of one sdf3d evaluation. */
 int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops);
 /* Operations per point when the lattice kernel evaluates runs of 4 points

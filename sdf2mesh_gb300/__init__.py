@@ -129,6 +129,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_compile_file": ([ctypes.c_char_p, i, ctypes.c_char_p, u32, ctypes.POINTER(vp),
                                   ctypes.c_char_p, sz], i),
             "s2m_sdf_cuda_source": ([vp], ctypes.c_char_p),
+            "s2m_sdf_compile_info": ([vp, dp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], i),
             "s2m_sdf_op_counts": ([vp, dp, dp], i),
             "s2m_sdf_run_op_counts": ([vp, dp, dp], i),
             "s2m_sdf_set_eval_variant": ([vp, i], i),
@@ -265,6 +266,13 @@ class CompiledSdf:
     @property
     def cuda_source(self) -> str:
         return load_library().s2m_sdf_cuda_source(self._h).decode()
+
+    def compile_info(self) -> dict:
+        """NVRTC wall seconds, programs, and programs read from the on-disk module cache."""
+        sec, progs, hits = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        _check(load_library().s2m_sdf_compile_info(self._h, ctypes.byref(sec), ctypes.byref(progs),
+                                                   ctypes.byref(hits)), None, "compile info")
+        return {"nvrtc_s": sec.value, "programs": progs.value, "cache_hits": hits.value}
 
     def run_op_counts(self):
         """Ops per point in runs of 4 sharing x and y, or None when the SDF has no run form."""

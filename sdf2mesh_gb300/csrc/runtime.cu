@@ -17,8 +17,13 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <errno.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +32,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sdf2mesh.h"
@@ -95,6 +101,31 @@ constexpr EvalVariant kEvalVariants[] = {
     {"s2m_evalpl_b8", 1, false, true, true},   {"s2m_evalpl_b8v4", 4, true, true, true}};
 constexpr int kNumEvalVariants = int(sizeof(kEvalVariants) / sizeof(kEvalVariants[0]));
 
+// The NVRTC programs of one SDF's module.  Each holds some of its kernels
+// (the S2M_WANT_* selections of s2m_dc_kernels.cuh) and compiles on its own
+// host thread, so a module builds in the time of its slowest program.
+// `variant`: the evaluation variant it holds (-1: none); `prune`: present only
+// for SDFs with a tile form; `full_only`: present only in modules without
+// pruning.  The full-evaluation run-of-4 variants are the slowest programs to
+// compile (12 s of a CSG module's 13 s on one core each) and are never the
+// fastest variant where tile pruning runs, so pruned modules leave them out.
+struct ModulePart {
+  const char *defines;
+  int variant;
+  bool prune;
+  bool full_only;
+};
+constexpr ModulePart kParts[] = {
+    {"#define S2M_WANT_EVAL_B2R4 1\n", 0, false, false},   {"#define S2M_WANT_EVAL_B3R4 1\n", 1, false, false},
+    {"#define S2M_WANT_EVAL_B4R4 1\n", 2, false, false},   {"#define S2M_WANT_EVAL_B2V4 1\n", 3, false, true},
+    {"#define S2M_WANT_EVAL_B3V4 1\n", 4, false, true},    {"#define S2M_WANT_EVALP_B8 1\n", 5, true, false},
+    {"#define S2M_WANT_EVALPL_B8 1\n", 6, true, false},    {"#define S2M_WANT_EVALPL_B8V4 1\n", 7, true, false},
+    {"#define S2M_WANT_TILES_COARSE 1\n", -1, true, false}, {"#define S2M_WANT_TILES_FINE 1\n", -1, true, false},
+    {"#define S2M_WANT_VERTICES 1\n", -1, false, false}};
+constexpr int kNumParts = int(sizeof(kParts) / sizeof(kParts[0]));
+constexpr int kPartTilesCoarse = 8, kPartTilesFine = 9, kPartVertices = 10;
+bool part_in_module(int i, bool prune) { return prune ? !kParts[i].full_only : !kParts[i].prune; }
+
 struct s2m_sdf {
   std::string user_cuda;
   double fp32_ops = 0, sfu_ops = 0;
@@ -102,7 +133,9 @@ struct s2m_sdf {
   int prune_words = 0;                        // activity words per pruning tile (0: no pruning form)
   int prune_combinators = 0;
   uint32_t flags = 0;
-  cudaLibrary_t lib = nullptr;
+  cudaLibrary_t libs[kNumParts] = {};           // one loaded library per NVRTC program (kParts)
+  double compile_s = 0;                         // wall time of the last module build
+  int programs = 0, cache_hits = 0;             // NVRTC programs of the build, and those read from the cache
   cudaKernel_t k_eval[kNumEvalVariants] = {};  // null: variant not in this module
   cudaKernel_t k_tiles = nullptr;               // tile pass of the pruned variants (tiles,
   cudaKernel_t k_tiles_coarse = nullptr;        // and the boxes of 4 x 4 tiles first)
@@ -116,7 +149,14 @@ struct s2m_sdf {
   mutable std::mutex tune_mu;
   mutable int eval_variant = -1;
   mutable int eval_variant_plain = -1;  // fastest variant without pruning (runs with no pruning buffers)
+  // full evaluation slow enough per point that deep slabs pay (set by the
+  // autotuner; see kDeepSlabNsPerPoint)
+  mutable bool deep_slabs = false;
   mutable double tune_ns[kNumEvalVariants] = {};
+  // candidates, vertices and triangles per N^2 cells of this SDF's largest job
+  // so far: the next job's initial capacities (an SDF whose surface outgrows
+  // the default estimate then overflows and re-runs only once)
+  mutable double seen_cand = 0, seen_vert = 0, seen_tri = 0;
   mutable int tune_regs[kNumEvalVariants] = {};
   mutable int tune_local[kNumEvalVariants] = {};  // local (spill/stack) bytes per thread
 };
@@ -146,6 +186,13 @@ struct s2m_mesh {
   size_t prune_sbits_off = 0;  // ... to the coarse boxes' activity words
   size_t prune_bits_off = 0;   // ... to the tiles' activity words
   size_t prune_list_off = 0;   // ... to the lists of undecided tiles
+  // decided-tile map (S2TileMap), when every slab's tile records stay
+  // resident: its words and the plane -> tile-row table
+  bool use_tmap = false;
+  size_t prune_tmap_off = 0, prune_prow_off = 0;
+  unsigned long long tmap_rows = 0;
+  int tmap_wt = 0;
+  std::vector<unsigned> prow_host;
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -199,42 +246,139 @@ namespace {
 // ---------------------------------------------------------------------------
 // NVRTC
 
+// ---------------------------------------------------------------------------
+// On-disk cache of compiled modules.  The key is everything the CUBIN depends
+// on: the NVRTC version, the options (architecture, contraction) and the whole
+// program text (pipeline sources + lowered SDF + kernel selection).  A file
+// holds the key itself beside the CUBIN, so a hit is an exact match, not a
+// hash match.  Directory: $S2M_CACHE_DIR (empty: no cache), else
+// $XDG_CACHE_HOME/sdf2mesh_gb300, else $HOME/.cache/sdf2mesh_gb300.
+
+std::string module_cache_dir() {
+  if (const char *d = std::getenv("S2M_CACHE_DIR")) return d;
+  if (const char *x = std::getenv("XDG_CACHE_HOME"))
+    if (*x) return std::string(x) + "/sdf2mesh_gb300";
+  if (const char *h = std::getenv("HOME"))
+    if (*h) return std::string(h) + "/.cache/sdf2mesh_gb300";
+  return "";
+}
+
+bool make_dirs(const std::string &dir) {
+  if (dir.empty()) return false;
+  for (size_t i = 1; i <= dir.size(); ++i) {
+    if (i == dir.size() || dir[i] == '/') {
+      const std::string sub = dir.substr(0, i);
+      if (::mkdir(sub.c_str(), 0755) != 0 && errno != EEXIST) return false;
+    }
+  }
+  return true;
+}
+
+// 128-bit file name of a key: two FNV-1a style 64-bit hashes with different
+// offsets and multipliers (a name, not a proof: the file holds the key).
+std::string key_name(const std::string &key) {
+  uint64_t a = 1469598103934665603ull, b = 0x9e3779b97f4a7c15ull;
+  for (unsigned char c : key) {
+    a = (a ^ c) * 1099511628211ull;
+    b = (b ^ c) * 0x100000001b3ull + 0x2545f4914f6cdd1dull;
+  }
+  char buf[40];
+  std::snprintf(buf, sizeof buf, "%016llx%016llx", (unsigned long long)a, (unsigned long long)b);
+  return buf;
+}
+
+constexpr char kCacheMagic[] = "S2MCUBIN1";
+
+bool cache_load(const std::string &dir, const std::string &key, std::vector<char> &cubin) {
+  if (dir.empty()) return false;
+  std::ifstream f(dir + "/" + key_name(key) + ".cubin", std::ios::binary);
+  if (!f) return false;
+  char magic[sizeof kCacheMagic];
+  uint64_t klen = 0, clen = 0;
+  if (!f.read(magic, sizeof magic) || std::memcmp(magic, kCacheMagic, sizeof magic) != 0) return false;
+  if (!f.read(reinterpret_cast<char *>(&klen), 8) || klen != key.size()) return false;
+  std::string k(klen, '\0');
+  if (!f.read(&k[0], std::streamsize(klen)) || k != key) return false;
+  if (!f.read(reinterpret_cast<char *>(&clen), 8) || clen == 0 || clen > (1ull << 31)) return false;
+  cubin.resize(size_t(clen));
+  return bool(f.read(cubin.data(), std::streamsize(clen)));
+}
+
+void cache_store(const std::string &dir, const std::string &key, const std::vector<char> &cubin) {
+  if (dir.empty() || !make_dirs(dir)) return;
+  static std::atomic<unsigned> seq{0};
+  const std::string name = dir + "/" + key_name(key) + ".cubin";
+  const std::string tmp = name + ".tmp" + std::to_string(::getpid()) + "." + std::to_string(seq++);
+  {
+    std::ofstream f(tmp, std::ios::binary);
+    if (!f) return;
+    const uint64_t klen = key.size(), clen = cubin.size();
+    f.write(kCacheMagic, sizeof kCacheMagic);
+    f.write(reinterpret_cast<const char *>(&klen), 8);
+    f.write(key.data(), std::streamsize(klen));
+    f.write(reinterpret_cast<const char *>(&clen), 8);
+    f.write(cubin.data(), std::streamsize(clen));
+    if (!f) {
+      std::remove(tmp.c_str());
+      return;
+    }
+  }
+  if (std::rename(tmp.c_str(), name.c_str()) != 0) std::remove(tmp.c_str());  // atomic publish
+}
+
 // NVRTC: the lowered SDF with the pipeline's device sources into a CUBIN for
-// sm_103a, loaded as a library.  `qef` builds the precision-mode vertex
-// kernel alone.
-int nvrtc_build(const s2m_sdf *s, bool qef, cudaLibrary_t *lib, char *err, size_t errlen) {
+// sm_103a (or the cached CUBIN of the same program), loaded as a library.
+// `defines` selects the program's kernels; `qef` builds the precision-mode
+// vertex kernel alone.  *hit tells whether the CUBIN came from the cache.
+int nvrtc_build(const s2m_sdf *s, bool qef, const char *defines, cudaLibrary_t *lib, bool *hit, char *err,
+                size_t errlen) {
   std::string src;
   src += "// sdf2mesh_gb300 per-SDF module\n";
   if (qef) src += "#define S2M_QEF_MODULE 1\n";
+  if (defines) {
+    src += "#define S2M_SELECT 1\n";
+    src += defines;
+  }
   src += kS2mDeviceH;
   src += kS2mLookbackCuh;
   src += kS2mPreludeCuh;
   src += kS2mDcCoreCuh;
   src += s->user_cuda;
   src += kS2mDcKernelsCuh;
-  nvrtcProgram prog;
-  if (nvrtcCreateProgram(&prog, src.c_str(), "s2m_module.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
-    set_err(err, errlen, "nvrtcCreateProgram failed");
-    return S2M_E_NVRTC;
-  }
   std::vector<const char *> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device"};
   if (std::getenv("S2M_NVRTC_LINEINFO")) opts.push_back("-lineinfo");
   opts.push_back((s->flags & S2M_COMPILE_FMAD) ? "--fmad=true" : "--fmad=false");
-  nvrtcResult rc = nvrtcCompileProgram(prog, int(opts.size()), opts.data());
-  if (rc != NVRTC_SUCCESS) {
-    size_t n = 0;
-    nvrtcGetProgramLogSize(prog, &n);
-    std::string log(n, '\0');
-    if (n) nvrtcGetProgramLog(prog, &log[0]);
+  int vmaj = 0, vmin = 0;
+  nvrtcVersion(&vmaj, &vmin);
+  std::string key = "nvrtc " + std::to_string(vmaj) + "." + std::to_string(vmin) + "\n";
+  for (const char *o : opts) key += std::string(o) + "\n";
+  key += src;
+  const std::string dir = module_cache_dir();
+  std::vector<char> cubin;
+  *hit = cache_load(dir, key, cubin);
+  if (!*hit) {
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "s2m_module.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+      set_err(err, errlen, "nvrtcCreateProgram failed");
+      return S2M_E_NVRTC;
+    }
+    nvrtcResult rc = nvrtcCompileProgram(prog, int(opts.size()), opts.data());
+    if (rc != NVRTC_SUCCESS) {
+      size_t n = 0;
+      nvrtcGetProgramLogSize(prog, &n);
+      std::string log(n, '\0');
+      if (n) nvrtcGetProgramLog(prog, &log[0]);
+      nvrtcDestroyProgram(&prog);
+      set_err(err, errlen, std::string("NVRTC: ") + nvrtcGetErrorString(rc) + "\n" + log);
+      return S2M_E_NVRTC;
+    }
+    size_t cubin_n = 0;
+    nvrtcGetCUBINSize(prog, &cubin_n);
+    cubin.resize(cubin_n);
+    nvrtcGetCUBIN(prog, cubin.data());
     nvrtcDestroyProgram(&prog);
-    set_err(err, errlen, std::string("NVRTC: ") + nvrtcGetErrorString(rc) + "\n" + log);
-    return S2M_E_NVRTC;
+    cache_store(dir, key, cubin);
   }
-  size_t cubin_n = 0;
-  nvrtcGetCUBINSize(prog, &cubin_n);
-  std::vector<char> cubin(cubin_n);
-  nvrtcGetCUBIN(prog, cubin.data());
-  nvrtcDestroyProgram(&prog);
   cudaError_t ce = cudaLibraryLoadData(lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (ce != cudaSuccess) {
     set_err(err, errlen, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce));
@@ -244,28 +388,52 @@ int nvrtc_build(const s2m_sdf *s, bool qef, cudaLibrary_t *lib, char *err, size_
 }
 
 int compile_module(s2m_sdf *s, char *err, size_t errlen) {
-  int rc = nvrtc_build(s, false, &s->lib, err, errlen);
-  if (rc != S2M_OK) return rc;
   // Pruned variants are bit-exact only without FMA contraction (their
   // interval bounds and the skipped arithmetic assume separately rounded
   // operations), so an S2M_COMPILE_FMAD module does not use them.
   const bool prune = s->prune_words > 0 && !(s->flags & (S2M_COMPILE_FMAD | S2M_COMPILE_NO_PRUNE));
-  for (int v = 0; v < kNumEvalVariants; ++v) {
-    if (kEvalVariants[v].pruned && !prune) {
-      s->k_eval[v] = nullptr;
-      continue;
+  const auto t0 = std::chrono::steady_clock::now();
+  struct Result {
+    int rc = S2M_OK;
+    bool hit = false;
+    char msg[2048] = {0};
+  };
+  std::vector<Result> res(kNumParts);
+  std::vector<std::thread> th;
+  for (int i = 0; i < kNumParts; ++i) {
+    if (!part_in_module(i, prune)) continue;
+    th.emplace_back([s, i, &res] {
+      res[size_t(i)].rc = nvrtc_build(s, false, kParts[i].defines, &s->libs[i], &res[size_t(i)].hit,
+                                      res[size_t(i)].msg, sizeof res[size_t(i)].msg);
+    });
+  }
+  for (auto &t : th) t.join();
+  s->programs = int(th.size());
+  s->cache_hits = 0;
+  for (int i = 0; i < kNumParts; ++i) {
+    if (!part_in_module(i, prune)) continue;
+    if (res[size_t(i)].rc != S2M_OK) {
+      set_err(err, errlen, res[size_t(i)].msg);
+      return res[size_t(i)].rc;
     }
-    if (cudaLibraryGetKernel(&s->k_eval[v], s->lib, kEvalVariants[v].name) != cudaSuccess) {
+    s->cache_hits += res[size_t(i)].hit ? 1 : 0;
+  }
+  s->compile_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  for (int i = 0; i < kNumParts; ++i) {
+    const int v = kParts[i].variant;
+    if (v < 0 || !part_in_module(i, prune)) continue;
+    if (cudaLibraryGetKernel(&s->k_eval[v], s->libs[i], kEvalVariants[v].name) != cudaSuccess) {
       set_err(err, errlen, std::string("kernel missing from the compiled module: ") + kEvalVariants[v].name);
       return S2M_E_CUDA;
     }
   }
-  if (prune && (cudaLibraryGetKernel(&s->k_tiles, s->lib, "s2m_tiles") != cudaSuccess ||
-                cudaLibraryGetKernel(&s->k_tiles_coarse, s->lib, "s2m_tiles_coarse") != cudaSuccess)) {
+  if (prune && (cudaLibraryGetKernel(&s->k_tiles, s->libs[kPartTilesFine], "s2m_tiles") != cudaSuccess ||
+                cudaLibraryGetKernel(&s->k_tiles_coarse, s->libs[kPartTilesCoarse], "s2m_tiles_coarse") !=
+                    cudaSuccess)) {
     set_err(err, errlen, "kernel missing from the compiled module: s2m_tiles / s2m_tiles_coarse");
     return S2M_E_CUDA;
   }
-  if (cudaLibraryGetKernel(&s->k_vertices, s->lib, "s2m_vertices") != cudaSuccess) {
+  if (cudaLibraryGetKernel(&s->k_vertices, s->libs[kPartVertices], "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
   }
@@ -277,7 +445,8 @@ int ensure_qef_module(const s2m_sdf *cs, char *err, size_t errlen) {
   s2m_sdf *s = const_cast<s2m_sdf *>(cs);
   std::lock_guard<std::mutex> lock(s->qef_mu);
   if (s->k_vertices_qef) return S2M_OK;
-  int rc = nvrtc_build(s, true, &s->qef_lib, err, errlen);
+  bool hit = false;
+  int rc = nvrtc_build(s, true, nullptr, &s->qef_lib, &hit, err, errlen);
   if (rc != S2M_OK) return rc;
   if (cudaLibraryGetKernel(&s->k_vertices_qef, s->qef_lib, "s2m_vertices") != cudaSuccess) {
     set_err(err, errlen, "QEF vertex kernel missing from the compiled module");
@@ -370,7 +539,8 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   m->nzc = j.lag ? int(N) - 1 : int(N);
   // Slab depth.  Full evaluation: the ring of D + 1 lattice planes is sized
   // to stay resident in the 126 MB L2 between the evaluation and the point
-  // bits pass.  An SDF with a tile form: the pruned evaluation writes the
+  // bits pass -- unless the autotuner measured the evaluation at
+  // kDeepSlabNsPerPoint or more, which then runs deep slabs as below.  An SDF with a tile form: the pruned evaluation writes the
   // point bits itself and classification reads only those (and the
   // candidates' corners), so the ring need not fit in L2; deep slabs (a ring
   // of up to 4 GB, slabs of equal depth) amortise each slab's evaluation
@@ -379,7 +549,7 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   int D = int(p.slab_depth);
   if (D <= 0) {
     const double plane_bytes = double(j.plane) * 4.0;
-    if (m->sdf && m->sdf->k_tiles) {
+    if (m->sdf && (m->sdf->k_tiles || m->sdf->deep_slabs)) {
       const int dmax = std::max(1, int(std::min(4.0e9 / plane_bytes, 1.0e9)) - 1);
       const int nz = std::max(1, m->nzc);
       const int ns = (nz + dmax - 1) / dmax;
@@ -469,7 +639,28 @@ size_t prune_layout(s2m_mesh *m) {
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * (words + 1) * 4);  // + each box's flag word
   m->prune_list_off = up16(m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4);  // + each tile's flag word
-  return m->prune_list_off + size_t(chunk_tiles) * 4;
+  size_t end = m->prune_list_off + size_t(chunk_tiles) * 4;
+  // The decided-tile map needs every slab's tile flags at once (a slab's
+  // first cell plane lies on the previous slab's last tile layer).
+  m->use_tmap = ns > 0 && m->prune_chunk >= ns;
+  m->prow_host.clear();
+  if (m->use_tmap) {
+    m->tmap_rows = m->slab_tile_base[size_t(ns)] / (unsigned long long)ntx;
+    m->tmap_wt = int((ntx + 15) / 16);
+    m->prow_host.assign(size_t(m->nzc) + 1, 0u);
+    for (int s = 0; s < ns; ++s) {
+      int k0, nk;
+      slab_planes(m, s, k0, nk);
+      const PruneGeom g = prune_geom(m->job, nk);
+      for (int k = k0; k < k0 + nk; ++k)
+        m->prow_host[size_t(k)] = unsigned(m->slab_tile_base[size_t(s)] / (unsigned long long)ntx +
+                                           (unsigned long long)((k - k0) / g.tzs) * (unsigned long long)ntx);
+    }
+    m->prune_tmap_off = up16(end);
+    m->prune_prow_off = up16(m->prune_tmap_off + size_t(m->tmap_rows) * size_t(m->tmap_wt) * 4);
+    end = m->prune_prow_off + m->prow_host.size() * 4;
+  }
+  return end;
 }
 template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
@@ -511,12 +702,14 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
                                                                         (size_t(m->sdf->prune_words) + 1);
   S2PointBits pb = point_bits(m);
   if (kEvalVariants[v].listed) {
-    const int W1 = m->sdf->prune_words + 1;
-    const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
-    const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
-    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (!m->use_tmap) {  // decided tiles' point bits (with the map, classification reads the map instead)
+      const int W1 = m->sdf->prune_words + 1;
+      const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
+      const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
+      s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
                            (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
     const unsigned *count = prune_list_counts(m) + s;
@@ -538,6 +731,12 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
 // per job.
 size_t vc_ctrl_offsets(size_t vc_tiles) { return 2 + (vc_tiles + 1) / 2; }
 size_t vc_ctrl_words(size_t vc_tiles) { return vc_ctrl_offsets(vc_tiles) + vc_tiles; }
+
+// Scan words of a job (u64): the row-start scan's look-back words, then the
+// quad passes' tile offsets, tile counts (u32, two per word) and base pair.
+size_t scan_status_words(size_t scan_tiles, size_t quad_tiles) {
+  return scan_tiles + quad_tiles + (quad_tiles + 1) / 2 + 2;
+}
 
 // Classification tiles: S2_CW_BLOCK words of 32 cells of one cell plane, nbp
 // per plane, D planes per slab.
@@ -611,7 +810,7 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   b.tris = m->tcap * 12;
   b.rowcnt = N * N * 4;
   b.rowstart = (N * N + 1) * 4;
-  b.scan_status = (m->scan_tiles + m->quad_tiles) * 8;
+  b.scan_status = scan_status_words(m->scan_tiles, m->quad_tiles) * 8;
   b.jobctl = 8 * 8;
   return b;
 }
@@ -622,10 +821,31 @@ void initial_caps(const s2m_mesh *m, const s2m_params &p, unsigned long long &ca
                   unsigned long long &tcap) {
   const unsigned long long N = (unsigned long long)m->N;
   const unsigned long long N3 = N * N * N;
-  cand_cap = std::min(N3, std::max<unsigned long long>(65536, 8 * N * N));
-  vcap = p.max_vertices ? p.max_vertices : std::min(N3, std::max<unsigned long long>(65536, 6 * N * N));
-  tcap = p.max_triangles ? p.max_triangles : std::max<unsigned long long>(131072, 2 * vcap + 4096);
+  double sc = 0, sv = 0, st = 0;
+  if (m->sdf) {
+    std::lock_guard<std::mutex> lock(m->sdf->tune_mu);
+    sc = m->sdf->seen_cand;
+    sv = m->sdf->seen_vert;
+    st = m->sdf->seen_tri;
+  }
+  const double n2 = double(N * N);
+  auto learned = [&](double ratio) { return (unsigned long long)(ratio * n2 * 1.1) + 4096; };
+  cand_cap = std::min(N3, std::max<unsigned long long>({65536, 8 * N * N, learned(sc)}));
+  vcap = p.max_vertices ? p.max_vertices
+                        : std::min(N3, std::max<unsigned long long>({65536, 6 * N * N, learned(sv)}));
+  tcap = p.max_triangles ? p.max_triangles
+                         : std::max<unsigned long long>({131072, 2 * vcap + 4096, learned(st)});
   if (p.max_vertices) cand_cap = std::min(N3, std::max<unsigned long long>(1024, p.max_vertices));
+}
+
+// Remember the surface density of a finished job for the SDF's next jobs.
+void learn_caps(const s2m_mesh *m) {
+  const double n2 = double(m->N) * double(m->N);
+  if (!m->sdf || n2 < 4096.0) return;  // tiny jobs say little about large ones
+  std::lock_guard<std::mutex> lock(m->sdf->tune_mu);
+  m->sdf->seen_cand = std::max(m->sdf->seen_cand, double(m->ncand) / n2);
+  m->sdf->seen_vert = std::max(m->sdf->seen_vert, double(m->nverts) / n2);
+  m->sdf->seen_tri = std::max(m->sdf->seen_tri, double(m->ntris) / n2);
 }
 
 // Host hook for failure tests: when S2M_TEST_FAIL_ALLOC=k is set, the k-th
@@ -665,6 +885,9 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
                             cudaMemcpyHostToDevice, st));
     S2_CUDA(cudaMemcpyAsync(prune_at<unsigned long long>(m, m->prune_cbase_off), m->slab_coarse_base.data(),
                             m->slab_coarse_base.size() * 8, cudaMemcpyHostToDevice, st));
+    if (m->use_tmap)
+      S2_CUDA(cudaMemcpyAsync(prune_at<unsigned>(m, m->prune_prow_off), m->prow_host.data(), m->prow_host.size() * 4,
+                              cudaMemcpyHostToDevice, st));
   }
   S2_CUDA(mesh_malloc((void **)&m->cand_key, b.cand_key, st));
   S2_CUDA(mesh_malloc((void **)&m->cand_val, b.cand_val, st));
@@ -757,7 +980,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   if ((e = cudaMemsetAsync(m->cand_base, 0, size_t(m->nslabs + 1) * 8, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->cand_status, 0, vc_ctrl_offsets(m->vc_tiles) * 8, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(m->rowcnt, 0, N * N * 4, st)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(m->scan_status, 0, (m->scan_tiles + m->quad_tiles) * 8, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(m->scan_status, 0, scan_status_words(m->scan_tiles, m->quad_tiles) * 8, st)) != cudaSuccess)
+    return e;
 
   S2Cand cand;
   cand.key = m->cand_key;
@@ -817,7 +1041,17 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     m->eval_points += double(pts) * nk;
     if (pruned) {
       const int cb = s - s % m->prune_chunk;
-      if (s == cb) S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
+      if (s == cb) {
+        S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
+        if (m->use_tmap) {
+          const unsigned long long words = m->tmap_rows * (unsigned long long)m->tmap_wt;
+          const int ntx = (j.P + S2_PT_XY - 1) / S2_PT_XY;
+          S2_LAUNCH(1, 0, (s2m_tile_map<<<unsigned((words + 255) / 256), 256, 0, st>>>(
+                              prune_at<unsigned>(m, m->prune_bits_off), m->sdf->prune_words + 1, m->tmap_rows, ntx,
+                              m->tmap_wt, prune_at<unsigned>(m, m->prune_tmap_off)),
+                          cudaGetLastError()));
+        }
+      }
       S2_LAUNCH(0, double(pts) * nk, launch_evalp(m, ev, s, cb, st));
     } else {
       void *eargs[] = {&jj, &ring, &k0, &nk};
@@ -832,12 +1066,16 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     const unsigned nbp = cell_tiles_per_plane(m);
     const unsigned ncp = unsigned(zc1 - zc0);
     const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
+    S2TileMap tm{nullptr, nullptr, 0};
+    if (pruned && m->use_tmap)
+      tm = S2TileMap{prune_at<unsigned>(m, m->prune_tmap_off), prune_at<unsigned>(m, m->prune_prow_off), m->tmap_wt};
     S2_LAUNCH(1, ncells, (s2m_cells_mark<<<mg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
                                                                     m->tile_cnt + m->cell_tiles, m->slab_ctrl,
-                                                                    m->cand_base, s, zc0, zc1),
+                                                                    m->cand_base, s, zc0, zc1, tm),
                           cudaGetLastError()));
     S2_LAUNCH(1, 0, (s2m_cells_emit<<<eg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
-                                                               m->cell_words, m->slab_ctrl, cand, c.err, zc0),
+                                                               m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err,
+                                                               zc0, tm),
                      cudaGetLastError()));
   }
   S2Job jj = j;
@@ -879,9 +1117,24 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   const unsigned scan_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->scan_tiles, size_t(sms) * 8)));
   S2_LAUNCH(4, 0, (s2m_rowscan<<<scan_grid, S2_SCAN_BLOCK, 0, st>>>(md, N * N), cudaGetLastError()));
   const unsigned q_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->quad_tiles, size_t(sms) * 8)));
-  S2_LAUNCH(5, 0, (s2m_quads<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, unsigned(m->scan_tiles)), cudaGetLastError()));
+  unsigned long long *qoff = m->scan_status + m->scan_tiles;  // quad scan words (s2m_quads_find ..)
+  unsigned *qcnt = reinterpret_cast<unsigned *>(qoff + m->quad_tiles);
+  unsigned long long *qbase = qoff + m->quad_tiles + (m->quad_tiles + 1) / 2;
+  unsigned *lk0 = reinterpret_cast<unsigned *>(m->cand_pos), *lk1 = reinterpret_cast<unsigned *>(m->cand_nrm);
+  S2_LAUNCH(5, 0, (s2m_quads_find<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, lk0, lk1, qcnt), cudaGetLastError()));
+  S2_LAUNCH(5, 0, (s2m_quads_scan<<<1, 256, 0, st>>>(md, qcnt, qoff, qbase), cudaGetLastError()));
+  S2_LAUNCH(5, 0, (s2m_quads_write<<<q_grid, S2_Q_BLOCK, 0, st>>>(md, lk0, lk1, qoff), cudaGetLastError()));
   return cudaSuccess;
 }
+
+// Deep slabs for full evaluation: a lattice point of a ring that no longer
+// fits in L2 costs 8 more bytes of DRAM traffic (its value written by the
+// evaluation, read back by the point-bit pass), about 0.0012 ns at 6.8 TB/s.
+// An evaluation measured at 0.01 ns per point or more keeps that under 12 %,
+// while the L2-sized ring would cost 4 launches and an evaluation tail per
+// slab of a few planes (at 2048^3 the L2 rule gives one-plane slabs: 8192
+// launches per job).
+constexpr double kDeepSlabNsPerPoint = 0.01;
 
 // Autotuner: time every evaluation variant of the module on the slabs at a
 // quarter, a half and three quarters of the job (into the job's own ring,
@@ -976,6 +1229,7 @@ int autotune_eval(s2m_mesh *m, cudaStream_t st, char *err, size_t errlen) {
   cudaEventDestroy(b);
   sdf->eval_variant = best_v;
   sdf->eval_variant_plain = best_plain_v;
+  sdf->deep_slabs = !kEvalVariants[best_v].pruned && best >= kDeepSlabNsPerPoint;
   return S2M_OK;
 }
 
@@ -1210,6 +1464,14 @@ int s2m_compile_file(const char *path, int lang, const char *sdf_name, uint32_t 
 
 const char *s2m_sdf_cuda_source(const s2m_sdf *sdf) { return sdf ? sdf->user_cuda.c_str() : nullptr; }
 
+int s2m_sdf_compile_info(const s2m_sdf *sdf, double *seconds, int *programs, int *cache_hits) {
+  if (!sdf) return S2M_E_INVALID;
+  if (seconds) *seconds = sdf->compile_s;
+  if (programs) *programs = sdf->programs;
+  if (cache_hits) *cache_hits = sdf->cache_hits;
+  return S2M_OK;
+}
+
 int s2m_sdf_run_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
   if (!sdf) return S2M_E_INVALID;
   if (fp32_ops) *fp32_ops = sdf->run_fp32_ops;
@@ -1269,7 +1531,8 @@ int s2m_sdf_op_counts(const s2m_sdf *sdf, double *fp32_ops, double *sfu_ops) {
 
 void s2m_sdf_free(s2m_sdf *sdf) {
   if (!sdf) return;
-  if (sdf->lib) cudaLibraryUnload(sdf->lib);
+  for (cudaLibrary_t l : sdf->libs)
+    if (l) cudaLibraryUnload(l);
   if (sdf->qef_lib) cudaLibraryUnload(sdf->qef_lib);
   delete sdf;
 }
@@ -1379,7 +1642,13 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
   for (int attempt = 0; attempt < 5; ++attempt) {
     rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen);
     if (rc != S2M_OK) break;
-    if (m->sdf->eval_variant < 0 && (rc = autotune_eval(m, st, err, errlen)) != S2M_OK) break;
+    if (m->sdf->eval_variant < 0) {
+      if ((rc = autotune_eval(m, st, err, errlen)) != S2M_OK) break;
+      const int d0 = m->D;
+      if (!params->slab_depth && setup_job(m, err, errlen) == S2M_OK && m->D != d0 &&
+          (rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen)) != S2M_OK)
+        break;  // the tuned slab depth needs a ring of another size
+    }
     cudaError_t e = enqueue(m, st);
     if (e != cudaSuccess) {
       set_err(err, errlen, std::string("launch: ") + cudaGetErrorString(e));
@@ -1420,6 +1689,7 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
     delete m;
     return rc;
   }
+  learn_caps(m);
   *out = m;
   return S2M_OK;
 }
@@ -1472,11 +1742,12 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   }
   // The rest holds the candidate list and its scan words: 64 bytes per
   // candidate plus 12 bytes of compaction counts and offsets per S2_VC_TILE
-  // candidates and one quad scan word per S2_Q_TILE vertices (vertices never
-  // outnumber candidates).
+  // candidates and 12 bytes of quad tile offset and count per S2_Q_TILE
+  // vertices (vertices never outnumber candidates).
   size_t left = size_t(S2M_NOALLOC_SCRATCH_BYTES) - used;
-  const double per_cand = 64.0 + 12.0 / S2_VC_TILE + 8.0 / S2_Q_TILE;
-  unsigned long long cap = (unsigned long long)((double(left) - 9 * 256.0 - 8.0 * double(m.scan_tiles)) / per_cand);
+  const double per_cand = 64.0 + 12.0 / S2_VC_TILE + 12.0 / S2_Q_TILE;
+  unsigned long long cap =
+      (unsigned long long)((double(left) - 10 * 256.0 - 8.0 * double(m.scan_tiles) - 64.0) / per_cand);
   cap = cap / 1024 * 1024;
   m.cand_cap = cap;
   m.vc_tiles = (cap + S2_VC_TILE - 1) / S2_VC_TILE;
@@ -1486,7 +1757,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   ok = carve(base, used, size_t(cap), &m.cand_key) && carve(base, used, size_t(cap) * 8, &m.cand_val) &&
        carve(base, used, size_t(cap) * 3, &m.cand_pos) && carve(base, used, size_t(cap) * 3, &m.cand_nrm) &&
        carve(base, used, vc_ctrl_words(m.vc_tiles), &m.cand_status) &&
-       carve(base, used, size_t(m.scan_tiles + m.quad_tiles), &m.scan_status);
+       carve(base, used, scan_status_words(m.scan_tiles, m.quad_tiles), &m.scan_status);
   if (!ok || cap == 0) {
     set_err(err, errlen, "no-allocation scratch layout failed");
     return S2M_E_INVALID;

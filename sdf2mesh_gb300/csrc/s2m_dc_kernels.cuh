@@ -96,13 +96,27 @@ __device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restri
 #define S2_EVAL_VARIANT(NAME, MINB, RUN, PAIR)                                                    \
   extern "C" __global__ void __launch_bounds__(S2_EVAL_BLOCK, MINB)                               \
   NAME(S2Job job, float *__restrict__ ring, int k0, int nk) { s2_eval_planes<RUN, PAIR>(job, ring, k0, nk); }
+// Kernel selection: the runtime compiles an SDF's kernels as several NVRTC
+// programs on parallel host threads.  Each program defines S2M_SELECT and the
+// S2M_WANT_* macros of the kernels it holds; a program without S2M_SELECT
+// holds them all.
 // Keep this table in step with kEvalVariants in runtime.cu.
 #ifndef S2M_QEF_MODULE
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVAL_B2R4)
 S2_EVAL_VARIANT(s2m_eval_b2r4, 2, 4, false)
+#endif
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVAL_B3R4)
 S2_EVAL_VARIANT(s2m_eval_b3r4, 3, 4, false)
+#endif
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVAL_B4R4)
 S2_EVAL_VARIANT(s2m_eval_b4r4, 4, 4, false)
+#endif
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVAL_B2V4)
 S2_EVAL_VARIANT(s2m_eval_b2v4, 2, 4, true)
+#endif
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVAL_B3V4)
 S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
+#endif
 #endif
 
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
@@ -127,8 +141,6 @@ struct S2PruneTile {
 // records get NaN for such corners, and the vertex kernel evaluates those
 // exactly, so the mesh does not change.
 #define S2M_TILE_WORDS (S2M_PRUNE_WORDS + 1)
-#define S2_TILE_DECIDED 1u
-#define S2_TILE_POSITIVE 2u
 __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long t, int k0, int nk, int tzs) {
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   S2PruneTile r;
@@ -197,6 +209,7 @@ __device__ __forceinline__ unsigned s2_root_flag(const S2Job &job, s2i root) {
   return 0u;
 }
 
+#if !defined(S2M_SELECT) || defined(S2M_WANT_TILES_COARSE)
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long long *__restrict__ cbase, int s_begin,
                  int s_end, int D, int nzc) {
@@ -228,7 +241,9 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
   dst[S2M_PRUNE_WORDS] = s2_root_flag(job, root);
 }
+#endif  // S2M_WANT_TILES_COARSE
 
+#if !defined(S2M_SELECT) || defined(S2M_WANT_TILES_FINE)
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops,
           const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
@@ -313,6 +328,7 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
     atomicAdd(ops + 1, sfu_ops);
   }
 }
+#endif  // S2M_WANT_TILES_FINE
 
 // Point bits of one warp-wide step of a tile: the 32 lanes hold 8 points
 // along x times 4 rows from `y0` in the plane at ring slot `slot`, so each
@@ -465,9 +481,15 @@ __device__ __forceinline__ void s2_eval_pruned_listed(const S2Job &job, float *_
     s2_eval_pruned<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt);                                  \
   }
 // Keep this table in step with kEvalVariants in runtime.cu.
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVALP_B8)
 S2_EVALP_VARIANT(s2m_evalp_b8, 8, false)
+#endif
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVALPL_B8)
 S2_EVALPL_VARIANT(s2m_evalpl_b8, 8, false)
+#endif
+#if !defined(S2M_SELECT) || defined(S2M_WANT_EVALPL_B8V4)
 S2_EVALPL_VARIANT(s2m_evalpl_b8v4, 8, true)
+#endif
 #endif
 
 
@@ -518,6 +540,7 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // grouped by tile (s2m_vtile_*), so that a warp's evaluations take one path
 // through the pruned SDF.  vc_cnt[t] counts the vertices of candidates
 // t * S2_VC_TILE .. (t + 1) * S2_VC_TILE - 1 (for s2m_vc_scan).
+#if !defined(S2M_SELECT) || defined(S2M_WANT_VERTICES)
 extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK, 8)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
              int nzc, const unsigned *perm, unsigned *vc_cnt) {
@@ -588,3 +611,4 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
     }
   }
 }
+#endif  // S2M_WANT_VERTICES

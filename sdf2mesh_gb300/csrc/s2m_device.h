@@ -97,7 +97,13 @@ struct S2MeshDev {
 // Test hooks (S2MeshDev::hold): a flag that nothing sets, so that a bounded
 // device wait runs out and the run reports S2M_E_TIMEOUT.  Only the waiting
 // is affected; every write stays bounds-checked.
-#define S2_HOLD_QUADS_TILE0 0x1u  /* tile 0 of the quad pass never publishes its prefix */
+#define S2_HOLD_ROWSCAN_TILE0 0x1u  /* tile 0 of the row-start scan never publishes its prefix */
+
+// Flag word of a pruning tile's record (the tile pass): the SDF's interval
+// over the tile's box lies at or beyond +guard (DECIDED | POSITIVE) or -guard
+// (DECIDED), so every point's sign is known and its near-zero bit is 0.
+#define S2_TILE_DECIDED 1u
+#define S2_TILE_POSITIVE 2u
 
 #define S2_ERR_LOOKBACK 0x1u      /* a look-back wait hit its iteration limit   */
 #define S2_ERR_CAND_OVF 0x2u      /* candidate arrays too small                 */

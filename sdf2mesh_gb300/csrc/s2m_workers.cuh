@@ -126,7 +126,11 @@ __device__ __forceinline__ void s2_rowscan_worker(const S2MeshDev &mesh, unsigne
     }
     unsigned pre = s2_block_exclusive(sum, s_warp, &s_total);
     if (warp == 0) {
-      unsigned long long excl = s2_lookback(mesh.scan_status, tile, s_total, mesh.err, mesh.wait_ns);
+      // S2_HOLD_ROWSCAN_TILE0 (tests): tile 0 keeps its status word at 0, so
+      // every later tile's look-back waits until its limit
+      const bool hold = tile == 0 && (mesh.hold & S2_HOLD_ROWSCAN_TILE0);
+      unsigned long long excl =
+          hold ? 0ull : s2_lookback(mesh.scan_status, tile, s_total, mesh.err, mesh.wait_ns);
       if (lane == 0) {
         s_excl = excl;
         if (tile == ntiles - 1) mesh.rowstart[R] = (unsigned)(excl + s_total);
@@ -190,34 +194,68 @@ struct S2Quads {
   unsigned invalid;  // quads dropped
 };
 
-template <bool NC>
-__device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, unsigned v, unsigned long long key) {
-  S2Quads r;
-  r.valid = 0;
-  r.invalid = 0;
+// The neighbour lookups of one vertex's quads: row a = (., y - 1, z) at x and
+// x - 1, row b = (., y, z - 1) at x and x - 1, row c = (., y - 1, z - 1) at
+// x, and (x - 1, y, z) in the vertex's own row; S2_NO_VERTEX where the cell
+// has no vertex or no wanted quad needs the lookup.
+struct S2QuadLookups {
+  unsigned ax, axm1, bx, bxm1, cx, own;
+};
+
+__device__ __forceinline__ unsigned s2_quad_want(unsigned long long key) {
   const int x = (int)(key & 0xffffull), y = (int)((key >> 16) & 0xffffull), z = (int)((key >> 32) & 0xffffull);
   const unsigned s = (unsigned)((key >> 48) & 0xfull);
   const bool b0 = s & 1u, b1 = s & 2u, b2 = s & 4u, b3 = s & 8u;
-  const bool want0 = b0 != b3 && y > 0 && z > 0, want1 = b1 != b3 && x > 0 && z > 0, want2 = b2 != b3 && x > 0 && y > 0;
+  return (b0 != b3 && y > 0 && z > 0 ? 1u : 0u) | (b1 != b3 && x > 0 && z > 0 ? 2u : 0u) |
+         (b2 != b3 && x > 0 && y > 0 ? 4u : 0u);
+}
+
+template <bool NC>
+__device__ __forceinline__ S2QuadLookups s2_quad_lookups(const S2MeshDev &m, int N, unsigned v,
+                                                         unsigned long long key) {
+  const int x = (int)(key & 0xffffull), y = (int)((key >> 16) & 0xffffull), z = (int)((key >> 32) & 0xffffull);
+  const unsigned want = s2_quad_want(key);
+  const S2RowHit none = {S2_NO_VERTEX, S2_NO_VERTEX};
+  const S2RowHit ra = (want & 5u) ? s2_row_find<NC>(m, N, x, y - 1, z) : none;      // (., y - 1, z)
+  const S2RowHit rb = (want & 3u) ? s2_row_find<NC>(m, N, x, y, z - 1) : none;      // (., y, z - 1)
+  const S2RowHit rc = (want & 1u) ? s2_row_find<NC>(m, N, x, y - 1, z - 1) : none;  // (., y - 1, z - 1)
+  S2QuadLookups l;
+  l.ax = ra.x;
+  l.axm1 = ra.xm1;
+  l.bx = rb.x;
+  l.bxm1 = rb.xm1;
+  l.cx = rc.x;
+  l.own = S2_NO_VERTEX;  // (x - 1, y, z): in the vertex's own row, only vertex v - 1 can be it
+  if ((want & 6u) && v > 0) {
+    const unsigned long long kp = s2_ldq<NC>(m.key + v - 1);
+    if (((kp ^ key) & 0x0000ffffffff0000ull) == 0ull && (int)(kp & 0xffffull) == x - 1) l.own = v - 1;
+  }
+  return l;
+}
+
+// Quads of one vertex from its lookups (mesh.rs:280-321).
+__device__ __forceinline__ S2Quads s2_quads_from(const S2QuadLookups &l, unsigned v, unsigned long long key) {
+  S2Quads r;
+  r.valid = 0;
+  r.invalid = 0;
+  const unsigned s = (unsigned)((key >> 48) & 0xfull);
+  const bool b0 = s & 1u, b1 = s & 2u, b2 = s & 4u;
+  const unsigned want = s2_quad_want(key);
   auto put = [&](int qi, unsigned a, unsigned b, unsigned c, unsigned d, bool swap) {
     if (swap) { unsigned t = a; a = d; d = t; t = b; b = c; c = t; }
     r.q[qi][0] = a; r.q[qi][1] = b; r.q[qi][2] = c; r.q[qi][3] = d;
     if (a != S2_NO_VERTEX && b != S2_NO_VERTEX && c != S2_NO_VERTEX && d != S2_NO_VERTEX) r.valid |= 1u << qi;
     else r.invalid++;
   };
-  const S2RowHit none = {S2_NO_VERTEX, S2_NO_VERTEX};
-  const S2RowHit ra = (want0 || want2) ? s2_row_find<NC>(m, N, x, y - 1, z) : none;      // (., y - 1, z)
-  const S2RowHit rb = (want0 || want1) ? s2_row_find<NC>(m, N, x, y, z - 1) : none;      // (., y, z - 1)
-  const S2RowHit rc = want0 ? s2_row_find<NC>(m, N, x, y - 1, z - 1) : none;             // (., y - 1, z - 1)
-  unsigned own = S2_NO_VERTEX;                                                           // (x - 1, y, z)
-  if ((want1 || want2) && v > 0) {
-    const unsigned long long kp = s2_ldq<NC>(m.key + v - 1);
-    if (((kp ^ key) & 0x0000ffffffff0000ull) == 0ull && (int)(kp & 0xffffull) == x - 1) own = v - 1;
-  }
-  if (want0) put(0, rc.x, rb.x, v, ra.x, b0);
-  if (want1) put(1, rb.xm1, rb.x, v, own, !b1);
-  if (want2) put(2, ra.xm1, ra.x, v, own, b2);
+  if (want & 1u) put(0, l.cx, l.bx, v, l.ax, b0);
+  if (want & 2u) put(1, l.bxm1, l.bx, v, l.own, !b1);
+  if (want & 4u) put(2, l.axm1, l.ax, v, l.own, b2);
   return r;
+}
+
+template <bool NC>
+__device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, unsigned v, unsigned long long key) {
+  return s2_quads_from(s2_quad_lookups<NC>(m, N, v, key), v, key);
 }
 
 template <bool NC>
@@ -272,10 +310,7 @@ __device__ __forceinline__ void s2_quads_worker(const S2Job &job, const S2MeshDe
     }
     __syncthreads();
     if (warp == 0) {
-      // S2_HOLD_QUADS_TILE0 (tests): tile 0 keeps its status word at 0, so every
-      // later tile's look-back waits until its limit
-      const bool hold = tile == 0 && (mesh.hold & S2_HOLD_QUADS_TILE0);
-      unsigned long long excl = hold ? 0ull : s2_lookback(status, tile, s_total, mesh.err, mesh.wait_ns);
+      unsigned long long excl = s2_lookback(status, tile, s_total, mesh.err, mesh.wait_ns);
       if (lane == 0) {
         s_excl = excl;
         if (tile == ntiles - 1) *mesh.ntris = excl + s_total;

@@ -135,10 +135,10 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
     const int tx = 4 * w + b;
     if (tx >= ntx) break;
     const unsigned flag = __ldg(tiles + (trow + tx) * tile_words + (tile_words - 1));
-    if (!(flag & 1u)) continue;  // S2_TILE_DECIDED
+    if (!(flag & S2_TILE_DECIDED)) continue;
     const unsigned bits = (1u << min(8, job.P - 8 * tx)) - 1u;
     unk |= bits << (8 * b);
-    if (flag & 2u) pos |= bits << (8 * b);  // S2_TILE_POSITIVE
+    if (flag & S2_TILE_POSITIVE) pos |= bits << (8 * b);
   }
   const int kb = k0 + (int)blockIdx.y * tzs, ke = min(kb + tzs, k0 + nk);
   const long long plane = (long long)job.P * WP;
@@ -152,6 +152,58 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
     o += plane;
     if (o >= wrap) o -= wrap;
   }
+}
+
+// Decided-tile map of a job with tile pruning, when every slab's tile records
+// stay resident: 2 bits per pruning tile -- S2_TILE_DECIDED at bit 2b,
+// S2_TILE_POSITIVE at bit 2b + 1 of word b / 16 -- in rows of the job's tiles
+// along x (`wt` words per row; tile t of the job is in row t / ntx at x tile
+// t % ntx, since every slab holds whole rows).  prow[k] is the row of
+// lattice plane k's tile layer at y tile 0, so the tile of point (x, y, k) is
+// at row prow[k] + y / 8, x tile x / 8.  Classification reads decided tiles'
+// bits from here instead of point-bit planes, so nothing writes those planes
+// for decided tiles (map == null: s2m_fill_decided wrote them).
+struct S2TileMap {
+  const unsigned *map;
+  const unsigned *prow;
+  int wt;
+};
+
+// One thread per map word: the flag words of 16 tiles of a row.
+__global__ void __launch_bounds__(256) s2m_tile_map(const unsigned *__restrict__ tiles, int tile_words,
+                                                    unsigned long long rows, int ntx, int wt,
+                                                    unsigned *__restrict__ map) {
+  const unsigned long long q = (unsigned long long)blockIdx.x * 256u + threadIdx.x;
+  if (q >= rows * (unsigned long long)wt) return;
+  const unsigned long long row = q / (unsigned)wt;
+  const int wq = (int)(q - row * (unsigned)wt);
+  unsigned out = 0u;
+#pragma unroll 4
+  for (int b = 0; b < 16; ++b) {
+    const int tx = 16 * wq + b;
+    if (tx >= ntx) break;
+    const unsigned flag = __ldg(tiles + (row * (unsigned)ntx + (unsigned)tx) * (unsigned)tile_words + (tile_words - 1));
+    if (flag & S2_TILE_DECIDED) out |= (1u | ((flag & S2_TILE_POSITIVE) ? 2u : 0u)) << (2 * b);
+  }
+  map[q] = out;
+}
+
+// The map's bits of tiles 4w .. 4w + 4 (the points of word w of a point row
+// and the first point of word w + 1): bits 2b, 2b + 1 of tile 4w + b.
+__device__ __forceinline__ unsigned s2_map_bits(const S2TileMap &tm, int k, int y, int w, bool more) {
+  const unsigned *mw = tm.map + ((unsigned long long)__ldg(tm.prow + k) + (unsigned)(y >> 3)) * (unsigned)tm.wt +
+                       (unsigned)(w >> 2);
+  const unsigned lo = __ldg(mw);
+  const unsigned hi = ((w & 3) == 3 && more) ? __ldg(mw + 1) : 0u;  // tile 4w + 4 in the next map word
+  return __funnelshift_r(lo, hi, 8 * (w & 3)) & 0x3ffu;
+}
+
+// A 32-point mask from the map bits of 4 tiles (sel 0: decided, 1: positive):
+// the 4 bits are spread to the bytes' low bits, then each byte filled.
+__device__ __forceinline__ unsigned s2_map_points(unsigned e, int sel) {
+  const unsigned x = (e >> sel) & 0x55u;  // bits 0, 2, 4, 6
+  const unsigned nib = (x & 1u) | ((x >> 1) & 2u) | ((x >> 2) & 4u) | ((x >> 3) & 8u);
+  return ((nib * 0x00204081u) & 0x01010101u) * 0xffu;
 }
 
 // Cell words and tiles of a slab: word yw = y * WN + w of cell plane dz
@@ -171,7 +223,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
                                                             unsigned *__restrict__ words, unsigned *tile_cnt,
                                                             unsigned *done, unsigned long long *__restrict__ tile_off,
                                                             unsigned long long *base, int slab_index, int zc0,
-                                                            int zc1) {
+                                                            int zc1, S2TileMap tm) {
   __shared__ unsigned s_cnt[S2_MARK_PLANES][S2_CW_BLOCK / 32];
   const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + threadIdx.x);
@@ -204,17 +256,40 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
     }
     const int dw = more ? 1 : 0;
     unsigned pw[S2_MARK_PLANES + 1][4], nw[S2_MARK_PLANES + 1][4];
+    if (tm.map) {
+      // Decided tiles' points from the map (sign from the flag, near-zero 0);
+      // the point-bit words are read only where a tile of the word is
+      // undecided, and only the undecided tiles' bytes of them are used.
 #pragma unroll
-    for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-      pw[p][0] = __ldg(pb.pos + rb[p]);
-      pw[p][1] = __ldg(pb.pos + rb[p] + dw);
-      pw[p][2] = __ldg(pb.pos + rb[p] + WP);
-      pw[p][3] = __ldg(pb.pos + rb[p] + WP + dw);
-      if (nearrule) {
-        nw[p][0] = __ldg(pb.near + rb[p]);
-        nw[p][1] = __ldg(pb.near + rb[p] + dw);
-        nw[p][2] = __ldg(pb.near + rb[p] + WP);
-        nw[p][3] = __ldg(pb.near + rb[p] + WP + dw);
+      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+        const int k = zc0 + dz0 + min(p, ncp);  // the plane of rb[p]
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const unsigned e = s2_map_bits(tm, k, y + r, w, more);
+          const unsigned dec = s2_map_points(e, 0), posd = s2_map_points(e, 1);
+          const bool decn = (e >> 8) & 1u, posn = (e >> 9) & 1u;  // first point of word w + 1
+          const long long o = rb[p] + (long long)r * WP;
+          pw[p][2 * r] = (dec == ~0u ? 0u : (__ldg(pb.pos + o) & ~dec)) | posd;
+          pw[p][2 * r + 1] = decn ? (posn ? 1u : 0u) : __ldg(pb.pos + o + dw);  // only its bit 0 is used
+          if (nearrule) {
+            nw[p][2 * r] = dec == ~0u ? 0u : (__ldg(pb.near + o) & ~dec);
+            nw[p][2 * r + 1] = decn ? 0u : __ldg(pb.near + o + dw);
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+        pw[p][0] = __ldg(pb.pos + rb[p]);
+        pw[p][1] = __ldg(pb.pos + rb[p] + dw);
+        pw[p][2] = __ldg(pb.pos + rb[p] + WP);
+        pw[p][3] = __ldg(pb.pos + rb[p] + WP + dw);
+        if (nearrule) {
+          nw[p][0] = __ldg(pb.near + rb[p]);
+          nw[p][1] = __ldg(pb.near + rb[p] + dw);
+          nw[p][2] = __ldg(pb.near + rb[p] + WP);
+          nw[p][3] = __ldg(pb.near + rb[p] + WP + dw);
+        }
       }
     }
 #pragma unroll
@@ -283,13 +358,15 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
                                                             const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
-                                                            S2Cand cand, unsigned *err, int zc0) {
+                                                            const unsigned *__restrict__ tile_cnt, S2Cand cand,
+                                                            unsigned *err, int zc0, S2TileMap tm) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const int WN = (job.N + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + tid);
   const int dz = (int)blockIdx.y;
+  if (__ldg(tile_cnt + (unsigned long long)dz * gridDim.x + blockIdx.x) == 0u) return;  // the whole tile: no candidate
   const unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
@@ -331,8 +408,25 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
       continue;
     }
     float v[8];
-    s2_load_corners<false>(job, ring, cell, v);
-    if (unk) {  // corners of decided tiles: no value in the ring
+    if (tm.map) {  // corners of decided tiles: no value in the ring, NaN in the record
+      unsigned dec = 0u;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
+        const unsigned *row = tm.map + ((unsigned long long)__ldg(tm.prow + cell.z + (q >> 1)) +
+                                        (unsigned)((cell.y + (q & 1)) >> 3)) * (unsigned)tm.wt;
+        const int t0 = cell.x >> 3, t1 = (cell.x + 1) >> 3;
+        dec |= ((__ldg(row + (t0 >> 4)) >> (2 * (t0 & 15))) & 1u) << (2 * q);
+        dec |= ((__ldg(row + (t1 >> 4)) >> (2 * (t1 & 15))) & 1u) << (2 * q + 1);
+      }
+      const float *p0 = ring + (long long)(cell.z % job.ring) * job.plane + (long long)cell.y * job.pitch + cell.x;
+      const float *p1 = ring + (long long)((cell.z + 1) % job.ring) * job.plane + (long long)cell.y * job.pitch + cell.x;
+      const float *pc[8] = {p0, p0 + 1, p0 + job.pitch, p0 + job.pitch + 1, p1, p1 + 1, p1 + job.pitch, p1 + job.pitch + 1};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = ((dec >> k) & 1u) ? __int_as_float(0x7fc00000) : __ldg(pc[k]);
+    } else {
+      s2_load_corners<false>(job, ring, cell, v);
+    }
+    if (unk && !tm.map) {  // corners of decided tiles: no value in the ring
       const bool more = w + 1 < WP;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
@@ -526,6 +620,134 @@ __global__ void __launch_bounds__(S2_SCAN_BLOCK) s2m_rowscan(S2MeshDev mesh, uns
 
 __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads(S2Job job, S2MeshDev mesh, unsigned scan_tiles) {
   s2_quads_worker<true>(job, mesh, scan_tiles, blockIdx.x == 0);
+}
+
+// Quads of the per-job pipeline in three passes that never wait on one
+// another (the look-back of s2m_quads made every tile's block wait at a
+// barrier while its first warp walked back over tiles still searching):
+//   s2m_quads_find   each vertex's neighbour lookups -- the row searches --
+//                    stored as 6 words per vertex in the candidates' position
+//                    and normal arrays (free once s2m_vcompact has copied the
+//                    vertices out; the vertices never outnumber the
+//                    candidates), each tile's triangle count, the invalid
+//                    quads (mesh.rs:275-277)
+//   s2m_quads_scan   one block: each tile's first triangle and the total
+//   s2m_quads_write  each tile's triangles from the stored lookups, at its
+//                    first triangle, in vertex order (mesh.rs:280-321)
+// Tiles of S2_Q_TILE vertices, S2_Q_VPT per thread (v = tile * S2_Q_TILE +
+// m * S2_Q_BLOCK + thread), as s2m_quads; quad scan words: tile offsets
+// (u64), then tile counts (u32), then the base pair (u64).
+__global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_find(S2Job job, S2MeshDev mesh, unsigned *__restrict__ lk0,
+                                                           unsigned *__restrict__ lk1, unsigned *__restrict__ tcnt) {
+  __shared__ unsigned s_red[S2_Q_BLOCK / 32];
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const unsigned long long V = *mesh.vtotal;
+  if (V > mesh.vcap) return;  // vertex overflow: the host re-runs with larger buffers
+  const unsigned ntiles = (unsigned)((V + S2_Q_TILE - 1) / S2_Q_TILE);
+  unsigned invalid = 0;
+  for (unsigned tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    unsigned cnt = 0;
+#pragma unroll
+    for (int m = 0; m < S2_Q_VPT; ++m) {
+      const unsigned long long v = (unsigned long long)tile * S2_Q_TILE + m * S2_Q_BLOCK + tid;
+      if (v >= V) continue;
+      const unsigned long long key = __ldg(mesh.key + v);
+      const S2QuadLookups l = s2_quad_lookups<true>(mesh, job.N, (unsigned)v, key);
+      const S2Quads q = s2_quads_from(l, (unsigned)v, key);
+      cnt += 2u * __popc(q.valid);
+      invalid += q.invalid;
+      lk0[3 * v] = l.ax;
+      lk0[3 * v + 1] = l.axm1;
+      lk0[3 * v + 2] = l.bx;
+      lk1[3 * v] = l.bxm1;
+      lk1[3 * v + 1] = l.cx;
+      lk1[3 * v + 2] = l.own;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(S2_FULL, cnt, o);
+    if (lane == 0) s_red[warp] = cnt;
+    __syncthreads();
+    if (tid == 0) {
+      unsigned t = 0;
+#pragma unroll
+      for (int k = 0; k < S2_Q_BLOCK / 32; ++k) t += s_red[k];
+      tcnt[tile] = t;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) invalid += __shfl_xor_sync(S2_FULL, invalid, o);
+  if (lane == 0 && invalid) atomicAdd(mesh.invalid, (unsigned long long)invalid);
+}
+
+__global__ void __launch_bounds__(256) s2m_quads_scan(S2MeshDev mesh, const unsigned *tcnt,
+                                                      unsigned long long *toff, unsigned long long *tbase) {
+  const unsigned long long V = *mesh.vtotal;
+  if (V > mesh.vcap) return;
+  const unsigned ntiles = (unsigned)((V + S2_Q_TILE - 1) / S2_Q_TILE);
+  s2_scan_tiles<256, 16>(tcnt, ntiles, toff, tbase, 0);
+  if (threadIdx.x == 0) *mesh.ntris = tbase[1];  // written by this thread in the scan
+}
+
+__global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_write(S2MeshDev mesh, const unsigned *__restrict__ lk0,
+                                                            const unsigned *__restrict__ lk1,
+                                                            const unsigned long long *__restrict__ toff) {
+  __shared__ unsigned s_warp[32];
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const unsigned long long V = *mesh.vtotal;
+  if (V > mesh.vcap) return;
+  const unsigned ntiles = (unsigned)((V + S2_Q_TILE - 1) / S2_Q_TILE);
+  for (unsigned tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    S2Quads qd[S2_Q_VPT];
+    unsigned ntri[S2_Q_VPT];
+#pragma unroll
+    for (int m = 0; m < S2_Q_VPT; ++m) {
+      const unsigned long long v = (unsigned long long)tile * S2_Q_TILE + m * S2_Q_BLOCK + tid;
+      qd[m].valid = 0;
+      if (v < V) {
+        S2QuadLookups l;
+        l.ax = __ldg(lk0 + 3 * v);
+        l.axm1 = __ldg(lk0 + 3 * v + 1);
+        l.bx = __ldg(lk0 + 3 * v + 2);
+        l.bxm1 = __ldg(lk1 + 3 * v);
+        l.cx = __ldg(lk1 + 3 * v + 1);
+        l.own = __ldg(lk1 + 3 * v + 2);
+        qd[m] = s2_quads_from(l, (unsigned)v, __ldg(mesh.key + v));
+      }
+      ntri[m] = 2u * __popc(qd[m].valid);
+      unsigned inc = ntri[m];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
+        if ((int)lane >= o) inc += t;
+      }
+      if (lane == 31) s_warp[m * (S2_Q_BLOCK / 32) + warp] = inc;
+      ntri[m] = inc - ntri[m];  // exclusive within the warp
+    }
+    if (tid < 32 - S2_Q_VPT * (S2_Q_BLOCK / 32)) s_warp[S2_Q_VPT * (S2_Q_BLOCK / 32) + tid] = 0u;
+    __syncthreads();
+    if (warp == 0) s2_warp_exclusive32(s_warp);
+    __syncthreads();
+    const unsigned long long first = toff[tile];
+#pragma unroll
+    for (int m = 0; m < S2_Q_VPT; ++m) {
+      unsigned long long t = first + s_warp[m * (S2_Q_BLOCK / 32) + warp] + ntri[m];
+      for (int qi = 0; qi < 3; ++qi) {
+        if (!((qd[m].valid >> qi) & 1u)) continue;
+        const unsigned *q = qd[m].q[qi];
+        if (t + 2 > mesh.tcap) {
+          atomicOr(mesh.err, S2_ERR_TRI_OVF);
+          t += 2;
+          continue;
+        }
+        unsigned *o = mesh.tris + 3 * t;
+        o[0] = q[2]; o[1] = q[1]; o[2] = q[0];
+        o[3] = q[0]; o[4] = q[3]; o[5] = q[2];
+        t += 2;
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // FP32 issue-rate probe: 8 independent dependent chains per thread of

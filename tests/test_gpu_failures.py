@@ -3,8 +3,8 @@
 The reference panics when a device step fails (main.rs:184, 196,
 texture.rs:110).  Here every device wait is bounded and reports a status:
 
-  * the look-back of the ordered compactions: a test hook (S2M_TEST_HOLD=1)
-    keeps tile 0 of the quad pass from publishing its prefix -- a flag that
+  * the look-back of the ordered scans: a test hook (S2M_TEST_HOLD=1) keeps
+    tile 0 of the row-start scan from publishing its prefix -- a flag that
     nothing sets -- so every later tile's wait runs out after the mesh's
     wait limit; the run returns S2M_E_TIMEOUT and the next run on the same
     handle is bit-exact again;

@@ -87,7 +87,7 @@ def test_cli_debug_cuda(lib, tmp_path):
     cuda = dbg.read_text()
     assert "s2m_user_sdf" in cuda and "letter_r_arc" in cuda
     sdf = s2m.Sdf3DShader.from_source(reference_example("martin_cube.sdf3d")).compile()
-    assert cuda == sdf.cuda_source()
+    assert cuda == sdf.cuda_source
     text = out.read_text()
     assert text.startswith("solid\n") and text.endswith("endsolid\n")
     assert np.isfinite([float(t) for t in text.split() if t[:1].isdigit() or t[:1] == "-"]).all()

@@ -49,8 +49,8 @@ def test_footprint_covers_pool_use(lib, case):
         src, _ = workloads.torus()
         sdf = s2m.Sdf3DShader.from_source(src).compile()
         state = s2m.AppState(resolution=200, bounds=2.0, max_vertices=1 << 20, max_triangles=3 << 20)
-    fp = s2m.mesh_footprint(sdf, state)
     s2m.generate(sdf, s2m.AppState(resolution=32, bounds=2.0))  # library and pool initialised
+    fp = s2m.mesh_footprint(sdf, state)
     used0 = pool_used()
     dm = s2m.mesh_device(sdf, state)
     used = pool_used() - used0

@@ -16,7 +16,7 @@ import pytest
 import oracle
 import sdf2mesh_gb300 as s2m
 from sdf2mesh_gb300 import workloads
-from tests.parity import assert_bit_exact, compare_with_ties, keys_of
+from tests.parity import assert_bit_exact, compare_with_ties, keys_of, same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -176,7 +176,7 @@ def test_csg64_1024_full_size(lib, oracle_lib):
         assert np.array_equal(gpu.cell_xyz[sel], ref.cell)
         assert np.array_equal(gpu.signs[sel], ref.signs)
         assert np.array_equal(gpu.positions[sel].view(np.uint32), ref.pos.astype(np.float32).view(np.uint32))
-        assert np.array_equal(gpu.normals[sel].view(np.uint32), ref.nrm.astype(np.float32).view(np.uint32))
+        assert same_bits(gpu.normals[sel], ref.nrm).all()
         return ref
 
     assert window_matches(500, 503).nverts > 0
@@ -214,11 +214,18 @@ def csg64_seed1(lib):
     return s2m.Sdf3DShader.from_source(src).compile(), prm
 
 
+@pytest.fixture(scope="module")
+def csg64_seed1_full(lib):
+    src, prm = workloads.csg64(seed=1)
+    return s2m.Sdf3DShader.from_source(src).compile(prune=False), prm
+
+
 @pytest.mark.parametrize("variant", range(s2m.EVAL_VARIANTS))
-def test_eval_variants_identical(csg64_seed1, variant):
+def test_eval_variants_identical(csg64_seed1, csg64_seed1_full, variant):
     """Every evaluation-kernel variant the autotuner may pick (5 to 7: tile
-    pruned) gives the same bits."""
-    sdf, prm = csg64_seed1
+    pruned) gives the same bits.  The full-evaluation run-of-4 variants (3, 4)
+    are compiled only into modules without pruning."""
+    sdf, prm = csg64_seed1_full if variant in (3, 4) else csg64_seed1
     sdf.set_eval_variant(variant)
     gpu = run(sdf, 96)
     assert sdf.eval_variant()[0] == sdf.eval_variants()[variant][0]
@@ -231,7 +238,10 @@ def test_autotuner_picks_a_variant(lib):
     assert sdf.eval_variant()[0] == "untuned"
     run(sdf, 512)  # large enough for the tuner to time (>= 2e6 points per trial)
     name, ns = sdf.eval_variant()
-    assert name.startswith("s2m_eval") and all(x > 0 for x in ns)
+    # every variant of the module was timed; a pruned module holds no
+    # full-evaluation run-of-4 variants (3, 4)
+    assert name.startswith("s2m_eval") and all(x > 0 for v, x in enumerate(ns) if v not in (3, 4))
+    assert ns[3] == 0 and ns[4] == 0
 
 
 # ---------------------------------------------------------------------------
