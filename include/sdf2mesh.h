@@ -360,18 +360,26 @@ void s2m_batch_free(s2m_batch *b);
 /* ---- serving: continuous batching ---------------------------------------
    No reference counterpart.  A request loop on its own host threads:
    requests (CSG programs, or compiled SDFs) from any thread are admitted in
-   arrival order while their device footprint fits memory_budget_bytes and
-   fewer than max_inflight persistent launches run; each admitted group is one
-   launch on its own stream, so requests that arrive while others are on the
-   GPU start as soon as a slot and memory free up and overlap with them.
-   Compiled-SDF requests run the per-job pipeline on a third stream.
-   Latency = completion - submission (host clock). */
+   arrival order while their device footprint fits memory_budget_bytes.  CSG
+   programs run on the batch interpreter: fewer than max_inflight persistent
+   launches at a time, each admitted group one launch on its own stream, so
+   requests that arrive while others are on the GPU start as soon as a slot
+   and memory free up and overlap with them.  Compiled-SDF requests run the
+   per-job pipeline on sdf_workers host threads, each with its own stream, so
+   several jobs share the GPU at once.
+   Sources (s2m_server_submit_source) are tiered: a CSG source whose compiled
+   module is not ready yet runs on the interpreter while a background thread
+   compiles it; its later requests run the compiled module (tile-pruned
+   per-job pipeline).  Latency = completion - submission (host clock). */
 typedef struct s2m_server s2m_server;
+#define S2M_SERVER_INTERPRET_ONLY 0x1u  /* CSG sources always on the interpreter (no background compile) */
 typedef struct {
   uint64_t memory_budget_bytes;  /* admission limit; 0 = none                         */
   uint32_t max_inflight;         /* concurrent persistent launches (default 2)        */
   uint32_t max_batch_jobs;       /* requests per launch (default 1024)                */
   uint32_t keep_results;         /* 1: meshes stay on the device until s2m_server_release */
+  uint32_t sdf_workers;          /* per-job pipelines at once, one stream each (default 4) */
+  uint32_t flags;                /* S2M_SERVER_*                                      */
   uint32_t reserved;
 } s2m_server_config;
 typedef struct {
@@ -379,16 +387,22 @@ typedef struct {
   double p50_ms, p99_ms, mean_ms;   /* latency of completed requests            */
   double span_s;                    /* first submission to last completion      */
   double meshes_per_s, gvoxels_per_s;
+  uint64_t ran_compiled;            /* completed on a compiled module (per-job pipeline) */
+  uint64_t ran_interpreted;         /* completed on the batch interpreter          */
+  uint64_t compiled_sources;        /* sources whose module is ready               */
+  uint64_t compiles_pending;        /* sources queued for or in background compilation */
 } s2m_server_stats;
 int s2m_server_create(const s2m_server_config *cfg, s2m_server **out, char *err, size_t errlen);
 int s2m_server_submit_csg(s2m_server *s, const float *program, uint32_t len, const s2m_params *params,
                           uint64_t *request_id, char *err, size_t errlen);
 int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *params, uint64_t *request_id,
                           char *err, size_t errlen);
-/* A request as source text, the reference's plugin surface: WGSL whose sdf3d
-   is a CSG expression (s2m_csg_from_source) runs on the batch interpreter;
-   any other source is compiled once (cached by its text) and runs the
-   per-job pipeline. */
+/* A request as source text, the reference's plugin surface.  WGSL whose
+   sdf3d is a CSG expression (s2m_csg_from_source) runs on the batch
+   interpreter until the background compile of its text finishes (unless
+   S2M_SERVER_INTERPRET_ONLY), then on its compiled module; any other source
+   is compiled once, in the call (cached by its text), and runs the per-job
+   pipeline. */
 int s2m_server_submit_source(s2m_server *s, const char *source, int lang, const char *sdf_name,
                              const s2m_params *params, uint64_t *request_id, char *err, size_t errlen);
 /* S2M_OK once the request completed, S2M_E_TIMEOUT if it has not yet, or its error. */

@@ -81,14 +81,20 @@ NOALLOC_MAX_RESOLUTION = 256
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
-                ("max_batch_jobs", ctypes.c_uint32), ("keep_results", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("max_batch_jobs", ctypes.c_uint32), ("keep_results", ctypes.c_uint32),
+                ("sdf_workers", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+SERVER_INTERPRET_ONLY = 0x1
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("batches", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64), ("p50_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double), ("span_s", ctypes.c_double),
-                ("meshes_per_s", ctypes.c_double), ("gvoxels_per_s", ctypes.c_double)]
+                ("meshes_per_s", ctypes.c_double), ("gvoxels_per_s", ctypes.c_double),
+                ("ran_compiled", ctypes.c_uint64), ("ran_interpreted", ctypes.c_uint64),
+                ("compiled_sources", ctypes.c_uint64), ("compiles_pending", ctypes.c_uint64)]
 
 
 KERNEL_KINDS = ("eval_planes", "cells", "vertices", "vcompact", "rowscan", "quads")
@@ -625,8 +631,9 @@ class Server:
     compiled SDFs from any thread; results complete asynchronously."""
 
     def __init__(self, memory_budget_bytes: int = 0, max_inflight: int = 2, max_batch_jobs: int = 1024,
-                 keep_results: bool = True):
-        cfg = ServerConfig(memory_budget_bytes, max_inflight, max_batch_jobs, 1 if keep_results else 0, 0)
+                 keep_results: bool = True, sdf_workers: int = 4, interpret_only: bool = False):
+        cfg = ServerConfig(memory_budget_bytes, max_inflight, max_batch_jobs, 1 if keep_results else 0, sdf_workers,
+                           SERVER_INTERPRET_ONLY if interpret_only else 0, 0)
         self._h = ctypes.c_void_p()
         err = _errbuf()
         _check(load_library().s2m_server_create(ctypes.byref(cfg), ctypes.byref(self._h), err, len(err)), err,

@@ -1087,6 +1087,7 @@ void s2m_batch_free(s2m_batch *b) {
 #include <deque>
 #include <map>
 #include <memory>
+#include <set>
 #include <thread>
 
 namespace {
@@ -1155,13 +1156,21 @@ struct s2m_server {
   std::vector<double> latencies_ms;
   bool stop = false;
   int inflight = 0;
+  uint64_t ran_compiled = 0, ran_interpreted = 0;
   cudaStream_t streams[2] = {nullptr, nullptr};
-  cudaStream_t sdf_stream = nullptr;
-  std::thread worker, sdf_worker;
+  std::vector<cudaStream_t> sdf_streams;  // one per per-job worker
+  std::thread worker;
+  std::vector<std::thread> sdf_workers;
   int device = 0;
-  // sources that are not CSG programs, compiled once (keyed by language, name, text)
+  // compiled sources (keyed by language, name, text): non-CSG sources compiled
+  // in the submitting call, CSG sources by the background compiler
   std::mutex compile_mu;
+  std::condition_variable compile_cv;
   std::map<std::string, s2m_sdf *> compiled;
+  std::deque<std::string> compile_queue;
+  std::set<std::string> compile_pending, compile_failed;
+  bool compile_stop = false;
+  std::thread compiler;
 };
 
 namespace {
@@ -1197,6 +1206,7 @@ void server_complete_locked(s2m_server *s, SReq &r, int status, const std::strin
   if (status == S2M_OK) {
     r.state = 2;
     ++s->completed;
+    ++(r.kind == 1 ? s->ran_compiled : s->ran_interpreted);
     s->latencies_ms.push_back((r.t_done - r.t_submit) * 1e3);
     s->voxels_done += double(r.info.cells);
   } else {
@@ -1315,8 +1325,12 @@ void server_loop(s2m_server *s) {
   }
 }
 
-void server_sdf_loop(s2m_server *s) {
+// One per-job worker: takes compiled-SDF requests in arrival order while
+// their footprint fits the budget and runs each on its own stream, so the
+// workers' jobs overlap on the device.
+void server_sdf_loop(s2m_server *s, int worker) {
   cudaSetDevice(s->device);
+  cudaStream_t stream = s->sdf_streams[size_t(worker)];
   std::unique_lock<std::mutex> lk(s->mu);
   char err[1024];
   while (true) {
@@ -1340,7 +1354,7 @@ void server_sdf_loop(s2m_server *s) {
     s2m_params p = r0.params;
     lk.unlock();
     s2m_mesh *m = nullptr;
-    int rc = s2m_mesh_create(sdf, &p, s->sdf_stream, &m, err, sizeof err);
+    int rc = s2m_mesh_create(sdf, &p, stream, &m, err, sizeof err);
     lk.lock();
     SReq &r = s->reqs[id];
     if (rc == S2M_OK) {
@@ -1349,6 +1363,49 @@ void server_sdf_loop(s2m_server *s) {
     }
     server_complete_locked(s, r, rc, rc == S2M_OK ? "" : err);
     s->done_cv.notify_all();
+  }
+}
+
+// The background compiler of CSG sources (tiering): each queued key is
+// compiled once; its later requests then run on the compiled module.
+void server_compile_loop(s2m_server *s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->compile_mu);
+  char err[4096];
+  while (true) {
+    if (s->compile_queue.empty()) {
+      if (s->compile_stop) break;
+      s->compile_cv.wait_for(lk, std::chrono::milliseconds(5));
+      continue;
+    }
+    if (s->compile_stop) break;
+    const std::string key = s->compile_queue.front();
+    s->compile_queue.pop_front();
+    lk.unlock();
+    // key: language, NUL, function name, NUL, source
+    const size_t a = key.find('\0'), b = key.find('\0', a + 1);
+    const int lang = std::atoi(key.substr(0, a).c_str());
+    const std::string name = key.substr(a + 1, b - a - 1), source = key.substr(b + 1);
+    std::string text = source;
+    s2m_sdf *sdf = nullptr;
+    int rc = S2M_OK;
+    if (lang == S2M_LANG_WGSL) {
+      char *pre = nullptr;
+      rc = s2m_preprocess_source(source.c_str(), nullptr, &pre, err, sizeof err);
+      if (rc == S2M_OK) {
+        text = pre;
+        s2m_free_string(pre);
+      }
+    }
+    if (rc == S2M_OK) rc = s2m_compile(text.c_str(), lang, name.c_str(), 0, &sdf, err, sizeof err);
+    lk.lock();
+    s->compile_pending.erase(key);
+    if (rc == S2M_OK && sdf) {
+      auto ins = s->compiled.emplace(key, sdf);
+      if (!ins.second) s2m_sdf_free(sdf);
+    } else {
+      s->compile_failed.insert(key);  // stays on the interpreter
+    }
   }
 }
 
@@ -1384,9 +1441,20 @@ int s2m_server_create(const s2m_server_config *cfg, s2m_server **out, char *err,
       delete s;
       return S2M_E_CUDA;
     }
-  cudaStreamCreateWithFlags(&s->sdf_stream, cudaStreamNonBlocking);
+  if (s->cfg.sdf_workers == 0) s->cfg.sdf_workers = 4;
+  s->sdf_streams.assign(s->cfg.sdf_workers, nullptr);
+  for (auto &st : s->sdf_streams)
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+      set_err(err, errlen, "cudaStreamCreate failed");
+      for (auto &t : s->sdf_streams)
+        if (t) cudaStreamDestroy(t);
+      for (int i = 0; i < 2; ++i) cudaStreamDestroy(s->streams[i]);
+      delete s;
+      return S2M_E_CUDA;
+    }
   s->worker = std::thread(server_loop, s);
-  s->sdf_worker = std::thread(server_sdf_loop, s);
+  for (uint32_t i = 0; i < s->cfg.sdf_workers; ++i) s->sdf_workers.emplace_back(server_sdf_loop, s, int(i));
+  s->compiler = std::thread(server_compile_loop, s);
   *out = s;
   return S2M_OK;
 }
@@ -1443,20 +1511,31 @@ int s2m_server_submit_sdf(s2m_server *s, const s2m_sdf *sdf, const s2m_params *p
 int s2m_server_submit_source(s2m_server *s, const char *source, int lang, const char *sdf_name,
                              const s2m_params *params, uint64_t *request_id, char *err, size_t errlen) {
   if (!s || !source || !params) return S2M_E_INVALID;
-  if (lang == S2M_LANG_WGSL) {
-    uint32_t n = 0;
-    if (s2m_csg_from_source(source, nullptr, 0, &n, nullptr, 0) == S2M_OK && n > 0) {
-      std::vector<float> prog(n);
-      if (s2m_csg_from_source(source, prog.data(), n, &n, err, errlen) == S2M_OK)
-        return s2m_server_submit_csg(s, prog.data(), n, params, request_id, err, errlen);
-    }
-  }
   const std::string key = std::to_string(lang) + '\0' + (sdf_name ? sdf_name : "sdf") + '\0' + source;
   s2m_sdf *sdf = nullptr;
   {
     std::lock_guard<std::mutex> lk(s->compile_mu);
     auto it = s->compiled.find(key);
     if (it != s->compiled.end()) sdf = it->second;
+  }
+  if (!sdf && lang == S2M_LANG_WGSL) {
+    // a CSG source without a compiled module yet: the interpreter now, and
+    // (tiering) its module compiled in the background for later requests
+    uint32_t n = 0;
+    if (s2m_csg_from_source(source, nullptr, 0, &n, nullptr, 0) == S2M_OK && n > 0) {
+      std::vector<float> prog(n);
+      if (s2m_csg_from_source(source, prog.data(), n, &n, err, errlen) == S2M_OK) {
+        if (!(s->cfg.flags & S2M_SERVER_INTERPRET_ONLY)) {
+          std::lock_guard<std::mutex> lk(s->compile_mu);
+          if (!s->compile_pending.count(key) && !s->compile_failed.count(key) && !s->compiled.count(key)) {
+            s->compile_pending.insert(key);
+            s->compile_queue.push_back(key);
+            s->compile_cv.notify_all();
+          }
+        }
+        return s2m_server_submit_csg(s, prog.data(), n, params, request_id, err, errlen);
+      }
+    }
   }
   if (!sdf) {
     std::string text = source;
@@ -1499,7 +1578,8 @@ int s2m_server_copy_to_host(s2m_server *s, uint64_t id, float *pos, float *nrm, 
   auto it = s->reqs.find(id);
   if (it == s->reqs.end() || it->second.state != 2) return S2M_E_INVALID;
   SReq &r = it->second;
-  if (r.kind == 1) return r.mesh ? s2m_mesh_copy_to_host(r.mesh, pos, nrm, cell, tris, s->sdf_stream) : S2M_E_INVALID;
+  // the mesh's work finished on its worker's stream (s2m_mesh_create synchronised it)
+  if (r.kind == 1) return r.mesh ? s2m_mesh_copy_to_host(r.mesh, pos, nrm, cell, tris, nullptr) : S2M_E_INVALID;
   if (r.wave < 0 || !s->waves[size_t(r.wave)].b) return S2M_E_INVALID;
   return s2m_batch_job_copy_to_host(s->waves[size_t(r.wave)].b, r.job, pos, nrm, cell, tris,
                                     s->waves[size_t(r.wave)].st);
@@ -1544,6 +1624,11 @@ int s2m_server_get_stats(s2m_server *s, s2m_server_stats *out) {
   out->span_s = span;
   out->meshes_per_s = span > 0 ? double(s->completed) / span : 0;
   out->gvoxels_per_s = span > 0 ? s->voxels_done / span / 1e9 : 0;
+  out->ran_compiled = s->ran_compiled;
+  out->ran_interpreted = s->ran_interpreted;
+  std::lock_guard<std::mutex> ck(s->compile_mu);
+  out->compiled_sources = s->compiled.size();
+  out->compiles_pending = s->compile_pending.size();
   return S2M_OK;
 }
 
@@ -1552,6 +1637,7 @@ int s2m_server_reset_stats(s2m_server *s) {
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->completed + s->failed < s->submitted) return S2M_E_INVALID;  // drain first
   s->submitted = s->completed = s->failed = s->batches = 0;
+  s->ran_compiled = s->ran_interpreted = 0;
   s->peak_bytes = s->used_bytes;
   s->first_submit = s->last_done = 0;
   s->voxels_done = 0;
@@ -1566,8 +1652,15 @@ void s2m_server_free(s2m_server *s) {
     s->stop = true;
     s->cv.notify_all();
   }
+  {
+    std::lock_guard<std::mutex> lk(s->compile_mu);
+    s->compile_stop = true;
+    s->compile_cv.notify_all();
+  }
+  if (s->compiler.joinable()) s->compiler.join();
   if (s->worker.joinable()) s->worker.join();
-  if (s->sdf_worker.joinable()) s->sdf_worker.join();
+  for (auto &t : s->sdf_workers)
+    if (t.joinable()) t.join();
   for (auto &kv : s->reqs) {
     kv.second.state = kv.second.state < 2 ? 3 : kv.second.state;
     server_release_locked(s, kv.second);
@@ -1583,7 +1676,11 @@ void s2m_server_free(s2m_server *s) {
       cudaStreamSynchronize(s->streams[i]);
       cudaStreamDestroy(s->streams[i]);
     }
-  if (s->sdf_stream) cudaStreamDestroy(s->sdf_stream);
+  for (auto &st : s->sdf_streams)
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
   for (auto &kv : s->compiled) s2m_sdf_free(kv.second);
   delete s;
 }

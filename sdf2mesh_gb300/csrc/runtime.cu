@@ -795,7 +795,8 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   m->vt_tiles = 0;
   if (prune && m->prune_chunk >= m->nslabs && m->cand_cap < (1ull << 32)) {
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-    m->vt_tiles = m->slab_tile_base[size_t(m->nslabs)] - m->slab_tile_base[0];
+    // sort keys: coarse box * 32 + tile within the box (s2m_vtile_count)
+    m->vt_tiles = (m->slab_coarse_base[size_t(m->nslabs)] - m->slab_coarse_base[0]) * 32ull;
     m->vt_blocks = unsigned((m->vt_tiles + S2_VT_TILE - 1) / S2_VT_TILE);
     m->vt_cnt_off = 16;
     m->vt_part_off = up16(m->vt_cnt_off + 4 * (size_t(m->vt_tiles) + 1));
@@ -1095,7 +1096,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     unsigned *vperm = reinterpret_cast<unsigned *>(m->vt_buf + m->vt_perm_off);
     if ((e = cudaMemsetAsync(m->vt_buf, 0, m->vt_part_off, st)) != cudaSuccess) return e;
     const unsigned cgrid = unsigned(sms) * 8;
-    S2_LAUNCH(2, 0, (s2m_vtile_count<<<cgrid, 256, 0, st>>>(j, cand, nslabs, tbase, D, nzc, tcnt, rank),
+    const unsigned long long *cbase = prune_at<unsigned long long>(m, m->prune_cbase_off);
+    S2_LAUNCH(2, 0, (s2m_vtile_count<<<cgrid, 256, 0, st>>>(j, cand, nslabs, cbase, D, nzc, tcnt, rank),
                      cudaGetLastError()));
     S2_LAUNCH(2, 0, (s2m_vtile_scan<<<m->vt_blocks, 256, 0, st>>>(tcnt, m->vt_tiles, part, poff, pbase,
                                                                   tcnt + m->vt_tiles),
@@ -1107,7 +1109,10 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   unsigned long long *vc_base = m->cand_status;
   unsigned *vc_cnt = reinterpret_cast<unsigned *>(m->cand_status + 2);
   unsigned long long *vc_off = m->cand_status + vc_ctrl_offsets(m->vc_tiles);
-  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt};
+  // the coarse boxes' bits, resident with the tiles' (the chunk holds every slab)
+  const unsigned *sbits = tbits ? prune_at<unsigned>(m, m->prune_sbits_off) : nullptr;
+  const unsigned long long *vcbase = m->prune_buf ? prune_at<unsigned long long>(m, m->prune_cbase_off) : nullptr;
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &sbits, &vcbase};
   const unsigned vx_grid = unsigned(sms) * 16;
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));

@@ -189,10 +189,10 @@ __global__ void __launch_bounds__(256) s2m_tile_map(const unsigned *__restrict__
 }
 
 // The map's bits of tiles 4w .. 4w + 4 (the points of word w of a point row
-// and the first point of word w + 1): bits 2b, 2b + 1 of tile 4w + b.
-__device__ __forceinline__ unsigned s2_map_bits(const S2TileMap &tm, int k, int y, int w, bool more) {
-  const unsigned *mw = tm.map + ((unsigned long long)__ldg(tm.prow + k) + (unsigned)(y >> 3)) * (unsigned)tm.wt +
-                       (unsigned)(w >> 2);
+// and the first point of word w + 1): bits 2b, 2b + 1 of tile 4w + b.  row0
+// = prow[k] of the row's plane k.
+__device__ __forceinline__ unsigned s2_map_bits_row(const S2TileMap &tm, unsigned row0, int y, int w, bool more) {
+  const unsigned *mw = tm.map + ((unsigned long long)row0 + (unsigned)(y >> 3)) * (unsigned)tm.wt + (unsigned)(w >> 2);
   const unsigned lo = __ldg(mw);
   const unsigned hi = ((w & 3) == 3 && more) ? __ldg(mw + 1) : 0u;  // tile 4w + 4 in the next map word
   return __funnelshift_r(lo, hi, 8 * (w & 3)) & 0x3ffu;
@@ -257,23 +257,46 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
     const int dw = more ? 1 : 0;
     unsigned pw[S2_MARK_PLANES + 1][4], nw[S2_MARK_PLANES + 1][4];
     if (tm.map) {
-      // Decided tiles' points from the map (sign from the flag, near-zero 0);
-      // the point-bit words are read only where a tile of the word is
-      // undecided, and only the undecided tiles' bytes of them are used.
+      // Decided tiles' points from the map (sign from the flag, near-zero 0),
+      // the rest from the point-bit words, of which only the undecided tiles'
+      // bytes are used.  The map words first (independent loads); the
+      // point-bit words only when some tile of the thread's rows is
+      // undecided, then all of them at once, as below.
+      unsigned e[S2_MARK_PLANES + 1][2];
+      bool all_dec = true;
 #pragma unroll
       for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-        const int k = zc0 + dz0 + min(p, ncp);  // the plane of rb[p]
+        const unsigned row0 = __ldg(tm.prow + zc0 + dz0 + min(p, ncp));  // the plane of rb[p]
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
-          const unsigned e = s2_map_bits(tm, k, y + r, w, more);
-          const unsigned dec = s2_map_points(e, 0), posd = s2_map_points(e, 1);
-          const bool decn = (e >> 8) & 1u, posn = (e >> 9) & 1u;  // first point of word w + 1
+          e[p][r] = s2_map_bits_row(tm, row0, y + r, w, more);
+          all_dec &= (e[p][r] & 0x55u) == 0x55u && (!more || ((e[p][r] >> 8) & 1u));
+        }
+      }
+#pragma unroll
+      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
           const long long o = rb[p] + (long long)r * WP;
-          pw[p][2 * r] = (dec == ~0u ? 0u : (__ldg(pb.pos + o) & ~dec)) | posd;
-          pw[p][2 * r + 1] = decn ? (posn ? 1u : 0u) : __ldg(pb.pos + o + dw);  // only its bit 0 is used
+          pw[p][2 * r] = all_dec ? 0u : __ldg(pb.pos + o);
+          pw[p][2 * r + 1] = all_dec ? 0u : __ldg(pb.pos + o + dw);
           if (nearrule) {
-            nw[p][2 * r] = dec == ~0u ? 0u : (__ldg(pb.near + o) & ~dec);
-            nw[p][2 * r + 1] = decn ? 0u : __ldg(pb.near + o + dw);
+            nw[p][2 * r] = all_dec ? 0u : __ldg(pb.near + o);
+            nw[p][2 * r + 1] = all_dec ? 0u : __ldg(pb.near + o + dw);
+          }
+        }
+      }
+#pragma unroll
+      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const unsigned dec = s2_map_points(e[p][r], 0), posd = s2_map_points(e[p][r], 1);
+          const bool decn = (e[p][r] >> 8) & 1u, posn = (e[p][r] >> 9) & 1u;  // first point of word w + 1
+          pw[p][2 * r] = (pw[p][2 * r] & ~dec) | posd;
+          if (decn) pw[p][2 * r + 1] = posn ? 1u : 0u;  // only its bit 0 is used
+          if (nearrule) {
+            nw[p][2 * r] &= ~dec;
+            if (decn) nw[p][2 * r + 1] = 0u;
           }
         }
       }
@@ -408,23 +431,21 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
       continue;
     }
     float v[8];
+    s2_load_corners<false>(job, ring, cell, v);
     if (tm.map) {  // corners of decided tiles: no value in the ring, NaN in the record
       unsigned dec = 0u;
+      const unsigned r0 = __ldg(tm.prow + cell.z), r1 = __ldg(tm.prow + cell.z + 1);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
-        const unsigned *row = tm.map + ((unsigned long long)__ldg(tm.prow + cell.z + (q >> 1)) +
-                                        (unsigned)((cell.y + (q & 1)) >> 3)) * (unsigned)tm.wt;
+        const unsigned *row =
+            tm.map + ((unsigned long long)((q >> 1) ? r1 : r0) + (unsigned)((cell.y + (q & 1)) >> 3)) * (unsigned)tm.wt;
         const int t0 = cell.x >> 3, t1 = (cell.x + 1) >> 3;
         dec |= ((__ldg(row + (t0 >> 4)) >> (2 * (t0 & 15))) & 1u) << (2 * q);
         dec |= ((__ldg(row + (t1 >> 4)) >> (2 * (t1 & 15))) & 1u) << (2 * q + 1);
       }
-      const float *p0 = ring + (long long)(cell.z % job.ring) * job.plane + (long long)cell.y * job.pitch + cell.x;
-      const float *p1 = ring + (long long)((cell.z + 1) % job.ring) * job.plane + (long long)cell.y * job.pitch + cell.x;
-      const float *pc[8] = {p0, p0 + 1, p0 + job.pitch, p0 + job.pitch + 1, p1, p1 + 1, p1 + job.pitch, p1 + job.pitch + 1};
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = ((dec >> k) & 1u) ? __int_as_float(0x7fc00000) : __ldg(pc[k]);
-    } else {
-      s2_load_corners<false>(job, ring, cell, v);
+      for (int k = 0; k < 8; ++k)
+        if ((dec >> k) & 1u) v[k] = __int_as_float(0x7fc00000);
     }
     if (unk && !tm.map) {  // corners of decided tiles: no value in the ring
       const bool more = w + 1 < WP;
@@ -443,19 +464,20 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
   }
 }
 
-// Vertex work in tile order (tile pruning).  The vertex kernel evaluates the
-// SDF with the activity bits of each candidate's tile; lanes of a warp whose
-// candidates lie in different tiles take different paths through the pruned
-// SDF, one after the other.  Candidates are listed in (z, y, x) order, so 32
-// consecutive ones span several tiles.  A counting sort by tile gives the
-// vertex kernel a permutation that groups them:
-//   s2m_vtile_count    each candidate's tile and its rank among the tile's
-//   s2m_vtile_scan     exclusive scan of the per-tile counts
-//   s2m_vtile_scatter  perm[first of the tile + rank] = candidate
-// The mesh does not depend on the order: a candidate's vertex is a function
-// of its cell and its tile's bits alone.
+// Vertex work in box order (tile pruning).  The vertex kernel evaluates the
+// SDF with activity bits shared by its warp where it can: lanes whose bits
+// differ take different paths through the pruned SDF, one after the other.
+// Candidates are listed in (z, y, x) order, so 32 consecutive ones span
+// several tiles and boxes.  A counting sort by coarse box of the tile pass,
+// then by tile within the box (key box * 32 + tile), gives the vertex kernel
+// a permutation that groups them:
+//   s2m_vtile_count    each candidate's key and its rank among the key's
+//   s2m_vtile_scan     exclusive scan of the per-key counts
+//   s2m_vtile_scatter  perm[first of the key + rank] = candidate
+// The mesh does not depend on the order or on which sound bits evaluate it:
+// a candidate's vertex is a function of its cell alone, bit for bit.
 __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, int nslabs,
-                                                       const unsigned long long *__restrict__ tbase, int D, int nzc,
+                                                       const unsigned long long *__restrict__ cbase, int D, int nzc,
                                                        unsigned *tcnt, unsigned long long *__restrict__ trank) {
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
   for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < n;
@@ -465,7 +487,9 @@ __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, i
     c.x = (int)(k & 0xffffull);
     c.y = (int)((k >> 16) & 0xffffull);
     c.z = (int)((k >> 32) & 0xffffull);
-    const unsigned long long t = s2_cell_prune_tile(job, c, tbase, D, nzc);
+    // sort key: the coarse box, then the tile within it (32 tiles per box)
+    unsigned local;
+    const unsigned long long t = s2_cell_prune_box(job, c, cbase, D, nzc, &local) * 32ull + local;
     // one atomic per tile and warp (a warp's candidates share a few tiles)
     const unsigned am = __activemask();
     const unsigned peers = __match_any_sync(am, t);

@@ -115,3 +115,36 @@ def test_submit_source_routes_and_matches(lib):
         alone = s2m.generate(s2m.Sdf3DShader.from_source(src, lang, "sdf").compile(), st)
         assert_bit_exact(got, per_job_as_oracle(alone), f"request {rid}")
     server.close()
+
+
+def test_source_tiering_interpreter_then_compiled(lib):
+    """A CSG source runs on the interpreter until its background compile is
+    done, then on its compiled module; both give the same mesh, bit for bit
+    (the interpreter's arithmetic is the library functions')."""
+    server = s2m.Server(sdf_workers=3)
+    srcs = [workloads.random_tree(seed)[0] for seed in (4, 5, 6)]
+    st = s2m.AppState(resolution=72, bounds=2.0)
+    first = [server.submit_source(src, st) for src in srcs]
+    server.drain(600)
+    t0 = time.time()
+    while server.stats()["compiles_pending"] and time.time() - t0 < 600:
+        time.sleep(0.05)
+    stats = server.stats()
+    assert stats["compiled_sources"] >= len(srcs) and stats["ran_interpreted"] >= len(srcs)
+    server.reset_stats()
+    second = [server.submit_source(src, st) for src in srcs]
+    server.drain(600)
+    assert server.stats()["ran_compiled"] == len(srcs)
+    for a, b in zip(first, second):
+        assert_bit_exact(server.mesh(b), per_job_as_oracle(server.mesh(a)), f"request {a} vs {b}")
+    server.close()
+    only = s2m.Server(interpret_only=True)
+    rid = only.submit_source(srcs[0], st)
+    only.drain(600)
+    assert only.stats()["ran_interpreted"] == 1 and only.stats()["compiles_pending"] == 0
+    assert_bit_exact(only.mesh(rid), per_job_as_oracle(server_mesh_alone(srcs[0], st)), "interpret only")
+    only.close()
+
+
+def server_mesh_alone(src, st):
+    return s2m.generate(s2m.Sdf3DShader.from_source(src).compile(), st)
