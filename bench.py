@@ -630,9 +630,32 @@ def sub_mandelbulb(s2m, L, stream, flush, barrier, pk, pk_kind, N=2048, B=2.5, s
             "mesh": {"vertices": r["nverts"], "triangles": r["ntris"],
                      "invalid_quads": int(r["info"].invalid_quads), "slab_depth": int(r["info"].slab_depth)},
             "clocks": r["clocks"]}
+        if mode == "reference_rule":
+            out[mode]["stl_binary_write"] = time_binary_stl(r["mesh"])
         r["mesh"].close()
     sdf.close()
     return out
+
+
+def time_binary_stl(dmesh):
+    """Write the mesh as binary STL from all host threads (s2m_write_stl_binary):
+    GB/s of file bytes, on a RAM-backed file system when there is one, so that
+    the figure is the writer's rather than the disk's."""
+    host = dmesh.to_host()
+    d = "/dev/shm" if os.path.isdir("/dev/shm") else tempfile.gettempdir()
+    path = os.path.join(d, f"s2m_bench_{os.getpid()}.stl")
+    try:
+        t = time.perf_counter()
+        host.write_stl_binary_to_file(path)
+        dt = time.perf_counter() - t
+        size = os.path.getsize(path)
+        return {"bytes": size, "seconds": dt, "gb_per_s": size / dt / 1e9, "threads": host_threads(),
+                "path": d, "triangles": int(host.triangle_indices.shape[0])}
+    except Exception as e:  # no room for the file: report, do not fail the bench
+        return {"error": str(e)[:200], "path": d}
+    finally:
+        if os.path.exists(path):
+            os.unlink(path)
 
 
 def batch_jobs(n=256, seed=4):

@@ -186,13 +186,6 @@ struct s2m_mesh {
   size_t prune_sbits_off = 0;  // ... to the coarse boxes' activity words
   size_t prune_bits_off = 0;   // ... to the tiles' activity words
   size_t prune_list_off = 0;   // ... to the lists of undecided tiles
-  // decided-tile map (S2TileMap), when every slab's tile records stay
-  // resident: its words and the plane -> tile-row table
-  bool use_tmap = false;
-  size_t prune_tmap_off = 0, prune_prow_off = 0;
-  unsigned long long tmap_rows = 0;
-  int tmap_wt = 0;
-  std::vector<unsigned> prow_host;
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -639,28 +632,7 @@ size_t prune_layout(s2m_mesh *m) {
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * (words + 1) * 4);  // + each box's flag word
   m->prune_list_off = up16(m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4);  // + each tile's flag word
-  size_t end = m->prune_list_off + size_t(chunk_tiles) * 4;
-  // The decided-tile map needs every slab's tile flags at once (a slab's
-  // first cell plane lies on the previous slab's last tile layer).
-  m->use_tmap = ns > 0 && m->prune_chunk >= ns;
-  m->prow_host.clear();
-  if (m->use_tmap) {
-    m->tmap_rows = m->slab_tile_base[size_t(ns)] / (unsigned long long)ntx;
-    m->tmap_wt = int((ntx + 15) / 16);
-    m->prow_host.assign(size_t(m->nzc) + 1, 0u);
-    for (int s = 0; s < ns; ++s) {
-      int k0, nk;
-      slab_planes(m, s, k0, nk);
-      const PruneGeom g = prune_geom(m->job, nk);
-      for (int k = k0; k < k0 + nk; ++k)
-        m->prow_host[size_t(k)] = unsigned(m->slab_tile_base[size_t(s)] / (unsigned long long)ntx +
-                                           (unsigned long long)((k - k0) / g.tzs) * (unsigned long long)ntx);
-    }
-    m->prune_tmap_off = up16(end);
-    m->prune_prow_off = up16(m->prune_tmap_off + size_t(m->tmap_rows) * size_t(m->tmap_wt) * 4);
-    end = m->prune_prow_off + m->prow_host.size() * 4;
-  }
-  return end;
+  return m->prune_list_off + size_t(chunk_tiles) * 4;
 }
 template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
@@ -702,14 +674,12 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
                                                                         (size_t(m->sdf->prune_words) + 1);
   S2PointBits pb = point_bits(m);
   if (kEvalVariants[v].listed) {
-    if (!m->use_tmap) {  // decided tiles' point bits (with the map, classification reads the map instead)
-      const int W1 = m->sdf->prune_words + 1;
-      const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
-      const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
-      s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs);
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-    }
+    const int W1 = m->sdf->prune_words + 1;
+    const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
+    const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
+    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
                            (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
     const unsigned *count = prune_list_counts(m) + s;
@@ -795,8 +765,7 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   m->vt_tiles = 0;
   if (prune && m->prune_chunk >= m->nslabs && m->cand_cap < (1ull << 32)) {
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-    // sort keys: coarse box * 32 + tile within the box (s2m_vtile_count)
-    m->vt_tiles = (m->slab_coarse_base[size_t(m->nslabs)] - m->slab_coarse_base[0]) * 32ull;
+    m->vt_tiles = m->slab_tile_base[size_t(m->nslabs)] - m->slab_tile_base[0];
     m->vt_blocks = unsigned((m->vt_tiles + S2_VT_TILE - 1) / S2_VT_TILE);
     m->vt_cnt_off = 16;
     m->vt_part_off = up16(m->vt_cnt_off + 4 * (size_t(m->vt_tiles) + 1));
@@ -886,9 +855,6 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
                             cudaMemcpyHostToDevice, st));
     S2_CUDA(cudaMemcpyAsync(prune_at<unsigned long long>(m, m->prune_cbase_off), m->slab_coarse_base.data(),
                             m->slab_coarse_base.size() * 8, cudaMemcpyHostToDevice, st));
-    if (m->use_tmap)
-      S2_CUDA(cudaMemcpyAsync(prune_at<unsigned>(m, m->prune_prow_off), m->prow_host.data(), m->prow_host.size() * 4,
-                              cudaMemcpyHostToDevice, st));
   }
   S2_CUDA(mesh_malloc((void **)&m->cand_key, b.cand_key, st));
   S2_CUDA(mesh_malloc((void **)&m->cand_val, b.cand_val, st));
@@ -1042,17 +1008,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     m->eval_points += double(pts) * nk;
     if (pruned) {
       const int cb = s - s % m->prune_chunk;
-      if (s == cb) {
-        S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
-        if (m->use_tmap) {
-          const unsigned long long words = m->tmap_rows * (unsigned long long)m->tmap_wt;
-          const int ntx = (j.P + S2_PT_XY - 1) / S2_PT_XY;
-          S2_LAUNCH(1, 0, (s2m_tile_map<<<unsigned((words + 255) / 256), 256, 0, st>>>(
-                              prune_at<unsigned>(m, m->prune_bits_off), m->sdf->prune_words + 1, m->tmap_rows, ntx,
-                              m->tmap_wt, prune_at<unsigned>(m, m->prune_tmap_off)),
-                          cudaGetLastError()));
-        }
-      }
+      if (s == cb) S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
       S2_LAUNCH(0, double(pts) * nk, launch_evalp(m, ev, s, cb, st));
     } else {
       void *eargs[] = {&jj, &ring, &k0, &nk};
@@ -1067,16 +1023,13 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     const unsigned nbp = cell_tiles_per_plane(m);
     const unsigned ncp = unsigned(zc1 - zc0);
     const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
-    S2TileMap tm{nullptr, nullptr, 0};
-    if (pruned && m->use_tmap)
-      tm = S2TileMap{prune_at<unsigned>(m, m->prune_tmap_off), prune_at<unsigned>(m, m->prune_prow_off), m->tmap_wt};
     S2_LAUNCH(1, ncells, (s2m_cells_mark<<<mg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
                                                                     m->tile_cnt + m->cell_tiles, m->slab_ctrl,
-                                                                    m->cand_base, s, zc0, zc1, tm),
+                                                                    m->cand_base, s, zc0, zc1),
                           cudaGetLastError()));
     S2_LAUNCH(1, 0, (s2m_cells_emit<<<eg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
                                                                m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err,
-                                                               zc0, tm),
+                                                               zc0),
                      cudaGetLastError()));
   }
   S2Job jj = j;
@@ -1096,8 +1049,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     unsigned *vperm = reinterpret_cast<unsigned *>(m->vt_buf + m->vt_perm_off);
     if ((e = cudaMemsetAsync(m->vt_buf, 0, m->vt_part_off, st)) != cudaSuccess) return e;
     const unsigned cgrid = unsigned(sms) * 8;
-    const unsigned long long *cbase = prune_at<unsigned long long>(m, m->prune_cbase_off);
-    S2_LAUNCH(2, 0, (s2m_vtile_count<<<cgrid, 256, 0, st>>>(j, cand, nslabs, cbase, D, nzc, tcnt, rank),
+    S2_LAUNCH(2, 0, (s2m_vtile_count<<<cgrid, 256, 0, st>>>(j, cand, nslabs, tbase, D, nzc, tcnt, rank),
                      cudaGetLastError()));
     S2_LAUNCH(2, 0, (s2m_vtile_scan<<<m->vt_blocks, 256, 0, st>>>(tcnt, m->vt_tiles, part, poff, pbase,
                                                                   tcnt + m->vt_tiles),
@@ -1109,10 +1061,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   unsigned long long *vc_base = m->cand_status;
   unsigned *vc_cnt = reinterpret_cast<unsigned *>(m->cand_status + 2);
   unsigned long long *vc_off = m->cand_status + vc_ctrl_offsets(m->vc_tiles);
-  // the coarse boxes' bits, resident with the tiles' (the chunk holds every slab)
-  const unsigned *sbits = tbits ? prune_at<unsigned>(m, m->prune_sbits_off) : nullptr;
-  const unsigned long long *vcbase = m->prune_buf ? prune_at<unsigned long long>(m, m->prune_cbase_off) : nullptr;
-  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &sbits, &vcbase};
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt};
   const unsigned vx_grid = unsigned(sms) * 16;
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));

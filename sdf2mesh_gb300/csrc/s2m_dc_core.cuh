@@ -52,26 +52,6 @@ __device__ __forceinline__ unsigned long long s2_cell_prune_tile(const S2Job &jo
   const unsigned long long t = ((unsigned long long)tz * ntx + c.y / S2_PT_XY) * ntx + c.x / S2_PT_XY;
   return tbase[s] + t - tbase[0];
 }
-// The coarse box of the tile pass (S2_PT_COARSE x S2_PT_COARSE tiles by
-// S2_PT_COARSE_Z layers) that holds cell c's pruning tile, among all boxes of
-// the job, and the tile's place in it (*local: x + 4 y + 16 z, 0 .. 31).  The
-// box's interval evaluation covers every point its tiles' boxes cover, so its
-// activity bits are sound for the same cells.  cbase[s] is slab s's first box.
-__device__ __forceinline__ unsigned long long s2_cell_prune_box(const S2Job &job, S2Cell c,
-                                                                const unsigned long long *cbase, int D, int nzc,
-                                                                unsigned *local) {
-  const int s = c.z / D;
-  int k0, nk;
-  s2_slab_planes(s, D, nzc, k0, nk);
-  const int tz = (c.z + 1 - k0) / s2_tile_depth(nk);
-  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
-  const int tx = c.x / S2_PT_XY, ty = c.y / S2_PT_XY;
-  *local = (unsigned)(tx % S2_PT_COARSE + S2_PT_COARSE * (ty % S2_PT_COARSE) +
-                      S2_PT_COARSE * S2_PT_COARSE * (tz % S2_PT_COARSE_Z));
-  return cbase[s] - cbase[0] +
-         ((unsigned long long)(tz / S2_PT_COARSE_Z) * ncx + ty / S2_PT_COARSE) * ncx + tx / S2_PT_COARSE;
-}
 
 __device__ __forceinline__ S2Cell s2_cell_of(const S2Job &j, long long c, int zc0) {
   S2Cell r;

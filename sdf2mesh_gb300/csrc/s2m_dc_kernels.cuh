@@ -536,17 +536,16 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
 // final key and writes cand.pos / cand.nrm for cells with a vertex.  With
 // tbits (tile pruning, every slab's bits resident), the SDF evaluations use
-// pruning bits, and `perm` (when given) lists the candidates grouped by
-// coarse box and tile (s2m_vtile_*).  A warp whose candidates all lie in one
-// coarse box evaluates every request with that box's bits (sbits), so its
-// lanes take one path through the pruned SDF; other warps use each cell's
-// tile bits.  vc_cnt[t] counts the vertices of candidates t * S2_VC_TILE ..
-// (t + 1) * S2_VC_TILE - 1 (for s2m_vc_scan).
+// the bits of each cell's tile, and `perm` (when given) lists the candidates
+// grouped by tile (s2m_vtile_*), so that a warp's evaluations take one path
+// through the pruned SDF.  (The coarse box's bits, shared by more
+// candidates, activate more segments; per-tile bits were faster.)  vc_cnt[t]
+// counts the vertices of candidates t * S2_VC_TILE .. (t + 1) * S2_VC_TILE -
+// 1 (for s2m_vc_scan).
 #if !defined(S2M_SELECT) || defined(S2M_WANT_VERTICES)
 extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK, 8)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
-             int nzc, const unsigned *perm, unsigned *vc_cnt, const unsigned *sbits,
-             const unsigned long long *cbase) {
+             int nzc, const unsigned *perm, unsigned *vc_cnt) {
   __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
@@ -554,7 +553,7 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
   S2UserSdfPruned psdf;
   psdf.mp = s_mp;
 #else
-  (void)tbits; (void)tbase; (void)D; (void)nzc; (void)sbits; (void)cbase;
+  (void)tbits; (void)tbase; (void)D; (void)nzc;
 #endif
   const S2UserSdfCall sdf;
   // grid-stride over warp-sized runs of candidates, all lanes together
@@ -587,14 +586,7 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
 #else
 #ifdef S2M_HAS_PRUNE
     if (S2UserSdfCall::kStdNormal && tbits) {
-      unsigned local = 0;
-      const unsigned long long box = active ? s2_cell_prune_box(job, c, cbase, D, nzc, &local) : ~0ull;
-      const unsigned am = __ballot_sync(0xffffffffu, active);
-      const unsigned same = __match_any_sync(0xffffffffu, box);
-      const bool one_box = __all_sync(0xffffffffu, !active || (same & am) == am) && sbits;
-      s_mp[threadIdx.x] = !active ? nullptr
-                          : one_box ? sbits + box * S2M_TILE_WORDS
-                                    : s2_cell_bits(job, c, tbits, tbase, D, nzc);
+      s_mp[threadIdx.x] = active ? s2_cell_bits(job, c, tbits, tbase, D, nzc) : nullptr;
       __syncwarp();
       key = s2_vertex_warp(psdf, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
       __syncwarp();

@@ -154,58 +154,6 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
   }
 }
 
-// Decided-tile map of a job with tile pruning, when every slab's tile records
-// stay resident: 2 bits per pruning tile -- S2_TILE_DECIDED at bit 2b,
-// S2_TILE_POSITIVE at bit 2b + 1 of word b / 16 -- in rows of the job's tiles
-// along x (`wt` words per row; tile t of the job is in row t / ntx at x tile
-// t % ntx, since every slab holds whole rows).  prow[k] is the row of
-// lattice plane k's tile layer at y tile 0, so the tile of point (x, y, k) is
-// at row prow[k] + y / 8, x tile x / 8.  Classification reads decided tiles'
-// bits from here instead of point-bit planes, so nothing writes those planes
-// for decided tiles (map == null: s2m_fill_decided wrote them).
-struct S2TileMap {
-  const unsigned *map;
-  const unsigned *prow;
-  int wt;
-};
-
-// One thread per map word: the flag words of 16 tiles of a row.
-__global__ void __launch_bounds__(256) s2m_tile_map(const unsigned *__restrict__ tiles, int tile_words,
-                                                    unsigned long long rows, int ntx, int wt,
-                                                    unsigned *__restrict__ map) {
-  const unsigned long long q = (unsigned long long)blockIdx.x * 256u + threadIdx.x;
-  if (q >= rows * (unsigned long long)wt) return;
-  const unsigned long long row = q / (unsigned)wt;
-  const int wq = (int)(q - row * (unsigned)wt);
-  unsigned out = 0u;
-#pragma unroll 4
-  for (int b = 0; b < 16; ++b) {
-    const int tx = 16 * wq + b;
-    if (tx >= ntx) break;
-    const unsigned flag = __ldg(tiles + (row * (unsigned)ntx + (unsigned)tx) * (unsigned)tile_words + (tile_words - 1));
-    if (flag & S2_TILE_DECIDED) out |= (1u | ((flag & S2_TILE_POSITIVE) ? 2u : 0u)) << (2 * b);
-  }
-  map[q] = out;
-}
-
-// The map's bits of tiles 4w .. 4w + 4 (the points of word w of a point row
-// and the first point of word w + 1): bits 2b, 2b + 1 of tile 4w + b.  row0
-// = prow[k] of the row's plane k.
-__device__ __forceinline__ unsigned s2_map_bits_row(const S2TileMap &tm, unsigned row0, int y, int w, bool more) {
-  const unsigned *mw = tm.map + ((unsigned long long)row0 + (unsigned)(y >> 3)) * (unsigned)tm.wt + (unsigned)(w >> 2);
-  const unsigned lo = __ldg(mw);
-  const unsigned hi = ((w & 3) == 3 && more) ? __ldg(mw + 1) : 0u;  // tile 4w + 4 in the next map word
-  return __funnelshift_r(lo, hi, 8 * (w & 3)) & 0x3ffu;
-}
-
-// A 32-point mask from the map bits of 4 tiles (sel 0: decided, 1: positive):
-// the 4 bits are spread to the bytes' low bits, then each byte filled.
-__device__ __forceinline__ unsigned s2_map_points(unsigned e, int sel) {
-  const unsigned x = (e >> sel) & 0x55u;  // bits 0, 2, 4, 6
-  const unsigned nib = (x & 1u) | ((x >> 1) & 2u) | ((x >> 2) & 4u) | ((x >> 3) & 8u);
-  return ((nib * 0x00204081u) & 0x01010101u) * 0xffu;
-}
-
 // Cell words and tiles of a slab: word yw = y * WN + w of cell plane dz
 // holds the cells (x = 32 w .., y, z = zc0 + dz), at words[dz * N * WN + yw].
 // Tile t = dz * nbp + b (nbp = ceil(N * WN / S2_CW_BLOCK) tiles per plane)
@@ -223,7 +171,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
                                                             unsigned *__restrict__ words, unsigned *tile_cnt,
                                                             unsigned *done, unsigned long long *__restrict__ tile_off,
                                                             unsigned long long *base, int slab_index, int zc0,
-                                                            int zc1, S2TileMap tm) {
+                                                            int zc1) {
   __shared__ unsigned s_cnt[S2_MARK_PLANES][S2_CW_BLOCK / 32];
   const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + threadIdx.x);
@@ -256,63 +204,17 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
     }
     const int dw = more ? 1 : 0;
     unsigned pw[S2_MARK_PLANES + 1][4], nw[S2_MARK_PLANES + 1][4];
-    if (tm.map) {
-      // Decided tiles' points from the map (sign from the flag, near-zero 0),
-      // the rest from the point-bit words, of which only the undecided tiles'
-      // bytes are used.  The map words first (independent loads); the
-      // point-bit words only when some tile of the thread's rows is
-      // undecided, then all of them at once, as below.
-      unsigned e[S2_MARK_PLANES + 1][2];
-      bool all_dec = true;
 #pragma unroll
-      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-        const unsigned row0 = __ldg(tm.prow + zc0 + dz0 + min(p, ncp));  // the plane of rb[p]
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          e[p][r] = s2_map_bits_row(tm, row0, y + r, w, more);
-          all_dec &= (e[p][r] & 0x55u) == 0x55u && (!more || ((e[p][r] >> 8) & 1u));
-        }
-      }
-#pragma unroll
-      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const long long o = rb[p] + (long long)r * WP;
-          pw[p][2 * r] = all_dec ? 0u : __ldg(pb.pos + o);
-          pw[p][2 * r + 1] = all_dec ? 0u : __ldg(pb.pos + o + dw);
-          if (nearrule) {
-            nw[p][2 * r] = all_dec ? 0u : __ldg(pb.near + o);
-            nw[p][2 * r + 1] = all_dec ? 0u : __ldg(pb.near + o + dw);
-          }
-        }
-      }
-#pragma unroll
-      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const unsigned dec = s2_map_points(e[p][r], 0), posd = s2_map_points(e[p][r], 1);
-          const bool decn = (e[p][r] >> 8) & 1u, posn = (e[p][r] >> 9) & 1u;  // first point of word w + 1
-          pw[p][2 * r] = (pw[p][2 * r] & ~dec) | posd;
-          if (decn) pw[p][2 * r + 1] = posn ? 1u : 0u;  // only its bit 0 is used
-          if (nearrule) {
-            nw[p][2 * r] &= ~dec;
-            if (decn) nw[p][2 * r + 1] = 0u;
-          }
-        }
-      }
-    } else {
-#pragma unroll
-      for (int p = 0; p <= S2_MARK_PLANES; ++p) {
-        pw[p][0] = __ldg(pb.pos + rb[p]);
-        pw[p][1] = __ldg(pb.pos + rb[p] + dw);
-        pw[p][2] = __ldg(pb.pos + rb[p] + WP);
-        pw[p][3] = __ldg(pb.pos + rb[p] + WP + dw);
-        if (nearrule) {
-          nw[p][0] = __ldg(pb.near + rb[p]);
-          nw[p][1] = __ldg(pb.near + rb[p] + dw);
-          nw[p][2] = __ldg(pb.near + rb[p] + WP);
-          nw[p][3] = __ldg(pb.near + rb[p] + WP + dw);
-        }
+    for (int p = 0; p <= S2_MARK_PLANES; ++p) {
+      pw[p][0] = __ldg(pb.pos + rb[p]);
+      pw[p][1] = __ldg(pb.pos + rb[p] + dw);
+      pw[p][2] = __ldg(pb.pos + rb[p] + WP);
+      pw[p][3] = __ldg(pb.pos + rb[p] + WP + dw);
+      if (nearrule) {
+        nw[p][0] = __ldg(pb.near + rb[p]);
+        nw[p][1] = __ldg(pb.near + rb[p] + dw);
+        nw[p][2] = __ldg(pb.near + rb[p] + WP);
+        nw[p][3] = __ldg(pb.near + rb[p] + WP + dw);
       }
     }
 #pragma unroll
@@ -382,7 +284,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ tile_off,
                                                             const unsigned *__restrict__ tile_cnt, S2Cand cand,
-                                                            unsigned *err, int zc0, S2TileMap tm) {
+                                                            unsigned *err, int zc0) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -432,22 +334,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     }
     float v[8];
     s2_load_corners<false>(job, ring, cell, v);
-    if (tm.map) {  // corners of decided tiles: no value in the ring, NaN in the record
-      unsigned dec = 0u;
-      const unsigned r0 = __ldg(tm.prow + cell.z), r1 = __ldg(tm.prow + cell.z + 1);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
-        const unsigned *row =
-            tm.map + ((unsigned long long)((q >> 1) ? r1 : r0) + (unsigned)((cell.y + (q & 1)) >> 3)) * (unsigned)tm.wt;
-        const int t0 = cell.x >> 3, t1 = (cell.x + 1) >> 3;
-        dec |= ((__ldg(row + (t0 >> 4)) >> (2 * (t0 & 15))) & 1u) << (2 * q);
-        dec |= ((__ldg(row + (t1 >> 4)) >> (2 * (t1 & 15))) & 1u) << (2 * q + 1);
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k)
-        if ((dec >> k) & 1u) v[k] = __int_as_float(0x7fc00000);
-    }
-    if (unk && !tm.map) {  // corners of decided tiles: no value in the ring
+    if (unk) {  // corners of decided tiles: no value in the ring
       const bool more = w + 1 < WP;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
@@ -464,20 +351,19 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
   }
 }
 
-// Vertex work in box order (tile pruning).  The vertex kernel evaluates the
-// SDF with activity bits shared by its warp where it can: lanes whose bits
-// differ take different paths through the pruned SDF, one after the other.
-// Candidates are listed in (z, y, x) order, so 32 consecutive ones span
-// several tiles and boxes.  A counting sort by coarse box of the tile pass,
-// then by tile within the box (key box * 32 + tile), gives the vertex kernel
-// a permutation that groups them:
-//   s2m_vtile_count    each candidate's key and its rank among the key's
-//   s2m_vtile_scan     exclusive scan of the per-key counts
-//   s2m_vtile_scatter  perm[first of the key + rank] = candidate
-// The mesh does not depend on the order or on which sound bits evaluate it:
-// a candidate's vertex is a function of its cell alone, bit for bit.
+// Vertex work in tile order (tile pruning).  The vertex kernel evaluates the
+// SDF with the activity bits of each candidate's tile; lanes of a warp whose
+// candidates lie in different tiles take different paths through the pruned
+// SDF, one after the other.  Candidates are listed in (z, y, x) order, so 32
+// consecutive ones span several tiles.  A counting sort by tile gives the
+// vertex kernel a permutation that groups them:
+//   s2m_vtile_count    each candidate's tile and its rank among the tile's
+//   s2m_vtile_scan     exclusive scan of the per-tile counts
+//   s2m_vtile_scatter  perm[first of the tile + rank] = candidate
+// The mesh does not depend on the order: a candidate's vertex is a function
+// of its cell and its tile's bits alone.
 __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, int nslabs,
-                                                       const unsigned long long *__restrict__ cbase, int D, int nzc,
+                                                       const unsigned long long *__restrict__ tbase, int D, int nzc,
                                                        unsigned *tcnt, unsigned long long *__restrict__ trank) {
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
   for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < n;
@@ -487,9 +373,7 @@ __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, i
     c.x = (int)(k & 0xffffull);
     c.y = (int)((k >> 16) & 0xffffull);
     c.z = (int)((k >> 32) & 0xffffull);
-    // sort key: the coarse box, then the tile within it (32 tiles per box)
-    unsigned local;
-    const unsigned long long t = s2_cell_prune_box(job, c, cbase, D, nzc, &local) * 32ull + local;
+    const unsigned long long t = s2_cell_prune_tile(job, c, tbase, D, nzc);
     // one atomic per tile and warp (a warp's candidates share a few tiles)
     const unsigned am = __activemask();
     const unsigned peers = __match_any_sync(am, t);

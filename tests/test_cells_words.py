@@ -118,78 +118,3 @@ def test_mark_words_match_the_cell_rule(N, mode):
     bad = np.argwhere(got != want)
     assert bad.size == 0, f"{len(bad)} cells differ, first (z, y, x) = {tuple(bad[0])}"
     assert want.any() and not want.all()
-
-
-# ---------------------------------------------------------------------------
-# Decided-tile map (s2m_tile_map, s2_map_bits, s2_map_points): with tile
-# pruning, nothing writes the point-bit words of decided tiles; the mark
-# kernel takes those points' bits from the map (sign from the tile's flag,
-# near-zero 0) and the rest from the words.  Restated here over random tile
-# flags and random stale bytes where decided tiles' bits would be.
-
-def map_rows(flags, ntx):
-    """s2m_tile_map: flags [rows, ntx] (bit 0 decided, bit 1 positive) -> words [rows, wt]."""
-    rows = flags.shape[0]
-    wt = (ntx + 15) // 16
-    out = np.zeros((rows, wt), np.uint64)
-    for tx in range(ntx):
-        f = flags[:, tx].astype(np.uint64)
-        bits = np.where(f & 1, np.uint64(1) | np.where(f & 2, np.uint64(2), np.uint64(0)), np.uint64(0))
-        out[:, tx // 16] |= bits << np.uint64(2 * (tx % 16))
-    return out
-
-
-def map_bits(mrow, w, more):
-    """s2_map_bits on one map row: 10 bits of tiles 4w .. 4w + 4."""
-    lo = int(mrow[w >> 2])
-    hi = int(mrow[(w >> 2) + 1]) if (w & 3) == 3 and more else 0
-    return (((hi << 32) | lo) >> (8 * (w & 3))) & 0x3FF
-
-
-def map_points(e, sel):
-    """s2_map_points: the kernel's nibble spread, in 32-bit arithmetic."""
-    x = (e >> sel) & 0x55
-    nib = (x & 1) | ((x >> 1) & 2) | ((x >> 2) & 4) | ((x >> 3) & 8)
-    return ((((nib * 0x00204081) & 0xFFFFFFFF) & 0x01010101) * 0xFF) & 0xFFFFFFFF
-
-
-@pytest.mark.parametrize("P", [33, 64, 129, 200])
-def test_tile_map_restores_decided_bits(P):
-    rng = np.random.default_rng(P)
-    ntx = (P + 7) // 8
-    WP = (P + 31) // 32
-    nrows_y = P
-    flags = rng.integers(0, 4, size=(ntx, ntx))          # one tile layer: [ty, tx]
-    flags[rng.random(flags.shape) < 0.3] = 0             # undecided
-    truth_pos = rng.random((nrows_y, P)) < 0.5
-    truth_near = rng.random((nrows_y, P)) < 0.2
-    dec_pt = np.zeros((nrows_y, P), bool)
-    for y in range(nrows_y):
-        for x in range(P):
-            f = flags[y // 8, x // 8]
-            if f & 1:
-                dec_pt[y, x] = True
-                truth_pos[y, x] = bool(f & 2)
-                truth_near[y, x] = False
-    # memory: true bits where undecided, random stale bits where decided
-    mem_pos = np.where(dec_pt, rng.random(dec_pt.shape) < 0.5, truth_pos)
-    mem_near = np.where(dec_pt, rng.random(dec_pt.shape) < 0.5, truth_near)
-    pos_w, near_w = pack_rows(mem_pos), pack_rows(mem_near)
-    want_pos, want_near = pack_rows(truth_pos), pack_rows(truth_near)
-    mp = map_rows(flags, ntx)
-    for y in range(nrows_y):
-        for w in range(WP):
-            more = w + 1 < WP
-            e = map_bits(mp[y >> 3], w, more)
-            dec, posd = map_points(e, 0), map_points(e, 1)
-            decn, posn = (e >> 8) & 1, (e >> 9) & 1
-            got_pos = ((0 if dec == 0xFFFFFFFF else int(pos_w[y, w]) & ~dec) | posd) & 0xFFFFFFFF
-            got_near = 0 if dec == 0xFFFFFFFF else int(near_w[y, w]) & ~dec & 0xFFFFFFFF
-            valid = (1 << min(32, P - 32 * w)) - 1  # points past the lattice edge are never used
-            assert got_pos & valid == int(want_pos[y, w]) & valid, (y, w)
-            assert got_near & valid == int(want_near[y, w]) & valid, (y, w)
-            if more:  # only bit 0 of the next word is used (the funnel shift)
-                nxt_pos = (1 if posn else 0) if decn else int(pos_w[y, w + 1])
-                nxt_near = 0 if decn else int(near_w[y, w + 1])
-                assert nxt_pos & 1 == int(want_pos[y, w + 1]) & 1, (y, w)
-                assert nxt_near & 1 == int(want_near[y, w + 1]) & 1, (y, w)
