@@ -355,6 +355,11 @@ int s2m_batch_stats(const s2m_batch *b, double *kernel_ms, uint64_t *launches, u
    30 s) and the look-back of its ordered compactions (default 2 s).  A wait
    that runs out makes s2m_batch_run return S2M_E_TIMEOUT. */
 int s2m_batch_set_wait_limit(s2m_batch *b, double stage_seconds, double lookback_seconds);
+/* Tile pruning of the CSG programs (default on), for the batch's jobs that
+   have not run yet: per tile of 8^3 lattice points an interval pass over the
+   program decides the tile's sign or which operands of its min / max /
+   smooth operators can be skipped; the results are bit-identical either way. */
+int s2m_batch_set_pruning(s2m_batch *b, int enabled);
 void s2m_batch_free(s2m_batch *b);
 
 /* ---- serving: continuous batching ---------------------------------------

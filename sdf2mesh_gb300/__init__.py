@@ -168,6 +168,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_mesh_set_graph": ([vp, i], i),
             "s2m_mesh_set_wait_limit": ([vp, ctypes.c_double], i),
             "s2m_batch_set_wait_limit": ([vp, ctypes.c_double, ctypes.c_double], i),
+            "s2m_batch_set_pruning": ([vp, i], i),
             "s2m_measure_sfu_peak": ([dp, vp], i),
             "s2m_csg_from_source": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(u32),
                                      ctypes.c_char_p, sz], i),
@@ -587,6 +588,11 @@ class Batch:
         """Bounds of the persistent kernel's device waits (defaults 30 s and 2 s)."""
         _check(load_library().s2m_batch_set_wait_limit(self._h, float(stage_seconds), float(lookback_seconds)),
                None, "wait limit")
+
+    def set_pruning(self, enabled: bool) -> None:
+        """Tile pruning of the programs (default on) for jobs not run yet; the
+        meshes are bit-identical either way."""
+        _check(load_library().s2m_batch_set_pruning(self._h, int(bool(enabled))), None, "pruning")
 
     def run(self, stream: int = 0) -> None:
         err = _errbuf()

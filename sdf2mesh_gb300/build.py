@@ -37,7 +37,7 @@ EMBEDDED = [
 ]
 SOURCES = ["runtime.cu", "batch.cu", "frontend.cpp", "frontend_lib.cpp", "prune.cpp", "mesh_io.cpp"]
 HEADERS = ["frontend.h", "prune.h", "mesh_io.h", "static_kernels.cuh", "s2m_device.h", "s2m_lookback.cuh",
-           "s2m_prelude.cuh", "s2m_dc_core.cuh", "s2m_dc_kernels.cuh", "s2m_workers.cuh"]
+           "s2m_prelude.cuh", "s2m_dc_core.cuh", "s2m_dc_kernels.cuh", "s2m_workers.cuh", "s2m_csg.cuh"]
 
 
 def _mtime(p):

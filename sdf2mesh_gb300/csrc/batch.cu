@@ -4,7 +4,8 @@
 // and operators, evaluated by an interpreter on the device, so no per-job
 // compilation) plus its own resolution and bounds.  All jobs of a batch run
 // in ONE launch of s2m_batch_kernel: its blocks take tickets from a device
-// work queue in which every job contributes six stages in order --
+// work queue in which every job contributes seven stages in order --
+//   T tile pass (interval pruning of the program per tile of the lattice),
 //   E evaluate the job's lattice, C classify cells (ordered candidate list),
 //   X place vertices, V compact vertices, R scan row starts, Q emit quads --
 // each stage a run of items.  A block that takes an item of stage s of a job
@@ -33,276 +34,15 @@
 #include "s2m_lookback.cuh"
 #include "s2m_dc_core.cuh"
 #include "s2m_workers.cuh"
-
-// ---------------------------------------------------------------------------
-// CSG program interpreter.  Opcodes and operands are floats; the arithmetic of
-// each opcode is that of the library function it names
-// (src/sdf3d_primitives.wgsl:7-36, src/sdf_op.wgsl:7-23), operation for
-// operation, so a program and the equivalent .sdf3d source give the same bits.
-
-#define S2_CSG_STACK 32
-
-struct S2CsgSdf {
-  static constexpr bool kStdNormal = true;
-  const float *prog;
-  int len;
-
-  __device__ __forceinline__ static float len3(float x, float y, float z) {
-    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
-  }
-  __device__ __forceinline__ static float len2(float x, float y) {
-    return __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
-  }
-  __device__ __forceinline__ static float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
-  // mix(e1, e2, t) = e1 * (1 - t) + e2 * t
-  __device__ __forceinline__ static float mix(float a, float b, float t) {
-    return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
-  }
-
-  __device__ __noinline__ float operator()(float x, float y, float z) const {
-    float st[S2_CSG_STACK];
-    int sp = 0;
-    int i = 0;
-    while (i < len) {
-      const int op = (int)__ldg(prog + i);
-      const float *a = prog + i + 1;
-      switch (op) {
-        case S2M_CSG_SPHERE: {  // sdf3d_sphere(p - c, r)
-          const float dx = __fsub_rn(x, __ldg(a)), dy = __fsub_rn(y, __ldg(a + 1)), dz = __fsub_rn(z, __ldg(a + 2));
-          st[sp++] = __fsub_rn(len3(dx, dy, dz), __ldg(a + 3));
-          i += 5;
-          break;
-        }
-        case S2M_CSG_BOX: {  // sdf3d_box(p - c, b), b the full size
-          const float qx = __fsub_rn(fabsf(__fsub_rn(x, __ldg(a))), __fmul_rn(0.5f, __ldg(a + 3)));
-          const float qy = __fsub_rn(fabsf(__fsub_rn(y, __ldg(a + 1))), __fmul_rn(0.5f, __ldg(a + 4)));
-          const float qz = __fsub_rn(fabsf(__fsub_rn(z, __ldg(a + 2))), __fmul_rn(0.5f, __ldg(a + 5)));
-          const float outside = len3(fmaxf(qx, 0.0f), fmaxf(qy, 0.0f), fmaxf(qz, 0.0f));
-          st[sp++] = __fadd_rn(outside, fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f));
-          i += 7;
-          break;
-        }
-        case S2M_CSG_TORUS: {  // sdf3d_torus(p - c, vec2(R, r))
-          const float dx = __fsub_rn(x, __ldg(a)), dy = __fsub_rn(y, __ldg(a + 1)), dz = __fsub_rn(z, __ldg(a + 2));
-          const float qx = __fsub_rn(len2(dx, dz), __ldg(a + 3));
-          st[sp++] = __fsub_rn(len2(qx, dy), __ldg(a + 4));
-          i += 6;
-          break;
-        }
-        case S2M_CSG_CAPSULE: {  // sdf3d_capsule(p, a, b, r)
-          const float pax = __fsub_rn(x, __ldg(a)), pay = __fsub_rn(y, __ldg(a + 1)), paz = __fsub_rn(z, __ldg(a + 2));
-          const float bax = __fsub_rn(__ldg(a + 3), __ldg(a)), bay = __fsub_rn(__ldg(a + 4), __ldg(a + 1)),
-                      baz = __fsub_rn(__ldg(a + 5), __ldg(a + 2));
-          const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(pax, bax), __fmul_rn(pay, bay)), __fmul_rn(paz, baz));
-          const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(bax, bax), __fmul_rn(bay, bay)), __fmul_rn(baz, baz));
-          const float h = clamp01(__fdiv_rn(d1, d2));
-          st[sp++] = __fsub_rn(len3(__fsub_rn(pax, __fmul_rn(bax, h)), __fsub_rn(pay, __fmul_rn(bay, h)),
-                                    __fsub_rn(paz, __fmul_rn(baz, h))),
-                               __ldg(a + 6));
-          i += 8;
-          break;
-        }
-        case S2M_CSG_PLANE: {  // dot(p, n) - d
-          const float d = __fadd_rn(__fadd_rn(__fmul_rn(x, __ldg(a)), __fmul_rn(y, __ldg(a + 1))), __fmul_rn(z, __ldg(a + 2)));
-          st[sp++] = __fsub_rn(d, __ldg(a + 3));
-          i += 5;
-          break;
-        }
-        case S2M_CSG_UNION: {
-          const float b = st[--sp];
-          st[sp - 1] = fminf(st[sp - 1], b);
-          i += 1;
-          break;
-        }
-        case S2M_CSG_SUBTRACT: {  // max(a, -b)
-          const float b = st[--sp];
-          st[sp - 1] = fmaxf(st[sp - 1], -b);
-          i += 1;
-          break;
-        }
-        case S2M_CSG_INTERSECT: {
-          const float b = st[--sp];
-          st[sp - 1] = fmaxf(st[sp - 1], b);
-          i += 1;
-          break;
-        }
-        case S2M_CSG_SMOOTH_UNION: {  // sdf_op_smooth_union(a, b, k)
-          const float b = st[--sp], d1 = st[sp - 1], k = __ldg(a);
-          const float h = clamp01(__fadd_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
-          st[sp - 1] = __fsub_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
-          i += 2;
-          break;
-        }
-        case S2M_CSG_SMOOTH_INTERSECTION: {  // sdf_op_smooth_intersection(a, b, k)
-          const float b = st[--sp], d1 = st[sp - 1], k = __ldg(a);
-          const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
-          st[sp - 1] = __fadd_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
-          i += 2;
-          break;
-        }
-        case S2M_CSG_SMOOTH_SUBTRACTION: {  // sdf_op_smooth_subtraction(a, b, k)
-          const float b = st[--sp], d1 = st[sp - 1], k = __ldg(a);
-          const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fadd_rn(b, d1)), k)));
-          st[sp - 1] = __fadd_rn(mix(b, -d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
-          i += 2;
-          break;
-        }
-        default:
-          return __int_as_float(0x7fc00000);  // rejected on the host; never reached
-      }
-    }
-    return st[sp - 1];
-  }
-
-  __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
-    s2_tetra_normal(*this, px, py, pz, eps, n);
-  }
-
-  // W points (x, y, z[w]) per decoded opcode: the same arithmetic as
-  // operator(), applied to W independent stacks (instruction-level
-  // parallelism, one decode for W evaluations).
-  template <int W>
-  __device__ void eval_run(float x, float y, const float z[W], float out[W]) const {
-    float st[S2_CSG_STACK][W];
-    int sp = 0;
-    int i = 0;
-    while (i < len) {
-      const int op = (int)__ldg(prog + i);
-      const float *a = prog + i + 1;
-      switch (op) {
-        case S2M_CSG_SPHERE: {
-          const float cx = __ldg(a), cy = __ldg(a + 1), cz = __ldg(a + 2), r = __ldg(a + 3);
-          const float dx = __fsub_rn(x, cx), dy = __fsub_rn(y, cy);
-#pragma unroll
-          for (int w = 0; w < W; ++w) st[sp][w] = __fsub_rn(len3(dx, dy, __fsub_rn(z[w], cz)), r);
-          ++sp;
-          i += 5;
-          break;
-        }
-        case S2M_CSG_BOX: {
-          const float qx = __fsub_rn(fabsf(__fsub_rn(x, __ldg(a))), __fmul_rn(0.5f, __ldg(a + 3)));
-          const float qy = __fsub_rn(fabsf(__fsub_rn(y, __ldg(a + 1))), __fmul_rn(0.5f, __ldg(a + 4)));
-          const float cz = __ldg(a + 2), hz = __fmul_rn(0.5f, __ldg(a + 5));
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const float qz = __fsub_rn(fabsf(__fsub_rn(z[w], cz)), hz);
-            const float outside = len3(fmaxf(qx, 0.0f), fmaxf(qy, 0.0f), fmaxf(qz, 0.0f));
-            st[sp][w] = __fadd_rn(outside, fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f));
-          }
-          ++sp;
-          i += 7;
-          break;
-        }
-        case S2M_CSG_TORUS: {
-          const float dx = __fsub_rn(x, __ldg(a)), dy = __fsub_rn(y, __ldg(a + 1)), cz = __ldg(a + 2);
-          const float R = __ldg(a + 3), r = __ldg(a + 4);
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const float qx = __fsub_rn(len2(dx, __fsub_rn(z[w], cz)), R);
-            st[sp][w] = __fsub_rn(len2(qx, dy), r);
-          }
-          ++sp;
-          i += 6;
-          break;
-        }
-        case S2M_CSG_CAPSULE: {
-          const float ax = __ldg(a), ay = __ldg(a + 1), az = __ldg(a + 2);
-          const float bax = __fsub_rn(__ldg(a + 3), ax), bay = __fsub_rn(__ldg(a + 4), ay),
-                      baz = __fsub_rn(__ldg(a + 5), az), r = __ldg(a + 6);
-          const float pax = __fsub_rn(x, ax), pay = __fsub_rn(y, ay);
-          const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(bax, bax), __fmul_rn(bay, bay)), __fmul_rn(baz, baz));
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const float paz = __fsub_rn(z[w], az);
-            const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(pax, bax), __fmul_rn(pay, bay)), __fmul_rn(paz, baz));
-            const float h = clamp01(__fdiv_rn(d1, d2));
-            st[sp][w] = __fsub_rn(len3(__fsub_rn(pax, __fmul_rn(bax, h)), __fsub_rn(pay, __fmul_rn(bay, h)),
-                                       __fsub_rn(paz, __fmul_rn(baz, h))),
-                                  r);
-          }
-          ++sp;
-          i += 8;
-          break;
-        }
-        case S2M_CSG_PLANE: {
-          const float dxy = __fadd_rn(__fmul_rn(x, __ldg(a)), __fmul_rn(y, __ldg(a + 1)));
-          const float nz = __ldg(a + 2), d = __ldg(a + 3);
-#pragma unroll
-          for (int w = 0; w < W; ++w) st[sp][w] = __fsub_rn(__fadd_rn(dxy, __fmul_rn(z[w], nz)), d);
-          ++sp;
-          i += 5;
-          break;
-        }
-        case S2M_CSG_UNION:
-          --sp;
-#pragma unroll
-          for (int w = 0; w < W; ++w) st[sp - 1][w] = fminf(st[sp - 1][w], st[sp][w]);
-          i += 1;
-          break;
-        case S2M_CSG_SUBTRACT:
-          --sp;
-#pragma unroll
-          for (int w = 0; w < W; ++w) st[sp - 1][w] = fmaxf(st[sp - 1][w], -st[sp][w]);
-          i += 1;
-          break;
-        case S2M_CSG_INTERSECT:
-          --sp;
-#pragma unroll
-          for (int w = 0; w < W; ++w) st[sp - 1][w] = fmaxf(st[sp - 1][w], st[sp][w]);
-          i += 1;
-          break;
-        case S2M_CSG_SMOOTH_UNION: {
-          --sp;
-          const float k = __ldg(a);
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const float b = st[sp][w], d1 = st[sp - 1][w];
-            const float h = clamp01(__fadd_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
-            st[sp - 1][w] = __fsub_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
-          }
-          i += 2;
-          break;
-        }
-        case S2M_CSG_SMOOTH_INTERSECTION: {
-          --sp;
-          const float k = __ldg(a);
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const float b = st[sp][w], d1 = st[sp - 1][w];
-            const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(b, d1)), k)));
-            st[sp - 1][w] = __fadd_rn(mix(b, d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
-          }
-          i += 2;
-          break;
-        }
-        case S2M_CSG_SMOOTH_SUBTRACTION: {
-          --sp;
-          const float k = __ldg(a);
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const float b = st[sp][w], d1 = st[sp - 1][w];
-            const float h = clamp01(__fsub_rn(0.5f, __fdiv_rn(__fmul_rn(0.5f, __fadd_rn(b, d1)), k)));
-            st[sp - 1][w] = __fadd_rn(mix(b, -d1, h), __fmul_rn(__fmul_rn(k, h), __fsub_rn(1.0f, h)));
-          }
-          i += 2;
-          break;
-        }
-        default:
-#pragma unroll
-          for (int w = 0; w < W; ++w) out[w] = __int_as_float(0x7fc00000);
-          return;
-      }
-    }
-#pragma unroll
-    for (int w = 0; w < W; ++w) out[w] = st[sp - 1][w];
-  }
-};
+#include "s2m_csg.cuh"
 
 // ---------------------------------------------------------------------------
 // Device-side batch description.
 
-enum { S2_ST_EVAL = 0, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_ST_ROWS, S2_ST_QUADS, S2_NSTAGES };
-#define S2_B_EVAL_ITEM 2048
+enum { S2_ST_TILES = 0, S2_ST_EVAL, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_ST_ROWS, S2_ST_QUADS, S2_NSTAGES };
+#define S2_B_TILE 8          // lattice points per edge of a tile
+#define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
+#define S2_B_EVAL_TILES 4    // tiles per item of the evaluation
 #define S2_B_VERT_CHUNK 256
 #define S2_ERR_BATCH_WAIT 0x20u
 
@@ -312,6 +52,9 @@ struct S2BatchJob {
   int prog_len;
   int nzc;                          // cell slices emitted (N, or N - 1 with the slice lag)
   float *lattice;
+  unsigned *tiles;                  // per tile: flag word, then the node codes (S2_CSG_TILE_WORDS)
+  int ntx;                          // tiles per lattice axis
+  int prune;                        // 0: every point with the full program (tiles unused)
   S2Cand cand;
   S2MeshDev mesh;
   unsigned long long *cell_status;  // look-back words of the classification tiles
@@ -338,28 +81,79 @@ struct S2BatchResult {
   unsigned err, pad;
 };
 
-// Lattice points of one item: S2_B_EVAL_ITEM / 4 units, a unit being a run
-// of 4 planes (k0 .. k0 + 3) at one (y, x); consecutive threads take
-// consecutive x, so each plane's stores are coalesced.
+// Tile pass: one thread per tile of 8 x 8 x 8 lattice points (fewer at the
+// lattice's far faces).  The program's interval pass over the box of the
+// tile's points (s2c_tile) gives the nodes' codes and the interval of the
+// value; the tile is DECIDED (| POSITIVE) when that interval lies at or
+// beyond +guard (-guard), as the per-job pipeline's tile pass decides.
+__device__ __forceinline__ s2i s2b_tile_axis(const S2Job &j, unsigned t) {
+  s2i a;
+  a.lo = s2_coord(j, (int)(S2_B_TILE * t));
+  a.hi = s2_coord(j, min((int)(S2_B_TILE * t) + S2_B_TILE - 1, j.P - 1));
+  return a;
+}
+
+__device__ __forceinline__ void s2b_stage_tiles(const S2BatchJob &J, unsigned item) {
+  const S2Job &j = J.job;
+  const unsigned nt = (unsigned)J.ntx, ntiles = nt * nt * nt;
+  const unsigned t = item * S2_B_TILES_ITEM + threadIdx.x;
+  if (!J.prune || t >= ntiles) return;
+  const unsigned tx = t % nt, q = t / nt, ty = q % nt, tz = q / nt;
+  unsigned codes[S2_CSG_CODE_WORDS];
+  s2i root;
+  s2c_tile(J.prog, J.prog_len, s2b_tile_axis(j, tx), s2b_tile_axis(j, ty), s2b_tile_axis(j, tz), codes, &root);
+  unsigned flag = 0u;
+  if (root.lo >= j.guard) flag = S2_TILE_DECIDED | S2_TILE_POSITIVE;
+  else if (root.hi <= -j.guard) flag = S2_TILE_DECIDED;
+  unsigned *rec = J.tiles + (size_t)t * S2_CSG_TILE_WORDS;
+  rec[0] = flag;
+#pragma unroll
+  for (int w = 0; w < S2_CSG_CODE_WORDS; ++w) rec[1 + w] = codes[w];
+}
+
+// Evaluation: S2_B_EVAL_TILES tiles per item, 128 runs of 4 planes per tile
+// (8 x 8 columns x 2 runs), x fastest, so the 32 lanes of a warp share one
+// tile and take one path through the pruned program.  A decided tile stores
+// +inf or -inf: the sign that classification needs, and a value that the
+// vertex stage treats as unknown and evaluates where a cell needs it.  Other
+// tiles evaluate the program with the tile's codes, which gives the same
+// bits as the full program at every point of the tile.
 #define S2_B_EVAL_RUN 4
 __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned item) {
+  __shared__ unsigned s_rec[256 / 32][S2_CSG_TILE_WORDS];
   const S2Job &j = J.job;
   const S2CsgSdf f{J.prog, J.prog_len};
-  const unsigned P = (unsigned)j.P, pp = P * P;  // P <= 4097: P * P < 2^32
-  const unsigned runs = (P + S2_B_EVAL_RUN - 1) / S2_B_EVAL_RUN;
-  const unsigned long long units = (unsigned long long)runs * pp;
+  const unsigned nt = (unsigned)J.ntx, ntiles = nt * nt * nt;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 #pragma unroll 1
-  for (int r = 0; r < S2_B_EVAL_ITEM / S2_B_EVAL_RUN / 256; ++r) {
-    const unsigned long long u = (unsigned long long)item * (S2_B_EVAL_ITEM / S2_B_EVAL_RUN) + r * 256 + threadIdx.x;
-    if (u >= units) break;
-    const unsigned run = (unsigned)(u / pp);
-    const unsigned c = (unsigned)(u - (unsigned long long)run * pp);
-    const unsigned y = s2_udiv(c, P, j.magic_p), x = c - y * P;
-    const int k0 = (int)(run * S2_B_EVAL_RUN);
+  for (int r = 0; r < S2_B_EVAL_TILES * 128 / 256; ++r) {
+    const unsigned u = r * 256u + threadIdx.x;
+    const unsigned t = item * S2_B_EVAL_TILES + (u >> 7);  // the same on the whole warp
+    if (t >= ntiles) break;
+    const unsigned lr = u & 127u;
+    const unsigned tx = t % nt, q = t / nt, ty = q % nt, tz = q / nt;
+    const int x = (int)(S2_B_TILE * tx + (lr & 7u)), y = (int)(S2_B_TILE * ty + ((lr >> 3) & 7u));
+    const int k0 = (int)(S2_B_TILE * tz + S2_B_EVAL_RUN * (lr >> 6));
+    unsigned flag = 0u;
+    if (J.prune) {
+      __syncwarp();
+      if (lane < S2_CSG_TILE_WORDS) s_rec[warp][lane] = __ldcg(J.tiles + (size_t)t * S2_CSG_TILE_WORDS + lane);
+      __syncwarp();
+      flag = s_rec[warp][0];
+    }
+    if (x >= j.P || y >= j.P || k0 >= j.P) continue;
     float z[S2_B_EVAL_RUN], v[S2_B_EVAL_RUN];
 #pragma unroll
     for (int w = 0; w < S2_B_EVAL_RUN; ++w) z[w] = s2_coord(j, min(k0 + w, j.P - 1));
-    f.eval_run<S2_B_EVAL_RUN>(s2_coord(j, (int)x), s2_coord(j, (int)y), z, v);
+    if (flag & S2_TILE_DECIDED) {
+      const float sv = (flag & S2_TILE_POSITIVE) ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
+#pragma unroll
+      for (int w = 0; w < S2_B_EVAL_RUN; ++w) v[w] = sv;
+    } else if (J.prune) {
+      f.eval_run_pruned<S2_B_EVAL_RUN>(s2_coord(j, x), s2_coord(j, y), z, v, s_rec[warp] + 1);
+    } else {
+      f.eval_run<S2_B_EVAL_RUN>(s2_coord(j, x), s2_coord(j, y), z, v);
+    }
     float *dst = J.lattice + (long long)k0 * j.plane + (long long)y * j.pitch + x;
 #pragma unroll
     for (int w = 0; w < S2_B_EVAL_RUN; ++w)
@@ -404,6 +198,11 @@ __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
     }
     float pos[3], nrm[3];
     unsigned long long key;
+    if (job.qef && active)  // corners of decided tiles (+-inf): their values, at their lattice coordinates
+#pragma unroll 1
+      for (int q = 0; q < 8; ++q)
+        if (!(fabsf(v[q]) <= 3.40282347e38f))
+          v[q] = f(s2_coord(job, c.x + (q & 1)), s2_coord(job, c.y + ((q >> 1) & 1)), s2_coord(job, c.z + (q >> 2)));
     if (job.qef) key = active ? s2_vertex_qef(f, job, c, v, pos, nrm) : 0ull;
     else key = s2_vertex_warp(f, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
     if (active) {
@@ -473,6 +272,7 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
     __syncthreads();
     if (s_ok) {
       switch (sg.stage) {
+        case S2_ST_TILES: s2b_stage_tiles(J, item); break;
         case S2_ST_EVAL: s2b_stage_eval(J, item); break;
         case S2_ST_CELLS: s2b_stage_cells(J, item); break;
         case S2_ST_VERT: s2b_stage_vertices(J); break;
@@ -586,6 +386,7 @@ struct HostJob {
   S2Job job{};
   int N = 0, nzc = 0;
   unsigned long long cand_cap = 0, vcap = 0, tcap = 0;
+  bool prune = true;  // tile pass and pruned evaluation
   // placement in the run's arena
   size_t zero_off = 0, data_off = 0;
   int run = -1;  // index of the run (arena) holding the results, -1 = not run yet
@@ -601,6 +402,12 @@ struct HostJob {
 
 size_t al(size_t b) { return (b + 255) / 256 * 256; }
 
+unsigned tiles_per_axis(const HostJob &h) { return unsigned((h.job.P + S2_B_TILE - 1) / S2_B_TILE); }
+size_t tile_records(const HostJob &h) {
+  const size_t nt = tiles_per_axis(h);
+  return h.prune ? nt * nt * nt : 0;
+}
+
 // Bytes of the zeroed control region and of the data region of a job.
 void job_sizes(const HostJob &h, size_t &zero_bytes, size_t &data_bytes) {
   const unsigned long long N = (unsigned long long)h.N;
@@ -612,7 +419,8 @@ void job_sizes(const HostJob &h, size_t &zero_bytes, size_t &data_bytes) {
   zero_bytes = al(2 * 8) + al(vc_tiles * 8) + al(cell_tiles * 8) + al((scan_tiles + quad_tiles) * 8) + al(N * N * 4) +
                al(8 * 4) /*counters*/ + al(8 * 4) /*done*/ + al(8 * 8) /*ntris, invalid, vtotal, err*/ + al(4);
   data_bytes = al(size_t(h.job.ring) * size_t(h.job.plane) * 4) + al(h.cand_cap * 8) + al(h.cand_cap * 32) +
-               al(h.cand_cap * 12) * 2 + al((N * N + 1) * 4) + al(h.vcap * 12) * 2 + al(h.vcap * 8) + al(h.tcap * 12);
+               al(h.cand_cap * 12) * 2 + al((N * N + 1) * 4) + al(h.vcap * 12) * 2 + al(h.vcap * 8) + al(h.tcap * 12) +
+               al(tile_records(h) * S2_CSG_TILE_WORDS * 4);
 }
 
 }  // namespace
@@ -635,6 +443,7 @@ struct s2m_batch {
   // stage waiting for its job's previous stage, and the look-backs
   unsigned long long stage_wait_ns = 30000000000ull;
   unsigned long long lookback_wait_ns = S2_WAIT_NS;
+  bool prune = true;  // for jobs that have not run yet
 };
 
 namespace {
@@ -745,6 +554,9 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
     J.mesh.nrm = reinterpret_cast<float *>(d); d += al(h.vcap * 12);
     J.mesh.key = reinterpret_cast<unsigned long long *>(d); d += al(h.vcap * 8);
     J.mesh.tris = reinterpret_cast<unsigned *>(d); d += al(h.tcap * 12);
+    J.tiles = reinterpret_cast<unsigned *>(d); d += al(tile_records(h) * S2_CSG_TILE_WORDS * 4);
+    J.ntx = int(tiles_per_axis(h));
+    J.prune = h.prune ? 1 : 0;
     doff += db[i];
     J.cand.cap = h.cand_cap;
     J.mesh.vcap = h.vcap;
@@ -756,12 +568,11 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
     J.prog_len = int(h.prog.size());
     poff += al(h.prog.size() * 4);
     // items per stage
-    const unsigned long long P = (unsigned long long)h.job.P;
     const unsigned long long n2 = N * N;
     {
-      const unsigned long long units = (P + S2_B_EVAL_RUN - 1) / S2_B_EVAL_RUN * P * P;
-      const unsigned long long per_item = S2_B_EVAL_ITEM / S2_B_EVAL_RUN;
-      J.nitems[S2_ST_EVAL] = unsigned((units + per_item - 1) / per_item);
+      const unsigned long long nt = tiles_per_axis(h), ntiles = nt * nt * nt;
+      J.nitems[S2_ST_TILES] = h.prune ? unsigned((ntiles + S2_B_TILES_ITEM - 1) / S2_B_TILES_ITEM) : 1u;
+      J.nitems[S2_ST_EVAL] = unsigned((ntiles + S2_B_EVAL_TILES - 1) / S2_B_EVAL_TILES);
     }
     J.nitems[S2_ST_CELLS] = unsigned(std::max<size_t>(1, cell_tiles));
     J.nitems[S2_ST_VERT] = unsigned(std::min<unsigned long long>(128, std::max<unsigned long long>(1, n2 / 2048)));
@@ -904,6 +715,7 @@ int s2m_batch_add_csg(s2m_batch *b, const float *program, uint32_t len, const s2
   HostJob h;
   h.prog.assign(program, program + len);
   h.params = *params;
+  h.prune = b->prune;
   uint32_t N = params->resolution;
   if (params->flags & S2M_JOB_POW2_ROUNDING)
     if (__builtin_popcount(N) > 1) N = 2u << (31u - uint32_t(__builtin_clz(N)));
@@ -1055,6 +867,14 @@ int s2m_batch_set_wait_limit(s2m_batch *b, double stage_seconds, double lookback
     return S2M_E_INVALID;
   b->stage_wait_ns = (unsigned long long)(stage_seconds * 1e9);
   b->lookback_wait_ns = (unsigned long long)(lookback_seconds * 1e9);
+  return S2M_OK;
+}
+
+int s2m_batch_set_pruning(s2m_batch *b, int enabled) {
+  if (!b) return S2M_E_INVALID;
+  b->prune = enabled != 0;
+  for (HostJob &h : b->jobs)
+    if (h.run < 0) h.prune = b->prune;
   return S2M_OK;
 }
 

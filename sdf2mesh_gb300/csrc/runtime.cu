@@ -169,7 +169,7 @@ struct s2m_mesh {
   int N = 0, D = 0, nzc = 0, nslabs = 0;
   // workspace
   float *ring = nullptr;
-  unsigned long long *slab_ctrl = nullptr;  // per cell tile of a slab: its first candidate slot
+  unsigned long long *slab_ctrl = nullptr;  // per cell plane of a slab: its first candidate slot
   unsigned *pt_bits = nullptr;               // sign, near-zero, then unknown-value bits of the ring's lattice points
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
   unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
@@ -743,7 +743,7 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   m->tcap = std::max<unsigned long long>(2048, tcap);
   m->cell_tiles = cell_word_tiles(m);
   m->vc_tiles = (m->cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
-  m->slab_ctrl_words = m->cell_tiles + 1;
+  m->slab_ctrl_words = size_t(m->D) + 1;
   m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   m->quad_tiles = (m->vcap + S2_Q_TILE - 1) / S2_Q_TILE;
   BufPlan b{};
@@ -752,7 +752,7 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   b.pt_bits = 3 * pt_bits_words(m) * 4;
   b.offx = size_t((j.N + 31) / 32) * 4;
   b.cell_words = m->cell_tiles * S2_CW_BLOCK * 4;
-  b.tile_cnt = (m->cell_tiles + 1) * 4;  // + the finished-block counter
+  b.tile_cnt = (m->cell_tiles + 1 + size_t(m->D)) * 4;  // + the finished-block counter, the plane counts
   const bool prune = m->sdf->k_tiles && m->nslabs > 0;
   b.prune = prune ? prune_layout(m) : 0;
   b.cand_key = m->cand_cap * 8;
@@ -995,7 +995,9 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }
-  if ((e = cudaMemsetAsync(m->tile_cnt + m->cell_tiles, 0, 4, st)) != cudaSuccess) return e;
+  // finished-block counter and plane counts of the classification (each slab's
+  // last mark block leaves them zero for the next)
+  if ((e = cudaMemsetAsync(m->tile_cnt + m->cell_tiles, 0, (1 + size_t(m->D)) * 4, st)) != cudaSuccess) return e;
   S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
   const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
@@ -1024,7 +1026,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     const unsigned ncp = unsigned(zc1 - zc0);
     const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
     S2_LAUNCH(1, ncells, (s2m_cells_mark<<<mg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
-                                                                    m->tile_cnt + m->cell_tiles, m->slab_ctrl,
+                                                                    m->tile_cnt + m->cell_tiles,
+                                                                    m->tile_cnt + m->cell_tiles + 1, m->slab_ctrl,
                                                                     m->cand_base, s, zc0, zc1),
                           cudaGetLastError()));
     S2_LAUNCH(1, 0, (s2m_cells_emit<<<eg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
@@ -1680,13 +1683,13 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   const S2Job &j = m.job;
   const unsigned long long N = (unsigned long long)m.N;
   m.cell_tiles = cell_word_tiles(&m);
-  m.slab_ctrl_words = m.cell_tiles + 1;
+  m.slab_ctrl_words = size_t(m.D) + 1;
   m.scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   size_t used = 0;
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
             carve(base, used, 3 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
-            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles + 1, &m.tile_cnt) &&
+            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles + 1 + size_t(m.D), &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
             carve(base, used, size_t(8), &m.jobctl);

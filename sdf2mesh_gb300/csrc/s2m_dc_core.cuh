@@ -539,16 +539,17 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
   float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
   float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
   // Corners evaluated here: the off-lattice ones (at the cell's reference
-  // coordinates) and those the lattice pass left unknown (NaN, decided tiles
-  // of the pruned evaluation).  An unknown corner that is on the lattice has
-  // reference coordinates equal to its lattice coordinates, so both kinds are
-  // evaluated at the cell's bounds.
+  // coordinates) and those the lattice pass left unknown (NaN or +-inf,
+  // decided tiles of the pruned evaluations; a value that really is
+  // non-finite is evaluated again, to the same value).  An unknown corner
+  // that is on the lattice has reference coordinates equal to its lattice
+  // coordinates, so both kinds are evaluated at the cell's bounds.
   unsigned off = 0u;
   if (active) {
     off = s2_off_mask(j, c) & 0xfeu;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-      if (v[k] != v[k]) off |= 1u << k;
+      if (!(fabsf(v[k]) <= 3.40282347e38f)) off |= 1u << k;
   }
 #pragma unroll
   for (int a = 0; a < 3; ++a) {

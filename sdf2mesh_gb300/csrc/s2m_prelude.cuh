@@ -310,7 +310,15 @@ S2M_PRUNED_FN float s2_op_smooth_subtraction_call(float a, float b, float k) {
 struct s2i {
   float lo, hi;
 };
-S2HD s2i s2i_unknown() { s2i r; r.lo = r.hi = __int_as_float(0x7fc00000u); return r; }
+// The quiet NaN 0x7fc00000 (device code, host code of nvcc and of a host compiler).
+S2HD float s2_qnan() {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(0x7fc00000u);
+#else
+  return __builtin_nanf("");
+#endif
+}
+S2HD s2i s2i_unknown() { s2i r; r.lo = r.hi = s2_qnan(); return r; }
 S2HD bool s2i_ok(s2i a) { return fabsf(a.lo) <= 3.40282347e38f && fabsf(a.hi) <= 3.40282347e38f; }
 S2HD s2i s2i_pt(float v) { s2i r; r.lo = v; r.hi = v; return r; }
 S2HD s2i s2i_fin(float lo, float hi) {

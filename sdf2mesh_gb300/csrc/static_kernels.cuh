@@ -161,15 +161,21 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
 //
 // s2m_cells_mark: grid (nbp, ceil(planes / S2_MARK_PLANES)); a thread takes
 // one word position over S2_MARK_PLANES cell planes, so each point row it
-// reads serves the planes above and below it.  The last block to finish (a
-// fence, then an atomic count of finished blocks) also scans the tile counts
-// into the slab's candidate offsets (tile_off, base[slab + 1]), so no
-// separate launch is needed; `done` returns to 0.
+// reads serves the planes above and below it.  Each block writes its tile
+// counts and adds them to the count of their cell plane (plane_cnt, zero on
+// entry).  The last block to finish (a fence, then an atomic count of
+// finished blocks) scans the slab's plane counts into plane offsets
+// (plane_off[dz] = base[slab] + candidates of planes < dz, base[slab + 1] =
+// the running total) and zeroes plane_cnt and `done` again.  (Scanning every
+// tile count in that one block made it run as long as the rest of the launch
+// together; s2m_cells_emit sums the counts before its tile within the plane
+// instead.)
 #define S2_MARK_PLANES 4
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2PointBits pb,
                                                             const unsigned *__restrict__ offx,
                                                             unsigned *__restrict__ words, unsigned *tile_cnt,
-                                                            unsigned *done, unsigned long long *__restrict__ tile_off,
+                                                            unsigned *done, unsigned *plane_cnt,
+                                                            unsigned long long *__restrict__ plane_off,
                                                             unsigned long long *base, int slab_index, int zc0,
                                                             int zc1) {
   __shared__ unsigned s_cnt[S2_MARK_PLANES][S2_CW_BLOCK / 32];
@@ -259,6 +265,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
     unsigned t = 0;
     for (int k = 0; k < S2_CW_BLOCK / 32; ++k) t += s_cnt[threadIdx.x][k];
     tile_cnt[(unsigned long long)(dz0 + (int)threadIdx.x) * gridDim.x + blockIdx.x] = t;
+    if (t) atomicAdd(plane_cnt + dz0 + (int)threadIdx.x, t);
     __threadfence();
   }
   __syncthreads();
@@ -267,7 +274,10 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  s2_scan_tiles<S2_CW_BLOCK, 16>(tile_cnt, (unsigned)(zc1 - zc0) * gridDim.x, tile_off, base, slab_index);
+  const unsigned nplanes = (unsigned)(zc1 - zc0);
+  s2_scan_tiles<S2_CW_BLOCK, 4>(plane_cnt, nplanes, plane_off, base, slab_index);
+  __syncthreads();  // every count read before it is cleared for the next slab
+  for (unsigned p = threadIdx.x; p < nplanes; p += S2_CW_BLOCK) plane_cnt[p] = 0u;
   if (threadIdx.x == 0) *done = 0u;
 }
 
@@ -278,20 +288,31 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
 // words in shared memory (word << 5 | bit, in (y, x) order), then writes
 // them one per thread: a word holds one or two candidates at most places of
 // the surface, and a warp's 32 words (a row at N = 1024) a handful, so the
-// block-wide list keeps the threads busy.
+// block-wide list keeps the threads busy.  The tile's first slot is its
+// plane's offset (s2m_cells_mark) plus the counts of the plane's tiles
+// before it, summed by the block's threads together.
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
                                                             const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
-                                                            const unsigned long long *__restrict__ tile_off,
+                                                            const unsigned long long *__restrict__ plane_off,
                                                             const unsigned *__restrict__ tile_cnt, S2Cand cand,
                                                             unsigned *err, int zc0) {
   __shared__ unsigned s_warp[32];
+  __shared__ unsigned s_pre[S2_CW_BLOCK / 32];
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const int WN = (job.N + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + tid);
   const int dz = (int)blockIdx.y;
-  if (__ldg(tile_cnt + (unsigned long long)dz * gridDim.x + blockIdx.x) == 0u) return;  // the whole tile: no candidate
+  const unsigned *plane_cnt = tile_cnt + (unsigned long long)dz * gridDim.x;
+  if (__ldg(plane_cnt + blockIdx.x) == 0u) return;  // the whole tile: no candidate
+  {
+    unsigned pre = 0u;
+    for (unsigned b = tid; b < blockIdx.x; b += S2_CW_BLOCK) pre += __ldg(plane_cnt + b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(S2_FULL, pre, o);
+    if (lane == 0) s_pre[warp] = pre;
+  }
   const unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
@@ -315,7 +336,9 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     }
   }
   __syncthreads();
-  const unsigned long long first = tile_off[(unsigned long long)dz * gridDim.x + blockIdx.x];
+  unsigned long long first = plane_off[dz];
+#pragma unroll
+  for (int k = 0; k < S2_CW_BLOCK / 32; ++k) first += s_pre[k];
   const int WP = (job.P + 31) >> 5;
 #pragma unroll 1
   for (unsigned r = tid; r < total; r += S2_CW_BLOCK) {

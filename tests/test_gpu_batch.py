@@ -110,3 +110,41 @@ def test_batch_256_random_trees(lib):
         if N > 200:
             continue
         assert_bit_exact(b.mesh(jid), oracle.mesh(oracle.TREE, prog, N, 2.0), f"job {jid} N={N}")
+
+
+def test_batch_pruning_on_and_off_identical(lib):
+    """Tile pruning (the interval pass per 8^3 tile, decided tiles stored as
+    +-inf, pruned programs elsewhere) changes no bit: the same jobs with pruning
+    off, and the oracle, in both rules, with the slice lag, every smooth
+    operator, and tiles at the lattice's ragged far faces (N + 1 not a
+    multiple of 8)."""
+    specs = []
+    for seed in range(20):
+        _, prog = workloads.random_tree(seed + 40)
+        prog = list(prog)
+        i = 0
+        while i < len(prog):  # turn some smooth unions into the other smooth operators
+            op = int(prog[i])
+            if op == 13 and seed % 3:
+                prog[i] = 13.0 + seed % 3
+            i += 1 + {0: 4, 1: 6, 2: 5, 3: 7, 4: 4, 10: 0, 11: 0, 12: 0, 13: 1, 14: 1, 15: 1}[op]
+        N = [37, 64, 71, 96, 50][seed % 5]
+        st = s2m.AppState(resolution=N, bounds=2.0, qef=(seed % 4 == 1), slice_lag=(seed % 5 == 3))
+        specs.append((prog, st))
+    meshes = {}
+    for prune in (True, False):
+        b = s2m.Batch()
+        b.set_pruning(prune)
+        ids = [b.add_csg(prog, st) for prog, st in specs]
+        b.run()
+        meshes[prune] = [b.mesh(j) for j in ids]
+        b.close()
+    for k, (prog, st) in enumerate(specs):
+        on, off = meshes[True][k], meshes[False][k]
+        assert on.positions.shape[0] > 0, k
+        for name in ("positions", "normals", "triangle_indices", "cells"):
+            a, c = getattr(on, name), getattr(off, name)
+            assert a.shape == c.shape and np.array_equal(a.view(np.uint8), c.view(np.uint8)), (k, name)
+        if k % 4 == 0:
+            ref = oracle.mesh(oracle.TREE, prog, st.resolution, st.bounds, qef=st.qef, slice_lag=st.slice_lag)
+            assert_bit_exact(on, ref, f"pruned batch job {k} vs oracle")
