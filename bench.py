@@ -327,6 +327,7 @@ def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=N
     p = state.params()
     err = ctypes.create_string_buffer(4096)
     e2e_ms = []
+    parts = {"create_ms": 0.0, "copy_to_host_ms": 0.0, "free_ms": 0.0}
     barrier()
     for i in range(e2e_steps or steps):
         with torch.cuda.stream(stream):
@@ -341,15 +342,22 @@ def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=N
         L.s2m_mesh_get_info(h, ctypes.byref(mi))
         if mi.nverts != nverts or mi.ntris != ntris:
             raise RuntimeError("e2e mesh differs from the timed mesh")
+        t1 = time.perf_counter()
         rc = L.s2m_mesh_copy_to_host(h, host_pos.data_ptr(), host_nrm.data_ptr(), None,
                                      host_tri.data_ptr(), ctypes.c_void_p(sp))
+        t2 = time.perf_counter()
         L.s2m_mesh_free(h)
-        e2e_ms.append((time.perf_counter() - t) * 1e3)
+        t3 = time.perf_counter()
+        e2e_ms.append((t3 - t) * 1e3)
+        parts["create_ms"] += (t1 - t) * 1e3
+        parts["copy_to_host_ms"] += (t2 - t1) * 1e3
+        parts["free_ms"] += (t3 - t2) * 1e3
         if rc != 0:
             raise RuntimeError("copy to host failed")
     barrier()
     out["e2e_ms"] = sum(e2e_ms)
     out["e2e_steps"] = len(e2e_ms)
+    out["e2e_parts_ms"] = {k: v / len(e2e_ms) for k, v in parts.items()}
     out["d2h"] = nverts * (12 + 12) + ntris * 12
     return out
 
@@ -557,7 +565,7 @@ def ours(a):
                    "evaluation": ("tile-pruned (exact: bit-identical to every operation at every point)"
                                   if eval_ops["pruned"] else "every SDF operation at every lattice point")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": r["d2h"],
-                "ms_per_step": e2e_tot / r["e2e_steps"],
+                "ms_per_step": e2e_tot / r["e2e_steps"], "parts_ms": r["e2e_parts_ms"],
                 "path": "s2m_mesh_create + s2m_mesh_copy_to_host (pinned: positions, normals, triangle indices, "
                         "the reference's TriangleMesh) + s2m_mesh_free; inputs are the "
                         "compiled SDF module and a 48-byte parameter block passed as kernel arguments"},
@@ -619,8 +627,8 @@ def sub_mandelbulb(s2m, L, stream, flush, barrier, pk, pk_kind, N=2048, B=2.5, s
         out[mode] = {
             "value": float(N) ** 3 * steps / (r["dev_ms"] * 1e-3) / 1e9, "ms_per_step": r["dev_ms"] / steps,
             "e2e": {"value": float(N) ** 3 * r["e2e_steps"] / (r["e2e_ms"] * 1e-3) / 1e9,
-                    "ms_per_step": r["e2e_ms"] / r["e2e_steps"], "d2h_bytes_per_step": r["d2h"],
-                    "h2d_bytes_per_step": 0},
+                    "ms_per_step": r["e2e_ms"] / r["e2e_steps"], "parts_ms": r["e2e_parts_ms"],
+                    "d2h_bytes_per_step": r["d2h"], "h2d_bytes_per_step": 0},
             "roofline": {k: roof[k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac",
                                               "dominant_by_time") if k in roof},
             "evaluation": {"sfu_frac": ev["sfu_frac"], "fp32_frac": ev["fp32_frac"], "bound": ev["bound"],

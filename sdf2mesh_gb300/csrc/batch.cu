@@ -82,16 +82,58 @@ struct S2BatchResult {
 };
 
 // Tile pass: one thread per tile of 8 x 8 x 8 lattice points (fewer at the
-// lattice's far faces).  The program's interval pass over the box of the
-// tile's points (s2c_tile) gives the nodes' codes and the interval of the
-// value; the tile is DECIDED (| POSITIVE) when that interval lies at or
-// beyond +guard (-guard), as the per-job pipeline's tile pass decides.
+// lattice's far faces).  The program's interval pass (s2c_tile) over the
+// tile's box gives the nodes' codes and the interval of the value; the tile
+// is DECIDED (| POSITIVE) when that interval lies at or beyond +guard
+// (-guard), as the per-job pipeline's tile pass decides.  The box reaches
+// one lattice point past the tile's points on each axis and is widened by
+// the per-job pipeline's margin (s2_prune_box: more than the normal epsilon
+// plus thousands of ulps of the coordinates), so the codes also hold at every
+// point the vertex stage evaluates for the cells whose lower corner lies in
+// the tile (cell x spans points x .. x + 1; its off-lattice corners mn + size
+// and normal samples p +- eps lie within the margin).
 __device__ __forceinline__ s2i s2b_tile_axis(const S2Job &j, unsigned t) {
+  const float mg = __fadd_rn(__fmul_rn(fabsf(j.eps), 1.0625f), __fmul_rn(__fadd_rn(fabsf(j.bmin), fabsf(j.size)), 0x1p-12f));
   s2i a;
-  a.lo = s2_coord(j, (int)(S2_B_TILE * t));
-  a.hi = s2_coord(j, min((int)(S2_B_TILE * t) + S2_B_TILE - 1, j.P - 1));
+  a.lo = __fsub_rn(s2_coord(j, (int)(S2_B_TILE * t)), mg);
+  a.hi = __fadd_rn(s2_coord(j, (int)(S2_B_TILE * t) + S2_B_TILE), mg);
   return a;
 }
+
+// The tile record of cell c (the tile of its lower corner).
+__device__ __forceinline__ const unsigned *s2b_cell_tile(const S2BatchJob &J, S2Cell c) {
+  const unsigned nt = (unsigned)J.ntx;
+  const unsigned t = ((unsigned)(c.z / S2_B_TILE) * nt + (unsigned)(c.y / S2_B_TILE)) * nt + (unsigned)(c.x / S2_B_TILE);
+  return J.tiles + (size_t)t * S2_CSG_TILE_WORDS;
+}
+
+// Evaluators of the vertex stage with the tile codes of each candidate's
+// cell: S2CsgLanes for s2_vertex_warp (lane l's requests with lane l's
+// record, from shared memory), S2CsgCell for one lane's own cell (precision
+// mode).  A null record evaluates the full program.
+struct S2CsgLanes {
+  static constexpr bool kStdNormal = true;
+  S2CsgSdf f;
+  const unsigned *const *rec;  // per thread of the block
+  __device__ __forceinline__ float at(unsigned l, float x, float y, float z) const {
+    const unsigned *r = rec[(threadIdx.x & ~31u) + l];
+    return r ? f.eval_tile(x, y, z, r + 1) : f(x, y, z);
+  }
+};
+__device__ __forceinline__ float s2_sdf_for(const S2CsgLanes &f, unsigned l, float x, float y, float z) {
+  return f.at(l, x, y, z);
+}
+struct S2CsgCell {
+  static constexpr bool kStdNormal = true;
+  S2CsgSdf f;
+  const unsigned *rec;
+  __device__ __forceinline__ float operator()(float x, float y, float z) const {
+    return rec ? f.eval_tile(x, y, z, rec + 1) : f(x, y, z);
+  }
+  __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
+    s2_tetra_normal(*this, px, py, pz, eps, n);
+  }
+};
 
 __device__ __forceinline__ void s2b_stage_tiles(const S2BatchJob &J, unsigned item) {
   const S2Job &j = J.job;
@@ -173,8 +215,10 @@ __device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned ti
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
   __shared__ unsigned s_chunk;
   __shared__ S2WarpScratch s_ws[256 / 32];
+  __shared__ const unsigned *s_rec[256];
   const S2Job &job = J.job;
   const S2CsgSdf f{J.prog, J.prog_len};
+  const S2CsgLanes lanes{f, s_rec};
   const unsigned long long n = min(__ldcg(J.cand.base + 1), J.cand.cap);
   const unsigned nchunks = (unsigned)((n + S2_B_VERT_CHUNK - 1) / S2_B_VERT_CHUNK);
   for (;;) {
@@ -198,13 +242,21 @@ __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
     }
     float pos[3], nrm[3];
     unsigned long long key;
-    if (job.qef && active)  // corners of decided tiles (+-inf): their values, at their lattice coordinates
+    const unsigned *rec = J.prune && active ? s2b_cell_tile(J, c) : nullptr;
+    if (job.qef) {
+      const S2CsgCell fc{f, rec};
+      if (active)  // corners of decided tiles (+-inf): their values, at their lattice coordinates
 #pragma unroll 1
-      for (int q = 0; q < 8; ++q)
-        if (!(fabsf(v[q]) <= 3.40282347e38f))
-          v[q] = f(s2_coord(job, c.x + (q & 1)), s2_coord(job, c.y + ((q >> 1) & 1)), s2_coord(job, c.z + (q >> 2)));
-    if (job.qef) key = active ? s2_vertex_qef(f, job, c, v, pos, nrm) : 0ull;
-    else key = s2_vertex_warp(f, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
+        for (int q = 0; q < 8; ++q)
+          if (!(fabsf(v[q]) <= 3.40282347e38f))
+            v[q] = fc(s2_coord(job, c.x + (q & 1)), s2_coord(job, c.y + ((q >> 1) & 1)), s2_coord(job, c.z + (q >> 2)));
+      key = active ? s2_vertex_qef(fc, job, c, v, pos, nrm) : 0ull;
+    } else {
+      s_rec[threadIdx.x] = rec;
+      __syncwarp();
+      key = s2_vertex_warp(lanes, job, active, c, v, pos, nrm, s_ws[threadIdx.x >> 5]);
+      __syncwarp();
+    }
     if (active) {
       J.cand.key[o] = key;
       if (key >> 63) {

@@ -72,10 +72,19 @@ S2HD int s2c_operands(int op) {
   return -1;
 }
 
-// Code of node n (nodes past the record's reach are always evaluated).
-S2HD unsigned s2c_code(const unsigned *codes, int n) {
-  return n < S2_CSG_MAX_NODES ? (codes[n >> 4] >> (2 * (n & 15))) & 3u : 1u;
-}
+// Where the pruned interpreter reads a tile's code words: plain loads
+// (shared memory, host), or L2 loads of a record that other blocks of the
+// same launch wrote.
+struct S2CodesPtr {
+  const unsigned *p;
+  S2C_FN unsigned word(int i) const { return p[i]; }
+};
+#if defined(__CUDACC__)
+struct S2CodesL2 {
+  const unsigned *p;
+  __device__ __forceinline__ unsigned word(int i) const { return __ldcg(p + i); }
+};
+#endif
 
 struct S2CsgSdf {
   static constexpr bool kStdNormal = true;
@@ -96,17 +105,19 @@ struct S2CsgSdf {
   // (instruction-level parallelism, one decode for W evaluations).  With
   // `codes` (PRUNED), nodes coded 0 are skipped and combinators coded 2 / 3
   // return their kept operand.
-  template <int W, bool PRUNED>
-  S2C_FN void run(float x, float y, const float z[W], float out[W], const unsigned *codes) const {
+  template <int W, bool PRUNED, class C>
+  S2C_FN void run(float x, float y, const float z[W], float out[W], const C &codes) const {
     float st[S2_CSG_STACK][W];
     int sp = 0;
     int i = 0, node = 0;
+    unsigned cw = 0x55555555u;  // the code word of nodes node & ~15 ..
     while (i < len) {
       const int op = (int)s2c_ld(prog + i);
       const float *a = prog + i + 1;
       unsigned code = 1u;
       if (PRUNED) {
-        code = s2c_code(codes, node);
+        if ((node & 15) == 0) cw = node < S2_CSG_MAX_NODES ? codes.word(node >> 4) : 0x55555555u;
+        code = (cw >> (2 * (node & 15))) & 3u;
         if (code == 0u) {  // a node of a skipped operand: nothing pushed or popped
           i += 1 + s2c_operands(op);
           ++node;
@@ -277,19 +288,25 @@ struct S2CsgSdf {
 
   template <int W>
   S2C_FN void eval_run(float x, float y, const float z[W], float out[W]) const {
-    run<W, false>(x, y, z, out, nullptr);
+    run<W, false>(x, y, z, out, S2CodesPtr{nullptr});
   }
   template <int W>
   S2C_FN void eval_run_pruned(float x, float y, const float z[W], float out[W], const unsigned *codes) const {
-    run<W, true>(x, y, z, out, codes);
+    run<W, true>(x, y, z, out, S2CodesPtr{codes});
   }
   S2C_FN float eval(float x, float y, float z) const {
     float zz[1] = {z}, v[1];
-    run<1, false>(x, y, zz, v, nullptr);
+    run<1, false>(x, y, zz, v, S2CodesPtr{nullptr});
     return v[0];
   }
 #if defined(__CUDACC__)
   __device__ __noinline__ float operator()(float x, float y, float z) const { return eval(x, y, z); }
+  // One point with a tile's codes, read from L2 (a record of this launch).
+  __device__ __noinline__ float eval_tile(float x, float y, float z, const unsigned *codes) const {
+    float zz[1] = {z}, v[1];
+    run<1, true>(x, y, zz, v, S2CodesL2{codes});
+    return v[0];
+  }
   __device__ __forceinline__ void normal(float px, float py, float pz, float eps, float n[3]) const {
     s2_tetra_normal(*this, px, py, pz, eps, n);
   }
@@ -297,8 +314,8 @@ struct S2CsgSdf {
 };
 
 // ---------------------------------------------------------------------------
-// The interval pass of one tile: X, Y, Z bound the coordinates of its points
-// (s2_coord of its first and last index per axis).  Writes the nodes' codes
+// The interval pass of one tile: X, Y, Z bound the coordinates of every
+// point the codes will be used at.  Writes the nodes' codes
 // (S2_CSG_CODE_WORDS words) and the interval of the program's value, and
 // returns 1; 0 (every code 1, root unknown) for a program of more than
 // S2_CSG_MAX_NODES nodes.

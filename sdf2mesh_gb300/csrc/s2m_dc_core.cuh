@@ -530,42 +530,22 @@ struct S2WarpScratch {
   float nv[32][4];
 };
 
+// Lane by lane, the corners in `req` (bit k: corner k) evaluated at the
+// cell's reference coordinates (ws.lo / ws.hi), 32 requests of the warp at a
+// time, whichever lanes they come from; the values replace v[k].
 template <class F>
-__device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const S2Job &j, bool active, S2Cell c,
-                                                             float v[8], float pos[3], float nrm[3],
-                                                             S2WarpScratch &ws) {
+__device__ __forceinline__ void s2_corner_requests(const F &sdf, unsigned req, float v[8], S2WarpScratch &ws) {
   const unsigned lane = threadIdx.x & 31u;
-  const unsigned lt = s2_lanemask_lt();
-  float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
-  float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
-  // Corners evaluated here: the off-lattice ones (at the cell's reference
-  // coordinates) and those the lattice pass left unknown (NaN or +-inf,
-  // decided tiles of the pruned evaluations; a value that really is
-  // non-finite is evaluated again, to the same value).  An unknown corner
-  // that is on the lattice has reference coordinates equal to its lattice
-  // coordinates, so both kinds are evaluated at the cell's bounds.
-  unsigned off = 0u;
-  if (active) {
-    off = s2_off_mask(j, c) & 0xfeu;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if (!(fabsf(v[k]) <= 3.40282347e38f)) off |= 1u << k;
-  }
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    ws.lo[lane][a] = mn[a];
-    ws.hi[lane][a] = mx[a];
-  }
-  // 1. off-lattice and unknown corners
-  unsigned cnt = __popc(off), inc = cnt;
+  unsigned cnt = __popc(req), inc = cnt;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const unsigned t = __shfl_up_sync(S2_FULL, inc, o);
     if ((int)lane >= o) inc += t;
   }
   const unsigned total = __shfl_sync(S2_FULL, inc, 31);
+  if (total == 0u) return;  // the same on the whole warp
   {
-    unsigned slot = inc - cnt, rem = off;
+    unsigned slot = inc - cnt, rem = req;
     while (rem) {
       const unsigned k = __ffs(rem) - 1;
       rem &= rem - 1u;
@@ -587,7 +567,61 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
   __syncwarp();
 #pragma unroll
   for (int k = 0; k < 8; ++k)
-    if ((off >> k) & 1u) v[k] = ws.val[lane][k];
+    if ((req >> k) & 1u) v[k] = ws.val[lane][k];
+}
+
+template <class F>
+__device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const S2Job &j, bool active, S2Cell c,
+                                                             float v[8], float pos[3], float nrm[3],
+                                                             S2WarpScratch &ws) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt = s2_lanemask_lt();
+  float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
+  float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
+  // Corners whose lattice value is not the reference's value: the off-lattice
+  // ones (evaluated at the cell's reference coordinates) and those the
+  // lattice pass left unknown (NaN or +-inf: decided tiles of the pruned
+  // evaluations; a value that really is non-finite is evaluated again, to
+  // the same value).  An unknown corner that is on the lattice has reference
+  // coordinates equal to its lattice coordinates, so both kinds are
+  // evaluated at the cell's bounds.
+  //   Where the lattice value lies at or beyond the guard (+-inf included),
+  // its sign is the reference value's sign -- the classification rests on
+  // the same fact -- so such a corner is evaluated only when it ends an edge
+  // whose signs differ, where the crossing needs its value (a second round
+  // of requests, after the others have settled every sign).  With
+  // S2M_JOB_EXACT_CORNERS every such corner is evaluated in the first round.
+  unsigned first = 0u, later = 0u;
+  if (active) {
+    unsigned diff = s2_off_mask(j, c) & 0xfeu;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (!(fabsf(v[k]) <= 3.40282347e38f)) diff |= 1u << k;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if ((diff >> k) & 1u) {
+        if (!j.exact && fabsf(v[k]) >= j.guard) later |= 1u << k;
+        else first |= 1u << k;
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ws.lo[lane][a] = mn[a];
+    ws.hi[lane][a] = mx[a];
+  }
+  // 1. off-lattice and unknown corners
+  s2_corner_requests(sdf, first, v, ws);
+  {
+    const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
+    const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
+    unsigned sg = 0u, need = 0u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sg |= (v[k] > 0.0f ? 1u : 0u) << k;
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+      if (((sg >> ea[e]) ^ (sg >> eb[e])) & 1u) need |= ((1u << ea[e]) | (1u << eb[e])) & later;
+    if (__any_sync(S2_FULL, need != 0u)) s2_corner_requests(sdf, need, v, ws);
+  }
   // 2. crossings and mass point (dualcontour.wgsl:86-131)
   const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
   const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
