@@ -714,8 +714,9 @@ def sub_batch(s2m, steps=3, warmup=3):
         bt.run()
         dt = time.perf_counter() - t
         ms, launches, _ = bt.stats()
+        prof = bt.stage_profile()
         bt.close()
-        return dt, ms, launches
+        return dt, ms, launches, prof
 
     for _ in range(warmup):
         one()
@@ -736,6 +737,7 @@ def sub_batch(s2m, steps=3, warmup=3):
             "steps": steps, "warmup": warmup, "ms_per_step": wall / steps * 1e3,
             "gvoxels_per_s": voxels * steps / wall / 1e9, "device_ms_per_step": sum(x[1] for x in res) / steps,
             "launches_per_step": res[0][2],
+            "stage_block_ms": {k: round(v, 3) for k, v in res[-1][3].items()},
             "plain_per_job_precompiled": {"meshes_per_s": 1.0 / plain_s, "gvoxels_per_s": voxels / len(jobs) / plain_s
                                           / 1e9, "path": "s2m_mesh_create + s2m_mesh_free per job, same 256 jobs, "
                                                          "modules compiled and tuned beforehand"},
@@ -866,7 +868,7 @@ def batch_arm(a):
             "gpu_launches": r["launches_per_step"] * a.steps,
             "e2e": {"value": r["value"], "unit": "meshes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             **{k: r[k] for k in ("gvoxels_per_s", "device_ms_per_step", "plain_per_job_precompiled",
-                                 "speedup_vs_precompiled_same_mix", "clocks")}}
+                                 "speedup_vs_precompiled_same_mix", "stage_block_ms", "clocks")}}
     print(json.dumps(line), flush=True)
 
 

@@ -169,6 +169,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_mesh_set_wait_limit": ([vp, ctypes.c_double], i),
             "s2m_batch_set_wait_limit": ([vp, ctypes.c_double, ctypes.c_double], i),
             "s2m_batch_set_pruning": ([vp, i], i),
+            "s2m_batch_stage_profile": ([vp, dp, u32, dp], i),
             "s2m_measure_sfu_peak": ([dp, vp], i),
             "s2m_csg_from_source": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(u32),
                                      ctypes.c_char_p, sz], i),
@@ -588,6 +589,19 @@ class Batch:
         """Bounds of the persistent kernel's device waits (defaults 30 s and 2 s)."""
         _check(load_library().s2m_batch_set_wait_limit(self._h, float(stage_seconds), float(lookback_seconds)),
                None, "wait limit")
+
+    BATCH_STAGES = ("tiles", "lattice", "cells", "vertices", "vcompact", "rowscan", "quads")
+
+    def stage_profile(self) -> dict:
+        """Block time (ms, summed over blocks) of the last run per stage, and the
+        block time spent waiting for a job's previous stage."""
+        n = len(self.BATCH_STAGES)
+        busy = (ctypes.c_double * n)()
+        wait = ctypes.c_double()
+        _check(load_library().s2m_batch_stage_profile(self._h, busy, n, ctypes.byref(wait)), None, "profile")
+        out = {k: float(busy[i]) for i, k in enumerate(self.BATCH_STAGES)}
+        out["waiting"] = float(wait.value)
+        return out
 
     def set_pruning(self, enabled: bool) -> None:
         """Tile pruning of the programs (default on) for jobs not run yet; the

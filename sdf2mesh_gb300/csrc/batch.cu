@@ -40,6 +40,7 @@
 // Device-side batch description.
 
 enum { S2_ST_TILES = 0, S2_ST_EVAL, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_ST_ROWS, S2_ST_QUADS, S2_NSTAGES };
+static_assert(S2_NSTAGES == S2M_BATCH_STAGES, "stage count of the C ABI");
 #define S2_B_TILE 8          // lattice points per edge of a tile
 #define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
 #define S2_B_EVAL_TILES 4    // tiles per item of the evaluation
@@ -73,6 +74,10 @@ struct S2BatchCtl {
   unsigned long long next;  // ticket counter
   unsigned err;
   unsigned pad;
+  // block time (GPU global timer ns, summed over blocks) spent on each
+  // stage's items, and waiting for a job's previous stage
+  unsigned long long busy_ns[S2_NSTAGES];
+  unsigned long long wait_ns;
 };
 
 // Results gathered for the host: ntris, invalid, vtotal, err, candidates.
@@ -284,6 +289,9 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
   __shared__ unsigned long long s_ticket;
   __shared__ int s_ok;
   const unsigned tid = threadIdx.x;
+  unsigned long long busy[S2_NSTAGES], waited = 0ull, t_item = 0ull;  // thread 0's accounting
+#pragma unroll
+  for (int k = 0; k < S2_NSTAGES; ++k) busy[k] = 0ull;
   for (;;) {
     if (tid == 0) s_ticket = atomicAdd(&ctl->next, 1ull);
     __syncthreads();
@@ -300,6 +308,7 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
     const S2BatchJob &J = jobs[sg.job];
     if (tid == 0) {
       int ok = 1;
+      const unsigned long long tw = s2_globaltimer();
       if (sg.stage > 0) {
         // wait for every item of the previous stage of this job (lower tickets),
         // bounded by time: stage_wait_ns of the GPU's global timer
@@ -319,6 +328,8 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
           __nanosleep(128);
         }
       }
+      t_item = s2_globaltimer();
+      waited += t_item - tw;
       s_ok = ok;
     }
     __syncthreads();
@@ -334,10 +345,21 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
       }
     }
     __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < S2_NSTAGES; ++k)
+        if (k == (int)sg.stage) busy[k] += s2_globaltimer() - t_item;
+    }
     if (tid == 0 && !((hold & S2_HOLD_BATCH_ROWS) && sg.job == 0 && sg.stage == S2_ST_ROWS)) {
       __threadfence();
       atomicAdd(J.done + sg.stage, 1u);
     }
+  }
+  if (tid == 0) {
+#pragma unroll
+    for (int k = 0; k < S2_NSTAGES; ++k)
+      if (busy[k]) atomicAdd(&ctl->busy_ns[k], busy[k]);
+    atomicAdd(&ctl->wait_ns, waited);
   }
 }
 
@@ -491,6 +513,8 @@ struct s2m_batch {
   int blocks_per_sm = 0;
   double last_ms = 0;
   uint64_t last_launches = 0;
+  double stage_busy_ms[S2_NSTAGES] = {};  // block time per stage, last run
+  double stage_wait_ms = 0;
   // bounds of the persistent kernel's device waits (GPU global timer ns): a
   // stage waiting for its job's previous stage, and the look-backs
   unsigned long long stage_wait_ns = 30000000000ull;
@@ -718,6 +742,8 @@ int finish_wave(s2m_batch *b, Wave &w, char *err, size_t errlen) {
                                                                  idx.size() * sizeof(S2BatchResult));
   b->pinned_free.push_back(w.res);
   w.res = PinnedBlock();
+  for (int k = 0; k < S2_NSTAGES; ++k) b->stage_busy_ms[k] += double(hctl.busy_ns[k]) * 1e-6;
+  b->stage_wait_ms += double(hctl.wait_ns) * 1e-6;
   if (hctl.err & S2_ERR_BATCH_WAIT) {
     set_err(err, errlen, "a batch stage wait hit its limit");
     return S2M_E_TIMEOUT;
@@ -823,6 +849,8 @@ int s2m_batch_run(s2m_batch *b, void *stream, char *err, size_t errlen) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   b->last_ms = 0;
   b->last_launches = 0;
+  for (double &x : b->stage_busy_ms) x = 0;
+  b->stage_wait_ms = 0;
   std::vector<int> pending;
   for (size_t i = 0; i < b->jobs.size(); ++i)
     if (b->jobs[i].run < 0) pending.push_back(int(i));
@@ -919,6 +947,13 @@ int s2m_batch_set_wait_limit(s2m_batch *b, double stage_seconds, double lookback
     return S2M_E_INVALID;
   b->stage_wait_ns = (unsigned long long)(stage_seconds * 1e9);
   b->lookback_wait_ns = (unsigned long long)(lookback_seconds * 1e9);
+  return S2M_OK;
+}
+
+int s2m_batch_stage_profile(const s2m_batch *b, double *busy_ms, uint32_t nstages, double *wait_ms) {
+  if (!b || (nstages && !busy_ms)) return S2M_E_INVALID;
+  for (uint32_t k = 0; k < nstages; ++k) busy_ms[k] = k < S2_NSTAGES ? b->stage_busy_ms[k] : 0.0;
+  if (wait_ms) *wait_ms = b->stage_wait_ms;
   return S2M_OK;
 }
 
