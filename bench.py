@@ -327,7 +327,8 @@ def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=N
     p = state.params()
     err = ctypes.create_string_buffer(4096)
     e2e_ms = []
-    parts = {"create_ms": 0.0, "copy_to_host_ms": 0.0, "free_ms": 0.0}
+    parts = {"create_ms": 0.0, "copy_to_host_ms": 0.0, "free_ms": 0.0, "create_setup_ms": 0.0,
+             "create_launch_ms": 0.0, "create_wait_ms": 0.0, "create_runs": 0.0}
     barrier()
     for i in range(e2e_steps or steps):
         with torch.cuda.stream(stream):
@@ -352,6 +353,10 @@ def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=N
         parts["create_ms"] += (t1 - t) * 1e3
         parts["copy_to_host_ms"] += (t2 - t1) * 1e3
         parts["free_ms"] += (t3 - t2) * 1e3
+        parts["create_setup_ms"] += mi.host_setup_ms
+        parts["create_launch_ms"] += mi.host_launch_ms
+        parts["create_wait_ms"] += mi.host_wait_ms
+        parts["create_runs"] += mi.runs
         if rc != 0:
             raise RuntimeError("copy to host failed")
     barrier()

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S2M_ABI_VERSION 1
+#define S2M_ABI_VERSION 2
 
 typedef enum {
   S2M_OK = 0,
@@ -101,6 +101,15 @@ typedef struct {
   const uint64_t *d_cell;   /* device: nverts keys x | y<<16 | z<<32 | signs<<48 */
   const uint32_t *d_tris;   /* device: 3 * ntris vertex indices              */
   uint64_t kernel_launches; /* kernels launched by the last run              */
+  /* Host time of the last s2m_mesh_create / s2m_mesh_run, ms: job setup and
+     buffer allocation, launching the pipeline, then waiting for the device
+     and reading its counters back; and the pipeline runs it took (more than
+     one after a capacity overflow). */
+  double host_setup_ms;
+  double host_launch_ms;
+  double host_wait_ms;
+  uint32_t runs;
+  uint32_t reserved;
 } s2m_mesh_info;
 
 /* ---- shader front end (src/shader.rs, src/shadertoy.rs) --------------- */

@@ -65,6 +65,8 @@ class MeshInfo(ctypes.Structure):
         ("cells", ctypes.c_uint64), ("candidate_cells", ctypes.c_uint64), ("resolution", ctypes.c_uint32),
         ("slab_depth", ctypes.c_uint32), ("d_pos", ctypes.c_void_p), ("d_nrm", ctypes.c_void_p),
         ("d_cell", ctypes.c_void_p), ("d_tris", ctypes.c_void_p), ("kernel_launches", ctypes.c_uint64),
+        ("host_setup_ms", ctypes.c_double), ("host_launch_ms", ctypes.c_double), ("host_wait_ms", ctypes.c_double),
+        ("runs", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
     ]
 
 

@@ -43,7 +43,7 @@ enum { S2_ST_TILES = 0, S2_ST_EVAL, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_
 static_assert(S2_NSTAGES == S2M_BATCH_STAGES, "stage count of the C ABI");
 #define S2_B_TILE 8          // lattice points per edge of a tile
 #define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
-#define S2_B_EVAL_TILES 4    // tiles per item of the evaluation
+#define S2_B_EVAL_TILES 16   // tiles per item of the evaluation (one warp per tile)
 #define S2_B_VERT_CHUNK 256
 #define S2_ERR_BATCH_WAIT 0x20u
 
@@ -158,13 +158,13 @@ __device__ __forceinline__ void s2b_stage_tiles(const S2BatchJob &J, unsigned it
   for (int w = 0; w < S2_CSG_CODE_WORDS; ++w) rec[1 + w] = codes[w];
 }
 
-// Evaluation: S2_B_EVAL_TILES tiles per item, 128 runs of 4 planes per tile
-// (8 x 8 columns x 2 runs), x fastest, so the 32 lanes of a warp share one
-// tile and take one path through the pruned program.  A decided tile stores
-// +inf or -inf: the sign that classification needs, and a value that the
-// vertex stage treats as unknown and evaluates where a cell needs it.  Other
-// tiles evaluate the program with the tile's codes, which gives the same
-// bits as the full program at every point of the tile.
+// Evaluation: S2_B_EVAL_TILES tiles per item, one warp per tile (so a warp
+// takes one path through the pruned program), S2_B_EVAL_TILES / 8 tiles per
+// warp.  A decided tile stores +inf or -inf (128 float4 stores for a whole
+// tile): the sign that classification needs, and a value that the vertex
+// stage treats as unknown and evaluates where a cell needs it.  Other tiles
+// evaluate 128 runs of 4 planes (8 x 8 columns x 2 runs), 4 runs per lane,
+// with the tile's codes, which give the same bits as the full program.
 #define S2_B_EVAL_RUN 4
 __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned item) {
   __shared__ unsigned s_rec[256 / 32][S2_CSG_TILE_WORDS];
@@ -173,14 +173,11 @@ __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned ite
   const unsigned nt = (unsigned)J.ntx, ntiles = nt * nt * nt;
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 #pragma unroll 1
-  for (int r = 0; r < S2_B_EVAL_TILES * 128 / 256; ++r) {
-    const unsigned u = r * 256u + threadIdx.x;
-    const unsigned t = item * S2_B_EVAL_TILES + (u >> 7);  // the same on the whole warp
+  for (unsigned q = 0; q < S2_B_EVAL_TILES / 8; ++q) {
+    const unsigned t = item * S2_B_EVAL_TILES + q * 8u + warp;  // the same on the whole warp
     if (t >= ntiles) break;
-    const unsigned lr = u & 127u;
-    const unsigned tx = t % nt, q = t / nt, ty = q % nt, tz = q / nt;
-    const int x = (int)(S2_B_TILE * tx + (lr & 7u)), y = (int)(S2_B_TILE * ty + ((lr >> 3) & 7u));
-    const int k0 = (int)(S2_B_TILE * tz + S2_B_EVAL_RUN * (lr >> 6));
+    const unsigned tx = t % nt, r = t / nt, ty = r % nt, tz = r / nt;
+    const int x0 = (int)(S2_B_TILE * tx), y0 = (int)(S2_B_TILE * ty), z0 = (int)(S2_B_TILE * tz);
     unsigned flag = 0u;
     if (J.prune) {
       __syncwarp();
@@ -188,23 +185,41 @@ __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned ite
       __syncwarp();
       flag = s_rec[warp][0];
     }
-    if (x >= j.P || y >= j.P || k0 >= j.P) continue;
-    float z[S2_B_EVAL_RUN], v[S2_B_EVAL_RUN];
-#pragma unroll
-    for (int w = 0; w < S2_B_EVAL_RUN; ++w) z[w] = s2_coord(j, min(k0 + w, j.P - 1));
     if (flag & S2_TILE_DECIDED) {
       const float sv = (flag & S2_TILE_POSITIVE) ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
+      if (x0 + S2_B_TILE <= j.P && y0 + S2_B_TILE <= j.P && z0 + S2_B_TILE <= j.P) {
+        // rows of 8 points start at 32-byte multiples (pitch: 32 points)
 #pragma unroll
-      for (int w = 0; w < S2_B_EVAL_RUN; ++w) v[w] = sv;
-    } else if (J.prune) {
-      f.eval_run_pruned<S2_B_EVAL_RUN>(s2_coord(j, x), s2_coord(j, y), z, v, s_rec[warp] + 1);
-    } else {
-      f.eval_run<S2_B_EVAL_RUN>(s2_coord(j, x), s2_coord(j, y), z, v);
+        for (int k = 0; k < 4; ++k) {
+          const int u = k * 32 + (int)lane, h = u & 1, y = (u >> 1) & 7, z = u >> 4;
+          float4 *dst = reinterpret_cast<float4 *>(J.lattice + (long long)(z0 + z) * j.plane +
+                                                   (long long)(y0 + y) * j.pitch + x0 + 4 * h);
+          *dst = make_float4(sv, sv, sv, sv);
+        }
+      } else {
+#pragma unroll 1
+        for (int u = (int)lane; u < S2_B_TILE * S2_B_TILE * S2_B_TILE; u += 32) {
+          const int x = x0 + (u & 7), y = y0 + ((u >> 3) & 7), z = z0 + (u >> 6);
+          if (x < j.P && y < j.P && z < j.P) J.lattice[(long long)z * j.plane + (long long)y * j.pitch + x] = sv;
+        }
+      }
+      continue;
     }
-    float *dst = J.lattice + (long long)k0 * j.plane + (long long)y * j.pitch + x;
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+      const unsigned lr = (unsigned)k * 32u + lane;
+      const int x = x0 + (int)(lr & 7u), y = y0 + (int)((lr >> 3) & 7u), k0 = z0 + S2_B_EVAL_RUN * (int)(lr >> 6);
+      if (x >= j.P || y >= j.P || k0 >= j.P) continue;
+      float z[S2_B_EVAL_RUN], v[S2_B_EVAL_RUN];
 #pragma unroll
-    for (int w = 0; w < S2_B_EVAL_RUN; ++w)
-      if (k0 + w < j.P) dst[(long long)w * j.plane] = v[w];
+      for (int w = 0; w < S2_B_EVAL_RUN; ++w) z[w] = s2_coord(j, min(k0 + w, j.P - 1));
+      if (J.prune) f.eval_run_pruned<S2_B_EVAL_RUN>(s2_coord(j, x), s2_coord(j, y), z, v, s_rec[warp] + 1);
+      else f.eval_run<S2_B_EVAL_RUN>(s2_coord(j, x), s2_coord(j, y), z, v);
+      float *dst = J.lattice + (long long)k0 * j.plane + (long long)y * j.pitch + x;
+#pragma unroll
+      for (int w = 0; w < S2_B_EVAL_RUN; ++w)
+        if (k0 + w < j.P) dst[(long long)w * j.plane] = v[w];
+    }
   }
 }
 
@@ -214,7 +229,8 @@ __device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned ti
   const long long ncells = (long long)J.nzc * J.job.N * J.job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
   s2_cell_tile<true>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, tile, ntiles, ncells, 0, 0ull,
-                     J.cand.base + 1, J.mesh.wait_ns);
+                     J.cand.base + 1, J.mesh.wait_ns,
+                     S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx});
 }
 
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {

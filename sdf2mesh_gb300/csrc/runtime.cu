@@ -212,6 +212,9 @@ struct s2m_mesh {
   unsigned long long *jobctl = nullptr;  // [ntris, invalid, vtotal, err | counters[8]]
   // host results
   unsigned long long *h_read = nullptr;  // pinned readback
+  // host time of the last s2m_mesh_create (ms) and its pipeline runs
+  double t_setup = 0, t_launch = 0, t_wait = 0;
+  unsigned runs = 0;
   uint64_t nverts = 0, ntris = 0, invalid = 0, ncand = 0;
   uint32_t errflags = 0;
   uint64_t launches = 0;
@@ -1570,6 +1573,14 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
                     size_t errlen) {
   if (!sdf || !params || !out) return S2M_E_INVALID;
   *out = nullptr;
+  using clk = std::chrono::steady_clock;
+  auto t = clk::now();
+  auto lap = [&t]() {
+    const auto now = clk::now();
+    const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+    t = now;
+    return ms;
+  };
   s2m_mesh *m = new s2m_mesh();
   m->sdf = sdf;
   m->stream = static_cast<cudaStream_t>(stream);
@@ -1606,13 +1617,17 @@ int s2m_mesh_create(const s2m_sdf *sdf, const s2m_params *params, void *stream, 
           (rc = alloc_buffers(m, cand_cap, vcap, tcap, err, errlen)) != S2M_OK)
         break;  // the tuned slab depth needs a ring of another size
     }
+    m->t_setup += lap();
     cudaError_t e = enqueue(m, st);
+    m->t_launch += lap();
+    ++m->runs;
     if (e != cudaSuccess) {
       set_err(err, errlen, std::string("launch: ") + cudaGetErrorString(e));
       rc = S2M_E_CUDA;
       break;
     }
     rc = readback(m, st, err, errlen);
+    m->t_wait += lap();
     if (rc != S2M_OK) break;
     if (m->errflags & S2_ERR_LOOKBACK) {
       set_err(err, errlen, "a device-side look-back wait hit its limit");
@@ -1781,6 +1796,10 @@ int s2m_mesh_get_info(const s2m_mesh *m, s2m_mesh_info *info) {
   info->d_cell = reinterpret_cast<const uint64_t *>(m->key);
   info->d_tris = m->tris;
   info->kernel_launches = m->launches;
+  info->host_setup_ms = m->t_setup;
+  info->host_launch_ms = m->t_launch;
+  info->host_wait_ms = m->t_wait;
+  info->runs = m->runs;
   return S2M_OK;
 }
 

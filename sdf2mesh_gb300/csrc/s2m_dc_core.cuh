@@ -442,24 +442,58 @@ __device__ __forceinline__ unsigned long long s2_vertex_qef(const F &sdf, const 
 }
 
 
+// Decided tiles of a pruned evaluation, for classification: the flag word of
+// the tile of 8 x 8 x 8 lattice points holding a cell's lower corner sits at
+// flags[stride * t], t = ((z / 8) * ntx + y / 8) * ntx + x / 8.  A decided
+// tile's interval bounds every corner of its cells (its box reaches one point
+// past the tile's points), at or beyond +-guard with one sign: no such cell
+// is a candidate, unless S2M_JOB_EXACT_CORNERS makes every cell with an
+// off-lattice corner one.
+struct S2CellSkip {
+  const unsigned *flags;  // null: no decided tiles
+  unsigned stride;
+  int ntx;
+};
+
 // One classification tile (S2_CELL_TILE cells, S2_CELL_BLOCK threads,
 // S2_CELL_CPT consecutive cells per thread in groups of 4): candidates
 // appended in (z, y, x) order at base + (look-back prefix over tiles), each
 // with its 8 corner values; the last tile stores the running total in
 // *next_base.  Large tiles keep the look-back short: all resident tiles start
 // together and each walks back over the aggregates of those still running.
+// With `skip`, a group of 4 cells that lies in one decided tile (N a multiple
+// of 4: a group is then 4 cells of one row, x from a multiple of 4) is not
+// loaded at all.
 template <bool CG>
 __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__restrict__ ring, const S2Cand &cand,
                                              unsigned long long *status, unsigned *err, unsigned tile,
                                              unsigned ntiles, long long ncells, int zc0, unsigned long long base,
-                                             unsigned long long *next_base, unsigned long long wait_ns) {
+                                             unsigned long long *next_base, unsigned long long wait_ns,
+                                             S2CellSkip skip = S2CellSkip{nullptr, 0u, 0}) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned long long s_excl;
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const long long c0 = (long long)tile * S2_CELL_TILE + (long long)S2_CELL_CPT * tid;
+  unsigned decided = 0;  // bit g: group g lies in a decided tile
+  if (skip.flags && !job.exact && (job.N & 3) == 0) {
+    unsigned f[S2_CELL_CPT / 4];
+#pragma unroll
+    for (int g = 0; g < S2_CELL_CPT / 4; ++g) {  // the flag loads first, in flight together
+      f[g] = 0u;
+      if (c0 + 4 * g + 3 < ncells) {
+        const S2Cell c = s2_cell_of(job, c0 + 4 * g, zc0);
+        const unsigned t = ((unsigned)(c.z >> 3) * (unsigned)skip.ntx + (unsigned)(c.y >> 3)) * (unsigned)skip.ntx +
+                           (unsigned)(c.x >> 3);
+        f[g] = __ldcg(skip.flags + (size_t)t * skip.stride);
+      }
+    }
+#pragma unroll
+    for (int g = 0; g < S2_CELL_CPT / 4; ++g) decided |= (f[g] & S2_TILE_DECIDED ? 1u : 0u) << g;
+  }
   unsigned mask = 0;  // bit g * 4 + m: cell c0 + 4g + m
 #pragma unroll
   for (int g = 0; g < S2_CELL_CPT / 4; ++g) {
+    if ((decided >> g) & 1u) continue;
     float v[4][8];
     mask |= s2_classify4<CG>(job, ring, c0 + 4 * g, ncells, zc0, v) << (4 * g);
   }
@@ -609,18 +643,23 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
     ws.lo[lane][a] = mn[a];
     ws.hi[lane][a] = mx[a];
   }
-  // 1. off-lattice and unknown corners
-  s2_corner_requests(sdf, first, v, ws);
-  {
+  // 1. off-lattice and unknown corners, in up to two rounds (one call site:
+  // the SDF's code is large, and a second copy of it costs instruction fetch)
+  unsigned req = first;
+#pragma unroll 1
+  for (int round = 0; round < 2; ++round) {
+    s2_corner_requests(sdf, req, v, ws);
+    if (round == 1) break;
     const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
     const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
-    unsigned sg = 0u, need = 0u;
+    unsigned sg = 0u;
+    req = 0u;
 #pragma unroll
     for (int k = 0; k < 8; ++k) sg |= (v[k] > 0.0f ? 1u : 0u) << k;
 #pragma unroll
     for (int e = 0; e < 12; ++e)
-      if (((sg >> ea[e]) ^ (sg >> eb[e])) & 1u) need |= ((1u << ea[e]) | (1u << eb[e])) & later;
-    if (__any_sync(S2_FULL, need != 0u)) s2_corner_requests(sdf, need, v, ws);
+      if (((sg >> ea[e]) ^ (sg >> eb[e])) & 1u) req |= ((1u << ea[e]) | (1u << eb[e])) & later;
+    if (!__any_sync(S2_FULL, req != 0u)) break;
   }
   // 2. crossings and mass point (dualcontour.wgsl:86-131)
   const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};

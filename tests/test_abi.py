@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_status(lib):
-    assert lib.s2m_abi_version() == 1
+    assert lib.s2m_abi_version() == 2
     assert lib.s2m_status_string(0) == b"ok"
     assert lib.s2m_status_string(5) == b"NVRTC compile error"
 

@@ -31,6 +31,35 @@ EVAL_TILES = const("S2_B_EVAL_TILES", "batch.cu")
 RUN = const("S2_B_EVAL_RUN", "batch.cu")
 
 
+def eval_tile_points(x0, y0, z0, P, decided):
+    """Points one warp writes for the tile at (x0, y0, z0): the decided path's
+    float4 stores of a whole tile (or its guarded scalar stores at the far
+    faces), or the 128 runs of 4 planes of the evaluation path."""
+    pts = []
+    if decided:
+        if x0 + TILE <= P and y0 + TILE <= P and z0 + TILE <= P:
+            for k in range(4):
+                for lane in range(32):
+                    u = k * 32 + lane
+                    h, y, z = u & 1, (u >> 1) & 7, u >> 4
+                    assert (x0 + 4 * h) % 4 == 0  # 16-byte aligned float4 (row starts are 32-point multiples)
+                    pts += [(z0 + z, y0 + y, x0 + 4 * h + i) for i in range(4)]
+        else:
+            for u in range(TILE ** 3):
+                x, y, z = x0 + (u & 7), y0 + ((u >> 3) & 7), z0 + (u >> 6)
+                if x < P and y < P and z < P:
+                    pts.append((z, y, x))
+        return pts
+    for k in range(4):
+        for lane in range(32):
+            lr = k * 32 + lane
+            x, y, k0 = x0 + (lr & 7), y0 + ((lr >> 3) & 7), z0 + RUN * (lr >> 6)
+            if x >= P or y >= P or k0 >= P:
+                continue
+            pts += [(k0 + w, y, x) for w in range(RUN) if k0 + w < P]
+    return pts
+
+
 @pytest.mark.parametrize("N", [2, 7, 8, 31, 40, 63, 64, 65, 100])
 def test_batch_eval_covers_lattice_once(N):
     P = N + 1
@@ -43,29 +72,41 @@ def test_batch_eval_covers_lattice_once(N):
         t = item * TILES_ITEM + np.arange(256)
         written[t[t < ntiles]] += 1
     assert (written == 1).all()
-    # evaluation
+    # evaluation: warp w of item i takes tiles i * EVAL_TILES + q * 8 + w
     items = (ntiles + EVAL_TILES - 1) // EVAL_TILES
+    seen = np.zeros(ntiles, int)
+    rng = np.random.default_rng(N)
     count = np.zeros((P, P, P), int)
     for item in range(items):
-        for r in range(EVAL_TILES * 128 // 256):
-            u = r * 256 + np.arange(256)
-            t = item * EVAL_TILES + (u >> 7)
-            for w in range(8):  # one tile per warp
-                assert len(set(t[32 * w:32 * w + 32].tolist())) == 1
-            ok = t < ntiles
-            u, t = u[ok], t[ok]
-            lr = u & 127
-            tx, q = t % nt, t // nt
-            ty, tz = q % nt, q // nt
-            x = TILE * tx + (lr & 7)
-            y = TILE * ty + ((lr >> 3) & 7)
-            k0 = TILE * tz + RUN * (lr >> 6)
-            inb = (x < P) & (y < P) & (k0 < P)
-            for w in range(RUN):
-                sel = inb & (k0 + w < P)
-                np.add.at(count, (k0[sel] + w, y[sel], x[sel]), 1)
-            assert (t[inb] < ntiles).all()
+        for q in range(EVAL_TILES // 8):
+            for w in range(8):
+                t = item * EVAL_TILES + q * 8 + w
+                if t >= ntiles:
+                    continue
+                seen[t] += 1
+                tx, r = t % nt, t // nt
+                ty, tz = r % nt, r // nt
+                for z, y, x in eval_tile_points(TILE * tx, TILE * ty, TILE * tz, P, bool(rng.integers(0, 2))):
+                    count[z, y, x] += 1
+    assert (seen == 1).all()
     assert (count == 1).all(), (N, np.argwhere(count != 1)[:5])
+
+
+@pytest.mark.parametrize("N", [4, 8, 12, 64, 96])
+def test_cell_groups_lie_in_one_tile(N):
+    """Classification skips a group of 4 cells by the flag of one tile: with N a
+    multiple of 4 the group is 4 cells of one row from x a multiple of 4, and the
+    tile's box (one point past its points) holds all their corners."""
+    CPT = const("S2_CELL_CPT", "s2m_device.h")
+    ncells = N ** 3
+    for c in range(0, ncells - 3, 4):
+        z, rem = divmod(c, N * N)
+        y, x = divmod(rem, N)
+        assert x % 4 == 0 and x + 3 < N
+        assert (x >> 3) == ((x + 3) >> 3)
+        lo, hi = TILE * (x >> 3), TILE * (x >> 3) + TILE  # box points lo .. hi
+        assert lo <= x and x + 3 + 1 <= hi
+    assert CPT % 4 == 0
 
 
 @pytest.mark.parametrize("N,planes", [(33, 5), (64, 9), (100, 3), (1024, 2)])

