@@ -329,6 +329,17 @@ def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=N
     e2e_ms = []
     parts = {"create_ms": 0.0, "copy_to_host_ms": 0.0, "free_ms": 0.0, "create_setup_ms": 0.0,
              "create_launch_ms": 0.0, "create_wait_ms": 0.0, "create_runs": 0.0}
+    # untimed warm-up of the same calls: the first create beside the timed mesh
+    # grows the stream-ordered pool (a one-time cost per process, like loading
+    # the module); later creates reuse the blocks the previous free returned
+    for _ in range(max(1, min(warmup, 3))):
+        h = ctypes.c_void_p()
+        rc = L.s2m_mesh_create(sdf.handle, ctypes.byref(p), ctypes.c_void_p(sp), ctypes.byref(h), err, len(err))
+        if rc != 0:
+            raise RuntimeError(err.value.decode())
+        L.s2m_mesh_copy_to_host(h, host_pos.data_ptr(), host_nrm.data_ptr(), None, host_tri.data_ptr(),
+                                ctypes.c_void_p(sp))
+        L.s2m_mesh_free(h)
     barrier()
     for i in range(e2e_steps or steps):
         with torch.cuda.stream(stream):

@@ -43,7 +43,8 @@ enum { S2_ST_TILES = 0, S2_ST_EVAL, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_
 static_assert(S2_NSTAGES == S2M_BATCH_STAGES, "stage count of the C ABI");
 #define S2_B_TILE 8          // lattice points per edge of a tile
 #define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
-#define S2_B_EVAL_TILES 16   // tiles per item of the evaluation (one warp per tile)
+#define S2_B_EVAL_TILES 64   // tiles per item of the evaluation (one warp per tile)
+#define S2_B_CELL_TILES 4    // classification tiles per item
 #define S2_B_VERT_CHUNK 256
 #define S2_ERR_BATCH_WAIT 0x20u
 
@@ -223,14 +224,20 @@ __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned ite
   }
 }
 
-// Classification tile `tile` of the job (the tickets of this stage come in
-// tile order, so the look-back only waits for tiles already taken).
-__device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned tile) {
+// Classification tiles item * S2_B_CELL_TILES .. of the job, in order (the
+// tickets of this stage come in tile order, so the look-back only waits for
+// tiles already taken).
+__device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned item) {
   const long long ncells = (long long)J.nzc * J.job.N * J.job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-  s2_cell_tile<true>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, tile, ntiles, ncells, 0, 0ull,
-                     J.cand.base + 1, J.mesh.wait_ns,
-                     S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx});
+#pragma unroll 1
+  for (unsigned k = 0; k < S2_B_CELL_TILES; ++k) {
+    const unsigned tile = item * S2_B_CELL_TILES + k;
+    if (tile >= ntiles) break;
+    s2_cell_tile<true>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, tile, ntiles, ncells, 0, 0ull,
+                       J.cand.base + 1, J.mesh.wait_ns,
+                       S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx});
+  }
 }
 
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
@@ -367,8 +374,9 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
         if (k == (int)sg.stage) busy[k] += s2_globaltimer() - t_item;
     }
     if (tid == 0 && !((hold & S2_HOLD_BATCH_ROWS) && sg.job == 0 && sg.stage == S2_ST_ROWS)) {
-      __threadfence();
-      atomicAdd(J.done + sg.stage, 1u);
+      // the block's writes (ordered before by the barrier), then the count:
+      // a release reduction that does not wait for its result
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(J.done + sg.stage) : "memory");
     }
   }
   if (tid == 0) {
@@ -666,27 +674,34 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
       J.nitems[S2_ST_TILES] = h.prune ? unsigned((ntiles + S2_B_TILES_ITEM - 1) / S2_B_TILES_ITEM) : 1u;
       J.nitems[S2_ST_EVAL] = unsigned((ntiles + S2_B_EVAL_TILES - 1) / S2_B_EVAL_TILES);
     }
-    J.nitems[S2_ST_CELLS] = unsigned(std::max<size_t>(1, cell_tiles));
+    J.nitems[S2_ST_CELLS] = unsigned(std::max<size_t>(1, (cell_tiles + S2_B_CELL_TILES - 1) / S2_B_CELL_TILES));
     J.nitems[S2_ST_VERT] = unsigned(std::min<unsigned long long>(128, std::max<unsigned long long>(1, n2 / 2048)));
     J.nitems[S2_ST_VCOMPACT] = unsigned(std::min<unsigned long long>(64, std::max<unsigned long long>(1, n2 / 8192)));
     J.nitems[S2_ST_ROWS] = unsigned(std::min<unsigned long long>(16, std::max<unsigned long long>(1, n2 / 16384)));
     J.nitems[S2_ST_QUADS] = unsigned(std::min<unsigned long long>(64, std::max<unsigned long long>(1, n2 / 8192)));
-    for (int s = 0; s < S2_NSTAGES; ++s) {
-      S2BatchSeg sg;
-      sg.start = ticket;
-      sg.job = unsigned(i);
-      sg.stage = unsigned(s);
-      sg.count = J.nitems[s];
-      sg.pad = 0;
-      segs.push_back(sg);
-      ticket += J.nitems[s];
-    }
     h.run = run_id;
     h.pos = J.mesh.pos;
     h.nrm = J.mesh.nrm;
     h.key = J.mesh.key;
     h.tris = J.mesh.tris;
   }
+  // Tickets stage by stage over the wave's jobs: every job's tile pass, then
+  // every job's lattice, and so on.  A job's stage still follows its previous
+  // stage in ticket order, and by the time its items are taken the previous
+  // stage's items were dispensed long before, so blocks rarely wait (in job
+  // order, each job's stages followed one another directly and blocks waited
+  // for the stage ahead of them).
+  for (int s = 0; s < S2_NSTAGES; ++s)
+    for (size_t i = 0; i < idx.size(); ++i) {
+      S2BatchSeg sg;
+      sg.start = ticket;
+      sg.job = unsigned(i);
+      sg.stage = unsigned(s);
+      sg.count = dj[i].nitems[s];
+      sg.pad = 0;
+      segs.push_back(sg);
+      ticket += dj[i].nitems[s];
+    }
   char *d_prog = arena + ztot + ctl_bytes + dtot;
   S2BatchJob *d_jobs = reinterpret_cast<S2BatchJob *>(d_prog + prog_bytes);
   S2BatchSeg *d_segs = reinterpret_cast<S2BatchSeg *>(reinterpret_cast<char *>(d_jobs) + jobs_bytes);

@@ -472,6 +472,8 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
                                              S2CellSkip skip = S2CellSkip{nullptr, 0u, 0}) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned long long s_excl;
+  __shared__ unsigned s_total;
+  __shared__ unsigned short s_cl[S2_CELL_TILE];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const long long c0 = (long long)tile * S2_CELL_TILE + (long long)S2_CELL_CPT * tid;
   unsigned decided = 0;  // bit g: group g lies in a decided tile
@@ -509,6 +511,22 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
   __syncthreads();
   if (warp == 0) {
     const unsigned tot = s2_warp_exclusive32(s_warp);
+    if (lane == 0) s_total = tot;
+  }
+  __syncthreads();
+  // the tile's candidates in order (cell offsets within the tile), then
+  // written one per thread: every thread's corner loads are in flight
+  // together, however the candidates fall among the threads
+  {
+    unsigned r = s_warp[warp] + (inc - cnt), rem = mask;
+    while (rem) {
+      const unsigned m = (unsigned)__ffs(rem) - 1u;
+      rem &= rem - 1u;
+      s_cl[r++] = (unsigned short)(S2_CELL_CPT * tid + m);
+    }
+  }
+  if (warp == 0) {
+    const unsigned tot = s_total;
     const unsigned long long excl = s2_lookback(status, tile, tot, err, wait_ns);
     if (lane == 0) {
       s_excl = excl;
@@ -516,26 +534,24 @@ __device__ __forceinline__ void s2_cell_tile(const S2Job &job, const float *__re
     }
   }
   __syncthreads();
-  unsigned long long o = base + s_excl + s_warp[warp] + (inc - cnt);
-  unsigned rem = mask;
-  while (rem) {
-    const int m = __ffs(rem) - 1;
-    rem &= rem - 1u;
+  const unsigned total = s_total;
+  const unsigned long long first = base + s_excl;
+#pragma unroll 1
+  for (unsigned r = tid; r < total; r += S2_CELL_BLOCK) {
+    const unsigned long long o = first + r;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
-      ++o;
       continue;
     }
-    const S2Cell cell = s2_cell_of(job, c0 + m, zc0);
+    const S2Cell cell = s2_cell_of(job, (long long)tile * S2_CELL_TILE + s_cl[r], zc0);
     float v[8];
     s2_load_corners<CG>(job, ring, cell, v);  // candidates are few: re-read their corners
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
     float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
     dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-    ++o;
   }
-  __syncthreads();  // s_warp / s_excl are reused by the block's next tile
+  __syncthreads();  // s_warp / s_excl / s_cl are reused by the block's next tile
 }
 
 // ---------------------------------------------------------------------------
@@ -612,55 +628,29 @@ __device__ __forceinline__ unsigned long long s2_vertex_warp(const F &sdf, const
   const unsigned lt = s2_lanemask_lt();
   float mn[3] = {s2_coord(j, c.x), s2_coord(j, c.y), s2_coord(j, c.z)};
   float mx[3] = {__fadd_rn(mn[0], j.size), __fadd_rn(mn[1], j.size), __fadd_rn(mn[2], j.size)};
-  // Corners whose lattice value is not the reference's value: the off-lattice
-  // ones (evaluated at the cell's reference coordinates) and those the
-  // lattice pass left unknown (NaN or +-inf: decided tiles of the pruned
-  // evaluations; a value that really is non-finite is evaluated again, to
-  // the same value).  An unknown corner that is on the lattice has reference
-  // coordinates equal to its lattice coordinates, so both kinds are
-  // evaluated at the cell's bounds.
-  //   Where the lattice value lies at or beyond the guard (+-inf included),
-  // its sign is the reference value's sign -- the classification rests on
-  // the same fact -- so such a corner is evaluated only when it ends an edge
-  // whose signs differ, where the crossing needs its value (a second round
-  // of requests, after the others have settled every sign).  With
-  // S2M_JOB_EXACT_CORNERS every such corner is evaluated in the first round.
-  unsigned first = 0u, later = 0u;
+  // Corners evaluated here: the off-lattice ones (at the cell's reference
+  // coordinates) and those the lattice pass left unknown (NaN or +-inf:
+  // decided tiles of the pruned evaluations; a value that really is
+  // non-finite is evaluated again, to the same value).  An unknown corner
+  // that is on the lattice has reference coordinates equal to its lattice
+  // coordinates, so both kinds are evaluated at the cell's bounds.  (Leaving
+  // out the off-lattice corners whose sign the lattice value settles and that
+  // end no crossing edge, in a second round of requests, was slower: fewer
+  // evaluations, but more registers and code in this latency-bound kernel.)
+  unsigned off = 0u;
   if (active) {
-    unsigned diff = s2_off_mask(j, c) & 0xfeu;
+    off = s2_off_mask(j, c) & 0xfeu;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-      if (!(fabsf(v[k]) <= 3.40282347e38f)) diff |= 1u << k;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if ((diff >> k) & 1u) {
-        if (!j.exact && fabsf(v[k]) >= j.guard) later |= 1u << k;
-        else first |= 1u << k;
-      }
+      if (!(fabsf(v[k]) <= 3.40282347e38f)) off |= 1u << k;
   }
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     ws.lo[lane][a] = mn[a];
     ws.hi[lane][a] = mx[a];
   }
-  // 1. off-lattice and unknown corners, in up to two rounds (one call site:
-  // the SDF's code is large, and a second copy of it costs instruction fetch)
-  unsigned req = first;
-#pragma unroll 1
-  for (int round = 0; round < 2; ++round) {
-    s2_corner_requests(sdf, req, v, ws);
-    if (round == 1) break;
-    const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
-    const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
-    unsigned sg = 0u;
-    req = 0u;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) sg |= (v[k] > 0.0f ? 1u : 0u) << k;
-#pragma unroll
-    for (int e = 0; e < 12; ++e)
-      if (((sg >> ea[e]) ^ (sg >> eb[e])) & 1u) req |= ((1u << ea[e]) | (1u << eb[e])) & later;
-    if (!__any_sync(S2_FULL, req != 0u)) break;
-  }
+  // 1. off-lattice and unknown corners
+  s2_corner_requests(sdf, off, v, ws);
   // 2. crossings and mass point (dualcontour.wgsl:86-131)
   const int ea[12] = {0, 2, 1, 3, 0, 4, 1, 5, 0, 4, 2, 6};
   const int eb[12] = {4, 6, 5, 7, 2, 6, 3, 7, 1, 5, 3, 7};
