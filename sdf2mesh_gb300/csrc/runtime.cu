@@ -326,6 +326,20 @@ void cache_store(const std::string &dir, const std::string &key, const std::vect
 // sm_103a (or the cached CUBIN of the same program), loaded as a library.
 // `defines` selects the program's kernels; `qef` builds the precision-mode
 // vertex kernel alone.  *hit tells whether the CUBIN came from the cache.
+// The vertex kernel's dynamic shared memory (S2_VX_SMEM_BYTES) is above the
+// 48 KB that a launch gets without asking.
+int vertex_smem_attribute(cudaKernel_t k, char *err, size_t errlen) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S2_VX_SMEM_BYTES), dev);
+  if (e != cudaSuccess) {
+    set_err(err, errlen, std::string("vertex kernel shared memory: ") + cudaGetErrorString(e));
+    return S2M_E_CUDA;
+  }
+  return S2M_OK;
+}
+
 int nvrtc_build(const s2m_sdf *s, bool qef, const char *defines, cudaLibrary_t *lib, bool *hit, char *err,
                 size_t errlen) {
   std::string src;
@@ -433,7 +447,7 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
   }
-  return S2M_OK;
+  return vertex_smem_attribute(s->k_vertices, err, errlen);
 }
 
 // The QEF vertex kernel of an SDF, built once on its first precision-mode job.
@@ -448,7 +462,7 @@ int ensure_qef_module(const s2m_sdf *cs, char *err, size_t errlen) {
     set_err(err, errlen, "QEF vertex kernel missing from the compiled module");
     return S2M_E_CUDA;
   }
-  return S2M_OK;
+  return vertex_smem_attribute(s->k_vertices_qef, err, errlen);
 }
 
 // ---------------------------------------------------------------------------
@@ -643,6 +657,22 @@ template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
 unsigned long long *prune_bases(const s2m_mesh *m) { return prune_at<unsigned long long>(m, m->prune_base_off); }
 unsigned *prune_list_counts(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
+// Device pointers of the counters inside jobctl.
+struct JobCtl {
+  unsigned long long *ntris, *invalid, *vtotal;
+  unsigned *err;
+  unsigned *counters;
+};
+JobCtl jobctl(const s2m_mesh *m) {
+  JobCtl c;
+  c.ntris = m->jobctl + 0;
+  c.invalid = m->jobctl + 1;
+  c.vtotal = m->jobctl + 2;
+  c.err = reinterpret_cast<unsigned *>(m->jobctl + 3);
+  c.counters = reinterpret_cast<unsigned *>(m->jobctl + 4);  // 8 x u32
+  return c;
+}
+
 // Tile pass over slabs [s_begin, s_end) (coarse boxes, then tiles) and the
 // pruned evaluation of slab s.
 cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t st) {
@@ -680,16 +710,18 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
     const int W1 = m->sdf->prune_words + 1;
     const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
     const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
-    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs);
+    unsigned *chunks = jobctl(m).counters + 5;  // set to zero by the fill, taken by the listed evaluation
+    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs, chunks);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
                            (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
     const unsigned *count = prune_list_counts(m) + s;
-    void *largs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &list, &count};
-    // warps stride over the list (its length is on the device): 16 blocks per SM
-    const long long lblocks = std::min<long long>((g.ntiles + 3) / 4, (long long)device_sm_count() * 16);
-    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned(lblocks)), dim3(S2_PT_BLOCK), largs, 0,
+    void *largs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &list, &count, &chunks};
+    // one block per SM takes chunks of the list (its length is on the device)
+    const long long lblocks = std::min<long long>((g.ntiles + S2_PL_BLOCK / 32 - 1) / (S2_PL_BLOCK / 32),
+                                                  (long long)device_sm_count());
+    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned(lblocks)), dim3(S2_PL_BLOCK), largs, 0,
                             st);
   }
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
@@ -882,22 +914,6 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   return S2M_OK;
 }
 
-// Device pointers of the counters inside jobctl.
-struct JobCtl {
-  unsigned long long *ntris, *invalid, *vtotal;
-  unsigned *err;
-  unsigned *counters;
-};
-JobCtl jobctl(const s2m_mesh *m) {
-  JobCtl c;
-  c.ntris = m->jobctl + 0;
-  c.invalid = m->jobctl + 1;
-  c.vtotal = m->jobctl + 2;
-  c.err = reinterpret_cast<unsigned *>(m->jobctl + 3);
-  c.counters = reinterpret_cast<unsigned *>(m->jobctl + 4);  // 8 x u32
-  return c;
-}
-
 // Two events per launch when profiling (created once, reused every run).
 cudaError_t prof_mark(s2m_mesh *m, cudaStream_t st, int kind, double units, bool after) {
   if (!m->profile) return cudaSuccess;
@@ -1067,10 +1083,11 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   unsigned long long *vc_base = m->cand_status;
   unsigned *vc_cnt = reinterpret_cast<unsigned *>(m->cand_status + 2);
   unsigned long long *vc_off = m->cand_status + vc_ctrl_offsets(m->vc_tiles);
-  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt};
-  const unsigned vx_grid = unsigned(sms) * 16;
+  unsigned *vx_chunks = c.counters + 4;  // zeroed with jobctl at the start of the job
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &vx_chunks};
+  const unsigned vx_grid = unsigned(sms);  // one block per SM (S2_VX_BLOCK threads, 64 registers each)
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
-  S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, 0, st));
+  S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, S2_VX_SMEM_BYTES, st));
   S2_LAUNCH(3, 0, (s2m_vc_scan<<<1, 256, 0, st>>>(cand, nslabs, vc_cnt, vc_off, vc_base, md), cudaGetLastError()));
   const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
   S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs, vc_off), cudaGetLastError()));

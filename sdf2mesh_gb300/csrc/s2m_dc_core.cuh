@@ -579,6 +579,8 @@ struct S2WarpScratch {
   float pos[32][3];
   float nv[32][4];
 };
+// Dynamic shared memory of the vertex kernel (s2m_vertices).
+#define S2_VX_SMEM_BYTES (sizeof(S2WarpScratch) * (S2_VX_BLOCK / 32) + sizeof(void *) * S2_VX_BLOCK)
 
 // Lane by lane, the corners in `req` (bit k: corner k) evaluated at the
 // cell's reference coordinates (ws.lo / ws.hi), 32 requests of the warp at a

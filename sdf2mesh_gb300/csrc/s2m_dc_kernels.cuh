@@ -451,17 +451,28 @@ template <bool RUN4>
 __device__ __forceinline__ void s2_eval_pruned_listed(const S2Job &job, float *__restrict__ ring, S2PointBits pb,
                                                       const unsigned *__restrict__ bits, int k0, int nk, int tzs,
                                                       const unsigned *__restrict__ list,
-                                                      const unsigned *__restrict__ list_count) {
-  // The list's length is known only on the device: the grid is sized for the
-  // GPU (a few blocks per SM), and its warps stride over the list.
-  __shared__ unsigned s_bits[S2_PT_BLOCK / 32][S2M_TILE_WORDS];
+                                                      const unsigned *__restrict__ list_count, unsigned *chunk_ctr) {
+  // The list's length is known only on the device.  One block of S2_PL_BLOCK
+  // threads per SM takes chunks of S2_PL_BLOCK / 32 consecutive listed tiles
+  // from `chunk_ctr` (zero at launch), one tile per warp: every warp on an SM
+  // then runs neighbouring tiles, whose pruned paths share code.  (With 16
+  // blocks of 4 warps per SM striding over the list, the SM's warps ran 64
+  // different places of the pruned SDF and stalled on instruction fetch.)
+  __shared__ unsigned s_bits[S2_PL_BLOCK / 32][S2M_TILE_WORDS];
+  __shared__ unsigned s_chunk;
   const int lane = (int)(threadIdx.x & 31u);
-  const unsigned n = __ldg(list_count), stride = gridDim.x * (S2_PT_BLOCK / 32);
-  for (unsigned i = blockIdx.x * (S2_PT_BLOCK / 32) + (threadIdx.x >> 5); i < n; i += stride) {  // whole warps
+  const unsigned n = __ldg(list_count);
+  for (;;) {
+    __syncthreads();  // every thread has read the previous chunk's number
+    if (threadIdx.x == 0) s_chunk = atomicAdd(chunk_ctr, 1u);
+    __syncthreads();
+    const unsigned long long first = (unsigned long long)s_chunk * (S2_PL_BLOCK / 32);
+    if (first >= n) break;
+    const unsigned long long i = first + (threadIdx.x >> 5);  // whole warps
+    if (i >= n) continue;
     const unsigned t = __ldg(list + i);
     const S2PruneTile tl = s2_prune_tile(job, (long long)t, k0, nk, tzs);
     if (tl.kb > tl.ke) continue;
-    __syncwarp();  // the previous tile's bits are no longer read
     if (lane < S2M_TILE_WORDS) s_bits[threadIdx.x >> 5][lane] = __ldg(bits + (unsigned long long)t * S2M_TILE_WORDS + lane);
     __syncwarp();
     s2_eval_tile<RUN4>(job, ring, pb, tl, s_bits[threadIdx.x >> 5]);
@@ -469,10 +480,11 @@ __device__ __forceinline__ void s2_eval_pruned_listed(const S2Job &job, float *_
 }
 
 #define S2_EVALPL_VARIANT(NAME, MINB, RUN4)                                                       \
-  extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
+  extern "C" __global__ void __launch_bounds__(S2_PL_BLOCK, 1)                                    \
   NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
-       int tzs, const unsigned *__restrict__ list, const unsigned *__restrict__ list_count) {     \
-    s2_eval_pruned_listed<RUN4>(job, ring, pb, bits, k0, nk, tzs, list, list_count);              \
+       int tzs, const unsigned *__restrict__ list, const unsigned *__restrict__ list_count,       \
+       unsigned *chunk_ctr) {                                                                     \
+    s2_eval_pruned_listed<RUN4>(job, ring, pb, bits, k0, nk, tzs, list, list_count, chunk_ctr);   \
   }
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
@@ -542,24 +554,39 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // candidates, activate more segments; per-tile bits were faster.)  vc_cnt[t]
 // counts the vertices of candidates t * S2_VC_TILE .. (t + 1) * S2_VC_TILE -
 // 1 (for s2m_vc_scan).
+//   One block of S2_VX_BLOCK threads per SM takes chunks of S2_VX_BLOCK
+// consecutive candidates (in tile order) from `chunk_ctr` (zero at launch),
+// one warp-sized run per warp: every warp on an SM then evaluates
+// neighbouring tiles, whose pruned paths share code.  (With 8 blocks of 128
+// threads per SM, each taking runs a grid stride apart, the SM's warps ran
+// 32 different places of the pruned SDF and stalled on instruction fetch.)
+// Dynamic shared memory: S2_VX_BLOCK / 32 warp scratch areas, then one
+// pointer per thread (s2_vertices_smem_bytes).
 #if !defined(S2M_SELECT) || defined(S2M_WANT_VERTICES)
-extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK, 8)
+extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK, 1)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
-             int nzc, const unsigned *perm, unsigned *vc_cnt) {
-  __shared__ S2WarpScratch s_ws[S2_VX_BLOCK / 32];
+             int nzc, const unsigned *perm, unsigned *vc_cnt, unsigned *chunk_ctr) {
+  extern __shared__ __align__(16) unsigned char s2_vx_smem[];
+  __shared__ unsigned s_chunk;
+  S2WarpScratch *const s_ws = reinterpret_cast<S2WarpScratch *>(s2_vx_smem);
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
-  __shared__ const unsigned *s_mp[S2_VX_BLOCK];
+  const unsigned **const s_mp =
+      reinterpret_cast<const unsigned **>(s2_vx_smem + sizeof(S2WarpScratch) * (S2_VX_BLOCK / 32));
   S2UserSdfPruned psdf;
   psdf.mp = s_mp;
 #else
   (void)tbits; (void)tbase; (void)D; (void)nzc;
 #endif
   const S2UserSdfCall sdf;
-  // grid-stride over warp-sized runs of candidates, all lanes together
-  const unsigned long long stride = (unsigned long long)gridDim.x * S2_VX_BLOCK;
-  for (unsigned long long base = (unsigned long long)blockIdx.x * S2_VX_BLOCK + (threadIdx.x & ~31u); base < n;
-       base += stride) {
+  const unsigned long long nchunks = (n + S2_VX_BLOCK - 1) / S2_VX_BLOCK;
+  for (;;) {
+    __syncthreads();  // every thread has read the previous chunk's number
+    if (threadIdx.x == 0) s_chunk = atomicAdd(chunk_ctr, 1u);
+    __syncthreads();
+    const unsigned long long chunk = s_chunk;
+    if (chunk >= nchunks) break;
+    const unsigned long long base = chunk * S2_VX_BLOCK + (threadIdx.x & ~31u);
     const unsigned long long i = base + (threadIdx.x & 31u);
     const bool active = i < n;
     const unsigned long long o = active && perm ? (unsigned long long)perm[i] : i;

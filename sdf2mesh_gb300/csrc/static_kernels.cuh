@@ -122,7 +122,9 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
 // bytes as 0, which s2m_evalpl_* overwrites afterwards.
 __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits pb,
                                                         const unsigned *__restrict__ tiles, int tile_words, int k0,
-                                                        int nk, int tzs) {
+                                                        int nk, int tzs, unsigned *chunk_reset) {
+  // the listed evaluation that follows this launch takes its chunks from zero
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *chunk_reset = 0u;
   const int WP = (job.P + 31) >> 5;
   const int q = (int)(blockIdx.x * 256u + threadIdx.x);  // word (y, w) of the plane
   if (q >= job.P * WP) return;
