@@ -44,7 +44,9 @@ static_assert(S2_NSTAGES == S2M_BATCH_STAGES, "stage count of the C ABI");
 #define S2_B_TILE 8          // lattice points per edge of a tile
 #define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
 #define S2_B_EVAL_TILES 64   // tiles per item of the evaluation (one warp per tile)
-#define S2_B_CELL_TILES 4    // classification tiles per item
+#define S2_B_CELL_TILES 1    // classification tiles per item (a later tile of an item would publish its
+                             // aggregate only after the item's earlier tiles, and the next item's
+                             // look-back waits for it: items ran one after another)
 #define S2_B_VERT_CHUNK 256
 #define S2_ERR_BATCH_WAIT 0x20u
 

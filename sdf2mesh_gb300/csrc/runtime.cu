@@ -447,7 +447,7 @@ int compile_module(s2m_sdf *s, char *err, size_t errlen) {
     set_err(err, errlen, "kernels missing from the compiled module");
     return S2M_E_CUDA;
   }
-  return vertex_smem_attribute(s->k_vertices, err, errlen);
+  return s->prune_words > 0 ? vertex_smem_attribute(s->k_vertices, err, errlen) : S2M_OK;
 }
 
 // The QEF vertex kernel of an SDF, built once on its first precision-mode job.
@@ -462,7 +462,7 @@ int ensure_qef_module(const s2m_sdf *cs, char *err, size_t errlen) {
     set_err(err, errlen, "QEF vertex kernel missing from the compiled module");
     return S2M_E_CUDA;
   }
-  return vertex_smem_attribute(s->k_vertices_qef, err, errlen);
+  return S2M_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1085,9 +1085,12 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   unsigned long long *vc_off = m->cand_status + vc_ctrl_offsets(m->vc_tiles);
   unsigned *vx_chunks = c.counters + 4;  // zeroed with jobctl at the start of the job
   void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &vx_chunks};
-  const unsigned vx_grid = unsigned(sms);  // one block per SM (S2_VX_BLOCK threads, 64 registers each)
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
-  S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(vx_grid), dim3(S2_VX_BLOCK), vargs, S2_VX_SMEM_BYTES, st));
+  if (m->sdf->prune_words > 0 && !j.qef)  // chunked form: one block per SM (S2_VX_BLOCK threads, 64 registers each)
+    S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(unsigned(sms)), dim3(S2_VX_BLOCK), vargs, S2_VX_SMEM_BYTES,
+                                     st));
+  else
+    S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(unsigned(sms) * 16), dim3(S2_VX_SMALL), vargs, 0, st));
   S2_LAUNCH(3, 0, (s2m_vc_scan<<<1, 256, 0, st>>>(cand, nslabs, vc_cnt, vc_off, vc_base, md), cudaGetLastError()));
   const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
   S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs, vc_off), cudaGetLastError()));

@@ -554,31 +554,37 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 // candidates, activate more segments; per-tile bits were faster.)  vc_cnt[t]
 // counts the vertices of candidates t * S2_VC_TILE .. (t + 1) * S2_VC_TILE -
 // 1 (for s2m_vc_scan).
-//   One block of S2_VX_BLOCK threads per SM takes chunks of S2_VX_BLOCK
-// consecutive candidates (in tile order) from `chunk_ctr` (zero at launch),
-// one warp-sized run per warp: every warp on an SM then evaluates
-// neighbouring tiles, whose pruned paths share code.  (With 8 blocks of 128
-// threads per SM, each taking runs a grid stride apart, the SM's warps ran
-// 32 different places of the pruned SDF and stalled on instruction fetch.)
-// Dynamic shared memory: S2_VX_BLOCK / 32 warp scratch areas, then one
-// pointer per thread (s2_vertices_smem_bytes).
+//   Modules with a pruning form (reference rule): one block of S2_VX_BLOCK
+// threads per SM takes chunks of S2_VX_BLOCK consecutive candidates (in tile
+// order) from `chunk_ctr` (zero at launch), one warp-sized run per warp:
+// every warp on an SM then evaluates neighbouring tiles, whose pruned paths
+// share code.  (With 8 blocks of 128 threads per SM, each taking runs a grid
+// stride apart, the SM's warps ran 32 different places of the pruned SDF and
+// stalled on instruction fetch.)  Dynamic shared memory: S2_VX_SMEM_BYTES.
+// Other modules (full SDF; precision mode, whose per-lane QEF work varies
+// too much for a block-wide step): blocks of S2_VX_SMALL threads, 8 per SM,
+// striding over the runs.
+#if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
+#define S2_VX_CHUNKED 1
+#define S2_VX_THREADS S2_VX_BLOCK
+#define S2_VX_MINB 1
+#else
+#define S2_VX_THREADS S2_VX_SMALL
+#define S2_VX_MINB 8
+#endif
 #if !defined(S2M_SELECT) || defined(S2M_WANT_VERTICES)
-extern "C" __global__ void __launch_bounds__(S2_VX_BLOCK, 1)
+extern "C" __global__ void __launch_bounds__(S2_VX_THREADS, S2_VX_MINB)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
              int nzc, const unsigned *perm, unsigned *vc_cnt, unsigned *chunk_ctr) {
+  const unsigned long long n = min(cand.base[nslabs], cand.cap);
+#ifdef S2_VX_CHUNKED
   extern __shared__ __align__(16) unsigned char s2_vx_smem[];
   __shared__ unsigned s_chunk;
   S2WarpScratch *const s_ws = reinterpret_cast<S2WarpScratch *>(s2_vx_smem);
-  const unsigned long long n = min(cand.base[nslabs], cand.cap);
-#if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
   const unsigned **const s_mp =
       reinterpret_cast<const unsigned **>(s2_vx_smem + sizeof(S2WarpScratch) * (S2_VX_BLOCK / 32));
   S2UserSdfPruned psdf;
   psdf.mp = s_mp;
-#else
-  (void)tbits; (void)tbase; (void)D; (void)nzc;
-#endif
-  const S2UserSdfCall sdf;
   const unsigned long long nchunks = (n + S2_VX_BLOCK - 1) / S2_VX_BLOCK;
   for (;;) {
     __syncthreads();  // every thread has read the previous chunk's number
@@ -587,6 +593,15 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
     const unsigned long long chunk = s_chunk;
     if (chunk >= nchunks) break;
     const unsigned long long base = chunk * S2_VX_BLOCK + (threadIdx.x & ~31u);
+#else
+  __shared__ S2WarpScratch s_ws[S2_VX_SMALL / 32];
+  (void)tbits; (void)tbase; (void)D; (void)nzc; (void)chunk_ctr;
+  // grid-stride over warp-sized runs of candidates, all lanes together
+  const unsigned long long stride = (unsigned long long)gridDim.x * S2_VX_SMALL;
+  for (unsigned long long base = (unsigned long long)blockIdx.x * S2_VX_SMALL + (threadIdx.x & ~31u); base < n;
+       base += stride) {
+#endif
+    const S2UserSdfCall sdf;
     const unsigned long long i = base + (threadIdx.x & 31u);
     const bool active = i < n;
     const unsigned long long o = active && perm ? (unsigned long long)perm[i] : i;

@@ -125,7 +125,8 @@ struct S2MeshDev {
 #define S2_PT_BLOCK 128
 #define S2_PT_COARSE 4            /* tiles per coarse box of the tile pass, along x and y */
 #define S2_PT_COARSE_Z 2          /* ... and layers of tiles along z */
-#define S2_VX_BLOCK 1024          /* s2m_vertices: one block per SM */
+#define S2_VX_BLOCK 1024          /* s2m_vertices with a pruning form: one block per SM */
+#define S2_VX_SMALL 128           /* s2m_vertices otherwise: 8 blocks per SM */
 #define S2_PL_BLOCK 1024          /* s2m_evalpl_*: one block per SM, one listed tile per warp */
 #define S2_VC_BLOCK 256
 #define S2_VC_CPT 4
