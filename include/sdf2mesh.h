@@ -237,6 +237,31 @@ int s2m_mesh_copy_to_host(const s2m_mesh *mesh, float *pos, float *nrm, uint64_t
 /* TriangleMesh::write_to_file (mesh.rs:182-196): STL or PLY by extension. */
 int s2m_mesh_write(const s2m_mesh *mesh, const char *path, char *err, size_t errlen);
 
+/* ---- one call to a mesh in host memory -----------------------------------
+   Replaces the reference's generate() returning its TriangleMesh in host
+   memory (main.rs:177-364, lib.rs TriangleMesh): s2m_mesh_create +
+   s2m_mesh_copy_to_host + s2m_mesh_free in one call, with the same bits.  A
+   large job runs as `parts` slices of cell planes along z (0: chosen by the
+   library, 1: one piece); each part's device-to-host copy then runs while the
+   next part's kernels do.  A part after the first also meshes the last cell
+   plane of the one below it (its quads need those vertices) and copies none
+   of it.  The arrays are pinned host memory owned by the library until
+   s2m_host_mesh_free. */
+typedef struct {
+  const float *pos;       /* 3 * nverts (x, y, z)                                  */
+  const float *nrm;       /* 3 * nverts unit normals                               */
+  const uint32_t *tris;   /* 3 * ntris vertex indices                              */
+  uint64_t nverts;
+  uint64_t ntris;
+  uint64_t invalid_quads;
+  uint32_t resolution;    /* N actually used                                       */
+  uint32_t parts;         /* z parts the job ran as                                */
+  void *owner;            /* library bookkeeping                                   */
+} s2m_host_mesh;
+int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t parts, void *stream,
+                      s2m_host_mesh *out, char *err, size_t errlen);
+void s2m_host_mesh_free(s2m_host_mesh *mesh);
+
 void s2m_mesh_free(s2m_mesh *mesh);
 
 /* Per-kernel device time of a mesh's runs, from CUDA events recorded on the

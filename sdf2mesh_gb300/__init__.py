@@ -70,6 +70,13 @@ class MeshInfo(ctypes.Structure):
     ]
 
 
+class HostMesh(ctypes.Structure):
+    """s2m_host_mesh: the mesh in library-owned pinned host memory."""
+    _fields_ = [("pos", ctypes.c_void_p), ("nrm", ctypes.c_void_p), ("tris", ctypes.c_void_p),
+                ("nverts", ctypes.c_uint64), ("ntris", ctypes.c_uint64), ("invalid_quads", ctypes.c_uint64),
+                ("resolution", ctypes.c_uint32), ("parts", ctypes.c_uint32), ("owner", ctypes.c_void_p)]
+
+
 class NoallocMesh(ctypes.Structure):
     """s2m_noalloc_mesh: caller-owned device outputs and the counts written back."""
     _fields_ = [("pos", ctypes.c_void_p), ("nrm", ctypes.c_void_p), ("cell", ctypes.c_void_p),
@@ -171,6 +178,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
             "s2m_mesh_set_wait_limit": ([vp, ctypes.c_double], i),
             "s2m_batch_set_wait_limit": ([vp, ctypes.c_double, ctypes.c_double], i),
             "s2m_batch_set_pruning": ([vp, i], i),
+            "s2m_mesh_generate": ([vp, ctypes.POINTER(Params), u32, vp, ctypes.POINTER(HostMesh), ctypes.c_char_p,
+                                   sz], i),
+            "s2m_host_mesh_free": ([ctypes.POINTER(HostMesh)], None),
             "s2m_batch_stage_profile": ([vp, dp, u32, dp], i),
             "s2m_measure_sfu_peak": ([dp, vp], i),
             "s2m_csg_from_source": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_float), u32, ctypes.POINTER(u32),
@@ -764,6 +774,33 @@ def generate(sdf, state: AppState | None = None, stream: int = 0) -> TriangleMes
         return dm.to_host(stream)
     finally:
         dm.close()
+
+
+def generate_host(sdf, state: AppState | None = None, parts: int = 0, stream: int = 0) -> TriangleMesh:
+    """One call to a host mesh (s2m_mesh_generate): positions, normals and
+    triangle indices, the same bits as `generate`; a large job runs as z parts
+    whose copies to host memory overlap the next part's kernels (parts=0: the
+    library's choice).  `info` holds the parts it ran as."""
+    if isinstance(sdf, Sdf3DShader):
+        sdf = sdf.compile()
+    st = state or AppState()
+    p = st.params()
+    hm = HostMesh()
+    err = _errbuf()
+    L = load_library()
+    _check(L.s2m_mesh_generate(sdf.handle, ctypes.byref(p), int(parts), ctypes.c_void_p(stream), ctypes.byref(hm),
+                               err, len(err)), err, "generate")
+    try:
+        nv, nt = int(hm.nverts), int(hm.ntris)
+        fp = ctypes.POINTER(ctypes.c_float)
+        pos = np.ctypeslib.as_array(ctypes.cast(hm.pos, fp), (max(nv, 1) * 3,))[:nv * 3].reshape(nv, 3).copy()
+        nrm = np.ctypeslib.as_array(ctypes.cast(hm.nrm, fp), (max(nv, 1) * 3,))[:nv * 3].reshape(nv, 3).copy()
+        tris = np.ctypeslib.as_array(ctypes.cast(hm.tris, ctypes.POINTER(ctypes.c_uint32)),
+                                     (max(nt, 1) * 3,))[:nt * 3].reshape(nt, 3).copy()
+        info = {"parts": int(hm.parts), "resolution": int(hm.resolution)}
+        return TriangleMesh(pos, nrm, tris, invalid_quads=int(hm.invalid_quads), info=info)
+    finally:
+        L.s2m_host_mesh_free(ctypes.byref(hm))
 
 
 def measure_sfu_peak(stream: int = 0) -> float:

@@ -212,6 +212,12 @@ struct s2m_mesh {
   unsigned long long *jobctl = nullptr;  // [ntris, invalid, vtotal, err | counters[8]]
   // host results
   unsigned long long *h_read = nullptr;  // pinned readback
+  // z part of the lattice (s2m_mesh_generate): cell planes zpart_begin ..
+  // zpart_end - 1, zpart_end < 0 for the whole job; zfrac = its share of the
+  // job's cell planes (for the learned capacities)
+  int zpart_begin = 0, zpart_end = -1;
+  double zfrac = 1.0;
+  unsigned quads_from_z = 0;  // vertices with a lower label z make no quads (the context plane of a part)
   // host time of the last s2m_mesh_create (ms) and its pipeline runs
   double t_setup = 0, t_launch = 0, t_wait = 0;
   unsigned runs = 0;
@@ -546,7 +552,18 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   j.qef = (p.flags & S2M_JOB_QEF) ? 1 : 0;
   j.magic_n = uint32_t((1ull << 32) / uint64_t(j.N) + 1);
   j.magic_p = uint32_t((1ull << 32) / uint64_t(j.P) + 1);
-  m->nzc = j.lag ? int(N) - 1 : int(N);
+  // cell planes of the job: the whole lattice, or the part zpart_begin ..
+  // zpart_end - 1 (s2m_mesh_generate's z parts)
+  const int full_nzc = j.lag ? int(N) - 1 : int(N);
+  if (m->zpart_end >= 0) {
+    j.zb = m->zpart_begin;
+    m->nzc = std::max(0, std::min(full_nzc, m->zpart_end) - m->zpart_begin);
+  } else {
+    j.zb = 0;
+    m->nzc = full_nzc;
+  }
+  j.pad = 0;
+  m->zfrac = full_nzc > 0 ? double(m->nzc) / double(full_nzc) : 1.0;
   // Slab depth.  Full evaluation: the ring of D + 1 lattice planes is sized
   // to stay resident in the 126 MB L2 between the evaluation and the point
   // bits pass -- unless the autotuner measured the evaluation at
@@ -591,9 +608,10 @@ S2PointBits point_bits(const s2m_mesh *m) {
 
 // Planes k0 .. k0 + nk - 1 that slab s evaluates.
 void slab_planes(const s2m_mesh *m, int s, int &k0, int &nk) {
-  const int zc0 = s * m->D;
-  const int zc1 = std::min(m->nzc, zc0 + m->D);
-  k0 = s == 0 ? 0 : zc0 + 1;
+  const int zb = m->job.zb;
+  const int zc0 = zb + s * m->D;
+  const int zc1 = std::min(zb + m->nzc, zc0 + m->D);
+  k0 = s == 0 ? zb : zc0 + 1;
   nk = zc1 - k0 + 1;
 }
 
@@ -834,7 +852,7 @@ void initial_caps(const s2m_mesh *m, const s2m_params &p, unsigned long long &ca
     st = m->sdf->seen_tri;
   }
   const double n2 = double(N * N);
-  auto learned = [&](double ratio) { return (unsigned long long)(ratio * n2 * 1.1) + 4096; };
+  auto learned = [&](double ratio) { return (unsigned long long)(ratio * n2 * m->zfrac * 1.1) + 4096; };
   cand_cap = std::min(N3, std::max<unsigned long long>({65536, 8 * N * N, learned(sc)}));
   vcap = p.max_vertices ? p.max_vertices
                         : std::min(N3, std::max<unsigned long long>({65536, 6 * N * N, learned(sv)}));
@@ -845,7 +863,7 @@ void initial_caps(const s2m_mesh *m, const s2m_params &p, unsigned long long &ca
 
 // Remember the surface density of a finished job for the SDF's next jobs.
 void learn_caps(const s2m_mesh *m) {
-  const double n2 = double(m->N) * double(m->N);
+  const double n2 = double(m->N) * double(m->N) * m->zfrac;  // per N^2 of a whole job
   if (!m->sdf || n2 < 4096.0) return;  // tiny jobs say little about large ones
   std::lock_guard<std::mutex> lock(m->sdf->tune_mu);
   m->sdf->seen_cand = std::max(m->sdf->seen_cand, double(m->ncand) / n2);
@@ -954,6 +972,31 @@ void prof_collect(s2m_mesh *m) {
     ++m->launches;                                                     \
   } while (0)
 
+// The device view of a mesh's outputs and counters.
+S2MeshDev mesh_dev(const s2m_mesh *m) {
+  const JobCtl c = jobctl(m);
+  S2MeshDev md;
+  md.pos = m->pos;
+  md.nrm = m->nrm;
+  md.key = m->key;
+  md.tris = m->tris;
+  md.vcap = m->vcap;
+  md.tcap = m->tcap;
+  md.vtotal = c.vtotal;
+  md.rowcnt = m->rowcnt;
+  md.rowstart = m->rowstart;
+  md.scan_status = m->scan_status;
+  md.counters = c.counters;
+  md.ntris = c.ntris;
+  md.invalid = c.invalid;
+  md.err = c.err;
+  md.wait_ns = m->wait_ns;
+  md.hold = 0;
+  if (const char *h = std::getenv("S2M_TEST_HOLD")) md.hold = unsigned(std::strtoul(h, nullptr, 0));  // tests only
+  md.zq = m->quads_from_z;
+  return md;
+}
+
 cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   const S2Job &j = m->job;
   const JobCtl c = jobctl(m);
@@ -979,25 +1022,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   cand.status = nullptr;  // the per-job compaction is wait-free (s2m_vc_scan, s2m_vcompact)
   cand.tile_counter = nullptr;
 
-  S2MeshDev md;
-  md.pos = m->pos;
-  md.nrm = m->nrm;
-  md.key = m->key;
-  md.tris = m->tris;
-  md.vcap = m->vcap;
-  md.tcap = m->tcap;
-  md.vtotal = c.vtotal;
-  md.rowcnt = m->rowcnt;
-  md.rowstart = m->rowstart;
-  md.scan_status = m->scan_status;
-  md.counters = c.counters;
-  md.ntris = c.ntris;
-  md.invalid = c.invalid;
-  md.err = c.err;
-  md.wait_ns = m->wait_ns;
-  md.hold = 0;
-  if (const char *h = std::getenv("S2M_TEST_HOLD")) md.hold = unsigned(std::strtoul(h, nullptr, 0));  // tests only
-  md.pad = 0;
+  const S2MeshDev md = mesh_dev(m);
 
   const long long pts = (long long)j.P * j.P;
   const unsigned eval_blocks = unsigned((pts + S2_EVAL_BLOCK - 1) / S2_EVAL_BLOCK);
@@ -1020,10 +1045,10 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
   const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
-    int zc0 = s * m->D;
-    int zc1 = std::min(m->nzc, zc0 + m->D);
-    int k0 = s == 0 ? 0 : zc0 + 1;
-    int nk = zc1 - k0 + 1;
+    int zc0 = j.zb + s * m->D;
+    int zc1 = std::min(j.zb + m->nzc, zc0 + m->D);
+    int k0, nk;
+    slab_planes(m, s, k0, nk);
     S2Job jj = j;
     float *ring = m->ring;
     m->eval_points += double(pts) * nk;
@@ -1302,6 +1327,84 @@ template <class T> bool carve(unsigned char *base, size_t &used, size_t count, T
   *out = reinterpret_cast<T *>(base + used);
   used += bytes;
   return true;
+}
+
+// ---------------------------------------------------------------------------
+// Pinned host arrays of s2m_mesh_generate, kept for reuse: pinning hundreds of
+// MB costs tens of ms, the copy into them well under one.  Blocks are mapped
+// into the device's address space (the z parts' copy kernels store into
+// them).  At most kHostPoolKeep bytes stay pooled.
+struct HostBlock {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_host_mu;
+std::vector<HostBlock> g_host_free;
+size_t g_host_free_bytes = 0;
+constexpr size_t kHostPoolKeep = size_t(16) << 30;
+
+HostBlock take_host_block(size_t bytes) {
+  bytes = std::max<size_t>(bytes, 4096);
+  {
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    int best = -1;
+    for (size_t i = 0; i < g_host_free.size(); ++i)
+      if (g_host_free[i].bytes >= bytes && g_host_free[i].bytes <= 4 * bytes &&
+          (best < 0 || g_host_free[i].bytes < g_host_free[size_t(best)].bytes))
+        best = int(i);
+    if (best >= 0) {
+      HostBlock b = g_host_free[size_t(best)];
+      g_host_free.erase(g_host_free.begin() + best);
+      g_host_free_bytes -= b.bytes;
+      return b;
+    }
+  }
+  HostBlock b;
+  b.bytes = bytes + bytes / 4;  // room for the next job's slightly larger mesh
+  if (cudaHostAlloc(&b.p, b.bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  return b;
+}
+
+void give_host_block(HostBlock b) {
+  if (!b.p) return;
+  std::vector<void *> drop;
+  {
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    g_host_free.push_back(b);
+    g_host_free_bytes += b.bytes;
+    while (g_host_free_bytes > kHostPoolKeep && !g_host_free.empty()) {  // drop the oldest
+      drop.push_back(g_host_free.front().p);
+      g_host_free_bytes -= g_host_free.front().bytes;
+      g_host_free.erase(g_host_free.begin());
+    }
+  }
+  for (void *p : drop) cudaFreeHost(p);
+}
+
+struct HostMeshOwner {
+  HostBlock pos, nrm, tris;
+};
+
+// Device pointer of a mapped pinned block.
+template <class T> T *mapped(const HostBlock &b) {
+  void *d = nullptr;
+  return cudaHostGetDevicePointer(&d, b.p, 0) == cudaSuccess ? static_cast<T *>(d) : nullptr;
+}
+
+// The side stream the z parts' host copies run on (one per device).
+cudaStream_t copy_stream() {
+  static std::mutex mu;
+  static cudaStream_t streams[kNoallocMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev] = nullptr;
+  return streams[dev];
 }
 
 }  // namespace
@@ -1833,6 +1936,185 @@ int s2m_mesh_copy_to_host(const s2m_mesh *m, float *pos, float *nrm, uint64_t *c
   if (e == cudaSuccess && tris && m->ntris) e = cudaMemcpyAsync(tris, m->tris, m->ntris * 12, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? S2M_OK : S2M_E_CUDA;
+}
+
+// s2m_mesh_generate in one part: create, copy into pooled pinned arrays, free.
+static int generate_one(const s2m_sdf *sdf, const s2m_params *params, void *stream, s2m_host_mesh *out, char *err,
+                        size_t errlen) {
+  s2m_mesh *m = nullptr;
+  int rc = s2m_mesh_create(sdf, params, stream, &m, err, errlen);
+  if (rc != S2M_OK) return rc;
+  HostMeshOwner *o = new HostMeshOwner();
+  o->pos = take_host_block(m->nverts * 12);
+  o->nrm = take_host_block(m->nverts * 12);
+  o->tris = take_host_block(m->ntris * 12);
+  if (!o->pos.p || !o->nrm.p || !o->tris.p) {
+    give_host_block(o->pos); give_host_block(o->nrm); give_host_block(o->tris);
+    delete o;
+    s2m_mesh_free(m);
+    set_err(err, errlen, "pinned host arrays");
+    return S2M_E_OOM;
+  }
+  rc = s2m_mesh_copy_to_host(m, static_cast<float *>(o->pos.p), static_cast<float *>(o->nrm.p), nullptr,
+                             static_cast<uint32_t *>(o->tris.p), stream);
+  out->pos = static_cast<const float *>(o->pos.p);
+  out->nrm = static_cast<const float *>(o->nrm.p);
+  out->tris = static_cast<const uint32_t *>(o->tris.p);
+  out->nverts = m->nverts;
+  out->ntris = m->ntris;
+  out->invalid_quads = m->invalid;
+  out->resolution = uint32_t(m->N);
+  out->parts = 1;
+  out->owner = o;
+  s2m_mesh_free(m);
+  if (rc != S2M_OK) {
+    s2m_host_mesh_free(out);
+    set_err(err, errlen, "device to host copy failed");
+  }
+  return rc;
+}
+
+int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t parts, void *stream,
+                      s2m_host_mesh *out, char *err, size_t errlen) {
+  if (!sdf || !params || !out) return S2M_E_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  // the job's geometry: resolution after rounding, cell planes, slice lag
+  s2m_mesh probe;
+  probe.sdf = sdf;
+  probe.params = *params;
+  if (!(probe.params.eps > 0.0f)) probe.params.eps = 1e-4f;
+  int rc = setup_job(&probe, err, errlen);
+  if (rc != S2M_OK) return rc;
+  const int nzc = probe.nzc, lag = probe.job.lag;
+  unsigned K = parts ? parts : (probe.N >= 512 ? 2u : 1u);
+  K = std::min<unsigned>(K, unsigned(std::max(1, nzc / 16)));  // parts of at least 16 cell planes
+  // an SDF's first job tunes its evaluation in one piece
+  if (K <= 1 || sdf->eval_variant < 0) return generate_one(sdf, params, stream, out, err, errlen);
+  if (probe.job.qef && (rc = ensure_qef_module(sdf, err, errlen)) != S2M_OK) return rc;
+
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStream_t side = copy_stream();
+  if (!side) return generate_one(sdf, params, stream, out, err, errlen);
+  std::vector<s2m_mesh *> pm;
+  std::vector<cudaEvent_t> ev;
+  HostMeshOwner *o = new HostMeshOwner();
+  HostBlock totals;
+  auto cleanup = [&]() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    for (s2m_mesh *m : pm) {
+      free_buffers(m);
+      delete m;
+    }
+    give_host_block(o->pos); give_host_block(o->nrm); give_host_block(o->tris);
+    give_host_block(totals);
+    delete o;
+  };
+  unsigned long long vcap = 0, tcap = 0;
+  for (unsigned k = 0; k < K; ++k) {
+    const int z0 = int((unsigned long long)nzc * k / K), z1 = int((unsigned long long)nzc * (k + 1) / K);
+    s2m_mesh *m = new s2m_mesh();
+    pm.push_back(m);
+    m->sdf = sdf;
+    m->stream = st;
+    m->params = probe.params;
+    m->zpart_begin = k ? z0 - 1 : 0;  // a later part also meshes the plane below it (context)
+    m->zpart_end = z1;
+    m->quads_from_z = k ? unsigned(z0 + lag) : 0u;
+    unsigned long long cc, vc, tc;
+    if ((rc = setup_job(m, err, errlen)) == S2M_OK) {
+      initial_caps(m, m->params, cc, vc, tc);
+      rc = alloc_buffers(m, cc, vc, tc, err, errlen);
+    }
+    if (rc != S2M_OK) {
+      cleanup();
+      return rc;
+    }
+    vcap += m->vcap;
+    tcap += m->tcap;
+  }
+  o->pos = take_host_block(vcap * 12);
+  o->nrm = take_host_block(vcap * 12);
+  o->tris = take_host_block(tcap * 12);
+  totals = take_host_block(K * sizeof(S2HostTotals));
+  float *hpos = mapped<float>(o->pos), *hnrm = mapped<float>(o->nrm);
+  unsigned *htris = mapped<unsigned>(o->tris);
+  S2HostTotals *tot_d = mapped<S2HostTotals>(totals);
+  if (!hpos || !hnrm || !htris || !tot_d) {
+    cleanup();
+    set_err(err, errlen, "pinned host arrays");
+    return S2M_E_OOM;
+  }
+  cudaError_t e = cudaSuccess;
+  for (unsigned k = 0; k < K && e == cudaSuccess; ++k) {
+    s2m_mesh *m = pm[k];
+    cudaEvent_t done;
+    if ((e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming)) != cudaSuccess) break;
+    ev.push_back(done);
+    if ((e = enqueue(m, st)) != cudaSuccess) break;
+    if ((e = cudaEventRecord(done, st)) != cudaSuccess) break;
+    if ((e = cudaStreamWaitEvent(side, done, 0)) != cudaSuccess) break;
+    // the part's first non-context row: its row start counts the context plane's vertices
+    const unsigned *skip_at = k ? m->rowstart + (unsigned long long)m->quads_from_z * m->N : nullptr;
+    s2m_host_copy<<<128, 256, 0, side>>>(mesh_dev(m), skip_at, k ? tot_d + (k - 1) : nullptr, tot_d + k, hpos, hnrm,
+                                         htris, vcap, tcap);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(side);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cleanup();
+    set_err(err, errlen, std::string("z parts: ") + cudaGetErrorString(e));
+    return S2M_E_CUDA;
+  }
+  unsigned flags = 0;
+  for (s2m_mesh *m : pm) {
+    if ((rc = readback(m, st, err, errlen)) != S2M_OK) {
+      cleanup();
+      return rc;
+    }
+    flags |= m->errflags;
+    if (!(m->errflags & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF))) learn_caps(m);
+  }
+  const S2HostTotals t = static_cast<const S2HostTotals *>(totals.p)[K - 1];
+  flags |= t.err;
+  if (flags & S2_ERR_LOOKBACK) {
+    cleanup();
+    set_err(err, errlen, "a device-side look-back wait hit its limit");
+    return S2M_E_TIMEOUT;
+  }
+  if (flags & S2_ERR_INDEX_OVF) {
+    cleanup();
+    set_err(err, errlen, "more than 2^32 - 2 vertices");
+    return S2M_E_OVERFLOW;
+  }
+  if (flags & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF | S2_ERR_HOST_OVF)) {
+    // a part outgrew its buffers: the job again in one piece (which re-runs
+    // with the exact totals), the parts' totals now learned for the next job
+    cleanup();
+    return generate_one(sdf, params, stream, out, err, errlen);
+  }
+  out->pos = static_cast<const float *>(o->pos.p);
+  out->nrm = static_cast<const float *>(o->nrm.p);
+  out->tris = static_cast<const uint32_t *>(o->tris.p);
+  out->nverts = t.nverts;
+  out->ntris = t.ntris;
+  out->invalid_quads = t.invalid;
+  out->resolution = uint32_t(probe.N);
+  out->parts = K;
+  out->owner = o;
+  o = new HostMeshOwner();  // the arrays now belong to `out`
+  cleanup();
+  return S2M_OK;
+}
+
+void s2m_host_mesh_free(s2m_host_mesh *mesh) {
+  if (!mesh || !mesh->owner) return;
+  HostMeshOwner *o = static_cast<HostMeshOwner *>(mesh->owner);
+  give_host_block(o->pos);
+  give_host_block(o->nrm);
+  give_host_block(o->tris);
+  delete o;
+  std::memset(mesh, 0, sizeof(*mesh));
 }
 
 int s2m_mesh_write(const s2m_mesh *m, const char *path, char *err, size_t errlen) {

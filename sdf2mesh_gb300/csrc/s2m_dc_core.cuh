@@ -24,14 +24,15 @@ struct S2Cell {
   int x, y, z;
 };
 
-// Slab s evaluates lattice planes k0 .. k0 + nk - 1 (k0 = 0 for the first
-// slab, else s * D + 1; the last plane is min(nzc, (s + 1) * D)).  The tile
+// Slab s evaluates lattice planes k0 .. k0 + nk - 1 (k0 = zb for the first
+// slab, else zb + s * D + 1; the last plane is min(zb + nzc, zb + (s + 1) * D):
+// the job's cells are planes zb .. zb + nzc - 1).  The tile
 // pruning cuts them into tiles of S2_PT_XY x S2_PT_XY points by
 // s2_tile_depth(nk) planes.
-__device__ __forceinline__ void s2_slab_planes(int s, int D, int nzc, int &k0, int &nk) {
-  const int zc0 = s * D;
-  const int zc1 = min(nzc, zc0 + D);
-  k0 = s == 0 ? 0 : zc0 + 1;
+__device__ __forceinline__ void s2_slab_planes(const S2Job &j, int s, int D, int nzc, int &k0, int &nk) {
+  const int zc0 = j.zb + s * D;
+  const int zc1 = min(j.zb + nzc, zc0 + D);
+  k0 = s == 0 ? j.zb : zc0 + 1;
   nk = zc1 - k0 + 1;
 }
 __device__ __forceinline__ int s2_tile_depth(int nk) {
@@ -44,9 +45,9 @@ __device__ __forceinline__ int s2_tile_depth(int nk) {
 // tbase[s] is slab s's first tile.
 __device__ __forceinline__ unsigned long long s2_cell_prune_tile(const S2Job &job, S2Cell c,
                                                                  const unsigned long long *tbase, int D, int nzc) {
-  const int s = c.z / D;
+  const int s = (c.z - job.zb) / D;
   int k0, nk;
-  s2_slab_planes(s, D, nzc, k0, nk);
+  s2_slab_planes(job, s, D, nzc, k0, nk);
   const int tz = (c.z + 1 - k0) / s2_tile_depth(nk);
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const unsigned long long t = ((unsigned long long)tz * ntx + c.y / S2_PT_XY) * ntx + c.x / S2_PT_XY;

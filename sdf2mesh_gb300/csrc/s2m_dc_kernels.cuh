@@ -121,8 +121,8 @@ S2_EVAL_VARIANT(s2m_eval_b3v4, 3, 4, true)
 
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
 // Tile pruning (the generated s2m_user_sdf_tile / s2m_user_sdf_pruned).
-// Slab s evaluates planes k0 .. k0 + nk - 1 (k0 = 0 for the first slab, else
-// s * D + 1; the last plane is min(nzc, (s + 1) * D)).  Its planes are cut
+// Slab s evaluates planes k0 .. k0 + nk - 1 (s2_slab_planes: from the job's
+// first cell plane zb).  Its planes are cut
 // into tiles of 8 x 8 points by `tzs` planes (at most S2_PT_ZMAX, balanced),
 // nzt tiles in z; tile t = (tz * nty + ty) * ntx + tx.  slab_base[s] is the
 // index of slab s's first tile among all tiles of the job.  (s2_slab_planes,
@@ -218,7 +218,7 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   if (c >= cbase[s_end]) return;
   const int s = s2_find_slab(cbase, s_begin, s_end, c);
   int k0, nk;
-  s2_slab_planes(s, D, nzc, k0, nk);
+  s2_slab_planes(job, s, D, nzc, k0, nk);
   const int tzs = s2_tile_depth(nk);
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
@@ -264,7 +264,7 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
   if (live) {
     s = s2_find_slab(cbase, s_begin, s_end, c);
     int k0s, nks;
-    s2_slab_planes(s, D, nzc, k0s, nks);
+    s2_slab_planes(job, s, D, nzc, k0s, nks);
     const int tzs = s2_tile_depth(nks), nzt = (nks + tzs - 1) / tzs;
     const long long lc = (long long)(c - cbase[s]);
     const int cx = (int)(lc % ncx);
@@ -277,7 +277,7 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
   unsigned long long fp_ops = 0, sfu_ops = 0;
   if (live) {
     int k0, nk;
-    s2_slab_planes(s, D, nzc, k0, nk);
+    s2_slab_planes(job, s, D, nzc, k0, nk);
     const long long t = ((long long)tz * ntx + ty) * ntx + tx;
     const unsigned long long g = tbase[s] + (unsigned long long)t;
     const S2PruneTile tl = s2_prune_tile(job, t, k0, nk, s2_tile_depth(nk));

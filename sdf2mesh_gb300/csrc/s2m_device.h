@@ -24,6 +24,8 @@ struct S2Job {
   int qef;                 // 1: precision mode (lattice corners, QEF vertex, FP64 solve)
   unsigned magic_n;        // floor(2^32 / N) + 1: division by N of 32-bit indices
   unsigned magic_p;        // floor(2^32 / P) + 1
+  int zb;                  // first cell plane of the job's z range (0: the whole lattice)
+  int pad;
 };
 
 // Division of a 32-bit index by d (2 <= d < 2^31) with the precomputed
@@ -91,7 +93,7 @@ struct S2MeshDev {
   unsigned *err;
   unsigned long long wait_ns;     // bound of each device wait (look-back), GPU global timer ns
   unsigned hold;                  // test hook: S2_HOLD_* (0 in normal runs)
-  unsigned pad;
+  unsigned zq;                    // vertices with label z below zq make no quads (a z part's context plane)
 };
 
 // Test hooks (S2MeshDev::hold): a flag that nothing sets, so that a bounded
@@ -110,6 +112,7 @@ struct S2MeshDev {
 #define S2_ERR_VERT_OVF 0x4u      /* vertex arrays too small                    */
 #define S2_ERR_TRI_OVF 0x8u       /* triangle array too small                   */
 #define S2_ERR_INDEX_OVF 0x10u    /* more than 2^32 - 2 vertices                */
+#define S2_ERR_HOST_OVF 0x40u     /* host arrays too small for a job's z parts   */
 
 #define S2_CELL_BLOCK 256
 #define S2_CELL_CPT 16

@@ -202,10 +202,12 @@ struct S2QuadLookups {
   unsigned ax, axm1, bx, bxm1, cx, own;
 };
 
-__device__ __forceinline__ unsigned s2_quad_want(unsigned long long key) {
+// zq: vertices labelled below plane zq make no quads (0: every vertex).
+__device__ __forceinline__ unsigned s2_quad_want(unsigned long long key, unsigned zq) {
   const int x = (int)(key & 0xffffull), y = (int)((key >> 16) & 0xffffull), z = (int)((key >> 32) & 0xffffull);
   const unsigned s = (unsigned)((key >> 48) & 0xfull);
   const bool b0 = s & 1u, b1 = s & 2u, b2 = s & 4u, b3 = s & 8u;
+  if ((unsigned)z < zq) return 0u;
   return (b0 != b3 && y > 0 && z > 0 ? 1u : 0u) | (b1 != b3 && x > 0 && z > 0 ? 2u : 0u) |
          (b2 != b3 && x > 0 && y > 0 ? 4u : 0u);
 }
@@ -214,7 +216,7 @@ template <bool NC>
 __device__ __forceinline__ S2QuadLookups s2_quad_lookups(const S2MeshDev &m, int N, unsigned v,
                                                          unsigned long long key) {
   const int x = (int)(key & 0xffffull), y = (int)((key >> 16) & 0xffffull), z = (int)((key >> 32) & 0xffffull);
-  const unsigned want = s2_quad_want(key);
+  const unsigned want = s2_quad_want(key, m.zq);
   const S2RowHit none = {S2_NO_VERTEX, S2_NO_VERTEX};
   const S2RowHit ra = (want & 5u) ? s2_row_find<NC>(m, N, x, y - 1, z) : none;      // (., y - 1, z)
   const S2RowHit rb = (want & 3u) ? s2_row_find<NC>(m, N, x, y, z - 1) : none;      // (., y, z - 1)
@@ -234,13 +236,14 @@ __device__ __forceinline__ S2QuadLookups s2_quad_lookups(const S2MeshDev &m, int
 }
 
 // Quads of one vertex from its lookups (mesh.rs:280-321).
-__device__ __forceinline__ S2Quads s2_quads_from(const S2QuadLookups &l, unsigned v, unsigned long long key) {
+__device__ __forceinline__ S2Quads s2_quads_from(const S2QuadLookups &l, unsigned v, unsigned long long key,
+                                                 unsigned zq) {
   S2Quads r;
   r.valid = 0;
   r.invalid = 0;
   const unsigned s = (unsigned)((key >> 48) & 0xfull);
   const bool b0 = s & 1u, b1 = s & 2u, b2 = s & 4u;
-  const unsigned want = s2_quad_want(key);
+  const unsigned want = s2_quad_want(key, zq);
   auto put = [&](int qi, unsigned a, unsigned b, unsigned c, unsigned d, bool swap) {
     if (swap) { unsigned t = a; a = d; d = t; t = b; b = c; c = t; }
     r.q[qi][0] = a; r.q[qi][1] = b; r.q[qi][2] = c; r.q[qi][3] = d;
@@ -255,7 +258,7 @@ __device__ __forceinline__ S2Quads s2_quads_from(const S2QuadLookups &l, unsigne
 
 template <bool NC>
 __device__ __forceinline__ S2Quads s2_vertex_quads(const S2MeshDev &m, int N, unsigned v, unsigned long long key) {
-  return s2_quads_from(s2_quad_lookups<NC>(m, N, v, key), v, key);
+  return s2_quads_from(s2_quad_lookups<NC>(m, N, v, key), v, key, m.zq);
 }
 
 template <bool NC>

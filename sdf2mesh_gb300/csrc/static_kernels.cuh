@@ -78,6 +78,77 @@ __device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned
   if (tid == 0) base[slab_index + 1] = s_carry;
 }
 
+// Host copy of one z part of a job (s2m_mesh_generate) into pinned host
+// arrays mapped into the device's address space.  The part's vertices from
+// index *skip_at on (its context plane, which the part below it has copied
+// already, comes first in (z, y, x) order; skip_at null: none) go to host
+// vertex prev.nverts + (v - skip); its triangles to host triangle
+// prev.ntris + t, every index + prev.nverts - skip.  Block 0 writes the
+// running totals after this part to *next.  A part that overflowed any of its
+// buffers (or the host arrays) copies nothing and leaves its flags in
+// next->err: the host then meshes the job again in one part.
+struct S2HostTotals {
+  unsigned long long nverts, ntris, invalid;
+  unsigned err, pad;
+};
+__global__ void __launch_bounds__(256) s2m_host_copy(S2MeshDev mesh, const unsigned *skip_at,
+                                                     const S2HostTotals *prev, S2HostTotals *next, float *hpos,
+                                                     float *hnrm, unsigned *htris, unsigned long long hvcap,
+                                                     unsigned long long htcap) {
+  const unsigned long long V = *mesh.vtotal, T = *mesh.ntris;
+  const unsigned long long skip = skip_at ? (unsigned long long)*skip_at : 0ull;
+  const unsigned long long vb = prev ? prev->nverts : 0ull, tb = prev ? prev->ntris : 0ull;
+  unsigned err = (prev ? prev->err : 0u) | *mesh.err;
+  if (V > mesh.vcap || T > mesh.tcap || skip > V) err |= S2_ERR_VERT_OVF;
+  else if (vb + (V - skip) > hvcap || tb + T > htcap) err |= S2_ERR_HOST_OVF;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    next->nverts = err ? 0ull : vb + (V - skip);
+    next->ntris = err ? 0ull : tb + T;
+    next->invalid = (prev ? prev->invalid : 0ull) + *mesh.invalid;
+    next->err = err;
+  }
+  if (err) return;
+  // 4 elements per thread and step, loads first: the stores cross the link
+  // to host memory, the loads come from HBM, and both want many in flight
+  const unsigned long long stride = (unsigned long long)gridDim.x * 256u;
+  const unsigned long long nf = 3ull * (V - skip), nt = 3ull * T;
+  const float *sp = mesh.pos + 3ull * skip, *sn = mesh.nrm + 3ull * skip;
+  float *dp = hpos + 3ull * vb, *dn = hnrm + 3ull * vb;
+  const unsigned long long i0 = (unsigned long long)blockIdx.x * 256u + threadIdx.x;
+  for (unsigned long long i = i0; i < nf; i += 4 * stride) {
+    float a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned long long k = i + u * stride;
+      a[u] = k < nf ? __ldg(sp + k) : 0.0f;
+      b[u] = k < nf ? __ldg(sn + k) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned long long k = i + u * stride;
+      if (k < nf) {
+        dp[k] = a[u];
+        dn[k] = b[u];
+      }
+    }
+  }
+  const unsigned shift = (unsigned)(vb - skip);  // indices stay below 2^32 - 1 (S2_ERR_INDEX_OVF otherwise)
+  unsigned *dt = htris + 3ull * tb;
+  for (unsigned long long i = i0; i < nt; i += 4 * stride) {
+    unsigned a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned long long k = i + u * stride;
+      a[u] = k < nt ? __ldg(mesh.tris + k) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned long long k = i + u * stride;
+      if (k < nt) dt[k] = a[u] + shift;
+    }
+  }
+}
+
 // Off-lattice bit of every cell column x: bit x % 32 of word x / 32 is
 // s2_off_lattice(x + 1).
 __global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict__ offx) {
@@ -586,7 +657,7 @@ __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_find(S2Job job, S2MeshDe
       if (v >= V) continue;
       const unsigned long long key = __ldg(mesh.key + v);
       const S2QuadLookups l = s2_quad_lookups<true>(mesh, job.N, (unsigned)v, key);
-      const S2Quads q = s2_quads_from(l, (unsigned)v, key);
+      const S2Quads q = s2_quads_from(l, (unsigned)v, key, mesh.zq);
       cnt += 2u * __popc(q.valid);
       invalid += q.invalid;
       lk0[3 * v] = l.ax;
@@ -645,7 +716,7 @@ __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_write(S2MeshDev mesh, co
         l.bxm1 = __ldg(lk1 + 3 * v);
         l.cx = __ldg(lk1 + 3 * v + 1);
         l.own = __ldg(lk1 + 3 * v + 2);
-        qd[m] = s2_quads_from(l, (unsigned)v, __ldg(mesh.key + v));
+        qd[m] = s2_quads_from(l, (unsigned)v, __ldg(mesh.key + v), mesh.zq);
       }
       ntri[m] = 2u * __popc(qd[m].valid);
       unsigned inc = ntri[m];
