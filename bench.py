@@ -393,9 +393,27 @@ def time_job(s2m, L, sdf, state, stream, flush, steps, warmup, barrier, clocks=N
         if i >= max(1, min(warmup, 3)):
             gen_ms.append((time.perf_counter() - t) * 1e3)
     barrier()
+    # the same call with the number of z parts fixed, for the record
+    by_parts = {}
+    for k in (1, 2, 3, 4):
+        ts = []
+        for i in range(3):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            rc = L.s2m_mesh_generate(sdf.handle, ctypes.byref(p), k, ctypes.c_void_p(sp), ctypes.byref(hm), err,
+                                     len(err))
+            if rc != 0:
+                raise RuntimeError(err.value.decode())
+            kk = int(hm.parts)
+            L.s2m_host_mesh_free(ctypes.byref(hm))
+            ts.append((time.perf_counter() - t) * 1e3)
+        by_parts[str(kk)] = round(min(ts[1:]), 4)
     out["e2e_ms"] = sum(gen_ms)
     out["e2e_steps"] = len(gen_ms)
     out["e2e_parts"] = gen_parts
+    out["e2e_ms_by_parts"] = by_parts
     out["e2e_parts_ms"] = {k: v / len(e2e_ms) for k, v in parts.items()}
     out["d2h"] = nverts * (12 + 12) + ntris * 12
     return out
@@ -605,6 +623,7 @@ def ours(a):
                                   if eval_ops["pruned"] else "every SDF operation at every lattice point")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": r["d2h"],
                 "ms_per_step": e2e_tot / r["e2e_steps"], "z_parts": r["e2e_parts"],
+                "ms_by_z_parts": r["e2e_ms_by_parts"],
                 "path": "s2m_mesh_generate + s2m_host_mesh_free: the reference's TriangleMesh (positions, normals, "
                         "triangle indices) in pinned host memory, the job in z parts whose device-to-host copies "
                         "overlap the next part's kernels; inputs are the compiled SDF module and a 48-byte "
