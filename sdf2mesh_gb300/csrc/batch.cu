@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
   __shared__ int s_ok;
   const unsigned tid = threadIdx.x;
   unsigned long long busy[S2_NSTAGES], waited = 0ull, t_item = 0ull;  // thread 0's accounting
+  unsigned ready_job = ~0u, ready_stage = ~0u;  // thread 0: the last (job, stage) whose previous stage was seen done
 #pragma unroll
   for (int k = 0; k < S2_NSTAGES; ++k) busy[k] = 0ull;
   for (;;) {
@@ -334,7 +335,9 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
     if (tid == 0) {
       int ok = 1;
       const unsigned long long tw = s2_globaltimer();
-      if (sg.stage > 0) {
+      // (the stage's items come in runs of tickets: once the previous stage
+      // was seen done, with acquire, later items of the run need not look again)
+      if (sg.stage > 0 && !(sg.job == ready_job && sg.stage == ready_stage)) {
         // wait for every item of the previous stage of this job (lower tickets),
         // bounded by time: stage_wait_ns of the GPU's global timer
         const unsigned need = J.nitems[sg.stage - 1];
@@ -351,6 +354,10 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
             break;
           }
           __nanosleep(128);
+        }
+        if (ok) {
+          ready_job = sg.job;
+          ready_stage = sg.stage;
         }
       }
       t_item = s2_globaltimer();

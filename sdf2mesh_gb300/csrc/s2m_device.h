@@ -115,7 +115,7 @@ struct S2MeshDev {
 #define S2_ERR_HOST_OVF 0x40u     /* host arrays too small for a job's z parts   */
 
 #define S2_CELL_BLOCK 256
-#define S2_CELL_CPT 16
+#define S2_CELL_CPT 32
 #define S2_CELL_TILE (S2_CELL_BLOCK * S2_CELL_CPT)
 #define S2_CW_BLOCK 256          /* words of 32 cells per classification tile */
 #define S2_EVAL_BLOCK 256
