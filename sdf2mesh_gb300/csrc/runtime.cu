@@ -2022,7 +2022,12 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
     m->quads_from_z = k ? unsigned(z0 + lag) : 0u;
     unsigned long long cc, vc, tc;
     if ((rc = setup_job(m, err, errlen)) == S2M_OK) {
+      // the whole job's capacities: a part's share of the surface can be far
+      // from its share of the planes (an overflow would mesh the job twice)
+      const double zf = m->zfrac;
+      m->zfrac = 1.0;
       initial_caps(m, m->params, cc, vc, tc);
+      m->zfrac = zf;
       rc = alloc_buffers(m, cc, vc, tc, err, errlen);
     }
     if (rc != S2M_OK) {
@@ -2036,14 +2041,15 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   o->nrm = take_host_block(vcap * 12);
   o->tris = take_host_block(tcap * 12);
   totals = take_host_block(K * sizeof(S2HostTotals));
-  float *hpos = mapped<float>(o->pos), *hnrm = mapped<float>(o->nrm);
-  unsigned *htris = mapped<unsigned>(o->tris);
   S2HostTotals *tot_d = mapped<S2HostTotals>(totals);
-  if (!hpos || !hnrm || !htris || !tot_d) {
+  if (!o->pos.p || !o->nrm.p || !o->tris.p || !tot_d) {
     cleanup();
     set_err(err, errlen, "pinned host arrays");
     return S2M_E_OOM;
   }
+  // All parts' kernels first (each ending with its copy plan), then, as each
+  // part finishes, its copies on the side stream's copy engine: they run
+  // while the later parts' kernels do.
   cudaError_t e = cudaSuccess;
   for (unsigned k = 0; k < K && e == cudaSuccess; ++k) {
     s2m_mesh *m = pm[k];
@@ -2051,13 +2057,31 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
     if ((e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming)) != cudaSuccess) break;
     ev.push_back(done);
     if ((e = enqueue(m, st)) != cudaSuccess) break;
-    if ((e = cudaEventRecord(done, st)) != cudaSuccess) break;
-    if ((e = cudaStreamWaitEvent(side, done, 0)) != cudaSuccess) break;
     // the part's first non-context row: its row start counts the context plane's vertices
     const unsigned *skip_at = k ? m->rowstart + (unsigned long long)m->quads_from_z * m->N : nullptr;
-    s2m_host_copy<<<128, 256, 0, side>>>(mesh_dev(m), skip_at, k ? tot_d + (k - 1) : nullptr, tot_d + k, hpos, hnrm,
-                                         htris, vcap, tcap);
-    e = cudaGetLastError();
+    s2m_part_finish<<<unsigned(device_sm_count()) * 4, 256, 0, st>>>(mesh_dev(m), skip_at,
+                                                                      k ? tot_d + (k - 1) : nullptr, tot_d + k,
+                                                                      vcap, tcap);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    e = cudaEventRecord(done, st);
+  }
+  const S2HostTotals *tot_h = static_cast<const S2HostTotals *>(totals.p);
+  for (unsigned k = 0; k < K && e == cudaSuccess; ++k) {
+    if ((e = cudaEventSynchronize(ev[k])) != cudaSuccess) break;
+    const S2HostTotals t = tot_h[k];
+    if (t.err) break;  // the one-piece fallback below
+    const s2m_mesh *m = pm[k];
+    char *hp = static_cast<char *>(o->pos.p), *hn = static_cast<char *>(o->nrm.p), *ht = static_cast<char *>(o->tris.p);
+    if (t.vcount) {
+      if ((e = cudaMemcpyAsync(hp + 12 * t.vbase, m->pos + 3 * t.vfirst, 12 * t.vcount, cudaMemcpyDeviceToHost,
+                               side)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(hn + 12 * t.vbase, m->nrm + 3 * t.vfirst, 12 * t.vcount, cudaMemcpyDeviceToHost,
+                               side)) != cudaSuccess)
+        break;
+    }
+    if (t.tcount &&
+        (e = cudaMemcpyAsync(ht + 12 * t.tbase, m->tris, 12 * t.tcount, cudaMemcpyDeviceToHost, side)) != cudaSuccess)
+      break;
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(side);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -78,75 +78,48 @@ __device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned
   if (tid == 0) base[slab_index + 1] = s_carry;
 }
 
-// Host copy of one z part of a job (s2m_mesh_generate) into pinned host
-// arrays mapped into the device's address space.  The part's vertices from
-// index *skip_at on (its context plane, which the part below it has copied
-// already, comes first in (z, y, x) order; skip_at null: none) go to host
-// vertex prev.nverts + (v - skip); its triangles to host triangle
-// prev.ntris + t, every index + prev.nverts - skip.  Block 0 writes the
-// running totals after this part to *next.  A part that overflowed any of its
-// buffers (or the host arrays) copies nothing and leaves its flags in
-// next->err: the host then meshes the job again in one part.
+// The end of one z part of a job (s2m_mesh_generate): its vertices from index
+// skip = *skip_at on (its context plane, which the part below it has already
+// delivered, comes first in (z, y, x) order; skip_at null: none) become host
+// vertices vbase .. vbase + vcount - 1, and its triangles host triangles
+// tbase .., every index shifted in place here by vbase - skip.  Block 0
+// writes the part's copy plan and the running totals to *cur (pinned host
+// memory mapped into the device's address space); the host then copies with
+// the copy engines while the next part's kernels run.  A part that
+// overflowed its buffers or the host arrays shifts nothing and leaves its
+// flags in cur->err: the host meshes the job again in one piece.
 struct S2HostTotals {
-  unsigned long long nverts, ntris, invalid;
+  unsigned long long nverts, ntris, invalid;       // running totals after this part
+  unsigned long long vfirst, vcount, vbase;        // copy: device vertices vfirst .. -> host vbase ..
+  unsigned long long tcount, tbase;                // copy: device triangles 0 .. tcount -> host tbase ..
   unsigned err, pad;
 };
-__global__ void __launch_bounds__(256) s2m_host_copy(S2MeshDev mesh, const unsigned *skip_at,
-                                                     const S2HostTotals *prev, S2HostTotals *next, float *hpos,
-                                                     float *hnrm, unsigned *htris, unsigned long long hvcap,
-                                                     unsigned long long htcap) {
+__global__ void __launch_bounds__(256) s2m_part_finish(S2MeshDev mesh, const unsigned *skip_at,
+                                                       const S2HostTotals *prev, S2HostTotals *cur,
+                                                       unsigned long long hvcap, unsigned long long htcap) {
   const unsigned long long V = *mesh.vtotal, T = *mesh.ntris;
   const unsigned long long skip = skip_at ? (unsigned long long)*skip_at : 0ull;
   const unsigned long long vb = prev ? prev->nverts : 0ull, tb = prev ? prev->ntris : 0ull;
   unsigned err = (prev ? prev->err : 0u) | *mesh.err;
-  if (V > mesh.vcap || T > mesh.tcap || skip > V) err |= S2_ERR_VERT_OVF;
+  if (V > mesh.vcap || T > mesh.tcap || skip > V || skip > vb) err |= S2_ERR_VERT_OVF;
   else if (vb + (V - skip) > hvcap || tb + T > htcap) err |= S2_ERR_HOST_OVF;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    next->nverts = err ? 0ull : vb + (V - skip);
-    next->ntris = err ? 0ull : tb + T;
-    next->invalid = (prev ? prev->invalid : 0ull) + *mesh.invalid;
-    next->err = err;
+    cur->nverts = err ? 0ull : vb + (V - skip);
+    cur->ntris = err ? 0ull : tb + T;
+    cur->invalid = (prev ? prev->invalid : 0ull) + *mesh.invalid;
+    cur->vfirst = skip;
+    cur->vcount = err ? 0ull : V - skip;
+    cur->vbase = vb;
+    cur->tcount = err ? 0ull : T;
+    cur->tbase = tb;
+    cur->err = err;
+    cur->pad = 0u;
   }
-  if (err) return;
-  // 4 elements per thread and step, loads first: the stores cross the link
-  // to host memory, the loads come from HBM, and both want many in flight
-  const unsigned long long stride = (unsigned long long)gridDim.x * 256u;
-  const unsigned long long nf = 3ull * (V - skip), nt = 3ull * T;
-  const float *sp = mesh.pos + 3ull * skip, *sn = mesh.nrm + 3ull * skip;
-  float *dp = hpos + 3ull * vb, *dn = hnrm + 3ull * vb;
-  const unsigned long long i0 = (unsigned long long)blockIdx.x * 256u + threadIdx.x;
-  for (unsigned long long i = i0; i < nf; i += 4 * stride) {
-    float a[4], b[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const unsigned long long k = i + u * stride;
-      a[u] = k < nf ? __ldg(sp + k) : 0.0f;
-      b[u] = k < nf ? __ldg(sn + k) : 0.0f;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const unsigned long long k = i + u * stride;
-      if (k < nf) {
-        dp[k] = a[u];
-        dn[k] = b[u];
-      }
-    }
-  }
+  if (err || vb == skip) return;
   const unsigned shift = (unsigned)(vb - skip);  // indices stay below 2^32 - 1 (S2_ERR_INDEX_OVF otherwise)
-  unsigned *dt = htris + 3ull * tb;
-  for (unsigned long long i = i0; i < nt; i += 4 * stride) {
-    unsigned a[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const unsigned long long k = i + u * stride;
-      a[u] = k < nt ? __ldg(mesh.tris + k) : 0u;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const unsigned long long k = i + u * stride;
-      if (k < nt) dt[k] = a[u] + shift;
-    }
-  }
+  for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < 3ull * T;
+       i += (unsigned long long)gridDim.x * 256u)
+    mesh.tris[i] += shift;
 }
 
 // Off-lattice bit of every cell column x: bit x % 32 of word x / 32 is
