@@ -44,9 +44,8 @@ static_assert(S2_NSTAGES == S2M_BATCH_STAGES, "stage count of the C ABI");
 #define S2_B_TILE 8          // lattice points per edge of a tile
 #define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
 #define S2_B_EVAL_TILES 64   // tiles per item of the evaluation (one warp per tile)
-#define S2_B_CELL_TILES 1    // classification tiles per item (a later tile of an item would publish its
-                             // aggregate only after the item's earlier tiles, and the next item's
-                             // look-back waits for it: items ran one after another)
+#define S2_B_CELL_TILES 4    // classification tiles per item (s2_cell_tiles publishes every tile's
+                             // aggregate before any look-back)
 #define S2_B_VERT_CHUNK 256
 #define S2_ERR_BATCH_WAIT 0x20u
 
@@ -232,14 +231,9 @@ __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned ite
 __device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned item) {
   const long long ncells = (long long)J.nzc * J.job.N * J.job.N;
   const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-#pragma unroll 1
-  for (unsigned k = 0; k < S2_B_CELL_TILES; ++k) {
-    const unsigned tile = item * S2_B_CELL_TILES + k;
-    if (tile >= ntiles) break;
-    s2_cell_tile<true>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, tile, ntiles, ncells, 0, 0ull,
-                       J.cand.base + 1, J.mesh.wait_ns,
-                       S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx});
-  }
+  s2_cell_tiles<true, S2_B_CELL_TILES>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, item * S2_B_CELL_TILES,
+                                       ntiles, ncells, 0, 0ull, J.cand.base + 1, J.mesh.wait_ns,
+                                       S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx});
 }
 
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {

@@ -157,6 +157,9 @@ struct s2m_sdf {
   // so far: the next job's initial capacities (an SDF whose surface outgrows
   // the default estimate then overflows and re-runs only once)
   mutable double seen_cand = 0, seen_vert = 0, seen_tri = 0;
+  // host copy time over meshing time of the SDF's last one-piece
+  // s2m_mesh_generate: sets the sizes of its z parts
+  mutable double copy_ratio = 0.5;
   mutable int tune_regs[kNumEvalVariants] = {};
   mutable int tune_local[kNumEvalVariants] = {};  // local (spill/stack) bytes per thread
 };
@@ -1942,8 +1945,10 @@ int s2m_mesh_copy_to_host(const s2m_mesh *m, float *pos, float *nrm, uint64_t *c
 static int generate_one(const s2m_sdf *sdf, const s2m_params *params, void *stream, s2m_host_mesh *out, char *err,
                         size_t errlen) {
   s2m_mesh *m = nullptr;
+  const auto t0 = std::chrono::steady_clock::now();
   int rc = s2m_mesh_create(sdf, params, stream, &m, err, errlen);
   if (rc != S2M_OK) return rc;
+  const auto t1 = std::chrono::steady_clock::now();
   HostMeshOwner *o = new HostMeshOwner();
   o->pos = take_host_block(m->nverts * 12);
   o->nrm = take_host_block(m->nverts * 12);
@@ -1957,6 +1962,14 @@ static int generate_one(const s2m_sdf *sdf, const s2m_params *params, void *stre
   }
   rc = s2m_mesh_copy_to_host(m, static_cast<float *>(o->pos.p), static_cast<float *>(o->nrm.p), nullptr,
                              static_cast<uint32_t *>(o->tris.p), stream);
+  if (rc == S2M_OK && m->runs == 1) {  // (an overflow re-run would inflate the meshing time)
+    const double mesh_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    const double copy_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+    if (mesh_ms > 0.0) {
+      std::lock_guard<std::mutex> lock(sdf->tune_mu);
+      sdf->copy_ratio = std::min(2.0, std::max(0.02, copy_ms / mesh_ms));
+    }
+  }
   out->pos = static_cast<const float *>(o->pos.p);
   out->nrm = static_cast<const float *>(o->nrm.p);
   out->tris = static_cast<const uint32_t *>(o->tris.p);
@@ -2009,9 +2022,34 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
     give_host_block(totals);
     delete o;
   };
+  // Part sizes: part k + 1's kernels should take as long as part k's copy, so
+  // the sizes fall geometrically by r = copy time / meshing time (learned
+  // from the SDF's one-piece runs): the last part, whose copy nothing hides,
+  // is the smallest.  Parts keep at least 16 cell planes.
+  std::vector<int> zcut(K + 1, 0);
+  {
+    double r;
+    {
+      std::lock_guard<std::mutex> lock(sdf->tune_mu);
+      r = sdf->copy_ratio;
+    }
+    r = std::min(1.0, std::max(0.05, r));
+    std::vector<double> w(K);
+    double sum = 0;
+    for (unsigned k = 0; k < K; ++k) sum += (w[k] = std::pow(r, double(k)));
+    double acc = 0;
+    for (unsigned k = 0; k < K; ++k) {
+      acc += w[k];
+      zcut[k + 1] = k + 1 == K ? nzc : int(std::lround(double(nzc) * acc / sum));
+    }
+    for (unsigned k = K - 1; k >= 1; --k) zcut[k] = std::min(zcut[k], zcut[k + 1] - 16);  // 16 planes each
+    zcut[0] = 0;
+    for (unsigned k = 1; k < K; ++k) zcut[k] = std::max(zcut[k], zcut[k - 1] + 16);
+    zcut[K] = nzc;
+  }
   unsigned long long vcap = 0, tcap = 0;
   for (unsigned k = 0; k < K; ++k) {
-    const int z0 = int((unsigned long long)nzc * k / K), z1 = int((unsigned long long)nzc * (k + 1) / K);
+    const int z0 = zcut[k], z1 = zcut[k + 1];
     s2m_mesh *m = new s2m_mesh();
     pm.push_back(m);
     m->sdf = sdf;

@@ -44,17 +44,12 @@ __device__ __forceinline__ unsigned long long s2_ldcg(const unsigned long long *
 __device__ __forceinline__ unsigned s2_ldcg(const unsigned *p) { return __ldcg(p); }
 __device__ __forceinline__ float s2_ldcg(const float *p) { return __ldcg(p); }
 
-// Called by all 32 lanes of one warp; returns the exclusive prefix of
-// `aggregate` over tiles 0 .. tile-1 (the same value in every lane).
-__device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *status, unsigned tile,
-                                                          unsigned long long aggregate, unsigned *err,
-                                                          unsigned long long wait_ns) {
+// The walk back alone (tile > 0, its aggregate already published): all 32
+// lanes of one warp; the exclusive prefix over tiles 0 .. tile-1, the same in
+// every lane.  Publishes nothing.
+__device__ __forceinline__ unsigned long long s2_lookback_walk(const unsigned long long *status, unsigned tile,
+                                                               unsigned *err, unsigned long long wait_ns) {
   const unsigned lane = threadIdx.x & 31u;
-  if (tile == 0) {
-    if (lane == 0) s2_st_release(status, (S2_LB_PRE << 62) | aggregate);
-    return 0ull;
-  }
-  if (lane == 0) s2_st_release(status + tile, (S2_LB_AGG << 62) | aggregate);
   unsigned long long excl = 0;
   long long base = (long long)tile - 1;
   unsigned long long t0 = 0;
@@ -67,7 +62,6 @@ __device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *st
     unsigned first = pmask ? (unsigned)(__ffs(pmask) - 1) : 32u;
     unsigned need = first >= 31u ? S2_FULL : ((2u << first) - 1u);
     if (zmask & need) {
-      // the same timer value in every lane (broadcast), so the warp leaves together
       const unsigned long long now = __shfl_sync(S2_FULL, s2_globaltimer(), 0);
       if (t0 == 0) t0 = now;
       else if (now - t0 > wait_ns) {
@@ -83,6 +77,21 @@ __device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *st
     if (first < 32u) break;
     base -= 32;
   }
+  return excl;
+}
+
+// Called by all 32 lanes of one warp; returns the exclusive prefix of
+// `aggregate` over tiles 0 .. tile-1 (the same value in every lane).
+__device__ __forceinline__ unsigned long long s2_lookback(unsigned long long *status, unsigned tile,
+                                                          unsigned long long aggregate, unsigned *err,
+                                                          unsigned long long wait_ns) {
+  const unsigned lane = threadIdx.x & 31u;
+  if (tile == 0) {
+    if (lane == 0) s2_st_release(status, (S2_LB_PRE << 62) | aggregate);
+    return 0ull;
+  }
+  if (lane == 0) s2_st_release(status + tile, (S2_LB_AGG << 62) | aggregate);
+  const unsigned long long excl = s2_lookback_walk(status, tile, err, wait_ns);
   if (lane == 0) s2_st_release(status + tile, (S2_LB_PRE << 62) | (excl + aggregate));
   return excl;
 }
