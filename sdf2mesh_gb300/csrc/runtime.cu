@@ -172,9 +172,11 @@ struct s2m_mesh {
   int N = 0, D = 0, nzc = 0, nslabs = 0;
   // workspace
   float *ring = nullptr;
-  unsigned long long *slab_ctrl = nullptr;  // look-back word of every classification tile of the job, then the slabs' tickets
+  unsigned long long *slab_ctrl = nullptr;  // per cell plane of a slab: its first candidate slot
   unsigned *pt_bits = nullptr;               // sign, near-zero, then unknown-value bits of the ring's lattice points
   unsigned *offx = nullptr;                  // off-lattice bits of the cell columns
+  unsigned *cell_words = nullptr;            // candidate bits, 32 cells per word
+  unsigned *tile_cnt = nullptr;              // per cell tile: candidates
   // tile pruning: [ops FP32, ops SFU] (2 u64), the length of each slab's list
   // of undecided tiles (u32), the first tile and the first coarse box of
   // every slab (2 x nslabs + 1 u64), then for `prune_chunk` slabs the
@@ -187,7 +189,7 @@ struct s2m_mesh {
   size_t prune_sbits_off = 0;  // ... to the coarse boxes' activity words
   size_t prune_bits_off = 0;   // ... to the tiles' activity words
   size_t prune_list_off = 0;   // ... to the lists of undecided tiles
-  size_t vc_tiles = 0, slab_ctrl_words = 0;
+  size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
   float *cand_val = nullptr, *cand_pos = nullptr, *cand_nrm = nullptr;
@@ -507,14 +509,14 @@ void give_pinned_slot(unsigned long long *p) {
 }
 
 void free_buffers(s2m_mesh *m) {
-  void *ptrs[] = {m->ring, m->slab_ctrl, m->pt_bits, m->offx, m->prune_buf, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
+  void *ptrs[] = {m->ring, m->slab_ctrl, m->pt_bits, m->offx, m->cell_words, m->tile_cnt, m->prune_buf, m->cand_key, m->cand_val, m->cand_pos, m->cand_nrm, m->cand_base,
                   m->cand_status, m->pos, m->nrm, m->key, m->tris, m->rowcnt, m->rowstart, m->scan_status,
                   m->jobctl, m->vt_buf};
   for (void *p : ptrs)
     if (p) cudaFreeAsync(p, m->stream);
   if (m->h_read) give_pinned_slot(m->h_read);
-  m->ring = nullptr; m->slab_ctrl = nullptr; m->pt_bits = nullptr; m->offx = nullptr;
-  m->prune_buf = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
+  m->ring = nullptr; m->slab_ctrl = nullptr; m->pt_bits = nullptr; m->offx = nullptr; m->cell_words = nullptr;
+  m->tile_cnt = nullptr; m->prune_buf = nullptr; m->cand_key = nullptr; m->cand_val = nullptr; m->cand_pos = nullptr;
   m->cand_nrm = nullptr; m->cand_base = nullptr; m->cand_status = nullptr; m->pos = nullptr; m->nrm = nullptr;
   m->key = nullptr; m->tris = nullptr; m->rowcnt = nullptr; m->rowstart = nullptr; m->scan_status = nullptr;
   m->jobctl = nullptr; m->h_read = nullptr; m->vt_buf = nullptr;
@@ -768,8 +770,7 @@ unsigned cell_tiles_per_plane(const s2m_mesh *m) {
   const size_t WN = size_t((m->N + 31) / 32);
   return unsigned((size_t(m->N) * WN + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
 }
-// Classification tiles of the whole job (every slab's, in (z, y, x) order).
-size_t job_cell_tiles(const s2m_mesh *m) { return size_t(std::max(m->nzc, 0)) * cell_tiles_per_plane(m); }
+size_t cell_word_tiles(const s2m_mesh *m) { return size_t(m->D) * cell_tiles_per_plane(m); }
 
 void drop_graph(s2m_mesh *m) {
   if (m->graph) cudaGraphExecDestroy(m->graph);
@@ -781,10 +782,10 @@ void drop_graph(s2m_mesh *m) {
 // exactly this plan, and the server's admission sums it (mesh_job_footprint),
 // so the two cannot drift apart.
 struct BufPlan {
-  size_t ring, slab_ctrl, pt_bits, offx, prune, cand_key, cand_val, cand_pos, cand_nrm,
+  size_t ring, slab_ctrl, pt_bits, offx, cell_words, tile_cnt, prune, cand_key, cand_val, cand_pos, cand_nrm,
       cand_base, cand_status, vt, pos, nrm, key, tris, rowcnt, rowstart, scan_status, jobctl;
   size_t total() const {
-    return ring + slab_ctrl + pt_bits + offx + prune + cand_key + cand_val + cand_pos +
+    return ring + slab_ctrl + pt_bits + offx + cell_words + tile_cnt + prune + cand_key + cand_val + cand_pos +
            cand_nrm + cand_base + cand_status + vt + pos + nrm + key + tris + rowcnt + rowstart + scan_status +
            jobctl;
   }
@@ -796,8 +797,9 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   m->cand_cap = std::max<unsigned long long>(1024, std::min(cand_cap, N * N * N));
   m->vcap = std::max<unsigned long long>(1024, std::min(vcap, N * N * N));
   m->tcap = std::max<unsigned long long>(2048, tcap);
+  m->cell_tiles = cell_word_tiles(m);
   m->vc_tiles = (m->cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
-  m->slab_ctrl_words = job_cell_tiles(m) + (size_t(m->nslabs) + 1) / 2 + 1;
+  m->slab_ctrl_words = size_t(m->D) + 1;
   m->scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   m->quad_tiles = (m->vcap + S2_Q_TILE - 1) / S2_Q_TILE;
   BufPlan b{};
@@ -805,6 +807,8 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   b.slab_ctrl = m->slab_ctrl_words * 8;
   b.pt_bits = 3 * pt_bits_words(m) * 4;
   b.offx = size_t((j.N + 31) / 32) * 4;
+  b.cell_words = m->cell_tiles * S2_CW_BLOCK * 4;
+  b.tile_cnt = (m->cell_tiles + 1 + size_t(m->D)) * 4;  // + the finished-block counter, the plane counts
   const bool prune = m->sdf->k_tiles && m->nslabs > 0;
   b.prune = prune ? prune_layout(m) : 0;
   b.cand_key = m->cand_cap * 8;
@@ -898,6 +902,8 @@ int alloc_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long long v
   // the words' bits past the lattice edge are never written and must read 0
   S2_CUDA(cudaMemsetAsync(m->pt_bits, 0, b.pt_bits, st));
   S2_CUDA(mesh_malloc((void **)&m->offx, b.offx, st));
+  S2_CUDA(mesh_malloc((void **)&m->cell_words, b.cell_words, st));
+  S2_CUDA(mesh_malloc((void **)&m->tile_cnt, b.tile_cnt, st));
   if (b.prune) {
     S2_CUDA(mesh_malloc((void **)&m->prune_buf, b.prune, st));
     // pageable source: the call returns once the words are staged
@@ -1036,8 +1042,9 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }
-  // the classification's look-back words and per-slab tile tickets
-  if ((e = cudaMemsetAsync(m->slab_ctrl, 0, m->slab_ctrl_words * 8, st)) != cudaSuccess) return e;
+  // finished-block counter and plane counts of the classification (each slab's
+  // last mark block leaves them zero for the next)
+  if ((e = cudaMemsetAsync(m->tile_cnt + m->cell_tiles, 0, (1 + size_t(m->D)) * 4, st)) != cudaSuccess) return e;
   S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
   const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
@@ -1064,12 +1071,16 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                        cudaGetLastError()));
     const unsigned nbp = cell_tiles_per_plane(m);
     const unsigned ncp = unsigned(zc1 - zc0);
-    unsigned *tickets = reinterpret_cast<unsigned *>(m->slab_ctrl + job_cell_tiles(m));
-    const unsigned long long g0 = (unsigned long long)(zc0 - j.zb) * nbp;
-    S2_LAUNCH(1, ncells, (s2m_cells_fused<<<ncp * nbp, S2_CW_BLOCK, 0, st>>>(
-                              j, pb, m->offx, m->ring, pruned ? pb.unk : nullptr, cand, m->slab_ctrl, tickets + s,
-                              m->cand_base, s, zc0, zc1, g0, c.err, m->wait_ns),
+    const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
+    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<mg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
+                                                                    m->tile_cnt + m->cell_tiles,
+                                                                    m->tile_cnt + m->cell_tiles + 1, m->slab_ctrl,
+                                                                    m->cand_base, s, zc0, zc1),
                           cudaGetLastError()));
+    S2_LAUNCH(1, 0, (s2m_cells_emit<<<eg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
+                                                               m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err,
+                                                               zc0),
+                     cudaGetLastError()));
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
@@ -1812,12 +1823,14 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
 
   const S2Job &j = m.job;
   const unsigned long long N = (unsigned long long)m.N;
-  m.slab_ctrl_words = job_cell_tiles(&m) + (size_t(m.nslabs) + 1) / 2 + 1;
+  m.cell_tiles = cell_word_tiles(&m);
+  m.slab_ctrl_words = size_t(m.D) + 1;
   m.scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   size_t used = 0;
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
             carve(base, used, 3 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
+            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles + 1 + size_t(m.D), &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
             carve(base, used, size_t(8), &m.jobctl);

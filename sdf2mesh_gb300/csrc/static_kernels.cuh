@@ -327,165 +327,6 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
   if (threadIdx.x == 0) *done = 0u;
 }
 
-// Classification in one pass (s2m_cells_fused): mark and emit per tile, the
-// tiles of the whole job (cell planes zb .., S2_CW_BLOCK words of one plane
-// each, in (z, y, x) order) chained by a decoupled look-back.  A block takes
-// the next tile of its slab from *ticket (tickets in tile order, so a tile
-// only ever waits for tiles already taken), forms its words of 32 cells from
-// the point bits of the 2 point planes around them (the rule of
-// s2m_cells_mark), publishes its count, and writes its candidates at the
-// look-back prefix (as s2m_cells_emit does).  The words never go to memory,
-// and one kernel mixes the ALU-bound word formation with the latency-bound
-// candidate writes.  status: one word per tile of the job, zero at job start;
-// g0: the slab's first tile among the job's; the slab's last tile writes the
-// running total to base[slab + 1].
-__device__ __forceinline__ unsigned s2_cell_word(const S2Job &job, const S2PointBits &pb,
-                                                 const unsigned *__restrict__ offx, int y, int w, int z) {
-  const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5;
-  const bool more = w + 1 < WP;
-  const bool nearrule = !job.qef && !job.exact;
-  const unsigned ox = job.qef ? 0u : __ldg(offx + w);
-  const unsigned oy = (!job.qef && s2_off_lattice(job, y + 1)) ? ~0u : 0u;
-  const int dw = more ? 1 : 0;
-  const long long rb0 = ((long long)(z % job.ring) * job.P + y) * WP + w;
-  const long long rb1 = ((long long)((z + 1) % job.ring) * job.P + y) * WP + w;
-  unsigned pw[2][4], nw[2][4];
-#pragma unroll
-  for (int p = 0; p < 2; ++p) {
-    const long long rb = p ? rb1 : rb0;
-    pw[p][0] = __ldg(pb.pos + rb);
-    pw[p][1] = __ldg(pb.pos + rb + dw);
-    pw[p][2] = __ldg(pb.pos + rb + WP);
-    pw[p][3] = __ldg(pb.pos + rb + WP + dw);
-    if (nearrule) {
-      nw[p][0] = __ldg(pb.near + rb);
-      nw[p][1] = __ldg(pb.near + rb + dw);
-      nw[p][2] = __ldg(pb.near + rb + WP);
-      nw[p][3] = __ldg(pb.near + rb + WP + dw);
-    }
-  }
-  unsigned andp[2], orp[2], tb = 0u, tt = 0u;
-#pragma unroll
-  for (int p = 0; p < 2; ++p) {
-    const unsigned p0 = pw[p][0], p1 = pw[p][2];
-    const unsigned p0s = __funnelshift_r(p0, more ? pw[p][1] : 0u, 1);
-    const unsigned p1s = __funnelshift_r(p1, more ? pw[p][3] : 0u, 1);
-    andp[p] = p0 & p0s & p1 & p1s;
-    orp[p] = p0 | p0s | p1 | p1s;
-    if (nearrule) {
-      const unsigned n0 = nw[p][0], n1 = nw[p][2];
-      const unsigned n0s = __funnelshift_r(n0, more ? nw[p][1] : 0u, 1);
-      const unsigned n1s = __funnelshift_r(n1, more ? nw[p][3] : 0u, 1);
-      if (p == 0) {  // the cell's bottom plane: corners k = 1, 2, 3
-        tb = (n0s & ox) | (n1 & oy) | (n1s & (ox | oy));
-      } else {  // its top plane: corners k = 4 .. 7
-        const unsigned oz = s2_off_lattice(job, z + 1) ? ~0u : 0u;
-        tt = (n0 & oz) | (n0s & (ox | oz)) | (n1 & (oy | oz)) | (n1s & (ox | oy | oz));
-      }
-    }
-  }
-  unsigned c = (orp[0] | orp[1]) & ~(andp[0] & andp[1]);
-  if (nearrule) c |= tb | tt;
-  else if (!job.qef) c |= ox | oy | (s2_off_lattice(job, z + 1) ? ~0u : 0u);
-  const unsigned edge = (w == WN - 1 && (job.N & 31)) ? (1u << (job.N & 31)) - 1u : ~0u;
-  return c & edge;
-}
-
-__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_fused(S2Job job, S2PointBits pb,
-                                                             const unsigned *__restrict__ offx,
-                                                             const float *__restrict__ ring,
-                                                             const unsigned *__restrict__ unk, S2Cand cand,
-                                                             unsigned long long *status, unsigned *ticket,
-                                                             unsigned long long *base, int slab_index, int zc0,
-                                                             int zc1, unsigned long long g0, unsigned *err,
-                                                             unsigned long long wait_ns) {
-  __shared__ unsigned s_warp[32];
-  __shared__ unsigned s_tile;
-  __shared__ unsigned long long s_excl;
-  __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const int WN = (job.N + 31) >> 5, NW = job.N * WN, WP = (job.P + 31) >> 5;
-  const unsigned nbp = (unsigned)((NW + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
-  const unsigned ntiles = (unsigned)(zc1 - zc0) * nbp;
-  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-  __syncthreads();
-  const unsigned t = s_tile;
-  if (t >= ntiles) return;  // (the grid has one block per tile)
-  const int dz = (int)(t / nbp), bx = (int)(t - (unsigned)dz * nbp);
-  const int z = zc0 + dz;
-  const int yw = bx * S2_CW_BLOCK + (int)tid;
-  unsigned mask = 0u;
-  int y = 0, w = 0;
-  if (yw < NW) {
-    y = yw / WN;
-    w = yw - y * WN;
-    mask = s2_cell_word(job, pb, offx, y, w, z);
-  }
-  const unsigned cnt = __popc(mask);
-  unsigned inc = cnt;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned x = __shfl_up_sync(S2_FULL, inc, o);
-    if ((int)lane >= o) inc += x;
-  }
-  if (lane == 31) s_warp[warp] = inc;
-  if (tid < 32 && tid >= S2_CW_BLOCK / 32) s_warp[tid] = 0u;
-  __syncthreads();
-  if (warp == 0) {
-    const unsigned tot = s2_warp_exclusive32(s_warp);
-    const unsigned long long excl = s2_lookback(status, (unsigned)(g0 + t), tot, err, wait_ns);
-    if (lane == 0) {
-      s_excl = excl;
-      if (t == ntiles - 1) base[slab_index + 1] = excl + tot;
-    }
-  }
-  __syncthreads();
-  const unsigned total = s_warp[31];  // slots past the block's warps are 0: slot 31 holds the total
-  if (total == 0u) return;
-  {
-    unsigned r = s_warp[warp] + inc - cnt, rem = mask;
-    while (rem) {
-      const unsigned bit = __ffs(rem) - 1u;
-      rem &= rem - 1u;
-      s_list[r++] = (unsigned short)((tid << 5) | bit);
-    }
-  }
-  __syncthreads();
-  const unsigned long long first = s_excl;
-#pragma unroll 1
-  for (unsigned r = tid; r < total; r += S2_CW_BLOCK) {
-    const unsigned e = s_list[r];
-    const int ywc = bx * S2_CW_BLOCK + (int)(e >> 5);
-    const int wy = ywc / WN, wc = ywc - wy * WN;
-    const unsigned bit = e & 31u;
-    S2Cell cell;
-    cell.x = 32 * wc + (int)bit;
-    cell.y = wy;
-    cell.z = z;
-    const unsigned long long o = first + r;
-    if (o >= cand.cap) {
-      atomicOr(err, S2_ERR_CAND_OVF);
-      continue;
-    }
-    float v[8];
-    s2_load_corners<false>(job, ring, cell, v);
-    if (unk) {  // corners of decided tiles: no value in the ring
-      const bool more = wc + 1 < WP;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
-        const long long rbase = ((long long)((cell.z + (q >> 1)) % job.ring) * job.P + (cell.y + (q & 1))) * WP + wc;
-        const unsigned lo = __ldg(unk + rbase), hi = more ? __ldg(unk + rbase + 1) : 0u;
-        if ((lo >> bit) & 1u) v[2 * q] = __int_as_float(0x7fc00000);
-        if ((__funnelshift_r(lo, hi, 1) >> bit) & 1u) v[2 * q + 1] = __int_as_float(0x7fc00000);
-      }
-    }
-    cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
-    float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
-    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
-    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-  }
-}
-
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
 // 8 lattice corner values (NaN where the point's unknown-value bit is set: a
 // decided tile of the pruned evaluation wrote no value there).  Grid (nbp,

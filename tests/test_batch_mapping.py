@@ -5,11 +5,11 @@
   thread, each item's warps see one tile each (so a warp takes one path
   through the pruned program), and every tile record that the evaluation
   reads was written by the tile pass;
-- the per-job classification's tiles (static_kernels.cuh: s2m_cells_fused):
-  slab by slab, each ticket t names one tile of S2_CW_BLOCK words of one cell
-  plane, and the job-wide tile index g0 + t that its look-back uses grows
-  with (z, y, x), covering every word of the job's cell planes once, so the
-  candidate list comes out in (z, y, x) order across slabs and z parts."""
+- the classification's candidate slots (static_kernels.cuh: s2m_cells_mark
+  adds its tile counts to per-plane counts and scans those; s2m_cells_emit
+  adds the counts of the plane's earlier tiles): each tile's first slot
+  equals the exclusive scan of all tile counts in (z, y, x) order, so the
+  candidate list is the same as with a scan over every tile."""
 import os
 import re
 
@@ -109,28 +109,19 @@ def test_cell_groups_lie_in_one_tile(N):
     assert CPT % 4 == 0
 
 
-@pytest.mark.parametrize("N,D,zb,nzc", [(33, 5, 0, 33), (64, 9, 0, 63), (100, 100, 0, 100), (1024, 512, 0, 1024),
-                                        (96, 20, 47, 49), (200, 64, 0, 199)])
-def test_fused_tiles_cover_job_in_order(N, D, zb, nzc):
+@pytest.mark.parametrize("N,planes", [(33, 5), (64, 9), (100, 3), (1024, 2)])
+def test_emit_slots_equal_full_scan(N, planes):
     CW = const("S2_CW_BLOCK", "s2m_device.h")
     WN = (N + 31) // 32
-    NW = N * WN
-    nbp = (NW + CW - 1) // CW
-    seen = np.zeros((nzc, NW), int)
-    last = -1
-    nslabs = (nzc + D - 1) // D
-    for s_ in range(nslabs):
-        zc0 = zb + s_ * D
-        zc1 = min(zb + nzc, zc0 + D)
-        ntiles = (zc1 - zc0) * nbp
-        g0 = (zc0 - zb) * nbp
-        for t in range(ntiles):  # tickets in order
-            dz, bx = divmod(t, nbp)
-            g = g0 + t
-            assert g == last + 1  # job-wide look-back order
-            last = g
-            yw = bx * CW + np.arange(CW)
-            yw = yw[yw < NW]
-            seen[zc0 + dz - zb, yw] += 1
-    assert (seen == 1).all()
-    assert last + 1 == nzc * nbp  # the status words of the job (slab_ctrl) cover every tile
+    nbp = (N * WN + CW - 1) // CW
+    rng = np.random.default_rng(N)
+    cnt = rng.integers(0, 50, (planes, nbp)) * (rng.random((planes, nbp)) < 0.6)
+    base = 12345
+    full = base + np.concatenate([[0], np.cumsum(cnt.reshape(-1))[:-1]]).reshape(planes, nbp)
+    plane_cnt = cnt.sum(1)
+    plane_off = base + np.concatenate([[0], np.cumsum(plane_cnt)[:-1]])
+    for dz in range(planes):
+        for bx in range(nbp):
+            first = plane_off[dz] + cnt[dz, :bx].sum()
+            assert first == full[dz, bx]
+    assert base + plane_cnt.sum() == base + cnt.sum()

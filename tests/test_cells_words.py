@@ -1,5 +1,5 @@
-"""Classification words on the CPU: the bitwise formulas of s2_cell_word
-(static_kernels.cuh, used by s2m_cells_fused), restated in numpy, against the per-cell rule of
+"""Classification words on the CPU: the bitwise formulas of s2m_cells_mark
+(static_kernels.cuh), restated in numpy, against the per-cell rule of
 s2_classify_values (s2m_dc_core.cuh; dualcontour.wgsl's sign test plus the
 reference rule's near-zero test of off-lattice corners).
 
@@ -32,7 +32,7 @@ def funnel1(lo, hi):
 
 
 def words_rule(V, guard, offx, offy, offz, qef=False, exact=False):
-    """Candidate words [nz, N, WN] as s2_cell_word forms them."""
+    """Candidate words [nz, N, WN] as s2m_cells_mark forms them."""
     nzp, P, _ = V.shape
     N = P - 1
     WN, WP = (N + 31) // 32, (P + 31) // 32
