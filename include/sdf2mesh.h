@@ -395,11 +395,12 @@ int s2m_batch_set_wait_limit(s2m_batch *b, double stage_seconds, double lookback
    smooth operators can be skipped; the results are bit-identical either way. */
 int s2m_batch_set_pruning(s2m_batch *b, int enabled);
 /* Where the last run's persistent launches spent their block time: for each
-   stage (0 tile pass, 1 lattice, 2 cells, 3 vertices, 4 vertex compaction,
-   5 row scan, 6 quads; nstages entries written, 0 past the last stage) the
-   summed block time of its items in ms of the GPU's global timer, and in
-   *wait_ms the block time spent waiting for a job's previous stage. */
-#define S2M_BATCH_STAGES 7
+   stage (0 tile pass, 1 lattice, 2 candidate bits, 3 candidate slots, 4
+   candidates, 5 vertices, 6 vertex compaction, 7 row scan, 8 quads; nstages
+   entries written, 0 past the last stage) the summed block time of its items
+   in ms of the GPU's global timer, and in *wait_ms the block time spent
+   waiting for a job's previous stage. */
+#define S2M_BATCH_STAGES 9
 int s2m_batch_stage_profile(const s2m_batch *b, double *busy_ms, uint32_t nstages, double *wait_ms);
 void s2m_batch_free(s2m_batch *b);
 

@@ -602,7 +602,8 @@ class Batch:
         _check(load_library().s2m_batch_set_wait_limit(self._h, float(stage_seconds), float(lookback_seconds)),
                None, "wait limit")
 
-    BATCH_STAGES = ("tiles", "lattice", "cells", "vertices", "vcompact", "rowscan", "quads")
+    BATCH_STAGES = ("tiles", "lattice", "cell_bits", "cell_slots", "candidates", "vertices", "vcompact", "rowscan",
+                    "quads")
 
     def stage_profile(self) -> dict:
         """Block time (ms, summed over blocks) of the last run per stage, and the

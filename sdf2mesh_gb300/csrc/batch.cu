@@ -4,10 +4,12 @@
 // and operators, evaluated by an interpreter on the device, so no per-job
 // compilation) plus its own resolution and bounds.  All jobs of a batch run
 // in ONE launch of s2m_batch_kernel: its blocks take tickets from a device
-// work queue in which every job contributes seven stages in order --
+// work queue in which every job contributes nine stages in order --
 //   T tile pass (interval pruning of the program per tile of the lattice),
-//   E evaluate the job's lattice, C classify cells (ordered candidate list),
-//   X place vertices, V compact vertices, R scan row starts, Q emit quads --
+//   E evaluate the job's lattice, M candidate bits per classification tile,
+//   S (one item) the tiles' first candidate slots, C the candidates in
+//   (z, y, x) order, X place vertices, V compact vertices, R scan row starts,
+//   Q emit quads --
 // each stage a run of items.  A block that takes an item of stage s of a job
 // first waits until every item of stage s-1 of that job is done.  Those items
 // hold lower tickets, so they were taken by blocks already running: the wait
@@ -39,13 +41,23 @@
 // ---------------------------------------------------------------------------
 // Device-side batch description.
 
-enum { S2_ST_TILES = 0, S2_ST_EVAL, S2_ST_CELLS, S2_ST_VERT, S2_ST_VCOMPACT, S2_ST_ROWS, S2_ST_QUADS, S2_NSTAGES };
+enum {
+  S2_ST_TILES = 0,
+  S2_ST_EVAL,
+  S2_ST_MARK,   // candidate bits and counts per classification tile
+  S2_ST_CSCAN,  // one item: the tiles' first candidate slots
+  S2_ST_EMIT,   // candidates with their corner values
+  S2_ST_VERT,
+  S2_ST_VCOMPACT,
+  S2_ST_ROWS,
+  S2_ST_QUADS,
+  S2_NSTAGES
+};
 static_assert(S2_NSTAGES == S2M_BATCH_STAGES, "stage count of the C ABI");
 #define S2_B_TILE 8          // lattice points per edge of a tile
 #define S2_B_TILES_ITEM 256  // tiles per item of the tile pass (one per thread)
 #define S2_B_EVAL_TILES 64   // tiles per item of the evaluation (one warp per tile)
-#define S2_B_CELL_TILES 4    // classification tiles per item (s2_cell_tiles publishes every tile's
-                             // aggregate before any look-back)
+#define S2_B_CELL_TILES 4    // classification tiles per item of the mark and emit stages
 #define S2_B_VERT_CHUNK 256
 #define S2_ERR_BATCH_WAIT 0x20u
 
@@ -60,7 +72,9 @@ struct S2BatchJob {
   int prune;                        // 0: every point with the full program (tiles unused)
   S2Cand cand;
   S2MeshDev mesh;
-  unsigned long long *cell_status;  // look-back words of the classification tiles
+  unsigned *cwords;                 // candidate bits: one word per thread and classification tile
+  unsigned *ctcnt;                  // candidates per classification tile
+  unsigned long long *ctoff;        // first candidate slot of each classification tile
   unsigned *xcounter;               // vertex chunk counter
   unsigned *done;                   // completed items per stage
   unsigned nitems[S2_NSTAGES];
@@ -225,15 +239,30 @@ __device__ __forceinline__ void s2b_stage_eval(const S2BatchJob &J, unsigned ite
   }
 }
 
-// Classification tiles item * S2_B_CELL_TILES .. of the job, in order (the
-// tickets of this stage come in tile order, so the look-back only waits for
-// tiles already taken).
-__device__ __forceinline__ void s2b_stage_cells(const S2BatchJob &J, unsigned item) {
-  const long long ncells = (long long)J.nzc * J.job.N * J.job.N;
-  const unsigned ntiles = (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
-  s2_cell_tiles<true, S2_B_CELL_TILES>(J.job, J.lattice, J.cand, J.cell_status, J.mesh.err, item * S2_B_CELL_TILES,
-                                       ntiles, ncells, 0, 0ull, J.cand.base + 1, J.mesh.wait_ns,
-                                       S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx});
+// Classification of the job (s2_cell_mark_tiles, s2_scan_tiles,
+// s2_cell_emit_tiles): S2_B_CELL_TILES tiles per item of the mark and emit
+// stages, one item for the scan.
+__device__ __forceinline__ unsigned s2b_cell_tiles(const S2BatchJob &J, long long &ncells) {
+  ncells = (long long)J.nzc * J.job.N * J.job.N;
+  return (unsigned)((ncells + S2_CELL_TILE - 1) / S2_CELL_TILE);
+}
+__device__ __forceinline__ void s2b_stage_mark(const S2BatchJob &J, unsigned item) {
+  long long ncells;
+  const unsigned ntiles = s2b_cell_tiles(J, ncells);
+  s2_cell_mark_tiles<true, S2_B_CELL_TILES>(J.job, J.lattice, item * S2_B_CELL_TILES, ntiles, ncells, 0,
+                                            S2CellSkip{J.prune ? J.tiles : nullptr, (unsigned)S2_CSG_TILE_WORDS, J.ntx},
+                                            J.cwords, J.ctcnt);
+}
+__device__ __forceinline__ void s2b_stage_cscan(const S2BatchJob &J) {
+  long long ncells;
+  const unsigned ntiles = s2b_cell_tiles(J, ncells);
+  s2_scan_tiles<256, 16>(J.ctcnt, ntiles, J.ctoff, J.cand.base, 0);  // cand.base[1] = the job's candidates
+}
+__device__ __forceinline__ void s2b_stage_emit(const S2BatchJob &J, unsigned item) {
+  long long ncells;
+  const unsigned ntiles = s2b_cell_tiles(J, ncells);
+  s2_cell_emit_tiles<true, S2_B_CELL_TILES>(J.job, J.lattice, J.cand, J.mesh.err, item * S2_B_CELL_TILES, ntiles, 0,
+                                            J.cwords, J.ctcnt, J.ctoff);
 }
 
 __device__ __forceinline__ void s2b_stage_vertices(const S2BatchJob &J) {
@@ -363,7 +392,9 @@ __global__ void __launch_bounds__(256) s2m_batch_kernel(const S2BatchJob *__rest
       switch (sg.stage) {
         case S2_ST_TILES: s2b_stage_tiles(J, item); break;
         case S2_ST_EVAL: s2b_stage_eval(J, item); break;
-        case S2_ST_CELLS: s2b_stage_cells(J, item); break;
+        case S2_ST_MARK: s2b_stage_mark(J, item); break;
+        case S2_ST_CSCAN: s2b_stage_cscan(J); break;
+        case S2_ST_EMIT: s2b_stage_emit(J, item); break;
         case S2_ST_VERT: s2b_stage_vertices(J); break;
         case S2_ST_VCOMPACT: s2_vcompact_worker(J.job, J.cand, J.mesh, 1, item == 0); break;
         case S2_ST_ROWS: s2_rowscan_worker(J.mesh, (unsigned long long)J.job.N * J.job.N); break;
@@ -517,11 +548,12 @@ void job_sizes(const HostJob &h, size_t &zero_bytes, size_t &data_bytes) {
   const size_t vc_tiles = (h.cand_cap + S2_VC_TILE - 1) / S2_VC_TILE;
   const size_t scan_tiles = (N * N + S2_SCAN_TILE - 1) / S2_SCAN_TILE;
   const size_t quad_tiles = (h.vcap + S2_Q_TILE - 1) / S2_Q_TILE;
-  zero_bytes = al(2 * 8) + al(vc_tiles * 8) + al(cell_tiles * 8) + al((scan_tiles + quad_tiles) * 8) + al(N * N * 4) +
+  zero_bytes = al(2 * 8) + al(vc_tiles * 8) + al((scan_tiles + quad_tiles) * 8) + al(N * N * 4) +
                al(8 * 4) /*counters*/ + al(8 * 4) /*done*/ + al(8 * 8) /*ntris, invalid, vtotal, err*/ + al(4);
   data_bytes = al(size_t(h.job.ring) * size_t(h.job.plane) * 4) + al(h.cand_cap * 8) + al(h.cand_cap * 32) +
                al(h.cand_cap * 12) * 2 + al((N * N + 1) * 4) + al(h.vcap * 12) * 2 + al(h.vcap * 8) + al(h.tcap * 12) +
-               al(tile_records(h) * S2_CSG_TILE_WORDS * 4);
+               al(tile_records(h) * S2_CSG_TILE_WORDS * 4) + al(cell_tiles * S2_CELL_BLOCK * 4) + al(cell_tiles * 4) +
+               al(cell_tiles * 8);
 }
 
 }  // namespace
@@ -631,7 +663,6 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
     char *z = arena + zoff;
     J.cand.base = reinterpret_cast<unsigned long long *>(z); z += al(2 * 8);
     J.cand.status = reinterpret_cast<unsigned long long *>(z); z += al(vc_tiles * 8);
-    J.cell_status = reinterpret_cast<unsigned long long *>(z); z += al(cell_tiles * 8);
     J.mesh.scan_status = reinterpret_cast<unsigned long long *>(z); z += al((scan_tiles + quad_tiles) * 8);
     J.mesh.rowcnt = reinterpret_cast<unsigned *>(z); z += al(N * N * 4);
     unsigned *counters = reinterpret_cast<unsigned *>(z); z += al(8 * 4);
@@ -658,6 +689,9 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
     J.mesh.key = reinterpret_cast<unsigned long long *>(d); d += al(h.vcap * 8);
     J.mesh.tris = reinterpret_cast<unsigned *>(d); d += al(h.tcap * 12);
     J.tiles = reinterpret_cast<unsigned *>(d); d += al(tile_records(h) * S2_CSG_TILE_WORDS * 4);
+    J.cwords = reinterpret_cast<unsigned *>(d); d += al(cell_tiles * S2_CELL_BLOCK * 4);
+    J.ctcnt = reinterpret_cast<unsigned *>(d); d += al(cell_tiles * 4);
+    J.ctoff = reinterpret_cast<unsigned long long *>(d); d += al(cell_tiles * 8);
     J.ntx = int(tiles_per_axis(h));
     J.prune = h.prune ? 1 : 0;
     doff += db[i];
@@ -677,7 +711,9 @@ int launch_wave(s2m_batch *b, const std::vector<int> &idx, cudaStream_t st, Wave
       J.nitems[S2_ST_TILES] = h.prune ? unsigned((ntiles + S2_B_TILES_ITEM - 1) / S2_B_TILES_ITEM) : 1u;
       J.nitems[S2_ST_EVAL] = unsigned((ntiles + S2_B_EVAL_TILES - 1) / S2_B_EVAL_TILES);
     }
-    J.nitems[S2_ST_CELLS] = unsigned(std::max<size_t>(1, (cell_tiles + S2_B_CELL_TILES - 1) / S2_B_CELL_TILES));
+    J.nitems[S2_ST_MARK] = unsigned(std::max<size_t>(1, (cell_tiles + S2_B_CELL_TILES - 1) / S2_B_CELL_TILES));
+    J.nitems[S2_ST_CSCAN] = 1u;
+    J.nitems[S2_ST_EMIT] = J.nitems[S2_ST_MARK];
     J.nitems[S2_ST_VERT] = unsigned(std::min<unsigned long long>(128, std::max<unsigned long long>(1, n2 / 2048)));
     J.nitems[S2_ST_VCOMPACT] = unsigned(std::min<unsigned long long>(64, std::max<unsigned long long>(1, n2 / 8192)));
     J.nitems[S2_ST_ROWS] = unsigned(std::min<unsigned long long>(16, std::max<unsigned long long>(1, n2 / 16384)));

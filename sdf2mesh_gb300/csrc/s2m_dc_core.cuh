@@ -456,39 +456,30 @@ struct S2CellSkip {
   int ntx;
 };
 
-// Classification tiles tile0 .. tile0 + M - 1 (S2_CELL_TILE cells each,
-// S2_CELL_BLOCK threads, S2_CELL_CPT consecutive cells per thread in groups
-// of 4): candidates appended in (z, y, x) order at base + (prefix over
-// tiles), each with its 8 corner values; the job's last tile stores the
-// running total in *next_base.  In two phases: every tile is classified and
-// its aggregate published first, then one look-back for the first tile gives
-// the prefixes of all M (the later ones chain within the block), and the
-// candidates are written.  (Published only after the earlier tiles of the same
-// block had looked back, a block's last aggregate came late, and the next
-// block's look-back waited for it: blocks ran one after another.)  With
-// `skip`, a group of 4 cells that lies in one decided tile (N a multiple of
-// 4: a group is then 4 cells of one row, x from a multiple of 4) is not
+// Classification of the batch engine in three stages that never wait on one
+// another inside a stage (a decoupled look-back over a job's tiles walked
+// far back behind the many tiles in flight):
+//   s2_cell_mark_tiles  tiles tile0 .. tile0 + M - 1 (S2_CELL_TILE cells each,
+//                       S2_CELL_BLOCK threads, S2_CELL_CPT consecutive cells
+//                       per thread in groups of 4): each thread's candidate
+//                       bits go to words[tile * S2_CELL_BLOCK + thread], the
+//                       tile's count to tcnt[tile];
+//   s2_scan_tiles       (one block) the counts into each tile's first slot;
+//   s2_cell_emit_tiles  each tile's candidates in (z, y, x) order, with their
+//                       8 corner values.
+// With `skip`, a group of 4 cells that lies in one decided tile (N a multiple
+// of 4: a group is then 4 cells of one row, x from a multiple of 4) is not
 // loaded at all.
 template <bool CG, int M>
-__device__ __forceinline__ void s2_cell_tiles(const S2Job &job, const float *__restrict__ ring, const S2Cand &cand,
-                                              unsigned long long *status, unsigned *err, unsigned tile0,
-                                              unsigned ntiles, long long ncells, int zc0, unsigned long long base,
-                                              unsigned long long *next_base, unsigned long long wait_ns,
-                                              S2CellSkip skip = S2CellSkip{nullptr, 0u, 0}) {
+__device__ __forceinline__ void s2_cell_mark_tiles(const S2Job &job, const float *__restrict__ ring, unsigned tile0,
+                                                   unsigned ntiles, long long ncells, int zc0, S2CellSkip skip,
+                                                   unsigned *words, unsigned *tcnt) {
   __shared__ unsigned s_warp[32];
-  __shared__ unsigned s_cnt[M];
-  __shared__ unsigned long long s_excl[M];
-  __shared__ unsigned short s_cl[S2_CELL_TILE];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const unsigned nt = tile0 < ntiles ? min((unsigned)M, ntiles - tile0) : 0u;  // the same in every thread
-  unsigned mask[M];  // bit g * 4 + m: cell c0 + 4g + m of tile tile0 + t
-  // phase 1: classify, count, publish each tile's aggregate at once (loops
-  // over t not unrolled: one copy of the classification code)
 #pragma unroll 1
   for (int t = 0; t < M; ++t) {
-    mask[t] = 0u;
-    if ((unsigned)t >= nt) continue;
     const unsigned tile = tile0 + (unsigned)t;
+    if (tile >= ntiles) break;  // the same in every thread
     const long long c0 = (long long)tile * S2_CELL_TILE + (long long)S2_CELL_CPT * tid;
     unsigned decided = 0;  // bit g: group g lies in a decided tile
     if (skip.flags && !job.exact && (job.N & 3) == 0) {
@@ -506,14 +497,14 @@ __device__ __forceinline__ void s2_cell_tiles(const S2Job &job, const float *__r
 #pragma unroll
       for (int g = 0; g < S2_CELL_CPT / 4; ++g) decided |= (f[g] & S2_TILE_DECIDED ? 1u : 0u) << g;
     }
-    unsigned mk = 0u;
+    unsigned mk = 0u;  // bit g * 4 + m: cell c0 + 4g + m
 #pragma unroll
     for (int g = 0; g < S2_CELL_CPT / 4; ++g) {
       if ((decided >> g) & 1u) continue;
       float v[4][8];
       mk |= s2_classify4<CG>(job, ring, c0 + 4 * g, ncells, zc0, v) << (4 * g);
     }
-    mask[t] = mk;
+    words[(size_t)tile * S2_CELL_BLOCK + tid] = mk;
     unsigned cnt = __popc(mk);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(S2_FULL, cnt, o);
@@ -523,35 +514,28 @@ __device__ __forceinline__ void s2_cell_tiles(const S2Job &job, const float *__r
       unsigned tot = lane < S2_CELL_BLOCK / 32 ? s_warp[lane] : 0u;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(S2_FULL, tot, o);
-      if (lane == 0) {
-        s_cnt[t] = tot;
-        s2_st_release(status + tile, ((tile == 0 ? S2_LB_PRE : S2_LB_AGG) << 62) | tot);
-      }
+      if (lane == 0) tcnt[tile] = tot;
     }
     __syncthreads();  // s_warp is reused
   }
-  // phase 2: the first tile's prefix by look-back, the others chained here
-  if (warp == 0 && nt > 0) {
-    const unsigned long long e0 = tile0 == 0 ? 0ull : s2_lookback_walk(status, tile0, err, wait_ns);
-    if (lane == 0) {
-      unsigned long long run = e0;
-      for (unsigned t = 0; t < nt; ++t) {
-        s_excl[t] = run;
-        run += s_cnt[t];
-        if (tile0 + t > 0) s2_st_release(status + tile0 + t, (S2_LB_PRE << 62) | run);
-      }
-      if (tile0 + nt == ntiles) *next_base = base + run;
-    }
-  }
-  __syncthreads();
-  // phase 3: each tile's candidates in order (cell offsets within the tile),
-  // then written one per thread: every thread's corner loads are in flight
-  // together, however the candidates fall among the threads
+}
+
+template <bool CG, int M>
+__device__ __forceinline__ void s2_cell_emit_tiles(const S2Job &job, const float *__restrict__ ring,
+                                                   const S2Cand &cand, unsigned *err, unsigned tile0, unsigned ntiles,
+                                                   int zc0, const unsigned *words, const unsigned *tcnt,
+                                                   const unsigned long long *toff) {
+  __shared__ unsigned s_warp[32];
+  __shared__ unsigned short s_cl[S2_CELL_TILE];
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
 #pragma unroll 1
   for (int t = 0; t < M; ++t) {
-    if ((unsigned)t >= nt) break;
     const unsigned tile = tile0 + (unsigned)t;
-    const unsigned cnt = __popc(mask[t]);
+    if (tile >= ntiles) break;  // the same in every thread
+    const unsigned total = __ldcg(tcnt + tile);
+    if (total == 0u) continue;  // the same in every thread
+    const unsigned mk = __ldcg(words + (size_t)tile * S2_CELL_BLOCK + tid);
+    const unsigned cnt = __popc(mk);
     unsigned inc = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -563,8 +547,8 @@ __device__ __forceinline__ void s2_cell_tiles(const S2Job &job, const float *__r
     __syncthreads();
     if (warp == 0) s2_warp_exclusive32(s_warp);
     __syncthreads();
-    {
-      unsigned r = s_warp[warp] + (inc - cnt), rem = mask[t];
+    {  // the tile's candidates in order (cell offsets within the tile)
+      unsigned r = s_warp[warp] + (inc - cnt), rem = mk;
       while (rem) {
         const unsigned m = (unsigned)__ffs(rem) - 1u;
         rem &= rem - 1u;
@@ -572,8 +556,9 @@ __device__ __forceinline__ void s2_cell_tiles(const S2Job &job, const float *__r
       }
     }
     __syncthreads();
-    const unsigned total = s_cnt[t];
-    const unsigned long long first = base + s_excl[t];
+    // written one per thread: every thread's corner loads are in flight
+    // together, however the candidates fall among the threads
+    const unsigned long long first = __ldcg(toff + tile);
 #pragma unroll 1
     for (unsigned r = tid; r < total; r += S2_CELL_BLOCK) {
       const unsigned long long o = first + r;
@@ -583,7 +568,7 @@ __device__ __forceinline__ void s2_cell_tiles(const S2Job &job, const float *__r
       }
       const S2Cell cell = s2_cell_of(job, (long long)tile * S2_CELL_TILE + s_cl[r], zc0);
       float v[8];
-      s2_load_corners<CG>(job, ring, cell, v);  // candidates are few: re-read their corners
+      s2_load_corners<CG>(job, ring, cell, v);
       cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
       float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
       dst[0] = make_float4(v[0], v[1], v[2], v[3]);

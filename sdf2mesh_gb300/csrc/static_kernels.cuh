@@ -22,61 +22,6 @@
 // corner whose reference coordinates are off the lattice is near zero (every
 // cell with such a corner when S2M_JOB_EXACT_CORNERS).
 
-// tile_off[t] = cand.base[slab] + (candidates of tiles < t); cand.base[slab + 1]
-// = the slab's running total.  Run by one block of NT threads, CPT
-// consecutive counts per thread and step, any tile count; the counts are
-// read from L2 (other blocks wrote them).
-template <int NT, int CPT>
-__device__ __forceinline__ void s2_scan_tiles(const unsigned *tile_cnt, unsigned ntiles,
-                                              unsigned long long *__restrict__ tile_off, unsigned long long *base,
-                                              int slab_index) {
-  __shared__ unsigned long long s_warp[32];
-  __shared__ unsigned long long s_carry;
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  if (tid == 0) s_carry = __ldcg(base + slab_index);
-  if (tid < 32) s_warp[tid] = 0ull;
-  __syncthreads();
-  for (unsigned t0 = 0; t0 < ntiles; t0 += NT * CPT) {
-    const unsigned tb = t0 + tid * CPT;
-    unsigned v[CPT];
-    unsigned long long sum = 0ull;
-#pragma unroll
-    for (int q = 0; q < CPT; ++q) {
-      v[q] = tb + q < ntiles ? __ldcg(tile_cnt + tb + q) : 0u;
-      sum += v[q];
-    }
-    unsigned long long inc = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long x = __shfl_up_sync(S2_FULL, inc, o);
-      if ((int)lane >= o) inc += x;
-    }
-    if (lane == 31) s_warp[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-      const unsigned long long w = s_warp[lane];
-      unsigned long long wi = w;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long x = __shfl_up_sync(S2_FULL, wi, o);
-        if ((int)lane >= o) wi += x;
-      }
-      s_warp[lane] = wi - w;
-    }
-    __syncthreads();
-    const unsigned long long carry = s_carry;
-    unsigned long long run = carry + s_warp[warp] + inc - sum;
-#pragma unroll
-    for (int q = 0; q < CPT; ++q) {
-      if (tb + q < ntiles) tile_off[tb + q] = run;
-      run += v[q];
-    }
-    __syncthreads();
-    if (tid == NT - 1) s_carry = run;  // the last thread's running total
-    __syncthreads();
-  }
-  if (tid == 0) base[slab_index + 1] = s_carry;
-}
 
 // The end of one z part of a job (s2m_mesh_generate): its vertices from index
 // skip = *skip_at on (its context plane, which the part below it has already
