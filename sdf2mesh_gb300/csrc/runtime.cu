@@ -221,6 +221,7 @@ struct s2m_mesh {
   int zpart_begin = 0, zpart_end = -1;
   double zfrac = 1.0;
   unsigned quads_from_z = 0;  // vertices with a lower label z make no quads (the context plane of a part)
+  bool tiles_ready = false;   // the tile pass of every slab was enqueued elsewhere (s2m_mesh_generate)
   // host time of the last s2m_mesh_create (ms) and its pipeline runs
   double t_setup = 0, t_launch = 0, t_wait = 0;
   unsigned runs = 0;
@@ -1038,7 +1039,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->last_variant = ev;
   m->eval_points = 0;
   m->eval_fp_ops = m->eval_sfu_ops = 0;
-  if (pruned) {  // operation counters and the slabs' list lengths
+  const bool tiles_ready = pruned && m->tiles_ready && m->prune_chunk >= m->nslabs;
+  if (pruned && !tiles_ready) {  // operation counters and the slabs' list lengths
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
   }
@@ -1057,7 +1059,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     m->eval_points += double(pts) * nk;
     if (pruned) {
       const int cb = s - s % m->prune_chunk;
-      if (s == cb) S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
+      if (s == cb && !tiles_ready) S2_LAUNCH(0, 0, launch_tiles(m, cb, std::min(m->nslabs, cb + m->prune_chunk), st));
       S2_LAUNCH(0, double(pts) * nk, launch_evalp(m, ev, s, cb, st));
     } else {
       void *eargs[] = {&jj, &ring, &k0, &nk};
@@ -1396,6 +1398,18 @@ struct HostMeshOwner {
 template <class T> T *mapped(const HostBlock &b) {
   void *d = nullptr;
   return cudaHostGetDevicePointer(&d, b.p, 0) == cudaSuccess ? static_cast<T *>(d) : nullptr;
+}
+
+// The stream the later z parts' tile passes run on (one per device).
+cudaStream_t tile_stream() {
+  static std::mutex mu;
+  static cudaStream_t streams[kNoallocMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev] = nullptr;
+  return streams[dev];
 }
 
 // The side stream the z parts' host copies run on (one per device).
@@ -2085,19 +2099,38 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
     set_err(err, errlen, "pinned host arrays");
     return S2M_E_OOM;
   }
-  // All parts' kernels first (each ending with its copy plan), then, as each
-  // part finishes, its copies on the side stream's copy engine: they run
-  // while the later parts' kernels do.
+  // The later parts' tile passes (independent of every other part) on a third
+  // stream, so that they run beside part 0's kernels; then all parts'
+  // kernels (each ending with its copy plan), then, as each part finishes,
+  // its copies on the side stream's copy engine: they run while the later
+  // parts' kernels do.
   cudaError_t e = cudaSuccess;
+  std::vector<cudaEvent_t> tev(K, nullptr), pev;
+  {
+    int ev_v = sdf->eval_variant >= 0 ? sdf->eval_variant : 0;
+    cudaStream_t ts = tile_stream();
+    for (unsigned k = 1; k < K && ts && e == cudaSuccess; ++k) {
+      s2m_mesh *m = pm[k];
+      if (!(kEvalVariants[ev_v].pruned && m->prune_buf && m->prune_chunk >= m->nslabs)) continue;
+      if ((e = cudaEventCreateWithFlags(&tev[k], cudaEventDisableTiming)) != cudaSuccess) break;
+      ev.push_back(tev[k]);
+      if ((e = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, ts)) != cudaSuccess) break;
+      if ((e = launch_tiles(m, 0, m->nslabs, ts)) != cudaSuccess) break;
+      if ((e = cudaEventRecord(tev[k], ts)) != cudaSuccess) break;
+      m->tiles_ready = true;
+    }
+  }
   for (unsigned k = 0; k < K && e == cudaSuccess; ++k) {
     s2m_mesh *m = pm[k];
     cudaEvent_t done;
     if ((e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming)) != cudaSuccess) break;
     ev.push_back(done);
+    pev.push_back(done);
+    if (tev[k] && (e = cudaStreamWaitEvent(st, tev[k], 0)) != cudaSuccess) break;
     if ((e = enqueue(m, st)) != cudaSuccess) break;
     // the part's first non-context row: its row start counts the context plane's vertices
     const unsigned *skip_at = k ? m->rowstart + (unsigned long long)m->quads_from_z * m->N : nullptr;
-    s2m_part_finish<<<unsigned(device_sm_count()) * 4, 256, 0, st>>>(mesh_dev(m), skip_at,
+    s2m_part_finish<<<unsigned(device_sm_count()) * 4, 256, 0, st>>>(mesh_dev(m), skip_at, m->cand_base + m->nslabs,
                                                                       k ? tot_d + (k - 1) : nullptr, tot_d + k,
                                                                       vcap, tcap);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
@@ -2105,7 +2138,7 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   }
   const S2HostTotals *tot_h = static_cast<const S2HostTotals *>(totals.p);
   for (unsigned k = 0; k < K && e == cudaSuccess; ++k) {
-    if ((e = cudaEventSynchronize(ev[k])) != cudaSuccess) break;
+    if ((e = cudaEventSynchronize(pev[k])) != cudaSuccess) break;
     const S2HostTotals t = tot_h[k];
     if (t.err) break;  // the one-piece fallback below
     const s2m_mesh *m = pm[k];
@@ -2129,13 +2162,15 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
     return S2M_E_CUDA;
   }
   unsigned flags = 0;
-  for (s2m_mesh *m : pm) {
-    if ((rc = readback(m, st, err, errlen)) != S2M_OK) {
-      cleanup();
-      return rc;
-    }
-    flags |= m->errflags;
-    if (!(m->errflags & (S2_ERR_CAND_OVF | S2_ERR_VERT_OVF | S2_ERR_TRI_OVF))) learn_caps(m);
+  for (unsigned k = 0; k < K; ++k) {  // the parts' counts, from their copy plans (no further readback)
+    s2m_mesh *m = pm[k];
+    const S2HostTotals &t = tot_h[k];
+    flags |= t.err;
+    if (t.err) continue;
+    m->ncand = t.ncand;
+    m->nverts = t.vfirst + t.vcount;
+    m->ntris = t.tcount;
+    learn_caps(m);
   }
   const S2HostTotals t = static_cast<const S2HostTotals *>(totals.p)[K - 1];
   flags |= t.err;

@@ -37,9 +37,11 @@ struct S2HostTotals {
   unsigned long long nverts, ntris, invalid;       // running totals after this part
   unsigned long long vfirst, vcount, vbase;        // copy: device vertices vfirst .. -> host vbase ..
   unsigned long long tcount, tbase;                // copy: device triangles 0 .. tcount -> host tbase ..
+  unsigned long long ncand;                        // the part's candidate cells
   unsigned err, pad;
 };
 __global__ void __launch_bounds__(256) s2m_part_finish(S2MeshDev mesh, const unsigned *skip_at,
+                                                       const unsigned long long *ncand,
                                                        const S2HostTotals *prev, S2HostTotals *cur,
                                                        unsigned long long hvcap, unsigned long long htcap) {
   const unsigned long long V = *mesh.vtotal, T = *mesh.ntris;
@@ -57,6 +59,7 @@ __global__ void __launch_bounds__(256) s2m_part_finish(S2MeshDev mesh, const uns
     cur->vbase = vb;
     cur->tcount = err ? 0ull : T;
     cur->tbase = tb;
+    cur->ncand = *ncand;
     cur->err = err;
     cur->pad = 0u;
   }
