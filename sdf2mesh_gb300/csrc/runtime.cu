@@ -679,6 +679,33 @@ template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
 unsigned long long *prune_bases(const s2m_mesh *m) { return prune_at<unsigned long long>(m, m->prune_base_off); }
 unsigned *prune_list_counts(const s2m_mesh *m) { return reinterpret_cast<unsigned *>(m->prune_buf + 2); }
 
+// Launches of the per-job pipeline with programmatic dependent launch: a
+// kernel's blocks may be scheduled while the kernel before it in the stream
+// drains, and wait at S2_PDL_WAIT until its writes are visible.
+cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  attr->id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr->val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchAttribute attr;
+  const cudaLaunchConfig_t cfg = pdl_config(grid, block, smem, st, &attr);
+  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+cudaError_t launch_pdl(cudaKernel_t k, dim3 grid, dim3 block, size_t smem, cudaStream_t st, void **args) {
+  cudaLaunchAttribute attr;
+  const cudaLaunchConfig_t cfg = pdl_config(grid, block, smem, st, &attr);
+  return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void *>(k), args);
+}
+
 // Device pointers of the counters inside jobctl.
 struct JobCtl {
   unsigned long long *ntris, *invalid, *vtotal;
@@ -707,16 +734,16 @@ cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t
   int D = m->D, nzc = m->nzc;
   const unsigned long long nc = m->slab_coarse_base[size_t(s_end)] - m->slab_coarse_base[size_t(s_begin)];
   void *cargs[] = {&jj, &sbits, &cbase, &s_begin, &s_end, &D, &nzc};
-  cudaError_t e = cudaLaunchKernel((const void *)m->sdf->k_tiles_coarse,
-                                   dim3(unsigned((nc + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), cargs, 0, st);
+  cudaError_t e = launch_pdl(m->sdf->k_tiles_coarse, dim3(unsigned((nc + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
+                             dim3(S2_PT_BLOCK), 0, st, cargs);
   if (e != cudaSuccess) return e;
   // one thread per tile slot of each coarse box (s2m_tiles)
   const unsigned long long n = nc * S2_PT_COARSE * S2_PT_COARSE * S2_PT_COARSE_Z;
   unsigned *list = prune_at<unsigned>(m, m->prune_list_off);
   unsigned *counts = prune_list_counts(m);
   void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc, &list, &counts};
-  return cudaLaunchKernel((const void *)m->sdf->k_tiles, dim3(unsigned((n + S2_PT_BLOCK - 1) / S2_PT_BLOCK)),
-                          dim3(S2_PT_BLOCK), targs, 0, st);
+  return launch_pdl(m->sdf->k_tiles, dim3(unsigned((n + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), 0, st,
+                    targs);
 }
 cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaStream_t st) {
   S2Job jj = m->job;
@@ -733,8 +760,7 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
     const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
     const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
     unsigned *chunks = jobctl(m).counters + 5;  // set to zero by the fill, taken by the listed evaluation
-    s2m_fill_decided<<<fg, 256, 0, st>>>(jj, pb, bits, W1, k0, nk, g.tzs, chunks);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_pdl(s2m_fill_decided, fg, dim3(256), 0, st, jj, pb, bits, W1, k0, nk, g.tzs, chunks);
     if (e != cudaSuccess) return e;
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
                            (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
@@ -743,12 +769,10 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
     // one block per SM takes chunks of the list (its length is on the device)
     const long long lblocks = std::min<long long>((g.ntiles + S2_PL_BLOCK / 32 - 1) / (S2_PL_BLOCK / 32),
                                                   (long long)device_sm_count());
-    return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned(lblocks)), dim3(S2_PL_BLOCK), largs, 0,
-                            st);
+    return launch_pdl(m->sdf->k_eval[v], dim3(unsigned(lblocks)), dim3(S2_PL_BLOCK), 0, st, largs);
   }
   void *pargs[] = {&jj, &ring, &pb, &bits, &k0, &nk, &g.tzs, &g.nzt};
-  return cudaLaunchKernel((const void *)m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), pargs,
-                          0, st);
+  return launch_pdl(m->sdf->k_eval[v], dim3(unsigned((g.ntiles + 3) / 4)), dim3(S2_PT_BLOCK), 0, st, pargs);
 }
 
 // Classification buffers: words of 32 cells per slab (tiles of S2_CW_BLOCK
@@ -1047,7 +1071,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   // finished-block counter and plane counts of the classification (each slab's
   // last mark block leaves them zero for the next)
   if ((e = cudaMemsetAsync(m->tile_cnt + m->cell_tiles, 0, (1 + size_t(m->D)) * 4, st)) != cudaSuccess) return e;
-  S2_LAUNCH(1, 0, (s2m_offx<<<unsigned((N + 255) / 256), 256, 0, st>>>(j, m->offx), cudaGetLastError()));
+  S2_LAUNCH(1, 0, launch_pdl(s2m_offx, unsigned((N + 255) / 256), 256, 0, st, j, m->offx));
   const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
     int zc0 = j.zb + s * m->D;
@@ -1064,25 +1088,21 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     } else {
       void *eargs[] = {&jj, &ring, &k0, &nk};
       dim3 eg(eval_blocks, unsigned((nk + run - 1) / run));
-      S2_LAUNCH(0, double(pts) * nk,
-                cudaLaunchKernel((const void *)m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), eargs, 0, st));
+      S2_LAUNCH(0, double(pts) * nk, launch_pdl(m->sdf->k_eval[ev], eg, dim3(S2_EVAL_BLOCK), 0, st, eargs));
     }
     unsigned long long ncells = (unsigned long long)(zc1 - zc0) * N * N;
     if (!pruned)  // the pruned evaluation writes the point bits of its planes itself
-      S2_LAUNCH(1, 0, (s2m_cells_bits<<<dim3(unsigned((j.P + 7) / 8), unsigned(nk)), 256, 0, st>>>(j, m->ring, pb, k0),
-                       cudaGetLastError()));
+      S2_LAUNCH(1, 0, launch_pdl(s2m_cells_bits, dim3(unsigned((j.P + 7) / 8), unsigned(nk)), 256, 0, st, j, m->ring, pb, k0));
     const unsigned nbp = cell_tiles_per_plane(m);
     const unsigned ncp = unsigned(zc1 - zc0);
     const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
-    S2_LAUNCH(1, ncells, (s2m_cells_mark<<<mg, S2_CW_BLOCK, 0, st>>>(j, pb, m->offx, m->cell_words, m->tile_cnt,
+    S2_LAUNCH(1, ncells, launch_pdl(s2m_cells_mark, mg, S2_CW_BLOCK, 0, st, j, pb, m->offx, m->cell_words, m->tile_cnt,
                                                                     m->tile_cnt + m->cell_tiles,
                                                                     m->tile_cnt + m->cell_tiles + 1, m->slab_ctrl,
-                                                                    m->cand_base, s, zc0, zc1),
-                          cudaGetLastError()));
-    S2_LAUNCH(1, 0, (s2m_cells_emit<<<eg, S2_CW_BLOCK, 0, st>>>(j, m->ring, pruned ? pb.unk : nullptr,
+                                                                    m->cand_base, s, zc0, zc1));
+    S2_LAUNCH(1, 0, launch_pdl(s2m_cells_emit, eg, S2_CW_BLOCK, 0, st, j, m->ring, pruned ? pb.unk : nullptr,
                                                                m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err,
-                                                               zc0),
-                     cudaGetLastError()));
+                                                               zc0));
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
@@ -1101,13 +1121,10 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     unsigned *vperm = reinterpret_cast<unsigned *>(m->vt_buf + m->vt_perm_off);
     if ((e = cudaMemsetAsync(m->vt_buf, 0, m->vt_part_off, st)) != cudaSuccess) return e;
     const unsigned cgrid = unsigned(sms) * 8;
-    S2_LAUNCH(2, 0, (s2m_vtile_count<<<cgrid, 256, 0, st>>>(j, cand, nslabs, tbase, D, nzc, tcnt, rank),
-                     cudaGetLastError()));
-    S2_LAUNCH(2, 0, (s2m_vtile_scan<<<m->vt_blocks, 256, 0, st>>>(tcnt, m->vt_tiles, part, poff, pbase,
-                                                                  tcnt + m->vt_tiles),
-                     cudaGetLastError()));
-    S2_LAUNCH(2, 0, (s2m_vtile_scatter<<<cgrid, 256, 0, st>>>(cand, nslabs, tcnt, poff, rank, vperm),
-                     cudaGetLastError()));
+    S2_LAUNCH(2, 0, launch_pdl(s2m_vtile_count, cgrid, 256, 0, st, j, cand, nslabs, tbase, D, nzc, tcnt, rank));
+    S2_LAUNCH(2, 0, launch_pdl(s2m_vtile_scan, m->vt_blocks, 256, 0, st, tcnt, m->vt_tiles, part, poff, pbase,
+                                                                  tcnt + m->vt_tiles));
+    S2_LAUNCH(2, 0, launch_pdl(s2m_vtile_scatter, cgrid, 256, 0, st, cand, nslabs, tcnt, poff, rank, vperm));
     perm = vperm;
   }
   unsigned long long *vc_base = m->cand_status;
@@ -1117,23 +1134,22 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &vx_chunks};
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   if (m->sdf->prune_words > 0 && !j.qef)  // chunked form: one block per SM (S2_VX_BLOCK threads, 64 registers each)
-    S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(unsigned(sms)), dim3(S2_VX_BLOCK), vargs, S2_VX_SMEM_BYTES,
-                                     st));
+    S2_LAUNCH(2, 0, launch_pdl(kv, dim3(unsigned(sms)), dim3(S2_VX_BLOCK), S2_VX_SMEM_BYTES, st, vargs));
   else
-    S2_LAUNCH(2, 0, cudaLaunchKernel((const void *)kv, dim3(unsigned(sms) * 16), dim3(S2_VX_SMALL), vargs, 0, st));
-  S2_LAUNCH(3, 0, (s2m_vc_scan<<<1, 256, 0, st>>>(cand, nslabs, vc_cnt, vc_off, vc_base, md), cudaGetLastError()));
+    S2_LAUNCH(2, 0, launch_pdl(kv, dim3(unsigned(sms) * 16), dim3(S2_VX_SMALL), 0, st, vargs));
+  S2_LAUNCH(3, 0, launch_pdl(s2m_vc_scan, 1, 256, 0, st, cand, nslabs, vc_cnt, vc_off, vc_base, md));
   const unsigned vc_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->vc_tiles, size_t(sms) * 8)));
-  S2_LAUNCH(3, 0, (s2m_vcompact<<<vc_grid, S2_VC_BLOCK, 0, st>>>(j, cand, md, m->nslabs, vc_off), cudaGetLastError()));
+  S2_LAUNCH(3, 0, launch_pdl(s2m_vcompact, vc_grid, S2_VC_BLOCK, 0, st, j, cand, md, m->nslabs, vc_off));
   const unsigned scan_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->scan_tiles, size_t(sms) * 8)));
-  S2_LAUNCH(4, 0, (s2m_rowscan<<<scan_grid, S2_SCAN_BLOCK, 0, st>>>(md, N * N), cudaGetLastError()));
+  S2_LAUNCH(4, 0, launch_pdl(s2m_rowscan, scan_grid, S2_SCAN_BLOCK, 0, st, md, N * N));
   const unsigned q_grid = unsigned(std::max<size_t>(1, std::min<size_t>(m->quad_tiles, size_t(sms) * 8)));
   unsigned long long *qoff = m->scan_status + m->scan_tiles;  // quad scan words (s2m_quads_find ..)
   unsigned *qcnt = reinterpret_cast<unsigned *>(qoff + m->quad_tiles);
   unsigned long long *qbase = qoff + m->quad_tiles + (m->quad_tiles + 1) / 2;
   unsigned *lk0 = reinterpret_cast<unsigned *>(m->cand_pos), *lk1 = reinterpret_cast<unsigned *>(m->cand_nrm);
-  S2_LAUNCH(5, 0, (s2m_quads_find<<<q_grid, S2_Q_BLOCK, 0, st>>>(j, md, lk0, lk1, qcnt), cudaGetLastError()));
-  S2_LAUNCH(5, 0, (s2m_quads_scan<<<1, 256, 0, st>>>(md, qcnt, qoff, qbase), cudaGetLastError()));
-  S2_LAUNCH(5, 0, (s2m_quads_write<<<q_grid, S2_Q_BLOCK, 0, st>>>(md, lk0, lk1, qoff), cudaGetLastError()));
+  S2_LAUNCH(5, 0, launch_pdl(s2m_quads_find, q_grid, S2_Q_BLOCK, 0, st, j, md, lk0, lk1, qcnt));
+  S2_LAUNCH(5, 0, launch_pdl(s2m_quads_scan, 1, 256, 0, st, md, qcnt, qoff, qbase));
+  S2_LAUNCH(5, 0, launch_pdl(s2m_quads_write, q_grid, S2_Q_BLOCK, 0, st, md, lk0, lk1, qoff));
   return cudaSuccess;
 }
 
@@ -2130,10 +2146,10 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
     if ((e = enqueue(m, st)) != cudaSuccess) break;
     // the part's first non-context row: its row start counts the context plane's vertices
     const unsigned *skip_at = k ? m->rowstart + (unsigned long long)m->quads_from_z * m->N : nullptr;
-    s2m_part_finish<<<unsigned(device_sm_count()) * 4, 256, 0, st>>>(mesh_dev(m), skip_at, m->cand_base + m->nslabs,
-                                                                      k ? tot_d + (k - 1) : nullptr, tot_d + k,
-                                                                      vcap, tcap);
-    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    if ((e = launch_pdl(s2m_part_finish, dim3(unsigned(device_sm_count()) * 4), dim3(256), 0, st, mesh_dev(m), skip_at,
+                        (const unsigned long long *)(m->cand_base + m->nslabs),
+                        (const S2HostTotals *)(k ? tot_d + (k - 1) : nullptr), tot_d + k, vcap, tcap)) != cudaSuccess)
+      break;
     e = cudaEventRecord(done, st);
   }
   const S2HostTotals *tot_h = static_cast<const S2HostTotals *>(totals.p);

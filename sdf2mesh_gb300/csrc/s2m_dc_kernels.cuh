@@ -95,7 +95,10 @@ __device__ __forceinline__ void s2_eval_planes(const S2Job &job, float *__restri
 
 #define S2_EVAL_VARIANT(NAME, MINB, RUN, PAIR)                                                    \
   extern "C" __global__ void __launch_bounds__(S2_EVAL_BLOCK, MINB)                               \
-  NAME(S2Job job, float *__restrict__ ring, int k0, int nk) { s2_eval_planes<RUN, PAIR>(job, ring, k0, nk); }
+  NAME(S2Job job, float *__restrict__ ring, int k0, int nk) {                                        \
+    S2_PDL_WAIT();                                                                                 \
+    s2_eval_planes<RUN, PAIR>(job, ring, k0, nk);                                                  \
+  }
 // Kernel selection: the runtime compiles an SDF's kernels as several NVRTC
 // programs on parallel host threads.  Each program defines S2M_SELECT and the
 // S2M_WANT_* macros of the kernels it holds; a program without S2M_SELECT
@@ -213,6 +216,7 @@ __device__ __forceinline__ unsigned s2_root_flag(const S2Job &job, s2i root) {
 extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long long *__restrict__ cbase, int s_begin,
                  int s_end, int D, int nzc) {
+  S2_PDL_WAIT();
   const unsigned long long b0 = cbase[s_begin];
   const unsigned long long c = b0 + (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
   if (c >= cbase[s_end]) return;
@@ -249,6 +253,7 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
           const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
           const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc,
           unsigned *__restrict__ list, unsigned *__restrict__ list_count) {
+  S2_PDL_WAIT();
   // Thread q takes tile q % 32 (4 x 4 along x, y, by 2 layers along z) of
   // coarse box q / 32, so a warp's tiles share one box's bits and take one
   // path through the interval code.
@@ -484,12 +489,14 @@ __device__ __forceinline__ void s2_eval_pruned_listed(const S2Job &job, float *_
   NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
        int tzs, const unsigned *__restrict__ list, const unsigned *__restrict__ list_count,       \
        unsigned *chunk_ctr) {                                                                     \
+    S2_PDL_WAIT();                                                                                 \
     s2_eval_pruned_listed<RUN4>(job, ring, pb, bits, k0, nk, tzs, list, list_count, chunk_ctr);   \
   }
 #define S2_EVALP_VARIANT(NAME, MINB, RUN4)                                                        \
   extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, MINB)                                 \
   NAME(S2Job job, float *__restrict__ ring, S2PointBits pb, const unsigned *__restrict__ bits, int k0, int nk,  \
        int tzs, int nzt) {                                                                        \
+    S2_PDL_WAIT();                                                                                 \
     s2_eval_pruned<RUN4>(job, ring, pb, bits, k0, nk, tzs, nzt);                                  \
   }
 // Keep this table in step with kEvalVariants in runtime.cu.
@@ -576,6 +583,7 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 extern "C" __global__ void __launch_bounds__(S2_VX_THREADS, S2_VX_MINB)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
              int nzc, const unsigned *perm, unsigned *vc_cnt, unsigned *chunk_ctr) {
+  S2_PDL_WAIT();
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
 #ifdef S2_VX_CHUNKED
   extern __shared__ __align__(16) unsigned char s2_vx_smem[];

@@ -96,6 +96,16 @@ struct S2MeshDev {
   unsigned zq;                    // vertices with label z below zq make no quads (a z part's context plane)
 };
 
+// Programmatic dependent launch: the per-job pipeline launches each kernel so
+// that its blocks may be scheduled while the kernel before it drains; every
+// such kernel waits here, before it reads anything, until that kernel has
+// finished and its writes are visible (a no-op for an ordinary launch).
+#if defined(__CUDA_ARCH__)
+#define S2_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+#else
+#define S2_PDL_WAIT()
+#endif
+
 // Test hooks (S2MeshDev::hold): a flag that nothing sets, so that a bounded
 // device wait runs out and the run reports S2M_E_TIMEOUT.  Only the waiting
 // is affected; every write stays bounds-checked.

@@ -44,6 +44,7 @@ __global__ void __launch_bounds__(256) s2m_part_finish(S2MeshDev mesh, const uns
                                                        const unsigned long long *ncand,
                                                        const S2HostTotals *prev, S2HostTotals *cur,
                                                        unsigned long long hvcap, unsigned long long htcap) {
+  S2_PDL_WAIT();
   const unsigned long long V = *mesh.vtotal, T = *mesh.ntris;
   const unsigned long long skip = skip_at ? (unsigned long long)*skip_at : 0ull;
   const unsigned long long vb = prev ? prev->nverts : 0ull, tb = prev ? prev->ntris : 0ull;
@@ -73,6 +74,7 @@ __global__ void __launch_bounds__(256) s2m_part_finish(S2MeshDev mesh, const uns
 // Off-lattice bit of every cell column x: bit x % 32 of word x / 32 is
 // s2_off_lattice(x + 1).
 __global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict__ offx) {
+  S2_PDL_WAIT();
   const int x = (int)(blockIdx.x * 256u + threadIdx.x);
   const unsigned b = __ballot_sync(S2_FULL, x < job.N && s2_off_lattice(job, x + 1));
   if ((threadIdx.x & 31u) == 0 && x < job.N) offx[x >> 5] = b;
@@ -84,6 +86,7 @@ __global__ void __launch_bounds__(256) s2m_offx(S2Job job, unsigned *__restrict_
 // load and two ballots each).
 __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__restrict__ ring, S2PointBits pb,
                                                       int k0) {
+  S2_PDL_WAIT();
   const int WP = (job.P + 31) >> 5;
   const int slot = (k0 + (int)blockIdx.y) % job.ring;
   const int y = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5);
@@ -115,6 +118,7 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
 __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits pb,
                                                         const unsigned *__restrict__ tiles, int tile_words, int k0,
                                                         int nk, int tzs, unsigned *chunk_reset) {
+  S2_PDL_WAIT();
   // the listed evaluation that follows this launch takes its chunks from zero
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *chunk_reset = 0u;
   const int WP = (job.P + 31) >> 5;
@@ -172,6 +176,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
                                                             unsigned long long *__restrict__ plane_off,
                                                             unsigned long long *base, int slab_index, int zc0,
                                                             int zc1) {
+  S2_PDL_WAIT();
   __shared__ unsigned s_cnt[S2_MARK_PLANES][S2_CW_BLOCK / 32];
   const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5, NW = job.N * WN;
   const int yw = (int)(blockIdx.x * S2_CW_BLOCK + threadIdx.x);
@@ -291,6 +296,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
                                                             const unsigned long long *__restrict__ plane_off,
                                                             const unsigned *__restrict__ tile_cnt, S2Cand cand,
                                                             unsigned *err, int zc0) {
+  S2_PDL_WAIT();
   __shared__ unsigned s_warp[32];
   __shared__ unsigned s_pre[S2_CW_BLOCK / 32];
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
@@ -382,6 +388,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
 __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, int nslabs,
                                                        const unsigned long long *__restrict__ tbase, int D, int nzc,
                                                        unsigned *tcnt, unsigned long long *__restrict__ trank) {
+  S2_PDL_WAIT();
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
   for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < n;
        i += (unsigned long long)gridDim.x * 256u) {
@@ -410,6 +417,7 @@ __global__ void __launch_bounds__(256) s2m_vtile_count(S2Job job, S2Cand cand, i
 __global__ void __launch_bounds__(256) s2m_vtile_scan(unsigned *tcnt, unsigned long long T, unsigned *part_cnt,
                                                       unsigned long long *part_off, unsigned long long *part_base,
                                                       unsigned *done) {
+  S2_PDL_WAIT();
   __shared__ unsigned s_warp[32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const unsigned long long b0 = (unsigned long long)blockIdx.x * S2_VT_TILE + 8ull * tid;
@@ -453,6 +461,7 @@ __global__ void __launch_bounds__(256) s2m_vtile_scatter(S2Cand cand, int nslabs
                                                          const unsigned long long *__restrict__ part_off,
                                                          const unsigned long long *__restrict__ trank,
                                                          unsigned *__restrict__ perm) {
+  S2_PDL_WAIT();
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
   for (unsigned long long i = (unsigned long long)blockIdx.x * 256u + threadIdx.x; i < n;
        i += (unsigned long long)gridDim.x * 256u) {
@@ -471,6 +480,7 @@ __global__ void __launch_bounds__(256) s2m_vtile_scatter(S2Cand cand, int nslabs
 __global__ void __launch_bounds__(256) s2m_vc_scan(S2Cand cand, int nslabs, const unsigned *vc_cnt,
                                                    unsigned long long *vc_off, unsigned long long *vc_base,
                                                    S2MeshDev mesh) {
+  S2_PDL_WAIT();
   const unsigned long long ncand = min(cand.base[nslabs], cand.cap);
   const unsigned ntiles = (unsigned)((ncand + S2_VC_TILE - 1) / S2_VC_TILE);
   s2_scan_tiles<256, 16>(vc_cnt, ntiles, vc_off, vc_base, 0);
@@ -479,6 +489,7 @@ __global__ void __launch_bounds__(256) s2m_vc_scan(S2Cand cand, int nslabs, cons
 
 __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand cand, S2MeshDev mesh, int nslabs,
                                                           const unsigned long long *__restrict__ vc_off) {
+  S2_PDL_WAIT();
   __shared__ unsigned s_warp[32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const unsigned long long ncand = min(cand.base[nslabs], cand.cap);
@@ -540,15 +551,12 @@ __global__ void __launch_bounds__(S2_VC_BLOCK) s2m_vcompact(S2Job job, S2Cand ca
 }
 
 __global__ void __launch_bounds__(S2_SCAN_BLOCK) s2m_rowscan(S2MeshDev mesh, unsigned long long R) {
+  S2_PDL_WAIT();
   s2_rowscan_worker(mesh, R);
 }
 
-__global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads(S2Job job, S2MeshDev mesh, unsigned scan_tiles) {
-  s2_quads_worker<true>(job, mesh, scan_tiles, blockIdx.x == 0);
-}
-
 // Quads of the per-job pipeline in three passes that never wait on one
-// another (the look-back of s2m_quads made every tile's block wait at a
+// another (a look-back over the tiles made every tile's block wait at a
 // barrier while its first warp walked back over tiles still searching):
 //   s2m_quads_find   each vertex's neighbour lookups -- the row searches --
 //                    stored as 6 words per vertex in the candidates' position
@@ -560,10 +568,11 @@ __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads(S2Job job, S2MeshDev mes
 //   s2m_quads_write  each tile's triangles from the stored lookups, at its
 //                    first triangle, in vertex order (mesh.rs:280-321)
 // Tiles of S2_Q_TILE vertices, S2_Q_VPT per thread (v = tile * S2_Q_TILE +
-// m * S2_Q_BLOCK + thread), as s2m_quads; quad scan words: tile offsets
+// m * S2_Q_BLOCK + thread); quad scan words: tile offsets
 // (u64), then tile counts (u32), then the base pair (u64).
 __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_find(S2Job job, S2MeshDev mesh, unsigned *__restrict__ lk0,
                                                            unsigned *__restrict__ lk1, unsigned *__restrict__ tcnt) {
+  S2_PDL_WAIT();
   __shared__ unsigned s_red[S2_Q_BLOCK / 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const unsigned long long V = *mesh.vtotal;
@@ -607,6 +616,7 @@ __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_find(S2Job job, S2MeshDe
 
 __global__ void __launch_bounds__(256) s2m_quads_scan(S2MeshDev mesh, const unsigned *tcnt,
                                                       unsigned long long *toff, unsigned long long *tbase) {
+  S2_PDL_WAIT();
   const unsigned long long V = *mesh.vtotal;
   if (V > mesh.vcap) return;
   const unsigned ntiles = (unsigned)((V + S2_Q_TILE - 1) / S2_Q_TILE);
@@ -617,6 +627,7 @@ __global__ void __launch_bounds__(256) s2m_quads_scan(S2MeshDev mesh, const unsi
 __global__ void __launch_bounds__(S2_Q_BLOCK) s2m_quads_write(S2MeshDev mesh, const unsigned *__restrict__ lk0,
                                                             const unsigned *__restrict__ lk1,
                                                             const unsigned long long *__restrict__ toff) {
+  S2_PDL_WAIT();
   __shared__ unsigned s_warp[32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const unsigned long long V = *mesh.vtotal;
