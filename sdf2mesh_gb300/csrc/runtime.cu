@@ -189,6 +189,7 @@ struct s2m_mesh {
   size_t prune_sbits_off = 0;  // ... to the coarse boxes' activity words
   size_t prune_bits_off = 0;   // ... to the tiles' activity words
   size_t prune_list_off = 0;   // ... to the lists of undecided tiles
+  size_t prune_flags_off = 0;  // ... to the tiles' flags as bytes (s2m_tiles -> classification)
   size_t cell_tiles = 0, vc_tiles = 0, slab_ctrl_words = 0;
   // candidate list of the whole job
   unsigned long long *cand_key = nullptr;
@@ -671,7 +672,10 @@ size_t prune_layout(s2m_mesh *m) {
   m->prune_sbits_off = up16(m->prune_cbase_off + 8 * (size_t(ns) + 1));
   m->prune_bits_off = up16(m->prune_sbits_off + size_t(chunk_coarse) * (words + 1) * 4);  // + each box's flag word
   m->prune_list_off = up16(m->prune_bits_off + size_t(chunk_tiles) * (words + 1) * 4);  // + each tile's flag word
-  return m->prune_list_off + size_t(chunk_tiles) * 4;
+  m->prune_flags_off = up16(m->prune_list_off + size_t(chunk_tiles) * 4);
+  // one byte per tile of the chunk, rows of 4 * WP bytes (one word per 32 lattice points along x)
+  const size_t flag_rows = size_t(chunk_tiles / (unsigned long long)ntx);
+  return m->prune_flags_off + flag_rows * size_t((m->job.P + 31) / 32) * 4;
 }
 template <class T> T *prune_at(const s2m_mesh *m, size_t off) {
   return reinterpret_cast<T *>(reinterpret_cast<char *>(m->prune_buf) + off);
@@ -741,7 +745,10 @@ cudaError_t launch_tiles(const s2m_mesh *m, int s_begin, int s_end, cudaStream_t
   const unsigned long long n = nc * S2_PT_COARSE * S2_PT_COARSE * S2_PT_COARSE_Z;
   unsigned *list = prune_at<unsigned>(m, m->prune_list_off);
   unsigned *counts = prune_list_counts(m);
-  void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc, &list, &counts};
+  unsigned char *tflags = prune_at<unsigned char>(m, m->prune_flags_off);
+  int fpitch = 4 * ((m->job.P + 31) / 32);
+  void *targs[] = {&jj, &bits, &ops, &sbits, &tbase, &cbase, &s_begin, &s_end, &D, &nzc, &list, &counts, &tflags,
+                   &fpitch};
   return launch_pdl(m->sdf->k_tiles, dim3(unsigned((n + S2_PT_BLOCK - 1) / S2_PT_BLOCK)), dim3(S2_PT_BLOCK), 0, st,
                     targs);
 }
@@ -758,9 +765,21 @@ cudaError_t launch_evalp(const s2m_mesh *m, int v, int s, int chunk_begin, cudaS
   if (kEvalVariants[v].listed) {
     const int W1 = m->sdf->prune_words + 1;
     const long long plane_words = (long long)m->job.P * ((m->job.P + 31) / 32);
-    const dim3 fg(unsigned((plane_words + 255) / 256), unsigned(g.nzt));
     unsigned *chunks = jobctl(m).counters + 5;  // set to zero by the fill, taken by the listed evaluation
-    cudaError_t e = launch_pdl(s2m_fill_decided, fg, dim3(256), 0, st, jj, pb, bits, W1, k0, nk, g.tzs, chunks);
+    cudaError_t e;
+    if (!m->job.exact) {
+      // classification by listed tiles (s2m_cells_mark_tiles): the bits of
+      // the slab's last plane in full (the next slab's first plane), the
+      // other planes' decided tiles read from the tile flags; the cell tile
+      // counts cleared
+      const long long ntx = (m->job.P + S2_PT_XY - 1) / S2_PT_XY;
+      const unsigned *lbits = bits + size_t(g.nzt - 1) * size_t(ntx * ntx) * size_t(W1);
+      e = launch_pdl(s2m_fill_decided, dim3(unsigned((plane_words + 255) / 256), 1u), dim3(256), 0, st, jj, pb, lbits,
+                     W1, k0 + nk - 1, 1, 1, chunks, m->tile_cnt, unsigned(m->cell_tiles));
+    } else {  // every cell is classified (s2m_cells_mark): every plane's bits
+      e = launch_pdl(s2m_fill_decided, dim3(unsigned((plane_words + 255) / 256), unsigned(g.nzt)), dim3(256), 0, st,
+                     jj, pb, bits, W1, k0, nk, g.tzs, chunks, static_cast<unsigned *>(nullptr), 0u);
+    }
     if (e != cudaSuccess) return e;
     const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
                            (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(chunk_begin)]);
@@ -796,6 +815,11 @@ unsigned cell_tiles_per_plane(const s2m_mesh *m) {
   return unsigned((size_t(m->N) * WN + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
 }
 size_t cell_word_tiles(const s2m_mesh *m) { return size_t(m->D) * cell_tiles_per_plane(m); }
+// Classification counters (u32): per cell tile its candidates, the finished
+// mark blocks, per cell plane its candidates.
+size_t tile_cnt_words(const s2m_mesh *m) { return m->cell_tiles + 1 + size_t(m->D); }
+unsigned *cls_done(const s2m_mesh *m) { return m->tile_cnt + m->cell_tiles; }
+unsigned *cls_plane_cnt(const s2m_mesh *m) { return m->tile_cnt + m->cell_tiles + 1; }
 
 void drop_graph(s2m_mesh *m) {
   if (m->graph) cudaGraphExecDestroy(m->graph);
@@ -833,7 +857,7 @@ BufPlan plan_buffers(s2m_mesh *m, unsigned long long cand_cap, unsigned long lon
   b.pt_bits = 3 * pt_bits_words(m) * 4;
   b.offx = size_t((j.N + 31) / 32) * 4;
   b.cell_words = m->cell_tiles * S2_CW_BLOCK * 4;
-  b.tile_cnt = (m->cell_tiles + 1 + size_t(m->D)) * 4;  // + the finished-block counter, the plane counts
+  b.tile_cnt = tile_cnt_words(m) * 4;
   const bool prune = m->sdf->k_tiles && m->nslabs > 0;
   b.prune = prune ? prune_layout(m) : 0;
   b.cand_key = m->cand_cap * 8;
@@ -1070,7 +1094,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   }
   // finished-block counter and plane counts of the classification (each slab's
   // last mark block leaves them zero for the next)
-  if ((e = cudaMemsetAsync(m->tile_cnt + m->cell_tiles, 0, (1 + size_t(m->D)) * 4, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(cls_done(m), 0, (1 + size_t(m->D)) * 4, st)) != cudaSuccess) return e;
   S2_LAUNCH(1, 0, launch_pdl(s2m_offx, unsigned((N + 255) / 256), 256, 0, st, j, m->offx));
   const S2PointBits pb = point_bits(m);
   for (int s = 0; s < m->nslabs; ++s) {
@@ -1096,13 +1120,34 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     const unsigned nbp = cell_tiles_per_plane(m);
     const unsigned ncp = unsigned(zc1 - zc0);
     const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
-    S2_LAUNCH(1, ncells, launch_pdl(s2m_cells_mark, mg, S2_CW_BLOCK, 0, st, j, pb, m->offx, m->cell_words, m->tile_cnt,
-                                                                    m->tile_cnt + m->cell_tiles,
-                                                                    m->tile_cnt + m->cell_tiles + 1, m->slab_ctrl,
-                                                                    m->cand_base, s, zc0, zc1));
+    // the listed evaluation (but for S2M_JOB_EXACT_CORNERS) writes no point
+    // bits of decided tiles but those of the slab's last plane: classification
+    // by the slab's listed tiles and the tiles' flags
+    const unsigned *tflags = nullptr;
+    const int tzs = pruned ? prune_geom(j, nk).tzs : 1;
+    if (kEvalVariants[ev].listed && !j.exact) {
+      const int cb = s - s % m->prune_chunk;
+      const unsigned long long ntx = (unsigned long long)((j.P + S2_PT_XY - 1) / S2_PT_XY);
+      tflags = reinterpret_cast<const unsigned *>(
+          prune_at<unsigned char>(m, m->prune_flags_off) +
+          (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(cb)]) / ntx * size_t(4 * ((j.P + 31) / 32)));
+      const unsigned *list = prune_at<unsigned>(m, m->prune_list_off) +
+                             (m->slab_tile_base[size_t(s)] - m->slab_tile_base[size_t(cb)]);
+      const unsigned *count = prune_list_counts(m) + s;
+      const unsigned long long stiles = m->slab_tile_base[size_t(s) + 1] - m->slab_tile_base[size_t(s)];
+      const unsigned mt_grid = unsigned(std::max<unsigned long long>(
+          1, std::min<unsigned long long>((stiles + S2_MT_BLOCK / 32 - 1) / (S2_MT_BLOCK / 32),
+                                          (unsigned long long)sms * 4)));  // resident: 64 registers a thread
+      S2_LAUNCH(1, ncells, launch_pdl(s2m_cells_mark_tiles, mt_grid, S2_MT_BLOCK, 0, st, j, pb, m->offx,
+                                      m->cell_words, m->tile_cnt, cls_done(m), cls_plane_cnt(m), m->slab_ctrl,
+                                      m->cand_base, s, zc0, zc1, tflags, k0, tzs, list, count));
+    } else {
+      S2_LAUNCH(1, ncells, launch_pdl(s2m_cells_mark, mg, S2_CW_BLOCK, 0, st, j, pb, m->offx, m->cell_words,
+                                      m->tile_cnt, cls_done(m), cls_plane_cnt(m), m->slab_ctrl, m->cand_base, s,
+                                      zc0, zc1));
+    }
     S2_LAUNCH(1, 0, launch_pdl(s2m_cells_emit, eg, S2_CW_BLOCK, 0, st, j, m->ring, pruned ? pb.unk : nullptr,
-                                                               m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err,
-                                                               zc0));
+                               m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err, zc0, tflags, k0, tzs));
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
@@ -1860,7 +1905,7 @@ int s2m_mesh_noalloc(const s2m_sdf *sdf, const s2m_params *params, s2m_noalloc_m
   bool ok = carve(base, used, size_t(j.ring) * size_t(j.plane), &m.ring) &&
             carve(base, used, m.slab_ctrl_words, &m.slab_ctrl) &&
             carve(base, used, 3 * pt_bits_words(&m), &m.pt_bits) && carve(base, used, size_t((N + 31) / 32), &m.offx) &&
-            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, m.cell_tiles + 1 + size_t(m.D), &m.tile_cnt) &&
+            carve(base, used, m.cell_tiles * S2_CW_BLOCK, &m.cell_words) && carve(base, used, tile_cnt_words(&m), &m.tile_cnt) &&
             carve(base, used, size_t(m.nslabs + 1), &m.cand_base) &&
             carve(base, used, size_t(N * N), &m.rowcnt) && carve(base, used, size_t(N * N + 1), &m.rowstart) &&
             carve(base, used, size_t(8), &m.jobctl);
@@ -2029,7 +2074,9 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   int rc = setup_job(&probe, err, errlen);
   if (rc != S2M_OK) return rc;
   const int nzc = probe.nzc, lag = probe.job.lag;
-  unsigned K = parts ? parts : (probe.N >= 512 ? 2u : 1u);
+  // automatic count (measured at 1024^3 on the CSG scene: one piece 2.57 ms,
+  // two parts 2.12, three 2.07, four 2.15 per mesh in host memory)
+  unsigned K = parts ? parts : (probe.N >= 1024 ? 3u : probe.N >= 512 ? 2u : 1u);
   K = std::min<unsigned>(K, unsigned(std::max(1, nzc / 16)));  // parts of at least 16 cell planes
   // an SDF's first job tunes its evaluation in one piece
   if (K <= 1 || sdf->eval_variant < 0) return generate_one(sdf, params, stream, out, err, errlen);

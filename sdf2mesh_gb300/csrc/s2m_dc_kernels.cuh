@@ -252,11 +252,13 @@ extern "C" __global__ void __launch_bounds__(S2_PT_BLOCK, 8)
 s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict__ ops,
           const unsigned *__restrict__ sbits, const unsigned long long *__restrict__ tbase,
           const unsigned long long *__restrict__ cbase, int s_begin, int s_end, int D, int nzc,
-          unsigned *__restrict__ list, unsigned *__restrict__ list_count) {
+          unsigned *__restrict__ list, unsigned *__restrict__ list_count, unsigned char *__restrict__ tflags,
+          int fpitch) {
   S2_PDL_WAIT();
-  // Thread q takes tile q % 32 (4 x 4 along x, y, by 2 layers along z) of
-  // coarse box q / 32, so a warp's tiles share one box's bits and take one
-  // path through the interval code.
+  // Thread q takes tile q % kPerBox (S2_PT_COARSE x S2_PT_COARSE along x, y,
+  // by S2_PT_COARSE_Z layers along z: 32 tiles) of coarse box q / kPerBox,
+  // so a warp's tiles share one box's bits and take one path through the
+  // interval code.
   constexpr unsigned kPerBox = S2_PT_COARSE * S2_PT_COARSE * S2_PT_COARSE_Z;
   const unsigned long long b0 = tbase[s_begin];
   const unsigned long long q = (unsigned long long)blockIdx.x * S2_PT_BLOCK + threadIdx.x;
@@ -274,9 +276,9 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
     const long long lc = (long long)(c - cbase[s]);
     const int cx = (int)(lc % ncx);
     const long long r = lc / ncx;
-    tx = cx * S2_PT_COARSE + (int)(sub & 3u);
-    ty = (int)(r % ncx) * S2_PT_COARSE + (int)((sub >> 2) & 3u);
-    tz = (int)(r / ncx) * S2_PT_COARSE_Z + (int)(sub >> 4);
+    tx = cx * S2_PT_COARSE + (int)(sub % S2_PT_COARSE);
+    ty = (int)(r % ncx) * S2_PT_COARSE + (int)((sub / S2_PT_COARSE) % S2_PT_COARSE);
+    tz = (int)(r / ncx) * S2_PT_COARSE_Z + (int)(sub / (S2_PT_COARSE * S2_PT_COARSE));
     live = tx < ntx && ty < ntx && tz < nzt;
   }
   unsigned long long fp_ops = 0, sfu_ops = 0;
@@ -305,6 +307,13 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
 #pragma unroll
     for (int w = 0; w < S2M_PRUNE_WORDS; ++w) dst[w] = m[w];
     dst[S2M_PRUNE_WORDS] = flag;
+    // the flag as a byte, rows of fpitch bytes per (layer, tile row) of the
+    // chunk; bytes past the last tile of a row read S2_TILE_DECIDED (they
+    // cover no cell)
+    unsigned char *frow = tflags + (g - b0) / (unsigned long long)ntx * (unsigned long long)fpitch;
+    frow[tx] = (unsigned char)(flag & (S2_TILE_DECIDED | S2_TILE_POSITIVE));
+    if (tx == ntx - 1)
+      for (int x = ntx; x < fpitch; ++x) frow[x] = (unsigned char)S2_TILE_DECIDED;
     // the slab's list of tiles to evaluate (in any order): one atomic per slab
     // and warp, since every thread of a slab adds to the same counter
     const unsigned am = __activemask();

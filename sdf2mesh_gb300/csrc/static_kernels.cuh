@@ -114,13 +114,21 @@ __global__ void __launch_bounds__(256) s2m_cells_bits(S2Job job, const float *__
 // no values.  One thread per 32-point word of a row (4 tiles along x) and
 // per layer of tiles (tzs planes, nk planes in all), grid (ceil(P * WP /
 // 256), layers): every word of the planes is written, the undecided tiles'
-// bytes as 0, which s2m_evalpl_* overwrites afterwards.
+// bytes as 0, which s2m_evalpl_* overwrites afterwards.  Before
+// s2m_cells_mark_tiles the per-job pipeline fills only a slab's last plane
+// this way, which the next slab's classification reads as its first (within
+// its own planes the classification takes decided tiles' bits from the tile
+// flags), and clears the slab's cell tile counts (zero[0 .. nzero - 1]).
 __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits pb,
                                                         const unsigned *__restrict__ tiles, int tile_words, int k0,
-                                                        int nk, int tzs, unsigned *chunk_reset) {
+                                                        int nk, int tzs, unsigned *chunk_reset, unsigned *zero,
+                                                        unsigned nzero) {
   S2_PDL_WAIT();
   // the listed evaluation that follows this launch takes its chunks from zero
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *chunk_reset = 0u;
+  // and s2m_cells_mark_tiles adds to cleared cell tile counts
+  if (blockIdx.y == 0)
+    for (unsigned i = blockIdx.x * 256u + threadIdx.x; i < nzero; i += gridDim.x * 256u) zero[i] = 0u;
   const int WP = (job.P + 31) >> 5;
   const int q = (int)(blockIdx.x * 256u + threadIdx.x);  // word (y, w) of the plane
   if (q >= job.P * WP) return;
@@ -169,6 +177,19 @@ __global__ void __launch_bounds__(256) s2m_fill_decided(S2Job job, S2PointBits p
 // together; s2m_cells_emit sums the counts before its tile within the plane
 // instead.)
 #define S2_MARK_PLANES 4
+// Sign and near-zero words of one point row's 32 points (lo) and its next
+// point (bit 0 of hi) with the bytes of decided tiles replaced by their flags:
+// f / fn hold the flags of the row's 4 tiles and of the 4 after them, one byte
+// each (bit 0 decided, bit 1 positive).
+__device__ __forceinline__ void s2_decided_bytes(unsigned f, unsigned fn, unsigned &pos_lo, unsigned &pos_hi,
+                                                 unsigned &near_lo, unsigned &near_hi) {
+  const unsigned dm = (f & 0x01010101u) * 0xffu, pm = ((f >> 1) & f & 0x01010101u) * 0xffu;
+  const unsigned dmn = fn & 1u, pmn = (fn >> 1) & fn & 1u;
+  pos_lo = (pos_lo & ~dm) | pm;
+  near_lo &= ~dm;
+  pos_hi = (pos_hi & ~dmn) | pmn;
+  near_hi &= ~dmn;
+}
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2PointBits pb,
                                                             const unsigned *__restrict__ offx,
                                                             unsigned *__restrict__ words, unsigned *tile_cnt,
@@ -280,6 +301,130 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
   if (threadIdx.x == 0) *done = 0u;
 }
 
+// s2m_cells_mark_tiles: classification of a slab by its undecided pruning
+// tiles only (the listed evaluation, not S2M_JOB_EXACT_CORNERS).  A cell lies
+// with all its corners in the box of the tile of its point (x, y, z + 1); when
+// that tile is decided the signs agree on the box and no corner is near zero,
+// so the cell is no candidate.  So only the cells of the slab's listed tiles
+// are classified: a warp per listed tile (from the list the tile pass wrote,
+// whose length is on the device), lane = row (8) by cell plane (4 at a time),
+// each forming the byte of its 8 cells with the word formulas of
+// s2m_cells_mark.  (Two cell planes per lane from three point planes, one
+// round for 8 planes, measured slower.)  Point bits are written only in undecided tiles of the
+// slab's planes (and in full in the plane before them): the bytes of decided
+// tiles read their flags (s2_decided_bytes).  The byte goes to the cell word
+// (byte tx % 4 of word tx / 4); bytes of decided tiles are never written
+// here, and s2m_cells_emit ignores them by the same flags.  Counts: per cell
+// tile of S2_CW_BLOCK words and per cell plane (atomic adds, one per group of
+// lanes of one tile; both zero on entry: s2m_fill_decided clears the tile
+// counts).  The last block to finish scans the plane counts into offsets, as
+// s2m_cells_mark does.
+#define S2_MT_BLOCK 256
+__global__ void __launch_bounds__(S2_MT_BLOCK) s2m_cells_mark_tiles(
+    S2Job job, S2PointBits pb, const unsigned *__restrict__ offx, unsigned *__restrict__ words, unsigned *tile_cnt,
+    unsigned *done, unsigned *plane_cnt, unsigned long long *__restrict__ plane_off, unsigned long long *base,
+    int slab_index, int zc0, int zc1, const unsigned *__restrict__ tflags, int tk0, int tzs,
+    const unsigned *__restrict__ list, const unsigned *__restrict__ list_count) {
+  S2_PDL_WAIT();
+  const int WN = (job.N + 31) >> 5, WP = (job.P + 31) >> 5, NW = job.N * WN;
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  const unsigned nbp = (unsigned)((NW + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
+  const int last = zc1;  // the slab's last lattice plane
+  const unsigned lane = threadIdx.x & 31u;
+  const int r = (int)(lane & 7u), pz = (int)(lane >> 3);
+  const bool nearrule = !job.qef;
+  const unsigned n = __ldg(list_count);
+  const unsigned nwarps = gridDim.x * (S2_MT_BLOCK / 32);
+  unsigned char *wb = reinterpret_cast<unsigned char *>(words);
+#pragma unroll 1
+  for (unsigned i = blockIdx.x * (S2_MT_BLOCK / 32) + (threadIdx.x >> 5); i < n; i += nwarps) {
+    const unsigned t = __ldg(list + i);
+    const int tx = (int)(t % (unsigned)ntx);
+    const unsigned q = t / (unsigned)ntx;
+    const int ty = (int)(q % (unsigned)ntx), tz = (int)(q / (unsigned)ntx);
+    if (tx * S2_PT_XY >= job.N) continue;  // the tile of the last lattice point only: no cell
+    const int kb = tk0 + tz * tzs, ke = min(kb + tzs, last + 1) - 1;
+    const int y = ty * S2_PT_XY + r;
+    const int w = tx >> 2, b = tx & 3;
+    const bool more = w + 1 < WP;
+    const int dw = more ? 1 : 0;
+    const unsigned ox = job.qef ? 0u : __ldg(offx + w);
+    const unsigned oy = (!job.qef && y < job.N && s2_off_lattice(job, y + 1)) ? ~0u : 0u;
+    const unsigned edge = (w == WN - 1 && (job.N & 31)) ? (1u << (job.N & 31)) - 1u : ~0u;
+#pragma unroll 1
+    for (int zb = kb - 1; zb <= ke - 1; zb += 4) {  // the same trips in every lane
+      const int zc = zb + pz;
+      const bool act = zc <= ke - 1 && zc >= zc0 && zc < zc1 && y < job.N;
+      unsigned cb = 0u;
+      if (act) {
+        unsigned andp[2], orp[2], tb[2], tt[2];
+#pragma unroll
+        for (int pp = 0; pp < 2; ++pp) {
+          const int K = zc + pp;
+          const long long rb = ((long long)(K % job.ring) * job.P + y) * WP + w;
+          unsigned pw[4], nw[4];
+          pw[0] = __ldg(pb.pos + rb);
+          pw[1] = __ldg(pb.pos + rb + dw);
+          pw[2] = __ldg(pb.pos + rb + WP);
+          pw[3] = __ldg(pb.pos + rb + WP + dw);
+          nw[0] = nw[1] = nw[2] = nw[3] = 0u;
+          if (nearrule) {
+            nw[0] = __ldg(pb.near + rb);
+            nw[1] = __ldg(pb.near + rb + dw);
+            nw[2] = __ldg(pb.near + rb + WP);
+            nw[3] = __ldg(pb.near + rb + WP + dw);
+          }
+          if (K >= tk0) {
+            const int layer = (K - tk0) / tzs;
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+              const long long fo = ((long long)layer * ntx + ((y + rr) >> 3)) * WP + w;
+              const unsigned f = __ldg(tflags + fo), fn = more ? __ldg(tflags + fo + 1) : 0u;
+              s2_decided_bytes(f, fn, pw[2 * rr], pw[2 * rr + 1], nw[2 * rr], nw[2 * rr + 1]);
+            }
+          }
+          const unsigned p0s = __funnelshift_r(pw[0], more ? pw[1] : 0u, 1);
+          const unsigned p1s = __funnelshift_r(pw[2], more ? pw[3] : 0u, 1);
+          andp[pp] = pw[0] & p0s & pw[2] & p1s;
+          orp[pp] = pw[0] | p0s | pw[2] | p1s;
+          tb[pp] = tt[pp] = 0u;
+          if (nearrule) {
+            const unsigned n0s = __funnelshift_r(nw[0], more ? nw[1] : 0u, 1);
+            const unsigned n1s = __funnelshift_r(nw[2], more ? nw[3] : 0u, 1);
+            const unsigned oz = s2_off_lattice(job, K) ? ~0u : 0u;
+            tb[pp] = (n0s & ox) | (nw[2] & oy) | (n1s & (ox | oy));
+            tt[pp] = (nw[0] & oz) | (n0s & (ox | oz)) | (nw[2] & (oy | oz)) | (n1s & (ox | oy | oz));
+          }
+        }
+        unsigned c = (orp[0] | orp[1]) & ~(andp[0] & andp[1]);
+        if (nearrule) c |= tb[0] | tt[1];
+        cb = ((c & edge) >> (8 * b)) & 0xffu;
+        wb[4 * ((long long)(zc - zc0) * NW + (long long)y * WN + w) + b] = (unsigned char)cb;
+      }
+      const unsigned T = act ? (unsigned)((y * WN + w) / S2_CW_BLOCK) : 0u;
+      const unsigned long long key = act ? ((unsigned long long)(unsigned)(zc - zc0) << 32) | T : ~0ull;
+      const unsigned peers = __match_any_sync(S2_FULL, key);
+      const unsigned sum = __reduce_add_sync(peers, (unsigned)__popc(cb));
+      if (act && sum && lane == (unsigned)(__ffs(peers) - 1)) {
+        atomicAdd(tile_cnt + (unsigned long long)(zc - zc0) * nbp + T, sum);
+        atomicAdd(plane_cnt + (zc - zc0), sum);
+      }
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const unsigned nplanes = (unsigned)(zc1 - zc0);
+  s2_scan_tiles<S2_MT_BLOCK, 4>(plane_cnt, nplanes, plane_off, base, slab_index);
+  __syncthreads();  // every count read before it is cleared for the next slab
+  for (unsigned p = threadIdx.x; p < nplanes; p += S2_MT_BLOCK) plane_cnt[p] = 0u;
+  if (threadIdx.x == 0) *done = 0u;
+}
+
 // The candidates of each tile in order: key (x | y << 16 | z << 32) and the
 // 8 lattice corner values (NaN where the point's unknown-value bit is set: a
 // decided tile of the pruned evaluation wrote no value there).  Grid (nbp,
@@ -289,31 +434,40 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
 // the surface, and a warp's 32 words (a row at N = 1024) a handful, so the
 // block-wide list keeps the threads busy.  The tile's first slot is its
 // plane's offset (s2m_cells_mark) plus the counts of the plane's tiles
-// before it, summed by the block's threads together.
-__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
-                                                            const unsigned *__restrict__ unk,
-                                                            const unsigned *__restrict__ words,
-                                                            const unsigned long long *__restrict__ plane_off,
-                                                            const unsigned *__restrict__ tile_cnt, S2Cand cand,
-                                                            unsigned *err, int zc0) {
-  S2_PDL_WAIT();
+// before it, summed by the block's threads together.  With tflags (after
+// s2m_cells_mark_tiles; tk0 / tzs as there): the bytes of cells in decided
+// tiles are cleared by the tiles' flags, and a corner of the slab's own planes
+// has no value in the ring when its tile is decided (its unknown-value bit
+// says so in the plane before them).
+// One tile (cell plane dz, tile b of nbp in the plane) of s2m_cells_emit.
+__device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__restrict__ ring,
+                                             const unsigned *__restrict__ unk, const unsigned *__restrict__ words,
+                                             const unsigned long long *__restrict__ plane_off,
+                                             const unsigned *__restrict__ tile_cnt, S2Cand cand, unsigned *err,
+                                             int zc0, const unsigned *__restrict__ tflags, int tk0, int tzs,
+                                             unsigned b, int dz, unsigned nbp) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned s_pre[S2_CW_BLOCK / 32];
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const int WN = (job.N + 31) >> 5, NW = job.N * WN;
-  const int yw = (int)(blockIdx.x * S2_CW_BLOCK + tid);
-  const int dz = (int)blockIdx.y;
-  const unsigned *plane_cnt = tile_cnt + (unsigned long long)dz * gridDim.x;
-  if (__ldg(plane_cnt + blockIdx.x) == 0u) return;  // the whole tile: no candidate
-  {
-    unsigned pre = 0u;
-    for (unsigned b = tid; b < blockIdx.x; b += S2_CW_BLOCK) pre += __ldg(plane_cnt + b);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(S2_FULL, pre, o);
-    if (lane == 0) s_pre[warp] = pre;
+  const int WN = (job.N + 31) >> 5, NW = job.N * WN, WP = (job.P + 31) >> 5;
+  const int yw = (int)(b * S2_CW_BLOCK + tid);
+  const unsigned *plane_cnt = tile_cnt + (unsigned long long)dz * nbp;
+  // every load first: the plane's offset, the counts of its tiles before this
+  // one, this thread's word and its tiles' flags
+  const unsigned long long poff = __ldg(plane_off + dz);
+  unsigned pre = 0u;
+  for (unsigned q = tid; q < b; q += S2_CW_BLOCK) pre += __ldg(plane_cnt + q);
+  unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
+  if (tflags && yw < NW) {  // bytes of cells in decided tiles were not written (s2m_cells_mark_tiles)
+    const int y = yw / WN, w = yw - y * WN;
+    const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+    const int layer = (zc0 + dz + 1 - tk0) / tzs;
+    const unsigned f = __ldg(tflags + ((long long)layer * ntx + (y >> 3)) * WP + w);
+    mask &= ~((f & 0x01010101u) * 0xffu);
   }
-  const unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
+  pre = __reduce_add_sync(S2_FULL, pre);
+  if (lane == 0) s_pre[warp] = pre;
   const unsigned cnt = __popc(mask);
   unsigned inc = cnt;
 #pragma unroll
@@ -336,14 +490,13 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     }
   }
   __syncthreads();
-  unsigned long long first = plane_off[dz];
+  unsigned long long first = poff;
 #pragma unroll
   for (int k = 0; k < S2_CW_BLOCK / 32; ++k) first += s_pre[k];
-  const int WP = (job.P + 31) >> 5;
 #pragma unroll 1
   for (unsigned r = tid; r < total; r += S2_CW_BLOCK) {
     const unsigned e = s_list[r];
-    const int ywc = (int)(blockIdx.x * S2_CW_BLOCK + (e >> 5));
+    const int ywc = (int)(b * S2_CW_BLOCK + (e >> 5));
     const int wy = ywc / WN, w = ywc - wy * WN;
     const unsigned bit = e & 31u;
     S2Cell cell;
@@ -359,12 +512,24 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     s2_load_corners<false>(job, ring, cell, v);
     if (unk) {  // corners of decided tiles: no value in the ring
       const bool more = w + 1 < WP;
+      const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+      const unsigned char *fb = reinterpret_cast<const unsigned char *>(tflags);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
-        const long long base = ((long long)((cell.z + (q >> 1)) % job.ring) * job.P + (cell.y + (q & 1))) * WP + w;
-        const unsigned lo = __ldg(unk + base), hi = more ? __ldg(unk + base + 1) : 0u;
-        if ((lo >> bit) & 1u) v[2 * q] = __int_as_float(0x7fc00000);
-        if ((__funnelshift_r(lo, hi, 1) >> bit) & 1u) v[2 * q + 1] = __int_as_float(0x7fc00000);
+        const int Z = cell.z + (q >> 1), Y = cell.y + (q & 1);
+        bool u0, u1;
+        if (tflags && Z >= tk0) {  // the slab's own planes: the flags of the points' tiles
+          const unsigned char *fr = fb + ((long long)((Z - tk0) / tzs) * ntx + (Y >> 3)) * (4 * WP);
+          u0 = __ldg(fr + (cell.x >> 3)) & S2_TILE_DECIDED;
+          u1 = __ldg(fr + ((cell.x + 1) >> 3)) & S2_TILE_DECIDED;
+        } else {  // unknown-value bits (planes written in full)
+          const long long base = ((long long)(Z % job.ring) * job.P + Y) * WP + w;
+          const unsigned lo = __ldg(unk + base), hi = more ? __ldg(unk + base + 1) : 0u;
+          u0 = (lo >> bit) & 1u;
+          u1 = (__funnelshift_r(lo, hi, 1) >> bit) & 1u;
+        }
+        if (u0) v[2 * q] = __int_as_float(0x7fc00000);
+        if (u1) v[2 * q + 1] = __int_as_float(0x7fc00000);
       }
     }
     cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
@@ -372,6 +537,24 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
     dst[1] = make_float4(v[4], v[5], v[6], v[7]);
   }
+}
+
+// Grid (nbp, cell planes), block = tile.  (A list of the non-empty tiles
+// taken by blocks resident on every SM measured slower: the list's order is
+// the atomic order, and the grid's (z, y, x) order keeps neighbouring tiles'
+// corner loads together.)
+__global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
+                                                            const unsigned *__restrict__ unk,
+                                                            const unsigned *__restrict__ words,
+                                                            const unsigned long long *__restrict__ plane_off,
+                                                            const unsigned *__restrict__ tile_cnt, S2Cand cand,
+                                                            unsigned *err, int zc0,
+                                                            const unsigned *__restrict__ tflags, int tk0,
+                                                            int tzs) {
+  S2_PDL_WAIT();
+  if (__ldg(tile_cnt + (unsigned long long)blockIdx.y * gridDim.x + blockIdx.x) == 0u) return;  // no candidate
+  s2_emit_tile(job, ring, unk, words, plane_off, tile_cnt, cand, err, zc0, tflags, tk0, tzs, blockIdx.x,
+               (int)blockIdx.y, gridDim.x);
 }
 
 // Vertex work in tile order (tile pruning).  The vertex kernel evaluates the

@@ -125,3 +125,85 @@ def test_emit_slots_equal_full_scan(N, planes):
             first = plane_off[dz] + cnt[dz, :bx].sum()
             assert first == full[dz, bx]
     assert base + plane_cnt.sum() == base + cnt.sum()
+
+
+def mark_local_word(WN, warp, lane):
+    """s2m_cells_mark's tile-local word of (warp, lane)."""
+    if 4 <= WN <= 256 and WN & (WN - 1) == 0:
+        R = 256 // WN
+        wr = min(8, R)
+        ww = 32 // wr
+        nwg = WN // ww
+        band, wg = warp // nwg, warp % nwg
+        return (band * wr + lane // ww) * WN + wg * ww + lane % ww
+    return warp * 32 + lane
+
+
+@pytest.mark.parametrize("N", [1, 31, 64, 96, 97, 128, 200, 512, 1000, 1024, 2048, 4096, 8192])
+def test_mark_warp_rectangles(N):
+    """Each tile's 256 words are taken once; with WN a power of two from 4 on, a
+    warp's words lie in at most 8 rows of one pruning tile row (rows 8k .. 8k +
+    7 of the lattice) and 32 / (its rows) consecutive words of each."""
+    WN = (N + 31) // 32
+    loc = np.array([[mark_local_word(WN, k, l) for l in range(32)] for k in range(8)])
+    assert sorted(loc.reshape(-1)) == list(range(256))
+    if 4 <= WN <= 256 and WN & (WN - 1) == 0:
+        R = 256 // WN
+        for b in range(3):  # tiles start at row b * R
+            rows = (b * 256 + loc) // WN
+            for k in range(8):
+                assert len(set(rows[k] // 8)) == 1, (N, b, k)
+                assert len(set(rows[k])) == min(8, R)
+
+
+def slab_planes(zb, s, D, nzc):
+    """s2_slab_planes: the first lattice plane and plane count of slab s."""
+    zc0 = zb + s * D
+    zc1 = min(zb + nzc, zc0 + D)
+    k0 = zb if s == 0 else zc0 + 1
+    return zc0, zc1, k0, zc1 - k0 + 1
+
+
+@pytest.mark.parametrize("N,D,zb,nzc", [(64, 64, 0, 64), (100, 37, 0, 100), (33, 10, 5, 20), (1024, 512, 0, 1024)])
+def test_mark_tiles_cover_each_cell_once(N, D, zb, nzc):
+    """s2m_cells_mark_tiles: the warp of tile (tx, ty, tz) writes, lane by lane
+    (row r = lane % 8, cell plane kb - 1 + lane / 8 + 4 j), the byte of cells
+    8 tx .. 8 tx + 7 of each row and plane it covers; over all tiles of a slab
+    every cell of the slab is written exactly once, by the tile of its point
+    (x, y, z + 1) (s2_cell_prune_tile), and reads point planes of the slab's
+    ring only."""
+    P = N + 1
+    ntx = (P + 7) // 8
+    nslabs = (nzc + D - 1) // D
+    rows = range(N) if N <= 100 else range(0, N, 61)  # a sample of rows at 1024
+    for s in range(nslabs):
+        zc0, zc1, k0, nk = slab_planes(zb, s, D, nzc)
+        parts = (nk + 7) // 8
+        tzs = (nk + parts - 1) // parts
+        nzt = (nk + tzs - 1) // tzs
+        seen = {}
+        for tz in range(nzt):
+            kb = k0 + tz * tzs
+            ke = min(kb + tzs, k0 + nk) - 1
+            for ty in range(ntx):
+                for tx in range(ntx):
+                    if 8 * tx >= N:
+                        continue
+                    for lane in range(32):
+                        r, pz = lane & 7, lane >> 3
+                        y = 8 * ty + r
+                        if y not in rows:
+                            continue
+                        for zbb in range(kb - 1, ke, 4):
+                            zc = zbb + pz
+                            if zc <= ke - 1 and zc0 <= zc < zc1 and y < N:
+                                assert zc0 <= zc and zc + 1 <= zc1  # point planes read: zc, zc + 1
+                                key = (zc, y, tx)
+                                assert key not in seen, key
+                                seen[key] = (tx, ty, tz)
+        for zc in range(zc0, zc1):
+            for y in rows:
+                for x in range(0, N, 8):
+                    tz = (zc + 1 - k0) // tzs  # s2_cell_prune_tile
+                    assert seen.get((zc, y, x // 8)) == (x // 8, y // 8, tz), (s, zc, y, x)
+        assert len(seen) == (zc1 - zc0) * len(rows) * ((N + 7) // 8)
