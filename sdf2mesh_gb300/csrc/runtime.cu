@@ -1119,7 +1119,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
       S2_LAUNCH(1, 0, launch_pdl(s2m_cells_bits, dim3(unsigned((j.P + 7) / 8), unsigned(nk)), 256, 0, st, j, m->ring, pb, k0));
     const unsigned nbp = cell_tiles_per_plane(m);
     const unsigned ncp = unsigned(zc1 - zc0);
-    const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, ncp);
+    const dim3 mg(nbp, (ncp + S2_MARK_PLANES - 1) / S2_MARK_PLANES), eg(nbp, (ncp + S2_EMIT_PLANES - 1) / S2_EMIT_PLANES);
     // the listed evaluation (but for S2M_JOB_EXACT_CORNERS) writes no point
     // bits of decided tiles but those of the slab's last plane: classification
     // by the slab's listed tiles and the tiles' flags
@@ -1147,7 +1147,8 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
                                       zc0, zc1));
     }
     S2_LAUNCH(1, 0, launch_pdl(s2m_cells_emit, eg, S2_CW_BLOCK, 0, st, j, m->ring, pruned ? pb.unk : nullptr,
-                               m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err, zc0, tflags, k0, tzs));
+                               m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err, zc0, tflags, k0, tzs,
+                               int(ncp)));
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
@@ -1473,16 +1474,20 @@ cudaStream_t tile_stream() {
   return streams[dev];
 }
 
-// The side stream the z parts' host copies run on (one per device).
-cudaStream_t copy_stream() {
+// The side streams the z parts' host copies run on (kCopyStreams per device:
+// positions, normals and triangles each on their own, so that several copy
+// engines move them at once).
+constexpr int kCopyStreams = 3;
+cudaStream_t copy_stream(int i = 0) {
   static std::mutex mu;
-  static cudaStream_t streams[kNoallocMaxDevices] = {};
+  static cudaStream_t streams[kNoallocMaxDevices][kCopyStreams] = {};
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return nullptr;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices || i < 0 || i >= kCopyStreams)
+    return nullptr;
   std::lock_guard<std::mutex> lock(mu);
-  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
-    streams[dev] = nullptr;
-  return streams[dev];
+  if (!streams[dev][i] && cudaStreamCreateWithFlags(&streams[dev][i], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev][i] = nullptr;
+  return streams[dev][i];
 }
 
 }  // namespace
@@ -2083,8 +2088,8 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   if (probe.job.qef && (rc = ensure_qef_module(sdf, err, errlen)) != S2M_OK) return rc;
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaStream_t side = copy_stream();
-  if (!side) return generate_one(sdf, params, stream, out, err, errlen);
+  cudaStream_t side = copy_stream(0), side_n = copy_stream(1), side_t = copy_stream(2);
+  if (!side || !side_n || !side_t) return generate_one(sdf, params, stream, out, err, errlen);
   std::vector<s2m_mesh *> pm;
   std::vector<cudaEvent_t> ev;
   HostMeshOwner *o = new HostMeshOwner();
@@ -2165,8 +2170,9 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   // The later parts' tile passes (independent of every other part) on a third
   // stream, so that they run beside part 0's kernels; then all parts'
   // kernels (each ending with its copy plan), then, as each part finishes,
-  // its copies on the side stream's copy engine: they run while the later
-  // parts' kernels do.
+  // its copies on the side streams' copy engines (positions, normals and
+  // triangles on one stream each): they run while the later parts' kernels
+  // do.
   cudaError_t e = cudaSuccess;
   std::vector<cudaEvent_t> tev(K, nullptr), pev;
   {
@@ -2210,15 +2216,19 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
       if ((e = cudaMemcpyAsync(hp + 12 * t.vbase, m->pos + 3 * t.vfirst, 12 * t.vcount, cudaMemcpyDeviceToHost,
                                side)) != cudaSuccess ||
           (e = cudaMemcpyAsync(hn + 12 * t.vbase, m->nrm + 3 * t.vfirst, 12 * t.vcount, cudaMemcpyDeviceToHost,
-                               side)) != cudaSuccess)
+                               side_n)) != cudaSuccess)
         break;
     }
     if (t.tcount &&
-        (e = cudaMemcpyAsync(ht + 12 * t.tbase, m->tris, 12 * t.tcount, cudaMemcpyDeviceToHost, side)) != cudaSuccess)
+        (e = cudaMemcpyAsync(ht + 12 * t.tbase, m->tris, 12 * t.tcount, cudaMemcpyDeviceToHost, side_t)) != cudaSuccess)
       break;
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(side);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  // every stream drained before the parts' buffers can be freed, whatever failed
+  for (cudaStream_t q : {side, side_n, side_t, tile_stream(), st}) {
+    if (!q) continue;
+    const cudaError_t es = cudaStreamSynchronize(q);
+    if (e == cudaSuccess) e = es;
+  }
   if (e != cudaSuccess) {
     cleanup();
     set_err(err, errlen, std::string("z parts: ") + cudaGetErrorString(e));

@@ -301,24 +301,82 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_mark(S2Job job, S2Point
   if (threadIdx.x == 0) *done = 0u;
 }
 
+// Sign and near-zero words (lo: the row's 32 points from 32 w, hi: bit 0 =
+// the next point) of lattice row y in the plane at ring slot `slot`, with the
+// bytes of decided tiles taken from their flags when the plane is one of the
+// slab's own (layer >= 0: its layer of tiles).
+struct S2RowBits {
+  unsigned plo, phi, nlo, nhi;
+};
+__device__ __forceinline__ S2RowBits s2_row_bits(const S2Job &job, S2PointBits pb, const unsigned *__restrict__ tflags,
+                                                 int ntx, int WP, int slot, int layer, int y, int w, bool more,
+                                                 bool nearrule) {
+  const long long rb = ((long long)slot * job.P + y) * WP + w;
+  S2RowBits r;
+  r.plo = __ldg(pb.pos + rb);
+  r.phi = more ? __ldg(pb.pos + rb + 1) : 0u;
+  r.nlo = nearrule ? __ldg(pb.near + rb) : 0u;
+  r.nhi = (nearrule && more) ? __ldg(pb.near + rb + 1) : 0u;
+  if (layer >= 0) {
+    const long long fo = ((long long)layer * ntx + (y >> 3)) * WP + w;
+    const unsigned f = __ldg(tflags + fo), fn = more ? __ldg(tflags + fo + 1) : 0u;
+    s2_decided_bytes(f, fn, r.plo, r.phi, r.nlo, r.nhi);
+  }
+  return r;
+}
+__device__ __forceinline__ S2RowBits s2_shfl_row(S2RowBits v, int src) {
+  S2RowBits r;
+  r.plo = __shfl_sync(S2_FULL, v.plo, src);
+  r.phi = __shfl_sync(S2_FULL, v.phi, src);
+  r.nlo = __shfl_sync(S2_FULL, v.nlo, src);
+  r.nhi = __shfl_sync(S2_FULL, v.nhi, src);
+  return r;
+}
+// The terms of a point plane for the 32 cells of a word (as s2m_cells_mark):
+// AND / OR of the 4 corner words, near-zero corners counting as a cell's
+// bottom (tb) or top (tt) plane; rows a (y) and c (y + 1), oz the plane's
+// off-lattice mask.
+struct S2PlaneTerms {
+  unsigned andp, orp, tb, tt;
+};
+__device__ __forceinline__ S2PlaneTerms s2_plane_terms(S2RowBits a, S2RowBits c, bool more, unsigned ox, unsigned oy,
+                                                      unsigned oz, bool nearrule) {
+  S2PlaneTerms t;
+  const unsigned p0s = __funnelshift_r(a.plo, more ? a.phi : 0u, 1);
+  const unsigned p1s = __funnelshift_r(c.plo, more ? c.phi : 0u, 1);
+  t.andp = a.plo & p0s & c.plo & p1s;
+  t.orp = a.plo | p0s | c.plo | p1s;
+  t.tb = t.tt = 0u;
+  if (nearrule) {
+    const unsigned n0s = __funnelshift_r(a.nlo, more ? a.nhi : 0u, 1);
+    const unsigned n1s = __funnelshift_r(c.nlo, more ? c.nhi : 0u, 1);
+    t.tb = (n0s & ox) | (c.nlo & oy) | (n1s & (ox | oy));
+    t.tt = (a.nlo & oz) | (n0s & (ox | oz)) | (c.nlo & (oy | oz)) | (n1s & (ox | oy | oz));
+  }
+  return t;
+}
+
 // s2m_cells_mark_tiles: classification of a slab by its undecided pruning
 // tiles only (the listed evaluation, not S2M_JOB_EXACT_CORNERS).  A cell lies
 // with all its corners in the box of the tile of its point (x, y, z + 1); when
 // that tile is decided the signs agree on the box and no corner is near zero,
 // so the cell is no candidate.  So only the cells of the slab's listed tiles
 // are classified: a warp per listed tile (from the list the tile pass wrote,
-// whose length is on the device), lane = row (8) by cell plane (4 at a time),
-// each forming the byte of its 8 cells with the word formulas of
-// s2m_cells_mark.  (Two cell planes per lane from three point planes, one
-// round for 8 planes, measured slower.)  Point bits are written only in undecided tiles of the
-// slab's planes (and in full in the plane before them): the bytes of decided
-// tiles read their flags (s2_decided_bytes).  The byte goes to the cell word
-// (byte tx % 4 of word tx / 4); bytes of decided tiles are never written
-// here, and s2m_cells_emit ignores them by the same flags.  Counts: per cell
-// tile of S2_CW_BLOCK words and per cell plane (atomic adds, one per group of
-// lanes of one tile; both zero on entry: s2m_fill_decided clears the tile
-// counts).  The last block to finish scans the plane counts into offsets, as
-// s2m_cells_mark does.
+// whose length is on the device), lane = row r (8) by cell plane (4 at a
+// time), each forming the byte of its 8 cells with the word formulas of
+// s2m_cells_mark.  A lane loads the point row of its own row and lower plane;
+// the row above and the plane above come from the neighbouring lanes
+// (shuffles), so each point row is loaded once per warp: a tile's rows are
+// whole words apart, and loading every corner row in every lane made the
+// kernel bound by L1 sectors.  Point bits are written only in undecided
+// tiles of the slab's planes (and in full in the plane before them): the
+// bytes of decided tiles read their flags (s2_decided_bytes).  The byte goes
+// to the cell word (byte tx % 4 of word tx / 4); bytes of decided tiles are
+// never written here, and s2m_cells_emit ignores them by the same flags.
+// Counts: per cell tile of S2_CW_BLOCK words and per cell plane (atomic
+// adds, one per group of lanes of one tile; both zero on entry:
+// s2m_fill_decided clears the tile counts).  The last block to finish scans
+// the plane counts into offsets, as s2m_cells_mark does.
 #define S2_MT_BLOCK 256
 __global__ void __launch_bounds__(S2_MT_BLOCK) s2m_cells_mark_tiles(
     S2Job job, S2PointBits pb, const unsigned *__restrict__ offx, unsigned *__restrict__ words, unsigned *tile_cnt,
@@ -330,6 +388,7 @@ __global__ void __launch_bounds__(S2_MT_BLOCK) s2m_cells_mark_tiles(
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const unsigned nbp = (unsigned)((NW + S2_CW_BLOCK - 1) / S2_CW_BLOCK);
   const int last = zc1;  // the slab's last lattice plane
+  const int slot0 = zc0 % job.ring;
   const unsigned lane = threadIdx.x & 31u;
   const int r = (int)(lane & 7u), pz = (int)(lane >> 3);
   const bool nearrule = !job.qef;
@@ -345,59 +404,48 @@ __global__ void __launch_bounds__(S2_MT_BLOCK) s2m_cells_mark_tiles(
     if (tx * S2_PT_XY >= job.N) continue;  // the tile of the last lattice point only: no cell
     const int kb = tk0 + tz * tzs, ke = min(kb + tzs, last + 1) - 1;
     const int y = ty * S2_PT_XY + r;
+    const int ya = min(y, job.N), yc = min(y + 1, job.N);  // lattice rows (past the last: unused)
     const int w = tx >> 2, b = tx & 3;
     const bool more = w + 1 < WP;
-    const int dw = more ? 1 : 0;
     const unsigned ox = job.qef ? 0u : __ldg(offx + w);
     const unsigned oy = (!job.qef && y < job.N && s2_off_lattice(job, y + 1)) ? ~0u : 0u;
     const unsigned edge = (w == WN - 1 && (job.N & 31)) ? (1u << (job.N & 31)) - 1u : ~0u;
 #pragma unroll 1
     for (int zb = kb - 1; zb <= ke - 1; zb += 4) {  // the same trips in every lane
-      const int zc = zb + pz;
+      const int zc = zb + pz;  // this lane's cell plane: point planes zc, zc + 1
+      const int K0 = min(max(zc, zc0), last), K1 = min(max(zc + 1, zc0), last);  // outside: unused
+      // ring slots (the slab's planes zc0 .. last hold consecutive slots from
+      // slot0, wrapping) and tile layers (K0, K1 lie in kb - 1 .. ke: this
+      // tile's layer or the one below; -1 before the slab's first plane)
+      const int s0 = slot0 + (K0 - zc0), s1 = slot0 + (K1 - zc0);
+      const int slotK0 = s0 >= job.ring ? s0 - job.ring : s0, slotK1 = s1 >= job.ring ? s1 - job.ring : s1;
+      const int lay0 = K0 < tk0 ? -1 : (K0 >= kb ? tz : tz - 1), lay1 = K1 < tk0 ? -1 : (K1 >= kb ? tz : tz - 1);
+      // own row and plane; the row above in row 7, the plane above in plane 3
+      const S2RowBits A = s2_row_bits(job, pb, tflags, ntx, WP, slotK0, lay0, ya, w, more, nearrule);
+      S2RowBits C = A, B = A, Dd = A;
+      if (r == 7) C = s2_row_bits(job, pb, tflags, ntx, WP, slotK0, lay0, yc, w, more, nearrule);
+      if (pz == 3) B = s2_row_bits(job, pb, tflags, ntx, WP, slotK1, lay1, ya, w, more, nearrule);
+      if (r == 7 && pz == 3) Dd = s2_row_bits(job, pb, tflags, ntx, WP, slotK1, lay1, yc, w, more, nearrule);
+      const int up = r < 7 ? (int)lane + 1 : (int)lane;  // lane of row y + 1, same plane
+      const S2RowBits A1 = s2_shfl_row(A, up), B1 = s2_shfl_row(B, up);
+      const S2RowBits rowc0 = r < 7 ? A1 : C;   // plane zc, row y + 1
+      const S2RowBits rowc1 = r < 7 ? B1 : Dd;  // plane zc + 1, row y + 1 (lanes of plane 3)
+      const unsigned oz0 = (!job.qef && s2_off_lattice(job, K0)) ? ~0u : 0u;
+      const unsigned oz1 = (!job.qef && s2_off_lattice(job, K1)) ? ~0u : 0u;
+      const S2PlaneTerms T0 = s2_plane_terms(A, rowc0, more, ox, oy, oz0, nearrule);
+      const S2PlaneTerms T3 = s2_plane_terms(B, rowc1, more, ox, oy, oz1, nearrule);  // used in plane 3's lanes
+      const int nxt = pz < 3 ? (int)lane + 8 : (int)lane;  // lane of plane zc + 1, same row
+      S2PlaneTerms T1;
+      T1.andp = __shfl_sync(S2_FULL, T0.andp, nxt);
+      T1.orp = __shfl_sync(S2_FULL, T0.orp, nxt);
+      T1.tb = __shfl_sync(S2_FULL, T0.tb, nxt);
+      T1.tt = __shfl_sync(S2_FULL, T0.tt, nxt);
+      if (pz == 3) T1 = T3;
       const bool act = zc <= ke - 1 && zc >= zc0 && zc < zc1 && y < job.N;
       unsigned cb = 0u;
       if (act) {
-        unsigned andp[2], orp[2], tb[2], tt[2];
-#pragma unroll
-        for (int pp = 0; pp < 2; ++pp) {
-          const int K = zc + pp;
-          const long long rb = ((long long)(K % job.ring) * job.P + y) * WP + w;
-          unsigned pw[4], nw[4];
-          pw[0] = __ldg(pb.pos + rb);
-          pw[1] = __ldg(pb.pos + rb + dw);
-          pw[2] = __ldg(pb.pos + rb + WP);
-          pw[3] = __ldg(pb.pos + rb + WP + dw);
-          nw[0] = nw[1] = nw[2] = nw[3] = 0u;
-          if (nearrule) {
-            nw[0] = __ldg(pb.near + rb);
-            nw[1] = __ldg(pb.near + rb + dw);
-            nw[2] = __ldg(pb.near + rb + WP);
-            nw[3] = __ldg(pb.near + rb + WP + dw);
-          }
-          if (K >= tk0) {
-            const int layer = (K - tk0) / tzs;
-#pragma unroll
-            for (int rr = 0; rr < 2; ++rr) {
-              const long long fo = ((long long)layer * ntx + ((y + rr) >> 3)) * WP + w;
-              const unsigned f = __ldg(tflags + fo), fn = more ? __ldg(tflags + fo + 1) : 0u;
-              s2_decided_bytes(f, fn, pw[2 * rr], pw[2 * rr + 1], nw[2 * rr], nw[2 * rr + 1]);
-            }
-          }
-          const unsigned p0s = __funnelshift_r(pw[0], more ? pw[1] : 0u, 1);
-          const unsigned p1s = __funnelshift_r(pw[2], more ? pw[3] : 0u, 1);
-          andp[pp] = pw[0] & p0s & pw[2] & p1s;
-          orp[pp] = pw[0] | p0s | pw[2] | p1s;
-          tb[pp] = tt[pp] = 0u;
-          if (nearrule) {
-            const unsigned n0s = __funnelshift_r(nw[0], more ? nw[1] : 0u, 1);
-            const unsigned n1s = __funnelshift_r(nw[2], more ? nw[3] : 0u, 1);
-            const unsigned oz = s2_off_lattice(job, K) ? ~0u : 0u;
-            tb[pp] = (n0s & ox) | (nw[2] & oy) | (n1s & (ox | oy));
-            tt[pp] = (nw[0] & oz) | (n0s & (ox | oz)) | (nw[2] & (oy | oz)) | (n1s & (ox | oy | oz));
-          }
-        }
-        unsigned c = (orp[0] | orp[1]) & ~(andp[0] & andp[1]);
-        if (nearrule) c |= tb[0] | tt[1];
+        unsigned c = (T0.orp | T1.orp) & ~(T0.andp & T1.andp);
+        if (nearrule) c |= T0.tb | T1.tt;
         cb = ((c & edge) >> (8 * b)) & 0xffu;
         wb[4 * ((long long)(zc - zc0) * NW + (long long)y * WN + w) + b] = (unsigned char)cb;
       }
@@ -440,6 +488,8 @@ __global__ void __launch_bounds__(S2_MT_BLOCK) s2m_cells_mark_tiles(
 // has no value in the ring when its tile is decided (its unknown-value bit
 // says so in the plane before them).
 // One tile (cell plane dz, tile b of nbp in the plane) of s2m_cells_emit.
+// Everything that depends on the plane alone (ring slots, flag rows, the
+// division by the words per row) is formed once per block.
 __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__restrict__ ring,
                                              const unsigned *__restrict__ unk, const unsigned *__restrict__ words,
                                              const unsigned long long *__restrict__ plane_off,
@@ -451,8 +501,24 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const int WN = (job.N + 31) >> 5, NW = job.N * WN, WP = (job.P + 31) >> 5;
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
+  // word index -> (row, word): division by WN (>= 2) with a reciprocal
+  const unsigned magic_wn = WN > 1 ? (unsigned)(0x100000000ull / (unsigned)WN) + 1u : 0u;
   const int yw = (int)(b * S2_CW_BLOCK + tid);
   const unsigned *plane_cnt = tile_cnt + (unsigned long long)dz * nbp;
+  const int Z0 = zc0 + dz;  // the cells' lower lattice plane; the upper one is Z0 + 1
+  const float *rz[2];
+  const unsigned *uz[2];
+  const unsigned char *fz[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int Z = Z0 + h;
+    rz[h] = ring + (long long)(Z % job.ring) * job.plane;
+    uz[h] = unk ? unk + (long long)(Z % job.ring) * job.P * WP : nullptr;
+    fz[h] = (tflags && Z >= tk0)
+                ? reinterpret_cast<const unsigned char *>(tflags) + (long long)((Z - tk0) / tzs) * ntx * (4 * WP)
+                : nullptr;
+  }
   // every load first: the plane's offset, the counts of its tiles before this
   // one, this thread's word and its tiles' flags
   const unsigned long long poff = __ldg(plane_off + dz);
@@ -460,9 +526,8 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
   for (unsigned q = tid; q < b; q += S2_CW_BLOCK) pre += __ldg(plane_cnt + q);
   unsigned mask = yw < NW ? words[(long long)dz * NW + yw] : 0u;
   if (tflags && yw < NW) {  // bytes of cells in decided tiles were not written (s2m_cells_mark_tiles)
-    const int y = yw / WN, w = yw - y * WN;
-    const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-    const int layer = (zc0 + dz + 1 - tk0) / tzs;
+    const int y = WN > 1 ? (int)s2_udiv((unsigned)yw, (unsigned)WN, magic_wn) : yw, w = yw - y * WN;
+    const int layer = (Z0 + 1 - tk0) / tzs;
     const unsigned f = __ldg(tflags + ((long long)layer * ntx + (y >> 3)) * WP + w);
     mask &= ~((f & 0x01010101u) * 0xffu);
   }
@@ -496,35 +561,37 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
 #pragma unroll 1
   for (unsigned r = tid; r < total; r += S2_CW_BLOCK) {
     const unsigned e = s_list[r];
-    const int ywc = (int)(b * S2_CW_BLOCK + (e >> 5));
-    const int wy = ywc / WN, w = ywc - wy * WN;
+    const unsigned ywc = b * S2_CW_BLOCK + (e >> 5);
+    const int wy = WN > 1 ? (int)s2_udiv(ywc, (unsigned)WN, magic_wn) : (int)ywc, w = (int)ywc - wy * WN;
     const unsigned bit = e & 31u;
-    S2Cell cell;
-    cell.x = 32 * w + (int)bit;
-    cell.y = wy;
-    cell.z = zc0 + dz;
+    const int x = 32 * w + (int)bit;
     const unsigned long long o = first + r;
     if (o >= cand.cap) {
       atomicOr(err, S2_ERR_CAND_OVF);
       continue;
     }
     float v[8];
-    s2_load_corners<false>(job, ring, cell, v);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {  // corner k = bx | by << 1 | bz << 2
+      const float *p = rz[h] + (long long)wy * job.pitch + x;
+      v[4 * h + 0] = __ldg(p);
+      v[4 * h + 1] = __ldg(p + 1);
+      v[4 * h + 2] = __ldg(p + job.pitch);
+      v[4 * h + 3] = __ldg(p + job.pitch + 1);
+    }
     if (unk) {  // corners of decided tiles: no value in the ring
       const bool more = w + 1 < WP;
-      const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-      const unsigned char *fb = reinterpret_cast<const unsigned char *>(tflags);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // corner k = 2 q + bx lies in point row q = by | bz << 1
-        const int Z = cell.z + (q >> 1), Y = cell.y + (q & 1);
+        const int h = q >> 1, Y = wy + (q & 1);
         bool u0, u1;
-        if (tflags && Z >= tk0) {  // the slab's own planes: the flags of the points' tiles
-          const unsigned char *fr = fb + ((long long)((Z - tk0) / tzs) * ntx + (Y >> 3)) * (4 * WP);
-          u0 = __ldg(fr + (cell.x >> 3)) & S2_TILE_DECIDED;
-          u1 = __ldg(fr + ((cell.x + 1) >> 3)) & S2_TILE_DECIDED;
+        if (fz[h]) {  // the slab's own planes: the flags of the points' tiles
+          const unsigned char *fr = fz[h] + (long long)(Y >> 3) * (4 * WP);
+          u0 = __ldg(fr + (x >> 3)) & S2_TILE_DECIDED;
+          u1 = __ldg(fr + ((x + 1) >> 3)) & S2_TILE_DECIDED;
         } else {  // unknown-value bits (planes written in full)
-          const long long base = ((long long)(Z % job.ring) * job.P + Y) * WP + w;
-          const unsigned lo = __ldg(unk + base), hi = more ? __ldg(unk + base + 1) : 0u;
+          const unsigned *ur = uz[h] + (long long)Y * WP + w;
+          const unsigned lo = __ldg(ur), hi = more ? __ldg(ur + 1) : 0u;
           u0 = (lo >> bit) & 1u;
           u1 = (__funnelshift_r(lo, hi, 1) >> bit) & 1u;
         }
@@ -532,29 +599,41 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
         if (u1) v[2 * q + 1] = __int_as_float(0x7fc00000);
       }
     }
-    cand.key[o] = (unsigned long long)cell.x | ((unsigned long long)cell.y << 16) | ((unsigned long long)cell.z << 32);
+    cand.key[o] = (unsigned long long)x | ((unsigned long long)wy << 16) | ((unsigned long long)Z0 << 32);
     float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
     dst[1] = make_float4(v[4], v[5], v[6], v[7]);
   }
 }
 
-// Grid (nbp, cell planes), block = tile.  (A list of the non-empty tiles
-// taken by blocks resident on every SM measured slower: the list's order is
-// the atomic order, and the grid's (z, y, x) order keeps neighbouring tiles'
-// corner loads together.)
+// Grid (nbp, ceil(cell planes / S2_EMIT_PLANES)): a block takes the tile at
+// the same place in S2_EMIT_PLANES consecutive planes (the upper corners of
+// one plane's cells are the lower corners of the next plane's), skipping those
+// without candidates.  (Measured slower: a list of the non-empty tiles taken
+// by blocks resident on every SM, since the list's order is the atomic order
+// and (z, y, x) order keeps neighbouring tiles' corner loads together; one
+// warp per tile, since a warp alone drains a dense tile's candidates long
+// after the others.)
+#define S2_EMIT_PLANES 2
 __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const float *__restrict__ ring,
                                                             const unsigned *__restrict__ unk,
                                                             const unsigned *__restrict__ words,
                                                             const unsigned long long *__restrict__ plane_off,
                                                             const unsigned *__restrict__ tile_cnt, S2Cand cand,
                                                             unsigned *err, int zc0,
-                                                            const unsigned *__restrict__ tflags, int tk0,
-                                                            int tzs) {
+                                                            const unsigned *__restrict__ tflags, int tk0, int tzs,
+                                                            int planes) {
   S2_PDL_WAIT();
-  if (__ldg(tile_cnt + (unsigned long long)blockIdx.y * gridDim.x + blockIdx.x) == 0u) return;  // no candidate
-  s2_emit_tile(job, ring, unk, words, plane_off, tile_cnt, cand, err, zc0, tflags, tk0, tzs, blockIdx.x,
-               (int)blockIdx.y, gridDim.x);
+  const int dz0 = (int)blockIdx.y * S2_EMIT_PLANES;
+#pragma unroll 1
+  for (int i = 0; i < S2_EMIT_PLANES; ++i) {
+    const int dz = dz0 + i;
+    if (dz >= planes) break;
+    if (__ldg(tile_cnt + (unsigned long long)dz * gridDim.x + blockIdx.x) == 0u) continue;  // no candidate
+    __syncthreads();  // the previous tile's shared lists are read
+    s2_emit_tile(job, ring, unk, words, plane_off, tile_cnt, cand, err, zc0, tflags, tk0, tzs, blockIdx.x, dz,
+                 gridDim.x);
+  }
 }
 
 // Vertex work in tile order (tile pruning).  The vertex kernel evaluates the

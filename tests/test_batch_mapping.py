@@ -207,3 +207,72 @@ def test_mark_tiles_cover_each_cell_once(N, D, zb, nzc):
                     tz = (zc + 1 - k0) // tzs  # s2_cell_prune_tile
                     assert seen.get((zc, y, x // 8)) == (x // 8, y // 8, tz), (s, zc, y, x)
         assert len(seen) == (zc1 - zc0) * len(rows) * ((N + 7) // 8)
+
+
+@pytest.mark.parametrize("N,zc0,zc1,kb,ke", [(64, 0, 64, 0, 7), (64, 9, 30, 10, 17), (100, 0, 100, 96, 100),
+                                             (37, 5, 12, 6, 12)])
+def test_mark_tiles_rows_from_neighbour_lanes(N, zc0, zc1, kb, ke):
+    """s2m_cells_mark_tiles loads, in lane (r, pz), point row min(y, N) of plane
+    K0 = clamp(zc) (A), plus row min(y + 1, N) in lanes r = 7 (C), plane K1 =
+    clamp(zc + 1) in lanes pz = 3 (B), both in lane (7, 3) (D); the row above
+    comes from lane + 1 for r < 7 and the plane above's terms from lane + 8
+    for pz < 3.  For every active lane the rows it combines are exactly
+    (zc, y), (zc, y + 1), (zc + 1, y), (zc + 1, y + 1)."""
+    last = zc1
+    for ty in range((N + 7) // 8 + 1):
+        for zb in range(kb - 1, ke, 4):
+            A, B, C, D, act, need = {}, {}, {}, {}, {}, {}
+            for lane in range(32):
+                r, pz = lane & 7, lane >> 3
+                y = 8 * ty + r
+                zc = zb + pz
+                K0, K1 = min(max(zc, zc0), last), min(max(zc + 1, zc0), last)
+                ya, yc = min(y, N), min(y + 1, N)
+                A[lane] = (K0, ya)
+                C[lane] = (K0, yc) if r == 7 else A[lane]
+                B[lane] = (K1, ya) if pz == 3 else A[lane]
+                D[lane] = (K1, yc) if (r == 7 and pz == 3) else A[lane]
+                act[lane] = zc <= ke - 1 and zc0 <= zc < zc1 and y < N
+                need[lane] = {(zc, y), (zc, y + 1), (zc + 1, y), (zc + 1, y + 1)}
+            for lane in range(32):
+                if not act[lane]:
+                    continue
+                r, pz = lane & 7, lane >> 3
+                up = lane + 1 if r < 7 else lane
+                rowc0 = A[up] if r < 7 else C[lane]
+                rowc1 = B[up] if r < 7 else D[lane]
+                # plane zc's terms: rows A, rowc0; plane zc + 1's: from lane + 8 (its A and its rowc0) or B, rowc1
+                if pz < 3:
+                    n8 = lane + 8
+                    up8 = n8 + 1 if r < 7 else n8
+                    t1 = {A[n8], A[up8] if r < 7 else C[n8]}
+                else:
+                    t1 = {B[lane], rowc1}
+                assert {A[lane], rowc0} | t1 == need[lane], (lane, ty, zb)
+                for K, yy in need[lane]:
+                    assert zc0 <= K <= last and yy <= N
+
+
+@pytest.mark.parametrize("nk,zc0_first", [(513, True), (512, False), (9, False), (3, True), (100, False)])
+def test_mark_tiles_layers_and_slots(nk, zc0_first):
+    """s2m_cells_mark_tiles forms a point plane's tile layer and ring slot
+    without dividing: K in kb - 1 .. ke of tile layer tz lies in layer tz when
+    K >= kb, tz - 1 below (none before the slab's first plane tk0), and the
+    slab's planes zc0 .. last take consecutive ring slots from zc0 % ring."""
+    parts = (nk + 7) // 8
+    tzs = (nk + parts - 1) // parts
+    nzt = (nk + tzs - 1) // tzs
+    for ring in (nk + 1, nk + 5, 2 * nk + 3):
+        for tk0 in (0, 7, 1000):
+            zc0 = tk0 if zc0_first else tk0 - 1
+            last = tk0 + nk - 1
+            slot0 = zc0 % ring
+            for K in range(zc0, last + 1):
+                s = slot0 + (K - zc0)
+                assert (s - ring if s >= ring else s) == K % ring
+            for tz in range(nzt):
+                kb = tk0 + tz * tzs
+                ke = min(kb + tzs, tk0 + nk) - 1
+                for K in range(max(kb - 1, zc0), ke + 1):
+                    lay = -1 if K < tk0 else (tz if K >= kb else tz - 1)
+                    assert lay == (-1 if K < tk0 else (K - tk0) // tzs), (K, tz)
