@@ -575,14 +575,16 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   // kDeepSlabNsPerPoint or more, which then runs deep slabs as below.  An SDF with a tile form: the pruned evaluation writes the
   // point bits itself and classification reads only those (and the
   // candidates' corners), so the ring need not fit in L2; deep slabs (a ring
-  // of up to 4 GB, slabs of equal depth) amortise each slab's evaluation
+  // of up to 4.6 GB, slabs of equal depth) amortise each slab's evaluation
   // tail, where its last heavy tiles run at low occupancy (a 1024^3 CSG job:
-  // 16.3 ms with 10-plane slabs, 7.9 ms with 512).
+  // 16.3 ms with 10-plane slabs, 7.9 ms with 512).  A job in one slab (1024^3
+  // and its z parts) keeps its whole lattice resident, and the vertex kernel
+  // reads the candidates' corners from it.
   int D = int(p.slab_depth);
   if (D <= 0) {
     const double plane_bytes = double(j.plane) * 4.0;
     if (m->sdf && (m->sdf->k_tiles || m->sdf->deep_slabs)) {
-      const int dmax = std::max(1, int(std::min(4.0e9 / plane_bytes, 1.0e9)) - 1);
+      const int dmax = std::max(1, int(std::min(4.6e9 / plane_bytes, 1.0e9)) - 1);
       const int nz = std::max(1, m->nzc);
       const int ns = (nz + dmax - 1) / dmax;
       D = (nz + ns - 1) / ns;
@@ -1088,6 +1090,10 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   m->eval_points = 0;
   m->eval_fp_ops = m->eval_sfu_ops = 0;
   const bool tiles_ready = pruned && m->tiles_ready && m->prune_chunk >= m->nslabs;
+  // one slab with the listed evaluation: the ring keeps the job's whole
+  // lattice, so the candidates carry no corner values and the vertex kernel
+  // reads them from the ring (decided tiles' points by their flags)
+  const bool resident = pruned && kEvalVariants[ev].listed && !j.exact && !j.qef && m->nslabs == 1 && m->prune_buf;
   if (pruned && !tiles_ready) {  // operation counters and the slabs' list lengths
     cudaError_t e0 = cudaMemsetAsync(m->prune_buf, 0, m->prune_base_off, st);
     if (e0 != cudaSuccess) return e0;
@@ -1148,7 +1154,7 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
     }
     S2_LAUNCH(1, 0, launch_pdl(s2m_cells_emit, eg, S2_CW_BLOCK, 0, st, j, m->ring, pruned ? pb.unk : nullptr,
                                m->cell_words, m->slab_ctrl, m->tile_cnt, cand, c.err, zc0, tflags, k0, tzs,
-                               int(ncp)));
+                               int(ncp), resident ? 0 : 1));
   }
   S2Job jj = j;
   int nslabs = m->nslabs;
@@ -1177,7 +1183,13 @@ cudaError_t enqueue(s2m_mesh *m, cudaStream_t st) {
   unsigned *vc_cnt = reinterpret_cast<unsigned *>(m->cand_status + 2);
   unsigned long long *vc_off = m->cand_status + vc_ctrl_offsets(m->vc_tiles);
   unsigned *vx_chunks = c.counters + 4;  // zeroed with jobctl at the start of the job
-  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &vx_chunks};
+  const float *vring = resident ? m->ring : nullptr;
+  const unsigned char *vflags = resident ? prune_at<unsigned char>(m, m->prune_flags_off) : nullptr;
+  int vk0 = 0, vnk = 0;
+  if (m->nslabs > 0) slab_planes(m, 0, vk0, vnk);
+  int vtzs = resident ? prune_geom(j, vnk).tzs : 1;
+  void *vargs[] = {&jj, &cand, &nslabs, &tbits, &tbase, &D, &nzc, &perm, &vc_cnt, &vx_chunks, &vring, &vflags, &vk0,
+                   &vtzs};
   const cudaKernel_t kv = j.qef ? m->sdf->k_vertices_qef : m->sdf->k_vertices;
   if (m->sdf->prune_words > 0 && !j.qef)  // chunked form: one block per SM (S2_VX_BLOCK threads, 64 registers each)
     S2_LAUNCH(2, 0, launch_pdl(kv, dim3(unsigned(sms)), dim3(S2_VX_BLOCK), S2_VX_SMEM_BYTES, st, vargs));

@@ -560,6 +560,33 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
                               s2_coord(job, c.z + ((k >> 2) & 1)));
 }
 
+// The 8 lattice corners of cell c from a ring that holds every plane of the
+// job (one slab), NaN where the point lies in a decided tile of the pruned
+// evaluation (its value was never written): tflags holds the tiles' flags as
+// bytes, rows of 4 * ceil(P / 32) bytes per (layer, tile row), layers of tzs
+// planes from tk0, as the tile pass writes them.
+__device__ __forceinline__ void s2_ring_corners(const S2Job &job, const float *__restrict__ ring,
+                                                const unsigned char *__restrict__ tflags, int tk0, int tzs, S2Cell c,
+                                                float v[8]) {
+  const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY, fpitch = 4 * ((job.P + 31) >> 5);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int Z = c.z + h;
+    const float *p = ring + (long long)(Z % job.ring) * job.plane + (long long)c.y * job.pitch + c.x;
+    const unsigned char *fr = tflags + (long long)((Z - tk0) / tzs) * ntx * fpitch;
+#pragma unroll
+    for (int by = 0; by < 2; ++by) {
+      const unsigned char *f = fr + (long long)((c.y + by) >> 3) * fpitch;
+#pragma unroll
+      for (int bx = 0; bx < 2; ++bx) {
+        const float x = __ldg(p + by * job.pitch + bx);
+        const bool unknown = __ldg(f + ((c.x + bx) >> 3)) & S2_TILE_DECIDED;
+        v[4 * h + 2 * by + bx] = unknown ? __int_as_float(0x7fc00000) : x;
+      }
+    }
+  }
+}
+
 // Vertices of every candidate of the job, one candidate per thread (dense:
 // candidates are a small fraction of the cells).  Rewrites cand.key with the
 // final key and writes cand.pos / cand.nrm for cells with a vertex.  With
@@ -591,7 +618,8 @@ __device__ __forceinline__ void s2_fill_unknown_corners(const S2Job &job, S2Cell
 #if !defined(S2M_SELECT) || defined(S2M_WANT_VERTICES)
 extern "C" __global__ void __launch_bounds__(S2_VX_THREADS, S2_VX_MINB)
 s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const unsigned long long *tbase, int D,
-             int nzc, const unsigned *perm, unsigned *vc_cnt, unsigned *chunk_ctr) {
+             int nzc, const unsigned *perm, unsigned *vc_cnt, unsigned *chunk_ctr, const float *__restrict__ ring,
+             const unsigned char *__restrict__ tflags, int tk0, int tzs) {
   S2_PDL_WAIT();
   const unsigned long long n = min(cand.base[nslabs], cand.cap);
 #ifdef S2_VX_CHUNKED
@@ -629,9 +657,13 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
     c.z = (int)((k >> 32) & 0xffffull);
     float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (active) {
-      const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
-      const float4 a = src[0], b = src[1];
-      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+      if (ring) {  // the job's lattice is resident: corners from the ring, NaN in decided tiles
+        s2_ring_corners(job, ring, tflags, tk0, tzs, c, v);
+      } else {
+        const float4 *src = reinterpret_cast<const float4 *>(cand.val + 8 * o);
+        const float4 a = src[0], b = src[1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+      }
 #ifndef S2M_QEF_MODULE
       if (!S2UserSdfCall::kStdNormal)  // s2_vertex_warp evaluates unknown corners with its requests
 #endif

@@ -495,7 +495,7 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
                                              const unsigned long long *__restrict__ plane_off,
                                              const unsigned *__restrict__ tile_cnt, S2Cand cand, unsigned *err,
                                              int zc0, const unsigned *__restrict__ tflags, int tk0, int tzs,
-                                             unsigned b, int dz, unsigned nbp) {
+                                             unsigned b, int dz, unsigned nbp, bool vals) {
   __shared__ unsigned s_warp[32];
   __shared__ unsigned s_pre[S2_CW_BLOCK / 32];
   __shared__ unsigned short s_list[S2_CW_BLOCK * 32];
@@ -570,6 +570,8 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
       atomicOr(err, S2_ERR_CAND_OVF);
       continue;
     }
+    cand.key[o] = (unsigned long long)x | ((unsigned long long)wy << 16) | ((unsigned long long)Z0 << 32);
+    if (!vals) continue;  // the vertex kernel reads the corners from the resident ring
     float v[8];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {  // corner k = bx | by << 1 | bz << 2
@@ -599,7 +601,6 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
         if (u1) v[2 * q + 1] = __int_as_float(0x7fc00000);
       }
     }
-    cand.key[o] = (unsigned long long)x | ((unsigned long long)wy << 16) | ((unsigned long long)Z0 << 32);
     float4 *dst = reinterpret_cast<float4 *>(cand.val + 8 * o);
     dst[0] = make_float4(v[0], v[1], v[2], v[3]);
     dst[1] = make_float4(v[4], v[5], v[6], v[7]);
@@ -609,9 +610,11 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
 // Grid (nbp, ceil(cell planes / S2_EMIT_PLANES)): a block takes the tile at
 // the same place in S2_EMIT_PLANES consecutive planes (the upper corners of
 // one plane's cells are the lower corners of the next plane's), skipping those
-// without candidates.  (Measured slower: a list of the non-empty tiles taken
-// by blocks resident on every SM, since the list's order is the atomic order
-// and (z, y, x) order keeps neighbouring tiles' corner loads together; one
+// without candidates.  vals = 0: keys only (the vertex kernel reads the
+// corners from a ring that holds the whole job).  (Measured slower: a list of
+// the non-empty tiles taken by blocks resident on every SM, since the list's
+// order is the atomic order and (z, y, x) order keeps neighbouring tiles'
+// corner loads together; one
 // warp per tile, since a warp alone drains a dense tile's candidates long
 // after the others.)
 #define S2_EMIT_PLANES 2
@@ -622,7 +625,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
                                                             const unsigned *__restrict__ tile_cnt, S2Cand cand,
                                                             unsigned *err, int zc0,
                                                             const unsigned *__restrict__ tflags, int tk0, int tzs,
-                                                            int planes) {
+                                                            int planes, int vals) {
   S2_PDL_WAIT();
   const int dz0 = (int)blockIdx.y * S2_EMIT_PLANES;
 #pragma unroll 1
@@ -632,7 +635,7 @@ __global__ void __launch_bounds__(S2_CW_BLOCK) s2m_cells_emit(S2Job job, const f
     if (__ldg(tile_cnt + (unsigned long long)dz * gridDim.x + blockIdx.x) == 0u) continue;  // no candidate
     __syncthreads();  // the previous tile's shared lists are read
     s2_emit_tile(job, ring, unk, words, plane_off, tile_cnt, cand, err, zc0, tflags, tk0, tzs, blockIdx.x, dz,
-                 gridDim.x);
+                 gridDim.x, vals != 0);
   }
 }
 
