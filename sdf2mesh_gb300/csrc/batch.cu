@@ -896,6 +896,10 @@ int s2m_batch_add_csg(s2m_batch *b, const float *program, uint32_t len, const s2
   j.qef = (params->flags & S2M_JOB_QEF) ? 1 : 0;
   j.magic_n = uint32_t((1ull << 32) / uint64_t(j.N) + 1);
   j.magic_p = uint32_t((1ull << 32) / uint64_t(j.P) + 1);
+  {
+    const uint64_t wn = (uint64_t(j.N) + 31) / 32;
+    j.magic_wn = wn >= 2 ? uint32_t((1ull << 32) / wn + 1) : 0u;
+  }
   h.nzc = j.lag ? int(N) - 1 : int(N);
   const unsigned long long n3 = (unsigned long long)N * N * N, n2 = (unsigned long long)N * N;
   h.cand_cap = std::min(n3, std::max<unsigned long long>(4096, 8 * n2));

@@ -557,6 +557,10 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
   j.qef = (p.flags & S2M_JOB_QEF) ? 1 : 0;
   j.magic_n = uint32_t((1ull << 32) / uint64_t(j.N) + 1);
   j.magic_p = uint32_t((1ull << 32) / uint64_t(j.P) + 1);
+  {
+    const uint64_t wn = (uint64_t(j.N) + 31) / 32;
+    j.magic_wn = wn >= 2 ? uint32_t((1ull << 32) / wn + 1) : 0u;
+  }
   // cell planes of the job: the whole lattice, or the part zpart_begin ..
   // zpart_end - 1 (s2m_mesh_generate's z parts)
   const int full_nzc = j.lag ? int(N) - 1 : int(N);
@@ -567,7 +571,6 @@ int setup_job(s2m_mesh *m, char *err, size_t errlen) {
     j.zb = 0;
     m->nzc = full_nzc;
   }
-  j.pad = 0;
   m->zfrac = full_nzc > 0 ? double(m->nzc) / double(full_nzc) : 1.0;
   // Slab depth.  Full evaluation: the ring of D + 1 lattice planes is sized
   // to stay resident in the 126 MB L2 between the evaluation and the point
@@ -1486,20 +1489,19 @@ cudaStream_t tile_stream() {
   return streams[dev];
 }
 
-// The side streams the z parts' host copies run on (kCopyStreams per device:
-// positions, normals and triangles each on their own, so that several copy
-// engines move them at once).
-constexpr int kCopyStreams = 3;
-cudaStream_t copy_stream(int i = 0) {
+// The side stream the z parts' host copies run on (one per device).  (Three
+// streams, one per array, moved nothing faster: device-to-host copies into
+// pinned memory top out near 190 GB/s here, by one copy engine, several, or
+// SM stores into mapped memory alike.)
+cudaStream_t copy_stream() {
   static std::mutex mu;
-  static cudaStream_t streams[kNoallocMaxDevices][kCopyStreams] = {};
+  static cudaStream_t streams[kNoallocMaxDevices] = {};
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices || i < 0 || i >= kCopyStreams)
-    return nullptr;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return nullptr;
   std::lock_guard<std::mutex> lock(mu);
-  if (!streams[dev][i] && cudaStreamCreateWithFlags(&streams[dev][i], cudaStreamNonBlocking) != cudaSuccess)
-    streams[dev][i] = nullptr;
-  return streams[dev][i];
+  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev] = nullptr;
+  return streams[dev];
 }
 
 }  // namespace
@@ -2100,8 +2102,8 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   if (probe.job.qef && (rc = ensure_qef_module(sdf, err, errlen)) != S2M_OK) return rc;
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaStream_t side = copy_stream(0), side_n = copy_stream(1), side_t = copy_stream(2);
-  if (!side || !side_n || !side_t) return generate_one(sdf, params, stream, out, err, errlen);
+  cudaStream_t side = copy_stream();
+  if (!side) return generate_one(sdf, params, stream, out, err, errlen);
   std::vector<s2m_mesh *> pm;
   std::vector<cudaEvent_t> ev;
   HostMeshOwner *o = new HostMeshOwner();
@@ -2182,9 +2184,8 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
   // The later parts' tile passes (independent of every other part) on a third
   // stream, so that they run beside part 0's kernels; then all parts'
   // kernels (each ending with its copy plan), then, as each part finishes,
-  // its copies on the side streams' copy engines (positions, normals and
-  // triangles on one stream each): they run while the later parts' kernels
-  // do.
+  // its copies on the side stream's copy engine: they run while the later
+  // parts' kernels do.
   cudaError_t e = cudaSuccess;
   std::vector<cudaEvent_t> tev(K, nullptr), pev;
   {
@@ -2228,15 +2229,15 @@ int s2m_mesh_generate(const s2m_sdf *sdf, const s2m_params *params, uint32_t par
       if ((e = cudaMemcpyAsync(hp + 12 * t.vbase, m->pos + 3 * t.vfirst, 12 * t.vcount, cudaMemcpyDeviceToHost,
                                side)) != cudaSuccess ||
           (e = cudaMemcpyAsync(hn + 12 * t.vbase, m->nrm + 3 * t.vfirst, 12 * t.vcount, cudaMemcpyDeviceToHost,
-                               side_n)) != cudaSuccess)
+                               side)) != cudaSuccess)
         break;
     }
     if (t.tcount &&
-        (e = cudaMemcpyAsync(ht + 12 * t.tbase, m->tris, 12 * t.tcount, cudaMemcpyDeviceToHost, side_t)) != cudaSuccess)
+        (e = cudaMemcpyAsync(ht + 12 * t.tbase, m->tris, 12 * t.tcount, cudaMemcpyDeviceToHost, side)) != cudaSuccess)
       break;
   }
   // every stream drained before the parts' buffers can be freed, whatever failed
-  for (cudaStream_t q : {side, side_n, side_t, tile_stream(), st}) {
+  for (cudaStream_t q : {side, tile_stream(), st}) {
     if (!q) continue;
     const cudaError_t es = cudaStreamSynchronize(q);
     if (e == cudaSuccess) e = es;

@@ -25,7 +25,7 @@ struct S2Job {
   unsigned magic_n;        // floor(2^32 / N) + 1: division by N of 32-bit indices
   unsigned magic_p;        // floor(2^32 / P) + 1
   int zb;                  // first cell plane of the job's z range (0: the whole lattice)
-  int pad;
+  unsigned magic_wn;       // floor(2^32 / WN) + 1 (WN = ceil(N / 32) >= 2; else 0): division by WN
 };
 
 // Division of a 32-bit index by d (2 <= d < 2^31) with the precomputed

@@ -502,22 +502,26 @@ __device__ __forceinline__ void s2_emit_tile(const S2Job &job, const float *__re
   const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const int WN = (job.N + 31) >> 5, NW = job.N * WN, WP = (job.P + 31) >> 5;
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
-  // word index -> (row, word): division by WN (>= 2) with a reciprocal
-  const unsigned magic_wn = WN > 1 ? (unsigned)(0x100000000ull / (unsigned)WN) + 1u : 0u;
+  const unsigned magic_wn = job.magic_wn;  // word index -> (row, word): division by WN (>= 2)
   const int yw = (int)(b * S2_CW_BLOCK + tid);
   const unsigned *plane_cnt = tile_cnt + (unsigned long long)dz * nbp;
   const int Z0 = zc0 + dz;  // the cells' lower lattice plane; the upper one is Z0 + 1
-  const float *rz[2];
-  const unsigned *uz[2];
-  const unsigned char *fz[2];
+  // the planes' ring slots and flag rows (for the corner values only)
+  const float *rz[2] = {ring, ring};
+  const unsigned *uz[2] = {unk, unk};
+  const unsigned char *fz[2] = {nullptr, nullptr};
+  if (vals) {
+    const int s0 = Z0 % job.ring, s1 = s0 + 1 == job.ring ? 0 : s0 + 1;
+    const int sl[2] = {s0, s1};
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int Z = Z0 + h;
-    rz[h] = ring + (long long)(Z % job.ring) * job.plane;
-    uz[h] = unk ? unk + (long long)(Z % job.ring) * job.P * WP : nullptr;
-    fz[h] = (tflags && Z >= tk0)
-                ? reinterpret_cast<const unsigned char *>(tflags) + (long long)((Z - tk0) / tzs) * ntx * (4 * WP)
-                : nullptr;
+    for (int h = 0; h < 2; ++h) {
+      const int Z = Z0 + h;
+      rz[h] = ring + (long long)sl[h] * job.plane;
+      uz[h] = unk ? unk + (long long)sl[h] * job.P * WP : nullptr;
+      fz[h] = (tflags && Z >= tk0)
+                  ? reinterpret_cast<const unsigned char *>(tflags) + (long long)((Z - tk0) / tzs) * ntx * (4 * WP)
+                  : nullptr;
+    }
   }
   // every load first: the plane's offset, the counts of its tiles before this
   // one, this thread's word and its tiles' flags
