@@ -144,13 +144,26 @@ struct S2PruneTile {
 // records get NaN for such corners, and the vertex kernel evaluates those
 // exactly, so the mesh does not change.
 #define S2M_TILE_WORDS (S2M_PRUNE_WORDS + 1)
+// v = (c * n + b) * n + a with a, b < n: (a, b, c), in 32-bit arithmetic when
+// v fits (a 64-bit division is a long instruction sequence).
+__device__ __forceinline__ void s2_split3(long long v, int n, int &a, int &b, int &c) {
+  if (v >= 0 && v < 0x100000000ll) {
+    const unsigned u = (unsigned)v, un = (unsigned)n, q = u / un;
+    a = (int)(u - q * un);
+    b = (int)(q % un);
+    c = (int)(q / un);
+  } else {
+    a = (int)(v % n);
+    const long long q = v / n;
+    b = (int)(q % n);
+    c = (int)(q / n);
+  }
+}
 __device__ __forceinline__ S2PruneTile s2_prune_tile(const S2Job &job, long long t, int k0, int nk, int tzs) {
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   S2PruneTile r;
-  const int tx = (int)(t % ntx);
-  const long long q = t / ntx;
-  const int ty = (int)(q % ntx);
-  const int tz = (int)(q / ntx);
+  int tx, ty, tz;
+  s2_split3(t, ntx, tx, ty, tz);
   r.i0 = tx * S2_PT_XY;
   r.i1 = min(r.i0 + S2_PT_XY, job.P) - 1;
   r.j0 = ty * S2_PT_XY;
@@ -226,11 +239,8 @@ s2m_tiles_coarse(S2Job job, unsigned *__restrict__ sbits, const unsigned long lo
   const int tzs = s2_tile_depth(nk);
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY;
   const int ncx = (ntx + S2_PT_COARSE - 1) / S2_PT_COARSE;
-  const long long lc = (long long)(c - cbase[s]);
-  const int cx = (int)(lc % ncx);
-  const long long q = lc / ncx;
-  const int cy = (int)(q % ncx);
-  const int cz = (int)(q / ncx);
+  int cx, cy, cz;
+  s2_split3((long long)(c - cbase[s]), ncx, cx, cy, cz);
   const int span = S2_PT_XY * S2_PT_COARSE;
   const int i0 = cx * span, i1 = min(i0 + span, job.P) - 1;
   const int j0 = cy * span, j1 = min(j0 + span, job.P) - 1;
@@ -273,12 +283,11 @@ s2m_tiles(S2Job job, unsigned *__restrict__ bits, unsigned long long *__restrict
     int k0s, nks;
     s2_slab_planes(job, s, D, nzc, k0s, nks);
     const int tzs = s2_tile_depth(nks), nzt = (nks + tzs - 1) / tzs;
-    const long long lc = (long long)(c - cbase[s]);
-    const int cx = (int)(lc % ncx);
-    const long long r = lc / ncx;
+    int cx, cy, cz;
+    s2_split3((long long)(c - cbase[s]), ncx, cx, cy, cz);
     tx = cx * S2_PT_COARSE + (int)(sub % S2_PT_COARSE);
-    ty = (int)(r % ncx) * S2_PT_COARSE + (int)((sub / S2_PT_COARSE) % S2_PT_COARSE);
-    tz = (int)(r / ncx) * S2_PT_COARSE_Z + (int)(sub / (S2_PT_COARSE * S2_PT_COARSE));
+    ty = cy * S2_PT_COARSE + (int)((sub / S2_PT_COARSE) % S2_PT_COARSE);
+    tz = cz * S2_PT_COARSE_Z + (int)(sub / (S2_PT_COARSE * S2_PT_COARSE));
     live = tx < ntx && ty < ntx && tz < nzt;
   }
   unsigned long long fp_ops = 0, sfu_ops = 0;
