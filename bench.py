@@ -261,15 +261,17 @@ def phase_traffic():
     return out
 
 
-def phase_bytes(phase, N, C, V, T, pruned):
+def phase_bytes(phase, N, C, V, T, pruned, resident=False):
     """Algorithmic DRAM bytes of one job's phase (what it must read and write at
     least): 2 point bits (sign, near-zero) per lattice point for classification
     (plus the 4-byte values when the lattice is materialised), 8-byte keys and
-    32 bytes of corner values per candidate, 28 bytes per vertex (position,
-    normal, cell key), 12 bytes per triangle."""
+    32 bytes of corner values per candidate (read and written by classification
+    unless the lattice stays resident for the vertex kernel, which then reads
+    them), 28 bytes per vertex (position, normal, cell key), 12 bytes per
+    triangle."""
     P3 = float(N + 1) ** 3
     if phase == "cells":
-        return 2.0 * P3 / 8.0 + (0.0 if pruned else 4.0 * P3) + C * (8 + 32) + C * 32
+        return 2.0 * P3 / 8.0 + (0.0 if pruned else 4.0 * P3) + C * 8 + (0.0 if resident else C * (32 + 32))
     if phase == "vertices":
         return C * (8 + 32) + C * (8 + 24)
     if phase == "vcompact":
@@ -464,13 +466,15 @@ def dominant_roofline(s2m, sp, sdf, r, N, steps, pk, pk_kind, traffic_per_job=No
     dom = max(ms, key=lambda k: ms[k])
     C, V, T = float(r["info"].candidate_cells), float(r["nverts"]), float(r["ntris"])
     pruned = bool(r["eval_ops"]["pruned"])
+    # one slab with the listed evaluation: the lattice stays resident for the vertex kernel
+    resident = pruned and "evalpl" in sdf.eval_variant()[0] and int(r["info"].slab_depth) >= N - 1
     if dom == "eval_planes":
         roof = eval_roofline(s2m, sp, sdf, r, steps)
     else:
         nl = max(1, prof["launches"][dom])
         per_launch_ms = ms[dom] / nl
         launches_per_job = nl / steps
-        b = phase_bytes(dom, N, C, V, T, pruned) / launches_per_job
+        b = phase_bytes(dom, N, C, V, T, pruned, resident) / launches_per_job
         achieved = b / (per_launch_ms * 1e-3) / 1e9
         tr = (traffic_per_job or {}).get(dom)
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -484,7 +488,7 @@ def dominant_roofline(s2m, sp, sdf, r, N, steps, pk, pk_kind, traffic_per_job=No
     roof["dominant_by_time"] = dom
     # contouring as a whole (every phase after the evaluation), per 8(d)
     cont_ms = sum(ms[k] for k in ms if k != "eval_planes") / steps
-    cont_b = sum(phase_bytes(k, N, C, V, T, pruned) for k in ("cells", "vertices", "vcompact", "rowscan", "quads"))
+    cont_b = sum(phase_bytes(k, N, C, V, T, pruned, resident) for k in ("cells", "vertices", "vcompact", "rowscan", "quads"))
     return roof, {"bound": "hbm", "ms_per_job": cont_ms, "bytes_per_job": cont_b,
                   "achieved": cont_b / (cont_ms * 1e-3) / 1e9 if cont_ms > 0 else None, "peak": pk["hbm_gbs"],
                   "unit": "GB/s", "frac": (cont_b / (cont_ms * 1e-3) / 1e9) / pk["hbm_gbs"] if cont_ms > 0 else None,

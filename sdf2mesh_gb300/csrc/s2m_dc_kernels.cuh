@@ -607,10 +607,12 @@ __device__ __forceinline__ void s2_ring_corners(const S2Job &job, const float *_
 // counts the vertices of candidates t * S2_VC_TILE .. (t + 1) * S2_VC_TILE -
 // 1 (for s2m_vc_scan).
 //   Modules with a pruning form (reference rule): one block of S2_VX_BLOCK
-// threads per SM takes chunks of S2_VX_BLOCK consecutive candidates (in tile
-// order) from `chunk_ctr` (zero at launch), one warp-sized run per warp:
-// every warp on an SM then evaluates neighbouring tiles, whose pruned paths
-// share code.  (With 8 blocks of 128 threads per SM, each taking runs a grid
+// threads per SM takes chunks of S2_VX_CHUNK consecutive candidates (in tile
+// order) from `chunk_ctr` (zero at launch), and its warps take the chunk's
+// warp-sized runs from a shared counter as they come free: every warp on an
+// SM evaluates neighbouring tiles, whose pruned paths share code, and a warp
+// with cheap candidates does not wait at a barrier for one with costly ones
+// (one run per warp and chunk left the warps stalled at the chunk's barrier).  (With 8 blocks of 128 threads per SM, each taking runs a grid
 // stride apart, the SM's warps ran 32 different places of the pruned SDF and
 // stalled on instruction fetch.)  Dynamic shared memory: S2_VX_SMEM_BYTES.
 // Other modules (full SDF; precision mode, whose per-lane QEF work varies
@@ -618,6 +620,7 @@ __device__ __forceinline__ void s2_ring_corners(const S2Job &job, const float *_
 // striding over the runs.
 #if defined(S2M_HAS_PRUNE) && !defined(S2M_QEF_MODULE)
 #define S2_VX_CHUNKED 1
+#define S2_VX_CHUNK (4 * S2_VX_BLOCK)
 #define S2_VX_THREADS S2_VX_BLOCK
 #define S2_VX_MINB 1
 #else
@@ -639,14 +642,24 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
       reinterpret_cast<const unsigned **>(s2_vx_smem + sizeof(S2WarpScratch) * (S2_VX_BLOCK / 32));
   S2UserSdfPruned psdf;
   psdf.mp = s_mp;
-  const unsigned long long nchunks = (n + S2_VX_BLOCK - 1) / S2_VX_BLOCK;
+  __shared__ unsigned s_run;
+  constexpr unsigned kRuns = S2_VX_CHUNK / 32;
+  const unsigned long long nchunks = (n + S2_VX_CHUNK - 1) / S2_VX_CHUNK;
   for (;;) {
-    __syncthreads();  // every thread has read the previous chunk's number
-    if (threadIdx.x == 0) s_chunk = atomicAdd(chunk_ctr, 1u);
+    __syncthreads();  // every thread has read the previous chunk's number and left its runs
+    if (threadIdx.x == 0) {
+      s_chunk = atomicAdd(chunk_ctr, 1u);
+      s_run = 0u;
+    }
     __syncthreads();
     const unsigned long long chunk = s_chunk;
     if (chunk >= nchunks) break;
-    const unsigned long long base = chunk * S2_VX_BLOCK + (threadIdx.x & ~31u);
+   for (;;) {  // the chunk's warp-sized runs, taken by whichever warp is free
+    unsigned run = 0u;
+    if ((threadIdx.x & 31u) == 0u) run = atomicAdd(&s_run, 1u);
+    run = __shfl_sync(0xffffffffu, run, 0);
+    if (run >= kRuns) break;
+    const unsigned long long base = chunk * S2_VX_CHUNK + 32ull * run;
 #else
   __shared__ S2WarpScratch s_ws[S2_VX_SMALL / 32];
   (void)tbits; (void)tbase; (void)D; (void)nzc; (void)chunk_ctr;
@@ -712,5 +725,8 @@ s2m_vertices(S2Job job, S2Cand cand, int nslabs, const unsigned *tbits, const un
       cand.nrm[3 * o + 2] = nrm[2];
     }
   }
+#ifdef S2_VX_CHUNKED
+  }
+#endif
 }
 #endif  // S2M_WANT_VERTICES
