@@ -578,20 +578,31 @@ __device__ __forceinline__ void s2_ring_corners(const S2Job &job, const float *_
                                                 const unsigned char *__restrict__ tflags, int tk0, int tzs, S2Cell c,
                                                 float v[8]) {
   const int ntx = (job.P + S2_PT_XY - 1) / S2_PT_XY, fpitch = 4 * ((job.P + 31) >> 5);
+  // ring slots and tile layers of planes z and z + 1 (one modulo, one division)
+  const int s0 = c.z % job.ring, d0 = c.z - tk0, l0 = d0 / tzs;
+  const int sl[2] = {s0, s0 + 1 == job.ring ? 0 : s0 + 1};
+  const int ly[2] = {l0, d0 - l0 * tzs + 1 == tzs ? l0 + 1 : l0};
+  const bool even = (c.x & 1) == 0;  // the row's two corners as one 8-byte load (rows start 128-byte aligned)
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
-    const int Z = c.z + h;
-    const float *p = ring + (long long)(Z % job.ring) * job.plane + (long long)c.y * job.pitch + c.x;
-    const unsigned char *fr = tflags + (long long)((Z - tk0) / tzs) * ntx * fpitch;
+    const float *p = ring + (long long)sl[h] * job.plane + (long long)c.y * job.pitch + c.x;
+    const unsigned char *fr = tflags + (long long)ly[h] * ntx * fpitch;
 #pragma unroll
     for (int by = 0; by < 2; ++by) {
       const unsigned char *f = fr + (long long)((c.y + by) >> 3) * fpitch;
-#pragma unroll
-      for (int bx = 0; bx < 2; ++bx) {
-        const float x = __ldg(p + by * job.pitch + bx);
-        const bool unknown = __ldg(f + ((c.x + bx) >> 3)) & S2_TILE_DECIDED;
-        v[4 * h + 2 * by + bx] = unknown ? __int_as_float(0x7fc00000) : x;
+      const float *q = p + by * job.pitch;
+      float a, b;
+      if (even) {
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(q));
+        a = t.x;
+        b = t.y;
+      } else {
+        a = __ldg(q);
+        b = __ldg(q + 1);
       }
+      const bool u0 = __ldg(f + (c.x >> 3)) & S2_TILE_DECIDED, u1 = __ldg(f + ((c.x + 1) >> 3)) & S2_TILE_DECIDED;
+      v[4 * h + 2 * by] = u0 ? __int_as_float(0x7fc00000) : a;
+      v[4 * h + 2 * by + 1] = u1 ? __int_as_float(0x7fc00000) : b;
     }
   }
 }
